@@ -1,0 +1,341 @@
+#!/usr/bin/env python
+"""Time-to-converge of the GB300 reduced-Schur bundle adjustment.
+
+Workload (one "step" = one complete bundle adjustment from the initial state to convergence):
+the 500-camera / 200k-point aerial grid (25x20 nadir cameras at 100 m, 80/60 % overlap,
+6000x4000 px, f=4000 px, sum-of-8-sinusoids terrain with 20 m amplitude, 3..12 observations per
+track, two calibration groups refining f, cx, cy, k1..k3, p1, p2, 0.5 px noise, 3 % outliers,
+Cauchy loss at 1.5 px), seeded synthetic data.  The headline arm runs FP32 Jacobians / Schur /
+PCG with compensated sums, FP64 cost and gain ratio and FP64-residual refinement; the FP64 GPU
+path runs the same kernels instantiated in double precision.
+
+`python bench.py [--gpus N --steps K --warmup W] [--impl reference]`
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "BA time-to-converge at 1e-6 rel cost, mixed vs FP64 on GB300; Schur/PCG HBM GB/s"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="aerial", choices=["aerial", "ring"])
+    ap.add_argument("--cpu-iterations", type=int, default=2,
+                    help="LM iterations of the bounded CPU sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def workload(name):
+    from plabundle_gb300 import synth
+    from plabundle_gb300.problem import ImageRobustLoss, SolveOptions
+    opts = SolveOptions()
+    if name == "aerial":
+        prob = synth.aerial_grid_problem(seed=11)
+        opts.solver.imageRobustLoss = ImageRobustLoss.Cauchy
+        opts.solver.imageRobustLossScalePixels = 1.5
+        opts.calibration.refineSharedFocalLength = True
+        opts.calibration.refineSharedPrincipalPoint = True
+        opts.calibration.refineSharedRadialDistortion = True
+        cfg = {"workload": "aerial_grid_500cam_200kpt", "cameras": prob.n_cameras, "tracks": prob.n_tracks,
+               "observations": prob.n_obs, "calibration_groups": 2, "loss": "cauchy_1.5px",
+               "max_lm_iterations": opts.solver.maxIterations}
+    else:
+        prob = synth.ring_problem(seed=7)
+        opts.solver.imageRobustLoss = ImageRobustLoss.Huber
+        opts.solver.imageRobustLossScalePixels = 1.5
+        cfg = {"workload": "ring_20cam_2kpt", "cameras": prob.n_cameras, "tracks": prob.n_tracks,
+               "observations": prob.n_obs, "loss": "huber_1.5px", "max_lm_iterations": opts.solver.maxIterations}
+    return prob, opts, cfg
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def cpu_cores():
+    return os.cpu_count() or 1
+
+
+def cpu_sample(prob, opts, iterations, full_iterations):
+    """Oracle (CPU FP64 restatement, all host threads) on `iterations` LM iterations of the
+    workload, scaled to `full_iterations` iterations (ms per full solve)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    import copy
+    o2 = copy.deepcopy(opts)
+    o2.solver.maxIterations = iterations
+    orc = O.Oracle(prob, o2, num_threads=cpu_cores())
+    t = time.perf_counter()
+    r = orc.solve()
+    dt = time.perf_counter() - t
+    it = max(1, r["report"]["iterations"])
+    per_it = dt / it
+    return per_it * full_iterations * 1e3, {"sample_iterations": it, "sample_seconds": dt,
+                                           "per_iteration_ms": per_it * 1e3}
+
+
+def problem_bytes(prob):
+    p = prob.normalized()
+    h2d = sum(a.nbytes for a in (p.cameras, p.points, p.track_offsets, p.obs_camera, p.obs_u, p.obs_v,
+                                 p.obs_weight, p.obs_scale))
+    if p.cameraCalibrationGroupIds is not None:
+        h2d += p.cameraCalibrationGroupIds.nbytes
+    d2h = p.cameras.nbytes + p.points.nbytes + p.n_tracks * (1 + 8 + 8)
+    return h2d, d2h
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    prob, opts, cfg = workload(args.workload)
+    full_it = opts.solver.maxIterations
+    vals = []
+    for i in range(args.warmup + args.steps):
+        ms, info = cpu_sample(prob, opts, args.cpu_iterations, full_it)
+        if i >= args.warmup:
+            vals.append(ms)
+    v = statistics.mean(vals)
+    line = {"metric": METRIC, "value": v, "unit": "ms", "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": v, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": cfg,
+            "cpu_baseline": {"value": v, "unit": "ms", "cores": cpu_cores(), "kind": "port",
+                             "sample": f"{info['sample_iterations']} LM iterations of the workload per step, "
+                                       f"scaled to {full_it} iterations (CPU FP64 restatement of the reference, "
+                                       f"OpenMP)"},
+            "e2e": {"value": v, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(args, rank, world, local_rank):
+    import ctypes as C
+    import numpy as np
+    import torch
+    from plabundle_gb300 import native
+    from plabundle_gb300.device import Gb300Context
+
+    torch.cuda.set_device(local_rank)
+    prob, opts, cfg = workload(args.workload)
+    opts.backend.enablePlaMatrixMixedPrecision = True
+    ctx = Gb300Context(local_rank)
+    assert ctx.upload(prob, opts) == 0, ctx.L.pb_gpu_last_error(ctx.ctx)
+    stream = torch.cuda.ExternalStream(ctx.stream_handle())
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def timed_solves(k, warm):
+        for _ in range(warm):
+            ctx.solve()
+        times, reps = [], []
+        for _ in range(k):
+            flush.fill_(1.0)  # L2 flush (256 MB > 129 MB L2) outside the timed events
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            reps.append(ctx.solve())
+            e1.record(stream)
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1))
+        return times, reps
+
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local_rank)
+    sampler.start()
+    t_mixed, reps_mixed = timed_solves(args.steps, args.warmup)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = sampler.stop()
+    ms_mixed = statistics.mean(t_mixed)
+    if world > 1:
+        t = torch.tensor([ms_mixed], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_mixed = float(t.item())
+    out_mixed = ctx.download()
+    launches = sum(r["gpu_kernel_launches"] for r in reps_mixed)
+
+    # FP64 GPU path (same kernels in double precision)
+    opts64 = opts
+    opts64.backend.enablePlaMatrixMixedPrecision = False
+    ctx.copts.precision = 0
+    t_64, reps_64 = timed_solves(max(1, args.steps // 2), 1)
+    out_64 = ctx.download()
+    ms_64 = statistics.mean(t_64)
+    ctx.copts.precision = 1
+
+    # per-kernel device times of one mixed solve (CUDA events on the context stream)
+    ctx.set_timing(True)
+    rep_t = ctx.solve()
+    kt = ctx.kernel_times()
+    ctx.set_timing(False)
+
+    s = ctx.sizes()
+    p = ctx.problem
+    nop, ntp = s["observation_count"], s["active_tracks"]
+    # algorithmic bytes of one assembly launch: observation records (camera index, u, v, weight,
+    # track index, local camera: 33 B) + robust weight written (4 B); per track the point (24 B),
+    # block id and observation offset (8 B) and the factor / rhs written (12 x 4 B); the reduced
+    # system written (pose blocks both triangles, border, rhs and direct rhs in FP32).
+    nnzb = 2 * s["n_pairs"] + s["camera_blocks"]
+    red_bytes = 4 * (36 * nnzb + 6 * s["camera_blocks"] * (s["dim"] - 6 * s["camera_blocks"]) + 2 * s["dim"])
+    asm_bytes = 37 * nop + (24 + 8 + 48) * ntp + red_bytes
+    asm_ms = kt["assemble_ms"] / max(1, kt["assemble_launches"])
+    peak, peak_kind = measured_peaks()
+    achieved = asm_bytes / (asm_ms * 1e-3) / 1e9 if asm_ms > 0 else None
+
+    # end to end through the C ABI with host buffers (upload + solve + download)
+    desc, keep = native.problem_desc(prob)
+    copts = native.solve_options(opts, prob)
+    copts.precision = 1
+    pp = keep[0]
+    cams = np.zeros_like(pp.cameras)
+    pts = np.zeros_like(pp.points)
+    valid = np.zeros(pp.n_tracks, np.int8)
+    rb = np.zeros(pp.n_tracks)
+    ra = np.zeros(pp.n_tracks)
+    rep = native.SolveReportC()
+    e2e = []
+    for i in range(args.warmup + args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        st = ctx.L.pb_gpu_solve_problem(ctx.ctx, C.byref(desc), C.byref(copts), C.byref(rep), cams.ctypes.data,
+                                        pts.ctypes.data, valid.ctypes.data, rb.ctypes.data, ra.ctypes.data)
+        dt = (time.perf_counter() - t0) * 1e3
+        assert st == 0
+        if i >= args.warmup:
+            e2e.append(dt)
+    h2d, d2h = problem_bytes(prob)
+    e2e_ms = statistics.mean(e2e)
+
+    # accuracy of the mixed path against the FP64 GPU path
+    f_m, f_d = reps_mixed[-1]["final_cost"], reps_64[-1]["final_cost"]
+    C64 = out_64["cameras"][:, 9:12]
+    scale = np.linalg.norm(C64 - C64.mean(0), axis=1).max()
+    cam_err = float(np.abs(out_mixed["cameras"][:, 9:12] - C64).max() / scale)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu_ms, info = cpu_sample(prob, opts, args.cpu_iterations, reps_64[-1]["iterations"])
+        cpu = {"value": cpu_ms, "unit": "ms", "cores": cpu_cores(), "kind": "port",
+               "sample": f"{info['sample_iterations']} LM iterations of the workload "
+                         f"({info['sample_seconds']:.1f} s), scaled to the {reps_64[-1]['iterations']} iterations "
+                         f"of the FP64 solve; CPU FP64 restatement of the reference with OpenMP"}
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": ms_mixed, "unit": "ms", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64 (mixed)", "data": "synthetic (seeded)",
+        "config": dict(cfg, l2="flushed between steps (256 MB write)", parallelism="replicas"),
+        "fp64_path_ms_per_step": ms_64, "speedup_vs_fp64_path": ms_64 / ms_mixed,
+        "mixed_vs_fp64": {"final_cost_rel_diff": abs(f_m - f_d) / f_d, "camera_centre_rel_err": cam_err,
+                          "mixed_iterations": reps_mixed[-1]["iterations"], "fp64_iterations": reps_64[-1]["iterations"],
+                          "mixed_status": reps_mixed[-1]["status"], "fp64_status": reps_64[-1]["status"]},
+        "roofline": {"kernel": "k_assemble<float> (linearise + online point Schur)", "bound": "hbm",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None, "traffic": None,
+                     "algorithmic_bytes_per_launch": asm_bytes, "avg_launch_ms": asm_ms,
+                     "peak_kind": f"{peak_kind} copy bandwidth"},
+        "kernel_ms_per_solve": {k: v for k, v in kt.items()},
+        "solve_breakdown_ms": {k: rep_t[k] for k in ("assembly_ms", "linear_ms", "back_substitution_ms",
+                                                     "objective_ms", "total_ms")},
+        "linear_iterations": reps_mixed[-1]["linear_iterations"],
+        "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "clocks": clocks,
+    }
+    if cpu:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl")
+    run_gb300(args, rank, world, local_rank)
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

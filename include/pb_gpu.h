@@ -1,0 +1,246 @@
+/*
+ * pb_gpu.h -- C ABI of the GB300 reduced-Schur bundle-adjustment backend.
+ *
+ * The backend replaces plabundle's device Schur path behind
+ *   plabundle::Solver::solve(const Problem&, const SolveOptions&, SolverWorkspace&)
+ *   (include/plabundle/solver.h:40 in the reference), selected through
+ *   SolveOptions.backend.requested (include/plabundle/options.h:151).
+ * Inside the reference the seam is runConcreteBackend (src/solver.cpp:275-302), which calls
+ *   internal::optimizePointsWithPlaMatrix(cameras, tracks, BAOptions, workspace)
+ *   (src/internal/BundleAdjustPlaMatrix.h:27-30, src/internal/BundleAdjustPlaMatrix.cpp:162-631).
+ * A context here plays the role of SolverWorkspace::Impl (src/solver.cpp:22-25): it owns the
+ * device buffers, the reduced-matrix pattern and the launch shapes, and is reused by sequential
+ * solves of problems with the same structure.
+ *
+ * Conventions
+ *   - Every entry point returns a pb_status; no C++ exception crosses the boundary.
+ *   - Host buffers are owned by the caller and only read or written during the call.
+ *   - A context is used by one host thread at a time (SolverWorkspace rule,
+ *     include/plabundle/solver.h:13-14); all its work runs on the context's own stream.
+ *   - Cameras are records of PB_CAMERA_STRIDE doubles:
+ *       0-8 camera-to-world rotation (row-major), 9-11 centre, 12 fx, 13 fy, 14 cx, 15 cy,
+ *       16 k1, 17 k2, 18 k3, 19 p1, 20 p2, 21 u sign, 22 v sign, 23 depth flip, 24 width,
+ *       25 height, 26-31 zero.
+ *   - Observations are grouped by track: track_offsets[t]..track_offsets[t+1].
+ *   - Reduced-system layout (pb_gpu_get_reduced): pose blocks of 6 columns
+ *     [rotation(3), centre(3)] (the gauge scale camera uses [rotation(3), tangent(2), 0]) in
+ *     camera-block order, followed by one column per refined intrinsic parameter of each
+ *     calibration group.  The reference pads every primary block to 13 columns
+ *     (src/internal/BundleAdjustPlaMatrixProblem.h:41); the padding carries no information.
+ */
+#ifndef PB_GPU_H
+#define PB_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PB_CAMERA_STRIDE 32
+#define PB_INTRINSIC_COUNT 13
+
+typedef enum pb_status {
+    PB_OK = 0,
+    PB_ERR_INVALID_ARGUMENT = 1,
+    PB_ERR_CUDA = 2,
+    PB_ERR_NO_CONVERGENCE = 3,
+    PB_ERR_SINGULAR_BLOCK = 4,
+    PB_ERR_CANCELLED = 5,
+    PB_ERR_BOUNDS = 6,
+    PB_ERR_TIMEOUT = 7,
+    PB_ERR_UNSUPPORTED = 8,
+    PB_ERR_INVALID_PROJECTION = 9,
+    PB_ERR_STATE = 10
+} pb_status;
+
+/* plabundle::SolveStatus numbering (include/plabundle/backend.h:17-27). */
+typedef enum pb_solve_status {
+    PB_SOLVE_NOT_RUN = 0,
+    PB_SOLVE_SUCCESS = 1,
+    PB_SOLVE_NO_CONVERGENCE = 2,
+    PB_SOLVE_CANCELLED = 3,
+    PB_SOLVE_INVALID_INPUT = 4,
+    PB_SOLVE_UNSUPPORTED = 5,
+    PB_SOLVE_BACKEND_UNAVAILABLE = 6,
+    PB_SOLVE_NUMERICAL_FAILURE = 7
+} pb_solve_status;
+
+typedef enum pb_precision { PB_PRECISION_FP64 = 0, PB_PRECISION_MIXED = 1 } pb_precision;
+
+typedef struct pb_gpu_ctx pb_gpu_ctx;
+
+/* Problem in track-CSR form: plabundle::Problem (include/plabundle/problem.h:37-54) for frame
+ * cameras (Track::initialPoint, Observation{cameraIndex,u,v,weight,measurementScale}). */
+typedef struct pb_problem_desc {
+    int32_t n_cameras;
+    const double* cameras;                     /* n_cameras * PB_CAMERA_STRIDE */
+    int32_t n_tracks;
+    const int64_t* track_offsets;              /* n_tracks + 1 */
+    const double* points;                      /* n_tracks * 3 */
+    int64_t n_obs;
+    const int32_t* obs_camera;
+    const double* obs_u;
+    const double* obs_v;
+    const double* obs_weight;
+    const double* obs_scale;
+    int32_t n_fixed_cameras;
+    const int32_t* fixed_cameras;
+    int32_t n_fixed_tracks;
+    const int32_t* fixed_tracks;
+    const int32_t* calibration_group_ids;      /* n_cameras or NULL: Problem::cameraCalibrationGroupIds */
+    const double* intrinsic_reference_cameras; /* n_cameras * 32 or NULL */
+} pb_problem_desc;
+
+/* SolveOptions (include/plabundle/options.h:58-187) as flat fields. */
+typedef struct pb_solve_options {
+    int32_t max_iterations;            /* SolverControlOptions::maxIterations */
+    int32_t robust_loss;               /* ImageRobustLoss: 0 LS, 1 Huber, 2 Cauchy */
+    double robust_loss_scale;          /* imageRobustLossScalePixels */
+    double armijo_coefficient;         /* referenceArmijoCoefficient */
+    int32_t line_search_steps;         /* referenceLineSearchSteps */
+    int32_t enable_point_filter;
+    double filter_max_reproj_error;
+    double filter_sigma_factor;
+    double max_initial_track_rms;
+    int32_t refine_camera_pose;        /* CalibrationOptions::refineCameraPose */
+    int32_t gauge_policy;              /* GaugePolicy: 0 AutoAnchor, 1 RequireExplicit, 2 CallerManaged */
+    int32_t gauge_anchor_camera;       /* Gauge::referenceAnchorCameraIndex */
+    int32_t gauge_scale_camera;        /* Gauge::referenceScaleCameraIndex */
+    double gauge_baseline;             /* Gauge::referenceBaseline */
+    uint32_t intrinsic_mask;           /* bit p: sharedIntrinsicParameterEnabled(options, p) */
+    int32_t precision;                 /* pb_precision */
+    int32_t max_linear_iterations;     /* 0: max(200, 30 * primary blocks) */
+    double linear_relative_tolerance;  /* 0: 2e-10 (online Schur path) */
+    double linear_absolute_tolerance;  /* 0: 1e-12 */
+    int32_t refinement_sweeps;         /* mixed precision: 1..3 iterative-refinement sweeps */
+    int32_t preconditioner_cluster_size; /* BackendOptions::plaMatrixPreconditionerClusterSize (1) */
+    double calibration[32];            /* CalibrationOptions numeric fields (27 used) */
+} pb_solve_options;
+
+/* PlaMatrixDiagnostics (include/plabundle/result.h:91-128) + QualitySummary fields. */
+typedef struct pb_solve_report {
+    int32_t status;                    /* pb_solve_status */
+    int32_t solution_usable;
+    int32_t iterations;
+    int32_t accepted_steps;
+    int32_t rejected_steps;
+    int32_t linearizations;
+    int32_t objective_evaluations;
+    int32_t linear_iterations;
+    int32_t refinement_sweeps;
+    int32_t active_tracks;
+    int32_t observation_count;
+    int32_t rejected_initial_tracks;
+    int32_t optimized_tracks;
+    int32_t camera_blocks;
+    int32_t intrinsic_blocks;
+    int32_t pattern_builds;
+    int32_t pattern_reuses;
+    int32_t gpu_kernel_launches;
+    double initial_cost;
+    double final_cost;
+    double mean_rms_before;
+    double mean_rms_after;
+    double valid_track_ratio;
+    double filter_threshold;
+    double assembly_ms;
+    double linear_ms;
+    double back_substitution_ms;
+    double objective_ms;
+    double total_ms;
+} pb_solve_report;
+
+/* Context lifetime (SolverWorkspace construction / clear()). */
+pb_status pb_gpu_create(int32_t device, pb_gpu_ctx** out);
+pb_status pb_gpu_destroy(pb_gpu_ctx* ctx);
+const char* pb_gpu_last_error(const pb_gpu_ctx* ctx);
+const char* pb_status_name(int32_t status);
+
+/* Uploads a problem: validation, AutoAnchor gauge (BundleAdjustValidation.cpp:814-893),
+ * active-track gate and block numbering (BundleAdjustPlaMatrixProblem.cpp:29-278), intrinsic
+ * groups (BundleAdjustPlaMatrixModel.cpp:84-231), reduced pattern and launch shapes
+ * (prepareOffDiagonalTopology, BundleAdjustPlaMatrixReferenceSchur.cpp:568-659).  The pattern is
+ * reused when a later upload has the identical structure. */
+pb_status pb_gpu_upload(pb_gpu_ctx* ctx, const pb_problem_desc* problem, const pb_solve_options* options);
+
+/* Reset the state to the uploaded initial cameras/points (device-side copy, no host traffic). */
+pb_status pb_gpu_reset_state(pb_gpu_ctx* ctx);
+
+/* Sizes: [n_cameras, n_tracks, n_obs, primary blocks, camera blocks, intrinsic blocks,
+ *         track blocks, active tracks, observation count, rejected initial tracks,
+ *         n_pairs (upper off-diagonal pairs, reference numbering), reduced dimension,
+ *         intrinsic columns per group, gauge anchor, gauge scale, chunks]. */
+pb_status pb_gpu_get_sizes(pb_gpu_ctx* ctx, int64_t* sizes, double* gauge_baseline);
+pb_status pb_gpu_get_active(pb_gpu_ctx* ctx, int8_t* active_track, int32_t* camera_block,
+                            int32_t* intrinsic_block, int32_t* track_block);
+/* Upper-triangular primary block pairs (row < col) in the reference's slot order. */
+pb_status pb_gpu_get_pairs(pb_gpu_ctx* ctx, int32_t* pairs);
+
+/* Kernel (a): per-observation residual, point Jacobian (2x3, scaled), pose Jacobian (2x6 as
+ * scattered for the camera block), intrinsic Jacobian (2x13), normal weight, robust cost and a
+ * validity flag, at the current state, in the original observation order. */
+pb_status pb_gpu_linearize_observations(pb_gpu_ctx* ctx, int32_t precision, double* residual,
+                                        double* point_jacobian, double* pose_jacobian,
+                                        double* intrinsic_jacobian, double* normal_weight, double* cost,
+                                        int8_t* valid);
+
+/* Kernel (b): online point Schur (buildReferenceReducedNormalEquations,
+ * BundleAdjustPlaMatrixReferenceSchur.cpp:675-980) with damping lambda. */
+pb_status pb_gpu_linearize_schur(pb_gpu_ctx* ctx, double lambda, int32_t precision, double* cost,
+                                 int32_t* point_system_singular);
+/* Dense copy of the reduced system (dimension from pb_gpu_get_sizes) and its right-hand sides:
+ * rhs = -gradient, direct_rhs = the image terms before point elimination (directPrimaryRhs). */
+pb_status pb_gpu_get_reduced(pb_gpu_ctx* ctx, double* dense_matrix, double* rhs, double* direct_rhs);
+
+/* Kernel (c): block-Jacobi PCG on the reduced system (FP64, or FP32 with FP64-residual
+ * iterative refinement when the last linearisation was mixed). */
+pb_status pb_gpu_solve_reduced(pb_gpu_ctx* ctx, double* step, int32_t* converged, int32_t* iterations,
+                               double* relative_residual);
+
+/* Kernel (d1): back-substitution (recoverReferencePointSteps, ...ReferenceSchur.cpp:982-1082);
+ * eliminated_step is in track-block order. */
+pb_status pb_gpu_back_substitute(pb_gpu_ctx* ctx, double* eliminated_step, double* directional_decrease,
+                                 int32_t* success);
+
+/* Kernel (d2): objective at the current state and at trial states state (+) alpha_k * step. */
+pb_status pb_gpu_eval_cost(pb_gpu_ctx* ctx, double* cost);
+pb_status pb_gpu_eval_cost_batch(pb_gpu_ctx* ctx, const double* alphas, int32_t n_alphas, double* costs);
+pb_status pb_gpu_apply_step(pb_gpu_ctx* ctx, double alpha);
+
+/* Whole LM solve (the online branch of optimizePointsWithPlaMatrix and
+ * finalizeBundleAdjustResult, src/internal/BundleAdjustQuality.cpp:403-502). */
+pb_status pb_gpu_solve(pb_gpu_ctx* ctx, const pb_solve_options* options, pb_solve_report* report);
+
+/* Results: refined cameras (published intrinsics applied), points, per-track valid mask and
+ * strict RMS before/after, intrinsic group parameters (n_groups * 13). Any pointer may be NULL. */
+pb_status pb_gpu_download_state(pb_gpu_ctx* ctx, double* cameras, double* points, int8_t* valid,
+                                double* rms_before, double* rms_after, double* intrinsics);
+
+/* One call: upload + solve + download (the path a caller of Solver::solve takes). */
+pb_status pb_gpu_solve_problem(pb_gpu_ctx* ctx, const pb_problem_desc* problem, const pb_solve_options* options,
+                               pb_solve_report* report, double* cameras_out, double* points_out, int8_t* valid_out,
+                               double* rms_before, double* rms_after);
+
+/* Cooperative cancellation (SolverControlOptions::cancelFlag): checked between LM iterations. */
+pb_status pb_gpu_request_cancel(pb_gpu_ctx* ctx, int32_t cancel);
+
+/* The context's CUDA stream (cudaStream_t), so that callers can order their own work and CUDA
+ * events with the backend's kernels. */
+pb_status pb_gpu_get_stream(pb_gpu_ctx* ctx, void** stream);
+
+/* Enables per-phase CUDA-event timing of the following solves (adds one synchronisation per
+ * timed phase; off by default). */
+pb_status pb_gpu_set_timing(pb_gpu_ctx* ctx, int32_t enable);
+
+/* Device time of the last solve's dominant kernels: [assembly kernel ms, assembly launches,
+ * pcg kernel ms, pcg launches, cost kernel ms, cost launches, reduce kernel ms, reduce launches],
+ * filled when timing is enabled. */
+pb_status pb_gpu_kernel_times(pb_gpu_ctx* ctx, double* out8);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PB_GPU_H */

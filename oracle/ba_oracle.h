@@ -1,0 +1,130 @@
+/*
+ * ba_oracle.h -- CPU FP64 restatement of plabundle's reduced-Schur bundle adjustment.
+ *
+ * TEST INFRASTRUCTURE ONLY.  Only tests/, __graft_entry__.smoke() and bench.py's
+ * cpu_baseline leg (and `bench.py --impl reference`) may load this library; the
+ * product path never does.
+ *
+ * Parity status: UNPINNED.  The reference cannot be built here (its linear solver
+ * PlaMatrix and camera model PlaCamera are not vendored and not installed) and its
+ * tests carry no golden vectors for this path.  This file restates the reference's
+ * own in-tree algorithm; the external pieces are restated from the reference's call
+ * sites and in-tree templates:
+ *   - projection: src/internal/BundleAdjustProjection.h:58-91 (Brown-Conrady, OpenCV
+ *     tangential convention, depth test 1e-9);
+ *   - intrinsic Jacobian column mapping: src/internal/CameraState.cpp:427-474;
+ *   - damping form of the online Schur path: V and reduced diagonals x (1 + lambda)
+ *     (src/internal/BundleAdjustPlaMatrixReferenceSchur.cpp:362-365, :930);
+ *   - finalizePrimaryDiagonal(scale, add): positive diagonal entries are scaled,
+ *     structurally empty (zero) diagonal entries are set to `add`;
+ *   - finiteMedian: median of the finite values, mean of the two middle values for
+ *     an even count;
+ *   - 3x3 inverse: adjugate / determinant, singular when |det| <= 1e-15.
+ * Same layout conventions as include/pb_gpu.h (camera records of 32 doubles).
+ */
+#pragma once
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum { ORC_CAMERA_STRIDE = 32 };
+
+typedef struct orc_problem {
+    int32_t n_cameras;
+    const double* cameras;               /* n_cameras * 32 */
+    int32_t n_tracks;
+    const int64_t* track_offsets;        /* n_tracks + 1, observations grouped by track */
+    const double* points;                /* n_tracks * 3 (initial points) */
+    int64_t n_obs;
+    const int32_t* obs_camera;
+    const double* obs_u;
+    const double* obs_v;
+    const double* obs_weight;
+    const double* obs_scale;
+    int32_t n_fixed_cameras;
+    const int32_t* fixed_cameras;
+    int32_t n_fixed_tracks;
+    const int32_t* fixed_tracks;
+    const int32_t* calibration_group_ids; /* n_cameras or NULL */
+    const double* intrinsic_reference_cameras; /* n_cameras * 32 or NULL */
+} orc_problem;
+
+typedef struct orc_options {
+    int32_t max_iterations;
+    int32_t robust_loss;            /* 0 least squares, 1 Huber, 2 Cauchy */
+    double robust_loss_scale;
+    double armijo_coefficient;
+    int32_t line_search_steps;
+    int32_t enable_point_filter;
+    double filter_max_reproj_error;
+    double filter_sigma_factor;
+    double max_initial_track_rms;
+    int32_t refine_camera_pose;
+    int32_t gauge_policy;           /* 0 AutoAnchor, 1 RequireExplicitGauge, 2 CallerManaged */
+    int32_t gauge_anchor_camera;
+    int32_t gauge_scale_camera;
+    double gauge_baseline;
+    uint32_t intrinsic_mask;        /* bit p set: shared intrinsic parameter p refined */
+    int32_t num_threads;            /* 0: all OpenMP threads */
+    int32_t linear_solver;          /* 0 auto, 1 dense Cholesky, 2 block-Jacobi PCG */
+    int32_t max_linear_iterations;  /* 0: max(50, 12 * primary blocks) */
+    double linear_relative_tolerance;
+    double linear_absolute_tolerance;
+    double calibration[32];         /* CalibrationOptions numeric fields, see ORC_CAL_* */
+} orc_options;
+
+typedef struct orc_report {
+    int32_t status;                 /* plabundle::SolveStatus numbering */
+    int32_t solution_usable;
+    int32_t iterations;
+    int32_t accepted_steps;
+    int32_t rejected_steps;
+    int32_t linearizations;
+    int32_t objective_evaluations;
+    int32_t linear_iterations;
+    double initial_cost;
+    double final_cost;
+    int32_t active_tracks;
+    int32_t observation_count;
+    int32_t rejected_initial_tracks;
+    int32_t optimized_tracks;
+    double mean_rms_before;
+    double mean_rms_after;
+    double valid_track_ratio;
+    double filter_threshold;
+    double solve_seconds;
+    double assembly_seconds;
+    double linear_seconds;
+} orc_report;
+
+void* orc_create(const orc_problem* problem, const orc_options* options, int32_t* status);
+void orc_destroy(void* handle);
+/* counts: [primary, camera_blocks, intrinsic_blocks, track_blocks, active_tracks,
+ *          observation_count, rejected_initial_tracks, n_pairs(after first build),
+ *          gauge_anchor, gauge_scale] */
+int32_t orc_info(void* handle, int32_t* counts, double* gauge_baseline);
+int32_t orc_active(void* handle, int8_t* active_track, int32_t* camera_block, int32_t* intrinsic_block,
+                   int32_t* track_block);
+/* Per-observation linearisation at the initial state (all observations; invalid ones flagged).
+ * residual[2], point_jacobian[6], pose_jacobian[2*13] (the camera primary term as
+ * scattered by observationPrimaryTerms, zero when the camera has no block),
+ * intrinsic_jacobian[2*13], normal_weight, cost, valid. */
+int32_t orc_linearize_observations(void* handle, double* residual, double* point_jacobian, double* pose_jacobian,
+                                   double* intrinsic_jacobian, double* normal_weight, double* cost, int8_t* valid);
+/* Builds the damped reduced system at the current state. */
+int32_t orc_build(void* handle, double damping, double* cost, int32_t* singular);
+int32_t orc_pairs(void* handle, int32_t* pairs);
+int32_t orc_reduced(void* handle, double* diagonal, double* off_diagonal, double* gradient, double* direct_rhs);
+int32_t orc_solve_linear(void* handle, double* primary_step, int32_t* converged, int32_t* iterations);
+int32_t orc_back_substitute(void* handle, const double* primary_step, double* eliminated_step,
+                            double* directional_decrease, int32_t* success);
+double orc_cost(void* handle);
+/* Full solve from the initial state. */
+int32_t orc_solve(void* handle, orc_report* report, double* cameras_out, double* points_out, int8_t* valid_out,
+                  double* rms_before, double* rms_after, double* intrinsics_out);
+
+#ifdef __cplusplus
+}
+#endif

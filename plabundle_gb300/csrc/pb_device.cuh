@@ -1,0 +1,234 @@
+// pb_device.cuh -- device-side camera model, robust loss and per-observation linearisation.
+//
+// Projection: frame pinhole with Brown-Conrady distortion (OpenCV tangential convention)
+// as stated in the reference's src/internal/BundleAdjustProjection.h:58-91.
+// Linearisation: src/internal/BundleAdjustPlaMatrixProjection.cpp:176-285 with the reference
+// point parameterisation of the online Schur path (:216-262, BundleAdjustPlaMatrixAssembly.cpp:24-40):
+//   rotation increment  C2W' = D E(w)^T D C2W, D = diag(1,-1,-1), E = Rx Ry Rz
+//   centre increment    C' = C + dC (world frame), or the 2-DoF gauge tangent for the scale camera
+//   point increment     X' = X + s(X) dX, s(X) = (|X|/1000) / atan(|X|/1000)
+// The projection, residual and robust cost are always evaluated in FP64; the Jacobians are
+// produced in the arithmetic type T of the kernel (float on the mixed path).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "pb_internal.h"
+
+namespace pb {
+
+struct DCam {
+    double R[9];
+    double C[3];
+    double fx, fy, cx, cy, k1, k2, k3, p1, p2, su, sv;
+    bool flip;
+};
+
+__device__ __forceinline__ void load_cam(const double* __restrict__ c, DCam& k) {
+#pragma unroll
+    for (int i = 0; i < 9; ++i) k.R[i] = __ldg(c + i);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) k.C[i] = __ldg(c + 9 + i);
+    k.fx = __ldg(c + 12); k.fy = __ldg(c + 13); k.cx = __ldg(c + 14); k.cy = __ldg(c + 15);
+    k.k1 = __ldg(c + 16); k.k2 = __ldg(c + 17); k.k3 = __ldg(c + 18); k.p1 = __ldg(c + 19); k.p2 = __ldg(c + 20);
+    k.su = __ldg(c + 21) < 0.0 ? -1.0 : 1.0;
+    k.sv = __ldg(c + 22) < 0.0 ? -1.0 : 1.0;
+    k.flip = __ldg(c + 23) != 0.0;
+}
+
+struct Proj {
+    double px, py;       // pixel
+    double x, y, r2, radial, xd, yd, zc;
+    double d0, d1, d2;   // X - C
+};
+
+// FP64 projection; false when the point is not in front (forward depth <= 1e-9) or not finite.
+__device__ __forceinline__ bool project64(const DCam& c, double X0, double X1, double X2, Proj& p) {
+    p.d0 = X0 - c.C[0];
+    p.d1 = X1 - c.C[1];
+    p.d2 = X2 - c.C[2];
+    const double xc = c.R[0] * p.d0 + c.R[3] * p.d1 + c.R[6] * p.d2;
+    const double yc = c.R[1] * p.d0 + c.R[4] * p.d1 + c.R[7] * p.d2;
+    const double zc = c.R[2] * p.d0 + c.R[5] * p.d1 + c.R[8] * p.d2;
+    const double fwd = c.flip ? -zc : zc;
+    if (!(fwd > 1e-9)) return false;
+    const double iz = 1.0 / zc;
+    const double x = xc * iz, y = yc * iz;
+    const double r2 = x * x + y * y;
+    const double radial = 1.0 + r2 * (c.k1 + r2 * (c.k2 + r2 * c.k3));
+    const double xy2 = 2.0 * x * y;
+    const double xd = x * radial + c.p1 * xy2 + c.p2 * (r2 + 2.0 * x * x);
+    const double yd = y * radial + c.p1 * (r2 + 2.0 * y * y) + c.p2 * xy2;
+    p.px = c.su * c.fx * xd + c.cx;
+    p.py = c.sv * c.fy * yd + c.cy;
+    p.x = x; p.y = y; p.r2 = r2; p.radial = radial; p.xd = xd; p.yd = yd; p.zc = zc;
+    return isfinite(p.px) && isfinite(p.py);
+}
+
+// evaluateImageRobustLoss (BundleAdjustPlaMatrixProjection.cpp:75-109) in FP64.
+__device__ __forceinline__ bool robust_loss(double s, int loss, double scale, double& cost, double& weight) {
+    if (!(s >= 0.0) || !isfinite(s)) return false;
+    if (loss == 0) { cost = 0.5 * s; weight = 1.0; return true; }
+    const double c2 = scale * scale;
+    if (loss == 1) {
+        if (s <= c2) { cost = 0.5 * s; weight = 1.0; return true; }
+        const double n = sqrt(s);
+        cost = scale * n - 0.5 * c2;
+        weight = scale / n;
+        return true;
+    }
+    const double ratio = s / c2;
+    cost = 0.5 * c2 * log1p(ratio);
+    weight = 1.0 / (1.0 + ratio);
+    return true;
+}
+
+__device__ __forceinline__ double point_scale(double X0, double X1, double X2) {
+    const double len = sqrt(X0 * X0 + X1 * X1 + X2 * X2) / 1000.0;
+    if (!isfinite(len) || len == 0.0) return 1.0;
+    return len / atan(len);
+}
+
+template <typename T>
+struct Lin {
+    T r0, r1;
+    T Jp[6];            // 2x3 point Jacobian (row-major, scaled)
+    T Jc[12];           // 2x6 pose Jacobian (row-major)
+    T Ji[2 * kMaxNI];   // 2 x ni intrinsic Jacobian (row-major, compact columns)
+    T w;                // normal weight
+    double cost;        // robust cost (FP64)
+};
+
+// Linearises one observation.  `tangent` selects the gauge tangent centre columns (basis: two
+// world-frame directions in gb[0..5]).  Returns false on an invalid projection or loss.
+template <typename T>
+__device__ __forceinline__ bool linearize_obs(const DCam& c, double X0, double X1, double X2, double u, double v,
+                                              double wobs, int loss, double lscale, bool tangent,
+                                              const double* __restrict__ gb, int ni, const int* __restrict__ cols,
+                                              bool want_jacobian, Lin<T>& L) {
+    Proj p;
+    if (!project64(c, X0, X1, X2, p)) return false;
+    const double r0 = p.px - u, r1 = p.py - v;
+    double cost, rw;
+    if (!robust_loss(wobs * (r0 * r0 + r1 * r1), loss, lscale, cost, rw)) return false;
+    L.cost = cost;
+    L.r0 = static_cast<T>(r0);
+    L.r1 = static_cast<T>(r1);
+    L.w = static_cast<T>(wobs * rw);
+    if (!isfinite(cost) || !isfinite(wobs * rw)) return false;
+    if (!want_jacobian) return true;
+    const T x = static_cast<T>(p.x), y = static_cast<T>(p.y), r2 = static_cast<T>(p.r2);
+    const T radial = static_cast<T>(p.radial);
+    const T k1 = static_cast<T>(c.k1), k2 = static_cast<T>(c.k2), k3 = static_cast<T>(c.k3);
+    const T p1 = static_cast<T>(c.p1), p2 = static_cast<T>(c.p2);
+    const T sfx = static_cast<T>(c.su * c.fx), sfy = static_cast<T>(c.sv * c.fy);
+    const T dr = k1 + r2 * (T(2) * k2 + T(3) * k3 * r2);
+    const T dxd_dx = radial + T(2) * x * x * dr + T(2) * p1 * y + T(6) * p2 * x;
+    const T dxd_dy = T(2) * x * y * dr + T(2) * p1 * x + T(2) * p2 * y;
+    const T dyd_dx = dxd_dy;
+    const T dyd_dy = radial + T(2) * y * y * dr + T(6) * p1 * y + T(2) * p2 * x;
+    const T iz = static_cast<T>(1.0 / p.zc);
+    const T du_dx = sfx * dxd_dx, du_dy = sfx * dxd_dy, dv_dx = sfy * dyd_dx, dv_dy = sfy * dyd_dy;
+    const T dc[6] = {du_dx * iz, du_dy * iz, -(du_dx * x + du_dy * y) * iz,
+                     dv_dx * iz, dv_dy * iz, -(dv_dx * x + dv_dy * y) * iz};
+    T R[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) R[i] = static_cast<T>(c.R[i]);
+    const T d0 = static_cast<T>(p.d0), d1 = static_cast<T>(p.d1), d2 = static_cast<T>(p.d2);
+    const T s = static_cast<T>(point_scale(X0, X1, X2));
+#pragma unroll
+    for (int pa = 0; pa < 2; ++pa) {
+        // world point Jacobian: dpi/dXw = dpi/dxc * R^T
+        const T jw0 = dc[pa * 3 + 0] * R[0] + dc[pa * 3 + 1] * R[1] + dc[pa * 3 + 2] * R[2];
+        const T jw1 = dc[pa * 3 + 0] * R[3] + dc[pa * 3 + 1] * R[4] + dc[pa * 3 + 2] * R[5];
+        const T jw2 = dc[pa * 3 + 0] * R[6] + dc[pa * 3 + 1] * R[7] + dc[pa * 3 + 2] * R[8];
+        // rotation columns of the target parameterisation: s_k * Jw (e_k x d), s = (1,-1,-1)
+        L.Jc[pa * 6 + 0] = jw2 * d1 - jw1 * d2;
+        L.Jc[pa * 6 + 1] = jw2 * d0 - jw0 * d2;
+        L.Jc[pa * 6 + 2] = jw0 * d1 - jw1 * d0;
+        if (tangent) {
+            L.Jc[pa * 6 + 3] = -(jw0 * static_cast<T>(gb[0]) + jw1 * static_cast<T>(gb[1]) + jw2 * static_cast<T>(gb[2]));
+            L.Jc[pa * 6 + 4] = -(jw0 * static_cast<T>(gb[3]) + jw1 * static_cast<T>(gb[4]) + jw2 * static_cast<T>(gb[5]));
+            L.Jc[pa * 6 + 5] = T(0);
+        } else {
+            L.Jc[pa * 6 + 3] = -jw0;
+            L.Jc[pa * 6 + 4] = -jw1;
+            L.Jc[pa * 6 + 5] = -jw2;
+        }
+        L.Jp[pa * 3 + 0] = jw0 * s;
+        L.Jp[pa * 3 + 1] = jw1 * s;
+        L.Jp[pa * 3 + 2] = jw2 * s;
+    }
+    if (ni > 0) {
+        const T xd = static_cast<T>(p.xd), yd = static_cast<T>(p.yd);
+        const T aspect = static_cast<T>(c.fx > 0.0 ? c.fy / c.fx : 1.0);
+        const T su = static_cast<T>(c.su), sv = static_cast<T>(c.sv);
+        for (int k = 0; k < ni; ++k) {
+            T ju = T(0), jv = T(0);
+            switch (cols[k]) {
+                case 0: ju = su * xd; jv = sv * yd * aspect; break;
+                case 1: ju = T(0); jv = sfy * yd; break;
+                case 2: ju = T(1); jv = T(0); break;
+                case 3: ju = T(0); jv = T(1); break;
+                case 4: ju = sfx * x * r2; jv = sfy * y * r2; break;
+                case 5: ju = sfx * x * r2 * r2; jv = sfy * y * r2 * r2; break;
+                case 6: ju = sfx * x * r2 * r2 * r2; jv = sfy * y * r2 * r2 * r2; break;
+                case 7: ju = sfx * T(2) * x * y; jv = sfy * (r2 + T(2) * y * y); break;
+                case 8: ju = sfx * (r2 + T(2) * x * x); jv = sfy * T(2) * x * y; break;
+                default: break;
+            }
+            L.Ji[k] = ju;
+            L.Ji[kMaxNI + k] = jv;
+        }
+    }
+    return true;
+}
+
+// Two-sum compensated accumulator (FP32 path) / plain FP64 accumulator.
+template <typename T>
+struct Acc;
+
+template <>
+struct Acc<double> {
+    double s = 0.0;
+    __device__ __forceinline__ void add(double v) { s += v; }
+    __device__ __forceinline__ void add_prod(double a, double b) { s = fma(a, b, s); }
+    __device__ __forceinline__ double value() const { return s; }
+    __device__ __forceinline__ void merge(const Acc<double>& o) { s += o.s; }
+};
+
+template <>
+struct Acc<float> {
+    float hi = 0.f, lo = 0.f;
+    __device__ __forceinline__ void add(float v) {
+        const float s = hi + v;
+        const float bp = s - hi;
+        const float e = (hi - (s - bp)) + (v - bp);
+        hi = s;
+        lo += e;
+    }
+    __device__ __forceinline__ void add_prod(float a, float b) {
+        const float p = a * b;
+        const float pe = fmaf(a, b, -p);
+        add(p);
+        lo += pe;
+    }
+    __device__ __forceinline__ float value() const { return hi + lo; }
+    __device__ __forceinline__ void merge(const Acc<float>& o) {
+        add(o.hi);
+        lo += o.lo;
+    }
+};
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+}  // namespace pb

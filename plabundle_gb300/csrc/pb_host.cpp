@@ -1,0 +1,595 @@
+// pb_host.cpp -- host preparation of a bundle-adjustment problem for the GB300 kernels:
+// validation, gauge, active-track gate and block numbering, intrinsic groups, the reduced
+// pattern, the processing order and the per-CTA chunks of the assembly kernel.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <numeric>
+
+#include "pb_internal.h"
+
+namespace pb {
+
+namespace {
+
+constexpr double kInf = std::numeric_limits<double>::infinity();
+
+bool finite3(const double* v) { return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]); }
+
+double sanitized_weight(double w) { return std::isfinite(w) && w > 0.0 ? w : 0.0; }
+double sanitized_scale(double s) { return std::isfinite(s) && s > 0.0 ? s : 1.0; }
+
+// Projection of a world point (BundleAdjustProjection.h:58-91): false when the point is not in
+// front of the camera or the pixel is not finite.
+bool project(const double* cam, const double* X, double* px) {
+    const double d0 = X[0] - cam[9], d1 = X[1] - cam[10], d2 = X[2] - cam[11];
+    const double xc = cam[0] * d0 + cam[3] * d1 + cam[6] * d2;
+    const double yc = cam[1] * d0 + cam[4] * d1 + cam[7] * d2;
+    const double zc = cam[2] * d0 + cam[5] * d1 + cam[8] * d2;
+    const double fwd = cam[23] != 0.0 ? -zc : zc;
+    if (!(fwd > 1e-9)) return false;
+    const double x = xc / zc, y = yc / zc, r2 = x * x + y * y;
+    const double radial = 1.0 + cam[16] * r2 + cam[17] * r2 * r2 + cam[18] * r2 * r2 * r2;
+    const double xd = x * radial + cam[19] * 2.0 * x * y + cam[20] * (r2 + 2.0 * x * x);
+    const double yd = y * radial + cam[19] * (r2 + 2.0 * y * y) + cam[20] * 2.0 * x * y;
+    px[0] = (cam[21] < 0 ? -1.0 : 1.0) * cam[12] * xd + cam[14];
+    px[1] = (cam[22] < 0 ? -1.0 : 1.0) * cam[13] * yd + cam[15];
+    return std::isfinite(px[0]) && std::isfinite(px[1]);
+}
+
+}  // namespace
+
+double finite_median(std::vector<double> v, double fallback) {
+    v.erase(std::remove_if(v.begin(), v.end(), [](double a) { return !std::isfinite(a); }), v.end());
+    if (v.empty()) return fallback;
+    const size_t n = v.size(), h = n / 2;
+    std::nth_element(v.begin(), v.begin() + h, v.end());
+    const double upper = v[h];
+    if (n % 2) return upper;
+    const double lower = *std::max_element(v.begin(), v.begin() + h);
+    return 0.5 * (lower + upper);
+}
+
+void camera_parameter_block(const double* cam, double* p) {
+    // CameraState::parameterBlock (CameraState.cpp:164-185) for this camera model.
+    std::fill(p, p + kP, 0.0);
+    p[0] = cam[12];
+    p[1] = (cam[12] > 0 && cam[13] > 0) ? std::log(cam[13] / cam[12]) : std::numeric_limits<double>::quiet_NaN();
+    for (int i = 2; i < 9; ++i) p[i] = cam[12 + i];
+}
+
+int build_host_model(const pb_problem_desc* pr, const pb_solve_options* op, HostModel* m, std::string* err) {
+    if (!pr || !op) { *err = "null problem or options"; return PB_SOLVE_INVALID_INPUT; }
+    if (pr->n_cameras <= 0 || pr->n_tracks <= 0 || !pr->cameras || !pr->track_offsets || !pr->points) {
+        *err = "cameras or tracks are empty";
+        return PB_SOLVE_INVALID_INPUT;
+    }
+    m->nc = pr->n_cameras;
+    m->nt = pr->n_tracks;
+    m->no = pr->n_obs;
+    m->cams_in.assign(pr->cameras, pr->cameras + static_cast<size_t>(m->nc) * kCamStride);
+    m->cams_ref = pr->intrinsic_reference_cameras
+                      ? std::vector<double>(pr->intrinsic_reference_cameras,
+                                            pr->intrinsic_reference_cameras + static_cast<size_t>(m->nc) * kCamStride)
+                      : m->cams_in;
+    m->points_in.assign(pr->points, pr->points + static_cast<size_t>(m->nt) * 3);
+    m->offs.assign(pr->track_offsets, pr->track_offsets + m->nt + 1);
+    if (m->offs[0] != 0 || m->offs[m->nt] != m->no) { *err = "track offsets do not cover the observations"; return PB_SOLVE_INVALID_INPUT; }
+    for (int t = 0; t < m->nt; ++t)
+        if (m->offs[t + 1] < m->offs[t]) { *err = "track offsets must be non-decreasing"; return PB_SOLVE_INVALID_INPUT; }
+    if (m->no > 0 && (!pr->obs_camera || !pr->obs_u || !pr->obs_v || !pr->obs_weight || !pr->obs_scale)) {
+        *err = "observation arrays missing";
+        return PB_SOLVE_INVALID_INPUT;
+    }
+    m->obs_cam.assign(pr->obs_camera, pr->obs_camera + m->no);
+    m->obs_u.assign(pr->obs_u, pr->obs_u + m->no);
+    m->obs_v.assign(pr->obs_v, pr->obs_v + m->no);
+    m->obs_weight.assign(pr->obs_weight, pr->obs_weight + m->no);
+    m->obs_scale.assign(pr->obs_scale, pr->obs_scale + m->no);
+    m->fixed_cams.assign(pr->fixed_cameras, pr->fixed_cameras + pr->n_fixed_cameras);
+    m->fixed_tracks.assign(pr->fixed_tracks, pr->fixed_tracks + pr->n_fixed_tracks);
+    m->group_ids = pr->calibration_group_ids
+                       ? std::vector<int>(pr->calibration_group_ids, pr->calibration_group_ids + m->nc)
+                       : std::vector<int>();
+    for (int c = 0; c < m->nc; ++c) {
+        const double* cam = &m->cams_in[static_cast<size_t>(c) * kCamStride];
+        for (int i = 0; i < 21; ++i)
+            if (!std::isfinite(cam[i])) { *err = "camera state must be finite"; return PB_SOLVE_INVALID_INPUT; }
+        if (cam[12] <= 0.0 || cam[13] <= 0.0) { *err = "camera focal lengths must be positive"; return PB_SOLVE_INVALID_INPUT; }
+        if (cam[24] < 0.0 || cam[25] < 0.0) { *err = "camera image size must be non-negative"; return PB_SOLVE_INVALID_INPUT; }
+    }
+    if (op->preconditioner_cluster_size > 1) {
+        *err = "only block-Jacobi cluster size 1 is implemented by the GB300 backend";
+        return PB_SOLVE_UNSUPPORTED;
+    }
+
+    // --- gauge (validateAndNormalizeBundleAdjustOptions, BundleAdjustValidation.cpp:772-893)
+    {
+        std::vector<int> fc = m->fixed_cams;
+        std::sort(fc.begin(), fc.end());
+        for (size_t i = 0; i < fc.size(); ++i) {
+            if (fc[i] < 0 || fc[i] >= m->nc) { *err = "fixed camera index out of range"; return PB_SOLVE_INVALID_INPUT; }
+            if (i && fc[i] == fc[i - 1]) { *err = "duplicate fixed camera index"; return PB_SOLVE_INVALID_INPUT; }
+        }
+        const bool requested = op->gauge_anchor_camera >= 0 || op->gauge_scale_camera >= 0 || op->gauge_baseline > 0.0;
+        if (requested && (op->gauge_anchor_camera < 0 || op->gauge_scale_camera < 0 || op->gauge_anchor_camera >= m->nc ||
+                          op->gauge_scale_camera >= m->nc || op->gauge_anchor_camera == op->gauge_scale_camera ||
+                          !std::isfinite(op->gauge_baseline) || op->gauge_baseline <= 0.0)) {
+            *err = "invalid fixed-baseline gauge";
+            return PB_SOLVE_INVALID_INPUT;
+        }
+        m->gauge_anchor = op->gauge_anchor_camera;
+        m->gauge_scale = op->gauge_scale_camera;
+        m->gauge_baseline = op->gauge_baseline;
+        std::sort(m->fixed_tracks.begin(), m->fixed_tracks.end());
+        for (size_t i = 0; i < m->fixed_tracks.size(); ++i) {
+            if (m->fixed_tracks[i] < 0 || m->fixed_tracks[i] >= m->nt) { *err = "fixed track index out of range"; return PB_SOLVE_INVALID_INPUT; }
+            if (i && m->fixed_tracks[i] == m->fixed_tracks[i - 1]) { *err = "duplicate fixed track index"; return PB_SOLVE_INVALID_INPUT; }
+        }
+        if (op->refine_camera_pose && op->gauge_policy != 2) {
+            if (op->gauge_policy == 1) {
+                if (fc.size() < 2) { *err = "incomplete gauge: two fixed cameras are required"; return PB_SOLVE_UNSUPPORTED; }
+            } else {
+                if (fc.empty()) { m->fixed_cams.push_back(0); fc.push_back(0); }
+                if (fc.size() < 2) {
+                    const int anchor = fc[0];
+                    const double* a = &m->cams_in[static_cast<size_t>(anchor) * kCamStride + 9];
+                    int best = -1;
+                    double bestD = 1.0e-20;
+                    for (int i = 0; i < m->nc; ++i) {
+                        if (i == anchor) continue;
+                        const double* c = &m->cams_in[static_cast<size_t>(i) * kCamStride + 9];
+                        const double d2 = (c[0] - a[0]) * (c[0] - a[0]) + (c[1] - a[1]) * (c[1] - a[1]) +
+                                          (c[2] - a[2]) * (c[2] - a[2]);
+                        if (std::isfinite(d2) && d2 > bestD) { bestD = d2; best = i; }
+                    }
+                    if (best < 0) { *err = "automatic gauge found no second camera with a non-zero baseline"; return PB_SOLVE_UNSUPPORTED; }
+                    m->gauge_anchor = anchor;
+                    m->gauge_scale = best;
+                    m->gauge_baseline = std::sqrt(bestD);
+                }
+            }
+        }
+    }
+
+    // --- active tracks and block numbering (prepareActiveProblem, BundleAdjustPlaMatrixProblem.cpp:29-278)
+    const int nc = m->nc, nt = m->nt;
+    m->active_track.assign(nt, 0);
+    m->camera_block.assign(nc, -1);
+    m->intrinsic_block.assign(nc, -1);
+    m->calib_group.assign(nc, -1);
+    m->track_block.assign(nt, -1);
+    std::vector<char> cam_has_residual(nc, 0), fixed_cam(nc, 0), fixed_trk(nt, 0);
+    for (int c : m->fixed_cams) fixed_cam[c] = 1;
+    for (int t : m->fixed_tracks) fixed_trk[t] = 1;
+    auto usable = [&](long long k) {
+        const int c = m->obs_cam[k];
+        return c >= 0 && c < nc && std::isfinite(m->obs_u[k]) && std::isfinite(m->obs_v[k]) &&
+               sanitized_weight(m->obs_weight[k]) > 0.0;
+    };
+    m->active_tracks = m->obs_count = m->rejected = 0;
+    for (int t = 0; t < nt; ++t) {
+        const double* X = &m->points_in[static_cast<size_t>(t) * 3];
+        if (!finite3(X)) continue;
+        int first = -1, count = 0;
+        bool second = false, positive = true;
+        double sq = 0.0;
+        for (long long k = m->offs[t]; k < m->offs[t + 1]; ++k) {
+            if (!usable(k)) continue;
+            const int c = m->obs_cam[k];
+            first = first < 0 ? c : first;
+            second = second || c != first;
+            double px[2];
+            if (!project(&m->cams_in[static_cast<size_t>(c) * kCamStride], X, px)) { positive = false; break; }
+            const double du = px[0] - m->obs_u[k], dv = px[1] - m->obs_v[k];
+            sq += sanitized_weight(m->obs_weight[k]) * (du * du + dv * dv);
+            ++count;
+        }
+        const double rms = count > 0 ? std::sqrt(sq / (2.0 * count)) : kInf;
+        if (count < 2 || !second || !positive) continue;
+        if (op->max_initial_track_rms > 0.0 && rms > op->max_initial_track_rms) { ++m->rejected; continue; }
+        m->active_track[t] = 1;
+        ++m->active_tracks;
+        m->obs_count += count;
+        for (long long k = m->offs[t]; k < m->offs[t + 1]; ++k)
+            if (usable(k)) cam_has_residual[m->obs_cam[k]] = 1;
+    }
+    m->ncb = 0;
+    if (op->refine_camera_pose)
+        for (int c = 0; c < nc; ++c)
+            if (cam_has_residual[c] && !fixed_cam[c]) m->camera_block[c] = m->ncb++;
+    m->P = m->ncb;
+    m->ng = 0;
+    m->ni = 0;
+    if (op->intrinsic_mask != 0) {
+        std::vector<int> ids;
+        for (int c = 0; c < nc; ++c) {
+            const int id = m->group_ids.empty() ? 0 : m->group_ids[c];
+            auto it = std::find(ids.begin(), ids.end(), id);
+            int g;
+            if (it == ids.end()) { g = static_cast<int>(ids.size()); ids.push_back(id); }
+            else g = static_cast<int>(it - ids.begin());
+            m->calib_group[c] = g;
+        }
+        m->ng = static_cast<int>(ids.size());
+        for (int c = 0; c < nc; ++c) m->intrinsic_block[c] = m->P + m->calib_group[c];
+        m->P += m->ng;
+        // Refined columns: enabled and supported by this camera model (f, aspect, cx, cy, k1-k3, p1, p2).
+        for (int p = 0; p < 9; ++p)
+            if ((op->intrinsic_mask >> p) & 1u) m->int_cols[m->ni++] = p;
+        if (m->ng > kMaxGroups) { *err = "more calibration groups than the dense intrinsic border holds (4)"; return PB_SOLVE_UNSUPPORTED; }
+    }
+    m->ntb = 0;
+    for (int t = 0; t < nt; ++t)
+        if (m->active_track[t] && !fixed_trk[t]) m->track_block[t] = m->ntb++;
+
+    // --- intrinsic groups (initializeIntrinsicGroups, BundleAdjustPlaMatrixModel.cpp:84-231)
+    m->groups.assign(m->ng, HostGroup{});
+    if (m->ng > 0) {
+        const double* cal = op->calibration;
+        std::vector<std::vector<double>> init(m->ng * kP), ref(m->ng * kP);
+        for (int c = 0; c < nc; ++c) {
+            const int g = m->calib_group[c];
+            double p[kP], rp[kP];
+            const double* cam = &m->cams_in[static_cast<size_t>(c) * kCamStride];
+            const double* rcam = &m->cams_ref[static_cast<size_t>(c) * kCamStride];
+            camera_parameter_block(cam, p);
+            camera_parameter_block(rcam, rp);
+            init[g * kP + 0].push_back(p[0]);
+            ref[g * kP + 0].push_back(rp[0]);
+            init[g * kP + 1].push_back(std::exp(p[1]));
+            ref[g * kP + 1].push_back(std::exp(rp[1]));
+            init[g * kP + 2].push_back(cam[14] - rcam[14]);
+            init[g * kP + 3].push_back(cam[15] - rcam[15]);
+            ref[g * kP + 2].push_back(0.0);
+            ref[g * kP + 3].push_back(0.0);
+            for (int i = 4; i < kP; ++i) {
+                init[g * kP + i].push_back(p[i]);
+                ref[g * kP + i].push_back(rp[i]);
+            }
+        }
+        const double low = std::max(1.0, cal[26]);
+        for (int g = 0; g < m->ng; ++g) {
+            HostGroup& G = m->groups[g];
+            for (int p = 0; p < kP; ++p) {
+                G.lower[p] = -kInf;
+                G.upper[p] = kInf;
+                G.enabled[p] = p < 9 && ((op->intrinsic_mask >> p) & 1u);
+            }
+            G.focalRef = finite_median(ref[g * kP + 0], 1.0);
+            G.aspectRef = finite_median(ref[g * kP + 1], 1.0);
+            G.params[0] = std::max(1e-12, finite_median(init[g * kP + 0], G.focalRef));
+            G.params[1] = std::log(std::max(1e-12, finite_median(init[g * kP + 1], G.aspectRef)));
+            G.prior[0] = G.focalRef;
+            G.prior[1] = std::log(G.aspectRef);
+            for (int p = 2; p < kP; ++p) {
+                G.prior[p] = finite_median(ref[g * kP + p], 0.0);
+                G.params[p] = finite_median(init[g * kP + p], G.prior[p]);
+            }
+            G.lower[0] = G.focalRef * cal[0];
+            G.upper[0] = G.focalRef * cal[1];
+            G.lower[1] = std::log(G.aspectRef * cal[2]);
+            G.upper[1] = std::log(G.aspectRef * cal[3]);
+            G.lower[2] = G.lower[3] = -G.focalRef * cal[4];
+            G.upper[2] = G.upper[3] = G.focalRef * cal[4];
+            const double lim[9] = {cal[8] * low, cal[9], cal[10], cal[11] * low, cal[12] * low, G.focalRef * cal[13],
+                                   cal[14], cal[15], cal[16]};
+            for (int i = 0; i < 9; ++i) { G.lower[4 + i] = -lim[i]; G.upper[4 + i] = lim[i]; }
+            const double pps = std::max(1e-6, G.focalRef * cal[6]);
+            const double sigma[kP] = {cal[5] * G.focalRef, cal[7], pps, pps, cal[17] * low, cal[18], cal[19],
+                                      cal[20] * low, cal[21] * low, G.focalRef * cal[22], cal[23], cal[24], cal[25]};
+            for (int p = 0; p < kP; ++p) {
+                G.params[p] = std::min(std::max(G.params[p], G.lower[p]), G.upper[p]);
+                G.invSigma[p] = G.enabled[p] ? 1.0 / std::max(1e-9, sigma[p]) : 0.0;
+            }
+        }
+    }
+
+    // --- reference topology: upper block pairs over all primary blocks, numbered row-major
+    // (prepareOffDiagonalTopology, BundleAdjustPlaMatrixReferenceSchur.cpp:568-659)
+    {
+        const int P = m->P;
+        std::vector<std::vector<int>> nbr(P);
+        std::vector<int> tb;
+        auto connect = [&](int a, int b) {
+            if (a < 0 || b < 0 || a == b) return;
+            nbr[std::min(a, b)].push_back(std::max(a, b));
+        };
+        for (int t = 0; t < nt; ++t) {
+            if (!m->active_track[t]) continue;
+            tb.clear();
+            for (long long k = m->offs[t]; k < m->offs[t + 1]; ++k) {
+                if (!usable(k)) continue;
+                const int c = m->obs_cam[k];
+                connect(m->camera_block[c], m->intrinsic_block[c]);
+                if (m->track_block[t] >= 0) {
+                    if (m->camera_block[c] >= 0) tb.push_back(m->camera_block[c]);
+                    if (m->intrinsic_block[c] >= 0) tb.push_back(m->intrinsic_block[c]);
+                }
+            }
+            if (m->track_block[t] < 0) continue;
+            std::sort(tb.begin(), tb.end());
+            tb.erase(std::unique(tb.begin(), tb.end()), tb.end());
+            for (size_t l = 0; l < tb.size(); ++l)
+                for (size_t r = l + 1; r < tb.size(); ++r) connect(tb[l], tb[r]);
+        }
+        m->pairs.clear();
+        for (int r = 0; r < P; ++r) {
+            auto& v = nbr[r];
+            std::sort(v.begin(), v.end());
+            v.erase(std::unique(v.begin(), v.end()), v.end());
+            for (int c : v) m->pairs.emplace_back(r, c);
+        }
+        // pose CSR (both triangles), diagonal always present
+        const int nb = m->ncb;
+        std::vector<std::vector<int>> rows(nb);
+        for (int i = 0; i < nb; ++i) rows[i].push_back(i);
+        for (const auto& pr2 : m->pairs)
+            if (pr2.second < nb) {
+                rows[pr2.first].push_back(pr2.second);
+                rows[pr2.second].push_back(pr2.first);
+            }
+        m->row_ptr.assign(nb + 1, 0);
+        m->col_idx.clear();
+        m->diag_pos.assign(nb, -1);
+        for (int i = 0; i < nb; ++i) {
+            std::sort(rows[i].begin(), rows[i].end());
+            for (int c : rows[i]) {
+                if (c == i) m->diag_pos[i] = static_cast<int>(m->col_idx.size());
+                m->col_idx.push_back(c);
+            }
+            m->row_ptr[i + 1] = static_cast<int>(m->col_idx.size());
+        }
+        // upper blocks (diagonal first in each row), with CSR positions of both orientations
+        m->up_row.clear();
+        m->up_col.clear();
+        m->up_csr.clear();
+        m->up_csr_t.clear();
+        for (int i = 0; i < nb; ++i)
+            for (int p = m->row_ptr[i]; p < m->row_ptr[i + 1]; ++p) {
+                const int j = m->col_idx[p];
+                if (j < i) continue;
+                m->up_row.push_back(i);
+                m->up_col.push_back(j);
+                m->up_csr.push_back(p);
+                int pt = -1;
+                if (j != i) {
+                    const int* b = &m->col_idx[m->row_ptr[j]];
+                    const int* e = &m->col_idx[m->row_ptr[j + 1]];
+                    pt = static_cast<int>(std::lower_bound(b, e, i) - &m->col_idx[0]);
+                }
+                m->up_csr_t.push_back(pt);
+            }
+    }
+
+    // --- processing order: active tracks sorted by their smallest pose block so that a chunk of
+    // consecutive tracks touches few cameras; observations of each track kept in input order.
+    {
+        std::vector<std::pair<long long, int>> key;
+        key.reserve(m->active_tracks);
+        for (int t = 0; t < nt; ++t) {
+            if (!m->active_track[t]) continue;
+            int mn = std::numeric_limits<int>::max();
+            for (long long k = m->offs[t]; k < m->offs[t + 1]; ++k)
+                if (usable(k)) mn = std::min(mn, m->camera_block[m->obs_cam[k]] >= 0 ? m->camera_block[m->obs_cam[k]]
+                                                                                    : nc + m->obs_cam[k]);
+            key.emplace_back(static_cast<long long>(mn) * (static_cast<long long>(nt) + 1) + t, t);
+        }
+        std::sort(key.begin(), key.end());
+        m->trk_order.resize(key.size());
+        m->trk_obs_begin.assign(key.size() + 1, 0);
+        m->p_obs_orig.clear();
+        m->p_obs_orig.reserve(m->obs_count);
+        for (size_t i = 0; i < key.size(); ++i) {
+            const int t = key[i].second;
+            m->trk_order[i] = t;
+            for (long long k = m->offs[t]; k < m->offs[t + 1]; ++k)
+                if (usable(k)) m->p_obs_orig.push_back(static_cast<int>(k));
+            m->trk_obs_begin[i + 1] = static_cast<int>(m->p_obs_orig.size());
+        }
+    }
+    // structure hash for pattern reuse
+    {
+        unsigned long long h = 1469598103934665603ull;
+        auto mix = [&](long long v) { h = (h ^ static_cast<unsigned long long>(v)) * 1099511628211ull; };
+        mix(nc); mix(nt); mix(m->no); mix(m->ncb); mix(m->ng); mix(m->ni);
+        for (size_t i = 0; i < m->p_obs_orig.size(); ++i) { mix(m->p_obs_orig[i]); mix(m->obs_cam[m->p_obs_orig[i]]); }
+        for (int t : m->trk_order) mix(t);
+        m->structure_hash = static_cast<long long>(h);
+    }
+    m->chunks_ready[0] = m->chunks_ready[1] = false;
+    return 0;
+}
+
+size_t chunk_smem_bytes(int precision, int max_obs, int max_cams, int max_pairs, int ng, int ni) {
+    const size_t ts = precision == PB_PRECISION_FP64 ? 8 : 4;
+    const size_t nb = static_cast<size_t>(ng) * ni;
+    auto al = [](size_t v) { return (v + 15) & ~static_cast<size_t>(15); };
+    size_t s = 0;
+    s += al(static_cast<size_t>(max_cams) * max_cams * 2);             // pair lookup
+    s += al(static_cast<size_t>(max_pairs) * 36 * ts);                 // pair accumulators
+    s += al(static_cast<size_t>(max_cams) * 12 * ts);                  // rhs accumulators
+    s += al(static_cast<size_t>(max_cams) * ng * 6 * ni * ts);         // border accumulators
+    s += al((nb * nb + 2 * nb) * ts);                                  // intrinsic block + rhs
+    const size_t per_obs = std::max<size_t>(18 + 3 * static_cast<size_t>(ni), 9);
+    s += al(static_cast<size_t>(max_obs) * per_obs * ts);              // G_o (aliased with V_o)
+    s += al(static_cast<size_t>(max_obs) * 9 * ts);                   // track factor and q
+    s += al(static_cast<size_t>(max_obs) * 4);                         // track start per obs
+    s += al(64 * 8);                                                   // warp partial costs, flags
+    return s;
+}
+
+int build_chunks(HostModel* m, int precision, size_t smem_budget, std::string* err) {
+    ChunkSet& cs = m->chunks[precision];
+    int max_obs = precision == PB_PRECISION_FP64 ? 128 : 256;
+    int max_cams = precision == PB_PRECISION_FP64 ? 48 : 64;
+    int max_pairs = precision == PB_PRECISION_FP64 ? 256 : 384;
+    while (chunk_smem_bytes(precision, max_obs, max_cams, max_pairs, m->ng, m->ni) > smem_budget && max_pairs > 64) {
+        max_pairs -= 32;
+        if (max_cams > 32) max_cams -= 8;
+    }
+    if (chunk_smem_bytes(precision, max_obs, max_cams, max_pairs, m->ng, m->ni) > smem_budget) {
+        *err = "assembly chunk does not fit in shared memory";
+        return PB_SOLVE_UNSUPPORTED;
+    }
+    cs = ChunkSet{};
+    cs.max_obs = max_obs;
+    cs.max_cams = max_cams;
+    cs.max_pairs = max_pairs;
+    const int ntp = static_cast<int>(m->trk_order.size());
+    cs.obs_lcam.assign(m->p_obs_orig.size(), 255);
+    std::vector<int> stamp(m->nc, -1), local(m->nc, -1);
+    std::vector<unsigned char> pair_seen;  // max_cams * max_cams
+    std::vector<int> ccams;                // cameras (with pose blocks) of the open chunk
+    std::vector<std::pair<int, int>> cpairs;
+    int chunk = 0;
+    int chunk_obs_start = 0;
+    cs.obs_begin.push_back(0);
+    cs.cam_begin.push_back(0);
+    cs.pair_begin.push_back(0);
+    auto close_chunk = [&](int obs_end) {
+        // order local cameras by pose block so that li < lj <=> block_i < block_j
+        std::vector<int> order(ccams.size());
+        std::iota(order.begin(), order.end(), 0);
+        std::sort(order.begin(), order.end(), [&](int a, int b) {
+            return m->camera_block[ccams[a]] < m->camera_block[ccams[b]];
+        });
+        std::vector<int> remap(ccams.size());
+        for (size_t i = 0; i < order.size(); ++i) remap[order[i]] = static_cast<int>(i);
+        for (size_t i = 0; i < order.size(); ++i) cs.cams.push_back(ccams[order[i]]);
+        for (int o = chunk_obs_start; o < obs_end; ++o)
+            if (cs.obs_lcam[o] != 255) cs.obs_lcam[o] = static_cast<unsigned char>(remap[cs.obs_lcam[o]]);
+        std::vector<std::pair<int, int>> rp;
+        rp.reserve(cpairs.size());
+        for (auto& p : cpairs) {
+            int a = remap[p.first], b = remap[p.second];
+            if (a > b) std::swap(a, b);
+            rp.emplace_back(a, b);
+        }
+        std::sort(rp.begin(), rp.end());
+        for (auto& p : rp) {
+            cs.pairs.push_back(p.first | (p.second << 16));
+            cs.pair_upper.push_back(-1);  // resolved once all chunks exist
+        }
+        cs.obs_begin.push_back(obs_end);
+        cs.cam_begin.push_back(static_cast<int>(cs.cams.size()));
+        cs.pair_begin.push_back(static_cast<int>(cs.pairs.size()));
+        for (int c : ccams) stamp[c] = -1;
+        ccams.clear();
+        cpairs.clear();
+        ++chunk;
+        chunk_obs_start = obs_end;
+    };
+    pair_seen.assign(static_cast<size_t>(max_cams) * max_cams, 0);
+    std::vector<int> tcams;
+    std::vector<std::pair<int, int>> tpairs;
+    for (int p = 0; p < ntp; ++p) {
+        const int t = m->trk_order[p];
+        const int o0 = m->trk_obs_begin[p], o1 = m->trk_obs_begin[p + 1];
+        const bool elim = m->track_block[t] >= 0;
+        for (int attempt = 0; attempt < 2; ++attempt) {
+            // cameras and pairs this track would add to the open chunk
+            tcams.clear();
+            tpairs.clear();
+            int new_cams = 0;
+            auto lidx = [&](int c) -> int {
+                if (stamp[c] == chunk) return local[c];
+                for (size_t i = 0; i < tcams.size(); ++i)
+                    if (tcams[i] == c) return static_cast<int>(ccams.size() + i);
+                tcams.push_back(c);
+                ++new_cams;
+                return static_cast<int>(ccams.size() + tcams.size() - 1);
+            };
+            std::vector<int> ol;
+            for (int o = o0; o < o1; ++o) {
+                const int c = m->obs_cam[m->p_obs_orig[o]];
+                ol.push_back(m->camera_block[c] >= 0 ? lidx(c) : -1);
+            }
+            const int ncams_after = static_cast<int>(ccams.size()) + new_cams;
+            int new_pairs = 0;
+            auto seen = [&](int a, int b) {
+                if (a > b) std::swap(a, b);
+                if (a < max_cams && b < max_cams && pair_seen[static_cast<size_t>(a) * max_cams + b]) return true;
+                for (auto& q : tpairs)
+                    if (q.first == a && q.second == b) return true;
+                return false;
+            };
+            for (int i = 0; i < o1 - o0; ++i) {
+                if (ol[i] < 0) continue;
+                if (!seen(ol[i], ol[i])) { tpairs.emplace_back(ol[i], ol[i]); ++new_pairs; }
+                if (!elim) continue;
+                for (int j = i + 1; j < o1 - o0; ++j) {
+                    if (ol[j] < 0) continue;
+                    const int a = std::min(ol[i], ol[j]), b = std::max(ol[i], ol[j]);
+                    if (!seen(a, b)) { tpairs.emplace_back(a, b); ++new_pairs; }
+                }
+            }
+            const int obs_after = o1 - chunk_obs_start;
+            const bool fits = obs_after <= max_obs && ncams_after <= max_cams &&
+                              static_cast<int>(cpairs.size()) + new_pairs <= max_pairs;
+            if (!fits) {
+                if (attempt == 0 && o0 > chunk_obs_start) {
+                    for (auto& q : cpairs) pair_seen[static_cast<size_t>(q.first) * max_cams + q.second] = 0;
+                    close_chunk(o0);
+                    continue;
+                }
+                *err = "a track has more observations than one assembly chunk holds";
+                return PB_SOLVE_UNSUPPORTED;
+            }
+            for (size_t i = 0; i < tcams.size(); ++i) {
+                stamp[tcams[i]] = chunk;
+                local[tcams[i]] = static_cast<int>(ccams.size());
+                ccams.push_back(tcams[i]);
+            }
+            for (auto& q : tpairs) {
+                pair_seen[static_cast<size_t>(q.first) * max_cams + q.second] = 1;
+                cpairs.push_back(q);
+            }
+            for (int i = 0; i < o1 - o0; ++i) cs.obs_lcam[o0 + i] = ol[i] < 0 ? 255 : static_cast<unsigned char>(ol[i]);
+            break;
+        }
+    }
+    if (chunk_obs_start < static_cast<int>(m->p_obs_orig.size()) || ntp == 0) {
+        for (auto& q : cpairs) pair_seen[static_cast<size_t>(q.first) * max_cams + q.second] = 0;
+        close_chunk(static_cast<int>(m->p_obs_orig.size()));
+    }
+    // map each chunk pair to its upper pose block and build the reduce lists
+    const int nupper = static_cast<int>(m->up_row.size());
+    // upper index lookup per row: sorted by col
+    std::vector<int> up_begin(m->ncb + 1, 0);
+    for (int u = 0; u < nupper; ++u) up_begin[m->up_row[u] + 1]++;
+    for (int i = 0; i < m->ncb; ++i) up_begin[i + 1] += up_begin[i];
+    std::vector<int> count_up(nupper + 1, 0), count_cam(m->ncb + 1, 0);
+    for (int c = 0; c < cs.n(); ++c) {
+        for (int s = cs.pair_begin[c]; s < cs.pair_begin[c + 1]; ++s) {
+            const int a = cs.pairs[s] & 0xFFFF, b = cs.pairs[s] >> 16;
+            const int bi = m->camera_block[cs.cams[cs.cam_begin[c] + a]];
+            const int bj = m->camera_block[cs.cams[cs.cam_begin[c] + b]];
+            const int* cb = &m->up_col[up_begin[bi]];
+            const int* ce = &m->up_col[0] + up_begin[bi + 1];
+            const int* f = std::lower_bound(cb, ce, bj);
+            if (f == ce || *f != bj) { *err = "internal: chunk pair outside the reduced pattern"; return PB_SOLVE_NUMERICAL_FAILURE; }
+            const int u = static_cast<int>(f - &m->up_col[0]);
+            cs.pair_upper[s] = u;
+            count_up[u + 1]++;
+        }
+        for (int l = cs.cam_begin[c]; l < cs.cam_begin[c + 1]; ++l) count_cam[m->camera_block[cs.cams[l]] + 1]++;
+    }
+    for (int u = 0; u < nupper; ++u) count_up[u + 1] += count_up[u];
+    for (int i = 0; i < m->ncb; ++i) count_cam[i + 1] += count_cam[i];
+    cs.up_contrib_begin = count_up;
+    cs.cam_contrib_begin = count_cam;
+    cs.up_contrib.assign(count_up[nupper], 0);
+    cs.cam_contrib.assign(count_cam[m->ncb], 0);
+    std::vector<int> fill_up(count_up.begin(), count_up.end() - 1), fill_cam(count_cam.begin(), count_cam.end() - 1);
+    for (int c = 0; c < cs.n(); ++c) {
+        for (int s = cs.pair_begin[c]; s < cs.pair_begin[c + 1]; ++s) cs.up_contrib[fill_up[cs.pair_upper[s]]++] = s;
+        for (int l = cs.cam_begin[c]; l < cs.cam_begin[c + 1]; ++l)
+            cs.cam_contrib[fill_cam[m->camera_block[cs.cams[l]]]++] = l;
+    }
+    m->chunks_ready[precision] = true;
+    return 0;
+}
+
+}  // namespace pb

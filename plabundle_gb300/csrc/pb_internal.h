@@ -1,0 +1,147 @@
+// pb_internal.h -- host/device shared declarations of the GB300 reduced-Schur BA backend.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/pb_gpu.h"
+
+namespace pb {
+
+constexpr int kCamStride = PB_CAMERA_STRIDE;
+constexpr int kP = PB_INTRINSIC_COUNT;  // intrinsic parameters per calibration group
+constexpr int kMaxNI = 9;               // refinable intrinsic columns of this camera model
+constexpr int kMaxGroups = 4;           // calibration groups held in the dense border
+constexpr int kMaxNB = kMaxGroups * kMaxNI;
+constexpr int kGroupRec = 6 * kP;       // params, prior, invSigma, lower, upper, enabled
+constexpr int kTrackRec = 12;           // L (upper 3x3: 6), q (3), rhs (3)
+
+// Device-side descriptors passed by value to kernels.
+struct Shape {
+    int nc;          // cameras
+    int ntp;         // processed (active) tracks
+    long long nop;   // processed observations
+    int ncb;         // pose blocks
+    int ng;          // calibration groups (0 when no intrinsic is refined)
+    int ni;          // refined intrinsic columns per group
+    int nb;          // ng * ni
+    int n;           // reduced dimension 6 * ncb + nb
+    int nchunks;
+    int nupper;      // upper pose blocks incl. diagonal
+    int nnzb;        // CSR pose blocks (both triangles)
+    int loss;
+    double loss_scale;
+    int gauge_anchor, gauge_scale;
+    double gauge_baseline;
+    int int_cols[kMaxNI];
+    int max_obs, max_cams, max_pairs;  // chunk limits of the active chunk set
+};
+
+struct DevPtrs {
+    // cameras
+    double* cams_state;   // nc * 32, pose state (intrinsics as input)
+    double* cams_input;   // nc * 32
+    double* cams_ref;     // nc * 32 intrinsic reference cameras
+    double* cams_eff;     // nc * 32 effective cameras of the current state
+    double* cams_trial;   // n_alpha * nc * 32 trial cameras
+    int* cam_block;       // nc
+    int* cam_group;       // nc (-1 without groups)
+    double* groups;       // ng * kGroupRec
+    double* groups_trial; // n_alpha * ng * kGroupRec
+    double* gauge_basis;  // 6 (two world-frame tangent directions)
+    // tracks (processing order)
+    int* trk_obs_begin;   // ntp + 1
+    int* trk_block;       // ntp
+    int* trk_orig;        // ntp
+    double* points;       // ntp * 3
+    double* points0;      // ntp * 3
+    // observations (processing order)
+    int* obs_cam;
+    double* obs_u;
+    double* obs_v;
+    double* obs_w;        // sanitized weight / measurementScale^2
+    int* obs_trk;
+    unsigned char* obs_lcam;
+    int* obs_orig;        // original observation index
+    // chunks
+    int* ch_obs_begin;
+    int* ch_cam_begin;
+    int* ch_cams;         // global camera indices
+    int* ch_pair_begin;
+    int* ch_pairs;        // li | lj << 16, li <= lj
+    // reduce lists
+    int* up_contrib_begin;  // nupper + 1
+    int* up_contrib;        // partial pair slots
+    int* up_csr;            // nupper: CSR position of the upper block
+    int* up_csr_t;          // nupper: CSR position of the transposed block (-1 on the diagonal)
+    int* cam_contrib_begin; // ncb + 1
+    int* cam_contrib;       // partial cam slots
+    // CSR pattern of pose blocks (both triangles)
+    int* row_ptr;         // ncb + 1
+    int* col_idx;         // nnzb
+    int* diag_pos;        // ncb
+    // raw observations (original order) for the strict RMS
+    long long* raw_offsets;  // nt + 1
+    int* raw_cam;
+    double* raw_u;
+    double* raw_v;
+    double* raw_w;        // sanitized weight / scale^2 (0 for unusable)
+    int* raw_bad;         // 1 when the observation makes the strict RMS infinite
+};
+
+// Host model built from the problem (gauge, active tracks, block numbering, groups, pattern).
+struct HostGroup {
+    double params[kP], prior[kP], invSigma[kP], lower[kP], upper[kP];
+    bool enabled[kP];
+    double focalRef, aspectRef;
+};
+
+struct ChunkSet {
+    int max_obs = 0, max_cams = 0, max_pairs = 0;
+    std::vector<int> obs_begin, cam_begin, cams, pair_begin, pairs, pair_upper;
+    std::vector<unsigned char> obs_lcam;
+    std::vector<int> up_contrib_begin, up_contrib, cam_contrib_begin, cam_contrib;
+    size_t n_pair_partials() const { return pairs.size(); }
+    size_t n_cam_partials() const { return cams.size(); }
+    int n() const { return static_cast<int>(obs_begin.empty() ? 0 : obs_begin.size() - 1); }
+};
+
+struct HostModel {
+    int nc = 0, nt = 0;
+    long long no = 0;
+    std::vector<double> cams_in, cams_ref, points_in;
+    std::vector<long long> offs;
+    std::vector<int> obs_cam;
+    std::vector<double> obs_u, obs_v, obs_weight, obs_scale;
+    std::vector<int> fixed_cams, fixed_tracks, group_ids;
+    int gauge_anchor = -1, gauge_scale = -1;
+    double gauge_baseline = 0.0;
+    // active problem
+    std::vector<signed char> active_track;
+    std::vector<int> camera_block, intrinsic_block, calib_group, track_block;
+    int P = 0, ncb = 0, ng = 0, ntb = 0, active_tracks = 0, obs_count = 0, rejected = 0;
+    int ni = 0;
+    int int_cols[kMaxNI] = {0};
+    std::vector<HostGroup> groups;
+    // reference topology (upper pairs over all primary blocks)
+    std::vector<std::pair<int, int>> pairs;
+    // processing order
+    std::vector<int> trk_order;       // processing index -> original track
+    std::vector<int> trk_obs_begin;   // processing obs ranges
+    std::vector<int> p_obs_orig;      // processing obs -> original obs
+    // pose CSR
+    std::vector<int> row_ptr, col_idx, diag_pos, up_row, up_col, up_csr, up_csr_t;
+    ChunkSet chunks[2];               // per precision
+    bool chunks_ready[2] = {false, false};
+    long long structure_hash = 0;
+};
+
+// pb_host.cpp
+int build_host_model(const pb_problem_desc* pr, const pb_solve_options* op, HostModel* m, std::string* err);
+int build_chunks(HostModel* m, int precision, size_t smem_budget, std::string* err);
+size_t chunk_smem_bytes(int precision, int max_obs, int max_cams, int max_pairs, int ng, int ni);
+double finite_median(std::vector<double> v, double fallback);
+void camera_parameter_block(const double* cam, double* p);
+
+}  // namespace pb

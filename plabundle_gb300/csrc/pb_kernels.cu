@@ -1,0 +1,961 @@
+// pb_kernels.cu -- assembly, reduction, back-substitution, objective and state-update kernels.
+//
+// Kernel (a)+(b) `k_assemble`: one CTA per chunk of consecutive tracks (host-built, bounded
+// observations / cameras / camera pairs).  One thread per observation linearises it; the
+// tracks' 3x3 point systems are reduced in shared memory, factored in FP64 (V = R R^T), and
+// every observation forms G_o = W_o R^-T so that the point Schur complement of a track is the
+// symmetric rank-3 update  S -= sum_(o,o') G_o G_o'^T  (online elimination of
+// BundleAdjustPlaMatrixReferenceSchur.cpp:350-490).  Contributions accumulate in shared memory
+// per (camera, camera) pair of the chunk and are written once per chunk as partial blocks;
+// `k_reduce_*` sum the partials per reduced block in a fixed order (two-sum compensated on the
+// FP32 path), so the reduced matrix is assembled without global atomics.
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+
+#include "pb_device.cuh"
+#include "pb_kernels.h"
+
+namespace pb {
+
+namespace {
+
+__device__ __forceinline__ void atomic_add_t(float* p, float v) { atomicAdd(p, v); }
+__device__ __forceinline__ void atomic_add_t(double* p, double v) { atomicAdd(p, v); }
+
+template <typename T>
+__device__ __forceinline__ T* carve(char*& ptr, size_t count) {
+    T* out = reinterpret_cast<T*>(ptr);
+    ptr += (count * sizeof(T) + 15) & ~static_cast<size_t>(15);
+    return out;
+}
+
+}  // namespace
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_assemble(Shape S, DevPtrs D, AsmOutT<T> O, double damping) {
+    extern __shared__ __align__(16) char smem[];
+    const int chunk = blockIdx.x;
+    const int tid = threadIdx.x;
+    const int MC = S.max_cams, MP = S.max_pairs, MO = S.max_obs;
+    const int ng = S.ng, ni = S.ni, nb = S.nb;
+    const int per_obs = max(18 + 3 * ni, 9);
+    char* ptr = smem;
+    unsigned short* s_lookup = carve<unsigned short>(ptr, static_cast<size_t>(MC) * MC);
+    T* s_pair = carve<T>(ptr, static_cast<size_t>(MP) * 36);
+    T* s_rhs = carve<T>(ptr, static_cast<size_t>(MC) * 12);
+    T* s_border = carve<T>(ptr, static_cast<size_t>(MC) * ng * 6 * ni);
+    T* s_C = carve<T>(ptr, static_cast<size_t>(nb) * nb + 2 * nb);
+    T* s_G = carve<T>(ptr, static_cast<size_t>(MO) * per_obs);
+    T* s_trk = carve<T>(ptr, static_cast<size_t>(MO) * 9);
+    int* s_first = carve<int>(ptr, MO);
+    double* s_misc = carve<double>(ptr, 64);
+    int* s_flags = reinterpret_cast<int*>(s_misc + 40);
+
+    const int obs0 = D.ch_obs_begin[chunk], nobs = D.ch_obs_begin[chunk + 1] - obs0;
+    const int cam0 = D.ch_cam_begin[chunk], ncams = D.ch_cam_begin[chunk + 1] - cam0;
+    const int pair0 = D.ch_pair_begin[chunk], npairs = D.ch_pair_begin[chunk + 1] - pair0;
+
+    for (int i = tid; i < MC * MC; i += blockDim.x) s_lookup[i] = 0xFFFF;
+    for (int i = tid; i < npairs * 36; i += blockDim.x) s_pair[i] = T(0);
+    for (int i = tid; i < ncams * 12; i += blockDim.x) s_rhs[i] = T(0);
+    for (int i = tid; i < ncams * ng * 6 * ni; i += blockDim.x) s_border[i] = T(0);
+    for (int i = tid; i < nb * nb + 2 * nb; i += blockDim.x) s_C[i] = T(0);
+    if (tid == 0) s_flags[0] = 0;
+    __syncthreads();
+    for (int s = tid; s < npairs; s += blockDim.x) {
+        const int pk = D.ch_pairs[pair0 + s];
+        s_lookup[(pk & 0xFFFF) * MC + (pk >> 16)] = static_cast<unsigned short>(s);
+    }
+
+    // ---- phase 1: linearise one observation per thread
+    const bool active = tid < nobs;
+    const int o = obs0 + tid;
+    Lin<T> L;
+    double cost = 0.0;
+    int trk = 0, first = 0, k = 0, cam = 0, lcam = 255, grp = -1;
+    bool elim = false, ok = true;
+    if (active) {
+        cam = D.obs_cam[o];
+        trk = D.obs_trk[o];
+        const int tb0 = D.trk_obs_begin[trk];
+        first = tb0 - obs0;
+        k = D.trk_obs_begin[trk + 1] - tb0;
+        elim = D.trk_block[trk] >= 0;
+        lcam = D.obs_lcam[o];
+        grp = D.cam_group[cam];
+        DCam c;
+        load_cam(D.cams_eff + static_cast<size_t>(cam) * kCamStride, c);
+        const double* X = D.points + static_cast<size_t>(trk) * 3;
+        const bool tangent = cam == S.gauge_scale && S.gauge_anchor >= 0 && S.gauge_baseline > 0.0;
+        ok = linearize_obs<T>(c, X[0], X[1], X[2], D.obs_u[o], D.obs_v[o], D.obs_w[o], S.loss, S.loss_scale, tangent,
+                              D.gauge_basis, ni, S.int_cols, true, L);
+        if (!ok) {
+            atomicOr(s_flags, 2);
+        } else {
+            cost = L.cost;
+            O.obs_wn[o] = L.w;
+        }
+        s_first[tid] = first;
+        if (elim && ok) {
+            T* V = s_G + static_cast<size_t>(tid) * per_obs;
+            const T w = L.w;
+            V[0] = w * (L.Jp[0] * L.Jp[0] + L.Jp[3] * L.Jp[3]);
+            V[1] = w * (L.Jp[0] * L.Jp[1] + L.Jp[3] * L.Jp[4]);
+            V[2] = w * (L.Jp[0] * L.Jp[2] + L.Jp[3] * L.Jp[5]);
+            V[3] = w * (L.Jp[1] * L.Jp[1] + L.Jp[4] * L.Jp[4]);
+            V[4] = w * (L.Jp[1] * L.Jp[2] + L.Jp[4] * L.Jp[5]);
+            V[5] = w * (L.Jp[2] * L.Jp[2] + L.Jp[5] * L.Jp[5]);
+            V[6] = -w * (L.Jp[0] * L.r0 + L.Jp[3] * L.r1);
+            V[7] = -w * (L.Jp[1] * L.r0 + L.Jp[4] * L.r1);
+            V[8] = -w * (L.Jp[2] * L.r0 + L.Jp[5] * L.r1);
+        } else if (elim) {
+            T* V = s_G + static_cast<size_t>(tid) * per_obs;
+            for (int i = 0; i < 9; ++i) V[i] = T(0);
+        }
+    }
+    __syncthreads();
+
+    // ---- phase 2: per-track 3x3 point system, FP64 Cholesky V(1+lambda) = R R^T
+    if (active && elim && tid == first) {
+        double V[6] = {0, 0, 0, 0, 0, 0}, rhs[3] = {0, 0, 0};
+        for (int j = 0; j < k; ++j) {
+            const T* v = s_G + static_cast<size_t>(first + j) * per_obs;
+            for (int i = 0; i < 6; ++i) V[i] += static_cast<double>(v[i]);
+            for (int i = 0; i < 3; ++i) rhs[i] += static_cast<double>(v[6 + i]);
+        }
+        V[0] *= 1.0 + damping;
+        V[3] *= 1.0 + damping;
+        V[5] *= 1.0 + damping;
+        // tryInverse3x3 singularity rule: |det| <= 1e-15
+        const double det = V[0] * (V[3] * V[5] - V[4] * V[4]) - V[1] * (V[1] * V[5] - V[4] * V[2]) +
+                           V[2] * (V[1] * V[4] - V[3] * V[2]);
+        double Ri[6] = {0, 0, 0, 0, 0, 0}, q[3] = {0, 0, 0};
+        bool singular = !(fabs(det) > 1e-15) || !isfinite(det);
+        if (!singular) {
+            const double R00 = sqrt(V[0]);
+            const double R10 = V[1] / R00, R20 = V[2] / R00;
+            const double a11 = V[3] - R10 * R10;
+            const double R11 = sqrt(a11);
+            const double R21 = (V[4] - R20 * R10) / R11;
+            const double a22 = V[5] - R20 * R20 - R21 * R21;
+            const double R22 = sqrt(a22);
+            if (!(V[0] > 0.0) || !(a11 > 0.0) || !(a22 > 0.0) || !isfinite(R22)) {
+                singular = true;
+            } else {
+                const double i00 = 1.0 / R00, i11 = 1.0 / R11, i22 = 1.0 / R22;
+                const double i10 = -R10 * i00 * i11;
+                const double i21 = -R21 * i11 * i22;
+                const double i20 = -(R20 * i00 + R21 * i10) * i22;
+                Ri[0] = i00; Ri[1] = i10; Ri[2] = i11; Ri[3] = i20; Ri[4] = i21; Ri[5] = i22;
+                q[0] = i00 * rhs[0];
+                q[1] = i10 * rhs[0] + i11 * rhs[1];
+                q[2] = i20 * rhs[0] + i21 * rhs[1] + i22 * rhs[2];
+            }
+        }
+        if (singular) atomicOr(s_flags, 1);
+        T* st = s_trk + static_cast<size_t>(first) * 9;
+        T* gt = O.trk_data + static_cast<size_t>(trk) * kTrackRec;
+        for (int i = 0; i < 6; ++i) { st[i] = static_cast<T>(Ri[i]); gt[i] = static_cast<T>(Ri[i]); }
+        for (int i = 0; i < 3; ++i) {
+            st[6 + i] = static_cast<T>(q[i]);
+            gt[6 + i] = static_cast<T>(q[i]);
+            gt[9 + i] = static_cast<T>(rhs[i]);
+        }
+    }
+    __syncthreads();
+
+    // ---- phase 3: G_o = W_o R^-T, direct terms
+    T q0 = T(0), q1 = T(0), q2 = T(0);
+    if (active && ok) {
+        const T w = L.w;
+        T* G = s_G + static_cast<size_t>(tid) * per_obs;
+        if (elim) {
+            const T* st = s_trk + static_cast<size_t>(first) * 9;
+            const T i00 = st[0], i10 = st[1], i11 = st[2], i20 = st[3], i21 = st[4], i22 = st[5];
+            q0 = st[6]; q1 = st[7]; q2 = st[8];
+            const int nrows = 6 + ni;
+            for (int a = 0; a < nrows; ++a) {
+                const T ja0 = a < 6 ? L.Jc[a] : L.Ji[a - 6];
+                const T ja1 = a < 6 ? L.Jc[6 + a] : L.Ji[kMaxNI + a - 6];
+                const T w0 = w * (ja0 * L.Jp[0] + ja1 * L.Jp[3]);
+                const T w1 = w * (ja0 * L.Jp[1] + ja1 * L.Jp[4]);
+                const T w2 = w * (ja0 * L.Jp[2] + ja1 * L.Jp[5]);
+                G[a * 3 + 0] = i00 * w0;
+                G[a * 3 + 1] = i10 * w0 + i11 * w1;
+                G[a * 3 + 2] = i20 * w0 + i21 * w1 + i22 * w2;
+            }
+        }
+        const int dslot = lcam < ncams ? s_lookup[lcam * MC + lcam] : 0xFFFF;
+        if (lcam != 255 && dslot >= npairs) atomicOr(s_flags, 4);
+        if (lcam != 255 && dslot < npairs) {
+            T* P = s_pair + static_cast<size_t>(dslot) * 36;
+            for (int a = 0; a < 6; ++a)
+                for (int b = 0; b < 6; ++b)
+                    atomic_add_t(P + a * 6 + b, w * (L.Jc[a] * L.Jc[b] + L.Jc[6 + a] * L.Jc[6 + b]));
+            for (int a = 0; a < 6; ++a) {
+                const T dr = -w * (L.Jc[a] * L.r0 + L.Jc[6 + a] * L.r1);
+                T sr = T(0);
+                if (elim) sr = G[a * 3] * q0 + G[a * 3 + 1] * q1 + G[a * 3 + 2] * q2;
+                atomic_add_t(s_rhs + lcam * 12 + a, dr - sr);
+                atomic_add_t(s_rhs + lcam * 12 + 6 + a, dr);
+            }
+        }
+        if (ng > 0 && grp >= 0) {
+            for (int a = 0; a < ni; ++a) {
+                const T ja0 = L.Ji[a], ja1 = L.Ji[kMaxNI + a];
+                for (int b = 0; b < ni; ++b)
+                    atomic_add_t(s_C + (grp * ni + a) * nb + grp * ni + b, w * (ja0 * L.Ji[b] + ja1 * L.Ji[kMaxNI + b]));
+                const T dr = -w * (ja0 * L.r0 + ja1 * L.r1);
+                atomic_add_t(s_C + nb * nb + grp * ni + a, dr);
+                atomic_add_t(s_C + nb * nb + nb + grp * ni + a, dr);
+                if (lcam != 255 && lcam < ncams)
+                    for (int b = 0; b < 6; ++b)
+                        atomic_add_t(s_border + ((lcam * ng + grp) * 6 + b) * ni + a,
+                                     w * (L.Jc[b] * ja0 + L.Jc[6 + b] * ja1));
+            }
+        }
+    }
+    __syncthreads();
+
+    // ---- phase 4: point Schur complement of each track, pairs spread over the track's threads
+    if (active && ok && elim) {
+        const int j = tid - first;
+        const int npt = k * (k + 1) / 2;
+        for (int p = j; p < npt; p += k) {
+            int a = 0, rem = p;
+            while (rem >= k - a) { rem -= k - a; ++a; }
+            const int b = a + rem;
+            const int oa = first + a, ob = first + b;
+            const int la = D.obs_lcam[obs0 + oa], lb = D.obs_lcam[obs0 + ob];
+            if (la == 255 || lb == 255) continue;
+            const T* Ga = s_G + static_cast<size_t>(oa) * per_obs;
+            const T* Gb = s_G + static_cast<size_t>(ob) * per_obs;
+            const int lo = min(la, lb), hi = max(la, lb);
+            const int slot = hi < ncams ? s_lookup[lo * MC + hi] : 0xFFFF;
+            if (slot >= npairs) {
+                atomicOr(s_flags, 4);
+                continue;
+            }
+            T* P = s_pair + static_cast<size_t>(slot) * 36;
+            for (int x = 0; x < 6; ++x)
+                for (int y = 0; y < 6; ++y) {
+                    const T m = Ga[x * 3] * Gb[y * 3] + Ga[x * 3 + 1] * Gb[y * 3 + 1] + Ga[x * 3 + 2] * Gb[y * 3 + 2];
+                    if (a == b || la < lb) {
+                        atomic_add_t(P + x * 6 + y, -m);
+                    } else if (la > lb) {
+                        atomic_add_t(P + y * 6 + x, -m);
+                    } else {
+                        atomic_add_t(P + x * 6 + y, -m);
+                        atomic_add_t(P + y * 6 + x, -m);
+                    }
+                }
+        }
+        if (ng > 0) {
+            // intrinsic coupling: K_g = sum over the track's observations of group g of G_o^int
+            for (int g = 0; g < ng; ++g) {
+                T K[3 * kMaxNI];
+                bool present = false;
+                for (int i = 0; i < 3 * ni; ++i) K[i] = T(0);
+                for (int jj = 0; jj < k; ++jj) {
+                    const int oo = obs0 + first + jj;
+                    if (D.cam_group[D.obs_cam[oo]] != g) continue;
+                    present = true;
+                    const T* Gj = s_G + static_cast<size_t>(first + jj) * per_obs + 18;
+                    for (int i = 0; i < 3 * ni; ++i) K[i] += Gj[i];
+                }
+                if (!present) continue;
+                const T* Go = s_G + static_cast<size_t>(tid) * per_obs;
+                if (lcam != 255 && lcam < ncams)
+                    for (int x = 0; x < 6; ++x)
+                        for (int c2 = 0; c2 < ni; ++c2)
+                            atomic_add_t(s_border + ((lcam * ng + g) * 6 + x) * ni + c2,
+                                         -(Go[x * 3] * K[c2 * 3] + Go[x * 3 + 1] * K[c2 * 3 + 1] +
+                                           Go[x * 3 + 2] * K[c2 * 3 + 2]));
+                if (j == 0) {
+                    for (int c2 = 0; c2 < ni; ++c2)
+                        atomic_add_t(s_C + nb * nb + g * ni + c2, -(K[c2 * 3] * q0 + K[c2 * 3 + 1] * q1 + K[c2 * 3 + 2] * q2));
+                    for (int g2 = g; g2 < ng; ++g2) {
+                        T K2[3 * kMaxNI];
+                        bool present2 = false;
+                        for (int i = 0; i < 3 * ni; ++i) K2[i] = T(0);
+                        for (int jj = 0; jj < k; ++jj) {
+                            const int oo = obs0 + first + jj;
+                            if (D.cam_group[D.obs_cam[oo]] != g2) continue;
+                            present2 = true;
+                            const T* Gj = s_G + static_cast<size_t>(first + jj) * per_obs + 18;
+                            for (int i = 0; i < 3 * ni; ++i) K2[i] += Gj[i];
+                        }
+                        if (!present2) continue;
+                        for (int c1 = 0; c1 < ni; ++c1)
+                            for (int c2 = 0; c2 < ni; ++c2) {
+                                const T m = K[c1 * 3] * K2[c2 * 3] + K[c1 * 3 + 1] * K2[c2 * 3 + 1] +
+                                            K[c1 * 3 + 2] * K2[c2 * 3 + 2];
+                                atomic_add_t(s_C + (g * ni + c1) * nb + g2 * ni + c2, -m);
+                                if (g2 != g) atomic_add_t(s_C + (g2 * ni + c2) * nb + g * ni + c1, -m);
+                            }
+                    }
+                }
+            }
+        }
+    }
+    // block cost (FP64, fixed order)
+    double cw = warp_sum(cost);
+    if ((tid & 31) == 0) s_misc[tid >> 5] = cw;
+    __syncthreads();
+
+    // ---- phase 5: write the chunk's partial blocks
+    T* pp = O.part_pair + static_cast<size_t>(pair0) * 36;
+    for (int i = tid; i < npairs * 36; i += blockDim.x) pp[i] = s_pair[i];
+    const int camrec = 12 + ng * 6 * ni;
+    T* pc = O.part_cam + static_cast<size_t>(cam0) * camrec;
+    for (int i = tid; i < ncams * camrec; i += blockDim.x) {
+        const int l = i / camrec, e = i - l * camrec;
+        pc[i] = e < 12 ? s_rhs[l * 12 + e] : s_border[l * ng * 6 * ni + (e - 12)];
+    }
+    const int chrec = nb * nb + 2 * nb;
+    T* pk = O.part_chunk + static_cast<size_t>(chunk) * chrec;
+    for (int i = tid; i < chrec; i += blockDim.x) pk[i] = s_C[i];
+    if (tid == 0) {
+        double c = 0.0;
+        for (int w = 0; w < static_cast<int>((blockDim.x + 31) >> 5); ++w) c += s_misc[w];
+        O.part_cost[chunk] = c;
+        O.part_flags[chunk] = s_flags[0];
+    }
+}
+
+// Sum of the chunk partials of every upper pose block, written to both CSR orientations.
+template <typename T>
+__global__ void k_reduce_pairs(Shape S, DevPtrs D, AsmOutT<T> O, T* __restrict__ vals) {
+    const long long idx = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (idx >= static_cast<long long>(S.nupper) * 36) return;
+    const int u = static_cast<int>(idx / 36), e = static_cast<int>(idx - static_cast<long long>(u) * 36);
+    Acc<T> acc;
+    for (int c = D.up_contrib_begin[u]; c < D.up_contrib_begin[u + 1]; ++c)
+        acc.add(O.part_pair[static_cast<size_t>(D.up_contrib[c]) * 36 + e]);
+    const T v = acc.value();
+    vals[static_cast<size_t>(D.up_csr[u]) * 36 + e] = v;
+    const int t = D.up_csr_t[u];
+    if (t >= 0) vals[static_cast<size_t>(t) * 36 + (e % 6) * 6 + e / 6] = v;
+}
+
+// Sum of the per-camera partials: rhs, direct rhs and the intrinsic border rows.
+template <typename T>
+__global__ void k_reduce_cams(Shape S, DevPtrs D, AsmOutT<T> O, T* __restrict__ rhs, T* __restrict__ direct,
+                              T* __restrict__ border) {
+    const int camrec = 12 + S.ng * 6 * S.ni;
+    const long long idx = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (idx >= static_cast<long long>(S.ncb) * camrec) return;
+    const int i = static_cast<int>(idx / camrec), e = static_cast<int>(idx - static_cast<long long>(i) * camrec);
+    Acc<T> acc;
+    for (int c = D.cam_contrib_begin[i]; c < D.cam_contrib_begin[i + 1]; ++c)
+        acc.add(O.part_cam[static_cast<size_t>(D.cam_contrib[c]) * camrec + e]);
+    const T v = acc.value();
+    if (e < 6) rhs[i * 6 + e] = v;
+    else if (e < 12) direct[i * 6 + e - 6] = v;
+    else {
+        const int f = e - 12;  // (g * 6 + a) * ni + c
+        const int g = f / (6 * S.ni), rem = f - g * 6 * S.ni, a = rem / S.ni, c = rem - a * S.ni;
+        border[(static_cast<size_t>(i) * 6 + a) * S.nb + g * S.ni + c] = v;
+    }
+}
+
+// Chunk-level sums (intrinsic block, intrinsic rhs, cost, flags); one CTA, fixed order.
+template <typename T>
+__global__ void k_reduce_chunks(Shape S, AsmOutT<T> O, T* __restrict__ Cm, T* __restrict__ rhs_b,
+                                T* __restrict__ direct_b, double* __restrict__ result) {
+    const int nb = S.nb, chrec = nb * nb + 2 * nb;
+    for (int e = threadIdx.x; e < chrec; e += blockDim.x) {
+        Acc<T> acc;
+        for (int c = 0; c < S.nchunks; ++c) acc.add(O.part_chunk[static_cast<size_t>(c) * chrec + e]);
+        const T v = acc.value();
+        if (e < nb * nb) Cm[e] = v;
+        else if (e < nb * nb + nb) rhs_b[e - nb * nb] = v;
+        else direct_b[e - nb * nb - nb] = v;
+    }
+    __shared__ double s_cost[256];
+    __shared__ int s_flag[256];
+    double c = 0.0;
+    int f = 0;
+    for (int i = threadIdx.x; i < S.nchunks; i += blockDim.x) {
+        c += O.part_cost[i];
+        f |= O.part_flags[i];
+    }
+    s_cost[threadIdx.x] = c;
+    s_flag[threadIdx.x] = f;
+    __syncthreads();
+    for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+        if (threadIdx.x < st) {
+            s_cost[threadIdx.x] += s_cost[threadIdx.x + st];
+            s_flag[threadIdx.x] |= s_flag[threadIdx.x + st];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        result[0] = s_cost[0];
+        result[1] = static_cast<double>(s_flag[0]);
+    }
+}
+
+// Intrinsic priors (assembleReferencePriors, ...ReferenceSchur.cpp:492-536) and
+// finalizePrimaryDiagonal(1 + lambda, 1): positive diagonal entries scaled, empty ones set to 1.
+template <typename T>
+__global__ void k_finalize(Shape S, DevPtrs D, T* __restrict__ vals, T* __restrict__ Cm, T* __restrict__ rhs_b,
+                           T* __restrict__ direct_b, double* __restrict__ result, double damping) {
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid < S.ncb * 6) {
+        const int i = tid / 6, a = tid - i * 6;
+        T* d = vals + static_cast<size_t>(D.diag_pos[i]) * 36 + a * 7;
+        const T v = *d;
+        *d = v != T(0) ? static_cast<T>(static_cast<double>(v) * (1.0 + damping)) : T(1);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0 && S.ng > 0) {
+        double cost = 0.0;
+        for (int g = 0; g < S.ng; ++g) {
+            const double* G = D.groups + static_cast<size_t>(g) * kGroupRec;
+            for (int c = 0; c < S.ni; ++c) {
+                const int p = S.int_cols[c];
+                const double w = G[2 * kP + p];
+                const double r = w * (G[p] - G[kP + p]);
+                cost += 0.5 * r * r;
+                const int col = g * S.ni + c;
+                T* cd = Cm + col * S.nb + col;
+                const double v = static_cast<double>(*cd) + w * w;
+                *cd = static_cast<T>(v != 0.0 ? v * (1.0 + damping) : 1.0);
+                rhs_b[col] = static_cast<T>(static_cast<double>(rhs_b[col]) - w * r);
+                direct_b[col] = static_cast<T>(static_cast<double>(direct_b[col]) - w * r);
+            }
+        }
+        result[0] += cost;
+    }
+}
+
+// Effective cameras of the current state (group intrinsics applied, makeCameraWithSharedIntrinsics,
+// BundleAdjustPlaMatrixProjection.cpp:134-171) and the gauge tangent basis
+// (referenceGaugeTargetTangentBasis, BundleAdjustPlaMatrixAssembly.cpp:69-99).
+__device__ void group_camera(const double* __restrict__ state, const double* __restrict__ ref,
+                             const double* __restrict__ G, double* __restrict__ out) {
+    for (int i = 0; i < kCamStride; ++i) out[i] = state[i];
+    if (!G) return;
+    const double* en = G + 5 * kP;
+    const double fx = en[0] != 0.0 ? G[0] : state[12];
+    const double src_aspect = state[12] > 1e-12 ? state[13] / state[12] : 1.0;
+    const double aspect = en[1] != 0.0 ? exp(G[1]) : src_aspect;
+    out[12] = fx;
+    out[13] = fx * aspect;
+    out[14] = en[2] != 0.0 ? ref[14] + G[2] : state[14];
+    out[15] = en[3] != 0.0 ? ref[15] + G[3] : state[15];
+    for (int p = 4; p < 9; ++p)
+        if (en[p] != 0.0) out[12 + p] = G[p];
+}
+
+__device__ void gauge_basis(const double* anchor_c, const double* scale_c, double* target_basis, double* world_basis) {
+    const double o[3] = {anchor_c[0], -anchor_c[1], -anchor_c[2]};
+    const double c[3] = {scale_c[0], -scale_c[1], -scale_c[2]};
+    double u[3] = {c[0] - o[0], c[1] - o[1], c[2] - o[2]};
+    const double len = sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+    const double il = len >= 1e-20 ? 1.0 / len : 0.0;
+    for (int i = 0; i < 3; ++i) u[i] *= il;
+    int axis = fabs(u[0]) > fabs(u[1]) ? 1 : 0;
+    if (fabs(u[axis]) > fabs(u[2])) axis = 2;
+    double ax[3] = {0, 0, 0};
+    ax[axis] = 1.0;
+    double s[3] = {ax[1] * u[2] - ax[2] * u[1], ax[2] * u[0] - ax[0] * u[2], ax[0] * u[1] - ax[1] * u[0]};
+    const double sl = sqrt(s[0] * s[0] + s[1] * s[1] + s[2] * s[2]);
+    const double isl = sl >= 1e-20 ? 1.0 / sl : 0.0;
+    for (int i = 0; i < 3; ++i) s[i] *= isl;
+    const double f[3] = {u[1] * s[2] - u[2] * s[1], u[2] * s[0] - u[0] * s[2], u[0] * s[1] - u[1] * s[0]};
+    for (int i = 0; i < 3; ++i) {
+        target_basis[i] = f[i];
+        target_basis[3 + i] = s[i];
+    }
+    world_basis[0] = f[0]; world_basis[1] = -f[1]; world_basis[2] = -f[2];
+    world_basis[3] = s[0]; world_basis[4] = -s[1]; world_basis[5] = -s[2];
+}
+
+__global__ void k_effective(Shape S, DevPtrs D) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < S.nc) {
+        const double* G = S.ng > 0 ? D.groups + static_cast<size_t>(D.cam_group[c]) * kGroupRec : nullptr;
+        group_camera(D.cams_state + static_cast<size_t>(c) * kCamStride, D.cams_ref + static_cast<size_t>(c) * kCamStride,
+                     G, D.cams_eff + static_cast<size_t>(c) * kCamStride);
+    }
+    if (c == 0 && S.gauge_anchor >= 0 && S.gauge_scale >= 0 && S.gauge_baseline > 0.0)
+        gauge_basis(D.cams_state + static_cast<size_t>(S.gauge_anchor) * kCamStride + 9,
+                    D.cams_state + static_cast<size_t>(S.gauge_scale) * kCamStride + 9, D.gauge_basis + 6,
+                    D.gauge_basis);
+}
+
+// Trial states for a batch of step lengths: pose retraction (applyReferenceCameraPoseStep,
+// BundleAdjustPlaMatrixAssembly.cpp:130-179; gauge tangent step :101-128) and clamped intrinsic
+// update (applyIntrinsicStep, BundleAdjustPlaMatrixModel.cpp:248-269).
+__global__ void k_trial_cameras(Shape S, DevPtrs D, const double* __restrict__ step_c, const double* __restrict__ alphas,
+                                int n_alpha) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= n_alpha * S.nc) return;
+    const int a = idx / S.nc, c = idx - a * S.nc;
+    const double alpha = alphas[a];
+    // trial groups (each camera thread of the first ng cameras writes one group)
+    double Gt[kGroupRec];
+    const double* Gs = nullptr;
+    if (S.ng > 0) {
+        const int g = D.cam_group[c];
+        const double* G = D.groups + static_cast<size_t>(g) * kGroupRec;
+        for (int i = 0; i < kGroupRec; ++i) Gt[i] = G[i];
+        for (int k = 0; k < S.ni; ++k) {
+            const int p = S.int_cols[k];
+            const double v = G[p] + alpha * step_c[6 * S.ncb + g * S.ni + k];
+            Gt[p] = fmin(fmax(v, G[3 * kP + p]), G[4 * kP + p]);
+        }
+        Gs = Gt;
+        if (c < S.ng) {
+            const double* G2 = D.groups + static_cast<size_t>(c) * kGroupRec;
+            double* out = D.groups_trial + (static_cast<size_t>(a) * S.ng + c) * kGroupRec;
+            for (int i = 0; i < kGroupRec; ++i) out[i] = G2[i];
+            for (int k = 0; k < S.ni; ++k) {
+                const int p = S.int_cols[k];
+                const double v = G2[p] + alpha * step_c[6 * S.ncb + c * S.ni + k];
+                out[p] = fmin(fmax(v, G2[3 * kP + p]), G2[4 * kP + p]);
+            }
+        }
+    }
+    double pose[kCamStride];
+    const double* st = D.cams_state + static_cast<size_t>(c) * kCamStride;
+    for (int i = 0; i < kCamStride; ++i) pose[i] = st[i];
+    const int b = D.cam_block[c];
+    if (b >= 0) {
+        const double* d = step_c + 6 * b;
+        const double dx = alpha * d[0], dy = alpha * d[1], dz = alpha * d[2];
+        double sx, cx, sy, cy, sz, cz;
+        sincos(dx, &sx, &cx);
+        sincos(dy, &sy, &cy);
+        sincos(dz, &sz, &cz);
+        // E = Rx Ry Rz
+        const double E[9] = {cy * cz, -cy * sz, sy,
+                             sx * sy * cz + cx * sz, -sx * sy * sz + cx * cz, -sx * cy,
+                             -cx * sy * cz + sx * sz, cx * sy * sz + sx * cz, cx * cy};
+        const double sg[3] = {1.0, -1.0, -1.0};
+        double Tl[9];
+        for (int r = 0; r < 3; ++r)
+            for (int q = 0; q < 3; ++q) Tl[r * 3 + q] = sg[r] * E[q * 3 + r] * sg[q];
+        double Rn[9];
+        for (int r = 0; r < 3; ++r)
+            for (int q = 0; q < 3; ++q)
+                Rn[r * 3 + q] = Tl[r * 3 + 0] * st[0 * 3 + q] + Tl[r * 3 + 1] * st[1 * 3 + q] + Tl[r * 3 + 2] * st[2 * 3 + q];
+        for (int i = 0; i < 9; ++i) pose[i] = Rn[i];
+        const bool tangent = c == S.gauge_scale && S.gauge_anchor >= 0 && S.gauge_baseline > 0.0;
+        if (tangent) {
+            const double* tb = D.gauge_basis + 6;
+            const double* ac = D.cams_state + static_cast<size_t>(S.gauge_anchor) * kCamStride + 9;
+            const double o[3] = {ac[0], -ac[1], -ac[2]};
+            const double ce[3] = {st[9], -st[10], -st[11]};
+            const double ta = alpha * d[3], tb2 = alpha * d[4];
+            double dir[3];
+            for (int i = 0; i < 3; ++i) dir[i] = ce[i] + tb[i] * ta + tb[3 + i] * tb2 - o[i];
+            const double len = sqrt(dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2]);
+            double nc[3];
+            if (len < 1e-20) {
+                for (int i = 0; i < 3; ++i) nc[i] = o[i];
+            } else {
+                const double il = 1.0 / len;
+                for (int i = 0; i < 3; ++i) nc[i] = o[i] + dir[i] * il * S.gauge_baseline;
+            }
+            pose[9] = nc[0];
+            pose[10] = -nc[1];
+            pose[11] = -nc[2];
+        } else {
+            pose[9] = st[9] + alpha * d[3];
+            pose[10] = st[10] + alpha * d[4];
+            pose[11] = st[11] + alpha * d[5];
+        }
+    }
+    group_camera(pose, D.cams_ref + static_cast<size_t>(c) * kCamStride, Gs,
+                 D.cams_trial + (static_cast<size_t>(a) * S.nc + c) * kCamStride);
+}
+
+// Objective of the trial states: image costs (FP64) per step length, block partials.
+__global__ void __launch_bounds__(256) k_cost_batch(Shape S, DevPtrs D, const double* __restrict__ step_p,
+                                                    const double* __restrict__ alphas, int n_alpha, int use_trial,
+                                                    double* __restrict__ part) {
+    __shared__ double s_c[kMaxAlpha][8];
+    __shared__ int s_bad[kMaxAlpha];
+    const long long o = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (threadIdx.x < kMaxAlpha) s_bad[threadIdx.x] = 0;
+    __syncthreads();
+    double c[kMaxAlpha];
+    for (int a = 0; a < kMaxAlpha; ++a) c[a] = 0.0;
+    if (o < S.nop) {
+        const int cam = D.obs_cam[o], trk = D.obs_trk[o];
+        const double* X = D.points + static_cast<size_t>(trk) * 3;
+        const double u = D.obs_u[o], v = D.obs_v[o], w = D.obs_w[o];
+        const bool moves = use_trial && D.trk_block[trk] >= 0;
+        const double s = moves ? point_scale(X[0], X[1], X[2]) : 0.0;
+        const double* dp = moves ? step_p + static_cast<size_t>(trk) * 3 : nullptr;
+        for (int a = 0; a < n_alpha; ++a) {
+            DCam k;
+            load_cam((use_trial ? D.cams_trial + (static_cast<size_t>(a) * S.nc) * kCamStride : D.cams_eff) +
+                         static_cast<size_t>(cam) * kCamStride,
+                     k);
+            double X0 = X[0], X1 = X[1], X2 = X[2];
+            if (moves) {
+                const double f = s * alphas[a];
+                X0 += f * dp[0];
+                X1 += f * dp[1];
+                X2 += f * dp[2];
+            }
+            Proj p;
+            double cost = 0.0, rw;
+            bool good = project64(k, X0, X1, X2, p);
+            if (good) {
+                const double r0 = p.px - u, r1 = p.py - v;
+                good = robust_loss(w * (r0 * r0 + r1 * r1), S.loss, S.loss_scale, cost, rw) && isfinite(cost);
+            }
+            if (!good) atomicOr(&s_bad[a], 1);
+            else c[a] = cost;
+        }
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int a = 0; a < n_alpha; ++a) {
+        const double v = warp_sum(c[a]);
+        if (lane == 0) s_c[a][wid] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < n_alpha) {
+        double t = 0.0;
+        for (int w2 = 0; w2 < static_cast<int>(blockDim.x >> 5); ++w2) t += s_c[threadIdx.x][w2];
+        part[static_cast<size_t>(blockIdx.x) * kMaxAlpha * 2 + threadIdx.x] = t;
+        part[static_cast<size_t>(blockIdx.x) * kMaxAlpha * 2 + kMaxAlpha + threadIdx.x] = s_bad[threadIdx.x];
+    }
+}
+
+// Final objective per step length: block partials in fixed order plus the intrinsic priors of the
+// trial groups (assemblePrimaryPriors cost, BundleAdjustPlaMatrixAssemblySurvey.cpp:43-91).
+__global__ void k_cost_final(Shape S, DevPtrs D, const double* __restrict__ part, int nblocks, int n_alpha,
+                             int use_trial, double* __restrict__ out) {
+    __shared__ double s_v[256];
+    __shared__ int s_b[256];
+    for (int a = 0; a < n_alpha; ++a) {
+        double v = 0.0;
+        int bad = 0;
+        for (int i = threadIdx.x; i < nblocks; i += blockDim.x) {
+            v += part[static_cast<size_t>(i) * kMaxAlpha * 2 + a];
+            bad |= part[static_cast<size_t>(i) * kMaxAlpha * 2 + kMaxAlpha + a] != 0.0;
+        }
+        s_v[threadIdx.x] = v;
+        s_b[threadIdx.x] = bad;
+        __syncthreads();
+        for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+            if (threadIdx.x < st) {
+                s_v[threadIdx.x] += s_v[threadIdx.x + st];
+                s_b[threadIdx.x] |= s_b[threadIdx.x + st];
+            }
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) {
+            double cost = s_v[0];
+            for (int g = 0; g < S.ng; ++g) {
+                const double* G = (use_trial ? D.groups_trial + static_cast<size_t>(a) * S.ng * kGroupRec : D.groups) +
+                                  static_cast<size_t>(g) * kGroupRec;
+                for (int c = 0; c < S.ni; ++c) {
+                    const int p = S.int_cols[c];
+                    const double r = G[2 * kP + p] * (G[p] - G[kP + p]);
+                    cost += 0.5 * r * r;
+                }
+            }
+            out[a] = s_b[0] ? __longlong_as_double(0x7ff0000000000000ll) : cost;
+        }
+        __syncthreads();
+    }
+}
+
+// Back-substitution (recoverReferencePointSteps, ...ReferenceSchur.cpp:982-1082), one thread per
+// track:  dp = R^-T (q - R^-1 u),  u = sum_o w J_p^T (J_o dc).
+template <typename T>
+__global__ void __launch_bounds__(256) k_back_substitute(Shape S, DevPtrs D, const T* __restrict__ trk_data,
+                                                         const T* __restrict__ obs_wn, const double* __restrict__ step_c,
+                                                         double* __restrict__ step_p, double* __restrict__ part) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    double dd = 0.0, ss = 0.0;
+    if (t < S.ntp && D.trk_block[t] >= 0) {
+        const double* X = D.points + static_cast<size_t>(t) * 3;
+        T u0 = T(0), u1 = T(0), u2 = T(0);
+        for (int o = D.trk_obs_begin[t]; o < D.trk_obs_begin[t + 1]; ++o) {
+            const int cam = D.obs_cam[o];
+            DCam c;
+            load_cam(D.cams_eff + static_cast<size_t>(cam) * kCamStride, c);
+            const bool tangent = cam == S.gauge_scale && S.gauge_anchor >= 0 && S.gauge_baseline > 0.0;
+            Lin<T> L;
+            if (!linearize_obs<T>(c, X[0], X[1], X[2], D.obs_u[o], D.obs_v[o], D.obs_w[o], S.loss, S.loss_scale,
+                                  tangent, D.gauge_basis, S.ni, S.int_cols, true, L))
+                continue;
+            T j0 = T(0), j1 = T(0);
+            const int b = D.cam_block[cam];
+            if (b >= 0)
+                for (int a = 0; a < 6; ++a) {
+                    const T dcv = static_cast<T>(step_c[6 * b + a]);
+                    j0 += L.Jc[a] * dcv;
+                    j1 += L.Jc[6 + a] * dcv;
+                }
+            const int g = D.cam_group[cam];
+            if (S.ng > 0 && g >= 0)
+                for (int a = 0; a < S.ni; ++a) {
+                    const T dcv = static_cast<T>(step_c[6 * S.ncb + g * S.ni + a]);
+                    j0 += L.Ji[a] * dcv;
+                    j1 += L.Ji[kMaxNI + a] * dcv;
+                }
+            const T w = obs_wn[o];
+            u0 += w * (L.Jp[0] * j0 + L.Jp[3] * j1);
+            u1 += w * (L.Jp[1] * j0 + L.Jp[4] * j1);
+            u2 += w * (L.Jp[2] * j0 + L.Jp[5] * j1);
+        }
+        const T* td = trk_data + static_cast<size_t>(t) * kTrackRec;
+        const T i00 = td[0], i10 = td[1], i11 = td[2], i20 = td[3], i21 = td[4], i22 = td[5];
+        const T v0 = td[6] - i00 * u0;
+        const T v1 = td[7] - (i10 * u0 + i11 * u1);
+        const T v2 = td[8] - (i20 * u0 + i21 * u1 + i22 * u2);
+        const double p0 = static_cast<double>(i00 * v0 + i10 * v1 + i20 * v2);
+        const double p1 = static_cast<double>(i11 * v1 + i21 * v2);
+        const double p2 = static_cast<double>(i22 * v2);
+        step_p[static_cast<size_t>(t) * 3 + 0] = p0;
+        step_p[static_cast<size_t>(t) * 3 + 1] = p1;
+        step_p[static_cast<size_t>(t) * 3 + 2] = p2;
+        dd = static_cast<double>(td[9]) * p0 + static_cast<double>(td[10]) * p1 + static_cast<double>(td[11]) * p2;
+        ss = p0 * p0 + p1 * p1 + p2 * p2;
+    } else if (t < S.ntp) {
+        step_p[static_cast<size_t>(t) * 3 + 0] = 0.0;
+        step_p[static_cast<size_t>(t) * 3 + 1] = 0.0;
+        step_p[static_cast<size_t>(t) * 3 + 2] = 0.0;
+    }
+    __shared__ double s_d[8], s_s[8];
+    dd = warp_sum(dd);
+    ss = warp_sum(ss);
+    if ((threadIdx.x & 31) == 0) {
+        s_d[threadIdx.x >> 5] = dd;
+        s_s[threadIdx.x >> 5] = ss;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0, b = 0.0;
+        for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w) {
+            a += s_d[w];
+            b += s_s[w];
+        }
+        part[2 * blockIdx.x] = a;
+        part[2 * blockIdx.x + 1] = b;
+    }
+}
+
+// Fixed-order sum of block partials (pairs of values) plus the camera-side terms of the
+// directional decrease (dc . direct rhs) and of the step RMS.
+__global__ void k_backsub_final(Shape S, DevPtrs D, const double* __restrict__ part, int nblocks,
+                                const double* __restrict__ step_c, const double* __restrict__ direct64,
+                                double* __restrict__ out) {
+    __shared__ double s_a[256], s_b[256], s_c[256];
+    double a = 0.0, b = 0.0, c = 0.0;
+    for (int i = threadIdx.x; i < nblocks; i += blockDim.x) {
+        a += part[2 * i];
+        b += part[2 * i + 1];
+    }
+    for (int i = threadIdx.x; i < S.n; i += blockDim.x) {
+        a += step_c[i] * direct64[i];
+        c += step_c[i] * step_c[i];
+    }
+    s_a[threadIdx.x] = a;
+    s_b[threadIdx.x] = b;
+    s_c[threadIdx.x] = c;
+    __syncthreads();
+    for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+        if (threadIdx.x < st) {
+            s_a[threadIdx.x] += s_a[threadIdx.x + st];
+            s_b[threadIdx.x] += s_b[threadIdx.x + st];
+            s_c[threadIdx.x] += s_c[threadIdx.x + st];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        out[0] = s_a[0];  // directional decrease
+        out[1] = s_b[0];  // sum of squared point steps
+        out[2] = s_c[0];  // sum of squared camera/intrinsic steps
+    }
+}
+
+// Accept trial `a`: poses and effective cameras from the trial, groups, points += s(X) alpha dp.
+__global__ void k_accept(Shape S, DevPtrs D, const double* __restrict__ step_p, double alpha, int a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < S.nc) {
+        const double* tr = D.cams_trial + (static_cast<size_t>(a) * S.nc + i) * kCamStride;
+        double* st = D.cams_state + static_cast<size_t>(i) * kCamStride;
+        double* ef = D.cams_eff + static_cast<size_t>(i) * kCamStride;
+        for (int q = 0; q < 12; ++q) st[q] = tr[q];
+        for (int q = 0; q < kCamStride; ++q) ef[q] = tr[q];
+    }
+    if (i < S.ng * kGroupRec) D.groups[i] = D.groups_trial[static_cast<size_t>(a) * S.ng * kGroupRec + i];
+    if (i < S.ntp && D.trk_block[i] >= 0) {
+        double* X = D.points + static_cast<size_t>(i) * 3;
+        const double f = point_scale(X[0], X[1], X[2]) * alpha;
+        X[0] += f * step_p[static_cast<size_t>(i) * 3 + 0];
+        X[1] += f * step_p[static_cast<size_t>(i) * 3 + 1];
+        X[2] += f * step_p[static_cast<size_t>(i) * 3 + 2];
+    }
+}
+
+// Strict per-track RMS (strictTrackRms, BundleAdjustQuality.cpp:302-364) over the raw observations.
+// `proc_of_track` maps an original track to its processing index (-1: use the initial point).
+__global__ void k_strict_rms(Shape S, DevPtrs D, const double* __restrict__ cams, const double* __restrict__ init_points,
+                             const int* __restrict__ proc_of_track, int use_state, int nt, double* __restrict__ out) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nt) return;
+    double X0, X1, X2;
+    const int pidx = use_state ? proc_of_track[t] : -1;
+    if (use_state && pidx < 0) { out[t] = __longlong_as_double(0x7ff0000000000000ll); return; }
+    if (pidx >= 0) {
+        X0 = D.points[3 * pidx]; X1 = D.points[3 * pidx + 1]; X2 = D.points[3 * pidx + 2];
+    } else {
+        X0 = init_points[3 * t]; X1 = init_points[3 * t + 1]; X2 = init_points[3 * t + 2];
+    }
+    const double inf = __longlong_as_double(0x7ff0000000000000ll);
+    if (!isfinite(X0) || !isfinite(X1) || !isfinite(X2)) { out[t] = inf; return; }
+    double sum = 0.0;
+    int count = 0, first = -1;
+    bool second = false;
+    for (long long k = D.raw_offsets[t]; k < D.raw_offsets[t + 1]; ++k) {
+        const double w = D.raw_w[k];
+        if (!(w > 0.0)) continue;
+        if (D.raw_bad[k]) { out[t] = inf; return; }
+        const int cam = D.raw_cam[k];
+        DCam c;
+        load_cam(cams + static_cast<size_t>(cam) * kCamStride, c);
+        Proj p;
+        if (!project64(c, X0, X1, X2, p)) { out[t] = inf; return; }
+        const double du = p.px - D.raw_u[k], dv = p.py - D.raw_v[k];
+        sum += w * (du * du + dv * dv);
+        count += 2;
+        if (first < 0) first = cam;
+        else if (cam != first) second = true;
+    }
+    out[t] = (count < 4 || !second) ? inf : sqrt(sum / count);
+}
+
+// Per-observation linearisation in the original observation order (parity export of kernel (a)).
+template <typename T>
+__global__ void k_linearize_export(Shape S, DevPtrs D, double* __restrict__ res, double* __restrict__ jp,
+                                   double* __restrict__ jpose, double* __restrict__ ji, double* __restrict__ nw,
+                                   double* __restrict__ cost, signed char* __restrict__ valid) {
+    const long long o = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (o >= S.nop) return;
+    const int cam = D.obs_cam[o], trk = D.obs_trk[o];
+    const long long k = D.obs_orig[o];
+    DCam c;
+    load_cam(D.cams_eff + static_cast<size_t>(cam) * kCamStride, c);
+    const double* X = D.points + static_cast<size_t>(trk) * 3;
+    const bool tangent = cam == S.gauge_scale && S.gauge_anchor >= 0 && S.gauge_baseline > 0.0;
+    Lin<T> L;
+    const bool ok = linearize_obs<T>(c, X[0], X[1], X[2], D.obs_u[o], D.obs_v[o], D.obs_w[o], S.loss, S.loss_scale,
+                                     tangent, D.gauge_basis, S.ni, S.int_cols, true, L);
+    valid[k] = ok ? 1 : 0;
+    if (!ok) return;
+    res[2 * k] = static_cast<double>(L.r0);
+    res[2 * k + 1] = static_cast<double>(L.r1);
+    for (int i = 0; i < 6; ++i) jp[6 * k + i] = static_cast<double>(L.Jp[i]);
+    for (int i = 0; i < 2 * kP; ++i) jpose[2 * kP * k + i] = 0.0;
+    if (D.cam_block[cam] >= 0)
+        for (int r = 0; r < 2; ++r)
+            for (int i = 0; i < 6; ++i) jpose[2 * kP * k + r * kP + i] = static_cast<double>(L.Jc[r * 6 + i]);
+    for (int i = 0; i < 2 * kP; ++i) ji[2 * kP * k + i] = 0.0;
+    for (int r = 0; r < 2; ++r)
+        for (int i = 0; i < S.ni; ++i) ji[2 * kP * k + r * kP + S.int_cols[i]] = static_cast<double>(L.Ji[r * kMaxNI + i]);
+    nw[k] = static_cast<double>(L.w);
+    cost[k] = L.cost;
+}
+
+// ---------------------------------------------------------------- launchers
+template <typename T>
+static AsmOutT<T> typed(const AsmOut& o) {
+    return {static_cast<T*>(o.part_pair_v), static_cast<T*>(o.part_cam_v), static_cast<T*>(o.part_chunk_v),
+            o.part_cost, o.part_flags, static_cast<T*>(o.trk_data_v), static_cast<T*>(o.obs_wn_v)};
+}
+
+template <typename T>
+void launch_assemble(const Shape& S, const DevPtrs& D, const AsmOut& O, double damping, size_t smem, cudaStream_t st) {
+    if (S.nchunks == 0) return;
+    k_assemble<T><<<S.nchunks, S.max_obs, smem, st>>>(S, D, typed<T>(O), damping);
+}
+
+template <typename T>
+void launch_reduce(const Shape& S, const DevPtrs& D, const AsmOut& O, const RedOut<T>& R, double damping,
+                   cudaStream_t st) {
+    const long long np = static_cast<long long>(S.nupper) * 36;
+    if (np > 0) k_reduce_pairs<T><<<static_cast<unsigned>((np + 255) / 256), 256, 0, st>>>(S, D, typed<T>(O), R.vals);
+    const long long nc = static_cast<long long>(S.ncb) * (12 + S.ng * 6 * S.ni);
+    if (nc > 0)
+        k_reduce_cams<T><<<static_cast<unsigned>((nc + 255) / 256), 256, 0, st>>>(S, D, typed<T>(O), R.rhs, R.direct,
+                                                                                       R.border);
+    k_reduce_chunks<T><<<1, 256, 0, st>>>(S, typed<T>(O), R.Cm, R.rhs + 6 * S.ncb, R.direct + 6 * S.ncb, R.result);
+    const int nf = std::max(S.ncb * 6, 1);
+    k_finalize<T><<<(nf + 255) / 256, 256, 0, st>>>(S, D, R.vals, R.Cm, R.rhs + 6 * S.ncb, R.direct + 6 * S.ncb, R.result,
+                                                     damping);
+}
+
+template <typename T>
+void launch_back_substitute(const Shape& S, const DevPtrs& D, const T* trk_data, const T* obs_wn, const double* step_c,
+                            double* step_p, double* part, const double* direct64, double* out, cudaStream_t st) {
+    const int nblk = std::max(1, (S.ntp + 255) / 256);
+    k_back_substitute<T><<<nblk, 256, 0, st>>>(S, D, trk_data, obs_wn, step_c, step_p, part);
+    k_backsub_final<<<1, 256, 0, st>>>(S, D, part, nblk, step_c, direct64, out);
+}
+
+template <typename T>
+void launch_linearize_export(const Shape& S, const DevPtrs& D, double* res, double* jp, double* jpose, double* ji,
+                             double* nw, double* cost, signed char* valid, cudaStream_t st) {
+    if (S.nop == 0) return;
+    k_linearize_export<T><<<static_cast<unsigned>((S.nop + 255) / 256), 256, 0, st>>>(S, D, res, jp, jpose, ji, nw, cost,
+                                                                                       valid);
+}
+
+void launch_effective(const Shape& S, const DevPtrs& D, cudaStream_t st) {
+    k_effective<<<(S.nc + 127) / 128, 128, 0, st>>>(S, D);
+}
+
+void launch_cost(const Shape& S, const DevPtrs& D, const double* step_c, const double* step_p, const double* alphas,
+                 int n_alpha, int use_trial, double* part, double* out, cudaStream_t st) {
+    if (use_trial) {
+        const int n = n_alpha * S.nc;
+        k_trial_cameras<<<(n + 127) / 128, 128, 0, st>>>(S, D, step_c, alphas, n_alpha);
+    }
+    const int nblk = static_cast<int>(std::max<long long>(1, (S.nop + 255) / 256));
+    k_cost_batch<<<nblk, 256, 0, st>>>(S, D, step_p, alphas, n_alpha, use_trial, part);
+    k_cost_final<<<1, 256, 0, st>>>(S, D, part, nblk, n_alpha, use_trial, out);
+}
+
+void launch_accept(const Shape& S, const DevPtrs& D, const double* step_p, double alpha, int a, cudaStream_t st) {
+    const int n = std::max(std::max(S.nc, S.ntp), S.ng * kGroupRec);
+    k_accept<<<(n + 255) / 256, 256, 0, st>>>(S, D, step_p, alpha, a);
+}
+
+void launch_strict_rms(const Shape& S, const DevPtrs& D, const double* cams, const double* init_points,
+                       const int* proc_of_track, int use_state, int nt, double* out, cudaStream_t st) {
+    k_strict_rms<<<(nt + 255) / 256, 256, 0, st>>>(S, D, cams, init_points, proc_of_track, use_state, nt, out);
+}
+
+void pb_set_assemble_smem_f32(size_t bytes) {
+    cudaFuncSetAttribute(k_assemble<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes));
+}
+void pb_set_assemble_smem_f64(size_t bytes) {
+    cudaFuncSetAttribute(k_assemble<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes));
+}
+
+template void launch_assemble<float>(const Shape&, const DevPtrs&, const AsmOut&, double, size_t, cudaStream_t);
+template void launch_assemble<double>(const Shape&, const DevPtrs&, const AsmOut&, double, size_t, cudaStream_t);
+template void launch_reduce<float>(const Shape&, const DevPtrs&, const AsmOut&, const RedOut<float>&, double,
+                                   cudaStream_t);
+template void launch_reduce<double>(const Shape&, const DevPtrs&, const AsmOut&, const RedOut<double>&, double,
+                                    cudaStream_t);
+template void launch_back_substitute<float>(const Shape&, const DevPtrs&, const float*, const float*, const double*,
+                                            double*, double*, const double*, double*, cudaStream_t);
+template void launch_back_substitute<double>(const Shape&, const DevPtrs&, const double*, const double*, const double*,
+                                             double*, double*, const double*, double*, cudaStream_t);
+template void launch_linearize_export<float>(const Shape&, const DevPtrs&, double*, double*, double*, double*, double*,
+                                             double*, signed char*, cudaStream_t);
+template void launch_linearize_export<double>(const Shape&, const DevPtrs&, double*, double*, double*, double*,
+                                              double*, double*, signed char*, cudaStream_t);
+
+}  // namespace pb

@@ -1,0 +1,109 @@
+// pb_kernels.h -- launch interface of the GB300 kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "pb_internal.h"
+
+namespace pb {
+
+constexpr int kMaxAlpha = 8;  // trial step lengths evaluated per objective pass
+
+// Outputs of the assembly kernel (per-chunk partials) and per-track / per-observation data kept
+// for the back-substitution.
+template <typename T>
+struct AsmOutT {
+    T* part_pair;     // pair partials * 36
+    T* part_cam;      // camera partials * (12 + ng*6*ni)
+    T* part_chunk;    // chunks * (nb*nb + 2*nb)
+    double* part_cost;
+    int* part_flags;  // bit 0: singular point system, bit 1: invalid projection
+    T* trk_data;      // processed tracks * kTrackRec
+    T* obs_wn;        // processed observations: robust normal weight
+};
+
+// The assembly kernel is instantiated for both precisions; AsmOut carries untyped pointers.
+struct AsmOut {
+    void* part_pair_v;
+    void* part_cam_v;
+    void* part_chunk_v;
+    double* part_cost;
+    int* part_flags;
+    void* trk_data_v;
+    void* obs_wn_v;
+};
+
+// Reduced system of one precision: pose CSR values (both triangles), border B (6*ncb x nb),
+// intrinsic block C (nb x nb), rhs and direct rhs (n), result[0] cost, result[1] flags.
+template <typename T>
+struct RedOut {
+    T* vals;
+    T* border;
+    T* Cm;
+    T* rhs;
+    T* direct;
+    double* result;
+};
+
+template <typename T>
+void launch_assemble(const Shape& S, const DevPtrs& D, const AsmOut& O, double damping, size_t smem, cudaStream_t st);
+template <typename T>
+void launch_reduce(const Shape& S, const DevPtrs& D, const AsmOut& O, const RedOut<T>& R, double damping,
+                   cudaStream_t st);
+template <typename T>
+void launch_back_substitute(const Shape& S, const DevPtrs& D, const T* trk_data, const T* obs_wn, const double* step_c,
+                            double* step_p, double* part, const double* direct64, double* out, cudaStream_t st);
+template <typename T>
+void launch_linearize_export(const Shape& S, const DevPtrs& D, double* res, double* jp, double* jpose, double* ji,
+                             double* nw, double* cost, signed char* valid, cudaStream_t st);
+void pb_set_assemble_smem_f32(size_t bytes);
+void pb_set_assemble_smem_f64(size_t bytes);
+void launch_effective(const Shape& S, const DevPtrs& D, cudaStream_t st);
+void launch_cost(const Shape& S, const DevPtrs& D, const double* step_c, const double* step_p, const double* alphas,
+                 int n_alpha, int use_trial, double* part, double* out, cudaStream_t st);
+void launch_accept(const Shape& S, const DevPtrs& D, const double* step_p, double alpha, int a, cudaStream_t st);
+void launch_strict_rms(const Shape& S, const DevPtrs& D, const double* cams, const double* init_points,
+                       const int* proc_of_track, int use_state, int nt, double* out, cudaStream_t st);
+
+// PCG (pb_pcg.cu)
+template <typename T>
+struct PcgSystem {
+    int ncb, nb, ng, ni;
+    const int* row_ptr;
+    const int* col_idx;
+    const int* diag_pos;
+    const T* vals;
+    const T* border;
+    const T* Cm;
+    T* Dinv;       // ncb * 36 block-Jacobi inverses
+    T* Cinv;       // ng * ni * ni
+};
+
+struct PcgResult {
+    int iterations;
+    int converged;
+    int status;     // 0 ok, 1 breakdown (not positive definite), 2 preconditioner not SPD
+    double rnorm;
+    double bnorm;
+};
+
+template <typename T>
+int pcg_precondition(const PcgSystem<T>& sys, int* d_status, cudaStream_t st);
+// Solves sys x = b with block-Jacobi PCG in one cooperative persistent kernel.
+template <typename T>
+int pcg_solve(const PcgSystem<T>& sys, const T* b, T* x, T* work, double* partials, PcgResult* d_result,
+              double abs_tol, double rel_tol, int max_iter, int grid, cudaStream_t st);
+template <typename T>
+int pcg_grid_size(int ncb);
+// r64 = b64 - A x64 (FP64 accumulation over the stored matrix), returns norms in out[0..1].
+template <typename T>
+void residual64(const PcgSystem<T>& sys, const double* b64, const double* x64, double* r64, double* out,
+                cudaStream_t st);
+void to_double(const float* in, double* out, int n, cudaStream_t st);
+void to_double(const double* in, double* out, int n, cudaStream_t st);
+void to_float(const double* in, float* out, int n, cudaStream_t st);
+void axpy64(double* x, const float* d, int n, cudaStream_t st);
+
+}  // namespace pb

@@ -1,0 +1,1237 @@
+// pb_solver.cu -- context (workspace), device buffers, the Levenberg-Marquardt / Armijo driver of
+// the online reduced-Schur path, and the C ABI declared in include/pb_gpu.h.
+//
+// The driver restates optimizePointsWithPlaMatrix's online branch
+// (src/internal/BundleAdjustPlaMatrix.cpp:162-631): relinearise, eliminate points, solve the
+// reduced system, back-substitute, Armijo line search with alpha = 1, 1/2, ... on the FP64
+// objective, damping x10 on a singular point system / linear failure, /10 on acceptance, and
+// termination when the line search fails.  Trial step lengths are evaluated in batches on the
+// device; the first one that meets the reference rule is accepted, so the accepted step equals
+// the serial search's.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <memory>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "pb_kernels.h"
+
+using namespace pb;
+
+namespace {
+
+constexpr double kNaN = std::numeric_limits<double>::quiet_NaN();
+constexpr double kInfD = std::numeric_limits<double>::infinity();
+
+struct DeviceArena {
+    std::vector<void*> blocks;
+    size_t bytes = 0;
+    template <typename T>
+    T* alloc(size_t count) {
+        if (count == 0) count = 1;
+        void* p = nullptr;
+        if (cudaMalloc(&p, count * sizeof(T)) != cudaSuccess) throw std::bad_alloc();
+        blocks.push_back(p);
+        bytes += count * sizeof(T);
+        return static_cast<T*>(p);
+    }
+    void release() {
+        for (void* p : blocks) cudaFree(p);
+        blocks.clear();
+        bytes = 0;
+    }
+};
+
+struct CudaError : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+
+void check(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) throw CudaError(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+template <typename T>
+struct PrecisionBuffers {
+    bool ready = false;
+    AsmOut out{};
+    RedOut<T> red{};
+    PcgSystem<T> sys{};
+    T* x = nullptr;
+    T* work = nullptr;
+    T* bvec = nullptr;  // right-hand side handed to the PCG (refinement residual on the mixed path)
+    int pcg_grid = 1;
+};
+
+}  // namespace
+
+struct pb_gpu_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string error;
+    HostModel model;
+    bool uploaded = false;
+    long long structure_hash = 0;
+    int pattern_builds = 0, pattern_reuses = 0;
+    DeviceArena arena;   // structure buffers
+    DeviceArena parena[2];
+    Shape S[2]{};
+    DevPtrs D[2]{};
+    PrecisionBuffers<double> p64;
+    PrecisionBuffers<float> p32;
+    // shared FP64 buffers
+    double* groups_init = nullptr;
+    double* step_c = nullptr;
+    double* step_p = nullptr;
+    double* direct64 = nullptr;
+    double* rhs64 = nullptr;
+    double* x64 = nullptr;
+    double* r64 = nullptr;
+    double* res_out = nullptr;
+    double* bs_part = nullptr;
+    double* bs_out = nullptr;
+    double* cost_part = nullptr;
+    double* cost_out = nullptr;
+    double* alphas_d = nullptr;
+    double* pcg_part = nullptr;
+    PcgResult* pcg_res = nullptr;
+    int* pre_status = nullptr;
+    double* rms_before_d = nullptr;
+    double* rms_after_d = nullptr;
+    double* init_points_all = nullptr;
+    int* proc_of_track = nullptr;
+    // pinned host scratch
+    double* h_scratch = nullptr;
+    // results of the last solve
+    std::vector<double> rms_before, rms_after;
+    std::vector<signed char> valid;
+    int last_precision = PB_PRECISION_FP64;
+    bool have_system = false;
+    volatile int cancel = 0;
+    // timing
+    bool timing = false;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    double kt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    int launches = 0;
+    int solved = 0;
+};
+
+namespace {
+
+size_t smem_budget(int device) {
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+    return v > 0 ? static_cast<size_t>(v) - 1024 : 48 * 1024;
+}
+
+template <typename T>
+void upload(T* dst, const std::vector<T>& src, cudaStream_t st) {
+    if (!src.empty()) check(cudaMemcpyAsync(dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice, st), "H2D");
+}
+
+template <typename T>
+T* upload_new(DeviceArena& a, const std::vector<T>& src, cudaStream_t st) {
+    T* p = a.alloc<T>(src.size());
+    upload(p, src, st);
+    return p;
+}
+
+void group_record(const HostGroup& g, double* rec) {
+    for (int p = 0; p < kP; ++p) {
+        rec[p] = g.params[p];
+        rec[kP + p] = g.prior[p];
+        rec[2 * kP + p] = g.invSigma[p];
+        rec[3 * kP + p] = g.lower[p];
+        rec[4 * kP + p] = g.upper[p];
+        rec[5 * kP + p] = g.enabled[p] ? 1.0 : 0.0;
+    }
+}
+
+// Builds the structure buffers shared by both precisions.
+void upload_structure(pb_gpu_ctx* c) {
+    HostModel& m = c->model;
+    DeviceArena& A = c->arena;
+    cudaStream_t st = c->stream;
+    const int nc = m.nc, nt = m.nt, ntp = static_cast<int>(m.trk_order.size());
+    const long long nop = static_cast<long long>(m.p_obs_orig.size());
+    DevPtrs D{};
+    Shape S{};
+    S.nc = nc;
+    S.ntp = ntp;
+    S.nop = nop;
+    S.ncb = m.ncb;
+    S.ng = m.ng;
+    S.ni = m.ni;
+    S.nb = m.ng * m.ni;
+    S.n = 6 * m.ncb + S.nb;
+    S.nupper = static_cast<int>(m.up_row.size());
+    S.nnzb = static_cast<int>(m.col_idx.size());
+    S.gauge_anchor = m.gauge_anchor;
+    S.gauge_scale = m.gauge_scale;
+    S.gauge_baseline = m.gauge_baseline;
+    for (int i = 0; i < kMaxNI; ++i) S.int_cols[i] = i < m.ni ? m.int_cols[i] : 0;
+
+    D.cams_input = upload_new(A, m.cams_in, st);
+    D.cams_ref = upload_new(A, m.cams_ref, st);
+    D.cams_state = A.alloc<double>(m.cams_in.size());
+    D.cams_eff = A.alloc<double>(m.cams_in.size());
+    D.cams_trial = A.alloc<double>(static_cast<size_t>(kMaxAlpha) * m.cams_in.size());
+    D.cam_block = upload_new(A, m.camera_block, st);
+    std::vector<int> grp(nc, -1);
+    if (m.ng > 0) grp = m.calib_group;
+    D.cam_group = upload_new(A, grp, st);
+    std::vector<double> groups(std::max(1, m.ng) * kGroupRec, 0.0);
+    for (int g = 0; g < m.ng; ++g) group_record(m.groups[g], &groups[static_cast<size_t>(g) * kGroupRec]);
+    c->groups_init = upload_new(A, groups, st);
+    D.groups = A.alloc<double>(groups.size());
+    D.groups_trial = A.alloc<double>(static_cast<size_t>(kMaxAlpha) * groups.size());
+    D.gauge_basis = A.alloc<double>(12);
+    check(cudaMemsetAsync(D.gauge_basis, 0, 12 * sizeof(double), st), "memset");
+    // tracks in processing order
+    std::vector<int> tblock(ntp), torig(ntp);
+    std::vector<double> pts(static_cast<size_t>(ntp) * 3);
+    for (int p = 0; p < ntp; ++p) {
+        const int t = m.trk_order[p];
+        torig[p] = t;
+        tblock[p] = m.track_block[t];
+        for (int a = 0; a < 3; ++a) pts[static_cast<size_t>(p) * 3 + a] = m.points_in[static_cast<size_t>(t) * 3 + a];
+    }
+    D.trk_obs_begin = upload_new(A, m.trk_obs_begin, st);
+    D.trk_block = upload_new(A, tblock, st);
+    D.trk_orig = upload_new(A, torig, st);
+    D.points0 = upload_new(A, pts, st);
+    D.points = A.alloc<double>(pts.size());
+    // observations in processing order
+    std::vector<int> ocam(nop), otrk(nop);
+    std::vector<double> ou(nop), ov(nop), ow(nop);
+    for (int p = 0; p < ntp; ++p)
+        for (int o = m.trk_obs_begin[p]; o < m.trk_obs_begin[p + 1]; ++o) otrk[o] = p;
+    for (long long o = 0; o < nop; ++o) {
+        const int k = m.p_obs_orig[o];
+        ocam[o] = m.obs_cam[k];
+        ou[o] = m.obs_u[k];
+        ov[o] = m.obs_v[k];
+        const double w = std::isfinite(m.obs_weight[k]) && m.obs_weight[k] > 0 ? m.obs_weight[k] : 0.0;
+        const double s = std::isfinite(m.obs_scale[k]) && m.obs_scale[k] > 0 ? m.obs_scale[k] : 1.0;
+        ow[o] = w / (s * s);
+    }
+    D.obs_cam = upload_new(A, ocam, st);
+    D.obs_u = upload_new(A, ou, st);
+    D.obs_v = upload_new(A, ov, st);
+    D.obs_w = upload_new(A, ow, st);
+    D.obs_trk = upload_new(A, otrk, st);
+    D.obs_orig = upload_new(A, m.p_obs_orig, st);
+    // pose CSR
+    D.row_ptr = upload_new(A, m.row_ptr, st);
+    D.col_idx = upload_new(A, m.col_idx, st);
+    D.diag_pos = upload_new(A, m.diag_pos, st);
+    D.up_csr = upload_new(A, m.up_csr, st);
+    D.up_csr_t = upload_new(A, m.up_csr_t, st);
+    // raw observations for the strict RMS
+    std::vector<int> rbad(m.no, 0);
+    std::vector<double> rw(m.no, 0.0);
+    for (long long k = 0; k < m.no; ++k) {
+        const double w = std::isfinite(m.obs_weight[k]) && m.obs_weight[k] > 0 ? m.obs_weight[k] : 0.0;
+        const double s = std::isfinite(m.obs_scale[k]) && m.obs_scale[k] > 0 ? m.obs_scale[k] : 1.0;
+        rw[k] = w / (s * s);
+        const int cam = m.obs_cam[k];
+        rbad[k] = (rw[k] > 0.0 && (cam < 0 || cam >= nc || !std::isfinite(m.obs_u[k]) || !std::isfinite(m.obs_v[k]))) ? 1 : 0;
+    }
+    std::vector<int> rcam(m.obs_cam);
+    for (auto& v : rcam) v = (v >= 0 && v < nc) ? v : 0;
+    D.raw_offsets = upload_new(A, m.offs, st);
+    D.raw_cam = upload_new(A, rcam, st);
+    D.raw_u = upload_new(A, m.obs_u, st);
+    D.raw_v = upload_new(A, m.obs_v, st);
+    D.raw_w = upload_new(A, rw, st);
+    D.raw_bad = upload_new(A, rbad, st);
+    c->init_points_all = upload_new(A, m.points_in, st);
+    std::vector<int> pot(nt, -1);
+    for (int p = 0; p < ntp; ++p) pot[m.trk_order[p]] = p;
+    c->proc_of_track = upload_new(A, pot, st);
+    // FP64 work buffers
+    const int n = S.n;
+    c->step_c = A.alloc<double>(n);
+    c->step_p = A.alloc<double>(static_cast<size_t>(ntp) * 3);
+    c->direct64 = A.alloc<double>(n);
+    c->rhs64 = A.alloc<double>(n);
+    c->x64 = A.alloc<double>(n);
+    c->r64 = A.alloc<double>(n);
+    c->res_out = A.alloc<double>(2 + static_cast<size_t>(std::max(1, (m.ncb + 7) / 8)) * kMaxNB);
+    const int bs_blocks = std::max(1, (ntp + 255) / 256);
+    c->bs_part = A.alloc<double>(2 * static_cast<size_t>(bs_blocks));
+    c->bs_out = A.alloc<double>(4);
+    const long long cost_blocks = std::max<long long>(1, (nop + 255) / 256);
+    c->cost_part = A.alloc<double>(static_cast<size_t>(cost_blocks) * kMaxAlpha * 2);
+    c->cost_out = A.alloc<double>(kMaxAlpha);
+    c->alphas_d = A.alloc<double>(kMaxAlpha);
+    c->pcg_res = A.alloc<PcgResult>(1);
+    c->pre_status = A.alloc<int>(1);
+    c->rms_before_d = A.alloc<double>(nt);
+    c->rms_after_d = A.alloc<double>(nt);
+    c->S[0] = c->S[1] = S;
+    c->D[0] = c->D[1] = D;
+    // strict RMS before (input cameras, initial points)
+    launch_strict_rms(S, D, D.cams_input, c->init_points_all, c->proc_of_track, 0, nt, c->rms_before_d, st);
+    c->rms_before.assign(nt, 0.0);
+    check(cudaMemcpyAsync(c->rms_before.data(), c->rms_before_d, nt * sizeof(double), cudaMemcpyDeviceToHost, st), "D2H");
+    check(cudaStreamSynchronize(st), "upload");
+}
+
+template <typename T>
+PrecisionBuffers<T>& pbuf(pb_gpu_ctx* c);
+template <>
+PrecisionBuffers<double>& pbuf<double>(pb_gpu_ctx* c) { return c->p64; }
+template <>
+PrecisionBuffers<float>& pbuf<float>(pb_gpu_ctx* c) { return c->p32; }
+
+template <typename T>
+void prepare_precision(pb_gpu_ctx* c, int precision) {
+    PrecisionBuffers<T>& B = pbuf<T>(c);
+    if (B.ready) return;
+    HostModel& m = c->model;
+    std::string err;
+    if (!m.chunks_ready[precision]) {
+        const int rc = build_chunks(&m, precision, smem_budget(c->device), &err);
+        if (rc) throw std::runtime_error(err);
+    }
+    const ChunkSet& cs = m.chunks[precision];
+    DeviceArena& A = c->parena[precision];
+    cudaStream_t st = c->stream;
+    Shape& S = c->S[precision];
+    DevPtrs& D = c->D[precision];
+    S.nchunks = cs.n();
+    S.max_obs = cs.max_obs;
+    S.max_cams = cs.max_cams;
+    S.max_pairs = cs.max_pairs;
+    D.ch_obs_begin = upload_new(A, cs.obs_begin, st);
+    D.ch_cam_begin = upload_new(A, cs.cam_begin, st);
+    D.ch_cams = upload_new(A, cs.cams, st);
+    D.ch_pair_begin = upload_new(A, cs.pair_begin, st);
+    D.ch_pairs = upload_new(A, cs.pairs, st);
+    D.up_contrib_begin = upload_new(A, cs.up_contrib_begin, st);
+    D.up_contrib = upload_new(A, cs.up_contrib, st);
+    D.cam_contrib_begin = upload_new(A, cs.cam_contrib_begin, st);
+    D.cam_contrib = upload_new(A, cs.cam_contrib, st);
+    D.obs_lcam = upload_new(A, cs.obs_lcam, st);
+    const int camrec = 12 + S.ng * 6 * S.ni, chrec = S.nb * S.nb + 2 * S.nb;
+    B.out.part_pair_v = A.alloc<T>(cs.n_pair_partials() * 36);
+    B.out.part_cam_v = A.alloc<T>(cs.n_cam_partials() * camrec);
+    B.out.part_chunk_v = A.alloc<T>(static_cast<size_t>(std::max(1, S.nchunks)) * std::max(1, chrec));
+    B.out.part_cost = A.alloc<double>(std::max(1, S.nchunks));
+    B.out.part_flags = A.alloc<int>(std::max(1, S.nchunks));
+    B.out.trk_data_v = A.alloc<T>(static_cast<size_t>(S.ntp) * kTrackRec);
+    B.out.obs_wn_v = A.alloc<T>(static_cast<size_t>(S.nop));
+    B.red.vals = A.alloc<T>(static_cast<size_t>(S.nnzb) * 36);
+    B.red.border = A.alloc<T>(static_cast<size_t>(S.ncb) * 6 * std::max(1, S.nb));
+    B.red.Cm = A.alloc<T>(static_cast<size_t>(std::max(1, S.nb * S.nb)));
+    B.red.rhs = A.alloc<T>(S.n);
+    B.red.direct = A.alloc<T>(S.n);
+    B.red.result = A.alloc<double>(2);
+    check(cudaMemsetAsync(B.red.vals, 0, static_cast<size_t>(std::max(1, S.nnzb)) * 36 * sizeof(T), st), "memset");
+    check(cudaMemsetAsync(B.red.border, 0, static_cast<size_t>(std::max(1, S.ncb)) * 6 * std::max(1, S.nb) * sizeof(T), st),
+          "memset");
+    B.sys.ncb = S.ncb;
+    B.sys.nb = S.nb;
+    B.sys.ng = S.ng;
+    B.sys.ni = S.ni;
+    B.sys.row_ptr = D.row_ptr;
+    B.sys.col_idx = D.col_idx;
+    B.sys.diag_pos = D.diag_pos;
+    B.sys.vals = B.red.vals;
+    B.sys.border = B.red.border;
+    B.sys.Cm = B.red.Cm;
+    B.sys.Dinv = A.alloc<T>(static_cast<size_t>(std::max(1, S.ncb)) * 36);
+    B.sys.Cinv = A.alloc<T>(static_cast<size_t>(std::max(1, S.ng)) * kMaxNI * kMaxNI);
+    B.x = A.alloc<T>(S.n);
+    B.work = A.alloc<T>(static_cast<size_t>(S.n) * 4);
+    B.bvec = A.alloc<T>(S.n);
+    B.pcg_grid = pcg_grid_size<T>(S.ncb);
+    c->pcg_part = nullptr;
+    const size_t smem = chunk_smem_bytes(precision, S.max_obs, S.max_cams, S.max_pairs, S.ng, S.ni);
+    // opt in to the large shared-memory carve-out for the assembly kernel
+    (void)smem;
+    B.ready = true;
+    check(cudaStreamSynchronize(st), "prepare");
+}
+
+void ensure_pcg_partials(pb_gpu_ctx* c) {
+    if (c->pcg_part) return;
+    const int grid = std::max(c->p64.ready ? c->p64.pcg_grid : 1, c->p32.ready ? c->p32.pcg_grid : 1);
+    c->pcg_part = c->arena.alloc<double>(static_cast<size_t>(2 * std::max(grid, 160)) * (2 + kMaxNB));
+}
+
+void set_assemble_smem(int precision, size_t bytes);
+
+struct Timer {
+    pb_gpu_ctx* c;
+    int slot;
+    Timer(pb_gpu_ctx* ctx, int s) : c(ctx), slot(s) {
+        if (c->timing) cudaEventRecord(c->ev0, c->stream);
+    }
+    ~Timer() {
+        if (!c->timing) return;
+        cudaEventRecord(c->ev1, c->stream);
+        cudaEventSynchronize(c->ev1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+        c->kt[2 * slot] += ms;
+        c->kt[2 * slot + 1] += 1;
+    }
+};
+
+template <typename T>
+void assemble(pb_gpu_ctx* c, double damping, int precision, double* cost, int* flags) {
+    prepare_precision<T>(c, precision);
+    PrecisionBuffers<T>& B = pbuf<T>(c);
+    const Shape& S = c->S[precision];
+    const DevPtrs& D = c->D[precision];
+    const size_t smem = chunk_smem_bytes(precision, S.max_obs, S.max_cams, S.max_pairs, S.ng, S.ni);
+    set_assemble_smem(precision, smem);
+    {
+        Timer t(c, 0);
+        launch_assemble<T>(S, D, B.out, damping, smem, c->stream);
+        c->launches += S.nchunks > 0 ? 1 : 0;
+    }
+    {
+        Timer t(c, 3);
+        launch_reduce<T>(S, D, B.out, B.red, damping, c->stream);
+        c->launches += 4;
+    }
+    to_double(B.red.direct, c->direct64, S.n, c->stream);
+    c->launches += 1;
+    check(cudaGetLastError(), "assemble launch");
+    check(cudaMemcpyAsync(c->h_scratch, B.red.result, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "D2H");
+    check(cudaStreamSynchronize(c->stream), "assemble");
+    *cost = c->h_scratch[0];
+    *flags = static_cast<int>(c->h_scratch[1]);
+    c->last_precision = precision;
+    c->have_system = true;
+}
+
+// Reduced solve.  Returns 0 ok, 1 breakdown / not positive definite, and sets converged/iterations.
+template <typename T>
+int solve_reduced_t(pb_gpu_ctx* c, const pb_solve_options& op, bool* converged, int* iterations, double* relres,
+                    int* sweeps) {
+    const int precision = c->last_precision;
+    PrecisionBuffers<T>& B = pbuf<T>(c);
+    const Shape& S = c->S[precision];
+    ensure_pcg_partials(c);
+    cudaStream_t st = c->stream;
+    check(cudaMemsetAsync(c->pre_status, 0, sizeof(int), st), "memset");
+    pcg_precondition<T>(B.sys, c->pre_status, st);
+    c->launches += 1;
+    const double rel = op.linear_relative_tolerance > 0 ? op.linear_relative_tolerance : 2.0e-10;
+    const double abs_tol = op.linear_absolute_tolerance > 0 ? op.linear_absolute_tolerance : 1.0e-12;
+    const int P = c->model.P;
+    const int max_it = op.max_linear_iterations > 0 ? op.max_linear_iterations : std::max(200, 30 * P);
+    *iterations = 0;
+    *sweeps = 0;
+    *converged = false;
+    PcgResult res{};
+    if (precision == PB_PRECISION_FP64) {
+        {
+            Timer t(c, 1);
+            if (pcg_solve<T>(B.sys, B.red.rhs, B.x, B.work, c->pcg_part, c->pcg_res, abs_tol, rel, max_it, B.pcg_grid, st))
+                throw CudaError(std::string("PCG launch failed: ") + cudaGetErrorString(cudaGetLastError()));
+            c->launches += 1;
+        }
+        check(cudaMemcpyAsync(c->h_scratch, c->pre_status, sizeof(int), cudaMemcpyDeviceToHost, st), "D2H");
+        check(cudaMemcpyAsync(c->h_scratch + 1, c->pcg_res, sizeof(PcgResult), cudaMemcpyDeviceToHost, st), "D2H");
+        check(cudaStreamSynchronize(st), "pcg");
+        int pre;
+        std::memcpy(&pre, c->h_scratch, sizeof(int));
+        std::memcpy(&res, c->h_scratch + 1, sizeof(PcgResult));
+        if (pre || res.status) return 1;
+        to_double(B.x, c->step_c, S.n, st);
+        c->launches += 1;
+        *converged = res.converged != 0;
+        *iterations = res.iterations;
+        *relres = res.bnorm > 0 ? res.rnorm / res.bnorm : 0.0;
+        return 0;
+    }
+    // mixed: FP32 PCG corrections against an FP64-accumulated residual of the stored system
+    const int max_sweeps = std::min(3, std::max(1, op.refinement_sweeps));
+    to_double(B.red.rhs, c->rhs64, S.n, st);
+    check(cudaMemsetAsync(c->x64, 0, S.n * sizeof(double), st), "memset");
+    c->launches += 1;
+    for (int sweep = 0;; ++sweep) {
+        residual64<T>(B.sys, c->rhs64, c->x64, c->r64, c->res_out, st);
+        c->launches += 2;
+        check(cudaMemcpyAsync(c->h_scratch, c->res_out, 2 * sizeof(double), cudaMemcpyDeviceToHost, st), "D2H");
+        check(cudaStreamSynchronize(st), "residual");
+        const double rn = c->h_scratch[0], bn = c->h_scratch[1];
+        *relres = bn > 0 ? rn / bn : 0.0;
+        if (!std::isfinite(rn)) return 1;
+        if (rn <= std::max(rel * bn, abs_tol)) {
+            *converged = true;
+            break;
+        }
+        if (sweep > max_sweeps) break;
+        to_float(c->r64, reinterpret_cast<float*>(B.bvec), S.n, st);
+        {
+            Timer t(c, 1);
+            if (pcg_solve<T>(B.sys, B.bvec, B.x, B.work, c->pcg_part, c->pcg_res, 0.0, 1.0e-5, max_it, B.pcg_grid, st))
+                throw CudaError(std::string("PCG launch failed: ") + cudaGetErrorString(cudaGetLastError()));
+            c->launches += 2;
+        }
+        check(cudaMemcpyAsync(c->h_scratch, c->pre_status, sizeof(int), cudaMemcpyDeviceToHost, st), "D2H");
+        check(cudaMemcpyAsync(c->h_scratch + 1, c->pcg_res, sizeof(PcgResult), cudaMemcpyDeviceToHost, st), "D2H");
+        check(cudaStreamSynchronize(st), "pcg");
+        int pre;
+        std::memcpy(&pre, c->h_scratch, sizeof(int));
+        std::memcpy(&res, c->h_scratch + 1, sizeof(PcgResult));
+        if (pre || res.status) return 1;
+        *iterations += res.iterations;
+        axpy64(c->x64, reinterpret_cast<const float*>(B.x), S.n, st);
+        c->launches += 1;
+        *sweeps = sweep + 1;
+    }
+    check(cudaMemcpyAsync(c->step_c, c->x64, S.n * sizeof(double), cudaMemcpyDeviceToDevice, st), "D2D");
+    return 0;
+}
+
+int solve_reduced(pb_gpu_ctx* c, const pb_solve_options& op, bool* converged, int* iterations, double* relres,
+                  int* sweeps) {
+    return c->last_precision == PB_PRECISION_FP64 ? solve_reduced_t<double>(c, op, converged, iterations, relres, sweeps)
+                                                  : solve_reduced_t<float>(c, op, converged, iterations, relres, sweeps);
+}
+
+void back_substitute(pb_gpu_ctx* c, double* dd, double* point_sq, double* cam_sq) {
+    const int precision = c->last_precision;
+    const Shape& S = c->S[precision];
+    const DevPtrs& D = c->D[precision];
+    if (precision == PB_PRECISION_FP64)
+        launch_back_substitute<double>(S, D, static_cast<const double*>(c->p64.out.trk_data_v),
+                                       static_cast<const double*>(c->p64.out.obs_wn_v), c->step_c, c->step_p,
+                                       c->bs_part, c->direct64, c->bs_out, c->stream);
+    else
+        launch_back_substitute<float>(S, D, static_cast<const float*>(c->p32.out.trk_data_v),
+                                      static_cast<const float*>(c->p32.out.obs_wn_v), c->step_c, c->step_p, c->bs_part,
+                                      c->direct64, c->bs_out, c->stream);
+    c->launches += 2;
+    check(cudaGetLastError(), "back-substitution launch");
+    check(cudaMemcpyAsync(c->h_scratch, c->bs_out, 3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "D2H");
+    check(cudaStreamSynchronize(c->stream), "back-substitution");
+    *dd = c->h_scratch[0];
+    *point_sq = c->h_scratch[1];
+    *cam_sq = c->h_scratch[2];
+}
+
+void eval_costs(pb_gpu_ctx* c, const double* alphas, int n, int use_trial, double* out) {
+    const Shape& S = c->S[0];
+    const DevPtrs& D = c->D[0];
+    if (use_trial) {
+        std::memcpy(c->h_scratch + 16, alphas, n * sizeof(double));
+        check(cudaMemcpyAsync(c->alphas_d, c->h_scratch + 16, n * sizeof(double), cudaMemcpyHostToDevice, c->stream), "H2D");
+    }
+    {
+        Timer t(c, 2);
+        launch_cost(S, D, c->step_c, c->step_p, c->alphas_d, n, use_trial, c->cost_part, c->cost_out, c->stream);
+        c->launches += use_trial ? 3 : 2;
+    }
+    check(cudaGetLastError(), "cost launch");
+    check(cudaMemcpyAsync(c->h_scratch, c->cost_out, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "D2H");
+    check(cudaStreamSynchronize(c->stream), "cost");
+    std::memcpy(out, c->h_scratch, n * sizeof(double));
+}
+
+void reset_state(pb_gpu_ctx* c) {
+    const HostModel& m = c->model;
+    const DevPtrs& D = c->D[0];
+    cudaStream_t st = c->stream;
+    check(cudaMemcpyAsync(D.cams_state, D.cams_input, m.cams_in.size() * sizeof(double), cudaMemcpyDeviceToDevice, st), "D2D");
+    check(cudaMemcpyAsync(D.groups, c->groups_init, static_cast<size_t>(std::max(1, m.ng)) * kGroupRec * sizeof(double),
+                          cudaMemcpyDeviceToDevice, st),
+          "D2D");
+    check(cudaMemcpyAsync(D.points, D.points0, m.trk_order.size() * 3 * sizeof(double), cudaMemcpyDeviceToDevice, st), "D2D");
+    launch_effective(c->S[0], D, st);
+    c->launches += 1;
+    c->have_system = false;
+}
+
+void finalize_quality(pb_gpu_ctx* c, const pb_solve_options& op, pb_solve_report* rep) {
+    const HostModel& m = c->model;
+    const int nt = m.nt;
+    launch_strict_rms(c->S[0], c->D[0], c->D[0].cams_eff, c->init_points_all, c->proc_of_track, 1, nt, c->rms_after_d,
+                      c->stream);
+    c->launches += 1;
+    c->rms_after.assign(nt, 0.0);
+    check(cudaMemcpyAsync(c->rms_after.data(), c->rms_after_d, nt * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "D2H");
+    check(cudaStreamSynchronize(c->stream), "quality");
+    // finalizeBundleAdjustResult (BundleAdjustQuality.cpp:403-502)
+    c->valid.assign(nt, 0);
+    std::vector<double> cand;
+    for (int t = 0; t < nt; ++t) {
+        if (!m.active_track[t]) {
+            c->rms_after[t] = kInfD;
+            continue;
+        }
+        c->valid[t] = std::isfinite(c->rms_after[t]) ? 1 : 0;
+        if (c->valid[t]) cand.push_back(c->rms_after[t]);
+    }
+    double thr = kInfD;
+    if (op.enable_point_filter) {
+        thr = std::isfinite(op.filter_max_reproj_error) && op.filter_max_reproj_error >= 0 ? op.filter_max_reproj_error : 0.0;
+        if (!cand.empty() && std::isfinite(op.filter_sigma_factor) && op.filter_sigma_factor > 0.0)
+            thr = std::max(thr, op.filter_sigma_factor * finite_median(cand, 0.0));
+    }
+    double sb = 0.0, sa = 0.0;
+    int kept = 0;
+    for (int t = 0; t < nt; ++t) {
+        if (c->valid[t] && c->rms_after[t] > thr) c->valid[t] = 0;
+        if (c->valid[t]) {
+            ++kept;
+            sb += c->rms_before[t];
+            sa += c->rms_after[t];
+        }
+    }
+    rep->filter_threshold = thr;
+    rep->optimized_tracks = kept;
+    rep->mean_rms_before = kept ? sb / kept : kInfD;
+    rep->mean_rms_after = kept ? sa / kept : kInfD;
+    rep->valid_track_ratio = nt ? static_cast<double>(kept) / nt : 0.0;
+    if (kept == 0 && (rep->status == PB_SOLVE_SUCCESS || rep->status == PB_SOLVE_NO_CONVERGENCE)) {
+        rep->status = PB_SOLVE_NUMERICAL_FAILURE;
+        rep->solution_usable = 0;
+    }
+}
+
+int do_assemble(pb_gpu_ctx* c, double damping, int precision, double* cost, int* flags) {
+    if (precision == PB_PRECISION_FP64) assemble<double>(c, damping, precision, cost, flags);
+    else assemble<float>(c, damping, precision, cost, flags);
+    return 0;
+}
+
+// The LM / Armijo driver (online branch of optimizePointsWithPlaMatrix).
+void lm_solve(pb_gpu_ctx* c, const pb_solve_options& op, pb_solve_report* rep) {
+    const auto t0 = std::chrono::steady_clock::now();
+    const HostModel& m = c->model;
+    std::memset(rep, 0, sizeof(*rep));
+    for (double& v : c->kt) v = 0.0;
+    c->launches = 0;
+    rep->active_tracks = m.active_tracks;
+    rep->observation_count = m.obs_count;
+    rep->rejected_initial_tracks = m.rejected;
+    rep->camera_blocks = m.ncb;
+    rep->intrinsic_blocks = m.ng;
+    rep->pattern_builds = c->pattern_builds;
+    rep->pattern_reuses = c->pattern_reuses;
+    reset_state(c);
+    if (m.obs_count == 0) {
+        rep->status = PB_SOLVE_INVALID_INPUT;
+        return;
+    }
+    const int precision = op.precision == PB_PRECISION_MIXED ? PB_PRECISION_MIXED : PB_PRECISION_FP64;
+    double current = kNaN, damping = 0.0;
+    int iterations = 0;
+    bool converged = m.P == 0 && m.ntb == 0;
+    bool failed = false, cancelled = false;
+    const double n_global = static_cast<double>(6 * m.ncb + m.ng * m.ni);
+    const double n_point = 3.0 * m.ntb;
+    auto t_asm = 0.0, t_lin = 0.0, t_bs = 0.0, t_obj = 0.0;
+    auto now = [] { return std::chrono::steady_clock::now(); };
+    auto ms = [](std::chrono::steady_clock::time_point a, std::chrono::steady_clock::time_point b) {
+        return std::chrono::duration<double, std::milli>(b - a).count();
+    };
+    try {
+        if (converged) {
+            double cst;
+            eval_costs(c, nullptr, 1, 0, &cst);
+            current = cst;
+            rep->initial_cost = current;
+            ++rep->objective_evaluations;
+        }
+        const int budget = std::max(1, op.max_iterations);
+        bool terminate = false;
+        while (iterations < budget && !converged && !terminate) {
+            if (c->cancel) { cancelled = true; break; }
+            bool relinearize = false;
+            while (iterations < budget && !converged && !relinearize) {
+                if (c->cancel) { cancelled = true; break; }
+                double cost;
+                int flags;
+                auto ta = now();
+                do_assemble(c, damping, precision, &cost, &flags);
+                t_asm += ms(ta, now());
+                if (flags & 4) throw std::runtime_error("assembly chunk table inconsistent (bounds check)");
+                if (flags & 2) throw std::runtime_error("online Schur linearisation produced an invalid projection");
+                ++rep->linearizations;
+                ++rep->objective_evaluations;
+                current = cost;
+                if (rep->linearizations == 1) rep->initial_cost = current;
+                if (flags & 1) {
+                    ++iterations;
+                    ++rep->rejected_steps;
+                    damping = damping == 0.0 ? 1e-3 : damping * 10.0;
+                    continue;
+                }
+                bool lconv = false;
+                int lit = 0, sweeps = 0;
+                double relres = 0.0;
+                auto tl = now();
+                const int lrc = solve_reduced(c, op, &lconv, &lit, &relres, &sweeps);
+                t_lin += ms(tl, now());
+                if (lrc) {
+                    ++iterations;
+                    ++rep->rejected_steps;
+                    damping = damping == 0.0 ? 1e-3 : damping * 10.0;
+                    continue;
+                }
+                rep->linear_iterations += lit;
+                rep->refinement_sweeps += sweeps;
+                ++iterations;
+                if (!lconv) {
+                    ++rep->rejected_steps;
+                    damping = damping == 0.0 ? 1e-3 : damping * 10.0;
+                    continue;
+                }
+                double dd, psq, csq;
+                auto tb = now();
+                back_substitute(c, &dd, &psq, &csq);
+                t_bs += ms(tb, now());
+                if (!std::isfinite(dd)) {
+                    ++rep->rejected_steps;
+                    damping = damping == 0.0 ? 1e-3 : damping * 10.0;
+                    continue;
+                }
+                const double rg = n_global > 0 ? std::sqrt(csq / n_global) : 0.0;
+                const double rp = n_point > 0 ? std::sqrt(psq / n_point) : 0.0;
+                // Armijo: alpha_k = 2^-k, first k with cost <= f - c alpha dd and cost < f
+                double cand = kInfD, alpha = 1.0;
+                int accepted_slot = -1;
+                double accepted_alpha = 1.0;
+                int k0 = 0;
+                auto tc = now();
+                while (k0 < op.line_search_steps && accepted_slot < 0) {
+                    const int nbatch = std::min(k0 == 0 ? 1 : kMaxAlpha, op.line_search_steps - k0);
+                    double al[kMaxAlpha], costs[kMaxAlpha];
+                    for (int i = 0; i < nbatch; ++i) al[i] = std::ldexp(1.0, -(k0 + i));
+                    eval_costs(c, al, nbatch, 1, costs);
+                    for (int i = 0; i < nbatch; ++i) {
+                        ++rep->objective_evaluations;
+                        cand = costs[i];
+                        alpha = al[i];
+                        const double limit = current - op.armijo_coefficient * alpha * dd;
+                        if (std::isfinite(cand) && cand <= limit && cand < current) {
+                            accepted_slot = i;
+                            accepted_alpha = alpha;
+                            break;
+                        }
+                    }
+                    k0 += nbatch;
+                }
+                t_obj += ms(tc, now());
+                if (accepted_slot >= 0) {
+                    launch_accept(c->S[0], c->D[0], c->step_p, accepted_alpha, accepted_slot, c->stream);
+                    c->launches += 1;
+                    current = cand;
+                    ++rep->accepted_steps;
+                    damping /= 10.0;
+                    converged = accepted_alpha * rg <= 1e-6 && accepted_alpha * rp <= 1e-6;
+                    relinearize = !converged;
+                } else {
+                    ++rep->rejected_steps;
+                    terminate = true;
+                    relinearize = true;
+                }
+            }
+        }
+        check(cudaStreamSynchronize(c->stream), "solve");
+    } catch (const CudaError&) {
+        throw;
+    } catch (const std::exception& e) {
+        failed = true;
+        c->error = e.what();
+    }
+    rep->iterations = iterations;
+    rep->final_cost = current;
+    rep->assembly_ms = t_asm;
+    rep->linear_ms = t_lin;
+    rep->back_substitution_ms = t_bs;
+    rep->objective_ms = t_obj;
+    if (cancelled) {
+        reset_state(c);
+        check(cudaStreamSynchronize(c->stream), "reset");
+        rep->status = PB_SOLVE_CANCELLED;
+        rep->solution_usable = 0;
+    } else if (failed) {
+        rep->status = PB_SOLVE_NUMERICAL_FAILURE;
+        rep->solution_usable = 0;
+    } else {
+        rep->status = converged ? PB_SOLVE_SUCCESS : PB_SOLVE_NO_CONVERGENCE;
+        rep->solution_usable = std::isfinite(current) ? 1 : 0;
+        finalize_quality(c, op, rep);
+    }
+    rep->gpu_kernel_launches = c->launches;
+    rep->total_ms = ms(t0, now());
+    c->solved = 1;
+}
+
+pb_status fail(pb_gpu_ctx* c, pb_status s, const std::string& msg) {
+    if (c) c->error = msg;
+    return s;
+}
+
+}  // namespace
+
+// Shared-memory opt-in for the assembly kernel (dynamic shared memory above 48 KB).
+namespace {
+void set_assemble_smem(int precision, size_t bytes) {
+    static size_t done[2] = {0, 0};
+    if (done[precision] >= bytes) return;
+    if (precision == PB_PRECISION_FP64) pb_set_assemble_smem_f64(bytes);
+    else pb_set_assemble_smem_f32(bytes);
+    done[precision] = bytes;
+}
+}  // namespace
+
+extern "C" {
+
+const char* pb_status_name(int32_t s) {
+    switch (s) {
+        case PB_OK: return "ok";
+        case PB_ERR_INVALID_ARGUMENT: return "invalid_argument";
+        case PB_ERR_CUDA: return "cuda_error";
+        case PB_ERR_NO_CONVERGENCE: return "no_convergence";
+        case PB_ERR_SINGULAR_BLOCK: return "singular_block";
+        case PB_ERR_CANCELLED: return "cancelled";
+        case PB_ERR_BOUNDS: return "bounds_check";
+        case PB_ERR_TIMEOUT: return "timeout";
+        case PB_ERR_UNSUPPORTED: return "unsupported";
+        case PB_ERR_INVALID_PROJECTION: return "invalid_projection";
+        case PB_ERR_STATE: return "bad_state";
+        default: return "unknown";
+    }
+}
+
+pb_status pb_gpu_create(int32_t device, pb_gpu_ctx** out) {
+    if (!out) return PB_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count) return PB_ERR_CUDA;
+    auto* c = new (std::nothrow) pb_gpu_ctx();
+    if (!c) return PB_ERR_CUDA;
+    c->device = device;
+    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMallocHost(&c->h_scratch, 64 * sizeof(double)) != cudaSuccess ||
+        cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) {
+        delete c;
+        return PB_ERR_CUDA;
+    }
+    *out = c;
+    return PB_OK;
+}
+
+pb_status pb_gpu_destroy(pb_gpu_ctx* c) {
+    if (!c) return PB_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    c->arena.release();
+    c->parena[0].release();
+    c->parena[1].release();
+    if (c->h_scratch) cudaFreeHost(c->h_scratch);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return PB_OK;
+}
+
+const char* pb_gpu_last_error(const pb_gpu_ctx* c) { return c ? c->error.c_str() : "null context"; }
+
+pb_status pb_gpu_upload(pb_gpu_ctx* c, const pb_problem_desc* pr, const pb_solve_options* op) {
+    if (!c || !pr || !op) return fail(c, PB_ERR_INVALID_ARGUMENT, "null argument");
+    try {
+        cudaSetDevice(c->device);
+        HostModel m;
+        std::string err;
+        const int rc = build_host_model(pr, op, &m, &err);
+        if (rc) {
+            c->uploaded = false;
+            return fail(c, rc == PB_SOLVE_UNSUPPORTED ? PB_ERR_UNSUPPORTED : PB_ERR_INVALID_ARGUMENT, err);
+        }
+        const bool reuse = c->uploaded && m.structure_hash == c->structure_hash && c->model.no == m.no;
+        if (reuse) {
+            // same structure: keep pattern, chunks and launch shapes; refresh the numeric inputs
+            m.chunks[0] = std::move(c->model.chunks[0]);
+            m.chunks[1] = std::move(c->model.chunks[1]);
+            m.chunks_ready[0] = c->model.chunks_ready[0];
+            m.chunks_ready[1] = c->model.chunks_ready[1];
+            const bool r64 = c->p64.ready, r32 = c->p32.ready;
+            DevPtrs d0 = c->D[0], d1 = c->D[1];
+            Shape s0 = c->S[0], s1 = c->S[1];
+            c->model = std::move(m);
+            c->arena.release();
+            c->pcg_part = nullptr;
+            upload_structure(c);
+            // restore the chunk fields of the per-precision descriptors
+            auto keep_chunks = [](DevPtrs& dst, const DevPtrs& src, Shape& sd, const Shape& ss) {
+                dst.ch_obs_begin = src.ch_obs_begin; dst.ch_cam_begin = src.ch_cam_begin; dst.ch_cams = src.ch_cams;
+                dst.ch_pair_begin = src.ch_pair_begin; dst.ch_pairs = src.ch_pairs;
+                dst.up_contrib_begin = src.up_contrib_begin; dst.up_contrib = src.up_contrib;
+                dst.cam_contrib_begin = src.cam_contrib_begin; dst.cam_contrib = src.cam_contrib; dst.obs_lcam = src.obs_lcam;
+                sd.nchunks = ss.nchunks; sd.max_obs = ss.max_obs; sd.max_cams = ss.max_cams; sd.max_pairs = ss.max_pairs;
+            };
+            keep_chunks(c->D[0], d0, c->S[0], s0);
+            keep_chunks(c->D[1], d1, c->S[1], s1);
+            // the per-precision system descriptors point at structure buffers that were re-uploaded
+            if (r64) { c->p64.sys.row_ptr = c->D[0].row_ptr; c->p64.sys.col_idx = c->D[0].col_idx; c->p64.sys.diag_pos = c->D[0].diag_pos; }
+            if (r32) { c->p32.sys.row_ptr = c->D[1].row_ptr; c->p32.sys.col_idx = c->D[1].col_idx; c->p32.sys.diag_pos = c->D[1].diag_pos; }
+            ++c->pattern_reuses;
+        } else {
+            c->arena.release();
+            c->parena[0].release();
+            c->parena[1].release();
+            c->p64 = PrecisionBuffers<double>{};
+            c->p32 = PrecisionBuffers<float>{};
+            c->pcg_part = nullptr;
+            c->model = std::move(m);
+            upload_structure(c);
+            ++c->pattern_builds;
+        }
+        c->structure_hash = c->model.structure_hash;
+        c->uploaded = true;
+        c->have_system = false;
+        reset_state(c);
+        check(cudaStreamSynchronize(c->stream), "upload");
+        return PB_OK;
+    } catch (const std::bad_alloc&) {
+        c->uploaded = false;
+        return fail(c, PB_ERR_CUDA, "device allocation failed");
+    } catch (const std::exception& e) {
+        c->uploaded = false;
+        return fail(c, PB_ERR_CUDA, e.what());
+    }
+}
+
+pb_status pb_gpu_reset_state(pb_gpu_ctx* c) {
+    if (!c || !c->uploaded) return fail(c, PB_ERR_STATE, "no problem uploaded");
+    try {
+        reset_state(c);
+        check(cudaStreamSynchronize(c->stream), "reset");
+        return PB_OK;
+    } catch (const std::exception& e) {
+        return fail(c, PB_ERR_CUDA, e.what());
+    }
+}
+
+pb_status pb_gpu_get_sizes(pb_gpu_ctx* c, int64_t* s, double* baseline) {
+    if (!c || !s || !c->uploaded) return fail(c, PB_ERR_STATE, "no problem uploaded");
+    const HostModel& m = c->model;
+    s[0] = m.nc; s[1] = m.nt; s[2] = m.no; s[3] = m.P; s[4] = m.ncb; s[5] = m.ng; s[6] = m.ntb;
+    s[7] = m.active_tracks; s[8] = m.obs_count; s[9] = m.rejected; s[10] = static_cast<int64_t>(m.pairs.size());
+    s[11] = 6 * m.ncb + m.ng * m.ni; s[12] = m.ni; s[13] = m.gauge_anchor; s[14] = m.gauge_scale;
+    s[15] = m.chunks_ready[1] ? m.chunks[1].n() : (m.chunks_ready[0] ? m.chunks[0].n() : 0);
+    if (baseline) *baseline = m.gauge_baseline;
+    return PB_OK;
+}
+
+pb_status pb_gpu_get_active(pb_gpu_ctx* c, int8_t* at, int32_t* cb, int32_t* ib, int32_t* tb) {
+    if (!c || !c->uploaded) return fail(c, PB_ERR_STATE, "no problem uploaded");
+    const HostModel& m = c->model;
+    for (int t = 0; t < m.nt; ++t) {
+        if (at) at[t] = m.active_track[t];
+        if (tb) tb[t] = m.track_block[t];
+    }
+    for (int i = 0; i < m.nc; ++i) {
+        if (cb) cb[i] = m.camera_block[i];
+        if (ib) ib[i] = m.intrinsic_block[i];
+    }
+    return PB_OK;
+}
+
+pb_status pb_gpu_get_pairs(pb_gpu_ctx* c, int32_t* pairs) {
+    if (!c || !pairs || !c->uploaded) return fail(c, PB_ERR_STATE, "no problem uploaded");
+    for (size_t i = 0; i < c->model.pairs.size(); ++i) {
+        pairs[2 * i] = c->model.pairs[i].first;
+        pairs[2 * i + 1] = c->model.pairs[i].second;
+    }
+    return PB_OK;
+}
+
+pb_status pb_gpu_linearize_observations(pb_gpu_ctx* c, int32_t precision, double* res, double* jp, double* jpose,
+                                        double* ji, double* nw, double* cost, int8_t* valid) {
+    if (!c || !c->uploaded) return fail(c, PB_ERR_STATE, "no problem uploaded");
+    try {
+        const HostModel& m = c->model;
+        const size_t no = static_cast<size_t>(m.no);
+        DeviceArena tmp;
+        double* dres = tmp.alloc<double>(no * 2);
+        double* djp = tmp.alloc<double>(no * 6);
+        double* djpose = tmp.alloc<double>(no * 2 * kP);
+        double* dji = tmp.alloc<double>(no * 2 * kP);
+        double* dnw = tmp.alloc<double>(no);
+        double* dcost = tmp.alloc<double>(no);
+        signed char* dvalid = tmp.alloc<signed char>(no);
+        cudaStream_t st = c->stream;
+        check(cudaMemsetAsync(dres, 0, no * 2 * sizeof(double), st), "memset");
+        check(cudaMemsetAsync(djp, 0, no * 6 * sizeof(double), st), "memset");
+        check(cudaMemsetAsync(djpose, 0, no * 2 * kP * sizeof(double), st), "memset");
+        check(cudaMemsetAsync(dji, 0, no * 2 * kP * sizeof(double), st), "memset");
+        check(cudaMemsetAsync(dnw, 0, no * sizeof(double), st), "memset");
+        check(cudaMemsetAsync(dcost, 0, no * sizeof(double), st), "memset");
+        check(cudaMemsetAsync(dvalid, 0, no, st), "memset");
+        if (precision == PB_PRECISION_MIXED)
+            launch_linearize_export<float>(c->S[0], c->D[0], dres, djp, djpose, dji, dnw, dcost, dvalid, st);
+        else
+            launch_linearize_export<double>(c->S[0], c->D[0], dres, djp, djpose, dji, dnw, dcost, dvalid, st);
+        check(cudaGetLastError(), "linearize launch");
+        auto d2h = [&](void* h, const void* d, size_t bytes) {
+            if (h) check(cudaMemcpyAsync(h, d, bytes, cudaMemcpyDeviceToHost, st), "D2H");
+        };
+        d2h(res, dres, no * 2 * sizeof(double));
+        d2h(jp, djp, no * 6 * sizeof(double));
+        d2h(jpose, djpose, no * 2 * kP * sizeof(double));
+        d2h(ji, dji, no * 2 * kP * sizeof(double));
+        d2h(nw, dnw, no * sizeof(double));
+        d2h(cost, dcost, no * sizeof(double));
+        d2h(valid, dvalid, no);
+        check(cudaStreamSynchronize(st), "linearize");
+        tmp.release();
+        return PB_OK;
+    } catch (const std::exception& e) {
+        return fail(c, PB_ERR_CUDA, e.what());
+    }
+}
+
+pb_status pb_gpu_linearize_schur(pb_gpu_ctx* c, double lambda, int32_t precision, double* cost, int32_t* singular) {
+    if (!c || !c->uploaded) return fail(c, PB_ERR_STATE, "no problem uploaded");
+    if (!std::isfinite(lambda) || lambda < 0.0) return fail(c, PB_ERR_INVALID_ARGUMENT, "invalid damping");
+    try {
+        double cst;
+        int flags;
+        do_assemble(c, lambda, precision == PB_PRECISION_MIXED ? PB_PRECISION_MIXED : PB_PRECISION_FP64, &cst, &flags);
+        if (cost) *cost = cst;
+        if (singular) *singular = flags & 1;
+        if (flags & 2) return fail(c, PB_ERR_INVALID_PROJECTION, "invalid projection during linearisation");
+        return PB_OK;
+    } catch (const std::exception& e) {
+        return fail(c, PB_ERR_CUDA, e.what());
+    }
+}
+
+pb_status pb_gpu_get_reduced(pb_gpu_ctx* c, double* dense, double* rhs, double* direct) {
+    if (!c || !c->uploaded || !c->have_system) return fail(c, PB_ERR_STATE, "no reduced system assembled");
+    try {
+        const HostModel& m = c->model;
+        const int prec = c->last_precision;
+        const Shape& S = c->S[prec];
+        const int n = S.n, nb = S.nb, n6 = 6 * S.ncb;
+        const size_t ts = prec == PB_PRECISION_FP64 ? 8 : 4;
+        std::vector<char> vals(static_cast<size_t>(std::max(1, S.nnzb)) * 36 * ts), border(static_cast<size_t>(std::max(1, S.ncb)) * 6 * std::max(1, nb) * ts),
+            Cm(static_cast<size_t>(std::max(1, nb * nb)) * ts), r(n * ts), d(n * ts);
+        const void* src_vals = prec == PB_PRECISION_FP64 ? static_cast<const void*>(c->p64.red.vals) : c->p32.red.vals;
+        const void* src_border = prec == PB_PRECISION_FP64 ? static_cast<const void*>(c->p64.red.border) : c->p32.red.border;
+        const void* src_C = prec == PB_PRECISION_FP64 ? static_cast<const void*>(c->p64.red.Cm) : c->p32.red.Cm;
+        const void* src_r = prec == PB_PRECISION_FP64 ? static_cast<const void*>(c->p64.red.rhs) : c->p32.red.rhs;
+        const void* src_d = prec == PB_PRECISION_FP64 ? static_cast<const void*>(c->p64.red.direct) : c->p32.red.direct;
+        check(cudaMemcpy(vals.data(), src_vals, static_cast<size_t>(S.nnzb) * 36 * ts, cudaMemcpyDeviceToHost), "D2H");
+        if (nb) {
+            check(cudaMemcpy(border.data(), src_border, static_cast<size_t>(S.ncb) * 6 * nb * ts, cudaMemcpyDeviceToHost), "D2H");
+            check(cudaMemcpy(Cm.data(), src_C, static_cast<size_t>(nb) * nb * ts, cudaMemcpyDeviceToHost), "D2H");
+        }
+        check(cudaMemcpy(r.data(), src_r, n * ts, cudaMemcpyDeviceToHost), "D2H");
+        check(cudaMemcpy(d.data(), src_d, n * ts, cudaMemcpyDeviceToHost), "D2H");
+        auto get = [&](const std::vector<char>& v, size_t i) {
+            return ts == 8 ? reinterpret_cast<const double*>(v.data())[i]
+                           : static_cast<double>(reinterpret_cast<const float*>(v.data())[i]);
+        };
+        if (dense) {
+            std::fill(dense, dense + static_cast<size_t>(n) * n, 0.0);
+            for (int i = 0; i < S.ncb; ++i)
+                for (int p = m.row_ptr[i]; p < m.row_ptr[i + 1]; ++p) {
+                    const int j = m.col_idx[p];
+                    for (int a = 0; a < 6; ++a)
+                        for (int b = 0; b < 6; ++b)
+                            dense[static_cast<size_t>(6 * i + a) * n + 6 * j + b] = get(vals, static_cast<size_t>(p) * 36 + a * 6 + b);
+                }
+            for (int row = 0; row < n6; ++row)
+                for (int col = 0; col < nb; ++col) {
+                    const double v = get(border, static_cast<size_t>(row) * nb + col);
+                    dense[static_cast<size_t>(row) * n + n6 + col] = v;
+                    dense[static_cast<size_t>(n6 + col) * n + row] = v;
+                }
+            for (int a = 0; a < nb; ++a)
+                for (int b = 0; b < nb; ++b) dense[static_cast<size_t>(n6 + a) * n + n6 + b] = get(Cm, static_cast<size_t>(a) * nb + b);
+        }
+        for (int i = 0; i < n; ++i) {
+            if (rhs) rhs[i] = get(r, i);
+            if (direct) direct[i] = get(d, i);
+        }
+        return PB_OK;
+    } catch (const std::exception& e) {
+        return fail(c, PB_ERR_CUDA, e.what());
+    }
+}
+
+pb_status pb_gpu_solve_reduced(pb_gpu_ctx* c, double* step, int32_t* converged, int32_t* iterations, double* relres) {
+    if (!c || !c->uploaded || !c->have_system) return fail(c, PB_ERR_STATE, "no reduced system assembled");
+    try {
+        pb_solve_options op{};
+        op.refinement_sweeps = 3;
+        bool cv = false;
+        int it = 0, sw = 0;
+        double rr = 0.0;
+        const int rc = solve_reduced(c, op, &cv, &it, &rr, &sw);
+        if (converged) *converged = cv ? 1 : 0;
+        if (iterations) *iterations = it;
+        if (relres) *relres = rr;
+        if (step) check(cudaMemcpy(step, c->step_c, c->S[0].n * sizeof(double), cudaMemcpyDeviceToHost), "D2H");
+        if (rc) return fail(c, PB_ERR_SINGULAR_BLOCK, "reduced system is not numerically SPD (positive definite)");
+        return PB_OK;
+    } catch (const std::exception& e) {
+        return fail(c, PB_ERR_CUDA, e.what());
+    }
+}
+
+pb_status pb_gpu_back_substitute(pb_gpu_ctx* c, double* elim, double* dd, int32_t* success) {
+    if (!c || !c->uploaded || !c->have_system) return fail(c, PB_ERR_STATE, "no reduced system assembled");
+    try {
+        double d, ps, cs;
+        back_substitute(c, &d, &ps, &cs);
+        if (dd) *dd = d;
+        if (success) *success = std::isfinite(d) ? 1 : 0;
+        if (elim) {
+            const HostModel& m = c->model;
+            std::vector<double> sp(m.trk_order.size() * 3);
+            check(cudaMemcpy(sp.data(), c->step_p, sp.size() * sizeof(double), cudaMemcpyDeviceToHost), "D2H");
+            for (size_t p = 0; p < m.trk_order.size(); ++p) {
+                const int tb = m.track_block[m.trk_order[p]];
+                if (tb < 0) continue;
+                for (int a = 0; a < 3; ++a) elim[static_cast<size_t>(tb) * 3 + a] = sp[p * 3 + a];
+            }
+        }
+        return PB_OK;
+    } catch (const std::exception& e) {
+        return fail(c, PB_ERR_CUDA, e.what());
+    }
+}
+
+pb_status pb_gpu_eval_cost(pb_gpu_ctx* c, double* cost) {
+    if (!c || !c->uploaded || !cost) return fail(c, PB_ERR_STATE, "no problem uploaded");
+    try {
+        eval_costs(c, nullptr, 1, 0, cost);
+        return PB_OK;
+    } catch (const std::exception& e) {
+        return fail(c, PB_ERR_CUDA, e.what());
+    }
+}
+
+pb_status pb_gpu_eval_cost_batch(pb_gpu_ctx* c, const double* alphas, int32_t n, double* costs) {
+    if (!c || !c->uploaded || !c->have_system) return fail(c, PB_ERR_STATE, "no step available");
+    if (!alphas || !costs || n <= 0) return fail(c, PB_ERR_INVALID_ARGUMENT, "bad alpha batch");
+    try {
+        for (int k = 0; k < n; k += kMaxAlpha) eval_costs(c, alphas + k, std::min(kMaxAlpha, n - k), 1, costs + k);
+        return PB_OK;
+    } catch (const std::exception& e) {
+        return fail(c, PB_ERR_CUDA, e.what());
+    }
+}
+
+pb_status pb_gpu_apply_step(pb_gpu_ctx* c, double alpha) {
+    if (!c || !c->uploaded || !c->have_system) return fail(c, PB_ERR_STATE, "no step available");
+    try {
+        double cst;
+        eval_costs(c, &alpha, 1, 1, &cst);
+        launch_accept(c->S[0], c->D[0], c->step_p, alpha, 0, c->stream);
+        check(cudaStreamSynchronize(c->stream), "apply");
+        c->have_system = false;
+        return PB_OK;
+    } catch (const std::exception& e) {
+        return fail(c, PB_ERR_CUDA, e.what());
+    }
+}
+
+pb_status pb_gpu_solve(pb_gpu_ctx* c, const pb_solve_options* op, pb_solve_report* rep) {
+    if (!c || !op || !rep) return fail(c, PB_ERR_INVALID_ARGUMENT, "null argument");
+    if (!c->uploaded) return fail(c, PB_ERR_STATE, "no problem uploaded");
+    try {
+        cudaSetDevice(c->device);
+        c->error.clear();
+        lm_solve(c, *op, rep);
+        return PB_OK;
+    } catch (const std::exception& e) {
+        rep->status = PB_SOLVE_NUMERICAL_FAILURE;
+        return fail(c, PB_ERR_CUDA, e.what());
+    }
+}
+
+pb_status pb_gpu_download_state(pb_gpu_ctx* c, double* cams, double* pts, int8_t* valid, double* rb, double* ra,
+                                double* intr) {
+    if (!c || !c->uploaded) return fail(c, PB_ERR_STATE, "no problem uploaded");
+    try {
+        const HostModel& m = c->model;
+        if (cams)
+            check(cudaMemcpy(cams, c->D[0].cams_eff, m.cams_in.size() * sizeof(double), cudaMemcpyDeviceToHost), "D2H");
+        if (pts) {
+            std::vector<double> sp(m.trk_order.size() * 3);
+            check(cudaMemcpy(sp.data(), c->D[0].points, sp.size() * sizeof(double), cudaMemcpyDeviceToHost), "D2H");
+            std::copy(m.points_in.begin(), m.points_in.end(), pts);
+            for (size_t p = 0; p < m.trk_order.size(); ++p)
+                for (int a = 0; a < 3; ++a) pts[static_cast<size_t>(m.trk_order[p]) * 3 + a] = sp[p * 3 + a];
+        }
+        for (int t = 0; t < m.nt; ++t) {
+            if (valid) valid[t] = c->solved && static_cast<size_t>(t) < c->valid.size() ? c->valid[t] : 0;
+            if (rb) rb[t] = static_cast<size_t>(t) < c->rms_before.size() ? c->rms_before[t] : kNaN;
+            if (ra) ra[t] = static_cast<size_t>(t) < c->rms_after.size() ? c->rms_after[t] : kNaN;
+        }
+        if (intr && m.ng > 0) {
+            std::vector<double> g(static_cast<size_t>(m.ng) * kGroupRec);
+            check(cudaMemcpy(g.data(), c->D[0].groups, g.size() * sizeof(double), cudaMemcpyDeviceToHost), "D2H");
+            for (int gi = 0; gi < m.ng; ++gi)
+                for (int p = 0; p < kP; ++p) intr[gi * kP + p] = g[static_cast<size_t>(gi) * kGroupRec + p];
+        }
+        return PB_OK;
+    } catch (const std::exception& e) {
+        return fail(c, PB_ERR_CUDA, e.what());
+    }
+}
+
+pb_status pb_gpu_solve_problem(pb_gpu_ctx* c, const pb_problem_desc* pr, const pb_solve_options* op,
+                               pb_solve_report* rep, double* cams, double* pts, int8_t* valid, double* rb, double* ra) {
+    pb_status s = pb_gpu_upload(c, pr, op);
+    if (s != PB_OK) {
+        if (rep) {
+            std::memset(rep, 0, sizeof(*rep));
+            rep->status = s == PB_ERR_UNSUPPORTED ? PB_SOLVE_UNSUPPORTED : PB_SOLVE_INVALID_INPUT;
+        }
+        return s;
+    }
+    s = pb_gpu_solve(c, op, rep);
+    if (s != PB_OK) return s;
+    return pb_gpu_download_state(c, cams, pts, valid, rb, ra, nullptr);
+}
+
+pb_status pb_gpu_request_cancel(pb_gpu_ctx* c, int32_t cancel) {
+    if (!c) return PB_ERR_INVALID_ARGUMENT;
+    c->cancel = cancel;
+    return PB_OK;
+}
+
+pb_status pb_gpu_kernel_times(pb_gpu_ctx* c, double* out8) {
+    if (!c || !out8) return PB_ERR_INVALID_ARGUMENT;
+    for (int i = 0; i < 8; ++i) out8[i] = c->kt[i];
+    return PB_OK;
+}
+
+pb_status pb_gpu_get_stream(pb_gpu_ctx* c, void** stream) {
+    if (!c || !stream) return PB_ERR_INVALID_ARGUMENT;
+    *stream = static_cast<void*>(c->stream);
+    return PB_OK;
+}
+
+pb_status pb_gpu_set_timing(pb_gpu_ctx* c, int32_t enable) {
+    if (!c) return PB_ERR_INVALID_ARGUMENT;
+    c->timing = enable != 0;
+    return PB_OK;
+}
+
+}  // extern "C"

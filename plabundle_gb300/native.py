@@ -1,0 +1,174 @@
+"""ctypes binding of the C ABI in include/pb_gpu.h (libpbgpu.so, built in-tree for sm_103a).
+
+There is no CPU fallback: if the library is missing or no CUDA device is usable, the calls
+raise ``BackendUnavailable``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libpbgpu.so")
+
+EXPORTED = [
+    "pb_gpu_create", "pb_gpu_destroy", "pb_gpu_last_error", "pb_status_name", "pb_gpu_upload",
+    "pb_gpu_reset_state", "pb_gpu_get_sizes", "pb_gpu_get_active", "pb_gpu_get_pairs",
+    "pb_gpu_linearize_observations", "pb_gpu_linearize_schur", "pb_gpu_get_reduced", "pb_gpu_solve_reduced",
+    "pb_gpu_back_substitute", "pb_gpu_eval_cost", "pb_gpu_eval_cost_batch", "pb_gpu_apply_step", "pb_gpu_solve",
+    "pb_gpu_download_state", "pb_gpu_solve_problem", "pb_gpu_request_cancel", "pb_gpu_get_stream",
+    "pb_gpu_set_timing",
+    "pb_gpu_kernel_times",
+]
+
+
+class BackendUnavailable(RuntimeError):
+    pass
+
+
+class ProblemDesc(C.Structure):
+    _fields_ = [("n_cameras", C.c_int32), ("cameras", C.c_void_p), ("n_tracks", C.c_int32),
+                ("track_offsets", C.c_void_p), ("points", C.c_void_p), ("n_obs", C.c_int64),
+                ("obs_camera", C.c_void_p), ("obs_u", C.c_void_p), ("obs_v", C.c_void_p),
+                ("obs_weight", C.c_void_p), ("obs_scale", C.c_void_p), ("n_fixed_cameras", C.c_int32),
+                ("fixed_cameras", C.c_void_p), ("n_fixed_tracks", C.c_int32), ("fixed_tracks", C.c_void_p),
+                ("calibration_group_ids", C.c_void_p), ("intrinsic_reference_cameras", C.c_void_p)]
+
+
+class SolveOptionsC(C.Structure):
+    _fields_ = [("max_iterations", C.c_int32), ("robust_loss", C.c_int32), ("robust_loss_scale", C.c_double),
+                ("armijo_coefficient", C.c_double), ("line_search_steps", C.c_int32),
+                ("enable_point_filter", C.c_int32), ("filter_max_reproj_error", C.c_double),
+                ("filter_sigma_factor", C.c_double), ("max_initial_track_rms", C.c_double),
+                ("refine_camera_pose", C.c_int32), ("gauge_policy", C.c_int32),
+                ("gauge_anchor_camera", C.c_int32), ("gauge_scale_camera", C.c_int32),
+                ("gauge_baseline", C.c_double), ("intrinsic_mask", C.c_uint32), ("precision", C.c_int32),
+                ("max_linear_iterations", C.c_int32), ("linear_relative_tolerance", C.c_double),
+                ("linear_absolute_tolerance", C.c_double), ("refinement_sweeps", C.c_int32),
+                ("preconditioner_cluster_size", C.c_int32), ("calibration", C.c_double * 32)]
+
+
+class SolveReportC(C.Structure):
+    _fields_ = [(n, C.c_int32) for n in (
+        "status", "solution_usable", "iterations", "accepted_steps", "rejected_steps", "linearizations",
+        "objective_evaluations", "linear_iterations", "refinement_sweeps", "active_tracks", "observation_count",
+        "rejected_initial_tracks", "optimized_tracks", "camera_blocks", "intrinsic_blocks", "pattern_builds",
+        "pattern_reuses", "gpu_kernel_launches")] + [(n, C.c_double) for n in (
+            "initial_cost", "final_cost", "mean_rms_before", "mean_rms_after", "valid_track_ratio",
+            "filter_threshold", "assembly_ms", "linear_ms", "back_substitution_ms", "objective_ms", "total_ms")]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+_lib = None
+
+
+def library_path() -> str:
+    return LIB_PATH
+
+
+def load(build_if_missing: bool = False):
+    """Loads libpbgpu.so (exports checked); raises BackendUnavailable when it is absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        if build_if_missing:
+            from . import build as _build
+            _build.build()
+        else:
+            raise BackendUnavailable(f"GB300 backend library not built: {LIB_PATH}")
+    L = C.CDLL(LIB_PATH)
+    for name in EXPORTED:
+        if not hasattr(L, name):
+            raise BackendUnavailable(f"{LIB_PATH} does not export {name}")
+    vp, i32, i64, dbl = C.c_void_p, C.c_int32, C.c_int64, C.c_double
+    L.pb_gpu_create.argtypes = [i32, C.POINTER(vp)]
+    L.pb_gpu_destroy.argtypes = [vp]
+    L.pb_gpu_last_error.restype = C.c_char_p
+    L.pb_gpu_last_error.argtypes = [vp]
+    L.pb_status_name.restype = C.c_char_p
+    L.pb_status_name.argtypes = [i32]
+    L.pb_gpu_upload.argtypes = [vp, C.POINTER(ProblemDesc), C.POINTER(SolveOptionsC)]
+    L.pb_gpu_reset_state.argtypes = [vp]
+    L.pb_gpu_get_sizes.argtypes = [vp, vp, C.POINTER(dbl)]
+    L.pb_gpu_get_active.argtypes = [vp, vp, vp, vp, vp]
+    L.pb_gpu_get_pairs.argtypes = [vp, vp]
+    L.pb_gpu_linearize_observations.argtypes = [vp, i32] + [vp] * 7
+    L.pb_gpu_linearize_schur.argtypes = [vp, dbl, i32, C.POINTER(dbl), C.POINTER(i32)]
+    L.pb_gpu_get_reduced.argtypes = [vp, vp, vp, vp]
+    L.pb_gpu_solve_reduced.argtypes = [vp, vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(dbl)]
+    L.pb_gpu_back_substitute.argtypes = [vp, vp, C.POINTER(dbl), C.POINTER(i32)]
+    L.pb_gpu_eval_cost.argtypes = [vp, C.POINTER(dbl)]
+    L.pb_gpu_eval_cost_batch.argtypes = [vp, vp, i32, vp]
+    L.pb_gpu_apply_step.argtypes = [vp, dbl]
+    L.pb_gpu_solve.argtypes = [vp, C.POINTER(SolveOptionsC), C.POINTER(SolveReportC)]
+    L.pb_gpu_download_state.argtypes = [vp] + [vp] * 6
+    L.pb_gpu_solve_problem.argtypes = [vp, C.POINTER(ProblemDesc), C.POINTER(SolveOptionsC),
+                                       C.POINTER(SolveReportC)] + [vp] * 5
+    L.pb_gpu_request_cancel.argtypes = [vp, i32]
+    L.pb_gpu_set_timing.argtypes = [vp, i32]
+    L.pb_gpu_get_stream.argtypes = [vp, C.POINTER(vp)]
+    L.pb_gpu_kernel_times.argtypes = [vp, vp]
+    for name in EXPORTED:
+        if name not in ("pb_gpu_last_error", "pb_status_name"):
+            getattr(L, name).restype = i32
+    _lib = L
+    return L
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+def problem_desc(problem):
+    """Builds the C descriptor; returns (desc, keepalive) where keepalive owns the arrays."""
+    p = problem.normalized()
+    fixed_c = np.ascontiguousarray(p.fixedCameraIndices, np.int32)
+    fixed_t = np.ascontiguousarray(p.fixedTrackIndices, np.int32)
+    keep = [p, fixed_c, fixed_t]
+    desc = ProblemDesc(p.n_cameras, _ptr(p.cameras), p.n_tracks, _ptr(p.track_offsets), _ptr(p.points), p.n_obs,
+                       _ptr(p.obs_camera), _ptr(p.obs_u), _ptr(p.obs_v), _ptr(p.obs_weight), _ptr(p.obs_scale),
+                       fixed_c.size, _ptr(fixed_c), fixed_t.size, _ptr(fixed_t), _ptr(p.cameraCalibrationGroupIds),
+                       _ptr(p.sharedIntrinsicReferenceCameras))
+    return desc, keep
+
+
+def solve_options(options, problem=None) -> SolveOptionsC:
+    from .problem import Precision, intrinsic_mask
+    s, cal, b = options.solver, options.calibration, options.backend
+    o = SolveOptionsC()
+    o.max_iterations = s.maxIterations
+    o.robust_loss = int(s.imageRobustLoss)
+    o.robust_loss_scale = s.imageRobustLossScalePixels
+    o.armijo_coefficient = s.referenceArmijoCoefficient
+    o.line_search_steps = s.referenceLineSearchSteps
+    o.enable_point_filter = int(s.enablePointFilter)
+    o.filter_max_reproj_error = s.filterMaxReprojError
+    o.filter_sigma_factor = s.filterSigmaFactor
+    o.max_initial_track_rms = s.maxInitialTrackRms
+    o.refine_camera_pose = int(cal.refineCameraPose)
+    g = problem.gauge if problem is not None else None
+    o.gauge_policy = int(g.policy) if g else 0
+    o.gauge_anchor_camera = g.referenceAnchorCameraIndex if g else -1
+    o.gauge_scale_camera = g.referenceScaleCameraIndex if g else -1
+    o.gauge_baseline = g.referenceBaseline if g else 0.0
+    o.intrinsic_mask = intrinsic_mask(cal)
+    o.precision = int(Precision.Mixed if b.enablePlaMatrixMixedPrecision else Precision.Fp64)
+    o.max_linear_iterations = b.maxLinearIterations
+    o.linear_relative_tolerance = 2.0e-10
+    o.linear_absolute_tolerance = 1.0e-12
+    o.refinement_sweeps = b.refinementSweeps
+    o.preconditioner_cluster_size = b.plaMatrixPreconditionerClusterSize
+    for i, v in enumerate(cal.numeric_block()):
+        o.calibration[i] = v
+    return o
+
+
+def check(L, ctx, status: int, what: str):
+    if status != 0:
+        msg = L.pb_gpu_last_error(ctx).decode() if ctx else ""
+        raise RuntimeError(f"{what} failed: {L.pb_status_name(status).decode()} {msg}")

@@ -1,0 +1,272 @@
+"""Seeded synthetic bundle-adjustment problems with the shapes of the benchmark workloads.
+
+No public dataset is involved: every workload is generated from a seed.
+
+* ``ring_problem``    -- 20 frame cameras on a circle (r=10 m, z=2 m) looking at the origin,
+  4000x3000 px, f=3500, Brown k1=-0.05, k2=0.01, p1=p2=1e-4, 2 000 points in [-2,2]^3, each
+  seen by a random 3..6 of the cameras that see it; 0.5 px noise, 2 % outliers, pose noise
+  N(0, 0.01 rad) / N(0, 0.05 m), point noise N(0, 0.05 m).
+* ``aerial_grid_problem`` -- 500 nadir cameras in a 25x20 grid at 100 m with 80 %/60 %
+  forward/side overlap, 6000x4000 px, f=4000 px, 200 000 points on a sum-of-8-sinusoids
+  terrain (20 m amplitude), 3..12 observations per track (~1.2 M), two shared calibration
+  groups, 0.5 px noise, 3 % outliers.
+* ``window_problems`` -- independent local windows generated like ``ring_problem`` with
+  their own seeds, camera counts in 10..60 and point counts in 1k..20k.
+
+The projector is the frame-pinhole Brown-Conrady model of
+src/internal/BundleAdjustProjection.h:58-91 in the reference.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .problem import CAMERA_STRIDE, Gauge, GaugePolicy, Problem
+
+
+def look_at_rotation(centre: np.ndarray, target: np.ndarray, up=(0.0, 0.0, 1.0)) -> np.ndarray:
+    """Camera-to-world rotation whose columns are the camera x (right), y (down), z (forward)."""
+    f = np.asarray(target, float) - np.asarray(centre, float)
+    f /= np.linalg.norm(f)
+    r = np.cross(f, np.asarray(up, float))
+    if np.linalg.norm(r) < 1e-9:
+        r = np.cross(f, np.array([0.0, 1.0, 0.0]))
+    r /= np.linalg.norm(r)
+    d = np.cross(f, r)
+    return np.stack([r, d, f], axis=1)
+
+
+def make_camera(R, C, fx, fy, cx, cy, k=(0.0, 0.0, 0.0), p=(0.0, 0.0), width=0.0, height=0.0,
+                u_sign=1.0, v_sign=1.0, flip=0.0) -> np.ndarray:
+    cam = np.zeros(CAMERA_STRIDE)
+    cam[0:9] = np.asarray(R, float).reshape(9)
+    cam[9:12] = C
+    cam[12:16] = (fx, fy, cx, cy)
+    cam[16:19] = k
+    cam[19:21] = p
+    cam[21:26] = (u_sign, v_sign, flip, width, height)
+    return cam
+
+
+def project(cameras: np.ndarray, cam_idx: np.ndarray, X: np.ndarray):
+    """Vectorised projection; returns (pixels [n,2], valid [n])."""
+    cams = cameras[cam_idx]
+    R = cams[:, 0:9].reshape(-1, 3, 3)
+    d = X - cams[:, 9:12]
+    xc = np.einsum("nij,ni->nj", R, d)
+    z = xc[:, 2]
+    fwd = np.where(cams[:, 23] != 0, -z, z)
+    valid = fwd > 1e-9
+    zs = np.where(valid, z, 1.0)
+    x = xc[:, 0] / zs
+    y = xc[:, 1] / zs
+    r2 = x * x + y * y
+    k1, k2, k3, p1, p2 = (cams[:, 16 + i] for i in range(5))
+    radial = 1 + k1 * r2 + k2 * r2 * r2 + k3 * r2 ** 3
+    xd = x * radial + p1 * 2 * x * y + p2 * (r2 + 2 * x * x)
+    yd = y * radial + p1 * (r2 + 2 * y * y) + p2 * 2 * x * y
+    u = cams[:, 21] * cams[:, 12] * xd + cams[:, 14]
+    v = cams[:, 22] * cams[:, 13] * yd + cams[:, 15]
+    return np.stack([u, v], axis=1), valid
+
+
+def rotation_from_axis_angle(w: np.ndarray) -> np.ndarray:
+    th = np.linalg.norm(w)
+    if th < 1e-15:
+        return np.eye(3)
+    k = w / th
+    K = np.array([[0, -k[2], k[1]], [k[2], 0, -k[0]], [-k[1], k[0], 0]])
+    return np.eye(3) + np.sin(th) * K + (1 - np.cos(th)) * K @ K
+
+
+def perturb_cameras(cameras: np.ndarray, rng, rot_sigma: float, centre_sigma: float) -> np.ndarray:
+    out = cameras.copy()
+    for i in range(out.shape[0]):
+        dR = rotation_from_axis_angle(rng.normal(0.0, rot_sigma, 3))
+        out[i, 0:9] = (dR @ out[i, 0:9].reshape(3, 3)).reshape(9)
+        out[i, 9:12] += rng.normal(0.0, centre_sigma, 3)
+    return out
+
+
+def _assemble(cameras_true, cameras_init, X_true, X_init, visible_lists, rng, noise, outlier_frac,
+              min_views, max_views):
+    """Picks views per point, projects, adds noise and outliers; returns track-CSR arrays."""
+    n_pts = X_true.shape[0]
+    counts = np.zeros(n_pts, np.int64)
+    chosen = []
+    for t in range(n_pts):
+        vis = visible_lists[t]
+        k = int(rng.integers(min_views, max_views + 1))
+        if vis.size > k:
+            vis = np.sort(rng.choice(vis, size=k, replace=False))
+        chosen.append(vis)
+        counts[t] = vis.size
+    offsets = np.zeros(n_pts + 1, np.int64)
+    np.cumsum(counts, out=offsets[1:])
+    cam_idx = np.concatenate(chosen).astype(np.int32) if n_pts else np.zeros(0, np.int32)
+    pt_idx = np.repeat(np.arange(n_pts), counts)
+    px, _ = project(cameras_true, cam_idx, X_true[pt_idx])
+    px = px + rng.normal(0.0, noise, px.shape)
+    n_obs = cam_idx.size
+    out_mask = rng.random(n_obs) < outlier_frac
+    w = cameras_true[cam_idx, 24]
+    h = cameras_true[cam_idx, 25]
+    px[out_mask, 0] = rng.random(out_mask.sum()) * w[out_mask]
+    px[out_mask, 1] = rng.random(out_mask.sum()) * h[out_mask]
+    return offsets, cam_idx, px
+
+
+def _problem(cameras_init, X_init, offsets, cam_idx, px, **kw) -> Problem:
+    n_obs = cam_idx.size
+    return Problem(cameras=cameras_init, points=X_init, track_offsets=offsets, obs_camera=cam_idx,
+                   obs_u=px[:, 0].copy(), obs_v=px[:, 1].copy(), obs_weight=np.ones(n_obs),
+                   obs_scale=np.ones(n_obs), **kw).normalized()
+
+
+def _visible(cameras, X, margin=0.0):
+    """Per point, the sorted indices of the cameras that see it in front and in frame."""
+    n_c = cameras.shape[0]
+    lists = []
+    chunk = max(1, 4_000_000 // max(1, n_c))
+    for s in range(0, X.shape[0], chunk):
+        Xs = X[s:s + chunk]
+        m = Xs.shape[0]
+        ci = np.tile(np.arange(n_c), m)
+        pi = np.repeat(np.arange(m), n_c)
+        px, valid = project(cameras, ci, Xs[pi])
+        inside = valid & (px[:, 0] >= margin) & (px[:, 0] < cameras[ci, 24] - margin) \
+            & (px[:, 1] >= margin) & (px[:, 1] < cameras[ci, 25] - margin)
+        inside = inside.reshape(m, n_c)
+        lists.extend(np.nonzero(row)[0] for row in inside)
+    return lists
+
+
+def ring_problem(seed: int = 7, n_cameras: int = 20, n_points: int = 2000, noise: float = 0.5,
+                 outlier_frac: float = 0.02, rot_sigma: float = 0.01, centre_sigma: float = 0.05,
+                 point_sigma: float = 0.05, min_views: int = 3, max_views: int = 6) -> Problem:
+    rng = np.random.default_rng(seed)
+    cams = []
+    for i in range(n_cameras):
+        a = 2 * np.pi * i / n_cameras
+        C = np.array([10 * np.cos(a), 10 * np.sin(a), 2.0])
+        R = look_at_rotation(C, np.zeros(3))
+        cams.append(make_camera(R, C, 3500.0, 3500.0, 2000.0, 1500.0, k=(-0.05, 0.01, 0.0), p=(1e-4, 1e-4),
+                                width=4000.0, height=3000.0))
+    cams = np.array(cams)
+    X = rng.uniform(-2.0, 2.0, (n_points, 3))
+    vis = _visible(cams, X)
+    offsets, cam_idx, px = _assemble(cams, None, X, None, vis, rng, noise, outlier_frac, min_views, max_views)
+    cams0 = perturb_cameras(cams, rng, rot_sigma, centre_sigma)
+    X0 = X + rng.normal(0.0, point_sigma, X.shape)
+    prob = _problem(cams0, X0, offsets, cam_idx, px)
+    prob.truth_cameras = cams
+    prob.truth_points = X
+    return prob
+
+
+def _terrain(rng, n_waves=8, amplitude=20.0):
+    k = rng.uniform(0.003, 0.03, (n_waves, 2)) * rng.choice([-1.0, 1.0], (n_waves, 2))
+    ph = rng.uniform(0, 2 * np.pi, n_waves)
+    a = rng.uniform(0.5, 1.5, n_waves)
+    a *= amplitude / a.sum()
+
+    def height(x, y):
+        return (a[None, :] * np.sin(x[:, None] * k[None, :, 0] + y[:, None] * k[None, :, 1] + ph[None, :])).sum(1)
+
+    return height
+
+
+def aerial_grid_problem(seed: int = 11, n_along: int = 25, n_lines: int = 20, n_points: int = 200_000,
+                        altitude: float = 100.0, width: float = 6000.0, height: float = 4000.0,
+                        focal: float = 4000.0, forward_overlap: float = 0.8, side_overlap: float = 0.6,
+                        noise: float = 0.5, outlier_frac: float = 0.03, rot_sigma: float = 0.01,
+                        centre_sigma: float = 0.05, point_sigma: float = 0.05, min_views: int = 3,
+                        max_views: int = 12, n_groups: int = 2, intrinsic_error: bool = True) -> Problem:
+    rng = np.random.default_rng(seed)
+    foot_x = width / focal * altitude     # image x along world x
+    foot_y = height / focal * altitude    # image y along world -y (flight direction)
+    step_along = (1 - forward_overlap) * foot_y
+    step_side = (1 - side_overlap) * foot_x
+    truth_models = []
+    for g in range(n_groups):
+        truth_models.append(dict(f=focal * (1 + 0.002 * g), cx=width / 2 + 3.0 * g, cy=height / 2 - 2.0 * g,
+                                 k=(-0.04 + 0.005 * g, 0.008, -0.001), p=(1e-4, -1e-4)))
+    R = look_at_rotation(np.zeros(3), np.array([0.0, 0.0, -1.0]), up=(0.0, 1.0, 0.0))
+    cams, groups = [], []
+    for line in range(n_lines):
+        for j in range(n_along):
+            g = line % n_groups
+            m = truth_models[g]
+            C = np.array([line * step_side, j * step_along, altitude])
+            cams.append(make_camera(R, C, m["f"], m["f"], m["cx"], m["cy"], k=m["k"], p=m["p"],
+                                    width=width, height=height))
+            groups.append(g)
+    cams = np.array(cams)
+    groups = np.array(groups, np.int32)
+    hfun = _terrain(rng)
+    xs = rng.uniform(-0.35 * foot_x, (n_lines - 1) * step_side + 0.35 * foot_x, n_points)
+    ys = rng.uniform(-0.35 * foot_y, (n_along - 1) * step_along + 0.35 * foot_y, n_points)
+    X = np.stack([xs, ys, hfun(xs, ys)], axis=1)
+    vis = _visible_grid(cams, X, foot_x, foot_y)
+    offsets, cam_idx, px = _assemble(cams, None, X, None, vis, rng, noise, outlier_frac, min_views, max_views)
+    keep = np.diff(offsets) >= 2
+    if not keep.all():
+        X, offsets, cam_idx, px = _drop_tracks(X, offsets, cam_idx, px, keep)
+    cams0 = perturb_cameras(cams, rng, rot_sigma, centre_sigma)
+    if intrinsic_error:
+        for g in range(n_groups):
+            sel = groups == g
+            cams0[sel, 12] *= 1.0 + 0.003 * (1 if g == 0 else -1)
+            cams0[sel, 13] = cams0[sel, 12]
+            cams0[sel, 14] += 4.0
+            cams0[sel, 15] -= 3.0
+            cams0[sel, 16] += 0.004
+    X0 = X + rng.normal(0.0, point_sigma, X.shape)
+    prob = _problem(cams0, X0, offsets, cam_idx, px, cameraCalibrationGroupIds=groups)
+    prob.truth_cameras = cams
+    prob.truth_points = X
+    return prob
+
+
+def _visible_grid(cams, X, foot_x, foot_y):
+    """Visibility for nadir grids: candidate cameras within one footprint, then exact test."""
+    C = cams[:, 9:12]
+    lists = []
+    order = np.argsort(C[:, 0] * 1e6 + C[:, 1])
+    chunk = 20000
+    for s in range(0, X.shape[0], chunk):
+        Xs = X[s:s + chunk]
+        near = (np.abs(Xs[:, None, 0] - C[None, :, 0]) < 0.6 * foot_x) & \
+               (np.abs(Xs[:, None, 1] - C[None, :, 1]) < 0.6 * foot_y)
+        pi, ci = np.nonzero(near)
+        px, valid = project(cams, ci, Xs[pi])
+        ok = valid & (px[:, 0] >= 0) & (px[:, 0] < cams[ci, 24]) & (px[:, 1] >= 0) & (px[:, 1] < cams[ci, 25])
+        pi, ci = pi[ok], ci[ok]
+        split = np.searchsorted(pi, np.arange(Xs.shape[0] + 1))
+        for t in range(Xs.shape[0]):
+            lists.append(np.sort(ci[split[t]:split[t + 1]]))
+    del order
+    return lists
+
+
+def _drop_tracks(X, offsets, cam_idx, px, keep):
+    counts = np.diff(offsets)
+    obs_keep = np.repeat(keep, counts)
+    counts = counts[keep]
+    new_off = np.zeros(counts.size + 1, np.int64)
+    np.cumsum(counts, out=new_off[1:])
+    return X[keep], new_off, cam_idx[obs_keep], px[obs_keep]
+
+
+def window_problems(n_windows: int = 256, seed: int = 1234, cameras=(10, 60), points=(1000, 20000)):
+    rng = np.random.default_rng(seed)
+    out = []
+    for w in range(n_windows):
+        nc = int(rng.integers(cameras[0], cameras[1] + 1))
+        npt = int(rng.integers(points[0], points[1] + 1))
+        out.append(ring_problem(seed=seed * 1000 + w, n_cameras=nc, n_points=npt))
+    return out
+
+
+def with_gauge(problem: Problem, policy=GaugePolicy.AutoAnchor) -> Problem:
+    problem.gauge = Gauge(policy=policy)
+    return problem

@@ -1,0 +1,179 @@
+"""GPU parity of the sm_103a kernels against the CPU FP64 oracle, through the C ABI.
+
+Integer work (active tracks, block numbering, reduced pattern, inlier masks) must match bit for
+bit.  Floating point tolerances are written in each test: FP64 path to FP64 rounding of a
+different summation order; mixed path (FP32 Jacobians/Schur/PCG with compensated sums and FP64
+cost / refinement) to the benchmark spec's targets, 1e-6 relative final cost and 1e-5 relative camera
+centre error.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from plabundle_gb300 import synth
+from plabundle_gb300.device import Gb300Context
+from plabundle_gb300.problem import ImageRobustLoss, Precision, SolveOptions, SolveStatus
+
+pytestmark = pytest.mark.gpu
+
+
+def ring(seed=5, n_cameras=8, n_points=300, **kw):
+    return synth.ring_problem(seed=seed, n_cameras=n_cameras, n_points=n_points, **kw)
+
+
+def ring_options(mixed=False):
+    o = SolveOptions()
+    o.solver.imageRobustLoss = ImageRobustLoss.Huber
+    o.solver.imageRobustLossScalePixels = 1.5
+    o.backend.enablePlaMatrixMixedPrecision = mixed
+    return o
+
+
+def aerial(n_along=5, n_lines=4, n_points=3000, seed=3):
+    return synth.aerial_grid_problem(seed=seed, n_along=n_along, n_lines=n_lines, n_points=n_points)
+
+
+def aerial_options(mixed=False):
+    o = SolveOptions()
+    o.solver.imageRobustLoss = ImageRobustLoss.Cauchy
+    o.solver.imageRobustLossScalePixels = 1.5
+    o.calibration.refineSharedFocalLength = True
+    o.calibration.refineSharedPrincipalPoint = True
+    o.calibration.refineSharedRadialDistortion = True
+    o.backend.enablePlaMatrixMixedPrecision = mixed
+    return o
+
+
+def gpu(problem, options):
+    ctx = Gb300Context(0)
+    st = ctx.upload(problem, options)
+    assert st == 0, ctx.L.pb_gpu_last_error(ctx.ctx)
+    return ctx
+
+
+def index_map(ctx, orc):
+    """GPU compact reduced index -> oracle 13-padded index."""
+    s = ctx.sizes()
+    ncb, ng, ni = s["camera_blocks"], s["intrinsic_blocks"], s["ni"]
+    cols = [p for p in range(9) if (int(ctx.copts.intrinsic_mask) >> p) & 1]
+    assert len(cols) == ni
+    idx = [13 * i + a for i in range(ncb) for a in range(6)]
+    idx += [13 * (ncb + g) + cols[c] for g in range(ng) for c in range(ni)]
+    return np.array(idx)
+
+
+CASES = [("ring", ring, ring_options), ("aerial", aerial, aerial_options)]
+
+
+@pytest.mark.parametrize("name,make,opts", CASES)
+def test_active_problem_pattern_and_gauge_are_identical(name, make, opts):
+    p = make()
+    ctx = gpu(p, opts())
+    orc = O.Oracle(p, opts())
+    a, b = ctx.active(), orc.active()
+    for k in ("active_track", "camera_block", "intrinsic_block", "track_block"):
+        assert np.array_equal(a[k], b[k]), k
+    orc.build(0.0)
+    assert np.array_equal(ctx.pairs(), orc.reduced()["pairs"])
+    s, i = ctx.sizes(), orc.info()
+    assert (s["gauge_anchor"], s["gauge_scale"]) == (i["gauge_anchor"], i["gauge_scale"])
+    assert s["gauge_baseline"] == i["gauge_baseline"]
+    assert s["active_tracks"] == i["active_tracks"] and s["observation_count"] == i["observation_count"]
+    assert s["rejected_initial_tracks"] == i["rejected_initial_tracks"]
+
+
+@pytest.mark.parametrize("name,make,opts", CASES)
+@pytest.mark.parametrize("precision", [Precision.Fp64, Precision.Mixed])
+def test_observation_linearization_matches_oracle(name, make, opts, precision):
+    p = make()
+    ctx = gpu(p, opts())
+    g = ctx.linearize_observations(precision)
+    r = O.Oracle(p, opts()).linearize_observations()
+    act = ctx.active()["active_track"]
+    trk = np.repeat(np.arange(p.n_tracks), np.diff(p.track_offsets))
+    sel = (act[trk] == 1) & (r["valid"] == 1)
+    assert np.array_equal(g["valid"][sel], r["valid"][sel])
+    tol = 1e-10 if precision == Precision.Fp64 else 2e-6
+    np.testing.assert_allclose(g["residual"][sel], r["residual"][sel], rtol=1e-12, atol=1e-9)
+    np.testing.assert_allclose(g["cost"][sel], r["cost"][sel], rtol=1e-12, atol=1e-12)
+    for key in ("point_jacobian", "pose_jacobian", "intrinsic_jacobian"):
+        scale = np.abs(r[key][sel]).max(axis=(1, 2), keepdims=True) + 1e-300
+        err = np.abs(g[key][sel] - r[key][sel]) / scale
+        assert err.max() < tol, (key, err.max())
+    np.testing.assert_allclose(g["normal_weight"][sel], r["normal_weight"][sel], rtol=tol)
+
+
+def normalized_error(Sg, So):
+    d = np.sqrt(np.abs(np.diag(So)))
+    d[d == 0] = 1.0
+    return np.abs((Sg - So) / np.outer(d, d)).max()
+
+
+@pytest.mark.parametrize("name,make,opts", CASES)
+@pytest.mark.parametrize("precision", [Precision.Fp64, Precision.Mixed])
+@pytest.mark.parametrize("damping", [0.0, 1e-3])
+def test_reduced_system_matches_oracle(name, make, opts, precision, damping):
+    p = make()
+    ctx = gpu(p, opts())
+    orc = O.Oracle(p, opts())
+    cg, sg = ctx.linearize_schur(damping, precision)
+    co, so = orc.build(damping)
+    assert sg == so
+    np.testing.assert_allclose(cg, co, rtol=1e-12)
+    S, rhs, direct = ctx.reduced()
+    So, red = orc.dense_reduced()
+    m = index_map(ctx, orc)
+    tol = 1e-9 if precision == Precision.Fp64 else 2e-4
+    assert normalized_error(S, So[np.ix_(m, m)]) < tol
+    d = np.sqrt(np.abs(np.diag(So[np.ix_(m, m)])))
+    assert np.abs((rhs + red["gradient"][m]) / d).max() < tol * max(1.0, np.abs(red["gradient"][m] / d).max())
+    assert np.abs((direct - red["direct_rhs"][m]) / d).max() < tol * max(1.0, np.abs(red["direct_rhs"][m] / d).max())
+
+
+@pytest.mark.parametrize("name,make,opts", CASES)
+@pytest.mark.parametrize("precision", [Precision.Fp64, Precision.Mixed])
+def test_reduced_solve_and_back_substitution_match_oracle(name, make, opts, precision):
+    p = make()
+    ctx = gpu(p, opts())
+    orc = O.Oracle(p, opts(), linear_solver=1)
+    ctx.linearize_schur(0.0, precision)
+    orc.build(0.0)
+    step, cv, it, rr = ctx.solve_reduced()
+    assert cv and rr <= 2e-10
+    ostep, ocv, _ = orc.solve_linear()
+    m = index_map(ctx, orc)
+    rel = np.linalg.norm(step - ostep[m]) / np.linalg.norm(ostep[m])
+    assert rel < (1e-7 if precision == Precision.Fp64 else 2e-4), rel
+    elim, dd, ok = ctx.back_substitute()
+    oelim, odd, ook = orc.back_substitute(ostep)
+    assert ok and ook
+    assert np.linalg.norm(elim - oelim) / np.linalg.norm(oelim) < (1e-7 if precision == Precision.Fp64 else 2e-4)
+    assert abs(dd - odd) / abs(odd) < (1e-7 if precision == Precision.Fp64 else 2e-4)
+
+
+@pytest.mark.parametrize("name,make,opts", CASES)
+@pytest.mark.parametrize("mixed", [False, True])
+def test_full_solve_matches_oracle(name, make, opts, mixed):
+    p = make()
+    ref = O.Oracle(p, opts()).solve()
+    ctx = gpu(p, opts(mixed))
+    rep = ctx.solve()
+    out = ctx.download()
+    rr = ref["report"]
+    assert rep["status"] == rr["status"] == SolveStatus.Success
+    rel_cost = abs(rep["final_cost"] - rr["final_cost"]) / rr["final_cost"]
+    assert rel_cost < (1e-9 if not mixed else 1e-6), rel_cost
+    np.testing.assert_allclose(rep["initial_cost"], rr["initial_cost"], rtol=1e-12)
+    C_ref = ref["cameras"][:, 9:12]
+    scale = np.linalg.norm(C_ref - C_ref.mean(0), axis=1).max()
+    cerr = np.abs(out["cameras"][:, 9:12] - C_ref).max() / scale
+    assert cerr < (1e-8 if not mixed else 1e-5), cerr
+    assert np.array_equal(out["valid"], ref["valid"])
+    if not mixed:
+        assert rep["iterations"] == rr["iterations"]
+        assert rep["accepted_steps"] == rr["accepted_steps"]
+        np.testing.assert_allclose(out["rms_after"][ref["valid"]], ref["rms_after"][ref["valid"]], rtol=1e-8)
+    np.testing.assert_allclose(out["rms_before"], ref["rms_before"], rtol=1e-12)
+    if ref["intrinsics"].size:
+        np.testing.assert_allclose(out["intrinsics"], ref["intrinsics"], rtol=1e-5 if mixed else 1e-8,
+                                   atol=1e-9)
