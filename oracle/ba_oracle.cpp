@@ -11,6 +11,8 @@
 #include <array>
 #include <chrono>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <memory>
@@ -1595,6 +1597,11 @@ int32_t orc_solve(void* h, orc_report* rep, double* camsOut, double* ptsOut, int
                     }
                     alpha *= 0.5;
                 }
+                if (std::getenv("PB_GPU_TRACE"))
+                    std::fprintf(stderr,
+                                 "ORACLE_TRACE it=%d cost=%.15e lambda=%.3e lin_it=%d dd=%.6e rms_global=%.3e "
+                                 "rms_point=%.3e alpha=%.6g cand=%.15e accepted=%d\n",
+                                 iterations, current, damping, lit, dd, rg, rp, alpha, cand, accepted ? 1 : 0);
                 if (std::isfinite(cand) && cand < current && accepted) {
                     o->state = std::move(cs);
                     current = cand;

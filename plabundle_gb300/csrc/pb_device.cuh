@@ -97,6 +97,8 @@ struct Lin {
     T Ji[2 * kMaxNI];   // 2 x ni intrinsic Jacobian (row-major, compact columns)
     T w;                // normal weight
     double cost;        // robust cost (FP64)
+    double rd0, rd1;    // residual (FP64)
+    double wd;          // normal weight (FP64)
 };
 
 // Linearises one observation.  `tangent` selects the gauge tangent centre columns (basis: two
@@ -112,6 +114,9 @@ __device__ __forceinline__ bool linearize_obs(const DCam& c, double X0, double X
     double cost, rw;
     if (!robust_loss(wobs * (r0 * r0 + r1 * r1), loss, lscale, cost, rw)) return false;
     L.cost = cost;
+    L.rd0 = r0;
+    L.rd1 = r1;
+    L.wd = wobs * rw;
     L.r0 = static_cast<T>(r0);
     L.r1 = static_cast<T>(r1);
     L.w = static_cast<T>(wobs * rw);

@@ -99,6 +99,13 @@ int build_host_model(const pb_problem_desc* pr, const pb_solve_options* op, Host
         if (cam[12] <= 0.0 || cam[13] <= 0.0) { *err = "camera focal lengths must be positive"; return PB_SOLVE_INVALID_INPUT; }
         if (cam[24] < 0.0 || cam[25] < 0.0) { *err = "camera image size must be non-negative"; return PB_SOLVE_INVALID_INPUT; }
     }
+    if (op->robust_loss < 0 || op->robust_loss > 2 || !std::isfinite(op->robust_loss_scale) ||
+        op->robust_loss_scale <= 0.0) {
+        *err = "image robust loss must be LeastSquares, Huber or Cauchy with a finite positive scale";
+        return PB_SOLVE_INVALID_INPUT;
+    }
+    m->loss = op->robust_loss;
+    m->loss_scale = op->robust_loss_scale;
     if (op->preconditioner_cluster_size > 1) {
         *err = "only block-Jacobi cluster size 1 is implemented by the GB300 backend";
         return PB_SOLVE_UNSUPPORTED;
@@ -408,13 +415,14 @@ size_t chunk_smem_bytes(int precision, int max_obs, int max_cams, int max_pairs,
     auto al = [](size_t v) { return (v + 15) & ~static_cast<size_t>(15); };
     size_t s = 0;
     s += al(static_cast<size_t>(max_cams) * max_cams * 2);             // pair lookup
-    s += al(static_cast<size_t>(max_pairs) * 36 * ts);                 // pair accumulators
-    s += al(static_cast<size_t>(max_cams) * 12 * ts);                  // rhs accumulators
-    s += al(static_cast<size_t>(max_cams) * ng * 6 * ni * ts);         // border accumulators
-    s += al((nb * nb + 2 * nb) * ts);                                  // intrinsic block + rhs
-    const size_t per_obs = std::max<size_t>(18 + 3 * static_cast<size_t>(ni), 9);
-    s += al(static_cast<size_t>(max_obs) * per_obs * ts);              // G_o (aliased with V_o)
-    s += al(static_cast<size_t>(max_obs) * 9 * ts);                   // track factor and q
+    s += al(static_cast<size_t>(max_pairs) * 36 * 8);                  // pair accumulators (FP64)
+    s += al(static_cast<size_t>(max_cams) * 12 * 8);                   // rhs accumulators (FP64)
+    s += al(static_cast<size_t>(max_cams) * ng * 6 * ni * 8);          // border accumulators (FP64)
+    s += al((nb * nb + 2 * nb) * 8);                                   // intrinsic block + rhs (FP64)
+    const size_t per_obs = 18 + 3 * static_cast<size_t>(ni);
+    s += al(static_cast<size_t>(max_obs) * per_obs * ts);              // G_o
+    s += al(static_cast<size_t>(max_obs) * 9 * 8);                    // V_o, rhs_o (FP64)
+    s += al(static_cast<size_t>(max_obs) * 9 * 8);                    // track factor and q (FP64)
     s += al(static_cast<size_t>(max_obs) * 4);                         // track start per obs
     s += al(64 * 8);                                                   // warp partial costs, flags
     return s;
@@ -424,7 +432,7 @@ int build_chunks(HostModel* m, int precision, size_t smem_budget, std::string* e
     ChunkSet& cs = m->chunks[precision];
     int max_obs = precision == PB_PRECISION_FP64 ? 128 : 256;
     int max_cams = precision == PB_PRECISION_FP64 ? 48 : 64;
-    int max_pairs = precision == PB_PRECISION_FP64 ? 256 : 384;
+    int max_pairs = precision == PB_PRECISION_FP64 ? 256 : 320;
     while (chunk_smem_bytes(precision, max_obs, max_cams, max_pairs, m->ng, m->ni) > smem_budget && max_pairs > 64) {
         max_pairs -= 32;
         if (max_cams > 32) max_cams -= 8;

@@ -117,6 +117,8 @@ struct HostModel {
     std::vector<int> fixed_cams, fixed_tracks, group_ids;
     int gauge_anchor = -1, gauge_scale = -1;
     double gauge_baseline = 0.0;
+    int loss = 0;
+    double loss_scale = 1.0;
     // active problem
     std::vector<signed char> active_track;
     std::vector<int> camera_block, intrinsic_block, calib_group, track_block;

@@ -19,7 +19,6 @@ namespace pb {
 
 namespace {
 
-__device__ __forceinline__ void atomic_add_t(float* p, float v) { atomicAdd(p, v); }
 __device__ __forceinline__ void atomic_add_t(double* p, double v) { atomicAdd(p, v); }
 
 template <typename T>
@@ -32,21 +31,22 @@ __device__ __forceinline__ T* carve(char*& ptr, size_t count) {
 }  // namespace
 
 template <typename T>
-__global__ void __launch_bounds__(256) k_assemble(Shape S, DevPtrs D, AsmOutT<T> O, double damping) {
+__global__ void __launch_bounds__(256, 1) k_assemble(Shape S, DevPtrs D, AsmOutT<T> O, double damping) {
     extern __shared__ __align__(16) char smem[];
     const int chunk = blockIdx.x;
     const int tid = threadIdx.x;
     const int MC = S.max_cams, MP = S.max_pairs, MO = S.max_obs;
     const int ng = S.ng, ni = S.ni, nb = S.nb;
-    const int per_obs = max(18 + 3 * ni, 9);
+    const int per_obs = 18 + 3 * ni;
     char* ptr = smem;
     unsigned short* s_lookup = carve<unsigned short>(ptr, static_cast<size_t>(MC) * MC);
-    T* s_pair = carve<T>(ptr, static_cast<size_t>(MP) * 36);
-    T* s_rhs = carve<T>(ptr, static_cast<size_t>(MC) * 12);
-    T* s_border = carve<T>(ptr, static_cast<size_t>(MC) * ng * 6 * ni);
-    T* s_C = carve<T>(ptr, static_cast<size_t>(nb) * nb + 2 * nb);
+    double* s_pair = carve<double>(ptr, static_cast<size_t>(MP) * 36);
+    double* s_rhs = carve<double>(ptr, static_cast<size_t>(MC) * 12);
+    double* s_border = carve<double>(ptr, static_cast<size_t>(MC) * ng * 6 * ni);
+    double* s_C = carve<double>(ptr, static_cast<size_t>(nb) * nb + 2 * nb);
     T* s_G = carve<T>(ptr, static_cast<size_t>(MO) * per_obs);
-    T* s_trk = carve<T>(ptr, static_cast<size_t>(MO) * 9);
+    double* s_V = carve<double>(ptr, static_cast<size_t>(MO) * 9);
+    double* s_trk = carve<double>(ptr, static_cast<size_t>(MO) * 9);
     int* s_first = carve<int>(ptr, MO);
     double* s_misc = carve<double>(ptr, 64);
     int* s_flags = reinterpret_cast<int*>(s_misc + 40);
@@ -56,10 +56,10 @@ __global__ void __launch_bounds__(256) k_assemble(Shape S, DevPtrs D, AsmOutT<T>
     const int pair0 = D.ch_pair_begin[chunk], npairs = D.ch_pair_begin[chunk + 1] - pair0;
 
     for (int i = tid; i < MC * MC; i += blockDim.x) s_lookup[i] = 0xFFFF;
-    for (int i = tid; i < npairs * 36; i += blockDim.x) s_pair[i] = T(0);
-    for (int i = tid; i < ncams * 12; i += blockDim.x) s_rhs[i] = T(0);
-    for (int i = tid; i < ncams * ng * 6 * ni; i += blockDim.x) s_border[i] = T(0);
-    for (int i = tid; i < nb * nb + 2 * nb; i += blockDim.x) s_C[i] = T(0);
+    for (int i = tid; i < npairs * 36; i += blockDim.x) s_pair[i] = 0.0;
+    for (int i = tid; i < ncams * 12; i += blockDim.x) s_rhs[i] = 0.0;
+    for (int i = tid; i < ncams * ng * 6 * ni; i += blockDim.x) s_border[i] = 0.0;
+    for (int i = tid; i < nb * nb + 2 * nb; i += blockDim.x) s_C[i] = 0.0;
     if (tid == 0) s_flags[0] = 0;
     __syncthreads();
     for (int s = tid; s < npairs; s += blockDim.x) {
@@ -67,7 +67,7 @@ __global__ void __launch_bounds__(256) k_assemble(Shape S, DevPtrs D, AsmOutT<T>
         s_lookup[(pk & 0xFFFF) * MC + (pk >> 16)] = static_cast<unsigned short>(s);
     }
 
-    // ---- phase 1: linearise one observation per thread
+    // ---- phase 1: linearise one observation per thread; FP64 point normal equations
     const bool active = tid < nobs;
     const int o = obs0 + tid;
     Lin<T> L;
@@ -96,21 +96,22 @@ __global__ void __launch_bounds__(256) k_assemble(Shape S, DevPtrs D, AsmOutT<T>
             O.obs_wn[o] = L.w;
         }
         s_first[tid] = first;
+        double* V = s_V + static_cast<size_t>(tid) * 9;
         if (elim && ok) {
-            T* V = s_G + static_cast<size_t>(tid) * per_obs;
-            const T w = L.w;
-            V[0] = w * (L.Jp[0] * L.Jp[0] + L.Jp[3] * L.Jp[3]);
-            V[1] = w * (L.Jp[0] * L.Jp[1] + L.Jp[3] * L.Jp[4]);
-            V[2] = w * (L.Jp[0] * L.Jp[2] + L.Jp[3] * L.Jp[5]);
-            V[3] = w * (L.Jp[1] * L.Jp[1] + L.Jp[4] * L.Jp[4]);
-            V[4] = w * (L.Jp[1] * L.Jp[2] + L.Jp[4] * L.Jp[5]);
-            V[5] = w * (L.Jp[2] * L.Jp[2] + L.Jp[5] * L.Jp[5]);
-            V[6] = -w * (L.Jp[0] * L.r0 + L.Jp[3] * L.r1);
-            V[7] = -w * (L.Jp[1] * L.r0 + L.Jp[4] * L.r1);
-            V[8] = -w * (L.Jp[2] * L.r0 + L.Jp[5] * L.r1);
+            // V_o = w Jp^T Jp and rhs_o = -w Jp^T r from the (rounded) Jacobian, summed in FP64
+            const double w = L.wd;
+            const double j0 = L.Jp[0], j1 = L.Jp[1], j2 = L.Jp[2], j3 = L.Jp[3], j4 = L.Jp[4], j5 = L.Jp[5];
+            V[0] = w * (j0 * j0 + j3 * j3);
+            V[1] = w * (j0 * j1 + j3 * j4);
+            V[2] = w * (j0 * j2 + j3 * j5);
+            V[3] = w * (j1 * j1 + j4 * j4);
+            V[4] = w * (j1 * j2 + j4 * j5);
+            V[5] = w * (j2 * j2 + j5 * j5);
+            V[6] = -w * (j0 * L.rd0 + j3 * L.rd1);
+            V[7] = -w * (j1 * L.rd0 + j4 * L.rd1);
+            V[8] = -w * (j2 * L.rd0 + j5 * L.rd1);
         } else if (elim) {
-            T* V = s_G + static_cast<size_t>(tid) * per_obs;
-            for (int i = 0; i < 9; ++i) V[i] = T(0);
+            for (int i = 0; i < 9; ++i) V[i] = 0.0;
         }
     }
     __syncthreads();
@@ -119,9 +120,9 @@ __global__ void __launch_bounds__(256) k_assemble(Shape S, DevPtrs D, AsmOutT<T>
     if (active && elim && tid == first) {
         double V[6] = {0, 0, 0, 0, 0, 0}, rhs[3] = {0, 0, 0};
         for (int j = 0; j < k; ++j) {
-            const T* v = s_G + static_cast<size_t>(first + j) * per_obs;
-            for (int i = 0; i < 6; ++i) V[i] += static_cast<double>(v[i]);
-            for (int i = 0; i < 3; ++i) rhs[i] += static_cast<double>(v[6 + i]);
+            const double* v = s_V + static_cast<size_t>(first + j) * 9;
+            for (int i = 0; i < 6; ++i) V[i] += v[i];
+            for (int i = 0; i < 3; ++i) rhs[i] += v[6 + i];
         }
         V[0] *= 1.0 + damping;
         V[3] *= 1.0 + damping;
@@ -153,78 +154,96 @@ __global__ void __launch_bounds__(256) k_assemble(Shape S, DevPtrs D, AsmOutT<T>
             }
         }
         if (singular) atomicOr(s_flags, 1);
-        T* st = s_trk + static_cast<size_t>(first) * 9;
-        T* gt = O.trk_data + static_cast<size_t>(trk) * kTrackRec;
-        for (int i = 0; i < 6; ++i) { st[i] = static_cast<T>(Ri[i]); gt[i] = static_cast<T>(Ri[i]); }
+        double* st = s_trk + static_cast<size_t>(first) * 9;
+        double* gt = O.trk_data + static_cast<size_t>(trk) * kTrackRec;
+        for (int i = 0; i < 6; ++i) { st[i] = Ri[i]; gt[i] = Ri[i]; }
         for (int i = 0; i < 3; ++i) {
-            st[6 + i] = static_cast<T>(q[i]);
-            gt[6 + i] = static_cast<T>(q[i]);
-            gt[9 + i] = static_cast<T>(rhs[i]);
+            st[6 + i] = q[i];
+            gt[6 + i] = q[i];
+            gt[9 + i] = rhs[i];
         }
     }
     __syncthreads();
 
-    // ---- phase 3: G_o = W_o R^-T, direct terms
-    T q0 = T(0), q1 = T(0), q2 = T(0);
+    // ---- phase 3: per observation, in FP64: Y = w Jp R^-T (2x3), the reduced weight
+    // M = w I - Y Y^T (2x2) and the reduced residual Mr = w r + Y q.  The observation's own
+    // contribution J^T M J, -J^T Mr is then formed with FP32 products: the cancellation between
+    // the direct term and the point elimination happens here, in FP64.  G_o = J^T Y (arithmetic
+    // type T) carries the couplings to the other observations of the track.
     if (active && ok) {
-        const T w = L.w;
-        T* G = s_G + static_cast<size_t>(tid) * per_obs;
+        const double w = L.wd;
+        double Y[2][3] = {{0, 0, 0}, {0, 0, 0}}, q[3] = {0, 0, 0};
         if (elim) {
-            const T* st = s_trk + static_cast<size_t>(first) * 9;
-            const T i00 = st[0], i10 = st[1], i11 = st[2], i20 = st[3], i21 = st[4], i22 = st[5];
-            q0 = st[6]; q1 = st[7]; q2 = st[8];
-            const int nrows = 6 + ni;
-            for (int a = 0; a < nrows; ++a) {
-                const T ja0 = a < 6 ? L.Jc[a] : L.Ji[a - 6];
-                const T ja1 = a < 6 ? L.Jc[6 + a] : L.Ji[kMaxNI + a - 6];
-                const T w0 = w * (ja0 * L.Jp[0] + ja1 * L.Jp[3]);
-                const T w1 = w * (ja0 * L.Jp[1] + ja1 * L.Jp[4]);
-                const T w2 = w * (ja0 * L.Jp[2] + ja1 * L.Jp[5]);
-                G[a * 3 + 0] = i00 * w0;
-                G[a * 3 + 1] = i10 * w0 + i11 * w1;
-                G[a * 3 + 2] = i20 * w0 + i21 * w1 + i22 * w2;
+            const double* st = s_trk + static_cast<size_t>(first) * 9;
+            const double i00 = st[0], i10 = st[1], i11 = st[2], i20 = st[3], i21 = st[4], i22 = st[5];
+            q[0] = st[6]; q[1] = st[7]; q[2] = st[8];
+            for (int pa = 0; pa < 2; ++pa) {
+                const double p0 = L.Jp[pa * 3], p1 = L.Jp[pa * 3 + 1], p2 = L.Jp[pa * 3 + 2];
+                Y[pa][0] = w * (i00 * p0);
+                Y[pa][1] = w * (i10 * p0 + i11 * p1);
+                Y[pa][2] = w * (i20 * p0 + i21 * p1 + i22 * p2);
             }
         }
-        const int dslot = lcam < ncams ? s_lookup[lcam * MC + lcam] : 0xFFFF;
+        const double m00 = w - (Y[0][0] * Y[0][0] + Y[0][1] * Y[0][1] + Y[0][2] * Y[0][2]);
+        const double m01 = -(Y[0][0] * Y[1][0] + Y[0][1] * Y[1][1] + Y[0][2] * Y[1][2]);
+        const double m11 = w - (Y[1][0] * Y[1][0] + Y[1][1] * Y[1][1] + Y[1][2] * Y[1][2]);
+        const double mr0 = w * L.rd0 + (Y[0][0] * q[0] + Y[0][1] * q[1] + Y[0][2] * q[2]);
+        const double mr1 = w * L.rd1 + (Y[1][0] * q[0] + Y[1][1] * q[1] + Y[1][2] * q[2]);
+        if (elim) {
+            T* G = s_G + static_cast<size_t>(tid) * per_obs;
+            const T y00 = static_cast<T>(Y[0][0]), y01 = static_cast<T>(Y[0][1]), y02 = static_cast<T>(Y[0][2]);
+            const T y10 = static_cast<T>(Y[1][0]), y11 = static_cast<T>(Y[1][1]), y12 = static_cast<T>(Y[1][2]);
+            for (int a = 0; a < 6 + ni; ++a) {
+                const T ja0 = a < 6 ? L.Jc[a] : L.Ji[a - 6];
+                const T ja1 = a < 6 ? L.Jc[6 + a] : L.Ji[kMaxNI + a - 6];
+                G[a * 3 + 0] = ja0 * y00 + ja1 * y10;
+                G[a * 3 + 1] = ja0 * y01 + ja1 * y11;
+                G[a * 3 + 2] = ja0 * y02 + ja1 * y12;
+            }
+        }
+        const T M00 = static_cast<T>(m00), M01 = static_cast<T>(m01), M11 = static_cast<T>(m11);
+        const int dslot = (lcam != 255 && lcam < ncams) ? s_lookup[lcam * MC + lcam] : 0xFFFF;
         if (lcam != 255 && dslot >= npairs) atomicOr(s_flags, 4);
         if (lcam != 255 && dslot < npairs) {
-            T* P = s_pair + static_cast<size_t>(dslot) * 36;
+            double* P = s_pair + static_cast<size_t>(dslot) * 36;
+            T mj0[6], mj1[6];
+            for (int b = 0; b < 6; ++b) {
+                mj0[b] = M00 * L.Jc[b] + M01 * L.Jc[6 + b];
+                mj1[b] = M01 * L.Jc[b] + M11 * L.Jc[6 + b];
+            }
             for (int a = 0; a < 6; ++a)
-                for (int b = 0; b < 6; ++b)
-                    atomic_add_t(P + a * 6 + b, w * (L.Jc[a] * L.Jc[b] + L.Jc[6 + a] * L.Jc[6 + b]));
+                for (int b = 0; b < 6; ++b) atomic_add_t(P + a * 6 + b, L.Jc[a] * mj0[b] + L.Jc[6 + a] * mj1[b]);
             for (int a = 0; a < 6; ++a) {
-                const T dr = -w * (L.Jc[a] * L.r0 + L.Jc[6 + a] * L.r1);
-                T sr = T(0);
-                if (elim) sr = G[a * 3] * q0 + G[a * 3 + 1] * q1 + G[a * 3 + 2] * q2;
-                atomic_add_t(s_rhs + lcam * 12 + a, dr - sr);
-                atomic_add_t(s_rhs + lcam * 12 + 6 + a, dr);
+                const double ja0 = L.Jc[a], ja1 = L.Jc[6 + a];
+                atomic_add_t(s_rhs + lcam * 12 + a, -(ja0 * mr0 + ja1 * mr1));
+                atomic_add_t(s_rhs + lcam * 12 + 6 + a, -w * (ja0 * L.rd0 + ja1 * L.rd1));
             }
         }
         if (ng > 0 && grp >= 0) {
             for (int a = 0; a < ni; ++a) {
-                const T ja0 = L.Ji[a], ja1 = L.Ji[kMaxNI + a];
+                const T mi0 = M00 * L.Ji[a] + M01 * L.Ji[kMaxNI + a];
+                const T mi1 = M01 * L.Ji[a] + M11 * L.Ji[kMaxNI + a];
                 for (int b = 0; b < ni; ++b)
-                    atomic_add_t(s_C + (grp * ni + a) * nb + grp * ni + b, w * (ja0 * L.Ji[b] + ja1 * L.Ji[kMaxNI + b]));
-                const T dr = -w * (ja0 * L.r0 + ja1 * L.r1);
-                atomic_add_t(s_C + nb * nb + grp * ni + a, dr);
-                atomic_add_t(s_C + nb * nb + nb + grp * ni + a, dr);
+                    atomic_add_t(s_C + (grp * ni + b) * nb + grp * ni + a, L.Ji[b] * mi0 + L.Ji[kMaxNI + b] * mi1);
+                const double ja0 = L.Ji[a], ja1 = L.Ji[kMaxNI + a];
+                atomic_add_t(s_C + nb * nb + grp * ni + a, -(ja0 * mr0 + ja1 * mr1));
+                atomic_add_t(s_C + nb * nb + nb + grp * ni + a, -w * (ja0 * L.rd0 + ja1 * L.rd1));
                 if (lcam != 255 && lcam < ncams)
                     for (int b = 0; b < 6; ++b)
-                        atomic_add_t(s_border + ((lcam * ng + grp) * 6 + b) * ni + a,
-                                     w * (L.Jc[b] * ja0 + L.Jc[6 + b] * ja1));
+                        atomic_add_t(s_border + ((lcam * ng + grp) * 6 + b) * ni + a, L.Jc[b] * mi0 + L.Jc[6 + b] * mi1);
             }
         }
     }
     __syncthreads();
 
-    // ---- phase 4: point Schur complement of each track, pairs spread over the track's threads
+    // ---- phase 4: couplings between different observations of an eliminated track
     if (active && ok && elim) {
         const int j = tid - first;
-        const int npt = k * (k + 1) / 2;
+        const int npt = k * (k - 1) / 2;  // strictly upper pairs a < b
         for (int p = j; p < npt; p += k) {
             int a = 0, rem = p;
-            while (rem >= k - a) { rem -= k - a; ++a; }
-            const int b = a + rem;
+            while (rem >= k - 1 - a) { rem -= k - 1 - a; ++a; }
+            const int b = a + 1 + rem;
             const int oa = first + a, ob = first + b;
             const int la = D.obs_lcam[obs0 + oa], lb = D.obs_lcam[obs0 + ob];
             if (la == 255 || lb == 255) continue;
@@ -236,11 +255,11 @@ __global__ void __launch_bounds__(256) k_assemble(Shape S, DevPtrs D, AsmOutT<T>
                 atomicOr(s_flags, 4);
                 continue;
             }
-            T* P = s_pair + static_cast<size_t>(slot) * 36;
+            double* P = s_pair + static_cast<size_t>(slot) * 36;
             for (int x = 0; x < 6; ++x)
                 for (int y = 0; y < 6; ++y) {
                     const T m = Ga[x * 3] * Gb[y * 3] + Ga[x * 3 + 1] * Gb[y * 3 + 1] + Ga[x * 3 + 2] * Gb[y * 3 + 2];
-                    if (a == b || la < lb) {
+                    if (la < lb) {
                         atomic_add_t(P + x * 6 + y, -m);
                     } else if (la > lb) {
                         atomic_add_t(P + y * 6 + x, -m);
@@ -251,7 +270,10 @@ __global__ void __launch_bounds__(256) k_assemble(Shape S, DevPtrs D, AsmOutT<T>
                 }
         }
         if (ng > 0) {
-            // intrinsic coupling: K_g = sum over the track's observations of group g of G_o^int
+            // K_g = sum of G^int over the track's observations of group g.  The pose-intrinsic and
+            // intrinsic-intrinsic couplings of distinct observations are -G^pose (K_g - own)^T and
+            // -(K_g K_g'^T - sum_own G^int G^int^T); the observation's own terms are in phase 3.
+            const T* Go = s_G + static_cast<size_t>(tid) * per_obs;
             for (int g = 0; g < ng; ++g) {
                 T K[3 * kMaxNI];
                 bool present = false;
@@ -264,16 +286,24 @@ __global__ void __launch_bounds__(256) k_assemble(Shape S, DevPtrs D, AsmOutT<T>
                     for (int i = 0; i < 3 * ni; ++i) K[i] += Gj[i];
                 }
                 if (!present) continue;
-                const T* Go = s_G + static_cast<size_t>(tid) * per_obs;
-                if (lcam != 255 && lcam < ncams)
+                if (lcam != 255 && lcam < ncams) {
+                    T Kx[3 * kMaxNI];
+                    for (int i = 0; i < 3 * ni; ++i) Kx[i] = K[i] - (g == grp ? Go[18 + i] : T(0));
                     for (int x = 0; x < 6; ++x)
                         for (int c2 = 0; c2 < ni; ++c2)
                             atomic_add_t(s_border + ((lcam * ng + g) * 6 + x) * ni + c2,
-                                         -(Go[x * 3] * K[c2 * 3] + Go[x * 3 + 1] * K[c2 * 3 + 1] +
-                                           Go[x * 3 + 2] * K[c2 * 3 + 2]));
+                                         -(Go[x * 3] * Kx[c2 * 3] + Go[x * 3 + 1] * Kx[c2 * 3 + 1] +
+                                           Go[x * 3 + 2] * Kx[c2 * 3 + 2]));
+                }
+                if (g == grp)
+                    for (int c1 = 0; c1 < ni; ++c1)
+                        for (int c2 = 0; c2 < ni; ++c2) {
+                            const T* gi = Go + 18;
+                            atomic_add_t(s_C + (g * ni + c1) * nb + g * ni + c2,
+                                         gi[c1 * 3] * gi[c2 * 3] + gi[c1 * 3 + 1] * gi[c2 * 3 + 1] +
+                                             gi[c1 * 3 + 2] * gi[c2 * 3 + 2]);
+                        }
                 if (j == 0) {
-                    for (int c2 = 0; c2 < ni; ++c2)
-                        atomic_add_t(s_C + nb * nb + g * ni + c2, -(K[c2 * 3] * q0 + K[c2 * 3 + 1] * q1 + K[c2 * 3 + 2] * q2));
                     for (int g2 = g; g2 < ng; ++g2) {
                         T K2[3 * kMaxNI];
                         bool present2 = false;
@@ -304,16 +334,16 @@ __global__ void __launch_bounds__(256) k_assemble(Shape S, DevPtrs D, AsmOutT<T>
     __syncthreads();
 
     // ---- phase 5: write the chunk's partial blocks
-    T* pp = O.part_pair + static_cast<size_t>(pair0) * 36;
+    double* pp = O.part_pair + static_cast<size_t>(pair0) * 36;
     for (int i = tid; i < npairs * 36; i += blockDim.x) pp[i] = s_pair[i];
     const int camrec = 12 + ng * 6 * ni;
-    T* pc = O.part_cam + static_cast<size_t>(cam0) * camrec;
+    double* pc = O.part_cam + static_cast<size_t>(cam0) * camrec;
     for (int i = tid; i < ncams * camrec; i += blockDim.x) {
         const int l = i / camrec, e = i - l * camrec;
         pc[i] = e < 12 ? s_rhs[l * 12 + e] : s_border[l * ng * 6 * ni + (e - 12)];
     }
     const int chrec = nb * nb + 2 * nb;
-    T* pk = O.part_chunk + static_cast<size_t>(chunk) * chrec;
+    double* pk = O.part_chunk + static_cast<size_t>(chunk) * chrec;
     for (int i = tid; i < chrec; i += blockDim.x) pk[i] = s_C[i];
     if (tid == 0) {
         double c = 0.0;
@@ -324,32 +354,30 @@ __global__ void __launch_bounds__(256) k_assemble(Shape S, DevPtrs D, AsmOutT<T>
 }
 
 // Sum of the chunk partials of every upper pose block, written to both CSR orientations.
-template <typename T>
-__global__ void k_reduce_pairs(Shape S, DevPtrs D, AsmOutT<T> O, T* __restrict__ vals) {
+__global__ void k_reduce_pairs(Shape S, DevPtrs D, const double* __restrict__ part_pair, double* __restrict__ vals) {
     const long long idx = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (idx >= static_cast<long long>(S.nupper) * 36) return;
     const int u = static_cast<int>(idx / 36), e = static_cast<int>(idx - static_cast<long long>(u) * 36);
-    Acc<T> acc;
+    Acc<double> acc;
     for (int c = D.up_contrib_begin[u]; c < D.up_contrib_begin[u + 1]; ++c)
-        acc.add(O.part_pair[static_cast<size_t>(D.up_contrib[c]) * 36 + e]);
-    const T v = acc.value();
+        acc.add(part_pair[static_cast<size_t>(D.up_contrib[c]) * 36 + e]);
+    const double v = acc.value();
     vals[static_cast<size_t>(D.up_csr[u]) * 36 + e] = v;
     const int t = D.up_csr_t[u];
     if (t >= 0) vals[static_cast<size_t>(t) * 36 + (e % 6) * 6 + e / 6] = v;
 }
 
 // Sum of the per-camera partials: rhs, direct rhs and the intrinsic border rows.
-template <typename T>
-__global__ void k_reduce_cams(Shape S, DevPtrs D, AsmOutT<T> O, T* __restrict__ rhs, T* __restrict__ direct,
-                              T* __restrict__ border) {
+__global__ void k_reduce_cams(Shape S, DevPtrs D, const double* __restrict__ part_cam, double* __restrict__ rhs,
+                              double* __restrict__ direct, double* __restrict__ border) {
     const int camrec = 12 + S.ng * 6 * S.ni;
     const long long idx = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (idx >= static_cast<long long>(S.ncb) * camrec) return;
     const int i = static_cast<int>(idx / camrec), e = static_cast<int>(idx - static_cast<long long>(i) * camrec);
-    Acc<T> acc;
+    Acc<double> acc;
     for (int c = D.cam_contrib_begin[i]; c < D.cam_contrib_begin[i + 1]; ++c)
-        acc.add(O.part_cam[static_cast<size_t>(D.cam_contrib[c]) * camrec + e]);
-    const T v = acc.value();
+        acc.add(part_cam[static_cast<size_t>(D.cam_contrib[c]) * camrec + e]);
+    const double v = acc.value();
     if (e < 6) rhs[i * 6 + e] = v;
     else if (e < 12) direct[i * 6 + e - 6] = v;
     else {
@@ -360,14 +388,14 @@ __global__ void k_reduce_cams(Shape S, DevPtrs D, AsmOutT<T> O, T* __restrict__ 
 }
 
 // Chunk-level sums (intrinsic block, intrinsic rhs, cost, flags); one CTA, fixed order.
-template <typename T>
-__global__ void k_reduce_chunks(Shape S, AsmOutT<T> O, T* __restrict__ Cm, T* __restrict__ rhs_b,
-                                T* __restrict__ direct_b, double* __restrict__ result) {
+__global__ void k_reduce_chunks(Shape S, const double* __restrict__ part_chunk, const double* __restrict__ part_cost,
+                                const int* __restrict__ part_flags, double* __restrict__ Cm, double* __restrict__ rhs_b,
+                                double* __restrict__ direct_b, double* __restrict__ result) {
     const int nb = S.nb, chrec = nb * nb + 2 * nb;
     for (int e = threadIdx.x; e < chrec; e += blockDim.x) {
-        Acc<T> acc;
-        for (int c = 0; c < S.nchunks; ++c) acc.add(O.part_chunk[static_cast<size_t>(c) * chrec + e]);
-        const T v = acc.value();
+        Acc<double> acc;
+        for (int c = 0; c < S.nchunks; ++c) acc.add(part_chunk[static_cast<size_t>(c) * chrec + e]);
+        const double v = acc.value();
         if (e < nb * nb) Cm[e] = v;
         else if (e < nb * nb + nb) rhs_b[e - nb * nb] = v;
         else direct_b[e - nb * nb - nb] = v;
@@ -377,8 +405,8 @@ __global__ void k_reduce_chunks(Shape S, AsmOutT<T> O, T* __restrict__ Cm, T* __
     double c = 0.0;
     int f = 0;
     for (int i = threadIdx.x; i < S.nchunks; i += blockDim.x) {
-        c += O.part_cost[i];
-        f |= O.part_flags[i];
+        c += part_cost[i];
+        f |= part_flags[i];
     }
     s_cost[threadIdx.x] = c;
     s_flag[threadIdx.x] = f;
@@ -398,15 +426,15 @@ __global__ void k_reduce_chunks(Shape S, AsmOutT<T> O, T* __restrict__ Cm, T* __
 
 // Intrinsic priors (assembleReferencePriors, ...ReferenceSchur.cpp:492-536) and
 // finalizePrimaryDiagonal(1 + lambda, 1): positive diagonal entries scaled, empty ones set to 1.
-template <typename T>
-__global__ void k_finalize(Shape S, DevPtrs D, T* __restrict__ vals, T* __restrict__ Cm, T* __restrict__ rhs_b,
-                           T* __restrict__ direct_b, double* __restrict__ result, double damping) {
+__global__ void k_finalize(Shape S, DevPtrs D, double* __restrict__ vals, double* __restrict__ Cm,
+                           double* __restrict__ rhs_b, double* __restrict__ direct_b, double* __restrict__ result,
+                           double damping) {
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
     if (tid < S.ncb * 6) {
         const int i = tid / 6, a = tid - i * 6;
-        T* d = vals + static_cast<size_t>(D.diag_pos[i]) * 36 + a * 7;
-        const T v = *d;
-        *d = v != T(0) ? static_cast<T>(static_cast<double>(v) * (1.0 + damping)) : T(1);
+        double* d = vals + static_cast<size_t>(D.diag_pos[i]) * 36 + a * 7;
+        const double v = *d;
+        *d = v != 0.0 ? v * (1.0 + damping) : 1.0;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0 && S.ng > 0) {
         double cost = 0.0;
@@ -418,11 +446,11 @@ __global__ void k_finalize(Shape S, DevPtrs D, T* __restrict__ vals, T* __restri
                 const double r = w * (G[p] - G[kP + p]);
                 cost += 0.5 * r * r;
                 const int col = g * S.ni + c;
-                T* cd = Cm + col * S.nb + col;
-                const double v = static_cast<double>(*cd) + w * w;
-                *cd = static_cast<T>(v != 0.0 ? v * (1.0 + damping) : 1.0);
-                rhs_b[col] = static_cast<T>(static_cast<double>(rhs_b[col]) - w * r);
-                direct_b[col] = static_cast<T>(static_cast<double>(direct_b[col]) - w * r);
+                double* cd = Cm + col * S.nb + col;
+                const double v = *cd + w * w;
+                *cd = v != 0.0 ? v * (1.0 + damping) : 1.0;
+                rhs_b[col] -= w * r;
+                direct_b[col] -= w * r;
             }
         }
         result[0] += cost;
@@ -670,14 +698,14 @@ __global__ void k_cost_final(Shape S, DevPtrs D, const double* __restrict__ part
 // Back-substitution (recoverReferencePointSteps, ...ReferenceSchur.cpp:982-1082), one thread per
 // track:  dp = R^-T (q - R^-1 u),  u = sum_o w J_p^T (J_o dc).
 template <typename T>
-__global__ void __launch_bounds__(256) k_back_substitute(Shape S, DevPtrs D, const T* __restrict__ trk_data,
+__global__ void __launch_bounds__(256) k_back_substitute(Shape S, DevPtrs D, const double* __restrict__ trk_data,
                                                          const T* __restrict__ obs_wn, const double* __restrict__ step_c,
                                                          double* __restrict__ step_p, double* __restrict__ part) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     double dd = 0.0, ss = 0.0;
     if (t < S.ntp && D.trk_block[t] >= 0) {
         const double* X = D.points + static_cast<size_t>(t) * 3;
-        T u0 = T(0), u1 = T(0), u2 = T(0);
+        double u0 = 0.0, u1 = 0.0, u2 = 0.0;
         for (int o = D.trk_obs_begin[t]; o < D.trk_obs_begin[t + 1]; ++o) {
             const int cam = D.obs_cam[o];
             DCam c;
@@ -687,38 +715,39 @@ __global__ void __launch_bounds__(256) k_back_substitute(Shape S, DevPtrs D, con
             if (!linearize_obs<T>(c, X[0], X[1], X[2], D.obs_u[o], D.obs_v[o], D.obs_w[o], S.loss, S.loss_scale,
                                   tangent, D.gauge_basis, S.ni, S.int_cols, true, L))
                 continue;
-            T j0 = T(0), j1 = T(0);
+            double j0 = 0.0, j1 = 0.0;
             const int b = D.cam_block[cam];
             if (b >= 0)
                 for (int a = 0; a < 6; ++a) {
-                    const T dcv = static_cast<T>(step_c[6 * b + a]);
-                    j0 += L.Jc[a] * dcv;
-                    j1 += L.Jc[6 + a] * dcv;
+                    const double dcv = step_c[6 * b + a];
+                    j0 = fma(static_cast<double>(L.Jc[a]), dcv, j0);
+                    j1 = fma(static_cast<double>(L.Jc[6 + a]), dcv, j1);
                 }
             const int g = D.cam_group[cam];
             if (S.ng > 0 && g >= 0)
                 for (int a = 0; a < S.ni; ++a) {
-                    const T dcv = static_cast<T>(step_c[6 * S.ncb + g * S.ni + a]);
-                    j0 += L.Ji[a] * dcv;
-                    j1 += L.Ji[kMaxNI + a] * dcv;
+                    const double dcv = step_c[6 * S.ncb + g * S.ni + a];
+                    j0 = fma(static_cast<double>(L.Ji[a]), dcv, j0);
+                    j1 = fma(static_cast<double>(L.Ji[kMaxNI + a]), dcv, j1);
                 }
-            const T w = obs_wn[o];
-            u0 += w * (L.Jp[0] * j0 + L.Jp[3] * j1);
-            u1 += w * (L.Jp[1] * j0 + L.Jp[4] * j1);
-            u2 += w * (L.Jp[2] * j0 + L.Jp[5] * j1);
+            const double w = L.wd;
+            u0 += w * (static_cast<double>(L.Jp[0]) * j0 + static_cast<double>(L.Jp[3]) * j1);
+            u1 += w * (static_cast<double>(L.Jp[1]) * j0 + static_cast<double>(L.Jp[4]) * j1);
+            u2 += w * (static_cast<double>(L.Jp[2]) * j0 + static_cast<double>(L.Jp[5]) * j1);
         }
-        const T* td = trk_data + static_cast<size_t>(t) * kTrackRec;
-        const T i00 = td[0], i10 = td[1], i11 = td[2], i20 = td[3], i21 = td[4], i22 = td[5];
-        const T v0 = td[6] - i00 * u0;
-        const T v1 = td[7] - (i10 * u0 + i11 * u1);
-        const T v2 = td[8] - (i20 * u0 + i21 * u1 + i22 * u2);
-        const double p0 = static_cast<double>(i00 * v0 + i10 * v1 + i20 * v2);
-        const double p1 = static_cast<double>(i11 * v1 + i21 * v2);
-        const double p2 = static_cast<double>(i22 * v2);
+        (void)obs_wn;
+        const double* td = trk_data + static_cast<size_t>(t) * kTrackRec;
+        const double i00 = td[0], i10 = td[1], i11 = td[2], i20 = td[3], i21 = td[4], i22 = td[5];
+        const double v0 = td[6] - i00 * u0;
+        const double v1 = td[7] - (i10 * u0 + i11 * u1);
+        const double v2 = td[8] - (i20 * u0 + i21 * u1 + i22 * u2);
+        const double p0 = i00 * v0 + i10 * v1 + i20 * v2;
+        const double p1 = i11 * v1 + i21 * v2;
+        const double p2 = i22 * v2;
         step_p[static_cast<size_t>(t) * 3 + 0] = p0;
         step_p[static_cast<size_t>(t) * 3 + 1] = p1;
         step_p[static_cast<size_t>(t) * 3 + 2] = p2;
-        dd = static_cast<double>(td[9]) * p0 + static_cast<double>(td[10]) * p1 + static_cast<double>(td[11]) * p2;
+        dd = td[9] * p0 + td[10] * p1 + td[11] * p2;
         ss = p0 * p0 + p1 * p1 + p2 * p2;
     } else if (t < S.ntp) {
         step_p[static_cast<size_t>(t) * 3 + 0] = 0.0;
@@ -870,8 +899,9 @@ __global__ void k_linearize_export(Shape S, DevPtrs D, double* __restrict__ res,
 // ---------------------------------------------------------------- launchers
 template <typename T>
 static AsmOutT<T> typed(const AsmOut& o) {
-    return {static_cast<T*>(o.part_pair_v), static_cast<T*>(o.part_cam_v), static_cast<T*>(o.part_chunk_v),
-            o.part_cost, o.part_flags, static_cast<T*>(o.trk_data_v), static_cast<T*>(o.obs_wn_v)};
+    return {static_cast<double*>(o.part_pair_v), static_cast<double*>(o.part_cam_v),
+            static_cast<double*>(o.part_chunk_v), o.part_cost, o.part_flags, static_cast<double*>(o.trk_data_v),
+            static_cast<T*>(o.obs_wn_v)};
 }
 
 template <typename T>
@@ -880,23 +910,24 @@ void launch_assemble(const Shape& S, const DevPtrs& D, const AsmOut& O, double d
     k_assemble<T><<<S.nchunks, S.max_obs, smem, st>>>(S, D, typed<T>(O), damping);
 }
 
-template <typename T>
-void launch_reduce(const Shape& S, const DevPtrs& D, const AsmOut& O, const RedOut<T>& R, double damping,
+void launch_reduce(const Shape& S, const DevPtrs& D, const AsmOut& O, const RedOut<double>& R, double damping,
                    cudaStream_t st) {
+    const double* pp = static_cast<const double*>(O.part_pair_v);
+    const double* pc = static_cast<const double*>(O.part_cam_v);
+    const double* pk = static_cast<const double*>(O.part_chunk_v);
     const long long np = static_cast<long long>(S.nupper) * 36;
-    if (np > 0) k_reduce_pairs<T><<<static_cast<unsigned>((np + 255) / 256), 256, 0, st>>>(S, D, typed<T>(O), R.vals);
+    if (np > 0) k_reduce_pairs<<<static_cast<unsigned>((np + 255) / 256), 256, 0, st>>>(S, D, pp, R.vals);
     const long long nc = static_cast<long long>(S.ncb) * (12 + S.ng * 6 * S.ni);
-    if (nc > 0)
-        k_reduce_cams<T><<<static_cast<unsigned>((nc + 255) / 256), 256, 0, st>>>(S, D, typed<T>(O), R.rhs, R.direct,
-                                                                                       R.border);
-    k_reduce_chunks<T><<<1, 256, 0, st>>>(S, typed<T>(O), R.Cm, R.rhs + 6 * S.ncb, R.direct + 6 * S.ncb, R.result);
+    if (nc > 0) k_reduce_cams<<<static_cast<unsigned>((nc + 255) / 256), 256, 0, st>>>(S, D, pc, R.rhs, R.direct, R.border);
+    k_reduce_chunks<<<1, 256, 0, st>>>(S, pk, O.part_cost, O.part_flags, R.Cm, R.rhs + 6 * S.ncb, R.direct + 6 * S.ncb,
+                                       R.result);
     const int nf = std::max(S.ncb * 6, 1);
-    k_finalize<T><<<(nf + 255) / 256, 256, 0, st>>>(S, D, R.vals, R.Cm, R.rhs + 6 * S.ncb, R.direct + 6 * S.ncb, R.result,
-                                                     damping);
+    k_finalize<<<(nf + 255) / 256, 256, 0, st>>>(S, D, R.vals, R.Cm, R.rhs + 6 * S.ncb, R.direct + 6 * S.ncb, R.result,
+                                                  damping);
 }
 
 template <typename T>
-void launch_back_substitute(const Shape& S, const DevPtrs& D, const T* trk_data, const T* obs_wn, const double* step_c,
+void launch_back_substitute(const Shape& S, const DevPtrs& D, const double* trk_data, const T* obs_wn, const double* step_c,
                             double* step_p, double* part, const double* direct64, double* out, cudaStream_t st) {
     const int nblk = std::max(1, (S.ntp + 255) / 256);
     k_back_substitute<T><<<nblk, 256, 0, st>>>(S, D, trk_data, obs_wn, step_c, step_p, part);
@@ -945,11 +976,7 @@ void pb_set_assemble_smem_f64(size_t bytes) {
 
 template void launch_assemble<float>(const Shape&, const DevPtrs&, const AsmOut&, double, size_t, cudaStream_t);
 template void launch_assemble<double>(const Shape&, const DevPtrs&, const AsmOut&, double, size_t, cudaStream_t);
-template void launch_reduce<float>(const Shape&, const DevPtrs&, const AsmOut&, const RedOut<float>&, double,
-                                   cudaStream_t);
-template void launch_reduce<double>(const Shape&, const DevPtrs&, const AsmOut&, const RedOut<double>&, double,
-                                    cudaStream_t);
-template void launch_back_substitute<float>(const Shape&, const DevPtrs&, const float*, const float*, const double*,
+template void launch_back_substitute<float>(const Shape&, const DevPtrs&, const double*, const float*, const double*,
                                             double*, double*, const double*, double*, cudaStream_t);
 template void launch_back_substitute<double>(const Shape&, const DevPtrs&, const double*, const double*, const double*,
                                              double*, double*, const double*, double*, cudaStream_t);

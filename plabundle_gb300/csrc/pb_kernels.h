@@ -13,14 +13,17 @@ constexpr int kMaxAlpha = 8;  // trial step lengths evaluated per objective pass
 
 // Outputs of the assembly kernel (per-chunk partials) and per-track / per-observation data kept
 // for the back-substitution.
+// The partial sums are FP64 on both paths: FP32 products are accumulated in double precision so
+// that the cancellation between the direct and the Schur terms of the reduced blocks keeps its
+// accuracy.
 template <typename T>
 struct AsmOutT {
-    T* part_pair;     // pair partials * 36
-    T* part_cam;      // camera partials * (12 + ng*6*ni)
-    T* part_chunk;    // chunks * (nb*nb + 2*nb)
+    double* part_pair;     // pair partials * 36
+    double* part_cam;      // camera partials * (12 + ng*6*ni)
+    double* part_chunk;    // chunks * (nb*nb + 2*nb)
     double* part_cost;
     int* part_flags;  // bit 0: singular point system, bit 1: invalid projection
-    T* trk_data;      // processed tracks * kTrackRec
+    double* trk_data; // processed tracks * kTrackRec (FP64 point factor, q, rhs)
     T* obs_wn;        // processed observations: robust normal weight
 };
 
@@ -49,11 +52,10 @@ struct RedOut {
 
 template <typename T>
 void launch_assemble(const Shape& S, const DevPtrs& D, const AsmOut& O, double damping, size_t smem, cudaStream_t st);
-template <typename T>
-void launch_reduce(const Shape& S, const DevPtrs& D, const AsmOut& O, const RedOut<T>& R, double damping,
+void launch_reduce(const Shape& S, const DevPtrs& D, const AsmOut& O, const RedOut<double>& R, double damping,
                    cudaStream_t st);
 template <typename T>
-void launch_back_substitute(const Shape& S, const DevPtrs& D, const T* trk_data, const T* obs_wn, const double* step_c,
+void launch_back_substitute(const Shape& S, const DevPtrs& D, const double* trk_data, const T* obs_wn, const double* step_c,
                             double* step_p, double* part, const double* direct64, double* out, cudaStream_t st);
 template <typename T>
 void launch_linearize_export(const Shape& S, const DevPtrs& D, double* res, double* jp, double* jpose, double* ji,
@@ -101,6 +103,34 @@ int pcg_grid_size(int ncb);
 template <typename T>
 void residual64(const PcgSystem<T>& sys, const double* b64, const double* x64, double* r64, double* out,
                 cudaStream_t st);
+// Dense Cholesky preconditioner + FP64 CG (pb_dense.cu).  A holds the scaled matrix, then its
+// factor L, then X^T; X holds L^-1; Dinv the inverses of the diagonal tiles of L.
+template <typename T>
+struct DenseWork {
+    int n = 0, np = 0, nt = 0, nnzb = 0;
+    T* A = nullptr;
+    T* X = nullptr;
+    T* Dinv = nullptr;
+    double* dscale = nullptr;
+    int* status = nullptr;
+    double *x = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr, *w = nullptr;
+    double* part = nullptr;
+    double* scal = nullptr;
+};
+
+template <typename T>
+size_t dense_bytes(int n);
+// Returns 0 on success, a status bitmask when the scaled matrix is not positive definite at this
+// shift (bit 1: non-positive diagonal, bit 2: non-positive pivot), -1 on a CUDA error.
+template <typename T>
+int dense_factor(const PcgSystem<double>& sys, DenseWork<T>& W, double shift, cudaStream_t st, int* launches);
+// CG on S x = b (FP64 S and vectors); the solution is left in W.x.  Returns 0, 1 on breakdown,
+// -1 on a CUDA error.
+template <typename T>
+int dense_pcg(const PcgSystem<double>& sys, DenseWork<T>& W, const double* b, double rel_tol, double abs_tol,
+              int max_it, int* iterations, double* relres, bool* converged, double* h_scal, cudaStream_t st,
+              int* launches);
+
 void to_double(const float* in, double* out, int n, cudaStream_t st);
 void to_double(const double* in, double* out, int n, cudaStream_t st);
 void to_float(const double* in, float* out, int n, cudaStream_t st);

@@ -14,7 +14,9 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <type_traits>
 #include <limits>
 #include <memory>
 #include <new>
@@ -58,16 +60,11 @@ void check(cudaError_t e, const char* what) {
     if (e != cudaSuccess) throw CudaError(std::string(what) + ": " + cudaGetErrorString(e));
 }
 
+// Assembly outputs of one arithmetic type (chunk partials, per-track factors, robust weights).
 template <typename T>
 struct PrecisionBuffers {
     bool ready = false;
     AsmOut out{};
-    RedOut<T> red{};
-    PcgSystem<T> sys{};
-    T* x = nullptr;
-    T* work = nullptr;
-    T* bvec = nullptr;  // right-hand side handed to the PCG (refinement residual on the mixed path)
-    int pcg_grid = 1;
 };
 
 }  // namespace
@@ -86,6 +83,17 @@ struct pb_gpu_ctx {
     DevPtrs D[2]{};
     PrecisionBuffers<double> p64;
     PrecisionBuffers<float> p32;
+    // reduced system (FP64 on both paths) and its solvers
+    RedOut<double> red{};
+    PcgSystem<double> sys{};
+    double* pcg_x = nullptr;
+    double* pcg_work = nullptr;
+    int pcg_grid = 1;
+    DeviceArena darena;           // dense preconditioner buffers (depend on the reduced dimension only)
+    DenseWork<float> dw32;
+    DenseWork<double> dw64;
+    bool dense_ready[2] = {false, false};
+    int last_solver = 0;
     // shared FP64 buffers
     double* groups_init = nullptr;
     double* step_c = nullptr;
@@ -173,6 +181,8 @@ void upload_structure(pb_gpu_ctx* c) {
     S.n = 6 * m.ncb + S.nb;
     S.nupper = static_cast<int>(m.up_row.size());
     S.nnzb = static_cast<int>(m.col_idx.size());
+    S.loss = m.loss;
+    S.loss_scale = m.loss_scale;
     S.gauge_anchor = m.gauge_anchor;
     S.gauge_scale = m.gauge_scale;
     S.gauge_baseline = m.gauge_baseline;
@@ -260,7 +270,6 @@ void upload_structure(pb_gpu_ctx* c) {
     const int n = S.n;
     c->step_c = A.alloc<double>(n);
     c->step_p = A.alloc<double>(static_cast<size_t>(ntp) * 3);
-    c->direct64 = A.alloc<double>(n);
     c->rhs64 = A.alloc<double>(n);
     c->x64 = A.alloc<double>(n);
     c->r64 = A.alloc<double>(n);
@@ -276,6 +285,33 @@ void upload_structure(pb_gpu_ctx* c) {
     c->pre_status = A.alloc<int>(1);
     c->rms_before_d = A.alloc<double>(nt);
     c->rms_after_d = A.alloc<double>(nt);
+    // reduced system (FP64) and the block-Jacobi PCG buffers
+    c->red.vals = A.alloc<double>(static_cast<size_t>(std::max(1, S.nnzb)) * 36);
+    c->red.border = A.alloc<double>(static_cast<size_t>(std::max(1, S.ncb)) * 6 * std::max(1, S.nb));
+    c->red.Cm = A.alloc<double>(static_cast<size_t>(std::max(1, S.nb * S.nb)));
+    c->red.rhs = A.alloc<double>(std::max(1, n));
+    c->red.direct = A.alloc<double>(std::max(1, n));
+    c->red.result = A.alloc<double>(2);
+    check(cudaMemsetAsync(c->red.vals, 0, static_cast<size_t>(std::max(1, S.nnzb)) * 36 * sizeof(double), st), "memset");
+    check(cudaMemsetAsync(c->red.border, 0, static_cast<size_t>(std::max(1, S.ncb)) * 6 * std::max(1, S.nb) * sizeof(double), st),
+          "memset");
+    c->direct64 = c->red.direct;
+    PcgSystem<double>& sy = c->sys;
+    sy.ncb = S.ncb;
+    sy.nb = S.nb;
+    sy.ng = S.ng;
+    sy.ni = S.ni;
+    sy.row_ptr = D.row_ptr;
+    sy.col_idx = D.col_idx;
+    sy.diag_pos = D.diag_pos;
+    sy.vals = c->red.vals;
+    sy.border = c->red.border;
+    sy.Cm = c->red.Cm;
+    sy.Dinv = A.alloc<double>(static_cast<size_t>(std::max(1, S.ncb)) * 36);
+    sy.Cinv = A.alloc<double>(static_cast<size_t>(std::max(1, S.ng)) * kMaxNI * kMaxNI);
+    c->pcg_x = A.alloc<double>(std::max(1, n));
+    c->pcg_work = A.alloc<double>(static_cast<size_t>(std::max(1, n)) * 4);
+    c->pcg_grid = pcg_grid_size<double>(S.ncb);
     c->S[0] = c->S[1] = S;
     c->D[0] = c->D[1] = D;
     // strict RMS before (input cameras, initial points)
@@ -322,38 +358,14 @@ void prepare_precision(pb_gpu_ctx* c, int precision) {
     D.cam_contrib = upload_new(A, cs.cam_contrib, st);
     D.obs_lcam = upload_new(A, cs.obs_lcam, st);
     const int camrec = 12 + S.ng * 6 * S.ni, chrec = S.nb * S.nb + 2 * S.nb;
-    B.out.part_pair_v = A.alloc<T>(cs.n_pair_partials() * 36);
-    B.out.part_cam_v = A.alloc<T>(cs.n_cam_partials() * camrec);
-    B.out.part_chunk_v = A.alloc<T>(static_cast<size_t>(std::max(1, S.nchunks)) * std::max(1, chrec));
+    // chunk partials are FP64 on both paths (the assembly accumulates in double precision)
+    B.out.part_pair_v = A.alloc<double>(cs.n_pair_partials() * 36);
+    B.out.part_cam_v = A.alloc<double>(cs.n_cam_partials() * camrec);
+    B.out.part_chunk_v = A.alloc<double>(static_cast<size_t>(std::max(1, S.nchunks)) * std::max(1, chrec));
     B.out.part_cost = A.alloc<double>(std::max(1, S.nchunks));
     B.out.part_flags = A.alloc<int>(std::max(1, S.nchunks));
-    B.out.trk_data_v = A.alloc<T>(static_cast<size_t>(S.ntp) * kTrackRec);
+    B.out.trk_data_v = A.alloc<double>(static_cast<size_t>(S.ntp) * kTrackRec);
     B.out.obs_wn_v = A.alloc<T>(static_cast<size_t>(S.nop));
-    B.red.vals = A.alloc<T>(static_cast<size_t>(S.nnzb) * 36);
-    B.red.border = A.alloc<T>(static_cast<size_t>(S.ncb) * 6 * std::max(1, S.nb));
-    B.red.Cm = A.alloc<T>(static_cast<size_t>(std::max(1, S.nb * S.nb)));
-    B.red.rhs = A.alloc<T>(S.n);
-    B.red.direct = A.alloc<T>(S.n);
-    B.red.result = A.alloc<double>(2);
-    check(cudaMemsetAsync(B.red.vals, 0, static_cast<size_t>(std::max(1, S.nnzb)) * 36 * sizeof(T), st), "memset");
-    check(cudaMemsetAsync(B.red.border, 0, static_cast<size_t>(std::max(1, S.ncb)) * 6 * std::max(1, S.nb) * sizeof(T), st),
-          "memset");
-    B.sys.ncb = S.ncb;
-    B.sys.nb = S.nb;
-    B.sys.ng = S.ng;
-    B.sys.ni = S.ni;
-    B.sys.row_ptr = D.row_ptr;
-    B.sys.col_idx = D.col_idx;
-    B.sys.diag_pos = D.diag_pos;
-    B.sys.vals = B.red.vals;
-    B.sys.border = B.red.border;
-    B.sys.Cm = B.red.Cm;
-    B.sys.Dinv = A.alloc<T>(static_cast<size_t>(std::max(1, S.ncb)) * 36);
-    B.sys.Cinv = A.alloc<T>(static_cast<size_t>(std::max(1, S.ng)) * kMaxNI * kMaxNI);
-    B.x = A.alloc<T>(S.n);
-    B.work = A.alloc<T>(static_cast<size_t>(S.n) * 4);
-    B.bvec = A.alloc<T>(S.n);
-    B.pcg_grid = pcg_grid_size<T>(S.ncb);
     c->pcg_part = nullptr;
     const size_t smem = chunk_smem_bytes(precision, S.max_obs, S.max_cams, S.max_pairs, S.ng, S.ni);
     // opt in to the large shared-memory carve-out for the assembly kernel
@@ -364,8 +376,7 @@ void prepare_precision(pb_gpu_ctx* c, int precision) {
 
 void ensure_pcg_partials(pb_gpu_ctx* c) {
     if (c->pcg_part) return;
-    const int grid = std::max(c->p64.ready ? c->p64.pcg_grid : 1, c->p32.ready ? c->p32.pcg_grid : 1);
-    c->pcg_part = c->arena.alloc<double>(static_cast<size_t>(2 * std::max(grid, 160)) * (2 + kMaxNB));
+    c->pcg_part = c->arena.alloc<double>(static_cast<size_t>(2 * std::max(c->pcg_grid, 160)) * (2 + kMaxNB));
 }
 
 void set_assemble_smem(int precision, size_t bytes);
@@ -402,13 +413,11 @@ void assemble(pb_gpu_ctx* c, double damping, int precision, double* cost, int* f
     }
     {
         Timer t(c, 3);
-        launch_reduce<T>(S, D, B.out, B.red, damping, c->stream);
+        launch_reduce(S, D, B.out, c->red, damping, c->stream);
         c->launches += 4;
     }
-    to_double(B.red.direct, c->direct64, S.n, c->stream);
-    c->launches += 1;
     check(cudaGetLastError(), "assemble launch");
-    check(cudaMemcpyAsync(c->h_scratch, B.red.result, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "D2H");
+    check(cudaMemcpyAsync(c->h_scratch, c->red.result, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "D2H");
     check(cudaStreamSynchronize(c->stream), "assemble");
     *cost = c->h_scratch[0];
     *flags = static_cast<int>(c->h_scratch[1]);
@@ -416,92 +425,115 @@ void assemble(pb_gpu_ctx* c, double damping, int precision, double* cost, int* f
     c->have_system = true;
 }
 
-// Reduced solve.  Returns 0 ok, 1 breakdown / not positive definite, and sets converged/iterations.
+// Reduced solve.  Returns 0 ok, 1 breakdown / not positive definite (retried by the LM driver
+// with more damping, as the reference does for "breakdown" / "positive definite" failures,
+// BundleAdjustPlaMatrix.cpp:34-40, :359-369).
 template <typename T>
-int solve_reduced_t(pb_gpu_ctx* c, const pb_solve_options& op, bool* converged, int* iterations, double* relres,
-                    int* sweeps) {
-    const int precision = c->last_precision;
-    PrecisionBuffers<T>& B = pbuf<T>(c);
-    const Shape& S = c->S[precision];
+DenseWork<T>& dwork(pb_gpu_ctx* c);
+template <>
+DenseWork<float>& dwork<float>(pb_gpu_ctx* c) { return c->dw32; }
+template <>
+DenseWork<double>& dwork<double>(pb_gpu_ctx* c) { return c->dw64; }
+
+template <typename T>
+void ensure_dense(pb_gpu_ctx* c) {
+    const int idx = std::is_same<T, float>::value ? 1 : 0;
+    if (c->dense_ready[idx]) return;
+    DenseWork<T>& W = dwork<T>(c);
+    const Shape& S = c->S[0];
+    DeviceArena& A = c->darena;
+    W.n = S.n;
+    W.nt = std::max(1, (S.n + 63) / 64);
+    W.np = W.nt * 64;
+    W.nnzb = S.nnzb;
+    W.A = A.alloc<T>(static_cast<size_t>(W.np) * W.np);
+    W.X = A.alloc<T>(static_cast<size_t>(W.np) * W.np);
+    W.Dinv = A.alloc<T>(static_cast<size_t>(W.nt) * 64 * 64);
+    W.dscale = A.alloc<double>(W.n);
+    W.status = A.alloc<int>(1);
+    W.x = A.alloc<double>(W.n);
+    W.r = A.alloc<double>(W.n);
+    W.z = A.alloc<double>(W.n);
+    W.p = A.alloc<double>(W.n);
+    W.q = A.alloc<double>(W.n);
+    W.w = A.alloc<double>(W.n);
+    const int nrow_blk = std::max(1, (S.ncb + 7) / 8);
+    W.part = A.alloc<double>(static_cast<size_t>(nrow_blk) * (1 + kMaxNB) + (W.n + 255) / 256 + (W.n + 7) / 8 + 8);
+    W.scal = A.alloc<double>(8);
+    c->dense_ready[idx] = true;
+}
+
+template <typename T>
+int solve_dense(pb_gpu_ctx* c, double rel, double abs_tol, int max_it, bool* converged, int* iterations,
+                double* relres) {
+    ensure_dense<T>(c);
+    DenseWork<T>& W = dwork<T>(c);
+    // FP32 factor of the Jacobi-scaled matrix with a small shift (kept positive definite in FP32);
+    // FP64 factor unshifted.  A failed factorisation is retried with a larger shift.
+    double shift = std::is_same<T, float>::value ? 1e-5 : 0.0;
+    int st = 0;
+    for (int attempt = 0; attempt < 4; ++attempt) {
+        st = dense_factor<T>(c->sys, W, shift, c->stream, &c->launches);
+        if (st < 0) throw CudaError(std::string("dense factorisation failed: ") + cudaGetErrorString(cudaGetLastError()));
+        if (st == 0 || (st & 1)) break;
+        shift = shift == 0.0 ? 1e-9 : shift * 100.0;
+    }
+    if (st) return 1;
+    const int rc = dense_pcg<T>(c->sys, W, c->red.rhs, rel, abs_tol, max_it, iterations, relres, converged,
+                                c->h_scratch + 40, c->stream, &c->launches);
+    if (rc < 0) throw CudaError(std::string("dense CG failed: ") + cudaGetErrorString(cudaGetLastError()));
+    if (rc) return 1;
+    check(cudaMemcpyAsync(c->step_c, W.x, c->S[0].n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream), "D2D");
+    return 0;
+}
+
+int solve_block_jacobi(pb_gpu_ctx* c, double rel, double abs_tol, int max_it, bool* converged, int* iterations,
+                       double* relres) {
     ensure_pcg_partials(c);
     cudaStream_t st = c->stream;
     check(cudaMemsetAsync(c->pre_status, 0, sizeof(int), st), "memset");
-    pcg_precondition<T>(B.sys, c->pre_status, st);
-    c->launches += 1;
-    const double rel = op.linear_relative_tolerance > 0 ? op.linear_relative_tolerance : 2.0e-10;
-    const double abs_tol = op.linear_absolute_tolerance > 0 ? op.linear_absolute_tolerance : 1.0e-12;
-    const int P = c->model.P;
-    const int max_it = op.max_linear_iterations > 0 ? op.max_linear_iterations : std::max(200, 30 * P);
-    *iterations = 0;
-    *sweeps = 0;
-    *converged = false;
+    pcg_precondition<double>(c->sys, c->pre_status, st);
+    if (pcg_solve<double>(c->sys, c->red.rhs, c->pcg_x, c->pcg_work, c->pcg_part, c->pcg_res, abs_tol, rel, max_it,
+                          c->pcg_grid, st))
+        throw CudaError(std::string("PCG launch failed: ") + cudaGetErrorString(cudaGetLastError()));
+    c->launches += 2;
     PcgResult res{};
-    if (precision == PB_PRECISION_FP64) {
-        {
-            Timer t(c, 1);
-            if (pcg_solve<T>(B.sys, B.red.rhs, B.x, B.work, c->pcg_part, c->pcg_res, abs_tol, rel, max_it, B.pcg_grid, st))
-                throw CudaError(std::string("PCG launch failed: ") + cudaGetErrorString(cudaGetLastError()));
-            c->launches += 1;
-        }
-        check(cudaMemcpyAsync(c->h_scratch, c->pre_status, sizeof(int), cudaMemcpyDeviceToHost, st), "D2H");
-        check(cudaMemcpyAsync(c->h_scratch + 1, c->pcg_res, sizeof(PcgResult), cudaMemcpyDeviceToHost, st), "D2H");
-        check(cudaStreamSynchronize(st), "pcg");
-        int pre;
-        std::memcpy(&pre, c->h_scratch, sizeof(int));
-        std::memcpy(&res, c->h_scratch + 1, sizeof(PcgResult));
-        if (pre || res.status) return 1;
-        to_double(B.x, c->step_c, S.n, st);
-        c->launches += 1;
-        *converged = res.converged != 0;
-        *iterations = res.iterations;
-        *relres = res.bnorm > 0 ? res.rnorm / res.bnorm : 0.0;
-        return 0;
-    }
-    // mixed: FP32 PCG corrections against an FP64-accumulated residual of the stored system
-    const int max_sweeps = std::min(3, std::max(1, op.refinement_sweeps));
-    to_double(B.red.rhs, c->rhs64, S.n, st);
-    check(cudaMemsetAsync(c->x64, 0, S.n * sizeof(double), st), "memset");
-    c->launches += 1;
-    for (int sweep = 0;; ++sweep) {
-        residual64<T>(B.sys, c->rhs64, c->x64, c->r64, c->res_out, st);
-        c->launches += 2;
-        check(cudaMemcpyAsync(c->h_scratch, c->res_out, 2 * sizeof(double), cudaMemcpyDeviceToHost, st), "D2H");
-        check(cudaStreamSynchronize(st), "residual");
-        const double rn = c->h_scratch[0], bn = c->h_scratch[1];
-        *relres = bn > 0 ? rn / bn : 0.0;
-        if (!std::isfinite(rn)) return 1;
-        if (rn <= std::max(rel * bn, abs_tol)) {
-            *converged = true;
-            break;
-        }
-        if (sweep > max_sweeps) break;
-        to_float(c->r64, reinterpret_cast<float*>(B.bvec), S.n, st);
-        {
-            Timer t(c, 1);
-            if (pcg_solve<T>(B.sys, B.bvec, B.x, B.work, c->pcg_part, c->pcg_res, 0.0, 1.0e-5, max_it, B.pcg_grid, st))
-                throw CudaError(std::string("PCG launch failed: ") + cudaGetErrorString(cudaGetLastError()));
-            c->launches += 2;
-        }
-        check(cudaMemcpyAsync(c->h_scratch, c->pre_status, sizeof(int), cudaMemcpyDeviceToHost, st), "D2H");
-        check(cudaMemcpyAsync(c->h_scratch + 1, c->pcg_res, sizeof(PcgResult), cudaMemcpyDeviceToHost, st), "D2H");
-        check(cudaStreamSynchronize(st), "pcg");
-        int pre;
-        std::memcpy(&pre, c->h_scratch, sizeof(int));
-        std::memcpy(&res, c->h_scratch + 1, sizeof(PcgResult));
-        if (pre || res.status) return 1;
-        *iterations += res.iterations;
-        axpy64(c->x64, reinterpret_cast<const float*>(B.x), S.n, st);
-        c->launches += 1;
-        *sweeps = sweep + 1;
-    }
-    check(cudaMemcpyAsync(c->step_c, c->x64, S.n * sizeof(double), cudaMemcpyDeviceToDevice, st), "D2D");
+    int pre = 0;
+    check(cudaMemcpyAsync(c->h_scratch, c->pre_status, sizeof(int), cudaMemcpyDeviceToHost, st), "D2H");
+    check(cudaMemcpyAsync(c->h_scratch + 1, c->pcg_res, sizeof(PcgResult), cudaMemcpyDeviceToHost, st), "D2H");
+    check(cudaStreamSynchronize(st), "pcg");
+    std::memcpy(&pre, c->h_scratch, sizeof(int));
+    std::memcpy(&res, c->h_scratch + 1, sizeof(PcgResult));
+    if (pre || res.status) return 1;
+    check(cudaMemcpyAsync(c->step_c, c->pcg_x, c->S[0].n * sizeof(double), cudaMemcpyDeviceToDevice, st), "D2D");
+    *converged = res.converged != 0;
+    *iterations = res.iterations;
+    *relres = res.bnorm > 0 ? res.rnorm / res.bnorm : 0.0;
     return 0;
 }
 
 int solve_reduced(pb_gpu_ctx* c, const pb_solve_options& op, bool* converged, int* iterations, double* relres,
                   int* sweeps) {
-    return c->last_precision == PB_PRECISION_FP64 ? solve_reduced_t<double>(c, op, converged, iterations, relres, sweeps)
-                                                  : solve_reduced_t<float>(c, op, converged, iterations, relres, sweeps);
+    const double rel = op.linear_relative_tolerance > 0 ? op.linear_relative_tolerance : 2.0e-10;
+    const double abs_tol = op.linear_absolute_tolerance > 0 ? op.linear_absolute_tolerance : 1.0e-12;
+    const int max_it = op.max_linear_iterations > 0 ? op.max_linear_iterations : std::max(200, 30 * c->model.P);
+    const int solver = (op.linear_solver == 1 || op.linear_solver == 2) ? op.linear_solver : (c->S[0].n <= 16384 ? 1 : 2);
+    c->last_solver = solver;
+    *converged = false;
+    *iterations = 0;
+    *sweeps = 0;
+    *relres = 0.0;
+    Timer t(c, 1);
+    int rc;
+    if (solver == 2) {
+        rc = solve_block_jacobi(c, rel, abs_tol, max_it, converged, iterations, relres);
+    } else if (c->last_precision == PB_PRECISION_MIXED) {
+        rc = solve_dense<float>(c, rel, abs_tol, max_it, converged, iterations, relres);
+        *sweeps = *iterations;  // FP64-residual corrections of the FP32 factor
+    } else {
+        rc = solve_dense<double>(c, rel, abs_tol, max_it, converged, iterations, relres);
+    }
+    return rc;
 }
 
 void back_substitute(pb_gpu_ctx* c, double* dd, double* point_sq, double* cam_sq) {
@@ -513,7 +545,7 @@ void back_substitute(pb_gpu_ctx* c, double* dd, double* point_sq, double* cam_sq
                                        static_cast<const double*>(c->p64.out.obs_wn_v), c->step_c, c->step_p,
                                        c->bs_part, c->direct64, c->bs_out, c->stream);
     else
-        launch_back_substitute<float>(S, D, static_cast<const float*>(c->p32.out.trk_data_v),
+        launch_back_substitute<float>(S, D, static_cast<const double*>(c->p32.out.trk_data_v),
                                       static_cast<const float*>(c->p32.out.obs_wn_v), c->step_c, c->step_p, c->bs_part,
                                       c->direct64, c->bs_out, c->stream);
     c->launches += 2;
@@ -624,12 +656,23 @@ void lm_solve(pb_gpu_ctx* c, const pb_solve_options& op, pb_solve_report* rep) {
     rep->intrinsic_blocks = m.ng;
     rep->pattern_builds = c->pattern_builds;
     rep->pattern_reuses = c->pattern_reuses;
+    if (!(op.robust_loss >= 0 && op.robust_loss <= 2 && std::isfinite(op.robust_loss_scale) && op.robust_loss_scale > 0)) {
+        rep->status = PB_SOLVE_INVALID_INPUT;
+        c->error = "invalid image robust loss";
+        return;
+    }
+    for (int p = 0; p < 2; ++p) {
+        c->S[p].loss = op.robust_loss;
+        c->S[p].loss_scale = op.robust_loss_scale;
+    }
     reset_state(c);
     if (m.obs_count == 0) {
         rep->status = PB_SOLVE_INVALID_INPUT;
         return;
     }
     const int precision = op.precision == PB_PRECISION_MIXED ? PB_PRECISION_MIXED : PB_PRECISION_FP64;
+    // Opt-in per-iteration trace on stderr (PB_GPU_TRACE=1), one line per linear solve.
+    const bool trace = std::getenv("PB_GPU_TRACE") != nullptr;
     double current = kNaN, damping = 0.0;
     int iterations = 0;
     bool converged = m.P == 0 && m.ntb == 0;
@@ -729,6 +772,13 @@ void lm_solve(pb_gpu_ctx* c, const pb_solve_options& op, pb_solve_report* rep) {
                     k0 += nbatch;
                 }
                 t_obj += ms(tc, now());
+                if (trace)
+                    std::fprintf(stderr,
+                                 "PB_GPU_TRACE it=%d precision=%d cost=%.15e lambda=%.3e lin_it=%d sweeps=%d "
+                                 "relres=%.3e dd=%.6e rms_global=%.3e rms_point=%.3e alpha=%.6g cand=%.15e "
+                                 "accepted=%d\n",
+                                 iterations, precision, current, damping, lit, sweeps, relres, dd, rg, rp,
+                                 accepted_slot >= 0 ? accepted_alpha : alpha, cand, accepted_slot >= 0 ? 1 : 0);
                 if (accepted_slot >= 0) {
                     launch_accept(c->S[0], c->D[0], c->step_p, accepted_alpha, accepted_slot, c->stream);
                     c->launches += 1;
@@ -837,6 +887,7 @@ pb_status pb_gpu_destroy(pb_gpu_ctx* c) {
     c->arena.release();
     c->parena[0].release();
     c->parena[1].release();
+    c->darena.release();
     if (c->h_scratch) cudaFreeHost(c->h_scratch);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
@@ -882,9 +933,8 @@ pb_status pb_gpu_upload(pb_gpu_ctx* c, const pb_problem_desc* pr, const pb_solve
             };
             keep_chunks(c->D[0], d0, c->S[0], s0);
             keep_chunks(c->D[1], d1, c->S[1], s1);
-            // the per-precision system descriptors point at structure buffers that were re-uploaded
-            if (r64) { c->p64.sys.row_ptr = c->D[0].row_ptr; c->p64.sys.col_idx = c->D[0].col_idx; c->p64.sys.diag_pos = c->D[0].diag_pos; }
-            if (r32) { c->p32.sys.row_ptr = c->D[1].row_ptr; c->p32.sys.col_idx = c->D[1].col_idx; c->p32.sys.diag_pos = c->D[1].diag_pos; }
+            (void)r64;
+            (void)r32;
             ++c->pattern_reuses;
         } else {
             c->arena.release();
@@ -892,6 +942,8 @@ pb_status pb_gpu_upload(pb_gpu_ctx* c, const pb_problem_desc* pr, const pb_solve
             c->parena[1].release();
             c->p64 = PrecisionBuffers<double>{};
             c->p32 = PrecisionBuffers<float>{};
+            c->darena.release();
+            c->dense_ready[0] = c->dense_ready[1] = false;
             c->pcg_part = nullptr;
             c->model = std::move(m);
             upload_structure(c);
@@ -1022,17 +1074,16 @@ pb_status pb_gpu_get_reduced(pb_gpu_ctx* c, double* dense, double* rhs, double* 
     if (!c || !c->uploaded || !c->have_system) return fail(c, PB_ERR_STATE, "no reduced system assembled");
     try {
         const HostModel& m = c->model;
-        const int prec = c->last_precision;
-        const Shape& S = c->S[prec];
+        const Shape& S = c->S[0];
         const int n = S.n, nb = S.nb, n6 = 6 * S.ncb;
-        const size_t ts = prec == PB_PRECISION_FP64 ? 8 : 4;
+        const size_t ts = 8;
         std::vector<char> vals(static_cast<size_t>(std::max(1, S.nnzb)) * 36 * ts), border(static_cast<size_t>(std::max(1, S.ncb)) * 6 * std::max(1, nb) * ts),
             Cm(static_cast<size_t>(std::max(1, nb * nb)) * ts), r(n * ts), d(n * ts);
-        const void* src_vals = prec == PB_PRECISION_FP64 ? static_cast<const void*>(c->p64.red.vals) : c->p32.red.vals;
-        const void* src_border = prec == PB_PRECISION_FP64 ? static_cast<const void*>(c->p64.red.border) : c->p32.red.border;
-        const void* src_C = prec == PB_PRECISION_FP64 ? static_cast<const void*>(c->p64.red.Cm) : c->p32.red.Cm;
-        const void* src_r = prec == PB_PRECISION_FP64 ? static_cast<const void*>(c->p64.red.rhs) : c->p32.red.rhs;
-        const void* src_d = prec == PB_PRECISION_FP64 ? static_cast<const void*>(c->p64.red.direct) : c->p32.red.direct;
+        const void* src_vals = c->red.vals;
+        const void* src_border = c->red.border;
+        const void* src_C = c->red.Cm;
+        const void* src_r = c->red.rhs;
+        const void* src_d = c->red.direct;
         check(cudaMemcpy(vals.data(), src_vals, static_cast<size_t>(S.nnzb) * 36 * ts, cudaMemcpyDeviceToHost), "D2H");
         if (nb) {
             check(cudaMemcpy(border.data(), src_border, static_cast<size_t>(S.ncb) * 6 * nb * ts, cudaMemcpyDeviceToHost), "D2H");

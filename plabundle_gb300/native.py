@@ -47,7 +47,8 @@ class SolveOptionsC(C.Structure):
                 ("gauge_baseline", C.c_double), ("intrinsic_mask", C.c_uint32), ("precision", C.c_int32),
                 ("max_linear_iterations", C.c_int32), ("linear_relative_tolerance", C.c_double),
                 ("linear_absolute_tolerance", C.c_double), ("refinement_sweeps", C.c_int32),
-                ("preconditioner_cluster_size", C.c_int32), ("calibration", C.c_double * 32)]
+                ("preconditioner_cluster_size", C.c_int32), ("linear_solver", C.c_int32),
+                ("calibration", C.c_double * 32)]
 
 
 class SolveReportC(C.Structure):
@@ -163,6 +164,7 @@ def solve_options(options, problem=None) -> SolveOptionsC:
     o.linear_absolute_tolerance = 1.0e-12
     o.refinement_sweeps = b.refinementSweeps
     o.preconditioner_cluster_size = b.plaMatrixPreconditionerClusterSize
+    o.linear_solver = int(b.linearSolver)
     for i, v in enumerate(cal.numeric_block()):
         o.calibration[i] = v
     return o

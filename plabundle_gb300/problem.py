@@ -293,6 +293,7 @@ class BackendOptions:
     minPlaMatrixCudaDenseObservations: int = 150000
     refinementSweeps: int = 3
     maxLinearIterations: int = 0
+    linearSolver: int = 0   # 0 auto, 1 dense-Cholesky-preconditioned CG, 2 block-Jacobi PCG
 
 
 @dataclass
