@@ -189,40 +189,109 @@ __device__ __forceinline__ bool linearize_obs(const DCam& c, double X0, double X
     return true;
 }
 
+// Float-float numbers (hi + lo, |lo| <= ulp(hi)/2) for the compensated FP32 arithmetic of the
+// mixed path: products use the exact FMA residual (Dekker / Ogita-Rump-Oishi "TwoProduct"),
+// sums the Knuth "TwoSum"; about 44 significant bits, all on the FP32 pipe.
+struct ff {
+    float hi, lo;
+};
+
+__device__ __forceinline__ ff ff_make(double d) {
+    const float h = static_cast<float>(d);
+    return {h, static_cast<float>(d - static_cast<double>(h))};
+}
+// __fmul_rn / __fadd_rn are never contracted into an FMA, which the error-free transformations
+// below depend on.
+__device__ __forceinline__ ff ff_norm(float s, float e) {
+    const float h = __fadd_rn(s, e);
+    return {h, __fadd_rn(e, -__fadd_rn(h, -s))};
+}
+__device__ __forceinline__ ff operator*(ff a, ff b) {
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = fmaf(a.hi, b.hi, -p);
+    e = fmaf(a.hi, b.lo, e);
+    e = fmaf(a.lo, b.hi, e);
+    return ff_norm(p, e);
+}
+__device__ __forceinline__ ff operator*(float a, ff b) {
+    const float p = __fmul_rn(a, b.hi);
+    float e = fmaf(a, b.hi, -p);
+    e = fmaf(a, b.lo, e);
+    return ff_norm(p, e);
+}
+__device__ __forceinline__ ff operator+(ff a, ff b) {
+    const float s = __fadd_rn(a.hi, b.hi);
+    const float bp = __fadd_rn(s, -a.hi);
+    const float e = __fadd_rn(__fadd_rn(a.hi, -__fadd_rn(s, -bp)), __fadd_rn(b.hi, -bp)) + (a.lo + b.lo);
+    return ff_norm(s, e);
+}
+__device__ __forceinline__ ff operator-(ff a) { return {-a.hi, -a.lo}; }
+
+// Value type of the reduced-system terms: float-float on the FP32 path, double on the FP64 path.
+template <typename T>
+struct ValueOf;
+template <>
+struct ValueOf<float> {
+    using type = ff;
+    __device__ static __forceinline__ ff make(double d) { return ff_make(d); }
+    __device__ static __forceinline__ ff zero() { return {0.f, 0.f}; }
+};
+template <>
+struct ValueOf<double> {
+    using type = double;
+    __device__ static __forceinline__ double make(double d) { return d; }
+    __device__ static __forceinline__ double zero() { return 0.0; }
+};
+
 // Two-sum compensated accumulator (FP32 path) / plain FP64 accumulator.
 template <typename T>
 struct Acc;
 
 template <>
 struct Acc<double> {
+    using part_type = double;  // partial sums written by the assembly
     double s = 0.0;
     __device__ __forceinline__ void add(double v) { s += v; }
     __device__ __forceinline__ void add_prod(double a, double b) { s = fma(a, b, s); }
     __device__ __forceinline__ double value() const { return s; }
+    __device__ __forceinline__ double value64() const { return s; }
     __device__ __forceinline__ void merge(const Acc<double>& o) { s += o.s; }
+    __device__ __forceinline__ void merge_part(double v) { s += v; }
+    __device__ __forceinline__ double part() const { return s; }
 };
 
 template <>
 struct Acc<float> {
     float hi = 0.f, lo = 0.f;
     __device__ __forceinline__ void add(float v) {
-        const float s = hi + v;
-        const float bp = s - hi;
-        const float e = (hi - (s - bp)) + (v - bp);
+        const float s = __fadd_rn(hi, v);
+        const float bp = __fadd_rn(s, -hi);
+        const float e = __fadd_rn(__fadd_rn(hi, -__fadd_rn(s, -bp)), __fadd_rn(v, -bp));
         hi = s;
         lo += e;
     }
     __device__ __forceinline__ void add_prod(float a, float b) {
-        const float p = a * b;
+        const float p = __fmul_rn(a, b);
         const float pe = fmaf(a, b, -p);
         add(p);
         lo += pe;
     }
     __device__ __forceinline__ float value() const { return hi + lo; }
+    __device__ __forceinline__ double value64() const { return static_cast<double>(hi) + static_cast<double>(lo); }
     __device__ __forceinline__ void merge(const Acc<float>& o) {
         add(o.hi);
         lo += o.lo;
     }
+    __device__ __forceinline__ void add(ff v) {
+        add(v.hi);
+        lo += v.lo;
+    }
+    using part_type = float2;  // (hi, lo) pair: the partial keeps the compensation term
+    __device__ __forceinline__ void merge_part(float2 v) {
+        add(v.x);
+        lo += v.y;
+    }
+    __device__ __forceinline__ float2 part() const { return make_float2(hi, lo); }
 };
 
 __device__ __forceinline__ double warp_sum(double v) {

@@ -409,35 +409,35 @@ int build_host_model(const pb_problem_desc* pr, const pb_solve_options* op, Host
     return 0;
 }
 
-size_t chunk_smem_bytes(int precision, int max_obs, int max_cams, int max_pairs, int ng, int ni) {
-    const size_t ts = precision == PB_PRECISION_FP64 ? 8 : 4;
-    const size_t nb = static_cast<size_t>(ng) * ni;
+size_t chunk_smem_bytes(int precision, int max_obs, int ni) {
+    const size_t ts = precision == PB_PRECISION_FP64 ? 8 : 4;  // Jacobian storage
+    const size_t vs = 8;                                        // double / float-float values
+    const size_t nA = 6 + static_cast<size_t>(ni);
+    const size_t mo = static_cast<size_t>(max_obs);
     auto al = [](size_t v) { return (v + 15) & ~static_cast<size_t>(15); };
     size_t s = 0;
-    s += al(static_cast<size_t>(max_cams) * max_cams * 2);             // pair lookup
-    s += al(static_cast<size_t>(max_pairs) * 36 * 8);                  // pair accumulators (FP64)
-    s += al(static_cast<size_t>(max_cams) * 12 * 8);                   // rhs accumulators (FP64)
-    s += al(static_cast<size_t>(max_cams) * ng * 6 * ni * 8);          // border accumulators (FP64)
-    s += al((nb * nb + 2 * nb) * 8);                                   // intrinsic block + rhs (FP64)
-    const size_t per_obs = 18 + 3 * static_cast<size_t>(ni);
-    s += al(static_cast<size_t>(max_obs) * per_obs * ts);              // G_o
-    s += al(static_cast<size_t>(max_obs) * 9 * 8);                    // V_o, rhs_o (FP64)
-    s += al(static_cast<size_t>(max_obs) * 9 * 8);                    // track factor and q (FP64)
-    s += al(static_cast<size_t>(max_obs) * 4);                         // track start per obs
-    s += al(64 * 8);                                                   // warp partial costs, flags
+    s += al(mo * 9 * 8);       // point normal equations per observation, then the track factor (FP64)
+    s += al(mo * 2 * nA * ts); // A_o = [J_pose | J_intrinsic]
+    s += al(mo * 3 * nA * vs); // G_o = A_o^T Y_o
+    s += al(mo * 7 * vs);      // reduced weight M_o, reduced residual M r_o, w r_o
+    s += al(mo * 4) * 2;       // observation flags, track ranges
+    s += al(40 * 8);           // warp partial costs, flags
     return s;
 }
 
 int build_chunks(HostModel* m, int precision, size_t smem_budget, std::string* err) {
     ChunkSet& cs = m->chunks[precision];
-    int max_obs = precision == PB_PRECISION_FP64 ? 128 : 256;
-    int max_cams = precision == PB_PRECISION_FP64 ? 48 : 64;
-    int max_pairs = precision == PB_PRECISION_FP64 ? 256 : 320;
-    while (chunk_smem_bytes(precision, max_obs, max_cams, max_pairs, m->ng, m->ni) > smem_budget && max_pairs > 64) {
-        max_pairs -= 32;
-        if (max_cams > 32) max_cams -= 8;
-    }
-    if (chunk_smem_bytes(precision, max_obs, max_cams, max_pairs, m->ng, m->ni) > smem_budget) {
+    // A chunk is bounded by its observations (one thread each, shared-memory records); cameras
+    // are chunk-local 8-bit indices (255 marks an observation without a pose block) and pairs
+    // only size the partial buffers.
+    // two CTAs per SM: at most half of the 228 KB of shared memory of an SM each, less the
+    // 1 KB the runtime reserves per CTA
+    const size_t per_cta = std::min(smem_budget, static_cast<size_t>(113 * 1024));
+    int max_obs = 256;
+    const int max_cams = 254;
+    const int max_pairs = 1 << 15;
+    while (chunk_smem_bytes(precision, max_obs, m->ni) > per_cta && max_obs > 32) max_obs -= 32;
+    if (chunk_smem_bytes(precision, max_obs, m->ni) > per_cta) {
         *err = "assembly chunk does not fit in shared memory";
         return PB_SOLVE_UNSUPPORTED;
     }
@@ -453,7 +453,11 @@ int build_chunks(HostModel* m, int precision, size_t smem_budget, std::string* e
     std::vector<std::pair<int, int>> cpairs;
     int chunk = 0;
     int chunk_obs_start = 0;
+    int chunk_trk_start = 0;
+    std::vector<int> slot_of;                        // local pair (a, b) -> chunk slot
     cs.obs_begin.push_back(0);
+    cs.slot_item_begin.push_back(0);
+    cs.lcam_obs_begin.push_back(0);
     cs.cam_begin.push_back(0);
     cs.pair_begin.push_back(0);
     auto close_chunk = [&](int obs_end) {
@@ -476,9 +480,74 @@ int build_chunks(HostModel* m, int precision, size_t smem_budget, std::string* e
             rp.emplace_back(a, b);
         }
         std::sort(rp.begin(), rp.end());
-        for (auto& p : rp) {
-            cs.pairs.push_back(p.first | (p.second << 16));
+        const int ncl = static_cast<int>(ccams.size());
+        slot_of.assign(static_cast<size_t>(ncl) * ncl, -1);
+        for (size_t i = 0; i < rp.size(); ++i) {
+            cs.pairs.push_back(rp[i].first | (rp[i].second << 16));
             cs.pair_upper.push_back(-1);  // resolved once all chunks exist
+            slot_of[static_cast<size_t>(rp[i].first) * ncl + rp[i].second] = static_cast<int>(i);
+        }
+        // Items of every pair slot, in track order: the observation's own term (oa == ob) on the
+        // diagonal slot, and for eliminated tracks the coupling -G_oa G_ob^T of two observations
+        // with oa on the lower chunk camera (both orientations when they share a camera).
+        // Two passes over the chunk's tracks: count the items of every slot, then place them.
+        std::vector<int> cnt(rp.size() + 1, 0);
+        int p_end = chunk_trk_start;
+        while (p_end < static_cast<int>(m->trk_order.size()) && m->trk_obs_begin[p_end] < obs_end) ++p_end;
+        for (int pass = 0; pass < 2; ++pass) {
+            auto emit = [&](int a, int b, unsigned short item) {
+                const int sl = slot_of[static_cast<size_t>(a) * ncl + b];
+                if (pass == 0) ++cnt[sl + 1];
+                else cs.slot_items[cnt[sl]++] = item;
+            };
+            for (int p = chunk_trk_start; p < p_end; ++p) {
+                const int o0 = m->trk_obs_begin[p], o1 = m->trk_obs_begin[p + 1];
+                const bool el = m->track_block[m->trk_order[p]] >= 0;
+                for (int i = o0; i < o1; ++i) {
+                    const int li = cs.obs_lcam[i];
+                    if (li == 255) continue;
+                    const int ii = i - chunk_obs_start;
+                    emit(li, li, static_cast<unsigned short>(ii | (ii << 8)));
+                    if (!el) continue;
+                    for (int j = i + 1; j < o1; ++j) {
+                        const int lj = cs.obs_lcam[j];
+                        if (lj == 255) continue;
+                        const int jj = j - chunk_obs_start;
+                        if (li < lj) {
+                            emit(li, lj, static_cast<unsigned short>(ii | (jj << 8)));
+                        } else if (li > lj) {
+                            emit(lj, li, static_cast<unsigned short>(jj | (ii << 8)));
+                        } else {
+                            emit(li, li, static_cast<unsigned short>(ii | (jj << 8)));
+                            emit(li, li, static_cast<unsigned short>(jj | (ii << 8)));
+                        }
+                    }
+                }
+            }
+            if (pass == 0) {
+                const int base = static_cast<int>(cs.slot_items.size());
+                cnt[0] = base;
+                for (size_t i = 0; i < rp.size(); ++i) cnt[i + 1] += cnt[i];
+                cs.slot_items.resize(static_cast<size_t>(cnt[rp.size()]));
+                // cnt[i] is now the begin of slot i: the fill position of the second pass
+                for (size_t i = 0; i < rp.size(); ++i) cs.slot_item_begin.push_back(cnt[i + 1]);
+            }
+        }
+        chunk_trk_start = p_end;
+        // observations of every chunk camera, in observation order (counting sort)
+        {
+            std::vector<int> cc(static_cast<size_t>(ncl) + 1, 0);
+            for (int o = chunk_obs_start; o < obs_end; ++o)
+                if (cs.obs_lcam[o] != 255) ++cc[cs.obs_lcam[o] + 1];
+            const int base = static_cast<int>(cs.lcam_obs.size());
+            cc[0] = base;
+            for (int l = 0; l < ncl; ++l) {
+                cc[l + 1] += cc[l];
+                cs.lcam_obs_begin.push_back(cc[l + 1]);
+            }
+            cs.lcam_obs.resize(static_cast<size_t>(cc[ncl]));
+            for (int o = chunk_obs_start; o < obs_end; ++o)
+                if (cs.obs_lcam[o] != 255) cs.lcam_obs[cc[cs.obs_lcam[o]]++] = static_cast<unsigned char>(o - chunk_obs_start);
         }
         cs.obs_begin.push_back(obs_end);
         cs.cam_begin.push_back(static_cast<int>(cs.cams.size()));

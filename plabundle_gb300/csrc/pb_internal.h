@@ -70,6 +70,10 @@ struct DevPtrs {
     int* ch_cams;         // global camera indices
     int* ch_pair_begin;
     int* ch_pairs;        // li | lj << 16, li <= lj
+    int* slot_item_begin; // pair slots + 1: items of each chunk pair slot
+    unsigned short* slot_items;  // oa | ob << 8 (chunk-local observations); oa == ob: own term
+    int* lcam_obs_begin;  // chunk cameras + 1: observations of each chunk camera
+    unsigned char* lcam_obs;     // chunk-local observation indices
     // reduce lists
     int* up_contrib_begin;  // nupper + 1
     int* up_contrib;        // partial pair slots
@@ -101,6 +105,9 @@ struct ChunkSet {
     int max_obs = 0, max_cams = 0, max_pairs = 0;
     std::vector<int> obs_begin, cam_begin, cams, pair_begin, pairs, pair_upper;
     std::vector<unsigned char> obs_lcam;
+    std::vector<int> slot_item_begin, lcam_obs_begin;
+    std::vector<unsigned short> slot_items;
+    std::vector<unsigned char> lcam_obs;
     std::vector<int> up_contrib_begin, up_contrib, cam_contrib_begin, cam_contrib;
     size_t n_pair_partials() const { return pairs.size(); }
     size_t n_cam_partials() const { return cams.size(); }
@@ -142,7 +149,7 @@ struct HostModel {
 // pb_host.cpp
 int build_host_model(const pb_problem_desc* pr, const pb_solve_options* op, HostModel* m, std::string* err);
 int build_chunks(HostModel* m, int precision, size_t smem_budget, std::string* err);
-size_t chunk_smem_bytes(int precision, int max_obs, int max_cams, int max_pairs, int ng, int ni);
+size_t chunk_smem_bytes(int precision, int max_obs, int ni);
 double finite_median(std::vector<double> v, double fallback);
 void camera_parameter_block(const double* cam, double* p);
 

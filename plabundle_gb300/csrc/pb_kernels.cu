@@ -1,14 +1,19 @@
 // pb_kernels.cu -- assembly, reduction, back-substitution, objective and state-update kernels.
 //
-// Kernel (a)+(b) `k_assemble`: one CTA per chunk of consecutive tracks (host-built, bounded
-// observations / cameras / camera pairs).  One thread per observation linearises it; the
-// tracks' 3x3 point systems are reduced in shared memory, factored in FP64 (V = R R^T), and
-// every observation forms G_o = W_o R^-T so that the point Schur complement of a track is the
-// symmetric rank-3 update  S -= sum_(o,o') G_o G_o'^T  (online elimination of
-// BundleAdjustPlaMatrixReferenceSchur.cpp:350-490).  Contributions accumulate in shared memory
-// per (camera, camera) pair of the chunk and are written once per chunk as partial blocks;
-// `k_reduce_*` sum the partials per reduced block in a fixed order (two-sum compensated on the
-// FP32 path), so the reduced matrix is assembled without global atomics.
+// Kernels (a)+(b) `k_assemble`: one CTA per chunk of consecutive tracks (host-built, at most
+// max_obs observations), one thread per observation.
+//   A. linearise the observation (FP64 residual and robust weight, Jacobians in T);
+//   B. per track, the 3x3 point system V = sum w Jp^T Jp (FP64) and its factor V = R R^T;
+//   C. per observation, in FP64: Y = w Jp R^-T (2x3), the reduced weight M = w I - Y Y^T and the
+//      reduced residual M r = w r + Y q (q = R^-1 g_p); then G = A^T Y with A = [J_pose | J_intr]
+//      in T.  The point elimination of a track (BundleAdjustPlaMatrixReferenceSchur.cpp:350-490)
+//      is then  S_track = sum_o A_o^T M_o A_o - sum_(o != o') G_o G_o'^T,  so the cancellation
+//      between the direct and the Schur terms of an observation is done in FP64, once;
+//   D. every output element of the chunk (pose-pair entry, camera rhs / border entry, intrinsic
+//      block entry) is owned by one thread, which gathers its terms over host-built item lists
+//      in a fixed order into an Acc<T> (two-sum compensated on the FP32 path) and writes the
+//      chunk partial once.  No shared-memory or global atomics; results are deterministic.
+// `k_reduce_*` then sum the partials of each reduced block in a fixed order.
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
@@ -19,8 +24,6 @@ namespace pb {
 
 namespace {
 
-__device__ __forceinline__ void atomic_add_t(double* p, double v) { atomicAdd(p, v); }
-
 template <typename T>
 __device__ __forceinline__ T* carve(char*& ptr, size_t count) {
     T* out = reinterpret_cast<T*>(ptr);
@@ -28,61 +31,51 @@ __device__ __forceinline__ T* carve(char*& ptr, size_t count) {
     return out;
 }
 
+// observation flags in shared memory
+constexpr int kOk = 1, kElim = 2;
+__device__ __forceinline__ int info_group(int info) { return ((info >> 2) & 7) - 1; }
+
 }  // namespace
 
 template <typename T>
-__global__ void __launch_bounds__(256, 1) k_assemble(Shape S, DevPtrs D, AsmOutT<T> O, double damping) {
+__global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT<T> O, double damping) {
+    using P = typename Acc<T>::part_type;
+    using Val = ValueOf<T>;
+    using VT = typename Val::type;
     extern __shared__ __align__(16) char smem[];
     const int chunk = blockIdx.x;
     const int tid = threadIdx.x;
-    const int MC = S.max_cams, MP = S.max_pairs, MO = S.max_obs;
-    const int ng = S.ng, ni = S.ni, nb = S.nb;
-    const int per_obs = 18 + 3 * ni;
+    const int MO = S.max_obs;
+    const int ng = S.ng, ni = S.ni, nb = S.nb, nA = 6 + ni;
     char* ptr = smem;
-    unsigned short* s_lookup = carve<unsigned short>(ptr, static_cast<size_t>(MC) * MC);
-    double* s_pair = carve<double>(ptr, static_cast<size_t>(MP) * 36);
-    double* s_rhs = carve<double>(ptr, static_cast<size_t>(MC) * 12);
-    double* s_border = carve<double>(ptr, static_cast<size_t>(MC) * ng * 6 * ni);
-    double* s_C = carve<double>(ptr, static_cast<size_t>(nb) * nb + 2 * nb);
-    T* s_G = carve<T>(ptr, static_cast<size_t>(MO) * per_obs);
     double* s_V = carve<double>(ptr, static_cast<size_t>(MO) * 9);
-    double* s_trk = carve<double>(ptr, static_cast<size_t>(MO) * 9);
-    int* s_first = carve<int>(ptr, MO);
-    double* s_misc = carve<double>(ptr, 64);
-    int* s_flags = reinterpret_cast<int*>(s_misc + 40);
+    T* s_A = carve<T>(ptr, static_cast<size_t>(MO) * 2 * nA);
+    VT* s_G = carve<VT>(ptr, static_cast<size_t>(MO) * 3 * nA);
+    VT* s_M = carve<VT>(ptr, static_cast<size_t>(MO) * 7);
+    int* s_info = carve<int>(ptr, MO);
+    int* s_trk = carve<int>(ptr, MO);
+    double* s_misc = carve<double>(ptr, 40);
+    int* s_flags = reinterpret_cast<int*>(s_misc + 32);
 
     const int obs0 = D.ch_obs_begin[chunk], nobs = D.ch_obs_begin[chunk + 1] - obs0;
-    const int cam0 = D.ch_cam_begin[chunk], ncams = D.ch_cam_begin[chunk + 1] - cam0;
-    const int pair0 = D.ch_pair_begin[chunk], npairs = D.ch_pair_begin[chunk + 1] - pair0;
-
-    for (int i = tid; i < MC * MC; i += blockDim.x) s_lookup[i] = 0xFFFF;
-    for (int i = tid; i < npairs * 36; i += blockDim.x) s_pair[i] = 0.0;
-    for (int i = tid; i < ncams * 12; i += blockDim.x) s_rhs[i] = 0.0;
-    for (int i = tid; i < ncams * ng * 6 * ni; i += blockDim.x) s_border[i] = 0.0;
-    for (int i = tid; i < nb * nb + 2 * nb; i += blockDim.x) s_C[i] = 0.0;
     if (tid == 0) s_flags[0] = 0;
     __syncthreads();
-    for (int s = tid; s < npairs; s += blockDim.x) {
-        const int pk = D.ch_pairs[pair0 + s];
-        s_lookup[(pk & 0xFFFF) * MC + (pk >> 16)] = static_cast<unsigned short>(s);
-    }
 
-    // ---- phase 1: linearise one observation per thread; FP64 point normal equations
+    // ---- A: linearise one observation per thread; FP64 point normal equations
     const bool active = tid < nobs;
     const int o = obs0 + tid;
     Lin<T> L;
     double cost = 0.0;
-    int trk = 0, first = 0, k = 0, cam = 0, lcam = 255, grp = -1;
-    bool elim = false, ok = true;
+    int first = 0;
+    bool elim = false, ok = false;
     if (active) {
-        cam = D.obs_cam[o];
-        trk = D.obs_trk[o];
+        const int cam = D.obs_cam[o];
+        const int trk = D.obs_trk[o];
         const int tb0 = D.trk_obs_begin[trk];
         first = tb0 - obs0;
-        k = D.trk_obs_begin[trk + 1] - tb0;
+        const int k = D.trk_obs_begin[trk + 1] - tb0;
         elim = D.trk_block[trk] >= 0;
-        lcam = D.obs_lcam[o];
-        grp = D.cam_group[cam];
+        const int grp = ng > 0 ? D.cam_group[cam] : -1;
         DCam c;
         load_cam(D.cams_eff + static_cast<size_t>(cam) * kCamStride, c);
         const double* X = D.points + static_cast<size_t>(trk) * 3;
@@ -95,10 +88,20 @@ __global__ void __launch_bounds__(256, 1) k_assemble(Shape S, DevPtrs D, AsmOutT
             cost = L.cost;
             O.obs_wn[o] = L.w;
         }
-        s_first[tid] = first;
+        s_info[tid] = (ok ? kOk : 0) | (elim ? kElim : 0) | ((grp + 1) << 2);
+        s_trk[tid] = first | (k << 16);
+        T* A = s_A + static_cast<size_t>(tid) * 2 * nA;
+        for (int a = 0; a < 6; ++a) {
+            A[a] = ok ? L.Jc[a] : T(0);
+            A[nA + a] = ok ? L.Jc[6 + a] : T(0);
+        }
+        for (int a = 0; a < ni; ++a) {
+            A[6 + a] = ok ? L.Ji[a] : T(0);
+            A[nA + 6 + a] = ok ? L.Ji[kMaxNI + a] : T(0);
+        }
         double* V = s_V + static_cast<size_t>(tid) * 9;
         if (elim && ok) {
-            // V_o = w Jp^T Jp and rhs_o = -w Jp^T r from the (rounded) Jacobian, summed in FP64
+            // V_o = w Jp^T Jp and g_o = -w Jp^T r from the (rounded) Jacobian, in FP64
             const double w = L.wd;
             const double j0 = L.Jp[0], j1 = L.Jp[1], j2 = L.Jp[2], j3 = L.Jp[3], j4 = L.Jp[4], j5 = L.Jp[5];
             V[0] = w * (j0 * j0 + j3 * j3);
@@ -110,14 +113,16 @@ __global__ void __launch_bounds__(256, 1) k_assemble(Shape S, DevPtrs D, AsmOutT
             V[6] = -w * (j0 * L.rd0 + j3 * L.rd1);
             V[7] = -w * (j1 * L.rd0 + j4 * L.rd1);
             V[8] = -w * (j2 * L.rd0 + j5 * L.rd1);
-        } else if (elim) {
+        } else {
             for (int i = 0; i < 9; ++i) V[i] = 0.0;
         }
     }
     __syncthreads();
 
-    // ---- phase 2: per-track 3x3 point system, FP64 Cholesky V(1+lambda) = R R^T
+    // ---- B: per track, FP64 Cholesky V(1+lambda) = R R^T; R^-1 and q = R^-1 g_p replace the
+    // track's first record of s_V (only this thread reads the track's records in this phase)
     if (active && elim && tid == first) {
+        const int k = s_trk[tid] >> 16;
         double V[6] = {0, 0, 0, 0, 0, 0}, rhs[3] = {0, 0, 0};
         for (int j = 0; j < k; ++j) {
             const double* v = s_V + static_cast<size_t>(first + j) * 9;
@@ -154,8 +159,8 @@ __global__ void __launch_bounds__(256, 1) k_assemble(Shape S, DevPtrs D, AsmOutT
             }
         }
         if (singular) atomicOr(s_flags, 1);
-        double* st = s_trk + static_cast<size_t>(first) * 9;
-        double* gt = O.trk_data + static_cast<size_t>(trk) * kTrackRec;
+        double* st = s_V + static_cast<size_t>(first) * 9;
+        double* gt = O.trk_data + static_cast<size_t>(D.obs_trk[o]) * kTrackRec;
         for (int i = 0; i < 6; ++i) { st[i] = Ri[i]; gt[i] = Ri[i]; }
         for (int i = 0; i < 3; ++i) {
             st[6 + i] = q[i];
@@ -165,186 +170,181 @@ __global__ void __launch_bounds__(256, 1) k_assemble(Shape S, DevPtrs D, AsmOutT
     }
     __syncthreads();
 
-    // ---- phase 3: per observation, in FP64: Y = w Jp R^-T (2x3), the reduced weight
-    // M = w I - Y Y^T (2x2) and the reduced residual Mr = w r + Y q.  The observation's own
-    // contribution J^T M J, -J^T Mr is then formed with FP32 products: the cancellation between
-    // the direct term and the point elimination happens here, in FP64.  G_o = J^T Y (arithmetic
-    // type T) carries the couplings to the other observations of the track.
-    if (active && ok) {
-        const double w = L.wd;
-        double Y[2][3] = {{0, 0, 0}, {0, 0, 0}}, q[3] = {0, 0, 0};
-        if (elim) {
-            const double* st = s_trk + static_cast<size_t>(first) * 9;
-            const double i00 = st[0], i10 = st[1], i11 = st[2], i20 = st[3], i21 = st[4], i22 = st[5];
-            q[0] = st[6]; q[1] = st[7]; q[2] = st[8];
-            for (int pa = 0; pa < 2; ++pa) {
-                const double p0 = L.Jp[pa * 3], p1 = L.Jp[pa * 3 + 1], p2 = L.Jp[pa * 3 + 2];
-                Y[pa][0] = w * (i00 * p0);
-                Y[pa][1] = w * (i10 * p0 + i11 * p1);
-                Y[pa][2] = w * (i20 * p0 + i21 * p1 + i22 * p2);
+    // ---- C: per observation, in FP64: Y = w Jp R^-T, M = w I - Y Y^T, M r = w r + Y q; then
+    // G = A^T Y.  All from the rounded Jacobians A, Jp, so that the reduced system is the exact
+    // Schur complement of one (slightly perturbed) linearisation; values are float-float on the
+    // FP32 path (zero for observations of tracks that are not eliminated).
+    if (active) {
+        VT* G = s_G + static_cast<size_t>(tid) * 3 * nA;
+        VT* Mo = s_M + static_cast<size_t>(tid) * 7;
+        if (ok) {
+            const double w = L.wd;
+            double Y[2][3] = {{0, 0, 0}, {0, 0, 0}}, q[3] = {0, 0, 0};
+            if (elim) {
+                const double* st = s_V + static_cast<size_t>(first) * 9;
+                const double i00 = st[0], i10 = st[1], i11 = st[2], i20 = st[3], i21 = st[4], i22 = st[5];
+                q[0] = st[6]; q[1] = st[7]; q[2] = st[8];
+                for (int pa = 0; pa < 2; ++pa) {
+                    const double p0 = L.Jp[pa * 3], p1 = L.Jp[pa * 3 + 1], p2 = L.Jp[pa * 3 + 2];
+                    Y[pa][0] = w * (i00 * p0);
+                    Y[pa][1] = w * (i10 * p0 + i11 * p1);
+                    Y[pa][2] = w * (i20 * p0 + i21 * p1 + i22 * p2);
+                }
             }
-        }
-        const double m00 = w - (Y[0][0] * Y[0][0] + Y[0][1] * Y[0][1] + Y[0][2] * Y[0][2]);
-        const double m01 = -(Y[0][0] * Y[1][0] + Y[0][1] * Y[1][1] + Y[0][2] * Y[1][2]);
-        const double m11 = w - (Y[1][0] * Y[1][0] + Y[1][1] * Y[1][1] + Y[1][2] * Y[1][2]);
-        const double mr0 = w * L.rd0 + (Y[0][0] * q[0] + Y[0][1] * q[1] + Y[0][2] * q[2]);
-        const double mr1 = w * L.rd1 + (Y[1][0] * q[0] + Y[1][1] * q[1] + Y[1][2] * q[2]);
-        if (elim) {
-            T* G = s_G + static_cast<size_t>(tid) * per_obs;
-            const T y00 = static_cast<T>(Y[0][0]), y01 = static_cast<T>(Y[0][1]), y02 = static_cast<T>(Y[0][2]);
-            const T y10 = static_cast<T>(Y[1][0]), y11 = static_cast<T>(Y[1][1]), y12 = static_cast<T>(Y[1][2]);
-            for (int a = 0; a < 6 + ni; ++a) {
-                const T ja0 = a < 6 ? L.Jc[a] : L.Ji[a - 6];
-                const T ja1 = a < 6 ? L.Jc[6 + a] : L.Ji[kMaxNI + a - 6];
+            Mo[0] = Val::make(w - (Y[0][0] * Y[0][0] + Y[0][1] * Y[0][1] + Y[0][2] * Y[0][2]));
+            Mo[1] = Val::make(-(Y[0][0] * Y[1][0] + Y[0][1] * Y[1][1] + Y[0][2] * Y[1][2]));
+            Mo[2] = Val::make(w - (Y[1][0] * Y[1][0] + Y[1][1] * Y[1][1] + Y[1][2] * Y[1][2]));
+            Mo[3] = Val::make(w * L.rd0 + (Y[0][0] * q[0] + Y[0][1] * q[1] + Y[0][2] * q[2]));
+            Mo[4] = Val::make(w * L.rd1 + (Y[1][0] * q[0] + Y[1][1] * q[1] + Y[1][2] * q[2]));
+            Mo[5] = Val::make(w * L.rd0);
+            Mo[6] = Val::make(w * L.rd1);
+            const VT y00 = Val::make(Y[0][0]), y01 = Val::make(Y[0][1]), y02 = Val::make(Y[0][2]);
+            const VT y10 = Val::make(Y[1][0]), y11 = Val::make(Y[1][1]), y12 = Val::make(Y[1][2]);
+            const T* A = s_A + static_cast<size_t>(tid) * 2 * nA;
+            for (int a = 0; a < nA; ++a) {
+                const T ja0 = A[a], ja1 = A[nA + a];
                 G[a * 3 + 0] = ja0 * y00 + ja1 * y10;
                 G[a * 3 + 1] = ja0 * y01 + ja1 * y11;
                 G[a * 3 + 2] = ja0 * y02 + ja1 * y12;
             }
-        }
-        const T M00 = static_cast<T>(m00), M01 = static_cast<T>(m01), M11 = static_cast<T>(m11);
-        const int dslot = (lcam != 255 && lcam < ncams) ? s_lookup[lcam * MC + lcam] : 0xFFFF;
-        if (lcam != 255 && dslot >= npairs) atomicOr(s_flags, 4);
-        if (lcam != 255 && dslot < npairs) {
-            double* P = s_pair + static_cast<size_t>(dslot) * 36;
-            T mj0[6], mj1[6];
-            for (int b = 0; b < 6; ++b) {
-                mj0[b] = M00 * L.Jc[b] + M01 * L.Jc[6 + b];
-                mj1[b] = M01 * L.Jc[b] + M11 * L.Jc[6 + b];
-            }
-            for (int a = 0; a < 6; ++a)
-                for (int b = 0; b < 6; ++b) atomic_add_t(P + a * 6 + b, L.Jc[a] * mj0[b] + L.Jc[6 + a] * mj1[b]);
-            for (int a = 0; a < 6; ++a) {
-                const double ja0 = L.Jc[a], ja1 = L.Jc[6 + a];
-                atomic_add_t(s_rhs + lcam * 12 + a, -(ja0 * mr0 + ja1 * mr1));
-                atomic_add_t(s_rhs + lcam * 12 + 6 + a, -w * (ja0 * L.rd0 + ja1 * L.rd1));
-            }
-        }
-        if (ng > 0 && grp >= 0) {
-            for (int a = 0; a < ni; ++a) {
-                const T mi0 = M00 * L.Ji[a] + M01 * L.Ji[kMaxNI + a];
-                const T mi1 = M01 * L.Ji[a] + M11 * L.Ji[kMaxNI + a];
-                for (int b = 0; b < ni; ++b)
-                    atomic_add_t(s_C + (grp * ni + b) * nb + grp * ni + a, L.Ji[b] * mi0 + L.Ji[kMaxNI + b] * mi1);
-                const double ja0 = L.Ji[a], ja1 = L.Ji[kMaxNI + a];
-                atomic_add_t(s_C + nb * nb + grp * ni + a, -(ja0 * mr0 + ja1 * mr1));
-                atomic_add_t(s_C + nb * nb + nb + grp * ni + a, -w * (ja0 * L.rd0 + ja1 * L.rd1));
-                if (lcam != 255 && lcam < ncams)
-                    for (int b = 0; b < 6; ++b)
-                        atomic_add_t(s_border + ((lcam * ng + grp) * 6 + b) * ni + a, L.Jc[b] * mi0 + L.Jc[6 + b] * mi1);
-            }
-        }
-    }
-    __syncthreads();
-
-    // ---- phase 4: couplings between different observations of an eliminated track
-    if (active && ok && elim) {
-        const int j = tid - first;
-        const int npt = k * (k - 1) / 2;  // strictly upper pairs a < b
-        for (int p = j; p < npt; p += k) {
-            int a = 0, rem = p;
-            while (rem >= k - 1 - a) { rem -= k - 1 - a; ++a; }
-            const int b = a + 1 + rem;
-            const int oa = first + a, ob = first + b;
-            const int la = D.obs_lcam[obs0 + oa], lb = D.obs_lcam[obs0 + ob];
-            if (la == 255 || lb == 255) continue;
-            const T* Ga = s_G + static_cast<size_t>(oa) * per_obs;
-            const T* Gb = s_G + static_cast<size_t>(ob) * per_obs;
-            const int lo = min(la, lb), hi = max(la, lb);
-            const int slot = hi < ncams ? s_lookup[lo * MC + hi] : 0xFFFF;
-            if (slot >= npairs) {
-                atomicOr(s_flags, 4);
-                continue;
-            }
-            double* P = s_pair + static_cast<size_t>(slot) * 36;
-            for (int x = 0; x < 6; ++x)
-                for (int y = 0; y < 6; ++y) {
-                    const T m = Ga[x * 3] * Gb[y * 3] + Ga[x * 3 + 1] * Gb[y * 3 + 1] + Ga[x * 3 + 2] * Gb[y * 3 + 2];
-                    if (la < lb) {
-                        atomic_add_t(P + x * 6 + y, -m);
-                    } else if (la > lb) {
-                        atomic_add_t(P + y * 6 + x, -m);
-                    } else {
-                        atomic_add_t(P + x * 6 + y, -m);
-                        atomic_add_t(P + y * 6 + x, -m);
-                    }
-                }
-        }
-        if (ng > 0) {
-            // K_g = sum of G^int over the track's observations of group g.  The pose-intrinsic and
-            // intrinsic-intrinsic couplings of distinct observations are -G^pose (K_g - own)^T and
-            // -(K_g K_g'^T - sum_own G^int G^int^T); the observation's own terms are in phase 3.
-            const T* Go = s_G + static_cast<size_t>(tid) * per_obs;
-            for (int g = 0; g < ng; ++g) {
-                T K[3 * kMaxNI];
-                bool present = false;
-                for (int i = 0; i < 3 * ni; ++i) K[i] = T(0);
-                for (int jj = 0; jj < k; ++jj) {
-                    const int oo = obs0 + first + jj;
-                    if (D.cam_group[D.obs_cam[oo]] != g) continue;
-                    present = true;
-                    const T* Gj = s_G + static_cast<size_t>(first + jj) * per_obs + 18;
-                    for (int i = 0; i < 3 * ni; ++i) K[i] += Gj[i];
-                }
-                if (!present) continue;
-                if (lcam != 255 && lcam < ncams) {
-                    T Kx[3 * kMaxNI];
-                    for (int i = 0; i < 3 * ni; ++i) Kx[i] = K[i] - (g == grp ? Go[18 + i] : T(0));
-                    for (int x = 0; x < 6; ++x)
-                        for (int c2 = 0; c2 < ni; ++c2)
-                            atomic_add_t(s_border + ((lcam * ng + g) * 6 + x) * ni + c2,
-                                         -(Go[x * 3] * Kx[c2 * 3] + Go[x * 3 + 1] * Kx[c2 * 3 + 1] +
-                                           Go[x * 3 + 2] * Kx[c2 * 3 + 2]));
-                }
-                if (g == grp)
-                    for (int c1 = 0; c1 < ni; ++c1)
-                        for (int c2 = 0; c2 < ni; ++c2) {
-                            const T* gi = Go + 18;
-                            atomic_add_t(s_C + (g * ni + c1) * nb + g * ni + c2,
-                                         gi[c1 * 3] * gi[c2 * 3] + gi[c1 * 3 + 1] * gi[c2 * 3 + 1] +
-                                             gi[c1 * 3 + 2] * gi[c2 * 3 + 2]);
-                        }
-                if (j == 0) {
-                    for (int g2 = g; g2 < ng; ++g2) {
-                        T K2[3 * kMaxNI];
-                        bool present2 = false;
-                        for (int i = 0; i < 3 * ni; ++i) K2[i] = T(0);
-                        for (int jj = 0; jj < k; ++jj) {
-                            const int oo = obs0 + first + jj;
-                            if (D.cam_group[D.obs_cam[oo]] != g2) continue;
-                            present2 = true;
-                            const T* Gj = s_G + static_cast<size_t>(first + jj) * per_obs + 18;
-                            for (int i = 0; i < 3 * ni; ++i) K2[i] += Gj[i];
-                        }
-                        if (!present2) continue;
-                        for (int c1 = 0; c1 < ni; ++c1)
-                            for (int c2 = 0; c2 < ni; ++c2) {
-                                const T m = K[c1 * 3] * K2[c2 * 3] + K[c1 * 3 + 1] * K2[c2 * 3 + 1] +
-                                            K[c1 * 3 + 2] * K2[c2 * 3 + 2];
-                                atomic_add_t(s_C + (g * ni + c1) * nb + g2 * ni + c2, -m);
-                                if (g2 != g) atomic_add_t(s_C + (g2 * ni + c2) * nb + g * ni + c1, -m);
-                            }
-                    }
-                }
-            }
+        } else {
+            for (int i = 0; i < 7; ++i) Mo[i] = Val::zero();
+            for (int i = 0; i < 3 * nA; ++i) G[i] = Val::zero();
         }
     }
     // block cost (FP64, fixed order)
-    double cw = warp_sum(cost);
+    const double cw = warp_sum(cost);
     if ((tid & 31) == 0) s_misc[tid >> 5] = cw;
     __syncthreads();
 
-    // ---- phase 5: write the chunk's partial blocks
-    double* pp = O.part_pair + static_cast<size_t>(pair0) * 36;
-    for (int i = tid; i < npairs * 36; i += blockDim.x) pp[i] = s_pair[i];
+    // ---- D: owner gathers.  Work index space: [pair entries | camera entries | chunk entries]
+    const int pair0 = D.ch_pair_begin[chunk], npairs = D.ch_pair_begin[chunk + 1] - pair0;
+    const int cam0 = D.ch_cam_begin[chunk], ncams = D.ch_cam_begin[chunk + 1] - cam0;
     const int camrec = 12 + ng * 6 * ni;
-    double* pc = O.part_cam + static_cast<size_t>(cam0) * camrec;
-    for (int i = tid; i < ncams * camrec; i += blockDim.x) {
-        const int l = i / camrec, e = i - l * camrec;
-        pc[i] = e < 12 ? s_rhs[l * 12 + e] : s_border[l * ng * 6 * ni + (e - 12)];
-    }
     const int chrec = nb * nb + 2 * nb;
-    double* pk = O.part_chunk + static_cast<size_t>(chunk) * chrec;
-    for (int i = tid; i < chrec; i += blockDim.x) pk[i] = s_C[i];
+    const int w_pair = npairs * 36, w_cam = ncams * camrec;
+    const int w_total = w_pair + w_cam + chrec;
+    for (int wk = tid; wk < w_total; wk += blockDim.x) {
+        Acc<T> acc;
+        if (wk < w_pair) {
+            // pose block entry (x, y) of chunk pair slot s
+            const int s = wk / 36, e = wk - s * 36;
+            const int x = e / 6, y = e - x * 6;
+            const int pk = D.ch_pairs[pair0 + s];
+            const bool diag = (pk & 0xFFFF) == (pk >> 16);
+            if (diag && x > y) continue;
+            const int i1 = D.slot_item_begin[pair0 + s + 1];
+            for (int it = D.slot_item_begin[pair0 + s]; it < i1; ++it) {
+                const unsigned item = D.slot_items[it];
+                const int oa = item & 0xFF, ob = item >> 8;
+                if (oa == ob) {
+                    const T* A = s_A + static_cast<size_t>(oa) * 2 * nA;
+                    const VT* M = s_M + static_cast<size_t>(oa) * 7;
+                    const T ax0 = A[x], ax1 = A[nA + x], ay0 = A[y], ay1 = A[nA + y];
+                    acc.add(ax0 * (ay0 * M[0] + ay1 * M[1]) + ax1 * (ay0 * M[1] + ay1 * M[2]));
+                } else {
+                    const VT* Ga = s_G + static_cast<size_t>(oa) * 3 * nA + 3 * x;
+                    const VT* Gb = s_G + static_cast<size_t>(ob) * 3 * nA + 3 * y;
+                    acc.add(-(Ga[0] * Gb[0] + Ga[1] * Gb[1] + Ga[2] * Gb[2]));
+                }
+            }
+            P* out = O.part_pair + static_cast<size_t>(pair0 + s) * 36;
+            out[e] = acc.part();
+            if (diag && x != y) out[y * 6 + x] = acc.part();
+        } else if (wk < w_pair + w_cam) {
+            // camera record entry: rhs (6), direct rhs (6), border (ng x 6 x ni)
+            const int l = (wk - w_pair) / camrec, e = wk - w_pair - l * camrec;
+            const int b0 = D.lcam_obs_begin[cam0 + l], b1 = D.lcam_obs_begin[cam0 + l + 1];
+            if (e < 12) {
+                const int a = e < 6 ? e : e - 6, mo = e < 6 ? 3 : 5;
+                for (int it = b0; it < b1; ++it) {
+                    const int ob = D.lcam_obs[it];
+                    const T* A = s_A + static_cast<size_t>(ob) * 2 * nA;
+                    const VT* M = s_M + static_cast<size_t>(ob) * 7;
+                    acc.add(-(A[a] * M[mo] + A[nA + a] * M[mo + 1]));
+                }
+            } else {
+                const int f = e - 12;
+                const int g = f / (6 * ni), rem = f - g * 6 * ni, a = rem / ni, c2 = rem - a * ni;
+                for (int it = b0; it < b1; ++it) {
+                    const int ob = D.lcam_obs[it];
+                    const int info = s_info[ob];
+                    const T* A = s_A + static_cast<size_t>(ob) * 2 * nA;
+                    if (info_group(info) == g) {
+                        // own term J_pose^T M J_intr
+                        const VT* M = s_M + static_cast<size_t>(ob) * 7;
+                        const T i0 = A[6 + c2], i1 = A[nA + 6 + c2];
+                        acc.add(A[a] * (i0 * M[0] + i1 * M[1]) + A[nA + a] * (i0 * M[1] + i1 * M[2]));
+                    }
+                    if (info & kElim) {
+                        // couplings to the group-g observations of the same track
+                        const int tr = s_trk[ob], f0 = tr & 0xFFFF, k = tr >> 16;
+                        VT k0 = Val::zero(), k1 = Val::zero(), k2 = Val::zero();
+                        for (int j = f0; j < f0 + k; ++j) {
+                            if (j == ob || info_group(s_info[j]) != g) continue;
+                            const VT* Gj = s_G + static_cast<size_t>(j) * 3 * nA + 3 * (6 + c2);
+                            k0 = k0 + Gj[0];
+                            k1 = k1 + Gj[1];
+                            k2 = k2 + Gj[2];
+                        }
+                        const VT* Go = s_G + static_cast<size_t>(ob) * 3 * nA + 3 * a;
+                        acc.add(-(Go[0] * k0 + Go[1] * k1 + Go[2] * k2));
+                    }
+                }
+            }
+            O.part_cam[static_cast<size_t>(cam0 + l) * camrec + e] = acc.part();
+        } else {
+            // chunk record entry: intrinsic block (nb x nb), intrinsic rhs (nb), direct rhs (nb)
+            const int e = wk - w_pair - w_cam;
+            P* out = O.part_chunk + static_cast<size_t>(chunk) * chrec;
+            if (e < nb * nb) {
+                const int i = e / nb, j = e - i * nb;
+                if (i > j) continue;
+                const int g1 = i / ni, c1 = i - g1 * ni, g2 = j / ni, c2 = j - g2 * ni;
+                for (int t0 = 0; t0 < nobs;) {
+                    const int k = s_trk[t0] >> 16;
+                    VT K1[3] = {Val::zero(), Val::zero(), Val::zero()}, K2[3] = {Val::zero(), Val::zero(), Val::zero()};
+                    for (int jj = t0; jj < t0 + k; ++jj) {
+                        const int gj = info_group(s_info[jj]);
+                        const VT* Gj = s_G + static_cast<size_t>(jj) * 3 * nA;
+                        if (gj == g1) {
+                            const VT* ga = Gj + 3 * (6 + c1);
+                            K1[0] = K1[0] + ga[0]; K1[1] = K1[1] + ga[1]; K1[2] = K1[2] + ga[2];
+                            if (g1 == g2) {
+                                // own term J_intr^T M J_intr, plus the observation's own G G^T that
+                                // the track product K K^T below also contains
+                                const T* A = s_A + static_cast<size_t>(jj) * 2 * nA;
+                                const VT* M = s_M + static_cast<size_t>(jj) * 7;
+                                const T a0 = A[6 + c1], a1 = A[nA + 6 + c1], b0 = A[6 + c2], b1 = A[nA + 6 + c2];
+                                const VT* gb = Gj + 3 * (6 + c2);
+                                acc.add(a0 * (b0 * M[0] + b1 * M[1]) + a1 * (b0 * M[1] + b1 * M[2]) +
+                                        (ga[0] * gb[0] + ga[1] * gb[1] + ga[2] * gb[2]));
+                            }
+                        }
+                        if (gj == g2) {
+                            const VT* gb = Gj + 3 * (6 + c2);
+                            K2[0] = K2[0] + gb[0]; K2[1] = K2[1] + gb[1]; K2[2] = K2[2] + gb[2];
+                        }
+                    }
+                    acc.add(-(K1[0] * K2[0] + K1[1] * K2[1] + K1[2] * K2[2]));
+                    t0 += k;
+                }
+                out[e] = acc.part();
+                if (i != j) out[j * nb + i] = acc.part();
+            } else {
+                const int idx = e - nb * nb;
+                const int col = idx < nb ? idx : idx - nb, mo = idx < nb ? 3 : 5;
+                const int g = col / ni, c = col - g * ni;
+                for (int ob = 0; ob < nobs; ++ob) {
+                    if (info_group(s_info[ob]) != g) continue;
+                    const T* A = s_A + static_cast<size_t>(ob) * 2 * nA;
+                    const VT* M = s_M + static_cast<size_t>(ob) * 7;
+                    acc.add(-(A[6 + c] * M[mo] + A[nA + 6 + c] * M[mo + 1]));
+                }
+                out[e] = acc.part();
+            }
+        }
+    }
     if (tid == 0) {
         double c = 0.0;
         for (int w = 0; w < static_cast<int>((blockDim.x + 31) >> 5); ++w) c += s_misc[w];
@@ -354,30 +354,33 @@ __global__ void __launch_bounds__(256, 1) k_assemble(Shape S, DevPtrs D, AsmOutT
 }
 
 // Sum of the chunk partials of every upper pose block, written to both CSR orientations.
-__global__ void k_reduce_pairs(Shape S, DevPtrs D, const double* __restrict__ part_pair, double* __restrict__ vals) {
+template <typename T>
+__global__ void k_reduce_pairs(Shape S, DevPtrs D, const typename Acc<T>::part_type* __restrict__ part_pair,
+                               double* __restrict__ vals) {
     const long long idx = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (idx >= static_cast<long long>(S.nupper) * 36) return;
     const int u = static_cast<int>(idx / 36), e = static_cast<int>(idx - static_cast<long long>(u) * 36);
-    Acc<double> acc;
+    Acc<T> acc;
     for (int c = D.up_contrib_begin[u]; c < D.up_contrib_begin[u + 1]; ++c)
-        acc.add(part_pair[static_cast<size_t>(D.up_contrib[c]) * 36 + e]);
-    const double v = acc.value();
+        acc.merge_part(part_pair[static_cast<size_t>(D.up_contrib[c]) * 36 + e]);
+    const double v = acc.value64();
     vals[static_cast<size_t>(D.up_csr[u]) * 36 + e] = v;
     const int t = D.up_csr_t[u];
     if (t >= 0) vals[static_cast<size_t>(t) * 36 + (e % 6) * 6 + e / 6] = v;
 }
 
 // Sum of the per-camera partials: rhs, direct rhs and the intrinsic border rows.
-__global__ void k_reduce_cams(Shape S, DevPtrs D, const double* __restrict__ part_cam, double* __restrict__ rhs,
-                              double* __restrict__ direct, double* __restrict__ border) {
+template <typename T>
+__global__ void k_reduce_cams(Shape S, DevPtrs D, const typename Acc<T>::part_type* __restrict__ part_cam,
+                              double* __restrict__ rhs, double* __restrict__ direct, double* __restrict__ border) {
     const int camrec = 12 + S.ng * 6 * S.ni;
     const long long idx = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (idx >= static_cast<long long>(S.ncb) * camrec) return;
     const int i = static_cast<int>(idx / camrec), e = static_cast<int>(idx - static_cast<long long>(i) * camrec);
-    Acc<double> acc;
+    Acc<T> acc;
     for (int c = D.cam_contrib_begin[i]; c < D.cam_contrib_begin[i + 1]; ++c)
-        acc.add(part_cam[static_cast<size_t>(D.cam_contrib[c]) * camrec + e]);
-    const double v = acc.value();
+        acc.merge_part(part_cam[static_cast<size_t>(D.cam_contrib[c]) * camrec + e]);
+    const double v = acc.value64();
     if (e < 6) rhs[i * 6 + e] = v;
     else if (e < 12) direct[i * 6 + e - 6] = v;
     else {
@@ -387,18 +390,33 @@ __global__ void k_reduce_cams(Shape S, DevPtrs D, const double* __restrict__ par
     }
 }
 
-// Chunk-level sums (intrinsic block, intrinsic rhs, cost, flags); one CTA, fixed order.
-__global__ void k_reduce_chunks(Shape S, const double* __restrict__ part_chunk, const double* __restrict__ part_cost,
-                                const int* __restrict__ part_flags, double* __restrict__ Cm, double* __restrict__ rhs_b,
-                                double* __restrict__ direct_b, double* __restrict__ result) {
+// Chunk-level sums (intrinsic block, intrinsic rhs): one CTA per 32 record entries, its warps
+// striding over the chunks, merged in warp order.  The last CTA sums the costs and flags.
+template <typename T>
+__global__ void k_reduce_chunks(Shape S, const typename Acc<T>::part_type* __restrict__ part_chunk,
+                                const double* __restrict__ part_cost, const int* __restrict__ part_flags,
+                                double* __restrict__ Cm, double* __restrict__ rhs_b, double* __restrict__ direct_b,
+                                double* __restrict__ result) {
     const int nb = S.nb, chrec = nb * nb + 2 * nb;
-    for (int e = threadIdx.x; e < chrec; e += blockDim.x) {
-        Acc<double> acc;
-        for (int c = 0; c < S.nchunks; ++c) acc.add(part_chunk[static_cast<size_t>(c) * chrec + e]);
-        const double v = acc.value();
-        if (e < nb * nb) Cm[e] = v;
-        else if (e < nb * nb + nb) rhs_b[e - nb * nb] = v;
-        else direct_b[e - nb * nb - nb] = v;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int tiles = (chrec + 31) / 32;
+    if (static_cast<int>(blockIdx.x) < tiles) {
+        __shared__ typename Acc<T>::part_type s_acc[8][32];
+        const int e = blockIdx.x * 32 + lane;
+        Acc<T> acc;
+        if (e < chrec)
+            for (int c = wid; c < S.nchunks; c += nw) acc.merge_part(part_chunk[static_cast<size_t>(c) * chrec + e]);
+        s_acc[wid][lane] = acc.part();
+        __syncthreads();
+        if (wid == 0 && e < chrec) {
+            Acc<T> tot;
+            for (int w = 0; w < nw; ++w) tot.merge_part(s_acc[w][lane]);
+            const double v = tot.value64();
+            if (e < nb * nb) Cm[e] = v;
+            else if (e < nb * nb + nb) rhs_b[e - nb * nb] = v;
+            else direct_b[e - nb * nb - nb] = v;
+        }
+        return;
     }
     __shared__ double s_cost[256];
     __shared__ int s_flag[256];
@@ -899,9 +917,9 @@ __global__ void k_linearize_export(Shape S, DevPtrs D, double* __restrict__ res,
 // ---------------------------------------------------------------- launchers
 template <typename T>
 static AsmOutT<T> typed(const AsmOut& o) {
-    return {static_cast<double*>(o.part_pair_v), static_cast<double*>(o.part_cam_v),
-            static_cast<double*>(o.part_chunk_v), o.part_cost, o.part_flags, static_cast<double*>(o.trk_data_v),
-            static_cast<T*>(o.obs_wn_v)};
+    using P = typename Acc<T>::part_type;
+    return {static_cast<P*>(o.part_pair_v), static_cast<P*>(o.part_cam_v), static_cast<P*>(o.part_chunk_v),
+            o.part_cost, o.part_flags, static_cast<double*>(o.trk_data_v), static_cast<T*>(o.obs_wn_v)};
 }
 
 template <typename T>
@@ -910,17 +928,20 @@ void launch_assemble(const Shape& S, const DevPtrs& D, const AsmOut& O, double d
     k_assemble<T><<<S.nchunks, S.max_obs, smem, st>>>(S, D, typed<T>(O), damping);
 }
 
+template <typename T>
 void launch_reduce(const Shape& S, const DevPtrs& D, const AsmOut& O, const RedOut<double>& R, double damping,
                    cudaStream_t st) {
-    const double* pp = static_cast<const double*>(O.part_pair_v);
-    const double* pc = static_cast<const double*>(O.part_cam_v);
-    const double* pk = static_cast<const double*>(O.part_chunk_v);
+    const AsmOutT<T> P = typed<T>(O);
     const long long np = static_cast<long long>(S.nupper) * 36;
-    if (np > 0) k_reduce_pairs<<<static_cast<unsigned>((np + 255) / 256), 256, 0, st>>>(S, D, pp, R.vals);
+    if (np > 0) k_reduce_pairs<T><<<static_cast<unsigned>((np + 255) / 256), 256, 0, st>>>(S, D, P.part_pair, R.vals);
     const long long nc = static_cast<long long>(S.ncb) * (12 + S.ng * 6 * S.ni);
-    if (nc > 0) k_reduce_cams<<<static_cast<unsigned>((nc + 255) / 256), 256, 0, st>>>(S, D, pc, R.rhs, R.direct, R.border);
-    k_reduce_chunks<<<1, 256, 0, st>>>(S, pk, O.part_cost, O.part_flags, R.Cm, R.rhs + 6 * S.ncb, R.direct + 6 * S.ncb,
-                                       R.result);
+    if (nc > 0)
+        k_reduce_cams<T><<<static_cast<unsigned>((nc + 255) / 256), 256, 0, st>>>(S, D, P.part_cam, R.rhs, R.direct,
+                                                                                  R.border);
+    const int chrec = S.nb * S.nb + 2 * S.nb;
+    const int tiles = (chrec + 31) / 32;
+    k_reduce_chunks<T><<<tiles + 1, 256, 0, st>>>(S, P.part_chunk, O.part_cost, O.part_flags, R.Cm, R.rhs + 6 * S.ncb,
+                                                  R.direct + 6 * S.ncb, R.result);
     const int nf = std::max(S.ncb * 6, 1);
     k_finalize<<<(nf + 255) / 256, 256, 0, st>>>(S, D, R.vals, R.Cm, R.rhs + 6 * S.ncb, R.direct + 6 * S.ncb, R.result,
                                                   damping);
@@ -976,6 +997,10 @@ void pb_set_assemble_smem_f64(size_t bytes) {
 
 template void launch_assemble<float>(const Shape&, const DevPtrs&, const AsmOut&, double, size_t, cudaStream_t);
 template void launch_assemble<double>(const Shape&, const DevPtrs&, const AsmOut&, double, size_t, cudaStream_t);
+template void launch_reduce<float>(const Shape&, const DevPtrs&, const AsmOut&, const RedOut<double>&, double,
+                                   cudaStream_t);
+template void launch_reduce<double>(const Shape&, const DevPtrs&, const AsmOut&, const RedOut<double>&, double,
+                                    cudaStream_t);
 template void launch_back_substitute<float>(const Shape&, const DevPtrs&, const double*, const float*, const double*,
                                             double*, double*, const double*, double*, cudaStream_t);
 template void launch_back_substitute<double>(const Shape&, const DevPtrs&, const double*, const double*, const double*,

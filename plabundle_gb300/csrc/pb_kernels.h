@@ -5,6 +5,7 @@
 
 #include <algorithm>
 
+#include "pb_device.cuh"
 #include "pb_internal.h"
 
 namespace pb {
@@ -12,15 +13,14 @@ namespace pb {
 constexpr int kMaxAlpha = 8;  // trial step lengths evaluated per objective pass
 
 // Outputs of the assembly kernel (per-chunk partials) and per-track / per-observation data kept
-// for the back-substitution.
-// The partial sums are FP64 on both paths: FP32 products are accumulated in double precision so
-// that the cancellation between the direct and the Schur terms of the reduced blocks keeps its
-// accuracy.
+// for the back-substitution.  Partials are the accumulator pairs of Acc<T>: (hi, lo) float pairs
+// of the two-sum accumulation on the FP32 path, doubles on the FP64 path.
 template <typename T>
 struct AsmOutT {
-    double* part_pair;     // pair partials * 36
-    double* part_cam;      // camera partials * (12 + ng*6*ni)
-    double* part_chunk;    // chunks * (nb*nb + 2*nb)
+    using P = typename Acc<T>::part_type;
+    P* part_pair;     // pair partials * 36
+    P* part_cam;      // camera partials * (12 + ng*6*ni)
+    P* part_chunk;    // chunks * (nb*nb + 2*nb)
     double* part_cost;
     int* part_flags;  // bit 0: singular point system, bit 1: invalid projection
     double* trk_data; // processed tracks * kTrackRec (FP64 point factor, q, rhs)
@@ -52,6 +52,7 @@ struct RedOut {
 
 template <typename T>
 void launch_assemble(const Shape& S, const DevPtrs& D, const AsmOut& O, double damping, size_t smem, cudaStream_t st);
+template <typename T>
 void launch_reduce(const Shape& S, const DevPtrs& D, const AsmOut& O, const RedOut<double>& R, double damping,
                    cudaStream_t st);
 template <typename T>

@@ -92,6 +92,7 @@ struct pb_gpu_ctx {
     DeviceArena darena;           // dense preconditioner buffers (depend on the reduced dimension only)
     DenseWork<float> dw32;
     DenseWork<double> dw64;
+    double shift32 = 1e-7;  // last FP32 factor shift that factorised
     bool dense_ready[2] = {false, false};
     int last_solver = 0;
     // shared FP64 buffers
@@ -357,19 +358,21 @@ void prepare_precision(pb_gpu_ctx* c, int precision) {
     D.cam_contrib_begin = upload_new(A, cs.cam_contrib_begin, st);
     D.cam_contrib = upload_new(A, cs.cam_contrib, st);
     D.obs_lcam = upload_new(A, cs.obs_lcam, st);
+    D.slot_item_begin = upload_new(A, cs.slot_item_begin, st);
+    D.slot_items = upload_new(A, cs.slot_items, st);
+    D.lcam_obs_begin = upload_new(A, cs.lcam_obs_begin, st);
+    D.lcam_obs = upload_new(A, cs.lcam_obs, st);
     const int camrec = 12 + S.ng * 6 * S.ni, chrec = S.nb * S.nb + 2 * S.nb;
-    // chunk partials are FP64 on both paths (the assembly accumulates in double precision)
-    B.out.part_pair_v = A.alloc<double>(cs.n_pair_partials() * 36);
-    B.out.part_cam_v = A.alloc<double>(cs.n_cam_partials() * camrec);
-    B.out.part_chunk_v = A.alloc<double>(static_cast<size_t>(std::max(1, S.nchunks)) * std::max(1, chrec));
+    // chunk partials: accumulator pairs of the assembly (float2 on the FP32 path, double on FP64)
+    using PT = typename Acc<T>::part_type;
+    B.out.part_pair_v = A.alloc<PT>(cs.n_pair_partials() * 36);
+    B.out.part_cam_v = A.alloc<PT>(cs.n_cam_partials() * camrec);
+    B.out.part_chunk_v = A.alloc<PT>(static_cast<size_t>(std::max(1, S.nchunks)) * std::max(1, chrec));
     B.out.part_cost = A.alloc<double>(std::max(1, S.nchunks));
     B.out.part_flags = A.alloc<int>(std::max(1, S.nchunks));
     B.out.trk_data_v = A.alloc<double>(static_cast<size_t>(S.ntp) * kTrackRec);
     B.out.obs_wn_v = A.alloc<T>(static_cast<size_t>(S.nop));
     c->pcg_part = nullptr;
-    const size_t smem = chunk_smem_bytes(precision, S.max_obs, S.max_cams, S.max_pairs, S.ng, S.ni);
-    // opt in to the large shared-memory carve-out for the assembly kernel
-    (void)smem;
     B.ready = true;
     check(cudaStreamSynchronize(st), "prepare");
 }
@@ -404,7 +407,7 @@ void assemble(pb_gpu_ctx* c, double damping, int precision, double* cost, int* f
     PrecisionBuffers<T>& B = pbuf<T>(c);
     const Shape& S = c->S[precision];
     const DevPtrs& D = c->D[precision];
-    const size_t smem = chunk_smem_bytes(precision, S.max_obs, S.max_cams, S.max_pairs, S.ng, S.ni);
+    const size_t smem = chunk_smem_bytes(precision, S.max_obs, S.ni);
     set_assemble_smem(precision, smem);
     {
         Timer t(c, 0);
@@ -413,7 +416,7 @@ void assemble(pb_gpu_ctx* c, double damping, int precision, double* cost, int* f
     }
     {
         Timer t(c, 3);
-        launch_reduce(S, D, B.out, c->red, damping, c->stream);
+        launch_reduce<T>(S, D, B.out, c->red, damping, c->stream);
         c->launches += 4;
     }
     check(cudaGetLastError(), "assemble launch");
@@ -468,17 +471,21 @@ int solve_dense(pb_gpu_ctx* c, double rel, double abs_tol, int max_it, bool* con
                 double* relres) {
     ensure_dense<T>(c);
     DenseWork<T>& W = dwork<T>(c);
-    // FP32 factor of the Jacobi-scaled matrix with a small shift (kept positive definite in FP32);
-    // FP64 factor unshifted.  A failed factorisation is retried with a larger shift.
-    double shift = std::is_same<T, float>::value ? 1e-5 : 0.0;
+    // FP32 factor of the Jacobi-scaled matrix with a small shift (FP32 rounding of a matrix of
+    // condition ~1e9 is not positive definite unshifted); the CG that follows runs on the
+    // FP64 matrix, so the shift only costs iterations.  It starts at the last shift that
+    // factorised and grows tenfold on failure.  The FP64 factor starts unshifted.
+    const bool f32 = std::is_same<T, float>::value;
+    double shift = f32 ? c->shift32 : 0.0;
     int st = 0;
-    for (int attempt = 0; attempt < 4; ++attempt) {
+    for (int attempt = 0; attempt < 6; ++attempt) {
         st = dense_factor<T>(c->sys, W, shift, c->stream, &c->launches);
         if (st < 0) throw CudaError(std::string("dense factorisation failed: ") + cudaGetErrorString(cudaGetLastError()));
         if (st == 0 || (st & 1)) break;
-        shift = shift == 0.0 ? 1e-9 : shift * 100.0;
+        shift = shift == 0.0 ? 1e-9 : shift * 10.0;
     }
     if (st) return 1;
+    if (f32) c->shift32 = shift;
     const int rc = dense_pcg<T>(c->sys, W, c->red.rhs, rel, abs_tol, max_it, iterations, relres, converged,
                                 c->h_scratch + 40, c->stream, &c->launches);
     if (rc < 0) throw CudaError(std::string("dense CG failed: ") + cudaGetErrorString(cudaGetLastError()));
@@ -904,6 +911,7 @@ pb_status pb_gpu_upload(pb_gpu_ctx* c, const pb_problem_desc* pr, const pb_solve
         cudaSetDevice(c->device);
         HostModel m;
         std::string err;
+        c->shift32 = 1e-7;
         const int rc = build_host_model(pr, op, &m, &err);
         if (rc) {
             c->uploaded = false;
@@ -929,6 +937,8 @@ pb_status pb_gpu_upload(pb_gpu_ctx* c, const pb_problem_desc* pr, const pb_solve
                 dst.ch_pair_begin = src.ch_pair_begin; dst.ch_pairs = src.ch_pairs;
                 dst.up_contrib_begin = src.up_contrib_begin; dst.up_contrib = src.up_contrib;
                 dst.cam_contrib_begin = src.cam_contrib_begin; dst.cam_contrib = src.cam_contrib; dst.obs_lcam = src.obs_lcam;
+                dst.slot_item_begin = src.slot_item_begin; dst.slot_items = src.slot_items;
+                dst.lcam_obs_begin = src.lcam_obs_begin; dst.lcam_obs = src.lcam_obs;
                 sd.nchunks = ss.nchunks; sd.max_obs = ss.max_obs; sd.max_cams = ss.max_cams; sd.max_pairs = ss.max_pairs;
             };
             keep_chunks(c->D[0], d0, c->S[0], s0);
