@@ -1,0 +1,472 @@
+// pb_assemble.cu -- kernels (a)+(b): per-observation linearisation and online point Schur
+// elimination into the block-sparse reduced camera system.
+//
+// One CTA per chunk of consecutive tracks (host-built: at most max_obs observations and
+// max_tracks tracks), one thread per observation:
+//   A. linearise the observation: FP64 residual, robust weight and cost; Jacobians A = [J_pose |
+//      J_intr] and Jp in T (FP32 on the mixed path);
+//   B. per track, V = sum w Jp^T Jp and the point gradient in FP64 and the factor V = R R^T
+//      (the 3x3 point block inverse of BundleAdjustPlaMatrixReferenceSchur.cpp:350-490);
+//   C. per observation, in FP64: Y = w Jp R^-T (2x3), the reduced weight M = w I - Y Y^T and Y q
+//      (q = R^-1 g_p); then G = J_pose^T Y.  The matrix derives from the rounded Jacobians only,
+//      so it is the exact Schur complement of one consistently perturbed linearisation (the
+//      FP32 rounding of a Jacobian perturbs the weakest mode of S by ~eps*sqrt(cond), rounding
+//      S itself by eps*cond).  The gradient g = -J^T w r is FP64-accurate (see linearize_obs):
+//      the rounded Jacobians shape the step, never the fixed point;
+//   K. per track and calibration group, K = sum over the group's observations of J_intr^T Y;
+//   D. every output element of the chunk is owned by one thread, which gathers its terms in a
+//      fixed order into compensated accumulators and writes the chunk partial once:
+//        pose block (a, b):  sum_o J^T M J (own terms)  -  sum_(o != o') G_o G_o'^T
+//        border (c, g):      sum_(o in c, g) w J_pose^T J_intr  -  sum_(o in c) G_o K_(t(o), g)^T
+//        intrinsic (g, g'):  sum_(o in g) w J_intr^T J_intr  -  sum_t K_(t,g) K_(t,g')^T
+//        rhs:                sum_o g_o - J^T Y q  (and the direct gradient sum_o g_o)
+//      (the own term J^T M J plus the observation's own G G^T is w J^T J).  No atomics; the
+//      result is deterministic.
+// On the FP32 path all products and sums of D run in float-float arithmetic (exact FMA product
+// residuals, two-sum accumulation): ~44 significant bits on the FP32 pipe, enough for reduced
+// matrices of condition ~1e9, where FP32 products alone leave the weakest modes indefinite.
+#include <cuda_runtime.h>
+
+#include "pb_device.cuh"
+#include "pb_kernels.h"
+
+namespace pb {
+
+namespace {
+
+template <typename T>
+__device__ __forceinline__ T* carve(char*& ptr, size_t count) {
+    T* out = reinterpret_cast<T*>(ptr);
+    ptr += (count * sizeof(T) + 15) & ~static_cast<size_t>(15);
+    return out;
+}
+
+constexpr int kOk = 1, kElim = 2;
+__device__ __forceinline__ int info_group(int info) { return ((info >> 2) & 7) - 1; }
+// per-observation track record: first observation (8 bits) | chunk track slot (8) | length (16)
+__device__ __forceinline__ int trk_first(int v) { return v & 0xFF; }
+__device__ __forceinline__ int trk_slot(int v) { return (v >> 8) & 0xFF; }
+__device__ __forceinline__ int trk_len(int v) { return v >> 16; }
+
+}  // namespace
+
+template <typename T>
+__global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT<T> O, double damping) {
+    using P = typename Acc<T>::part_type;
+    using Val = ValueOf<T>;
+    using VT = typename Val::type;
+    extern __shared__ __align__(16) char smem[];
+    const int chunk = blockIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const int MO = S.max_obs, MT = S.max_tracks;
+    const int ng = S.ng, ni = S.ni, nb = S.nb, nA = 6 + ni;
+    char* ptr = smem;
+    double* s_V = carve<double>(ptr, static_cast<size_t>(MO) * 9);
+    T* s_A = carve<T>(ptr, static_cast<size_t>(MO) * 2 * nA);
+    VT* s_G = carve<VT>(ptr, static_cast<size_t>(MO) * 18);
+    VT* s_Y = carve<VT>(ptr, static_cast<size_t>(MO) * 6);
+    VT* s_M = carve<VT>(ptr, static_cast<size_t>(MO) * 6);
+    VT* s_D = carve<VT>(ptr, static_cast<size_t>(MO) * nA);
+    int* s_info = carve<int>(ptr, MO);
+    int* s_trk = carve<int>(ptr, MO);
+    VT* s_K = carve<VT>(ptr, static_cast<size_t>(MT) * nb * 3);
+    int* s_tfirst = carve<int>(ptr, MT + 1);
+    double* s_misc = carve<double>(ptr, 40);
+    int* s_flags = reinterpret_cast<int*>(s_misc + 32);
+    int* s_wcount = reinterpret_cast<int*>(s_misc + 34);
+
+    const int obs0 = D.ch_obs_begin[chunk], nobs = D.ch_obs_begin[chunk + 1] - obs0;
+    if (tid == 0) s_flags[0] = 0;
+    __syncthreads();
+
+    // ---- A: linearise one observation per thread; FP64 point normal equations
+    const bool active = tid < nobs;
+    const int o = obs0 + tid;
+    Lin<T> L;
+    double grad[9 + kMaxNI];
+    double cost = 0.0;
+    int first = 0, k = 0;
+    bool elim = false, ok = false;
+    if (active) {
+        const int cam = D.obs_cam[o];
+        const int trk = D.obs_trk[o];
+        const int tb0 = D.trk_obs_begin[trk];
+        first = tb0 - obs0;
+        k = D.trk_obs_begin[trk + 1] - tb0;
+        elim = D.trk_block[trk] >= 0;
+        const int grp = ng > 0 ? D.cam_group[cam] : -1;
+        DCam c;
+        load_cam(D.cams_eff + static_cast<size_t>(cam) * kCamStride, c);
+        const double* X = D.points + static_cast<size_t>(trk) * 3;
+        const bool tangent = cam == S.gauge_scale && S.gauge_anchor >= 0 && S.gauge_baseline > 0.0;
+        ok = linearize_obs<T>(c, X[0], X[1], X[2], D.obs_u[o], D.obs_v[o], D.obs_w[o], S.loss, S.loss_scale, tangent,
+                              D.gauge_basis, ni, S.int_cols, true, L, grad);
+        if (!ok) {
+            atomicOr(s_flags, 2);
+        } else {
+            cost = L.cost;
+            O.obs_wn[o] = L.w;
+        }
+        s_info[tid] = (ok ? kOk : 0) | (elim ? kElim : 0) | ((grp + 1) << 2);
+        T* A = s_A + static_cast<size_t>(tid) * 2 * nA;
+        for (int a = 0; a < 6; ++a) {
+            A[a] = ok ? L.Jc[a] : T(0);
+            A[nA + a] = ok ? L.Jc[6 + a] : T(0);
+        }
+        for (int a = 0; a < ni; ++a) {
+            A[6 + a] = ok ? L.Ji[a] : T(0);
+            A[nA + 6 + a] = ok ? L.Ji[kMaxNI + a] : T(0);
+        }
+        // the observation's gradient -J^T w r (FP64): pose and intrinsic columns
+        VT* Dg = s_D + static_cast<size_t>(tid) * nA;
+        for (int a = 0; a < 6; ++a) Dg[a] = ok ? Val::make(grad[a]) : Val::zero();
+        for (int a = 0; a < ni; ++a) Dg[6 + a] = ok ? Val::make(grad[9 + a]) : Val::zero();
+        double* V = s_V + static_cast<size_t>(tid) * 9;
+        if (elim && ok) {
+            // V_o = w Jp^T Jp from the (rounded) Jacobian and the point gradient, in FP64
+            const double w = L.wd;
+            const double j0 = L.Jp[0], j1 = L.Jp[1], j2 = L.Jp[2], j3 = L.Jp[3], j4 = L.Jp[4], j5 = L.Jp[5];
+            V[0] = w * (j0 * j0 + j3 * j3);
+            V[1] = w * (j0 * j1 + j3 * j4);
+            V[2] = w * (j0 * j2 + j3 * j5);
+            V[3] = w * (j1 * j1 + j4 * j4);
+            V[4] = w * (j1 * j2 + j4 * j5);
+            V[5] = w * (j2 * j2 + j5 * j5);
+            V[6] = grad[6];
+            V[7] = grad[7];
+            V[8] = grad[8];
+        } else {
+            for (int i = 0; i < 9; ++i) V[i] = 0.0;
+        }
+    }
+    // chunk-local track slots: rank of each track's first observation among the chunk's
+    // track starts (all lanes of every warp take part: blockDim is a multiple of 32)
+    const bool start = active && tid == first;
+    const unsigned ballot = __ballot_sync(0xffffffffu, start);
+    if (lane == 0) s_wcount[wid] = __popc(ballot);
+    // block cost (FP64, fixed order)
+    const double cw = warp_sum(cost);
+    if (lane == 0) s_misc[wid] = cw;
+    __syncthreads();
+
+    // ---- B: track slots; per track FP64 Cholesky V(1+lambda) = R R^T.  R^-1 and q = R^-1 g_p
+    // replace the track's first record of s_V (only this thread reads them in this phase).
+    int ntc = 0, slot = 0;
+    for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w) {
+        if (w == wid) slot = ntc + __popc(ballot & ((1u << lane) - 1u));
+        ntc += s_wcount[w];
+    }
+    if (ntc > MT) {
+        // the host bounds the tracks of a chunk; a larger count would overrun s_K
+        if (tid == 0) atomicOr(s_flags, 4);
+        ntc = 0;
+    }
+    if (start) {
+        s_trk[tid] = first | (slot << 8) | (k << 16);
+        if (slot < MT) s_tfirst[slot] = tid;
+    }
+    if (tid == 0 && ntc <= MT) s_tfirst[ntc] = nobs;
+    if (start && elim) {
+        double V[6] = {0, 0, 0, 0, 0, 0}, rhs[3] = {0, 0, 0};
+        for (int j = 0; j < k; ++j) {
+            const double* v = s_V + static_cast<size_t>(first + j) * 9;
+            for (int i = 0; i < 6; ++i) V[i] += v[i];
+            for (int i = 0; i < 3; ++i) rhs[i] += v[6 + i];
+        }
+        V[0] *= 1.0 + damping;
+        V[3] *= 1.0 + damping;
+        V[5] *= 1.0 + damping;
+        // tryInverse3x3 singularity rule: |det| <= 1e-15
+        const double det = V[0] * (V[3] * V[5] - V[4] * V[4]) - V[1] * (V[1] * V[5] - V[4] * V[2]) +
+                           V[2] * (V[1] * V[4] - V[3] * V[2]);
+        double Ri[6] = {0, 0, 0, 0, 0, 0}, q[3] = {0, 0, 0};
+        bool singular = !(fabs(det) > 1e-15) || !isfinite(det);
+        if (!singular) {
+            const double R00 = sqrt(V[0]);
+            const double R10 = V[1] / R00, R20 = V[2] / R00;
+            const double a11 = V[3] - R10 * R10;
+            const double R11 = sqrt(a11);
+            const double R21 = (V[4] - R20 * R10) / R11;
+            const double a22 = V[5] - R20 * R20 - R21 * R21;
+            const double R22 = sqrt(a22);
+            if (!(V[0] > 0.0) || !(a11 > 0.0) || !(a22 > 0.0) || !isfinite(R22)) {
+                singular = true;
+            } else {
+                const double i00 = 1.0 / R00, i11 = 1.0 / R11, i22 = 1.0 / R22;
+                const double i10 = -R10 * i00 * i11;
+                const double i21 = -R21 * i11 * i22;
+                const double i20 = -(R20 * i00 + R21 * i10) * i22;
+                Ri[0] = i00; Ri[1] = i10; Ri[2] = i11; Ri[3] = i20; Ri[4] = i21; Ri[5] = i22;
+                q[0] = i00 * rhs[0];
+                q[1] = i10 * rhs[0] + i11 * rhs[1];
+                q[2] = i20 * rhs[0] + i21 * rhs[1] + i22 * rhs[2];
+            }
+        }
+        if (singular) atomicOr(s_flags, 1);
+        double* st = s_V + static_cast<size_t>(first) * 9;
+        double* gt = O.trk_data + static_cast<size_t>(D.obs_trk[o]) * kTrackRec;
+        for (int i = 0; i < 6; ++i) { st[i] = Ri[i]; gt[i] = Ri[i]; }
+        for (int i = 0; i < 3; ++i) {
+            st[6 + i] = q[i];
+            gt[6 + i] = q[i];
+            gt[9 + i] = rhs[i];
+        }
+    }
+    __syncthreads();
+
+    // ---- C: per observation, in FP64: Y = w Jp R^-T, M = w I - Y Y^T and Y q; then
+    // G = J_pose^T Y (values: float-float on the FP32 path; zero for tracks not eliminated)
+    if (active) {
+        if (!start) s_trk[tid] = s_trk[first];
+        VT* G = s_G + static_cast<size_t>(tid) * 18;
+        VT* Ys = s_Y + static_cast<size_t>(tid) * 6;
+        VT* Mo = s_M + static_cast<size_t>(tid) * 6;
+        if (ok) {
+            const double w = L.wd;
+            double Y[2][3] = {{0, 0, 0}, {0, 0, 0}}, q[3] = {0, 0, 0};
+            if (elim) {
+                const double* st = s_V + static_cast<size_t>(first) * 9;
+                const double i00 = st[0], i10 = st[1], i11 = st[2], i20 = st[3], i21 = st[4], i22 = st[5];
+                q[0] = st[6]; q[1] = st[7]; q[2] = st[8];
+                for (int pa = 0; pa < 2; ++pa) {
+                    const double p0 = L.Jp[pa * 3], p1 = L.Jp[pa * 3 + 1], p2 = L.Jp[pa * 3 + 2];
+                    Y[pa][0] = w * (i00 * p0);
+                    Y[pa][1] = w * (i10 * p0 + i11 * p1);
+                    Y[pa][2] = w * (i20 * p0 + i21 * p1 + i22 * p2);
+                }
+            }
+            Mo[0] = Val::make(w - (Y[0][0] * Y[0][0] + Y[0][1] * Y[0][1] + Y[0][2] * Y[0][2]));
+            Mo[1] = Val::make(-(Y[0][0] * Y[1][0] + Y[0][1] * Y[1][1] + Y[0][2] * Y[1][2]));
+            Mo[2] = Val::make(w - (Y[1][0] * Y[1][0] + Y[1][1] * Y[1][1] + Y[1][2] * Y[1][2]));
+            Mo[3] = Val::make(Y[0][0] * q[0] + Y[0][1] * q[1] + Y[0][2] * q[2]);
+            Mo[4] = Val::make(Y[1][0] * q[0] + Y[1][1] * q[1] + Y[1][2] * q[2]);
+            Mo[5] = Val::make(w);
+            VT y[6];
+            for (int i = 0; i < 6; ++i) {
+                y[i] = Val::make(Y[i / 3][i % 3]);
+                Ys[i] = y[i];
+            }
+            const T* A = s_A + static_cast<size_t>(tid) * 2 * nA;
+            for (int a = 0; a < 6; ++a) {
+                const T ja0 = A[a], ja1 = A[nA + a];
+                G[a * 3 + 0] = ja0 * y[0] + ja1 * y[3];
+                G[a * 3 + 1] = ja0 * y[1] + ja1 * y[4];
+                G[a * 3 + 2] = ja0 * y[2] + ja1 * y[5];
+            }
+        } else {
+            for (int i = 0; i < 6; ++i) Mo[i] = Val::zero();
+            for (int i = 0; i < 6; ++i) Ys[i] = Val::zero();
+            for (int i = 0; i < 18; ++i) G[i] = Val::zero();
+        }
+    }
+    __syncthreads();
+
+    // ---- K: per track and group, K[(g, c), k] = sum_(o in track, group g) (J_intr^T Y)[c, k]
+    if (nb > 0) {
+        const int per = nb * 3;
+        for (int it = tid; it < ntc * per; it += blockDim.x) {
+            const int t = it / per, r = it - t * per;
+            const int gc = r / 3, kk = r - gc * 3;
+            const int g = gc / ni, c = gc - g * ni;
+            VT acc = Val::zero();
+            for (int ob = s_tfirst[t]; ob < s_tfirst[t + 1]; ++ob) {
+                if (info_group(s_info[ob]) != g) continue;
+                const T* A = s_A + static_cast<size_t>(ob) * 2 * nA;
+                const VT* Y = s_Y + static_cast<size_t>(ob) * 6;
+                acc = acc + (A[6 + c] * Y[kk] + A[nA + 6 + c] * Y[3 + kk]);
+            }
+            s_K[it] = acc;
+        }
+        __syncthreads();
+    }
+
+    // ---- D: owner gathers over [pose block rows | camera rows | intrinsic entries]
+    const int pair0 = D.ch_pair_begin[chunk], npairs = D.ch_pair_begin[chunk + 1] - pair0;
+    const int cam0 = D.ch_cam_begin[chunk], ncams = D.ch_cam_begin[chunk + 1] - cam0;
+    const int camrec = 12 + ng * 6 * ni;
+    const int crow = 2 + ng * ni;  // rows of a camera record: rhs, direct rhs, border (g, c)
+    const int chrec = nb * nb + 2 * nb;
+    const int w_pair = npairs * 6, w_cam = ncams * crow;
+    const int w_total = w_pair + w_cam + chrec;
+    for (int wk = tid; wk < w_total; wk += blockDim.x) {
+        if (wk < w_pair) {
+            // row x of the pose block of chunk pair slot s
+            const int s = wk / 6, x = wk - s * 6;
+            const int pk = D.ch_pairs[pair0 + s];
+            const bool diag = (pk & 0xFFFF) == (pk >> 16);
+            Acc<T> acc[6];
+            const int i1 = D.slot_item_begin[pair0 + s + 1];
+            for (int it = D.slot_item_begin[pair0 + s]; it < i1; ++it) {
+                const unsigned item = D.slot_items[it];
+                const int oa = item & 0xFF, ob = item >> 8;
+                if (oa == ob) {
+                    // own term: row x of J^T M J
+                    const T* A = s_A + static_cast<size_t>(oa) * 2 * nA;
+                    const VT* M = s_M + static_cast<size_t>(oa) * 6;
+                    const T ax0 = A[x], ax1 = A[nA + x];
+                    const VT u0 = ax0 * M[0] + ax1 * M[1];
+                    const VT u1 = ax0 * M[1] + ax1 * M[2];
+#pragma unroll
+                    for (int y = 0; y < 6; ++y) {
+                        acc_fma(acc[y], A[y], u0);
+                        acc_fma(acc[y], A[nA + y], u1);
+                    }
+                } else {
+                    const VT* Ga = s_G + static_cast<size_t>(oa) * 18 + 3 * x;
+                    const VT* Gb = s_G + static_cast<size_t>(ob) * 18;
+                    const VT g0 = -Ga[0], g1 = -Ga[1], g2 = -Ga[2];
+#pragma unroll
+                    for (int y = 0; y < 6; ++y) {
+                        acc_fma(acc[y], g0, Gb[3 * y]);
+                        acc_fma(acc[y], g1, Gb[3 * y + 1]);
+                        acc_fma(acc[y], g2, Gb[3 * y + 2]);
+                    }
+                }
+            }
+            P* out = O.part_pair + static_cast<size_t>(pair0 + s) * 36;
+#pragma unroll
+            for (int y = 0; y < 6; ++y) {
+                if (!diag) {
+                    out[x * 6 + y] = acc[y].part();
+                } else if (y >= x) {
+                    out[x * 6 + y] = acc[y].part();
+                    out[y * 6 + x] = acc[y].part();
+                }
+            }
+        } else if (wk < w_pair + w_cam) {
+            const int r = wk - w_pair;
+            const int l = r / crow, row = r - l * crow;
+            const int b0 = D.lcam_obs_begin[cam0 + l], b1 = D.lcam_obs_begin[cam0 + l + 1];
+            P* out = O.part_cam + static_cast<size_t>(cam0 + l) * camrec;
+            Acc<T> acc[6];
+            if (row < 2) {
+                // gradient rows: the reduced gradient -J_pose^T (w r + Y q) and the direct
+                // gradient -J_pose^T w r (the point term with the rounded Jacobian)
+                for (int it = b0; it < b1; ++it) {
+                    const int ob = D.lcam_obs[it];
+                    const VT* Dg = s_D + static_cast<size_t>(ob) * nA;
+#pragma unroll
+                    for (int a = 0; a < 6; ++a) acc[a].add(Dg[a]);
+                    if (row == 0) {
+                        const T* A = s_A + static_cast<size_t>(ob) * 2 * nA;
+                        const VT* M = s_M + static_cast<size_t>(ob) * 6;
+                        const VT m0 = -M[3], m1 = -M[4];
+#pragma unroll
+                        for (int a = 0; a < 6; ++a) {
+                            acc_fma(acc[a], A[a], m0);
+                            acc_fma(acc[a], A[nA + a], m1);
+                        }
+                    }
+                }
+#pragma unroll
+                for (int a = 0; a < 6; ++a) out[row * 6 + a] = acc[a].part();
+            } else {
+                // border column (g, c2) of the camera's pose rows
+                const int gc = row - 2, g = gc / ni, c2 = gc - g * ni;
+                for (int it = b0; it < b1; ++it) {
+                    const int ob = D.lcam_obs[it];
+                    const int info = s_info[ob];
+                    const T* A = s_A + static_cast<size_t>(ob) * 2 * nA;
+                    if (info_group(info) == g) {
+                        const VT w = s_M[static_cast<size_t>(ob) * 6 + 5];
+                        const VT u0 = A[6 + c2] * w, u1 = A[nA + 6 + c2] * w;
+#pragma unroll
+                        for (int a = 0; a < 6; ++a) {
+                            acc_fma(acc[a], A[a], u0);
+                            acc_fma(acc[a], A[nA + a], u1);
+                        }
+                    }
+                    const int ts = trk_slot(s_trk[ob]);
+                    if ((info & kElim) && ts < ntc) {
+                        const VT* Kt = s_K + (static_cast<size_t>(ts) * nb + gc) * 3;
+                        const VT k0 = -Kt[0], k1 = -Kt[1], k2 = -Kt[2];
+                        const VT* Go = s_G + static_cast<size_t>(ob) * 18;
+#pragma unroll
+                        for (int a = 0; a < 6; ++a) {
+                            acc_fma(acc[a], Go[3 * a], k0);
+                            acc_fma(acc[a], Go[3 * a + 1], k1);
+                            acc_fma(acc[a], Go[3 * a + 2], k2);
+                        }
+                    }
+                }
+#pragma unroll
+                for (int a = 0; a < 6; ++a) out[12 + (g * 6 + a) * ni + c2] = acc[a].part();
+            }
+        } else {
+            // intrinsic block entry (i, j), i <= j, or an intrinsic gradient entry
+            const int e = wk - w_pair - w_cam;
+            P* out = O.part_chunk + static_cast<size_t>(chunk) * chrec;
+            Acc<T> acc;
+            if (e < nb * nb) {
+                const int i = e / nb, j = e - i * nb;
+                if (i > j) continue;
+                const int g1 = i / ni, c1 = i - g1 * ni, g2 = j / ni, c2 = j - g2 * ni;
+                if (g1 == g2) {
+                    for (int ob = 0; ob < nobs; ++ob) {
+                        if (info_group(s_info[ob]) != g1) continue;
+                        const T* A = s_A + static_cast<size_t>(ob) * 2 * nA;
+                        const VT w = s_M[static_cast<size_t>(ob) * 6 + 5];
+                        acc_fma(acc, w, two_prod(A[6 + c1], A[6 + c2]));
+                        acc_fma(acc, w, two_prod(A[nA + 6 + c1], A[nA + 6 + c2]));
+                    }
+                }
+                for (int t = 0; t < ntc; ++t) {
+                    const VT* K1 = s_K + (static_cast<size_t>(t) * nb + i) * 3;
+                    const VT* K2 = s_K + (static_cast<size_t>(t) * nb + j) * 3;
+                    acc_fma(acc, -K1[0], K2[0]);
+                    acc_fma(acc, -K1[1], K2[1]);
+                    acc_fma(acc, -K1[2], K2[2]);
+                }
+                out[e] = acc.part();
+                if (i != j) out[j * nb + i] = acc.part();
+            } else {
+                const int idx = e - nb * nb;
+                const bool reduced = idx < nb;
+                const int col = reduced ? idx : idx - nb;
+                const int g = col / ni, c = col - g * ni;
+                for (int ob = 0; ob < nobs; ++ob) {
+                    if (info_group(s_info[ob]) != g) continue;
+                    acc.add(s_D[static_cast<size_t>(ob) * nA + 6 + c]);
+                    if (reduced) {
+                        const T* A = s_A + static_cast<size_t>(ob) * 2 * nA;
+                        const VT* M = s_M + static_cast<size_t>(ob) * 6;
+                        acc_fma(acc, A[6 + c], -M[3]);
+                        acc_fma(acc, A[nA + 6 + c], -M[4]);
+                    }
+                }
+                out[e] = acc.part();
+            }
+        }
+    }
+    if (tid == 0) {
+        double c = 0.0;
+        for (int w = 0; w < static_cast<int>((blockDim.x + 31) >> 5); ++w) c += s_misc[w];
+        O.part_cost[chunk] = c;
+        O.part_flags[chunk] = s_flags[0];
+    }
+}
+
+template <typename T>
+static AsmOutT<T> typed_out(const AsmOut& o) {
+    using P = typename Acc<T>::part_type;
+    return {static_cast<P*>(o.part_pair_v), static_cast<P*>(o.part_cam_v), static_cast<P*>(o.part_chunk_v),
+            o.part_cost, o.part_flags, static_cast<double*>(o.trk_data_v), static_cast<T*>(o.obs_wn_v)};
+}
+
+template <typename T>
+void launch_assemble(const Shape& S, const DevPtrs& D, const AsmOut& O, double damping, size_t smem, cudaStream_t st) {
+    if (S.nchunks == 0) return;
+    k_assemble<T><<<S.nchunks, S.max_obs, smem, st>>>(S, D, typed_out<T>(O), damping);
+}
+
+void pb_set_assemble_smem_f32(size_t bytes) {
+    cudaFuncSetAttribute(k_assemble<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes));
+}
+void pb_set_assemble_smem_f64(size_t bytes) {
+    cudaFuncSetAttribute(k_assemble<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes));
+}
+
+template void launch_assemble<float>(const Shape&, const DevPtrs&, const AsmOut&, double, size_t, cudaStream_t);
+template void launch_assemble<double>(const Shape&, const DevPtrs&, const AsmOut&, double, size_t, cudaStream_t);
+
+}  // namespace pb

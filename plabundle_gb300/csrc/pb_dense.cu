@@ -10,6 +10,7 @@
 // factorisation positive definite; the FP64 CG recovers the FP64 solution (it plays the role of
 // iterative refinement).  On the FP64 path the factor is FP64 and CG converges in one or two
 // iterations.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include "pb_device.cuh"
@@ -297,24 +298,60 @@ __global__ void __launch_bounds__(256) k_transpose_lower(const T* __restrict__ X
     for (int e = threadIdx.x; e < TS * TS; e += blockDim.x) out[static_cast<size_t>(e / TS) * np + e % TS] = s[(e / TS) * TP + e % TS];
 }
 
-// ---- conjugate gradients on the FP64 reduced matrix, dense preconditioner M^-1 = D X^T X D
+// ---- conjugate gradients on the FP64 reduced matrix, dense preconditioner M^-1 = D X^T X D.
+// One cooperative persistent kernel runs the whole solve: per iteration the block-CSR SpMV (a
+// warp per pose block row or border row), x/r updates, the two triangular products of the
+// preconditioner (a warp per row) and the direction update, separated by five grid barriers.
+// Dot products go through per-block partials that every block sums in the same fixed order, so
+// all blocks take the same convergence / breakdown decision and no result depends on timing.
 namespace {
 constexpr int kCgThreads = 256;
 constexpr int kCgWarps = kCgThreads / 32;
+constexpr int kCgPart = 4;  // partial slots per block
 }  // namespace
 
-// out_i = so_i * sum_j M_ij * (si_j * in_j), j over the lower (j <= i) or upper (j >= i) triangle;
-// one warp per row.  With `dot_with` set, per-block partial sums of dot_with . out go to part.
-template <typename T, bool LOWER>
-__global__ void __launch_bounds__(kCgThreads) k_gemv_tri(const T* __restrict__ M, int np, int n,
-                                                         const double* __restrict__ in, const double* __restrict__ si,
-                                                         double* __restrict__ out, const double* __restrict__ so,
-                                                         const double* __restrict__ dot_with, double* __restrict__ part) {
-    __shared__ double s_part[kCgWarps];
+namespace cgk = cooperative_groups;
+
+// Block sum of v (all threads), written by thread 0 to *dst.
+__device__ __forceinline__ void block_partial(double v, double* s_red, double* dst) {
+    v = warp_sum(v);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int i = blockIdx.x * kCgWarps + warp;
+    if (lane == 0) s_red[warp] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < kCgWarps; ++w) t += s_red[w];
+        *dst = t;
+    }
+    __syncthreads();
+}
+
+// Sum over blocks of partial slot `slot`, identical in every block (fixed order: lane-strided
+// sums, then a fixed shuffle tree).
+__device__ __forceinline__ double grid_total(const double* part, int slot, double* s_red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (warp == 0) {
+        double v = 0.0;
+        for (int k = lane; k < static_cast<int>(gridDim.x); k += 32) v += part[k * kCgPart + slot];
+        v = warp_sum(v);
+        if (lane == 0) s_red[kCgWarps] = v;
+    }
+    __syncthreads();
+    const double t = s_red[kCgWarps];
+    __syncthreads();
+    return t;
+}
+
+// out_i = so_i * sum_j M_ij (si_j in_j), j <= i (LOWER) or j >= i; one warp per row, rows
+// interleaved over all warps of the grid; optional partial of dot_with . out.
+template <typename T, bool LOWER>
+__device__ __forceinline__ double tri_rows(const T* __restrict__ M, int np, int n, const double* __restrict__ in,
+                                           const double* __restrict__ si, double* __restrict__ out,
+                                           const double* __restrict__ so, const double* __restrict__ dot_with) {
+    const int lane = threadIdx.x & 31;
+    const int gw = blockIdx.x * kCgWarps + (threadIdx.x >> 5), nw = gridDim.x * kCgWarps;
     double contrib = 0.0;
-    if (i < n) {
+    for (int i = gw; i < n; i += nw) {
         const T* row = M + static_cast<size_t>(i) * np;
         const int j0 = LOWER ? 0 : i, j1 = LOWER ? i + 1 : n;
         T acc = T(0);
@@ -323,168 +360,143 @@ __global__ void __launch_bounds__(kCgThreads) k_gemv_tri(const T* __restrict__ M
         if (so) v *= so[i];
         if (lane == 0) {
             out[i] = v;
-            if (dot_with) contrib = dot_with[i] * v;
+            if (dot_with) contrib += dot_with[i] * v;
         }
     }
-    if (part) {
-        if (lane == 0) s_part[warp] = contrib;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double t = 0.0;
-            for (int w = 0; w < kCgWarps; ++w) t += s_part[w];
-            part[blockIdx.x] = t;
-        }
-    }
+    return contrib;
 }
 
-// q = S p for the pose rows (warp per block row) with per-block partials of p.q and B^T p.
-__global__ void __launch_bounds__(kCgThreads) k_cg_spmv_rows(PcgSystem<double> sys, const double* __restrict__ p,
-                                                             double* __restrict__ q, double* __restrict__ part) {
-    __shared__ double s_bt[kCgWarps][kMaxNB];
-    __shared__ double s_pq[kCgWarps];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int i = blockIdx.x * kCgWarps + warp;
-    const int nb = sys.nb, n6 = 6 * sys.ncb;
-    for (int c = lane; c < kMaxNB; c += 32) s_bt[warp][c] = 0.0;
-    double pq = 0.0;
-    if (i < sys.ncb) {
-        double acc[6] = {0, 0, 0, 0, 0, 0};
-        for (int e = sys.row_ptr[i] + lane; e < sys.row_ptr[i + 1]; e += 32) {
-            const int j = sys.col_idx[e];
-            const double* A = sys.vals + static_cast<size_t>(e) * 36;
-            double pj[6];
-            for (int c = 0; c < 6; ++c) pj[c] = p[6 * j + c];
-            for (int a = 0; a < 6; ++a)
-                for (int c = 0; c < 6; ++c) acc[a] = fma(A[a * 6 + c], pj[c], acc[a]);
-        }
-        const double* Bi = sys.border + static_cast<size_t>(i) * 6 * nb;
-        for (int c = lane; c < nb; c += 32)
-            for (int a = 0; a < 6; ++a) acc[a] = fma(Bi[a * nb + c], p[n6 + c], acc[a]);
-        for (int a = 0; a < 6; ++a) acc[a] = warp_sum(acc[a]);
-        if (lane < 6) {
-            double v = acc[0];
-            for (int a = 1; a < 6; ++a)
-                if (lane == a) v = acc[a];
-            q[6 * i + lane] = v;
-            pq = p[6 * i + lane] * v;
-        }
-        for (int c = lane; c < nb; c += 32) {
-            double s = 0.0;
-            for (int a = 0; a < 6; ++a) s = fma(Bi[a * nb + c], p[6 * i + a], s);
-            s_bt[warp][c] = s;
-        }
-    }
-    pq = warp_sum(pq);
-    if (lane == 0) s_pq[warp] = pq;
-    __syncthreads();
-    double* pb = part + static_cast<size_t>(blockIdx.x) * (1 + kMaxNB);
-    if (threadIdx.x == 0) {
-        double t = 0.0;
-        for (int w = 0; w < kCgWarps; ++w) t += s_pq[w];
-        pb[0] = t;
-    }
-    for (int c = threadIdx.x; c < nb; c += blockDim.x) {
-        double s = 0.0;
-        for (int w = 0; w < kCgWarps; ++w) s += s_bt[w][c];
-        pb[1 + c] = s;
-    }
-}
-
-// Border rows q_b = B^T p + C p_b and the total p.q (scal[0]); one block.
-__global__ void k_cg_spmv_border(PcgSystem<double> sys, const double* __restrict__ p, double* __restrict__ q,
-                                 const double* __restrict__ part, int nblk, double* __restrict__ scal) {
-    __shared__ double s_pq[256];
+// q = S p over the pose block rows and the border rows; returns this thread's share of p.q.
+__device__ __forceinline__ double spmv_rows(const PcgSystem<double>& sys, const double* __restrict__ p,
+                                            double* __restrict__ q) {
+    const int lane = threadIdx.x & 31;
+    const int gw = blockIdx.x * kCgWarps + (threadIdx.x >> 5), nw = gridDim.x * kCgWarps;
     const int nb = sys.nb, n6 = 6 * sys.ncb;
     double pq = 0.0;
-    if (threadIdx.x < nb) {
-        double v = 0.0;
-        for (int k = 0; k < nblk; ++k) v += part[static_cast<size_t>(k) * (1 + kMaxNB) + 1 + threadIdx.x];
-        for (int d = 0; d < nb; ++d) v = fma(sys.Cm[threadIdx.x * nb + d], p[n6 + d], v);
-        q[n6 + threadIdx.x] = v;
-        pq = p[n6 + threadIdx.x] * v;
-    }
-    for (int k = threadIdx.x; k < nblk; k += blockDim.x) pq += part[static_cast<size_t>(k) * (1 + kMaxNB)];
-    s_pq[threadIdx.x] = pq;
-    __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if (threadIdx.x < s) s_pq[threadIdx.x] += s_pq[threadIdx.x + s];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) scal[0] = s_pq[0];
-}
-
-// x += alpha p, r -= alpha q (alpha = rz / pq), per-block partials of r.r.
-__global__ void k_cg_axpy(double* __restrict__ x, double* __restrict__ r, const double* __restrict__ p,
-                          const double* __restrict__ q, int n, const double* __restrict__ scal, double* __restrict__ part) {
-    __shared__ double s_rr[256];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const double alpha = scal[1] / scal[0];
-    double rr = 0.0;
-    if (i < n) {
-        x[i] = fma(alpha, p[i], x[i]);
-        const double rv = fma(-alpha, q[i], r[i]);
-        r[i] = rv;
-        rr = rv * rv;
-    }
-    s_rr[threadIdx.x] = rr;
-    __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if (threadIdx.x < s) s_rr[threadIdx.x] += s_rr[threadIdx.x + s];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) part[blockIdx.x] = s_rr[0];
-}
-
-// Scalars after the preconditioner: scal[2] = r.z, scal[3] = r.r, scal[4] = beta, scal[1] = r.z.
-__global__ void k_cg_scalars(const double* __restrict__ part_rz, int nrz, const double* __restrict__ part_rr, int nrr,
-                             double* __restrict__ scal, int first) {
-    __shared__ double s_a[256], s_b[256];
-    double a = 0.0, b = 0.0;
-    for (int k = threadIdx.x; k < nrz; k += blockDim.x) a += part_rz[k];
-    for (int k = threadIdx.x; k < nrr; k += blockDim.x) b += part_rr[k];
-    s_a[threadIdx.x] = a;
-    s_b[threadIdx.x] = b;
-    __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if (threadIdx.x < s) {
-            s_a[threadIdx.x] += s_a[threadIdx.x + s];
-            s_b[threadIdx.x] += s_b[threadIdx.x + s];
+    for (int r = gw; r < sys.ncb + nb; r += nw) {
+        if (r < sys.ncb) {
+            double acc[6] = {0, 0, 0, 0, 0, 0};
+            for (int e = sys.row_ptr[r] + lane; e < sys.row_ptr[r + 1]; e += 32) {
+                const int j = sys.col_idx[e];
+                const double* A = sys.vals + static_cast<size_t>(e) * 36;
+                double pj[6];
+#pragma unroll
+                for (int c = 0; c < 6; ++c) pj[c] = p[6 * j + c];
+#pragma unroll
+                for (int a = 0; a < 6; ++a)
+#pragma unroll
+                    for (int c = 0; c < 6; ++c) acc[a] = fma(A[a * 6 + c], pj[c], acc[a]);
+            }
+            const double* Bi = sys.border + static_cast<size_t>(r) * 6 * nb;
+            for (int c = lane; c < nb; c += 32)
+#pragma unroll
+                for (int a = 0; a < 6; ++a) acc[a] = fma(Bi[a * nb + c], p[n6 + c], acc[a]);
+#pragma unroll
+            for (int a = 0; a < 6; ++a) acc[a] = warp_sum(acc[a]);
+            if (lane < 6) {
+                double v = acc[0];
+#pragma unroll
+                for (int a = 1; a < 6; ++a)
+                    if (lane == a) v = acc[a];
+                q[6 * r + lane] = v;
+                pq += p[6 * r + lane] * v;
+            }
+        } else {
+            const int c = r - sys.ncb;
+            double v = 0.0;
+            for (int k = lane; k < n6; k += 32) v = fma(sys.border[static_cast<size_t>(k) * nb + c], p[k], v);
+            for (int d = lane; d < nb; d += 32) v = fma(sys.Cm[c * nb + d], p[n6 + d], v);
+            v = warp_sum(v);
+            if (lane == 0) {
+                q[n6 + c] = v;
+                pq += p[n6 + c] * v;
+            }
         }
-        __syncthreads();
     }
-    if (threadIdx.x == 0) {
-        scal[2] = s_a[0];
-        scal[3] = s_b[0];
-        scal[4] = first ? 0.0 : s_a[0] / scal[1];
-        scal[1] = s_a[0];
-    }
+    return pq;
 }
 
-// p = z + beta p (beta = scal[4]); on the first iteration p = z.
-__global__ void k_cg_direction(double* __restrict__ p, const double* __restrict__ z, int n,
-                               const double* __restrict__ scal) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) p[i] = fma(scal[4], p[i], z[i]);
-}
-
-// r = b, x = 0, partials of b.b.
-__global__ void k_cg_init(double* __restrict__ x, double* __restrict__ r, const double* __restrict__ b, int n,
-                          double* __restrict__ part) {
-    __shared__ double s_rr[256];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double v = 0.0;
-    if (i < n) {
+// out: [0] iterations, [1] relative residual, [2] converged, [3] status (1: breakdown)
+template <typename T>
+__global__ void __launch_bounds__(kCgThreads) k_dense_cg(PcgSystem<double> sys, const T* __restrict__ X,
+                                                         const T* __restrict__ XT, int np,
+                                                         const double* __restrict__ dscale,
+                                                         const double* __restrict__ b, double* __restrict__ x,
+                                                         double* __restrict__ r, double* __restrict__ z,
+                                                         double* __restrict__ p, double* __restrict__ q,
+                                                         double* __restrict__ w, double* __restrict__ part,
+                                                         double* __restrict__ out, double rel_tol, double abs_tol,
+                                                         int max_it) {
+    cgk::grid_group grid = cgk::this_grid();
+    __shared__ double s_red[kCgWarps + 1];
+    const int n = 6 * sys.ncb + sys.nb;
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x, nt = gridDim.x * blockDim.x;
+    double* mypart = part + static_cast<size_t>(blockIdx.x) * kCgPart;
+    // r = b, x = 0; w = X D r
+    double bb = 0.0;
+    for (int i = gt; i < n; i += nt) {
         x[i] = 0.0;
         r[i] = b[i];
-        v = b[i] * b[i];
+        bb += b[i] * b[i];
     }
-    s_rr[threadIdx.x] = v;
-    __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if (threadIdx.x < s) s_rr[threadIdx.x] += s_rr[threadIdx.x + s];
-        __syncthreads();
+    block_partial(bb, s_red, mypart + 0);
+    grid.sync();
+    tri_rows<T, true>(X, np, n, b, dscale, w, nullptr, nullptr);
+    grid.sync();
+    block_partial(tri_rows<T, false>(XT, np, n, w, nullptr, z, dscale, b), s_red, mypart + 1);
+    grid.sync();
+    const double bnorm = sqrt(grid_total(part, 0, s_red));
+    double rz = grid_total(part, 1, s_red);
+    const double tol = fmax(rel_tol * bnorm, abs_tol);
+    for (int i = gt; i < n; i += nt) p[i] = z[i];
+    double rn = bnorm;
+    int it = 0, status = 0;
+    bool converged = rn <= tol;
+    grid.sync();
+    while (!converged && it < max_it) {
+        block_partial(spmv_rows(sys, p, q), s_red, mypart + 2);
+        grid.sync();
+        const double pq = grid_total(part, 2, s_red);
+        if (!(pq > 0.0) || !isfinite(pq) || !isfinite(rz)) {
+            status = 1;
+            break;
+        }
+        const double alpha = rz / pq;
+        double rr = 0.0;
+        for (int i = gt; i < n; i += nt) {
+            x[i] = fma(alpha, p[i], x[i]);
+            const double rv = fma(-alpha, q[i], r[i]);
+            r[i] = rv;
+            rr += rv * rv;
+        }
+        block_partial(rr, s_red, mypart + 0);
+        grid.sync();
+        ++it;
+        rn = sqrt(grid_total(part, 0, s_red));
+        if (!isfinite(rn)) {
+            status = 1;
+            break;
+        }
+        if (rn <= tol) {
+            converged = true;
+            break;
+        }
+        tri_rows<T, true>(X, np, n, r, dscale, w, nullptr, nullptr);
+        grid.sync();
+        block_partial(tri_rows<T, false>(XT, np, n, w, nullptr, z, dscale, r), s_red, mypart + 1);
+        grid.sync();
+        const double rz_new = grid_total(part, 1, s_red);
+        const double beta = rz_new / rz;
+        rz = rz_new;
+        for (int i = gt; i < n; i += nt) p[i] = fma(beta, p[i], z[i]);
+        grid.sync();
     }
-    if (threadIdx.x == 0) part[blockIdx.x] = s_rr[0];
+    if (gt == 0) {
+        out[0] = it;
+        out[1] = bnorm > 0.0 ? rn / bnorm : 0.0;
+        out[2] = converged ? 1.0 : 0.0;
+        out[3] = status;
+    }
 }
 
 // ---------------------------------------------------------------- host orchestration
@@ -558,62 +570,34 @@ template <typename T>
 int dense_pcg(const PcgSystem<double>& sys, DenseWork<T>& W, const double* b, double rel_tol, double abs_tol,
               int max_it, int* iterations, double* relres, bool* converged, double* h_scal, cudaStream_t st,
               int* launches) {
-    const int n = W.n, np = W.np;
-    const int nrow_blk = std::max(1, (sys.ncb + kCgWarps - 1) / kCgWarps);
-    const int nvec_blk = (n + 255) / 256;
-    const int ngemv_blk = (n + kCgWarps - 1) / kCgWarps;
-    double* part_spmv = W.part;
-    double* part_rr = part_spmv + static_cast<size_t>(nrow_blk) * (1 + kMaxNB);
-    double* part_rz = part_rr + nvec_blk;
-    int L = 0;
-    auto precondition = [&]() {
-        k_gemv_tri<T, true><<<ngemv_blk, kCgThreads, 0, st>>>(W.X, np, n, W.r, W.dscale, W.w, nullptr, nullptr, nullptr);
-        k_gemv_tri<T, false><<<ngemv_blk, kCgThreads, 0, st>>>(W.A, np, n, W.w, nullptr, W.z, W.dscale, W.r, part_rz);
-        L += 2;
-    };
-    k_cg_init<<<nvec_blk, 256, 0, st>>>(W.x, W.r, b, n, part_rr);
-    precondition();
-    k_cg_scalars<<<1, 256, 0, st>>>(part_rz, ngemv_blk, part_rr, nvec_blk, W.scal, 1);
-    cudaMemcpyAsync(W.p, W.z, n * sizeof(double), cudaMemcpyDeviceToDevice, st);
-    cudaMemcpyAsync(h_scal, W.scal, 8 * sizeof(double), cudaMemcpyDeviceToHost, st);
-    L += 2;
-    if (cudaStreamSynchronize(st) != cudaSuccess) return -1;
-    const double bnorm = std::sqrt(h_scal[3]);
-    const double tol = std::max(rel_tol * bnorm, abs_tol);
-    double rn = bnorm;
-    int it = 0;
-    *converged = rn <= tol;
-    int status = 0;
-    while (!*converged && it < max_it) {
-        k_cg_spmv_rows<<<nrow_blk, kCgThreads, 0, st>>>(sys, W.p, W.q, part_spmv);
-        k_cg_spmv_border<<<1, 256, 0, st>>>(sys, W.p, W.q, part_spmv, nrow_blk, W.scal);
-        k_cg_axpy<<<nvec_blk, 256, 0, st>>>(W.x, W.r, W.p, W.q, n, W.scal, part_rr);
-        precondition();
-        k_cg_scalars<<<1, 256, 0, st>>>(part_rz, ngemv_blk, part_rr, nvec_blk, W.scal, 0);
-        cudaMemcpyAsync(h_scal, W.scal, 8 * sizeof(double), cudaMemcpyDeviceToHost, st);
-        L += 4;
-        if (cudaStreamSynchronize(st) != cudaSuccess) return -1;
-        ++it;
-        if (!(h_scal[0] > 0.0) || !std::isfinite(h_scal[0]) || !std::isfinite(h_scal[3])) {
-            status = 1;
-            break;
-        }
-        rn = std::sqrt(h_scal[3]);
-        if (rn <= tol) {
-            *converged = true;
-            break;
-        }
-        k_cg_direction<<<nvec_blk, 256, 0, st>>>(W.p, W.z, n, W.scal);
-        ++L;
+    if (W.coop_grid == 0) {
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dense_cg<T>, kCgThreads, 0);
+        W.coop_grid = std::max(1, std::min(per_sm, 2) * sms);
     }
-    *iterations = it;
-    *relres = bnorm > 0 ? rn / bnorm : 0.0;
-    if (launches) *launches += L;
-    return status;
+    const int grid = W.coop_grid;
+    PcgSystem<double> s = sys;
+    const T* X = W.X;
+    const T* XT = W.A;
+    int np = W.np;
+    const double* dscale = W.dscale;
+    double rt = rel_tol, at = abs_tol;
+    int mi = max_it;
+    void* args[] = {&s, &X, &XT, &np, &dscale, &b, &W.x, &W.r, &W.z, &W.p, &W.q, &W.w, &W.part, &W.scal, &rt, &at, &mi};
+    const cudaError_t e = cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(&k_dense_cg<T>), dim3(grid),
+                                                      dim3(kCgThreads), args, 0, st);
+    if (e != cudaSuccess) return -1;
+    if (launches) *launches += 1;
+    cudaMemcpyAsync(h_scal, W.scal, 4 * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return -1;
+    *iterations = static_cast<int>(h_scal[0]);
+    *relres = h_scal[1];
+    *converged = h_scal[2] != 0.0;
+    return h_scal[3] != 0.0 ? 1 : 0;
 }
 
-template size_t dense_bytes<float>(int);
-template size_t dense_bytes<double>(int);
 template int dense_factor<float>(const PcgSystem<double>&, DenseWork<float>&, double, cudaStream_t, int*);
 template int dense_factor<double>(const PcgSystem<double>&, DenseWork<double>&, double, cudaStream_t, int*);
 template int dense_pcg<float>(const PcgSystem<double>&, DenseWork<float>&, const double*, double, double, int, int*,

@@ -38,7 +38,7 @@ __device__ __forceinline__ void load_cam(const double* __restrict__ c, DCam& k) 
 
 struct Proj {
     double px, py;       // pixel
-    double x, y, r2, radial, xd, yd, zc;
+    double x, y, r2, radial, xd, yd, zc, iz;
     double d0, d1, d2;   // X - C
 };
 
@@ -61,7 +61,7 @@ __device__ __forceinline__ bool project64(const DCam& c, double X0, double X1, d
     const double yd = y * radial + c.p1 * (r2 + 2.0 * y * y) + c.p2 * xy2;
     p.px = c.su * c.fx * xd + c.cx;
     p.py = c.sv * c.fy * yd + c.cy;
-    p.x = x; p.y = y; p.r2 = r2; p.radial = radial; p.xd = xd; p.yd = yd; p.zc = zc;
+    p.x = x; p.y = y; p.r2 = r2; p.radial = radial; p.xd = xd; p.yd = yd; p.zc = zc; p.iz = iz;
     return isfinite(p.px) && isfinite(p.py);
 }
 
@@ -101,13 +101,38 @@ struct Lin {
     double wd;          // normal weight (FP64)
 };
 
+// Intrinsic Jacobian column `col` of the parameter block [fx, log(fy/fx), cx, cy, k1, k2, k3, p1,
+// p2] (referenceIntrinsicParameterJacobian, BundleAdjustPlaMatrixProjection.cpp:228-262).
+template <typename U>
+__device__ __forceinline__ void intrinsic_column(int col, U x, U y, U r2, U xd, U yd, U su, U sv, U sfx, U sfy,
+                                                 U aspect, U& ju, U& jv) {
+    ju = U(0);
+    jv = U(0);
+    switch (col) {
+        case 0: ju = su * xd; jv = sv * yd * aspect; break;
+        case 1: jv = sfy * yd; break;
+        case 2: ju = U(1); break;
+        case 3: jv = U(1); break;
+        case 4: ju = sfx * x * r2; jv = sfy * y * r2; break;
+        case 5: ju = sfx * x * r2 * r2; jv = sfy * y * r2 * r2; break;
+        case 6: ju = sfx * x * r2 * r2 * r2; jv = sfy * y * r2 * r2 * r2; break;
+        case 7: ju = sfx * U(2) * x * y; jv = sfy * (r2 + U(2) * y * y); break;
+        case 8: ju = sfx * (r2 + U(2) * x * x); jv = sfy * U(2) * x * y; break;
+        default: break;
+    }
+}
+
 // Linearises one observation.  `tangent` selects the gauge tangent centre columns (basis: two
 // world-frame directions in gb[0..5]).  Returns false on an invalid projection or loss.
+// With `grad`, also writes the observation's gradient -J^T w r in FP64: pose [0, 6), point
+// [6, 9), intrinsic columns [9, 9 + ni).  On the FP64 path it comes from the FP64 Jacobian; on
+// the FP32 path from the FP64 projection through v = R (dpi/dx_c)^T (w r), so that the gradient
+// (and the fixed point of the mixed solve) does not carry the FP32 rounding of the Jacobian.
 template <typename T>
 __device__ __forceinline__ bool linearize_obs(const DCam& c, double X0, double X1, double X2, double u, double v,
                                               double wobs, int loss, double lscale, bool tangent,
                                               const double* __restrict__ gb, int ni, const int* __restrict__ cols,
-                                              bool want_jacobian, Lin<T>& L) {
+                                              bool want_jacobian, Lin<T>& L, double* grad = nullptr) {
     Proj p;
     if (!project64(c, X0, X1, X2, p)) return false;
     const double r0 = p.px - u, r1 = p.py - v;
@@ -132,7 +157,7 @@ __device__ __forceinline__ bool linearize_obs(const DCam& c, double X0, double X
     const T dxd_dy = T(2) * x * y * dr + T(2) * p1 * x + T(2) * p2 * y;
     const T dyd_dx = dxd_dy;
     const T dyd_dy = radial + T(2) * y * y * dr + T(6) * p1 * y + T(2) * p2 * x;
-    const T iz = static_cast<T>(1.0 / p.zc);
+    const T iz = static_cast<T>(p.iz);
     const T du_dx = sfx * dxd_dx, du_dy = sfx * dxd_dy, dv_dx = sfy * dyd_dx, dv_dy = sfy * dyd_dy;
     const T dc[6] = {du_dx * iz, du_dy * iz, -(du_dx * x + du_dy * y) * iz,
                      dv_dx * iz, dv_dy * iz, -(dv_dx * x + dv_dy * y) * iz};
@@ -140,7 +165,8 @@ __device__ __forceinline__ bool linearize_obs(const DCam& c, double X0, double X
 #pragma unroll
     for (int i = 0; i < 9; ++i) R[i] = static_cast<T>(c.R[i]);
     const T d0 = static_cast<T>(p.d0), d1 = static_cast<T>(p.d1), d2 = static_cast<T>(p.d2);
-    const T s = static_cast<T>(point_scale(X0, X1, X2));
+    const double s64 = point_scale(X0, X1, X2);
+    const T s = static_cast<T>(s64);
 #pragma unroll
     for (int pa = 0; pa < 2; ++pa) {
         // world point Jacobian: dpi/dXw = dpi/dxc * R^T
@@ -164,26 +190,57 @@ __device__ __forceinline__ bool linearize_obs(const DCam& c, double X0, double X
         L.Jp[pa * 3 + 1] = jw1 * s;
         L.Jp[pa * 3 + 2] = jw2 * s;
     }
-    if (ni > 0) {
-        const T xd = static_cast<T>(p.xd), yd = static_cast<T>(p.yd);
-        const T aspect = static_cast<T>(c.fx > 0.0 ? c.fy / c.fx : 1.0);
-        const T su = static_cast<T>(c.su), sv = static_cast<T>(c.sv);
-        for (int k = 0; k < ni; ++k) {
-            T ju = T(0), jv = T(0);
-            switch (cols[k]) {
-                case 0: ju = su * xd; jv = sv * yd * aspect; break;
-                case 1: ju = T(0); jv = sfy * yd; break;
-                case 2: ju = T(1); jv = T(0); break;
-                case 3: ju = T(0); jv = T(1); break;
-                case 4: ju = sfx * x * r2; jv = sfy * y * r2; break;
-                case 5: ju = sfx * x * r2 * r2; jv = sfy * y * r2 * r2; break;
-                case 6: ju = sfx * x * r2 * r2 * r2; jv = sfy * y * r2 * r2 * r2; break;
-                case 7: ju = sfx * T(2) * x * y; jv = sfy * (r2 + T(2) * y * y); break;
-                case 8: ju = sfx * (r2 + T(2) * x * x); jv = sfy * T(2) * x * y; break;
-                default: break;
+    const T xd = static_cast<T>(p.xd), yd = static_cast<T>(p.yd);
+    const T aspect = static_cast<T>(c.fx > 0.0 ? c.fy / c.fx : 1.0);
+    const T su = static_cast<T>(c.su), sv = static_cast<T>(c.sv);
+    for (int k = 0; k < ni; ++k) intrinsic_column<T>(cols[k], x, y, r2, xd, yd, su, sv, sfx, sfy, aspect, L.Ji[k],
+                                                     L.Ji[kMaxNI + k]);
+    if (grad) {
+        const double w = L.wd;
+        if (sizeof(T) == sizeof(double)) {
+            for (int a = 0; a < 6; ++a)
+                grad[a] = -w * (static_cast<double>(L.Jc[a]) * r0 + static_cast<double>(L.Jc[6 + a]) * r1);
+            for (int a = 0; a < 3; ++a)
+                grad[6 + a] = -w * (static_cast<double>(L.Jp[a]) * r0 + static_cast<double>(L.Jp[3 + a]) * r1);
+            for (int a = 0; a < ni; ++a)
+                grad[9 + a] = -w * (static_cast<double>(L.Ji[a]) * r0 + static_cast<double>(L.Ji[kMaxNI + a]) * r1);
+        } else {
+            const double wr0 = w * r0, wr1 = w * r1;
+            const double gx = p.x, gy = p.y, gr2 = p.r2;
+            const double gdr = c.k1 + gr2 * (2.0 * c.k2 + 3.0 * c.k3 * gr2);
+            const double gxx = p.radial + 2.0 * gx * gx * gdr + 2.0 * c.p1 * gy + 6.0 * c.p2 * gx;
+            const double gxy = 2.0 * gx * gy * gdr + 2.0 * c.p1 * gx + 2.0 * c.p2 * gy;
+            const double gyy = p.radial + 2.0 * gy * gy * gdr + 6.0 * c.p1 * gy + 2.0 * c.p2 * gx;
+            const double gsfx = c.su * c.fx, gsfy = c.sv * c.fy;
+            const double a0 = gsfx * wr0, a1 = gsfy * wr1;
+            // t = (dpi/dx_c)^T (w r); v = R t is J_world^T (w r)
+            const double tx = (a0 * gxx + a1 * gxy) * p.iz;
+            const double ty = (a0 * gxy + a1 * gyy) * p.iz;
+            const double tz = -(tx * gx + ty * gy);
+            const double v0 = c.R[0] * tx + c.R[1] * ty + c.R[2] * tz;
+            const double v1 = c.R[3] * tx + c.R[4] * ty + c.R[5] * tz;
+            const double v2 = c.R[6] * tx + c.R[7] * ty + c.R[8] * tz;
+            grad[0] = -(v2 * p.d1 - v1 * p.d2);
+            grad[1] = -(v2 * p.d0 - v0 * p.d2);
+            grad[2] = -(v0 * p.d1 - v1 * p.d0);
+            if (tangent) {
+                grad[3] = v0 * gb[0] + v1 * gb[1] + v2 * gb[2];
+                grad[4] = v0 * gb[3] + v1 * gb[4] + v2 * gb[5];
+                grad[5] = 0.0;
+            } else {
+                grad[3] = v0;
+                grad[4] = v1;
+                grad[5] = v2;
             }
-            L.Ji[k] = ju;
-            L.Ji[kMaxNI + k] = jv;
+            grad[6] = -s64 * v0;
+            grad[7] = -s64 * v1;
+            grad[8] = -s64 * v2;
+            const double gaspect = c.fx > 0.0 ? c.fy / c.fx : 1.0;
+            for (int k = 0; k < ni; ++k) {
+                double ju, jv;
+                intrinsic_column<double>(cols[k], gx, gy, gr2, p.xd, p.yd, c.su, c.sv, gsfx, gsfy, gaspect, ju, jv);
+                grad[9 + k] = -(ju * wr0 + jv * wr1);
+            }
         }
     }
     return true;
@@ -293,6 +350,32 @@ struct Acc<float> {
     }
     __device__ __forceinline__ float2 part() const { return make_float2(hi, lo); }
 };
+
+// acc += a * b, the product's rounding error carried into the compensation term (FP32 path) /
+// one FMA (FP64 path).
+__device__ __forceinline__ void acc_fma(Acc<float>& acc, ff a, ff b) {
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = fmaf(a.hi, b.hi, -p);
+    e = fmaf(a.hi, b.lo, e);
+    e = fmaf(a.lo, b.hi, e);
+    acc.add(p);
+    acc.lo += e;
+}
+__device__ __forceinline__ void acc_fma(Acc<float>& acc, float a, ff b) {
+    const float p = __fmul_rn(a, b.hi);
+    float e = fmaf(a, b.hi, -p);
+    e = fmaf(a, b.lo, e);
+    acc.add(p);
+    acc.lo += e;
+}
+__device__ __forceinline__ void acc_fma(Acc<double>& acc, double a, double b) { acc.s = fma(a, b, acc.s); }
+
+// exact product of two floats as a float-float
+__device__ __forceinline__ ff two_prod(float a, float b) {
+    const float p = __fmul_rn(a, b);
+    return {p, fmaf(a, b, -p)};
+}
+__device__ __forceinline__ double two_prod(double a, double b) { return a * b; }
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll

@@ -409,19 +409,23 @@ int build_host_model(const pb_problem_desc* pr, const pb_solve_options* op, Host
     return 0;
 }
 
-size_t chunk_smem_bytes(int precision, int max_obs, int ni) {
+size_t chunk_smem_bytes(int precision, int max_obs, int max_tracks, int ni, int nb) {
     const size_t ts = precision == PB_PRECISION_FP64 ? 8 : 4;  // Jacobian storage
     const size_t vs = 8;                                        // double / float-float values
     const size_t nA = 6 + static_cast<size_t>(ni);
-    const size_t mo = static_cast<size_t>(max_obs);
+    const size_t mo = static_cast<size_t>(max_obs), mt = static_cast<size_t>(max_tracks);
     auto al = [](size_t v) { return (v + 15) & ~static_cast<size_t>(15); };
     size_t s = 0;
-    s += al(mo * 9 * 8);       // point normal equations per observation, then the track factor (FP64)
-    s += al(mo * 2 * nA * ts); // A_o = [J_pose | J_intrinsic]
-    s += al(mo * 3 * nA * vs); // G_o = A_o^T Y_o
-    s += al(mo * 7 * vs);      // reduced weight M_o, reduced residual M r_o, w r_o
-    s += al(mo * 4) * 2;       // observation flags, track ranges
-    s += al(40 * 8);           // warp partial costs, flags
+    s += al(mo * 9 * 8);        // point normal equations per observation, then the track factor (FP64)
+    s += al(mo * 2 * nA * ts);  // A_o = [J_pose | J_intrinsic]
+    s += al(mo * 18 * vs);      // G_o = J_pose^T Y_o
+    s += al(mo * 6 * vs);       // Y_o
+    s += al(mo * 6 * vs);       // M_o, Y_o q, w
+    s += al(mo * nA * vs);      // gradient -J^T w r of the pose and intrinsic columns
+    s += al(mo * 4) * 2;        // observation flags, track records
+    s += al(mt * static_cast<size_t>(nb) * 3 * vs);  // per-track K
+    s += al((mt + 1) * 4);      // track starts
+    s += al(40 * 8);            // warp partial costs and track counts, flags
     return s;
 }
 
@@ -433,11 +437,16 @@ int build_chunks(HostModel* m, int precision, size_t smem_budget, std::string* e
     // two CTAs per SM: at most half of the 228 KB of shared memory of an SM each, less the
     // 1 KB the runtime reserves per CTA
     const size_t per_cta = std::min(smem_budget, static_cast<size_t>(113 * 1024));
+    const int nb = m->ng * m->ni;
     int max_obs = 256;
     const int max_cams = 254;
     const int max_pairs = 1 << 15;
-    while (chunk_smem_bytes(precision, max_obs, m->ni) > per_cta && max_obs > 32) max_obs -= 32;
-    if (chunk_smem_bytes(precision, max_obs, m->ni) > per_cta) {
+    // tracks of a chunk: per-track intrinsic sums in shared memory; a quarter of the observations
+    // (tracks of four or more views fill a chunk, shorter ones close it early)
+    auto tracks_for = [](int mo) { return std::max(8, mo / 4); };
+    while (chunk_smem_bytes(precision, max_obs, tracks_for(max_obs), m->ni, nb) > per_cta && max_obs > 32) max_obs -= 32;
+    const int max_tracks = tracks_for(max_obs);
+    if (chunk_smem_bytes(precision, max_obs, max_tracks, m->ni, nb) > per_cta) {
         *err = "assembly chunk does not fit in shared memory";
         return PB_SOLVE_UNSUPPORTED;
     }
@@ -445,6 +454,7 @@ int build_chunks(HostModel* m, int precision, size_t smem_budget, std::string* e
     cs.max_obs = max_obs;
     cs.max_cams = max_cams;
     cs.max_pairs = max_pairs;
+    cs.max_tracks = max_tracks;
     const int ntp = static_cast<int>(m->trk_order.size());
     cs.obs_lcam.assign(m->p_obs_orig.size(), 255);
     std::vector<int> stamp(m->nc, -1), local(m->nc, -1);
@@ -604,7 +614,8 @@ int build_chunks(HostModel* m, int precision, size_t smem_budget, std::string* e
             }
             const int obs_after = o1 - chunk_obs_start;
             const bool fits = obs_after <= max_obs && ncams_after <= max_cams &&
-                              static_cast<int>(cpairs.size()) + new_pairs <= max_pairs;
+                              static_cast<int>(cpairs.size()) + new_pairs <= max_pairs &&
+                              p - chunk_trk_start + 1 <= max_tracks;
             if (!fits) {
                 if (attempt == 0 && o0 > chunk_obs_start) {
                     for (auto& q : cpairs) pair_seen[static_cast<size_t>(q.first) * max_cams + q.second] = 0;

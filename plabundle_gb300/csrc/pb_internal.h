@@ -35,7 +35,7 @@ struct Shape {
     int gauge_anchor, gauge_scale;
     double gauge_baseline;
     int int_cols[kMaxNI];
-    int max_obs, max_cams, max_pairs;  // chunk limits of the active chunk set
+    int max_obs, max_cams, max_pairs, max_tracks;  // chunk limits of the active chunk set
 };
 
 struct DevPtrs {
@@ -102,7 +102,7 @@ struct HostGroup {
 };
 
 struct ChunkSet {
-    int max_obs = 0, max_cams = 0, max_pairs = 0;
+    int max_obs = 0, max_cams = 0, max_pairs = 0, max_tracks = 0;
     std::vector<int> obs_begin, cam_begin, cams, pair_begin, pairs, pair_upper;
     std::vector<unsigned char> obs_lcam;
     std::vector<int> slot_item_begin, lcam_obs_begin;
@@ -149,7 +149,7 @@ struct HostModel {
 // pb_host.cpp
 int build_host_model(const pb_problem_desc* pr, const pb_solve_options* op, HostModel* m, std::string* err);
 int build_chunks(HostModel* m, int precision, size_t smem_budget, std::string* err);
-size_t chunk_smem_bytes(int precision, int max_obs, int ni);
+size_t chunk_smem_bytes(int precision, int max_obs, int max_tracks, int ni, int nb);
 double finite_median(std::vector<double> v, double fallback);
 void camera_parameter_block(const double* cam, double* p);
 

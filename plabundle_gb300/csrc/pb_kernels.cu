@@ -1,19 +1,9 @@
-// pb_kernels.cu -- assembly, reduction, back-substitution, objective and state-update kernels.
+// pb_kernels.cu -- reduction of the assembly partials, back-substitution, objective and
+// state-update kernels (the assembly kernel itself is in pb_assemble.cu).
 //
-// Kernels (a)+(b) `k_assemble`: one CTA per chunk of consecutive tracks (host-built, at most
-// max_obs observations), one thread per observation.
-//   A. linearise the observation (FP64 residual and robust weight, Jacobians in T);
-//   B. per track, the 3x3 point system V = sum w Jp^T Jp (FP64) and its factor V = R R^T;
-//   C. per observation, in FP64: Y = w Jp R^-T (2x3), the reduced weight M = w I - Y Y^T and the
-//      reduced residual M r = w r + Y q (q = R^-1 g_p); then G = A^T Y with A = [J_pose | J_intr]
-//      in T.  The point elimination of a track (BundleAdjustPlaMatrixReferenceSchur.cpp:350-490)
-//      is then  S_track = sum_o A_o^T M_o A_o - sum_(o != o') G_o G_o'^T,  so the cancellation
-//      between the direct and the Schur terms of an observation is done in FP64, once;
-//   D. every output element of the chunk (pose-pair entry, camera rhs / border entry, intrinsic
-//      block entry) is owned by one thread, which gathers its terms over host-built item lists
-//      in a fixed order into an Acc<T> (two-sum compensated on the FP32 path) and writes the
-//      chunk partial once.  No shared-memory or global atomics; results are deterministic.
-// `k_reduce_*` then sum the partials of each reduced block in a fixed order.
+// `k_reduce_*` sum the chunk partials of every reduced block in a fixed order, with the
+// accumulator of the arithmetic path (two-sum compensated float-float on the FP32 path), so the
+// reduced matrix is assembled without atomics and reproducibly.
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
@@ -21,337 +11,6 @@
 #include "pb_kernels.h"
 
 namespace pb {
-
-namespace {
-
-template <typename T>
-__device__ __forceinline__ T* carve(char*& ptr, size_t count) {
-    T* out = reinterpret_cast<T*>(ptr);
-    ptr += (count * sizeof(T) + 15) & ~static_cast<size_t>(15);
-    return out;
-}
-
-// observation flags in shared memory
-constexpr int kOk = 1, kElim = 2;
-__device__ __forceinline__ int info_group(int info) { return ((info >> 2) & 7) - 1; }
-
-}  // namespace
-
-template <typename T>
-__global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT<T> O, double damping) {
-    using P = typename Acc<T>::part_type;
-    using Val = ValueOf<T>;
-    using VT = typename Val::type;
-    extern __shared__ __align__(16) char smem[];
-    const int chunk = blockIdx.x;
-    const int tid = threadIdx.x;
-    const int MO = S.max_obs;
-    const int ng = S.ng, ni = S.ni, nb = S.nb, nA = 6 + ni;
-    char* ptr = smem;
-    double* s_V = carve<double>(ptr, static_cast<size_t>(MO) * 9);
-    T* s_A = carve<T>(ptr, static_cast<size_t>(MO) * 2 * nA);
-    VT* s_G = carve<VT>(ptr, static_cast<size_t>(MO) * 3 * nA);
-    VT* s_M = carve<VT>(ptr, static_cast<size_t>(MO) * 7);
-    int* s_info = carve<int>(ptr, MO);
-    int* s_trk = carve<int>(ptr, MO);
-    double* s_misc = carve<double>(ptr, 40);
-    int* s_flags = reinterpret_cast<int*>(s_misc + 32);
-
-    const int obs0 = D.ch_obs_begin[chunk], nobs = D.ch_obs_begin[chunk + 1] - obs0;
-    if (tid == 0) s_flags[0] = 0;
-    __syncthreads();
-
-    // ---- A: linearise one observation per thread; FP64 point normal equations
-    const bool active = tid < nobs;
-    const int o = obs0 + tid;
-    Lin<T> L;
-    double cost = 0.0;
-    int first = 0;
-    bool elim = false, ok = false;
-    if (active) {
-        const int cam = D.obs_cam[o];
-        const int trk = D.obs_trk[o];
-        const int tb0 = D.trk_obs_begin[trk];
-        first = tb0 - obs0;
-        const int k = D.trk_obs_begin[trk + 1] - tb0;
-        elim = D.trk_block[trk] >= 0;
-        const int grp = ng > 0 ? D.cam_group[cam] : -1;
-        DCam c;
-        load_cam(D.cams_eff + static_cast<size_t>(cam) * kCamStride, c);
-        const double* X = D.points + static_cast<size_t>(trk) * 3;
-        const bool tangent = cam == S.gauge_scale && S.gauge_anchor >= 0 && S.gauge_baseline > 0.0;
-        ok = linearize_obs<T>(c, X[0], X[1], X[2], D.obs_u[o], D.obs_v[o], D.obs_w[o], S.loss, S.loss_scale, tangent,
-                              D.gauge_basis, ni, S.int_cols, true, L);
-        if (!ok) {
-            atomicOr(s_flags, 2);
-        } else {
-            cost = L.cost;
-            O.obs_wn[o] = L.w;
-        }
-        s_info[tid] = (ok ? kOk : 0) | (elim ? kElim : 0) | ((grp + 1) << 2);
-        s_trk[tid] = first | (k << 16);
-        T* A = s_A + static_cast<size_t>(tid) * 2 * nA;
-        for (int a = 0; a < 6; ++a) {
-            A[a] = ok ? L.Jc[a] : T(0);
-            A[nA + a] = ok ? L.Jc[6 + a] : T(0);
-        }
-        for (int a = 0; a < ni; ++a) {
-            A[6 + a] = ok ? L.Ji[a] : T(0);
-            A[nA + 6 + a] = ok ? L.Ji[kMaxNI + a] : T(0);
-        }
-        double* V = s_V + static_cast<size_t>(tid) * 9;
-        if (elim && ok) {
-            // V_o = w Jp^T Jp and g_o = -w Jp^T r from the (rounded) Jacobian, in FP64
-            const double w = L.wd;
-            const double j0 = L.Jp[0], j1 = L.Jp[1], j2 = L.Jp[2], j3 = L.Jp[3], j4 = L.Jp[4], j5 = L.Jp[5];
-            V[0] = w * (j0 * j0 + j3 * j3);
-            V[1] = w * (j0 * j1 + j3 * j4);
-            V[2] = w * (j0 * j2 + j3 * j5);
-            V[3] = w * (j1 * j1 + j4 * j4);
-            V[4] = w * (j1 * j2 + j4 * j5);
-            V[5] = w * (j2 * j2 + j5 * j5);
-            V[6] = -w * (j0 * L.rd0 + j3 * L.rd1);
-            V[7] = -w * (j1 * L.rd0 + j4 * L.rd1);
-            V[8] = -w * (j2 * L.rd0 + j5 * L.rd1);
-        } else {
-            for (int i = 0; i < 9; ++i) V[i] = 0.0;
-        }
-    }
-    __syncthreads();
-
-    // ---- B: per track, FP64 Cholesky V(1+lambda) = R R^T; R^-1 and q = R^-1 g_p replace the
-    // track's first record of s_V (only this thread reads the track's records in this phase)
-    if (active && elim && tid == first) {
-        const int k = s_trk[tid] >> 16;
-        double V[6] = {0, 0, 0, 0, 0, 0}, rhs[3] = {0, 0, 0};
-        for (int j = 0; j < k; ++j) {
-            const double* v = s_V + static_cast<size_t>(first + j) * 9;
-            for (int i = 0; i < 6; ++i) V[i] += v[i];
-            for (int i = 0; i < 3; ++i) rhs[i] += v[6 + i];
-        }
-        V[0] *= 1.0 + damping;
-        V[3] *= 1.0 + damping;
-        V[5] *= 1.0 + damping;
-        // tryInverse3x3 singularity rule: |det| <= 1e-15
-        const double det = V[0] * (V[3] * V[5] - V[4] * V[4]) - V[1] * (V[1] * V[5] - V[4] * V[2]) +
-                           V[2] * (V[1] * V[4] - V[3] * V[2]);
-        double Ri[6] = {0, 0, 0, 0, 0, 0}, q[3] = {0, 0, 0};
-        bool singular = !(fabs(det) > 1e-15) || !isfinite(det);
-        if (!singular) {
-            const double R00 = sqrt(V[0]);
-            const double R10 = V[1] / R00, R20 = V[2] / R00;
-            const double a11 = V[3] - R10 * R10;
-            const double R11 = sqrt(a11);
-            const double R21 = (V[4] - R20 * R10) / R11;
-            const double a22 = V[5] - R20 * R20 - R21 * R21;
-            const double R22 = sqrt(a22);
-            if (!(V[0] > 0.0) || !(a11 > 0.0) || !(a22 > 0.0) || !isfinite(R22)) {
-                singular = true;
-            } else {
-                const double i00 = 1.0 / R00, i11 = 1.0 / R11, i22 = 1.0 / R22;
-                const double i10 = -R10 * i00 * i11;
-                const double i21 = -R21 * i11 * i22;
-                const double i20 = -(R20 * i00 + R21 * i10) * i22;
-                Ri[0] = i00; Ri[1] = i10; Ri[2] = i11; Ri[3] = i20; Ri[4] = i21; Ri[5] = i22;
-                q[0] = i00 * rhs[0];
-                q[1] = i10 * rhs[0] + i11 * rhs[1];
-                q[2] = i20 * rhs[0] + i21 * rhs[1] + i22 * rhs[2];
-            }
-        }
-        if (singular) atomicOr(s_flags, 1);
-        double* st = s_V + static_cast<size_t>(first) * 9;
-        double* gt = O.trk_data + static_cast<size_t>(D.obs_trk[o]) * kTrackRec;
-        for (int i = 0; i < 6; ++i) { st[i] = Ri[i]; gt[i] = Ri[i]; }
-        for (int i = 0; i < 3; ++i) {
-            st[6 + i] = q[i];
-            gt[6 + i] = q[i];
-            gt[9 + i] = rhs[i];
-        }
-    }
-    __syncthreads();
-
-    // ---- C: per observation, in FP64: Y = w Jp R^-T, M = w I - Y Y^T, M r = w r + Y q; then
-    // G = A^T Y.  All from the rounded Jacobians A, Jp, so that the reduced system is the exact
-    // Schur complement of one (slightly perturbed) linearisation; values are float-float on the
-    // FP32 path (zero for observations of tracks that are not eliminated).
-    if (active) {
-        VT* G = s_G + static_cast<size_t>(tid) * 3 * nA;
-        VT* Mo = s_M + static_cast<size_t>(tid) * 7;
-        if (ok) {
-            const double w = L.wd;
-            double Y[2][3] = {{0, 0, 0}, {0, 0, 0}}, q[3] = {0, 0, 0};
-            if (elim) {
-                const double* st = s_V + static_cast<size_t>(first) * 9;
-                const double i00 = st[0], i10 = st[1], i11 = st[2], i20 = st[3], i21 = st[4], i22 = st[5];
-                q[0] = st[6]; q[1] = st[7]; q[2] = st[8];
-                for (int pa = 0; pa < 2; ++pa) {
-                    const double p0 = L.Jp[pa * 3], p1 = L.Jp[pa * 3 + 1], p2 = L.Jp[pa * 3 + 2];
-                    Y[pa][0] = w * (i00 * p0);
-                    Y[pa][1] = w * (i10 * p0 + i11 * p1);
-                    Y[pa][2] = w * (i20 * p0 + i21 * p1 + i22 * p2);
-                }
-            }
-            Mo[0] = Val::make(w - (Y[0][0] * Y[0][0] + Y[0][1] * Y[0][1] + Y[0][2] * Y[0][2]));
-            Mo[1] = Val::make(-(Y[0][0] * Y[1][0] + Y[0][1] * Y[1][1] + Y[0][2] * Y[1][2]));
-            Mo[2] = Val::make(w - (Y[1][0] * Y[1][0] + Y[1][1] * Y[1][1] + Y[1][2] * Y[1][2]));
-            Mo[3] = Val::make(w * L.rd0 + (Y[0][0] * q[0] + Y[0][1] * q[1] + Y[0][2] * q[2]));
-            Mo[4] = Val::make(w * L.rd1 + (Y[1][0] * q[0] + Y[1][1] * q[1] + Y[1][2] * q[2]));
-            Mo[5] = Val::make(w * L.rd0);
-            Mo[6] = Val::make(w * L.rd1);
-            const VT y00 = Val::make(Y[0][0]), y01 = Val::make(Y[0][1]), y02 = Val::make(Y[0][2]);
-            const VT y10 = Val::make(Y[1][0]), y11 = Val::make(Y[1][1]), y12 = Val::make(Y[1][2]);
-            const T* A = s_A + static_cast<size_t>(tid) * 2 * nA;
-            for (int a = 0; a < nA; ++a) {
-                const T ja0 = A[a], ja1 = A[nA + a];
-                G[a * 3 + 0] = ja0 * y00 + ja1 * y10;
-                G[a * 3 + 1] = ja0 * y01 + ja1 * y11;
-                G[a * 3 + 2] = ja0 * y02 + ja1 * y12;
-            }
-        } else {
-            for (int i = 0; i < 7; ++i) Mo[i] = Val::zero();
-            for (int i = 0; i < 3 * nA; ++i) G[i] = Val::zero();
-        }
-    }
-    // block cost (FP64, fixed order)
-    const double cw = warp_sum(cost);
-    if ((tid & 31) == 0) s_misc[tid >> 5] = cw;
-    __syncthreads();
-
-    // ---- D: owner gathers.  Work index space: [pair entries | camera entries | chunk entries]
-    const int pair0 = D.ch_pair_begin[chunk], npairs = D.ch_pair_begin[chunk + 1] - pair0;
-    const int cam0 = D.ch_cam_begin[chunk], ncams = D.ch_cam_begin[chunk + 1] - cam0;
-    const int camrec = 12 + ng * 6 * ni;
-    const int chrec = nb * nb + 2 * nb;
-    const int w_pair = npairs * 36, w_cam = ncams * camrec;
-    const int w_total = w_pair + w_cam + chrec;
-    for (int wk = tid; wk < w_total; wk += blockDim.x) {
-        Acc<T> acc;
-        if (wk < w_pair) {
-            // pose block entry (x, y) of chunk pair slot s
-            const int s = wk / 36, e = wk - s * 36;
-            const int x = e / 6, y = e - x * 6;
-            const int pk = D.ch_pairs[pair0 + s];
-            const bool diag = (pk & 0xFFFF) == (pk >> 16);
-            if (diag && x > y) continue;
-            const int i1 = D.slot_item_begin[pair0 + s + 1];
-            for (int it = D.slot_item_begin[pair0 + s]; it < i1; ++it) {
-                const unsigned item = D.slot_items[it];
-                const int oa = item & 0xFF, ob = item >> 8;
-                if (oa == ob) {
-                    const T* A = s_A + static_cast<size_t>(oa) * 2 * nA;
-                    const VT* M = s_M + static_cast<size_t>(oa) * 7;
-                    const T ax0 = A[x], ax1 = A[nA + x], ay0 = A[y], ay1 = A[nA + y];
-                    acc.add(ax0 * (ay0 * M[0] + ay1 * M[1]) + ax1 * (ay0 * M[1] + ay1 * M[2]));
-                } else {
-                    const VT* Ga = s_G + static_cast<size_t>(oa) * 3 * nA + 3 * x;
-                    const VT* Gb = s_G + static_cast<size_t>(ob) * 3 * nA + 3 * y;
-                    acc.add(-(Ga[0] * Gb[0] + Ga[1] * Gb[1] + Ga[2] * Gb[2]));
-                }
-            }
-            P* out = O.part_pair + static_cast<size_t>(pair0 + s) * 36;
-            out[e] = acc.part();
-            if (diag && x != y) out[y * 6 + x] = acc.part();
-        } else if (wk < w_pair + w_cam) {
-            // camera record entry: rhs (6), direct rhs (6), border (ng x 6 x ni)
-            const int l = (wk - w_pair) / camrec, e = wk - w_pair - l * camrec;
-            const int b0 = D.lcam_obs_begin[cam0 + l], b1 = D.lcam_obs_begin[cam0 + l + 1];
-            if (e < 12) {
-                const int a = e < 6 ? e : e - 6, mo = e < 6 ? 3 : 5;
-                for (int it = b0; it < b1; ++it) {
-                    const int ob = D.lcam_obs[it];
-                    const T* A = s_A + static_cast<size_t>(ob) * 2 * nA;
-                    const VT* M = s_M + static_cast<size_t>(ob) * 7;
-                    acc.add(-(A[a] * M[mo] + A[nA + a] * M[mo + 1]));
-                }
-            } else {
-                const int f = e - 12;
-                const int g = f / (6 * ni), rem = f - g * 6 * ni, a = rem / ni, c2 = rem - a * ni;
-                for (int it = b0; it < b1; ++it) {
-                    const int ob = D.lcam_obs[it];
-                    const int info = s_info[ob];
-                    const T* A = s_A + static_cast<size_t>(ob) * 2 * nA;
-                    if (info_group(info) == g) {
-                        // own term J_pose^T M J_intr
-                        const VT* M = s_M + static_cast<size_t>(ob) * 7;
-                        const T i0 = A[6 + c2], i1 = A[nA + 6 + c2];
-                        acc.add(A[a] * (i0 * M[0] + i1 * M[1]) + A[nA + a] * (i0 * M[1] + i1 * M[2]));
-                    }
-                    if (info & kElim) {
-                        // couplings to the group-g observations of the same track
-                        const int tr = s_trk[ob], f0 = tr & 0xFFFF, k = tr >> 16;
-                        VT k0 = Val::zero(), k1 = Val::zero(), k2 = Val::zero();
-                        for (int j = f0; j < f0 + k; ++j) {
-                            if (j == ob || info_group(s_info[j]) != g) continue;
-                            const VT* Gj = s_G + static_cast<size_t>(j) * 3 * nA + 3 * (6 + c2);
-                            k0 = k0 + Gj[0];
-                            k1 = k1 + Gj[1];
-                            k2 = k2 + Gj[2];
-                        }
-                        const VT* Go = s_G + static_cast<size_t>(ob) * 3 * nA + 3 * a;
-                        acc.add(-(Go[0] * k0 + Go[1] * k1 + Go[2] * k2));
-                    }
-                }
-            }
-            O.part_cam[static_cast<size_t>(cam0 + l) * camrec + e] = acc.part();
-        } else {
-            // chunk record entry: intrinsic block (nb x nb), intrinsic rhs (nb), direct rhs (nb)
-            const int e = wk - w_pair - w_cam;
-            P* out = O.part_chunk + static_cast<size_t>(chunk) * chrec;
-            if (e < nb * nb) {
-                const int i = e / nb, j = e - i * nb;
-                if (i > j) continue;
-                const int g1 = i / ni, c1 = i - g1 * ni, g2 = j / ni, c2 = j - g2 * ni;
-                for (int t0 = 0; t0 < nobs;) {
-                    const int k = s_trk[t0] >> 16;
-                    VT K1[3] = {Val::zero(), Val::zero(), Val::zero()}, K2[3] = {Val::zero(), Val::zero(), Val::zero()};
-                    for (int jj = t0; jj < t0 + k; ++jj) {
-                        const int gj = info_group(s_info[jj]);
-                        const VT* Gj = s_G + static_cast<size_t>(jj) * 3 * nA;
-                        if (gj == g1) {
-                            const VT* ga = Gj + 3 * (6 + c1);
-                            K1[0] = K1[0] + ga[0]; K1[1] = K1[1] + ga[1]; K1[2] = K1[2] + ga[2];
-                            if (g1 == g2) {
-                                // own term J_intr^T M J_intr, plus the observation's own G G^T that
-                                // the track product K K^T below also contains
-                                const T* A = s_A + static_cast<size_t>(jj) * 2 * nA;
-                                const VT* M = s_M + static_cast<size_t>(jj) * 7;
-                                const T a0 = A[6 + c1], a1 = A[nA + 6 + c1], b0 = A[6 + c2], b1 = A[nA + 6 + c2];
-                                const VT* gb = Gj + 3 * (6 + c2);
-                                acc.add(a0 * (b0 * M[0] + b1 * M[1]) + a1 * (b0 * M[1] + b1 * M[2]) +
-                                        (ga[0] * gb[0] + ga[1] * gb[1] + ga[2] * gb[2]));
-                            }
-                        }
-                        if (gj == g2) {
-                            const VT* gb = Gj + 3 * (6 + c2);
-                            K2[0] = K2[0] + gb[0]; K2[1] = K2[1] + gb[1]; K2[2] = K2[2] + gb[2];
-                        }
-                    }
-                    acc.add(-(K1[0] * K2[0] + K1[1] * K2[1] + K1[2] * K2[2]));
-                    t0 += k;
-                }
-                out[e] = acc.part();
-                if (i != j) out[j * nb + i] = acc.part();
-            } else {
-                const int idx = e - nb * nb;
-                const int col = idx < nb ? idx : idx - nb, mo = idx < nb ? 3 : 5;
-                const int g = col / ni, c = col - g * ni;
-                for (int ob = 0; ob < nobs; ++ob) {
-                    if (info_group(s_info[ob]) != g) continue;
-                    const T* A = s_A + static_cast<size_t>(ob) * 2 * nA;
-                    const VT* M = s_M + static_cast<size_t>(ob) * 7;
-                    acc.add(-(A[6 + c] * M[mo] + A[nA + 6 + c] * M[mo + 1]));
-                }
-                out[e] = acc.part();
-            }
-        }
-    }
-    if (tid == 0) {
-        double c = 0.0;
-        for (int w = 0; w < static_cast<int>((blockDim.x + 31) >> 5); ++w) c += s_misc[w];
-        O.part_cost[chunk] = c;
-        O.part_flags[chunk] = s_flags[0];
-    }
-}
 
 // Sum of the chunk partials of every upper pose block, written to both CSR orientations.
 template <typename T>
@@ -923,12 +582,6 @@ static AsmOutT<T> typed(const AsmOut& o) {
 }
 
 template <typename T>
-void launch_assemble(const Shape& S, const DevPtrs& D, const AsmOut& O, double damping, size_t smem, cudaStream_t st) {
-    if (S.nchunks == 0) return;
-    k_assemble<T><<<S.nchunks, S.max_obs, smem, st>>>(S, D, typed<T>(O), damping);
-}
-
-template <typename T>
 void launch_reduce(const Shape& S, const DevPtrs& D, const AsmOut& O, const RedOut<double>& R, double damping,
                    cudaStream_t st) {
     const AsmOutT<T> P = typed<T>(O);
@@ -988,15 +641,7 @@ void launch_strict_rms(const Shape& S, const DevPtrs& D, const double* cams, con
     k_strict_rms<<<(nt + 255) / 256, 256, 0, st>>>(S, D, cams, init_points, proc_of_track, use_state, nt, out);
 }
 
-void pb_set_assemble_smem_f32(size_t bytes) {
-    cudaFuncSetAttribute(k_assemble<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes));
-}
-void pb_set_assemble_smem_f64(size_t bytes) {
-    cudaFuncSetAttribute(k_assemble<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes));
-}
 
-template void launch_assemble<float>(const Shape&, const DevPtrs&, const AsmOut&, double, size_t, cudaStream_t);
-template void launch_assemble<double>(const Shape&, const DevPtrs&, const AsmOut&, double, size_t, cudaStream_t);
 template void launch_reduce<float>(const Shape&, const DevPtrs&, const AsmOut&, const RedOut<double>&, double,
                                    cudaStream_t);
 template void launch_reduce<double>(const Shape&, const DevPtrs&, const AsmOut&, const RedOut<double>&, double,

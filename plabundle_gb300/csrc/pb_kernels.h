@@ -115,8 +115,9 @@ struct DenseWork {
     double* dscale = nullptr;
     int* status = nullptr;
     double *x = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr, *w = nullptr;
-    double* part = nullptr;
+    double* part = nullptr;  // per-block partials of the cooperative CG (grid * 4)
     double* scal = nullptr;
+    int coop_grid = 0;       // blocks of the cooperative CG launch
 };
 
 template <typename T>

@@ -93,6 +93,8 @@ struct pb_gpu_ctx {
     DenseWork<float> dw32;
     DenseWork<double> dw64;
     double shift32 = 1e-7;  // last FP32 factor shift that factorised
+    int f32_age = -1;       // LM solves served by the current FP32 factor (-1: none)
+    int f32_base_iters = 0; // CG iterations of the first solve with that factor
     bool dense_ready[2] = {false, false};
     int last_solver = 0;
     // shared FP64 buffers
@@ -348,6 +350,7 @@ void prepare_precision(pb_gpu_ctx* c, int precision) {
     S.max_obs = cs.max_obs;
     S.max_cams = cs.max_cams;
     S.max_pairs = cs.max_pairs;
+    S.max_tracks = cs.max_tracks;
     D.ch_obs_begin = upload_new(A, cs.obs_begin, st);
     D.ch_cam_begin = upload_new(A, cs.cam_begin, st);
     D.ch_cams = upload_new(A, cs.cams, st);
@@ -407,7 +410,7 @@ void assemble(pb_gpu_ctx* c, double damping, int precision, double* cost, int* f
     PrecisionBuffers<T>& B = pbuf<T>(c);
     const Shape& S = c->S[precision];
     const DevPtrs& D = c->D[precision];
-    const size_t smem = chunk_smem_bytes(precision, S.max_obs, S.ni);
+    const size_t smem = chunk_smem_bytes(precision, S.max_obs, S.max_tracks, S.ni, S.nb);
     set_assemble_smem(precision, smem);
     {
         Timer t(c, 0);
@@ -460,22 +463,43 @@ void ensure_dense(pb_gpu_ctx* c) {
     W.p = A.alloc<double>(W.n);
     W.q = A.alloc<double>(W.n);
     W.w = A.alloc<double>(W.n);
-    const int nrow_blk = std::max(1, (S.ncb + 7) / 8);
-    W.part = A.alloc<double>(static_cast<size_t>(nrow_blk) * (1 + kMaxNB) + (W.n + 255) / 256 + (W.n + 7) / 8 + 8);
+    // partials of the cooperative CG: 4 per block, at most 32 blocks per SM
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+    W.part = A.alloc<double>(static_cast<size_t>(std::max(1, sms)) * 32 * 4);
     W.scal = A.alloc<double>(8);
     c->dense_ready[idx] = true;
 }
+
+constexpr int kMaxFactorAge = 8;  // LM solves one FP32 factor may precondition
 
 template <typename T>
 int solve_dense(pb_gpu_ctx* c, double rel, double abs_tol, int max_it, bool* converged, int* iterations,
                 double* relres) {
     ensure_dense<T>(c);
     DenseWork<T>& W = dwork<T>(c);
+    const bool f32 = std::is_same<T, float>::value;
+    int spent = 0;
+    if (f32 && c->f32_age >= 0 && c->f32_age < kMaxFactorAge) {
+        // The reduced matrix changes little between LM iterations: the FP32 factor of an earlier
+        // one still preconditions the CG on the current FP64 matrix.  Refactor when it needs
+        // clearly more iterations than it did on its own matrix.
+        const int cap = std::min(max_it, std::max(2 * c->f32_base_iters + 8, 24));
+        const int rc = dense_pcg<T>(c->sys, W, c->red.rhs, rel, abs_tol, cap, iterations, relres, converged,
+                                    c->h_scratch + 40, c->stream, &c->launches);
+        if (rc < 0) throw CudaError(std::string("dense CG failed: ") + cudaGetErrorString(cudaGetLastError()));
+        if (rc == 0 && *converged) {
+            ++c->f32_age;
+            check(cudaMemcpyAsync(c->step_c, W.x, c->S[0].n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream),
+                  "D2D");
+            return 0;
+        }
+        spent = *iterations;
+    }
     // FP32 factor of the Jacobi-scaled matrix with a small shift (FP32 rounding of a matrix of
     // condition ~1e9 is not positive definite unshifted); the CG that follows runs on the
     // FP64 matrix, so the shift only costs iterations.  It starts at the last shift that
     // factorised and grows tenfold on failure.  The FP64 factor starts unshifted.
-    const bool f32 = std::is_same<T, float>::value;
     double shift = f32 ? c->shift32 : 0.0;
     int st = 0;
     for (int attempt = 0; attempt < 6; ++attempt) {
@@ -489,6 +513,11 @@ int solve_dense(pb_gpu_ctx* c, double rel, double abs_tol, int max_it, bool* con
     const int rc = dense_pcg<T>(c->sys, W, c->red.rhs, rel, abs_tol, max_it, iterations, relres, converged,
                                 c->h_scratch + 40, c->stream, &c->launches);
     if (rc < 0) throw CudaError(std::string("dense CG failed: ") + cudaGetErrorString(cudaGetLastError()));
+    if (f32) {
+        c->f32_age = rc == 0 ? 1 : -1;
+        c->f32_base_iters = *iterations;
+    }
+    *iterations += spent;
     if (rc) return 1;
     check(cudaMemcpyAsync(c->step_c, W.x, c->S[0].n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream), "D2D");
     return 0;
@@ -651,6 +680,7 @@ int do_assemble(pb_gpu_ctx* c, double damping, int precision, double* cost, int*
 
 // The LM / Armijo driver (online branch of optimizePointsWithPlaMatrix).
 void lm_solve(pb_gpu_ctx* c, const pb_solve_options& op, pb_solve_report* rep) {
+    c->f32_age = -1;  // every solve starts from a fresh factor: repeated solves run identically
     const auto t0 = std::chrono::steady_clock::now();
     const HostModel& m = c->model;
     std::memset(rep, 0, sizeof(*rep));
@@ -912,6 +942,7 @@ pb_status pb_gpu_upload(pb_gpu_ctx* c, const pb_problem_desc* pr, const pb_solve
         HostModel m;
         std::string err;
         c->shift32 = 1e-7;
+        c->f32_age = -1;
         const int rc = build_host_model(pr, op, &m, &err);
         if (rc) {
             c->uploaded = false;
@@ -939,7 +970,7 @@ pb_status pb_gpu_upload(pb_gpu_ctx* c, const pb_problem_desc* pr, const pb_solve
                 dst.cam_contrib_begin = src.cam_contrib_begin; dst.cam_contrib = src.cam_contrib; dst.obs_lcam = src.obs_lcam;
                 dst.slot_item_begin = src.slot_item_begin; dst.slot_items = src.slot_items;
                 dst.lcam_obs_begin = src.lcam_obs_begin; dst.lcam_obs = src.lcam_obs;
-                sd.nchunks = ss.nchunks; sd.max_obs = ss.max_obs; sd.max_cams = ss.max_cams; sd.max_pairs = ss.max_pairs;
+                sd.nchunks = ss.nchunks; sd.max_obs = ss.max_obs; sd.max_cams = ss.max_cams; sd.max_pairs = ss.max_pairs; sd.max_tracks = ss.max_tracks;
             };
             keep_chunks(c->D[0], d0, c->S[0], s0);
             keep_chunks(c->D[1], d1, c->S[1], s1);

@@ -55,6 +55,11 @@ extern "C" int probe_chunks(const pb_problem_desc* pr, const pb_solve_options* o
     for (int c = 0; c < nch; ++c) {
         const int o0 = cs.obs_begin[c], o1 = cs.obs_begin[c + 1];
         if (o1 - o0 > cs.max_obs || o1 < o0) return fail("chunk larger than max_obs");
+        {
+            int tracks = 0;
+            for (int o = o0; o < o1; ++o) tracks += m.trk_obs_begin[trk_of[o]] == o;
+            if (tracks > cs.max_tracks || cs.max_tracks > 255) return fail("chunk holds more than max_tracks tracks");
+        }
         if (o1 > o0 && (m.trk_obs_begin[trk_of[o0]] != o0 || (o1 < nobs && m.trk_obs_begin[trk_of[o1]] != o1)))
             return fail("chunk splits a track");
         const int c0 = cs.cam_begin[c], ncl = cs.cam_begin[c + 1] - c0;
@@ -144,7 +149,7 @@ extern "C" int probe_chunks(const pb_problem_desc* pr, const pb_solve_options* o
         stats[3] = items_total;
         stats[4] = static_cast<long long>(cs.cams.size());
         stats[5] = nobs;
-        stats[6] = static_cast<long long>(chunk_smem_bytes(precision, cs.max_obs, m.ni));
+        stats[6] = static_cast<long long>(chunk_smem_bytes(precision, cs.max_obs, cs.max_tracks, m.ni, m.ng * m.ni));
     }
     return 0;
 }
