@@ -44,9 +44,7 @@ __device__ __forceinline__ T* carve(char*& ptr, size_t count) {
 constexpr int kOk = 1, kElim = 2;
 __device__ __forceinline__ int info_group(int info) { return ((info >> 2) & 7) - 1; }
 // per-observation track record: first observation (8 bits) | chunk track slot (8) | length (16)
-__device__ __forceinline__ int trk_first(int v) { return v & 0xFF; }
 __device__ __forceinline__ int trk_slot(int v) { return (v >> 8) & 0xFF; }
-__device__ __forceinline__ int trk_len(int v) { return v >> 16; }
 
 }  // namespace
 
@@ -71,6 +69,7 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
     int* s_trk = carve<int>(ptr, MO);
     VT* s_K = carve<VT>(ptr, static_cast<size_t>(MT) * nb * 3);
     int* s_tfirst = carve<int>(ptr, MT + 1);
+    int* s_tmask = carve<int>(ptr, MT);  // calibration groups present in each chunk track
     double* s_misc = carve<double>(ptr, 40);
     int* s_flags = reinterpret_cast<int*>(s_misc + 32);
     int* s_wcount = reinterpret_cast<int*>(s_misc + 34);
@@ -99,13 +98,12 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
         load_cam(D.cams_eff + static_cast<size_t>(cam) * kCamStride, c);
         const double* X = D.points + static_cast<size_t>(trk) * 3;
         const bool tangent = cam == S.gauge_scale && S.gauge_anchor >= 0 && S.gauge_baseline > 0.0;
-        ok = linearize_obs<T>(c, X[0], X[1], X[2], D.obs_u[o], D.obs_v[o], D.obs_w[o], S.loss, S.loss_scale, tangent,
-                              D.gauge_basis, ni, S.int_cols, true, L, grad);
+        ok = linearize_obs<T>(c, X[0], X[1], X[2], D.pscale[trk], D.obs_u[o], D.obs_v[o], D.obs_w[o], S.loss,
+                              S.loss_scale, tangent, D.gauge_basis, ni, S.int_cols, true, L, grad);
         if (!ok) {
             atomicOr(s_flags, 2);
         } else {
             cost = L.cost;
-            O.obs_wn[o] = L.w;
         }
         s_info[tid] = (ok ? kOk : 0) | (elim ? kElim : 0) | ((grp + 1) << 2);
         T* A = s_A + static_cast<size_t>(tid) * 2 * nA;
@@ -163,7 +161,15 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
     }
     if (start) {
         s_trk[tid] = first | (slot << 8) | (k << 16);
-        if (slot < MT) s_tfirst[slot] = tid;
+        if (slot < MT) {
+            s_tfirst[slot] = tid;
+            int mask = 0;
+            for (int j = first; j < first + k; ++j) {
+                const int g = info_group(s_info[j]);
+                if (g >= 0) mask |= 1 << g;
+            }
+            s_tmask[slot] = mask;
+        }
     }
     if (tid == 0 && ntc <= MT) s_tfirst[ntc] = nobs;
     if (start && elim) {
@@ -247,6 +253,10 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
                 Ys[i] = y[i];
             }
             const T* A = s_A + static_cast<size_t>(tid) * 2 * nA;
+            // back-substitution record of the observation: A rows, then Y
+            T* rec = O.obs_rec + static_cast<size_t>(o) * (2 * nA + 6);
+            for (int i = 0; i < 2 * nA; ++i) rec[i] = A[i];
+            for (int i = 0; i < 6; ++i) rec[2 * nA + i] = static_cast<T>(Y[i / 3][i % 3]);
             for (int a = 0; a < 6; ++a) {
                 const T ja0 = A[a], ja1 = A[nA + a];
                 G[a * 3 + 0] = ja0 * y[0] + ja1 * y[3];
@@ -254,6 +264,8 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
                 G[a * 3 + 2] = ja0 * y[2] + ja1 * y[5];
             }
         } else {
+            T* rec = O.obs_rec + static_cast<size_t>(o) * (2 * nA + 6);
+            for (int i = 0; i < 2 * nA + 6; ++i) rec[i] = T(0);
             for (int i = 0; i < 6; ++i) Mo[i] = Val::zero();
             for (int i = 0; i < 6; ++i) Ys[i] = Val::zero();
             for (int i = 0; i < 18; ++i) G[i] = Val::zero();
@@ -377,7 +389,7 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
                         }
                     }
                     const int ts = trk_slot(s_trk[ob]);
-                    if ((info & kElim) && ts < ntc) {
+                    if ((info & kElim) && ts < ntc && ((s_tmask[ts] >> g) & 1)) {
                         const VT* Kt = s_K + (static_cast<size_t>(ts) * nb + gc) * 3;
                         const VT k0 = -Kt[0], k1 = -Kt[1], k2 = -Kt[2];
                         const VT* Go = s_G + static_cast<size_t>(ob) * 18;
@@ -410,7 +422,9 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
                         acc_fma(acc, w, two_prod(A[nA + 6 + c1], A[nA + 6 + c2]));
                     }
                 }
+                const int need = (1 << g1) | (1 << g2);
                 for (int t = 0; t < ntc; ++t) {
+                    if ((s_tmask[t] & need) != need) continue;
                     const VT* K1 = s_K + (static_cast<size_t>(t) * nb + i) * 3;
                     const VT* K2 = s_K + (static_cast<size_t>(t) * nb + j) * 3;
                     acc_fma(acc, -K1[0], K2[0]);
@@ -450,7 +464,7 @@ template <typename T>
 static AsmOutT<T> typed_out(const AsmOut& o) {
     using P = typename Acc<T>::part_type;
     return {static_cast<P*>(o.part_pair_v), static_cast<P*>(o.part_cam_v), static_cast<P*>(o.part_chunk_v),
-            o.part_cost, o.part_flags, static_cast<double*>(o.trk_data_v), static_cast<T*>(o.obs_wn_v)};
+            o.part_cost, o.part_flags, static_cast<double*>(o.trk_data_v), static_cast<T*>(o.obs_rec_v)};
 }
 
 template <typename T>

@@ -9,7 +9,8 @@
 // On the mixed path the factor and inverse are FP32 with a small shift that keeps the FP32
 // factorisation positive definite; the FP64 CG recovers the FP64 solution (it plays the role of
 // iterative refinement).  On the FP64 path the factor is FP64 and CG converges in one or two
-// iterations.
+// iterations.  The factorisation with its inverse and the whole CG solve are each one cooperative
+// persistent kernel (grid barriers between phases, no host round trips).
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
@@ -17,6 +18,8 @@
 #include "pb_kernels.h"
 
 namespace pb {
+
+namespace cgk = cooperative_groups;
 
 namespace {
 constexpr int TS = 64;        // tile size
@@ -89,65 +92,6 @@ __global__ void k_dense_diag(T* __restrict__ A, int n, int np, double shift) {
     *d = i < n ? static_cast<T>(static_cast<double>(*d) + shift) : T(1);
 }
 
-// Cholesky of the diagonal tile k (one CTA).  A non-positive pivot sets status bit 2 and is
-// replaced by 1 so that the remaining steps stay finite; the caller retries with a larger shift.
-template <typename T>
-__global__ void __launch_bounds__(256) k_potrf_diag(T* __restrict__ A, int np, int k, int* __restrict__ status) {
-    __shared__ T s[TS * TP];
-    T* tile = A + static_cast<size_t>(k) * TS * np + static_cast<size_t>(k) * TS;
-    for (int e = threadIdx.x; e < TS * TS; e += blockDim.x) s[(e / TS) * TP + e % TS] = tile[static_cast<size_t>(e / TS) * np + e % TS];
-    __syncthreads();
-    for (int j = 0; j < TS; ++j) {
-        if (threadIdx.x == 0) {
-            T d = s[j * TP + j];
-            if (!(d > T(0)) || !isfinite(static_cast<double>(d))) {
-                atomicOr(status, 2);
-                d = T(1);
-            }
-            s[j * TP + j] = sqrt(d);
-        }
-        __syncthreads();
-        const T inv = T(1) / s[j * TP + j];
-        for (int i = j + 1 + threadIdx.x; i < TS; i += blockDim.x) s[i * TP + j] *= inv;
-        __syncthreads();
-        const int m = TS - 1 - j;
-        for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
-            const int i = j + 1 + e / m, l = j + 1 + e % m;
-            if (l <= i) s[i * TP + l] -= s[i * TP + j] * s[l * TP + j];
-        }
-        __syncthreads();
-    }
-    for (int e = threadIdx.x; e < TS * TS; e += blockDim.x) {
-        const int r = e / TS, c = e % TS;
-        tile[static_cast<size_t>(r) * np + c] = c <= r ? s[r * TP + c] : T(0);
-    }
-}
-
-// A_ik <- A_ik L_kk^-T for every tile below the diagonal tile k (one CTA of 64 threads per tile,
-// one row per thread).
-template <typename T>
-__global__ void __launch_bounds__(64) k_trsm_col(T* __restrict__ A, int np, int k) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* sL = reinterpret_cast<T*>(smem_raw);
-    T* sX = sL + TS * TP;
-    const int i = k + 1 + blockIdx.x;
-    const T* L = A + static_cast<size_t>(k) * TS * np + static_cast<size_t>(k) * TS;
-    T* X = A + static_cast<size_t>(i) * TS * np + static_cast<size_t>(k) * TS;
-    for (int e = threadIdx.x; e < TS * TS; e += blockDim.x) {
-        sL[(e / TS) * TP + e % TS] = L[static_cast<size_t>(e / TS) * np + e % TS];
-        sX[(e / TS) * TP + e % TS] = X[static_cast<size_t>(e / TS) * np + e % TS];
-    }
-    __syncthreads();
-    const int r = threadIdx.x;
-    for (int c = 0; c < TS; ++c) {
-        T v = sX[r * TP + c];
-        for (int m = 0; m < c; ++m) v -= sX[r * TP + m] * sL[c * TP + m];
-        sX[r * TP + c] = v / sL[c * TP + c];
-    }
-    __syncthreads();
-    for (int e = threadIdx.x; e < TS * TS; e += blockDim.x) X[static_cast<size_t>(e / TS) * np + e % TS] = sX[(e / TS) * TP + e % TS];
-}
-
 // C (64x64) += A (64x64) * B (64x64): sA holds A row-major [r][k], sB holds B k-major [k][c];
 // 256 threads, thread (ty, tx) owns rows ty + 16 m and columns tx + 16 m'.
 template <typename T>
@@ -168,134 +112,227 @@ __device__ __forceinline__ void tile_mma(const T* __restrict__ sA, const T* __re
     }
 }
 
-// Loads a global 64x64 tile (row stride np) into shared memory, row-major or transposed.
+// Loads a global 64x64 tile (row stride np, 16-byte aligned rows) into shared memory, row-major
+// or transposed, with 16-byte loads.
+template <typename T>
+struct Vec16;
+template <>
+struct Vec16<float> {
+    using type = float4;
+    static constexpr int n = 4;
+    __device__ static __forceinline__ float get(const float4& v, int i) { return i == 0 ? v.x : i == 1 ? v.y : i == 2 ? v.z : v.w; }
+    __device__ static __forceinline__ float dot(const float4& a, const float4& b) {
+        return a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w;
+    }
+};
+template <>
+struct Vec16<double> {
+    using type = double2;
+    static constexpr int n = 2;
+    __device__ static __forceinline__ double get(const double2& v, int i) { return i == 0 ? v.x : v.y; }
+    __device__ static __forceinline__ double dot(const double2& a, const double2& b) { return a.x * b.x + a.y * b.y; }
+};
+
 template <typename T, bool TRANSPOSE>
 __device__ __forceinline__ void tile_load(const T* __restrict__ g, int np, T* __restrict__ s) {
+    using V = Vec16<T>;
+    constexpr int per_row = TS / V::n;
+    for (int e = threadIdx.x; e < TS * per_row; e += blockDim.x) {
+        const int r = e / per_row, c0 = (e % per_row) * V::n;
+        const typename V::type v = *reinterpret_cast<const typename V::type*>(g + static_cast<size_t>(r) * np + c0);
+#pragma unroll
+        for (int q = 0; q < V::n; ++q) {
+            if (TRANSPOSE) s[(c0 + q) * TP + r] = V::get(v, q);
+            else s[r * TP + c0 + q] = V::get(v, q);
+        }
+    }
+}
+
+// Lower-triangle elements of a 64x64 tile owned by this thread (up to 9 of 2080).
+__device__ __forceinline__ int owned_elements(int* ii, int* ll) {
+    int cnt = 0;
+#pragma unroll
+    for (int s = 0; s < 9; ++s) {
+        const int e = threadIdx.x + 256 * s;
+        if (e < TS * (TS + 1) / 2) {
+            const int i = tri_row(e);
+            ii[s] = i;
+            ll[s] = e - i * (i + 1) / 2;
+            ++cnt;
+        } else {
+            ii[s] = -1;
+            ll[s] = -1;
+        }
+    }
+    return cnt;
+}
+
+// Block 0 of step k: L_kk (written to A_kk, zeros above the diagonal) and D_k = L_kk^-1.
+template <typename T>
+__device__ void diag_factor_inverse(T* __restrict__ A, T* __restrict__ Dinv, int np, int k, T* sA, T* sB,
+                                    int* __restrict__ status) {
+    T* Akk = A + static_cast<size_t>(k) * TS * np + static_cast<size_t>(k) * TS;
+    tile_load<T, false>(Akk, np, sA);
+    int ii[9], ll[9];
+    owned_elements(ii, ll);
+    // unscaled right-looking elimination: after step j, column j holds d_j * L_:j
+    for (int j = 0; j < TS; ++j) {
+        __syncthreads();
+        const T d = sA[j * TP + j];
+        if (!(d > T(0))) {
+            if (threadIdx.x == 0) atomicOr(status, 2);
+        }
+        const T inv = d > T(0) ? T(1) / d : T(0);
+#pragma unroll
+        for (int s = 0; s < 9; ++s)
+            if (ll[s] > j) sA[ii[s] * TP + ll[s]] -= sA[ii[s] * TP + j] * sA[ll[s] * TP + j] * inv;
+    }
+    __syncthreads();
+    T v[9];
+#pragma unroll
+    for (int s = 0; s < 9; ++s) {
+        if (ii[s] < 0) continue;
+        const T d = sA[ll[s] * TP + ll[s]];
+        const T sd = d > T(0) ? sqrt(d) : T(1);
+        v[s] = ii[s] == ll[s] ? sd : sA[ii[s] * TP + ll[s]] / sd;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int s = 0; s < 9; ++s) {
+        if (ii[s] < 0) continue;
+        sA[ii[s] * TP + ll[s]] = v[s];
+        if (ii[s] != ll[s]) sA[ll[s] * TP + ii[s]] = T(0);
+        sB[ii[s] * TP + ll[s]] = ii[s] == ll[s] ? T(1) : T(0);  // R = I (lower part)
+        if (ii[s] != ll[s]) sB[ll[s] * TP + ii[s]] = T(0);
+    }
+    // inverse: right-looking on R = I, one barrier per column: R_ic -= L_ij R_jc / L_jj
+    for (int j = 0; j < TS; ++j) {
+        __syncthreads();
+        const T inv = T(1) / sA[j * TP + j];
+#pragma unroll
+        for (int s = 0; s < 9; ++s)
+            if (ii[s] > j && ll[s] <= j) sB[ii[s] * TP + ll[s]] -= sA[ii[s] * TP + j] * sB[j * TP + ll[s]] * inv;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int s = 0; s < 9; ++s)
+        if (ii[s] >= 0) v[s] = sB[ii[s] * TP + ll[s]] / sA[ii[s] * TP + ii[s]];
+    __syncthreads();
+    T* D = Dinv + static_cast<size_t>(k) * TS * TS;
     for (int e = threadIdx.x; e < TS * TS; e += blockDim.x) {
         const int r = e / TS, c = e % TS;
-        const T v = g[static_cast<size_t>(r) * np + c];
-        if (TRANSPOSE) s[c * TP + r] = v;
-        else s[r * TP + c] = v;
-    }
-}
-
-// Trailing update of the right-looking Cholesky: A_ij -= A_ik A_jk^T for k < j <= i.
-template <typename T>
-__global__ void __launch_bounds__(256) k_syrk_update(T* __restrict__ A, int np, int k) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* sA = reinterpret_cast<T*>(smem_raw);
-    T* sB = sA + TS * TP;
-    const int t = tri_row(blockIdx.x);
-    const int i = k + 1 + t, j = k + 1 + (blockIdx.x - t * (t + 1) / 2);
-    tile_load<T, false>(A + static_cast<size_t>(i) * TS * np + static_cast<size_t>(k) * TS, np, sA);
-    tile_load<T, true>(A + static_cast<size_t>(j) * TS * np + static_cast<size_t>(k) * TS, np, sB);
-    __syncthreads();
-    T acc[4][4];
-#pragma unroll
-    for (int m = 0; m < 4; ++m)
-#pragma unroll
-        for (int q = 0; q < 4; ++q) acc[m][q] = T(0);
-    tile_mma<T>(sA, sB, acc);
-    T* C = A + static_cast<size_t>(i) * TS * np + static_cast<size_t>(j) * TS;
-    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-#pragma unroll
-    for (int m = 0; m < 4; ++m)
-#pragma unroll
-        for (int q = 0; q < 4; ++q) C[static_cast<size_t>(ty + 16 * m) * np + tx + 16 * q] -= acc[m][q];
-}
-
-// Inverses of all diagonal tiles of L (lower triangular), one CTA of 64 threads per tile,
-// thread c solves L x = e_c.
-template <typename T>
-__global__ void __launch_bounds__(64) k_tile_inverse(const T* __restrict__ A, int np, T* __restrict__ Dinv) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* sL = reinterpret_cast<T*>(smem_raw);
-    T* sX = sL + TS * TP;
-    const int k = blockIdx.x;
-    tile_load<T, false>(A + static_cast<size_t>(k) * TS * np + static_cast<size_t>(k) * TS, np, sL);
-    __syncthreads();
-    const int c = threadIdx.x;
-    for (int r = 0; r < TS; ++r) {
-        T v = r == c ? T(1) : T(0);
-        if (r >= c)
-            for (int m = c; m < r; ++m) v -= sL[r * TP + m] * sX[m * TP + c];
-        sX[r * TP + c] = r >= c ? v / sL[r * TP + r] : T(0);
+        Akk[static_cast<size_t>(r) * np + c] = sA[r * TP + c];
+        D[e] = T(0);
     }
     __syncthreads();
-    T* out = Dinv + static_cast<size_t>(k) * TS * TS;
-    for (int e = threadIdx.x; e < TS * TS; e += blockDim.x) out[e] = sX[(e / TS) * TP + e % TS];
+#pragma unroll
+    for (int s = 0; s < 9; ++s)
+        if (ii[s] >= 0) D[ii[s] * TS + ll[s]] = v[s];
 }
 
-// X <- identity (the right-hand side of L X = I).
+// C = (accumulate ? C : 0) + alpha * sA sB over one 64x64 tile (row stride ldc).
 template <typename T>
-__global__ void k_identity(T* __restrict__ X, int np) {
-    const long long e = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (e < static_cast<long long>(np) * np) X[e] = (e / np == e % np) ? T(1) : T(0);
-}
-
-// Row step k of X = L^-1 (right-looking forward substitution with identity right-hand side):
-// X_kc <- Dinv_k X_kc for every tile column c <= k.
-template <typename T>
-__global__ void __launch_bounds__(256) k_trtri_row(T* __restrict__ X, int np, const T* __restrict__ Dinv, int k) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* sA = reinterpret_cast<T*>(smem_raw);
-    T* sB = sA + TS * TP;
-    const int c = blockIdx.x;
-    const T* D = Dinv + static_cast<size_t>(k) * TS * TS;
-    for (int e = threadIdx.x; e < TS * TS; e += blockDim.x) sA[(e / TS) * TP + e % TS] = D[e];
-    T* Xt = X + static_cast<size_t>(k) * TS * np + static_cast<size_t>(c) * TS;
-    tile_load<T, false>(Xt, np, sB);
-    __syncthreads();
+__device__ __forceinline__ void tile_product_store(T* __restrict__ C, int ldc, const T* sA, const T* sB, T alpha,
+                                                   bool accumulate) {
     T acc[4][4];
 #pragma unroll
     for (int m = 0; m < 4; ++m)
 #pragma unroll
         for (int q = 0; q < 4; ++q) acc[m][q] = T(0);
     tile_mma<T>(sA, sB, acc);
-    __syncthreads();
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
 #pragma unroll
     for (int m = 0; m < 4; ++m)
 #pragma unroll
-        for (int q = 0; q < 4; ++q) Xt[static_cast<size_t>(ty + 16 * m) * np + tx + 16 * q] = acc[m][q];
+        for (int q = 0; q < 4; ++q) {
+            T* c = C + static_cast<size_t>(ty + 16 * m) * ldc + tx + 16 * q;
+            *c = accumulate ? *c + alpha * acc[m][q] : alpha * acc[m][q];
+        }
 }
 
-// X_ic -= L_ik X_kc for i > k, c <= k.
 template <typename T>
-__global__ void __launch_bounds__(256) k_trtri_update(const T* __restrict__ A, T* __restrict__ X, int np, int k) {
+__global__ void __launch_bounds__(256) k_potrf_coop(T* __restrict__ A, T* __restrict__ X, T* __restrict__ Dinv, int np,
+                                                   int nt, int* __restrict__ status) {
+    cgk::grid_group grid = cgk::this_grid();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* sA = reinterpret_cast<T*>(smem_raw);
     T* sB = sA + TS * TP;
-    const int ncol = k + 1;
-    const int i = k + 1 + blockIdx.x / ncol, c = blockIdx.x % ncol;
-    tile_load<T, false>(A + static_cast<size_t>(i) * TS * np + static_cast<size_t>(k) * TS, np, sA);
-    tile_load<T, false>(X + static_cast<size_t>(k) * TS * np + static_cast<size_t>(c) * TS, np, sB);
-    __syncthreads();
-    T acc[4][4];
-#pragma unroll
-    for (int m = 0; m < 4; ++m)
-#pragma unroll
-        for (int q = 0; q < 4; ++q) acc[m][q] = T(0);
-    tile_mma<T>(sA, sB, acc);
-    T* Ct = X + static_cast<size_t>(i) * TS * np + static_cast<size_t>(c) * TS;
-    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-#pragma unroll
-    for (int m = 0; m < 4; ++m)
-#pragma unroll
-        for (int q = 0; q < 4; ++q) Ct[static_cast<size_t>(ty + 16 * m) * np + tx + 16 * q] -= acc[m][q];
-}
-
-// XT = X^T restricted to the lower triangle of X (tile transposes through shared memory).
-template <typename T>
-__global__ void __launch_bounds__(256) k_transpose_lower(const T* __restrict__ X, T* __restrict__ XT, int np) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* s = reinterpret_cast<T*>(smem_raw);
-    const int t = tri_row(blockIdx.x);
-    const int i = t, j = blockIdx.x - t * (t + 1) / 2;  // tile (i, j), j <= i
-    tile_load<T, true>(X + static_cast<size_t>(i) * TS * np + static_cast<size_t>(j) * TS, np, s);
-    __syncthreads();
-    T* out = XT + static_cast<size_t>(j) * TS * np + static_cast<size_t>(i) * TS;
-    for (int e = threadIdx.x; e < TS * TS; e += blockDim.x) out[static_cast<size_t>(e / TS) * np + e % TS] = s[(e / TS) * TP + e % TS];
+    auto tile = [np](T* M, int i, int j) { return M + static_cast<size_t>(i) * TS * np + static_cast<size_t>(j) * TS; };
+    // X = I
+    const int nrow = np, nthreads = gridDim.x * blockDim.x;
+    for (int r = blockIdx.x; r < nrow; r += gridDim.x)
+        for (int c = threadIdx.x; c < np; c += blockDim.x) X[static_cast<size_t>(r) * np + c] = r == c ? T(1) : T(0);
+    (void)nthreads;
+    grid.sync();
+    if (blockIdx.x == 0) diag_factor_inverse<T>(A, Dinv, np, 0, sA, sB, status);
+    grid.sync();
+    for (int k = 0; k < nt; ++k) {
+        const int m = nt - 1 - k;
+        const T* Dk = Dinv + static_cast<size_t>(k) * TS * TS;
+        for (int it = blockIdx.x; it < m + k + 1; it += gridDim.x) {
+            if (it < m) {
+                // L_ik = A_ik D_k^T
+                T* Aik = tile(A, k + 1 + it, k);
+                tile_load<T, false>(Aik, np, sA);
+                tile_load<T, true>(Dk, TS, sB);
+                __syncthreads();
+                tile_product_store<T>(Aik, np, sA, sB, T(1), false);
+            } else {
+                // X_kj = D_k R_kj
+                T* Xkj = tile(X, k, it - m);
+                tile_load<T, false>(Dk, TS, sA);
+                tile_load<T, false>(Xkj, np, sB);
+                __syncthreads();
+                tile_product_store<T>(Xkj, np, sA, sB, T(1), false);
+            }
+            __syncthreads();
+        }
+        grid.sync();
+        // Trailing update and R update.  Item 0 is the next diagonal tile (k+1, k+1): block 0
+        // updates it and factors it at once (lookahead), while the other blocks share the rest.
+        const int ntrail = m * (m + 1) / 2;
+        const int nitems = ntrail + m * (k + 1);
+        const int first_it = blockIdx.x == 0 ? 0 : (gridDim.x > 1 ? blockIdx.x : 1);
+        const int stride = gridDim.x > 1 ? static_cast<int>(gridDim.x) - 1 : 1;
+        for (int it = first_it; it < nitems; it = (it == 0 && gridDim.x > 1) ? nitems : it + stride) {
+            if (it < ntrail) {
+                // A_ij -= L_ik L_jk^T
+                const int t = tri_row(it);
+                const int i = k + 1 + t, j = k + 1 + (it - t * (t + 1) / 2);
+                tile_load<T, false>(tile(A, i, k), np, sA);
+                tile_load<T, true>(tile(A, j, k), np, sB);
+                __syncthreads();
+                tile_product_store<T>(tile(A, i, j), np, sA, sB, T(-1), true);
+            } else {
+                // R_ij -= L_ik X_kj
+                const int q = it - ntrail;
+                const int i = k + 1 + q / (k + 1), j = q % (k + 1);
+                tile_load<T, false>(tile(A, i, k), np, sA);
+                tile_load<T, false>(tile(X, k, j), np, sB);
+                __syncthreads();
+                tile_product_store<T>(tile(X, i, j), np, sA, sB, T(-1), true);
+            }
+            __syncthreads();
+            if (it == 0 && m > 0) {
+                // tile (k+1, k+1) is final: factor it for the next step
+                __threadfence_block();
+                diag_factor_inverse<T>(A, Dinv, np, k + 1, sA, sB, status);
+            }
+        }
+        grid.sync();
+    }
+    // X^T into the upper triangle of A (tile (j, i) = X_ij^T, j <= i)
+    for (int it = blockIdx.x; it < nt * (nt + 1) / 2; it += gridDim.x) {
+        const int i = tri_row(it), j = it - i * (i + 1) / 2;
+        tile_load<T, true>(tile(X, i, j), np, sA);
+        __syncthreads();
+        T* dst = tile(A, j, i);
+        for (int e = threadIdx.x; e < TS * TS; e += blockDim.x) {
+            const int r = e / TS, c = e % TS;
+            dst[static_cast<size_t>(r) * np + c] = sA[r * TP + c];
+        }
+        __syncthreads();
+    }
 }
 
 // ---- conjugate gradients on the FP64 reduced matrix, dense preconditioner M^-1 = D X^T X D.
@@ -309,8 +346,6 @@ constexpr int kCgThreads = 256;
 constexpr int kCgWarps = kCgThreads / 32;
 constexpr int kCgPart = 4;  // partial slots per block
 }  // namespace
-
-namespace cgk = cooperative_groups;
 
 // Block sum of v (all threads), written by thread 0 to *dst.
 __device__ __forceinline__ void block_partial(double v, double* s_red, double* dst) {
@@ -342,25 +377,36 @@ __device__ __forceinline__ double grid_total(const double* part, int slot, doubl
     return t;
 }
 
-// out_i = so_i * sum_j M_ij (si_j in_j), j <= i (LOWER) or j >= i; one warp per row, rows
-// interleaved over all warps of the grid; optional partial of dot_with . out.
+// out_i = so_i * sum_j M_ij in_j over j <= i (LOWER) or j >= i, with in and the product in the
+// factor's type T (FP32 on the mixed path: the preconditioner needs no more); one warp per row,
+// rows interleaved over all warps of the grid.  Writes out_t (T) or out_d (double, scaled by so)
+// and returns this thread's share of dot_with . out_d.
 template <typename T, bool LOWER>
-__device__ __forceinline__ double tri_rows(const T* __restrict__ M, int np, int n, const double* __restrict__ in,
-                                           const double* __restrict__ si, double* __restrict__ out,
+__device__ __forceinline__ double tri_rows(const T* __restrict__ M, int np, int n, const T* __restrict__ in,
+                                           T* __restrict__ out_t, double* __restrict__ out_d,
                                            const double* __restrict__ so, const double* __restrict__ dot_with) {
     const int lane = threadIdx.x & 31;
     const int gw = blockIdx.x * kCgWarps + (threadIdx.x >> 5), nw = gridDim.x * kCgWarps;
     double contrib = 0.0;
+    using V = Vec16<T>;
+    using VV = typename V::type;
+    const VV* in_v = reinterpret_cast<const VV*>(in);
     for (int i = gw; i < n; i += nw) {
-        const T* row = M + static_cast<size_t>(i) * np;
-        const int j0 = LOWER ? 0 : i, j1 = LOWER ? i + 1 : n;
+        // 16-byte loads from an aligned start: the extra elements lie in the diagonal tile, where
+        // the triangular factor is zero, and the vector's padding beyond n is zero
+        const VV* row = reinterpret_cast<const VV*>(M + static_cast<size_t>(i) * np);
+        const int q0 = LOWER ? 0 : i / V::n, q1 = LOWER ? (i + V::n) / V::n : (n + V::n - 1) / V::n;
         T acc = T(0);
-        for (int j = j0 + lane; j < j1; j += 32) acc += row[j] * static_cast<T>(si ? si[j] * in[j] : in[j]);
-        double v = warp_sum(static_cast<double>(acc));
-        if (so) v *= so[i];
+#pragma unroll 8
+        for (int q = q0 + lane; q < q1; q += 32) acc += V::dot(row[q], in_v[q]);
+        acc = warp_sum(acc);
         if (lane == 0) {
-            out[i] = v;
-            if (dot_with) contrib += dot_with[i] * v;
+            if (out_t) out_t[i] = acc;
+            if (out_d) {
+                const double v = static_cast<double>(acc) * so[i];
+                out_d[i] = v;
+                if (dot_with) contrib += dot_with[i] * v;
+            }
         }
     }
     return contrib;
@@ -424,9 +470,9 @@ __global__ void __launch_bounds__(kCgThreads) k_dense_cg(PcgSystem<double> sys, 
                                                          const double* __restrict__ b, double* __restrict__ x,
                                                          double* __restrict__ r, double* __restrict__ z,
                                                          double* __restrict__ p, double* __restrict__ q,
-                                                         double* __restrict__ w, double* __restrict__ part,
-                                                         double* __restrict__ out, double rel_tol, double abs_tol,
-                                                         int max_it) {
+                                                         T* __restrict__ u, T* __restrict__ w,
+                                                         double* __restrict__ part, double* __restrict__ out,
+                                                         double rel_tol, double abs_tol, int max_it) {
     cgk::grid_group grid = cgk::this_grid();
     __shared__ double s_red[kCgWarps + 1];
     const int n = 6 * sys.ncb + sys.nb;
@@ -437,11 +483,12 @@ __global__ void __launch_bounds__(kCgThreads) k_dense_cg(PcgSystem<double> sys, 
     for (int i = gt; i < n; i += nt) {
         x[i] = 0.0;
         r[i] = b[i];
+        u[i] = static_cast<T>(dscale[i] * b[i]);
         bb += b[i] * b[i];
     }
     block_partial(bb, s_red, mypart + 0);
     grid.sync();
-    tri_rows<T, true>(X, np, n, b, dscale, w, nullptr, nullptr);
+    tri_rows<T, true>(X, np, n, u, w, nullptr, nullptr, nullptr);
     grid.sync();
     block_partial(tri_rows<T, false>(XT, np, n, w, nullptr, z, dscale, b), s_red, mypart + 1);
     grid.sync();
@@ -467,6 +514,7 @@ __global__ void __launch_bounds__(kCgThreads) k_dense_cg(PcgSystem<double> sys, 
             x[i] = fma(alpha, p[i], x[i]);
             const double rv = fma(-alpha, q[i], r[i]);
             r[i] = rv;
+            u[i] = static_cast<T>(dscale[i] * rv);
             rr += rv * rv;
         }
         block_partial(rr, s_red, mypart + 0);
@@ -481,7 +529,7 @@ __global__ void __launch_bounds__(kCgThreads) k_dense_cg(PcgSystem<double> sys, 
             converged = true;
             break;
         }
-        tri_rows<T, true>(X, np, n, r, dscale, w, nullptr, nullptr);
+        tri_rows<T, true>(X, np, n, u, w, nullptr, nullptr, nullptr);
         grid.sync();
         block_partial(tri_rows<T, false>(XT, np, n, w, nullptr, z, dscale, r), s_red, mypart + 1);
         grid.sync();
@@ -515,15 +563,10 @@ template <typename T>
 int dense_factor(const PcgSystem<double>& sys, DenseWork<T>& W, double shift, cudaStream_t st, int* launches) {
     const int n = W.n, np = W.np, nt = W.nt;
     const size_t two_tiles = 2 * static_cast<size_t>(TS) * TP * sizeof(T);
-    static bool attrs = false;
-    if (!attrs) {
-        set_smem<T>(reinterpret_cast<const void*>(&k_trsm_col<T>), two_tiles);
-        set_smem<T>(reinterpret_cast<const void*>(&k_syrk_update<T>), two_tiles);
-        set_smem<T>(reinterpret_cast<const void*>(&k_tile_inverse<T>), two_tiles);
-        set_smem<T>(reinterpret_cast<const void*>(&k_trtri_row<T>), two_tiles);
-        set_smem<T>(reinterpret_cast<const void*>(&k_trtri_update<T>), two_tiles);
-        set_smem<T>(reinterpret_cast<const void*>(&k_transpose_lower<T>), two_tiles / 2);
-        attrs = true;
+    static bool attrs[2] = {false, false};
+    if (!attrs[sizeof(T) == 8]) {
+        set_smem<T>(reinterpret_cast<const void*>(&k_potrf_coop<T>), two_tiles);
+        attrs[sizeof(T) == 8] = true;
     }
     int L = 0;
     cudaMemsetAsync(W.status, 0, sizeof(int), st);
@@ -534,30 +577,25 @@ int dense_factor(const PcgSystem<double>& sys, DenseWork<T>& W, double shift, cu
     if (nfill > 0) k_dense_fill<T><<<static_cast<unsigned>((nfill + 255) / 256), 256, 0, st>>>(sys, W.dscale, W.A, np);
     k_dense_diag<T><<<(np + 255) / 256, 256, 0, st>>>(W.A, n, np, shift);
     L += 3;
-    for (int k = 0; k < nt; ++k) {
-        k_potrf_diag<T><<<1, 256, 0, st>>>(W.A, np, k, W.status);
-        ++L;
-        const int m = nt - 1 - k;
-        if (m > 0) {
-            k_trsm_col<T><<<m, 64, two_tiles, st>>>(W.A, np, k);
-            k_syrk_update<T><<<m * (m + 1) / 2, 256, two_tiles, st>>>(W.A, np, k);
-            L += 2;
-        }
+    if (W.fact_grid == 0) {
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_potrf_coop<T>, 256, two_tiles);
+        W.fact_grid = std::max(1, std::min(per_sm, 2) * sms);
     }
-    k_tile_inverse<T><<<nt, 64, two_tiles, st>>>(W.A, np, W.Dinv);
-    const long long nn = static_cast<long long>(np) * np;
-    k_identity<T><<<static_cast<unsigned>((nn + 255) / 256), 256, 0, st>>>(W.X, np);
-    L += 2;
-    for (int k = 0; k < nt; ++k) {
-        k_trtri_row<T><<<k + 1, 256, two_tiles, st>>>(W.X, np, W.Dinv, k);
+    {
+        T* A = W.A;
+        T* X = W.X;
+        T* Dv = W.Dinv;
+        int npv = np, ntv = nt;
+        int* stv = W.status;
+        void* args[] = {&A, &X, &Dv, &npv, &ntv, &stv};
+        if (cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(&k_potrf_coop<T>), dim3(W.fact_grid), dim3(256),
+                                        args, two_tiles, st) != cudaSuccess)
+            return -1;
         ++L;
-        if (k + 1 < nt) {
-            k_trtri_update<T><<<(nt - 1 - k) * (k + 1), 256, two_tiles, st>>>(W.A, W.X, np, k);
-            ++L;
-        }
     }
-    k_transpose_lower<T><<<nt * (nt + 1) / 2, 256, two_tiles / 2, st>>>(W.X, W.A, np);
-    ++L;
     if (launches) *launches += L;
     if (cudaGetLastError() != cudaSuccess) return -1;
     int status = 0;
@@ -585,7 +623,7 @@ int dense_pcg(const PcgSystem<double>& sys, DenseWork<T>& W, const double* b, do
     const double* dscale = W.dscale;
     double rt = rel_tol, at = abs_tol;
     int mi = max_it;
-    void* args[] = {&s, &X, &XT, &np, &dscale, &b, &W.x, &W.r, &W.z, &W.p, &W.q, &W.w, &W.part, &W.scal, &rt, &at, &mi};
+    void* args[] = {&s, &X, &XT, &np, &dscale, &b, &W.x, &W.r, &W.z, &W.p, &W.q, &W.ut, &W.wt, &W.part, &W.scal, &rt, &at, &mi};
     const cudaError_t e = cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(&k_dense_cg<T>), dim3(grid),
                                                       dim3(kCgThreads), args, 0, st);
     if (e != cudaSuccess) return -1;

@@ -122,15 +122,15 @@ __device__ __forceinline__ void intrinsic_column(int col, U x, U y, U r2, U xd, 
     }
 }
 
-// Linearises one observation.  `tangent` selects the gauge tangent centre columns (basis: two
+// Linearises one observation; s64 is the point step scale s(X) of its track.  `tangent` selects the gauge tangent centre columns (basis: two
 // world-frame directions in gb[0..5]).  Returns false on an invalid projection or loss.
 // With `grad`, also writes the observation's gradient -J^T w r in FP64: pose [0, 6), point
 // [6, 9), intrinsic columns [9, 9 + ni).  On the FP64 path it comes from the FP64 Jacobian; on
 // the FP32 path from the FP64 projection through v = R (dpi/dx_c)^T (w r), so that the gradient
 // (and the fixed point of the mixed solve) does not carry the FP32 rounding of the Jacobian.
 template <typename T>
-__device__ __forceinline__ bool linearize_obs(const DCam& c, double X0, double X1, double X2, double u, double v,
-                                              double wobs, int loss, double lscale, bool tangent,
+__device__ __forceinline__ bool linearize_obs(const DCam& c, double X0, double X1, double X2, double s64, double u,
+                                              double v, double wobs, int loss, double lscale, bool tangent,
                                               const double* __restrict__ gb, int ni, const int* __restrict__ cols,
                                               bool want_jacobian, Lin<T>& L, double* grad = nullptr) {
     Proj p;
@@ -165,7 +165,6 @@ __device__ __forceinline__ bool linearize_obs(const DCam& c, double X0, double X
 #pragma unroll
     for (int i = 0; i < 9; ++i) R[i] = static_cast<T>(c.R[i]);
     const T d0 = static_cast<T>(p.d0), d1 = static_cast<T>(p.d1), d2 = static_cast<T>(p.d2);
-    const double s64 = point_scale(X0, X1, X2);
     const T s = static_cast<T>(s64);
 #pragma unroll
     for (int pa = 0; pa < 2; ++pa) {

@@ -425,6 +425,7 @@ size_t chunk_smem_bytes(int precision, int max_obs, int max_tracks, int ni, int 
     s += al(mo * 4) * 2;        // observation flags, track records
     s += al(mt * static_cast<size_t>(nb) * 3 * vs);  // per-track K
     s += al((mt + 1) * 4);      // track starts
+    s += al(mt * 4);            // calibration groups present per track
     s += al(40 * 8);            // warp partial costs and track counts, flags
     return s;
 }

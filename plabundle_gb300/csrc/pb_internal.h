@@ -56,6 +56,7 @@ struct DevPtrs {
     int* trk_orig;        // ntp
     double* points;       // ntp * 3
     double* points0;      // ntp * 3
+    double* pscale;       // ntp: point step scale s(X) of the current points
     // observations (processing order)
     int* obs_cam;
     double* obs_u;

@@ -179,6 +179,10 @@ __device__ void gauge_basis(const double* anchor_c, const double* scale_c, doubl
 
 __global__ void k_effective(Shape S, DevPtrs D) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < S.ntp) {
+        const double* X = D.points + static_cast<size_t>(c) * 3;
+        D.pscale[c] = point_scale(X[0], X[1], X[2]);
+    }
     if (c < S.nc) {
         const double* G = S.ng > 0 ? D.groups + static_cast<size_t>(D.cam_group[c]) * kGroupRec : nullptr;
         group_camera(D.cams_state + static_cast<size_t>(c) * kCamStride, D.cams_ref + static_cast<size_t>(c) * kCamStride,
@@ -293,7 +297,7 @@ __global__ void __launch_bounds__(256) k_cost_batch(Shape S, DevPtrs D, const do
         const double* X = D.points + static_cast<size_t>(trk) * 3;
         const double u = D.obs_u[o], v = D.obs_v[o], w = D.obs_w[o];
         const bool moves = use_trial && D.trk_block[trk] >= 0;
-        const double s = moves ? point_scale(X[0], X[1], X[2]) : 0.0;
+        const double s = moves ? D.pscale[trk] : 0.0;
         const double* dp = moves ? step_p + static_cast<size_t>(trk) * 3 : nullptr;
         for (int a = 0; a < n_alpha; ++a) {
             DCam k;
@@ -376,48 +380,44 @@ __global__ void k_cost_final(Shape S, DevPtrs D, const double* __restrict__ part
 // track:  dp = R^-T (q - R^-1 u),  u = sum_o w J_p^T (J_o dc).
 template <typename T>
 __global__ void __launch_bounds__(256) k_back_substitute(Shape S, DevPtrs D, const double* __restrict__ trk_data,
-                                                         const T* __restrict__ obs_wn, const double* __restrict__ step_c,
+                                                         const T* __restrict__ obs_rec, const double* __restrict__ step_c,
                                                          double* __restrict__ step_p, double* __restrict__ part) {
+    // Point steps dp = V^-1 (g_p - W^T dc) = R^-T (q - sum_o Y_o^T A_o dc) from the records the
+    // assembly kept (A = [J_pose | J_intr] rows and Y = w Jp R^-T of every observation), with
+    // FP64 accumulation (backSubstituteReferencePoints, ...ReferenceSchur.cpp:538-590).
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nA = 6 + S.ni, stride = 2 * nA + 6;
     double dd = 0.0, ss = 0.0;
     if (t < S.ntp && D.trk_block[t] >= 0) {
-        const double* X = D.points + static_cast<size_t>(t) * 3;
         double u0 = 0.0, u1 = 0.0, u2 = 0.0;
         for (int o = D.trk_obs_begin[t]; o < D.trk_obs_begin[t + 1]; ++o) {
             const int cam = D.obs_cam[o];
-            DCam c;
-            load_cam(D.cams_eff + static_cast<size_t>(cam) * kCamStride, c);
-            const bool tangent = cam == S.gauge_scale && S.gauge_anchor >= 0 && S.gauge_baseline > 0.0;
-            Lin<T> L;
-            if (!linearize_obs<T>(c, X[0], X[1], X[2], D.obs_u[o], D.obs_v[o], D.obs_w[o], S.loss, S.loss_scale,
-                                  tangent, D.gauge_basis, S.ni, S.int_cols, true, L))
-                continue;
-            double j0 = 0.0, j1 = 0.0;
+            const T* rec = obs_rec + static_cast<size_t>(o) * stride;
+            double e0 = 0.0, e1 = 0.0;
             const int b = D.cam_block[cam];
             if (b >= 0)
                 for (int a = 0; a < 6; ++a) {
                     const double dcv = step_c[6 * b + a];
-                    j0 = fma(static_cast<double>(L.Jc[a]), dcv, j0);
-                    j1 = fma(static_cast<double>(L.Jc[6 + a]), dcv, j1);
+                    e0 = fma(static_cast<double>(rec[a]), dcv, e0);
+                    e1 = fma(static_cast<double>(rec[nA + a]), dcv, e1);
                 }
-            const int g = D.cam_group[cam];
-            if (S.ng > 0 && g >= 0)
+            const int g = S.ng > 0 ? D.cam_group[cam] : -1;
+            if (g >= 0)
                 for (int a = 0; a < S.ni; ++a) {
                     const double dcv = step_c[6 * S.ncb + g * S.ni + a];
-                    j0 = fma(static_cast<double>(L.Ji[a]), dcv, j0);
-                    j1 = fma(static_cast<double>(L.Ji[kMaxNI + a]), dcv, j1);
+                    e0 = fma(static_cast<double>(rec[6 + a]), dcv, e0);
+                    e1 = fma(static_cast<double>(rec[nA + 6 + a]), dcv, e1);
                 }
-            const double w = L.wd;
-            u0 += w * (static_cast<double>(L.Jp[0]) * j0 + static_cast<double>(L.Jp[3]) * j1);
-            u1 += w * (static_cast<double>(L.Jp[1]) * j0 + static_cast<double>(L.Jp[4]) * j1);
-            u2 += w * (static_cast<double>(L.Jp[2]) * j0 + static_cast<double>(L.Jp[5]) * j1);
+            const T* Y = rec + 2 * nA;
+            u0 += static_cast<double>(Y[0]) * e0 + static_cast<double>(Y[3]) * e1;
+            u1 += static_cast<double>(Y[1]) * e0 + static_cast<double>(Y[4]) * e1;
+            u2 += static_cast<double>(Y[2]) * e0 + static_cast<double>(Y[5]) * e1;
         }
-        (void)obs_wn;
         const double* td = trk_data + static_cast<size_t>(t) * kTrackRec;
         const double i00 = td[0], i10 = td[1], i11 = td[2], i20 = td[3], i21 = td[4], i22 = td[5];
-        const double v0 = td[6] - i00 * u0;
-        const double v1 = td[7] - (i10 * u0 + i11 * u1);
-        const double v2 = td[8] - (i20 * u0 + i21 * u1 + i22 * u2);
+        const double v0 = td[6] - u0;
+        const double v1 = td[7] - u1;
+        const double v2 = td[8] - u2;
         const double p0 = i00 * v0 + i10 * v1 + i20 * v2;
         const double p1 = i11 * v1 + i21 * v2;
         const double p2 = i22 * v2;
@@ -497,10 +497,11 @@ __global__ void k_accept(Shape S, DevPtrs D, const double* __restrict__ step_p, 
     if (i < S.ng * kGroupRec) D.groups[i] = D.groups_trial[static_cast<size_t>(a) * S.ng * kGroupRec + i];
     if (i < S.ntp && D.trk_block[i] >= 0) {
         double* X = D.points + static_cast<size_t>(i) * 3;
-        const double f = point_scale(X[0], X[1], X[2]) * alpha;
+        const double f = D.pscale[i] * alpha;
         X[0] += f * step_p[static_cast<size_t>(i) * 3 + 0];
         X[1] += f * step_p[static_cast<size_t>(i) * 3 + 1];
         X[2] += f * step_p[static_cast<size_t>(i) * 3 + 2];
+        D.pscale[i] = point_scale(X[0], X[1], X[2]);
     }
 }
 
@@ -555,8 +556,8 @@ __global__ void k_linearize_export(Shape S, DevPtrs D, double* __restrict__ res,
     const double* X = D.points + static_cast<size_t>(trk) * 3;
     const bool tangent = cam == S.gauge_scale && S.gauge_anchor >= 0 && S.gauge_baseline > 0.0;
     Lin<T> L;
-    const bool ok = linearize_obs<T>(c, X[0], X[1], X[2], D.obs_u[o], D.obs_v[o], D.obs_w[o], S.loss, S.loss_scale,
-                                     tangent, D.gauge_basis, S.ni, S.int_cols, true, L);
+    const bool ok = linearize_obs<T>(c, X[0], X[1], X[2], D.pscale[trk], D.obs_u[o], D.obs_v[o], D.obs_w[o], S.loss,
+                                     S.loss_scale, tangent, D.gauge_basis, S.ni, S.int_cols, true, L);
     valid[k] = ok ? 1 : 0;
     if (!ok) return;
     res[2 * k] = static_cast<double>(L.r0);
@@ -578,7 +579,7 @@ template <typename T>
 static AsmOutT<T> typed(const AsmOut& o) {
     using P = typename Acc<T>::part_type;
     return {static_cast<P*>(o.part_pair_v), static_cast<P*>(o.part_cam_v), static_cast<P*>(o.part_chunk_v),
-            o.part_cost, o.part_flags, static_cast<double*>(o.trk_data_v), static_cast<T*>(o.obs_wn_v)};
+            o.part_cost, o.part_flags, static_cast<double*>(o.trk_data_v), static_cast<T*>(o.obs_rec_v)};
 }
 
 template <typename T>
@@ -601,10 +602,10 @@ void launch_reduce(const Shape& S, const DevPtrs& D, const AsmOut& O, const RedO
 }
 
 template <typename T>
-void launch_back_substitute(const Shape& S, const DevPtrs& D, const double* trk_data, const T* obs_wn, const double* step_c,
+void launch_back_substitute(const Shape& S, const DevPtrs& D, const double* trk_data, const T* obs_rec, const double* step_c,
                             double* step_p, double* part, const double* direct64, double* out, cudaStream_t st) {
     const int nblk = std::max(1, (S.ntp + 255) / 256);
-    k_back_substitute<T><<<nblk, 256, 0, st>>>(S, D, trk_data, obs_wn, step_c, step_p, part);
+    k_back_substitute<T><<<nblk, 256, 0, st>>>(S, D, trk_data, obs_rec, step_c, step_p, part);
     k_backsub_final<<<1, 256, 0, st>>>(S, D, part, nblk, step_c, direct64, out);
 }
 
@@ -617,7 +618,8 @@ void launch_linearize_export(const Shape& S, const DevPtrs& D, double* res, doub
 }
 
 void launch_effective(const Shape& S, const DevPtrs& D, cudaStream_t st) {
-    k_effective<<<(S.nc + 127) / 128, 128, 0, st>>>(S, D);
+    const int n = std::max(std::max(S.nc, S.ntp), 1);
+    k_effective<<<(n + 127) / 128, 128, 0, st>>>(S, D);
 }
 
 void launch_cost(const Shape& S, const DevPtrs& D, const double* step_c, const double* step_p, const double* alphas,

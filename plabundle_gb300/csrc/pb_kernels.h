@@ -24,7 +24,7 @@ struct AsmOutT {
     double* part_cost;
     int* part_flags;  // bit 0: singular point system, bit 1: invalid projection
     double* trk_data; // processed tracks * kTrackRec (FP64 point factor, q, rhs)
-    T* obs_wn;        // processed observations: robust normal weight
+    T* obs_rec;       // processed observations: A rows (2 x (6 + ni)) and Y (2 x 3), for the back-substitution
 };
 
 // The assembly kernel is instantiated for both precisions; AsmOut carries untyped pointers.
@@ -35,7 +35,7 @@ struct AsmOut {
     double* part_cost;
     int* part_flags;
     void* trk_data_v;
-    void* obs_wn_v;
+    void* obs_rec_v;
 };
 
 // Reduced system of one precision: pose CSR values (both triangles), border B (6*ncb x nb),
@@ -56,7 +56,7 @@ template <typename T>
 void launch_reduce(const Shape& S, const DevPtrs& D, const AsmOut& O, const RedOut<double>& R, double damping,
                    cudaStream_t st);
 template <typename T>
-void launch_back_substitute(const Shape& S, const DevPtrs& D, const double* trk_data, const T* obs_wn, const double* step_c,
+void launch_back_substitute(const Shape& S, const DevPtrs& D, const double* trk_data, const T* obs_rec, const double* step_c,
                             double* step_p, double* part, const double* direct64, double* out, cudaStream_t st);
 template <typename T>
 void launch_linearize_export(const Shape& S, const DevPtrs& D, double* res, double* jp, double* jpose, double* ji,
@@ -115,9 +115,11 @@ struct DenseWork {
     double* dscale = nullptr;
     int* status = nullptr;
     double *x = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr, *w = nullptr;
+    T *ut = nullptr, *wt = nullptr;  // scaled residual and X D r in the factor's type
     double* part = nullptr;  // per-block partials of the cooperative CG (grid * 4)
     double* scal = nullptr;
     int coop_grid = 0;       // blocks of the cooperative CG launch
+    int fact_grid = 0;       // blocks of the cooperative factorisation
 };
 
 template <typename T>

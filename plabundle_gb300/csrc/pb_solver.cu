@@ -221,6 +221,7 @@ void upload_structure(pb_gpu_ctx* c) {
     D.trk_orig = upload_new(A, torig, st);
     D.points0 = upload_new(A, pts, st);
     D.points = A.alloc<double>(pts.size());
+    D.pscale = A.alloc<double>(std::max<size_t>(1, pts.size() / 3));
     // observations in processing order
     std::vector<int> ocam(nop), otrk(nop);
     std::vector<double> ou(nop), ov(nop), ow(nop);
@@ -374,7 +375,7 @@ void prepare_precision(pb_gpu_ctx* c, int precision) {
     B.out.part_cost = A.alloc<double>(std::max(1, S.nchunks));
     B.out.part_flags = A.alloc<int>(std::max(1, S.nchunks));
     B.out.trk_data_v = A.alloc<double>(static_cast<size_t>(S.ntp) * kTrackRec);
-    B.out.obs_wn_v = A.alloc<T>(static_cast<size_t>(S.nop));
+    B.out.obs_rec_v = A.alloc<T>(static_cast<size_t>(S.nop) * (2 * (6 + S.ni) + 6));
     c->pcg_part = nullptr;
     B.ready = true;
     check(cudaStreamSynchronize(st), "prepare");
@@ -463,6 +464,11 @@ void ensure_dense(pb_gpu_ctx* c) {
     W.p = A.alloc<double>(W.n);
     W.q = A.alloc<double>(W.n);
     W.w = A.alloc<double>(W.n);
+    W.ut = A.alloc<T>(W.np);
+    W.wt = A.alloc<T>(W.np);
+    // the CG's triangular products read these vectors up to the padded size: padding stays zero
+    check(cudaMemsetAsync(W.ut, 0, static_cast<size_t>(W.np) * sizeof(T), c->stream), "memset");
+    check(cudaMemsetAsync(W.wt, 0, static_cast<size_t>(W.np) * sizeof(T), c->stream), "memset");
     // partials of the cooperative CG: 4 per block, at most 32 blocks per SM
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
@@ -471,7 +477,8 @@ void ensure_dense(pb_gpu_ctx* c) {
     c->dense_ready[idx] = true;
 }
 
-constexpr int kMaxFactorAge = 8;  // LM solves one FP32 factor may precondition
+constexpr int kMaxFactorAge = 10;     // LM solves one FP32 factor may precondition
+constexpr int kReuseIterations = 150; // CG iterations allowed on a kept factor before refactoring
 
 template <typename T>
 int solve_dense(pb_gpu_ctx* c, double rel, double abs_tol, int max_it, bool* converged, int* iterations,
@@ -482,9 +489,10 @@ int solve_dense(pb_gpu_ctx* c, double rel, double abs_tol, int max_it, bool* con
     int spent = 0;
     if (f32 && c->f32_age >= 0 && c->f32_age < kMaxFactorAge) {
         // The reduced matrix changes little between LM iterations: the FP32 factor of an earlier
-        // one still preconditions the CG on the current FP64 matrix.  Refactor when it needs
-        // clearly more iterations than it did on its own matrix.
-        const int cap = std::min(max_it, std::max(2 * c->f32_base_iters + 8, 24));
+        // one still preconditions the CG on the current FP64 matrix.  A factorisation costs
+        // about as much as a few hundred CG iterations, so the kept factor is used until the
+        // CG needs more than kReuseIterations on it.
+        const int cap = std::min(max_it, std::max(kReuseIterations, 4 * c->f32_base_iters));
         const int rc = dense_pcg<T>(c->sys, W, c->red.rhs, rel, abs_tol, cap, iterations, relres, converged,
                                     c->h_scratch + 40, c->stream, &c->launches);
         if (rc < 0) throw CudaError(std::string("dense CG failed: ") + cudaGetErrorString(cudaGetLastError()));
@@ -578,11 +586,11 @@ void back_substitute(pb_gpu_ctx* c, double* dd, double* point_sq, double* cam_sq
     const DevPtrs& D = c->D[precision];
     if (precision == PB_PRECISION_FP64)
         launch_back_substitute<double>(S, D, static_cast<const double*>(c->p64.out.trk_data_v),
-                                       static_cast<const double*>(c->p64.out.obs_wn_v), c->step_c, c->step_p,
+                                       static_cast<const double*>(c->p64.out.obs_rec_v), c->step_c, c->step_p,
                                        c->bs_part, c->direct64, c->bs_out, c->stream);
     else
         launch_back_substitute<float>(S, D, static_cast<const double*>(c->p32.out.trk_data_v),
-                                      static_cast<const float*>(c->p32.out.obs_wn_v), c->step_c, c->step_p, c->bs_part,
+                                      static_cast<const float*>(c->p32.out.obs_rec_v), c->step_c, c->step_p, c->bs_part,
                                       c->direct64, c->bs_out, c->stream);
     c->launches += 2;
     check(cudaGetLastError(), "back-substitution launch");
