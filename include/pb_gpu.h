@@ -243,6 +243,32 @@ pb_status pb_gpu_set_timing(pb_gpu_ctx* ctx, int32_t enable);
  * filled when timing is enabled. */
 pb_status pb_gpu_kernel_times(pb_gpu_ctx* ctx, double* out8);
 
+/* Allocation-free robust objective of caller-owned device arrays.  No counterpart in the
+ * reference: it serves callers that keep their own cameras, points and observations in device
+ * memory and may not allocate (a real-time loop whose device memory is reserved up front, where
+ * a cudaMalloc or cudaFree would synchronise the device and stall its other streams), and that
+ * cannot create a context (pb_gpu_create / pb_gpu_upload allocate).  It is the line-search cost
+ * kernel with its per-block partials in one fixed file-scope device array:
+ *   - cameras: n_cameras * PB_CAMERA_STRIDE records (effective intrinsics), points: n_points * 3,
+ *     observations: camera index, point index, u, v and w = weight / measurementScale^2; all
+ *     device pointers, read only;
+ *   - cost (host): sum of the robust costs of the observations that project validly;
+ *     invalid_projections (host, may be NULL): how many did not (behind the camera, non-finite);
+ *   - at most PB_NOALLOC_MAX_OBS observations, else PB_ERR_BOUNDS before any launch; a camera or
+ *     point index out of range is skipped on the device and reported as PB_ERR_BOUNDS;
+ *   - the scratch array is shared by all calls on a device: calls that overlap in time on one
+ *     device race, so callers serialise them; nothing in it has to start at zero (every element
+ *     read is written earlier in the same call);
+ *   - the first call on a device resolves the array's address (cudaGetSymbolAddress, which may
+ *     load the module): make it before any stream capture;
+ *   - work is enqueued on `stream` (a cudaStream_t, NULL for the legacy default stream) and the
+ *     call returns after that stream has finished it. */
+#define PB_NOALLOC_MAX_OBS 4194304
+pb_status pb_gpu_objective_noalloc(const double* cameras, int32_t n_cameras, const double* points, int32_t n_points,
+                                   const int32_t* obs_camera, const int32_t* obs_point, const double* obs_u,
+                                   const double* obs_v, const double* obs_w, int64_t n_obs, int32_t robust_loss,
+                                   double robust_loss_scale, void* stream, double* cost, int64_t* invalid_projections);
+
 #ifdef __cplusplus
 }
 #endif

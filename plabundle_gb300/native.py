@@ -20,7 +20,7 @@ EXPORTED = [
     "pb_gpu_back_substitute", "pb_gpu_eval_cost", "pb_gpu_eval_cost_batch", "pb_gpu_apply_step", "pb_gpu_solve",
     "pb_gpu_download_state", "pb_gpu_solve_problem", "pb_gpu_request_cancel", "pb_gpu_get_stream",
     "pb_gpu_set_timing",
-    "pb_gpu_kernel_times",
+    "pb_gpu_kernel_times", "pb_gpu_objective_noalloc",
 ]
 
 
@@ -114,6 +114,8 @@ def load(build_if_missing: bool = False):
     L.pb_gpu_set_timing.argtypes = [vp, i32]
     L.pb_gpu_get_stream.argtypes = [vp, C.POINTER(vp)]
     L.pb_gpu_kernel_times.argtypes = [vp, vp]
+    L.pb_gpu_objective_noalloc.argtypes = [vp, i32, vp, i32, vp, vp, vp, vp, vp, i64, i32, dbl, vp,
+                                           C.POINTER(dbl), C.POINTER(i64)]
     for name in EXPORTED:
         if name not in ("pb_gpu_last_error", "pb_status_name"):
             getattr(L, name).restype = i32
