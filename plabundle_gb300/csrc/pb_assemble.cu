@@ -1,8 +1,8 @@
 // pb_assemble.cu -- kernels (a)+(b): per-observation linearisation and online point Schur
 // elimination into the block-sparse reduced camera system.
 //
-// One CTA per chunk of consecutive tracks (host-built: at most max_obs observations and
-// max_tracks tracks), one thread per observation:
+// One CTA of 256 threads per chunk of consecutive tracks (host-built: at most max_obs <= 256
+// observations and max_tracks tracks), one thread per observation in phases A-C:
 //   A. linearise the observation: FP64 residual, robust weight and cost; Jacobians A = [J_pose |
 //      J_intr] and Jp in T (FP32 on the mixed path);
 //   B. per track, V = sum w Jp^T Jp and the point gradient in FP64 and the factor V = R R^T
@@ -467,10 +467,14 @@ static AsmOutT<T> typed_out(const AsmOut& o) {
             o.part_cost, o.part_flags, static_cast<double*>(o.trk_data_v), static_cast<T*>(o.obs_rec_v)};
 }
 
+// 256 threads per chunk whatever its observation count (at most 256): threads beyond the chunk's
+// observations idle in phases A-C and take their share of the gathers of phase D.
+constexpr int kAssembleThreads = 256;
+
 template <typename T>
 void launch_assemble(const Shape& S, const DevPtrs& D, const AsmOut& O, double damping, size_t smem, cudaStream_t st) {
     if (S.nchunks == 0) return;
-    k_assemble<T><<<S.nchunks, S.max_obs, smem, st>>>(S, D, typed_out<T>(O), damping);
+    k_assemble<T><<<S.nchunks, kAssembleThreads, smem, st>>>(S, D, typed_out<T>(O), damping);
 }
 
 void pb_set_assemble_smem_f32(size_t bytes) {

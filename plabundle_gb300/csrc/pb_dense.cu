@@ -14,6 +14,9 @@
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
+#include <cstdio>
+#include <cstdlib>
+
 #include "pb_device.cuh"
 #include "pb_kernels.h"
 
@@ -321,7 +324,9 @@ __global__ void __launch_bounds__(256) k_potrf_coop(T* __restrict__ A, T* __rest
         }
         grid.sync();
     }
-    // X^T into the upper triangle of A (tile (j, i) = X_ij^T, j <= i)
+    // X^T into the upper triangle of A (tile (j, i) = X_ij^T, j <= i).  The preconditioner is
+    // applied as X^T (X u): forming X^T X explicitly in the factor's precision would square the
+    // condition number of its rounding error.
     for (int it = blockIdx.x; it < nt * (nt + 1) / 2; it += gridDim.x) {
         const int i = tri_row(it), j = it - i * (i + 1) / 2;
         tile_load<T, true>(tile(X, i, j), np, sA);
@@ -335,10 +340,11 @@ __global__ void __launch_bounds__(256) k_potrf_coop(T* __restrict__ A, T* __rest
     }
 }
 
-// ---- conjugate gradients on the FP64 reduced matrix, dense preconditioner M^-1 = D X^T X D.
-// One cooperative persistent kernel runs the whole solve: per iteration the block-CSR SpMV (a
-// warp per pose block row or border row), x/r updates, the two triangular products of the
-// preconditioner (a warp per row) and the direction update, separated by five grid barriers.
+// ---- conjugate gradients on the FP64 reduced matrix, preconditioner D X^T X D (X = L^-1).
+// One cooperative persistent kernel runs the whole solve; per iteration four phases separated
+// by grid barriers: (1) the direction update fused with the block-CSR SpMV (q = S z + beta q, a
+// warp per pose block row or border row), (2) the x / r updates, (3) w = X D r and (4)
+// z = D X^T w (a warp per row).
 // Dot products go through per-block partials that every block sums in the same fixed order, so
 // all blocks take the same convergence / breakdown decision and no result depends on timing.
 namespace {
@@ -361,39 +367,40 @@ __device__ __forceinline__ void block_partial(double v, double* s_red, double* d
     __syncthreads();
 }
 
-// Sum over blocks of partial slot `slot`, identical in every block (fixed order: lane-strided
-// sums, then a fixed shuffle tree).
+// Sum over blocks of partial slot `slot`, identical in every block: every thread loads at most
+// a couple of partials at once (no dependent load chain), then a fixed shuffle and warp order.
 __device__ __forceinline__ double grid_total(const double* part, int slot, double* s_red) {
+    double v = 0.0;
+    for (int k = threadIdx.x; k < static_cast<int>(gridDim.x); k += blockDim.x) v += part[k * kCgPart + slot];
+    v = warp_sum(v);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (warp == 0) {
-        double v = 0.0;
-        for (int k = lane; k < static_cast<int>(gridDim.x); k += 32) v += part[k * kCgPart + slot];
-        v = warp_sum(v);
-        if (lane == 0) s_red[kCgWarps] = v;
-    }
     __syncthreads();
-    const double t = s_red[kCgWarps];
+    if (lane == 0) s_red[warp] = v;
+    __syncthreads();
+    double t = 0.0;
+    for (int w = 0; w < kCgWarps; ++w) t += s_red[w];
     __syncthreads();
     return t;
 }
 
 // out_i = so_i * sum_j M_ij in_j over j <= i (LOWER) or j >= i, with in and the product in the
 // factor's type T (FP32 on the mixed path: the preconditioner needs no more); one warp per row,
-// rows interleaved over all warps of the grid.  Writes out_t (T) or out_d (double, scaled by so)
-// and returns this thread's share of dot_with . out_d.
+// rows interleaved over all warps of the grid, 16-byte loads from an aligned start (the extra
+// elements lie in the diagonal tile, where the triangular factor is zero, and the padding of
+// `in` beyond n is zero).  Writes out_t (T) or out_d (double, scaled by so) and returns this
+// thread's share of dot_with . out_d.
 template <typename T, bool LOWER>
 __device__ __forceinline__ double tri_rows(const T* __restrict__ M, int np, int n, const T* __restrict__ in,
                                            T* __restrict__ out_t, double* __restrict__ out_d,
                                            const double* __restrict__ so, const double* __restrict__ dot_with) {
-    const int lane = threadIdx.x & 31;
-    const int gw = blockIdx.x * kCgWarps + (threadIdx.x >> 5), nw = gridDim.x * kCgWarps;
-    double contrib = 0.0;
     using V = Vec16<T>;
     using VV = typename V::type;
+    const int lane = threadIdx.x & 31;
+    // warp-major row order: consecutive rows go to different blocks (SMs)
+    const int gw = (threadIdx.x >> 5) * gridDim.x + blockIdx.x, nw = gridDim.x * kCgWarps;
     const VV* in_v = reinterpret_cast<const VV*>(in);
+    double contrib = 0.0;
     for (int i = gw; i < n; i += nw) {
-        // 16-byte loads from an aligned start: the extra elements lie in the diagonal tile, where
-        // the triangular factor is zero, and the vector's padding beyond n is zero
         const VV* row = reinterpret_cast<const VV*>(M + static_cast<size_t>(i) * np);
         const int q0 = LOWER ? 0 : i / V::n, q1 = LOWER ? (i + V::n) / V::n : (n + V::n - 1) / V::n;
         T acc = T(0);
@@ -412,12 +419,20 @@ __device__ __forceinline__ double tri_rows(const T* __restrict__ M, int np, int 
     return contrib;
 }
 
-// q = S p over the pose block rows and the border rows; returns this thread's share of p.q.
-__device__ __forceinline__ double spmv_rows(const PcgSystem<double>& sys, const double* __restrict__ p,
-                                            double* __restrict__ q) {
+// Direction update fused with the SpMV: p = z + beta p_old, written by each row's owner to p_new,
+// and q = S p with the neighbours' entries of p formed on the fly by the same expression (so
+// bitwise equal to what their owners write), over the pose block rows and the border rows (a
+// warp per row).  On the first iteration (beta == 0) p = z exactly, whatever p_old holds.
+// Returns this thread's share of p.q.
+__device__ __forceinline__ double spmv_update(const PcgSystem<double>& sys, const double* __restrict__ z,
+                                              double beta, const double* __restrict__ p_old,
+                                              double* __restrict__ p_new, double* __restrict__ q) {
     const int lane = threadIdx.x & 31;
-    const int gw = blockIdx.x * kCgWarps + (threadIdx.x >> 5), nw = gridDim.x * kCgWarps;
+    // warp-major row order: consecutive rows go to different blocks (SMs)
+    const int gw = (threadIdx.x >> 5) * gridDim.x + blockIdx.x, nw = gridDim.x * kCgWarps;
     const int nb = sys.nb, n6 = 6 * sys.ncb;
+    const bool first = beta == 0.0;
+    auto pv = [&](int i) { return first ? z[i] : fma(beta, p_old[i], z[i]); };
     double pq = 0.0;
     for (int r = gw; r < sys.ncb + nb; r += nw) {
         if (r < sys.ncb) {
@@ -427,16 +442,18 @@ __device__ __forceinline__ double spmv_rows(const PcgSystem<double>& sys, const 
                 const double* A = sys.vals + static_cast<size_t>(e) * 36;
                 double pj[6];
 #pragma unroll
-                for (int c = 0; c < 6; ++c) pj[c] = p[6 * j + c];
+                for (int c = 0; c < 6; ++c) pj[c] = pv(6 * j + c);
 #pragma unroll
                 for (int a = 0; a < 6; ++a)
 #pragma unroll
                     for (int c = 0; c < 6; ++c) acc[a] = fma(A[a * 6 + c], pj[c], acc[a]);
             }
             const double* Bi = sys.border + static_cast<size_t>(r) * 6 * nb;
-            for (int c = lane; c < nb; c += 32)
+            for (int c = lane; c < nb; c += 32) {
+                const double pc = pv(n6 + c);
 #pragma unroll
-                for (int a = 0; a < 6; ++a) acc[a] = fma(Bi[a * nb + c], p[n6 + c], acc[a]);
+                for (int a = 0; a < 6; ++a) acc[a] = fma(Bi[a * nb + c], pc, acc[a]);
+            }
 #pragma unroll
             for (int a = 0; a < 6; ++a) acc[a] = warp_sum(acc[a]);
             if (lane < 6) {
@@ -444,18 +461,26 @@ __device__ __forceinline__ double spmv_rows(const PcgSystem<double>& sys, const 
 #pragma unroll
                 for (int a = 1; a < 6; ++a)
                     if (lane == a) v = acc[a];
-                q[6 * r + lane] = v;
-                pq += p[6 * r + lane] * v;
+                const int i = 6 * r + lane;
+                const double pi = pv(i);
+                q[i] = v;
+                p_new[i] = pi;
+                pq += pi * v;
             }
         } else {
             const int c = r - sys.ncb;
             double v = 0.0;
-            for (int k = lane; k < n6; k += 32) v = fma(sys.border[static_cast<size_t>(k) * nb + c], p[k], v);
-            for (int d = lane; d < nb; d += 32) v = fma(sys.Cm[c * nb + d], p[n6 + d], v);
+            const double* Bc = sys.border_t + static_cast<size_t>(c) * n6;
+#pragma unroll 4
+            for (int k = lane; k < n6; k += 32) v = fma(Bc[k], pv(k), v);
+            for (int d = lane; d < nb; d += 32) v = fma(sys.Cm[c * nb + d], pv(n6 + d), v);
             v = warp_sum(v);
             if (lane == 0) {
-                q[n6 + c] = v;
-                pq += p[n6 + c] * v;
+                const int i = n6 + c;
+                const double pi = pv(i);
+                q[i] = v;
+                p_new[i] = pi;
+                pq += pi * v;
             }
         }
     }
@@ -469,16 +494,17 @@ __global__ void __launch_bounds__(kCgThreads) k_dense_cg(PcgSystem<double> sys, 
                                                          const double* __restrict__ dscale,
                                                          const double* __restrict__ b, double* __restrict__ x,
                                                          double* __restrict__ r, double* __restrict__ z,
-                                                         double* __restrict__ p, double* __restrict__ q,
-                                                         T* __restrict__ u, T* __restrict__ w,
-                                                         double* __restrict__ part, double* __restrict__ out,
-                                                         double rel_tol, double abs_tol, int max_it) {
+                                                         double* __restrict__ p, double* __restrict__ p2,
+                                                         double* __restrict__ q, T* __restrict__ u,
+                                                         T* __restrict__ w, double* __restrict__ part,
+                                                         double* __restrict__ out, double rel_tol, double abs_tol,
+                                                         int max_it) {
     cgk::grid_group grid = cgk::this_grid();
     __shared__ double s_red[kCgWarps + 1];
     const int n = 6 * sys.ncb + sys.nb;
     const int gt = blockIdx.x * blockDim.x + threadIdx.x, nt = gridDim.x * blockDim.x;
     double* mypart = part + static_cast<size_t>(blockIdx.x) * kCgPart;
-    // r = b, x = 0; w = X D r
+    // r = b, x = 0, u = D r; z = D M u
     double bb = 0.0;
     for (int i = gt; i < n; i += nt) {
         x[i] = 0.0;
@@ -495,13 +521,19 @@ __global__ void __launch_bounds__(kCgThreads) k_dense_cg(PcgSystem<double> sys, 
     const double bnorm = sqrt(grid_total(part, 0, s_red));
     double rz = grid_total(part, 1, s_red);
     const double tol = fmax(rel_tol * bnorm, abs_tol);
-    for (int i = gt; i < n; i += nt) p[i] = z[i];
-    double rn = bnorm;
+    double rn = bnorm, beta = 0.0;
     int it = 0, status = 0;
     bool converged = rn <= tol;
-    grid.sync();
+    double* p_old = p2;
+    double* p_cur = p;
     while (!converged && it < max_it) {
-        block_partial(spmv_rows(sys, p, q), s_red, mypart + 2);
+        // p = z + beta p, q = S p (the direction buffers alternate)
+        {
+            double* t = p_old;
+            p_old = p_cur;
+            p_cur = t;
+        }
+        block_partial(spmv_update(sys, z, beta, p_old, p_cur, q), s_red, mypart + 2);
         grid.sync();
         const double pq = grid_total(part, 2, s_red);
         if (!(pq > 0.0) || !isfinite(pq) || !isfinite(rz)) {
@@ -511,7 +543,7 @@ __global__ void __launch_bounds__(kCgThreads) k_dense_cg(PcgSystem<double> sys, 
         const double alpha = rz / pq;
         double rr = 0.0;
         for (int i = gt; i < n; i += nt) {
-            x[i] = fma(alpha, p[i], x[i]);
+            x[i] = fma(alpha, p_cur[i], x[i]);
             const double rv = fma(-alpha, q[i], r[i]);
             r[i] = rv;
             u[i] = static_cast<T>(dscale[i] * rv);
@@ -529,15 +561,14 @@ __global__ void __launch_bounds__(kCgThreads) k_dense_cg(PcgSystem<double> sys, 
             converged = true;
             break;
         }
+        // z = D X^T X D r
         tri_rows<T, true>(X, np, n, u, w, nullptr, nullptr, nullptr);
         grid.sync();
         block_partial(tri_rows<T, false>(XT, np, n, w, nullptr, z, dscale, r), s_red, mypart + 1);
         grid.sync();
         const double rz_new = grid_total(part, 1, s_red);
-        const double beta = rz_new / rz;
+        beta = rz_new / rz;
         rz = rz_new;
-        for (int i = gt; i < n; i += nt) p[i] = fma(beta, p[i], z[i]);
-        grid.sync();
     }
     if (gt == 0) {
         out[0] = it;
@@ -623,7 +654,8 @@ int dense_pcg(const PcgSystem<double>& sys, DenseWork<T>& W, const double* b, do
     const double* dscale = W.dscale;
     double rt = rel_tol, at = abs_tol;
     int mi = max_it;
-    void* args[] = {&s, &X, &XT, &np, &dscale, &b, &W.x, &W.r, &W.z, &W.p, &W.q, &W.ut, &W.wt, &W.part, &W.scal, &rt, &at, &mi};
+    void* args[] = {&s, &X, &XT, &np, &dscale, &b, &W.x, &W.r, &W.z, &W.p, &W.w, &W.q, &W.ut, &W.wt, &W.part,
+                    &W.scal, &rt, &at, &mi};
     const cudaError_t e = cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(&k_dense_cg<T>), dim3(grid),
                                                       dim3(kCgThreads), args, 0, st);
     if (e != cudaSuccess) return -1;
@@ -633,6 +665,11 @@ int dense_pcg(const PcgSystem<double>& sys, DenseWork<T>& W, const double* b, do
     *iterations = static_cast<int>(h_scal[0]);
     *relres = h_scal[1];
     *converged = h_scal[2] != 0.0;
+    // opt-in trace (PB_GPU_TRACE=1): one line per CG launch
+    static const bool trace = std::getenv("PB_GPU_TRACE") != nullptr;
+    if (trace)
+        std::fprintf(stderr, "PB_GPU_CG precision=%d iterations=%d relres=%.3e converged=%d max_it=%d grid=%d\n",
+                     sizeof(T) == 4 ? 1 : 0, *iterations, *relres, *converged ? 1 : 0, max_it, grid);
     return h_scal[3] != 0.0 ? 1 : 0;
 }
 

@@ -31,7 +31,8 @@ __global__ void k_reduce_pairs(Shape S, DevPtrs D, const typename Acc<T>::part_t
 // Sum of the per-camera partials: rhs, direct rhs and the intrinsic border rows.
 template <typename T>
 __global__ void k_reduce_cams(Shape S, DevPtrs D, const typename Acc<T>::part_type* __restrict__ part_cam,
-                              double* __restrict__ rhs, double* __restrict__ direct, double* __restrict__ border) {
+                              double* __restrict__ rhs, double* __restrict__ direct, double* __restrict__ border,
+                              double* __restrict__ border_t) {
     const int camrec = 12 + S.ng * 6 * S.ni;
     const long long idx = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (idx >= static_cast<long long>(S.ncb) * camrec) return;
@@ -46,6 +47,7 @@ __global__ void k_reduce_cams(Shape S, DevPtrs D, const typename Acc<T>::part_ty
         const int f = e - 12;  // (g * 6 + a) * ni + c
         const int g = f / (6 * S.ni), rem = f - g * 6 * S.ni, a = rem / S.ni, c = rem - a * S.ni;
         border[(static_cast<size_t>(i) * 6 + a) * S.nb + g * S.ni + c] = v;
+        border_t[static_cast<size_t>(g * S.ni + c) * 6 * S.ncb + i * 6 + a] = v;
     }
 }
 
@@ -591,7 +593,7 @@ void launch_reduce(const Shape& S, const DevPtrs& D, const AsmOut& O, const RedO
     const long long nc = static_cast<long long>(S.ncb) * (12 + S.ng * 6 * S.ni);
     if (nc > 0)
         k_reduce_cams<T><<<static_cast<unsigned>((nc + 255) / 256), 256, 0, st>>>(S, D, P.part_cam, R.rhs, R.direct,
-                                                                                  R.border);
+                                                                                  R.border, R.border_t);
     const int chrec = S.nb * S.nb + 2 * S.nb;
     const int tiles = (chrec + 31) / 32;
     k_reduce_chunks<T><<<tiles + 1, 256, 0, st>>>(S, P.part_chunk, O.part_cost, O.part_flags, R.Cm, R.rhs + 6 * S.ncb,

@@ -44,6 +44,7 @@ template <typename T>
 struct RedOut {
     T* vals;
     T* border;
+    T* border_t;  // B^T (nb x 6*ncb), for coalesced border rows in the solvers
     T* Cm;
     T* rhs;
     T* direct;
@@ -79,6 +80,7 @@ struct PcgSystem {
     const int* diag_pos;
     const T* vals;
     const T* border;
+    const T* border_t;  // B^T, nb x 6*ncb
     const T* Cm;
     T* Dinv;       // ncb * 36 block-Jacobi inverses
     T* Cinv;       // ng * ni * ni

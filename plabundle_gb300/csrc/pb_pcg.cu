@@ -82,10 +82,25 @@ __global__ void k_precond(PcgSystem<T> sys, int* status) {
     }
 }
 
-// Sum of per-block partial `slot` over the grid in a fixed order (every block obtains the same value).
+// Sum of per-block partial `slot` over the grid in a fixed order (every block obtains the same
+// value).  A lane's loads are issued back to back (no dependent chain through L2), then summed in
+// block order.
 __device__ __forceinline__ double grid_total(const double* part, int slot, int nblocks) {
+    constexpr int kPerLane = 16;  // up to 512 blocks
+    const int lane = threadIdx.x & 31;
     double v = 0.0;
-    for (int b = threadIdx.x & 31; b < nblocks; b += 32) v += part[static_cast<size_t>(b) * kPartStride + slot];
+    if (nblocks <= 32 * kPerLane) {
+        double t[kPerLane];
+#pragma unroll
+        for (int m = 0; m < kPerLane; ++m) {
+            const int b = lane + 32 * m;
+            t[m] = b < nblocks ? part[static_cast<size_t>(b) * kPartStride + slot] : 0.0;
+        }
+#pragma unroll
+        for (int m = 0; m < kPerLane; ++m) v += t[m];
+    } else {
+        for (int b = lane; b < nblocks; b += 32) v += part[static_cast<size_t>(b) * kPartStride + slot];
+    }
     return warp_sum(v);
 }
 
@@ -107,7 +122,8 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg(PcgSystem<T> sys, const T* 
     __shared__ double s_tot[kPartStride];
     __shared__ T s_pb[kMaxNB], s_qb[kMaxNB], s_rb[kMaxNB];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int gw = blockIdx.x * kPcgWarps + warp, tw = gridDim.x * kPcgWarps;
+    // warp-major row order: consecutive block rows go to different blocks (SMs)
+    const int gw = warp * gridDim.x + blockIdx.x, tw = gridDim.x * kPcgWarps;
     const int ncb = sys.ncb, nb = sys.nb, n6 = 6 * ncb, ng = sys.ng, ni = sys.ni;
     const int nblk = gridDim.x;
 
@@ -120,13 +136,12 @@ __global__ void __launch_bounds__(kPcgThreads) k_pcg(PcgSystem<T> sys, const T* 
         }
     };
     auto totals = [&](const double* part, int nslots) {
-        // warp 0 sums slots; results broadcast through shared memory
+        // slots spread over the warps; results broadcast through shared memory
         __syncthreads();
-        if (warp == 0)
-            for (int s = 0; s < nslots; ++s) {
-                const double v = grid_total(part, s, nblk);
-                if (lane == 0) s_tot[s] = v;
-            }
+        for (int s = warp; s < nslots; s += kPcgWarps) {
+            const double v = grid_total(part, s, nblk);
+            if (lane == 0) s_tot[s] = v;
+        }
         __syncthreads();
     };
     for (int i = threadIdx.x; i < kPcgWarps * kPartStride; i += blockDim.x) s_red[i] = 0.0;

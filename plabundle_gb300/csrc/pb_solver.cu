@@ -94,6 +94,7 @@ struct pb_gpu_ctx {
     DenseWork<double> dw64;
     double shift32 = 1e-7;  // last FP32 factor shift that factorised
     int f32_age = -1;       // LM solves served by the current FP32 factor (-1: none)
+    bool f32_stale = false; // the last accepted step changed the cost by more than 1 %
     int f32_base_iters = 0; // CG iterations of the first solve with that factor
     bool dense_ready[2] = {false, false};
     int last_solver = 0;
@@ -292,12 +293,15 @@ void upload_structure(pb_gpu_ctx* c) {
     // reduced system (FP64) and the block-Jacobi PCG buffers
     c->red.vals = A.alloc<double>(static_cast<size_t>(std::max(1, S.nnzb)) * 36);
     c->red.border = A.alloc<double>(static_cast<size_t>(std::max(1, S.ncb)) * 6 * std::max(1, S.nb));
+    c->red.border_t = A.alloc<double>(static_cast<size_t>(std::max(1, S.ncb)) * 6 * std::max(1, S.nb));
     c->red.Cm = A.alloc<double>(static_cast<size_t>(std::max(1, S.nb * S.nb)));
     c->red.rhs = A.alloc<double>(std::max(1, n));
     c->red.direct = A.alloc<double>(std::max(1, n));
     c->red.result = A.alloc<double>(2);
     check(cudaMemsetAsync(c->red.vals, 0, static_cast<size_t>(std::max(1, S.nnzb)) * 36 * sizeof(double), st), "memset");
     check(cudaMemsetAsync(c->red.border, 0, static_cast<size_t>(std::max(1, S.ncb)) * 6 * std::max(1, S.nb) * sizeof(double), st),
+          "memset");
+    check(cudaMemsetAsync(c->red.border_t, 0, static_cast<size_t>(std::max(1, S.ncb)) * 6 * std::max(1, S.nb) * sizeof(double), st),
           "memset");
     c->direct64 = c->red.direct;
     PcgSystem<double>& sy = c->sys;
@@ -310,6 +314,7 @@ void upload_structure(pb_gpu_ctx* c) {
     sy.diag_pos = D.diag_pos;
     sy.vals = c->red.vals;
     sy.border = c->red.border;
+    sy.border_t = c->red.border_t;
     sy.Cm = c->red.Cm;
     sy.Dinv = A.alloc<double>(static_cast<size_t>(std::max(1, S.ncb)) * 36);
     sy.Cinv = A.alloc<double>(static_cast<size_t>(std::max(1, S.ng)) * kMaxNI * kMaxNI);
@@ -478,7 +483,7 @@ void ensure_dense(pb_gpu_ctx* c) {
 }
 
 constexpr int kMaxFactorAge = 10;     // LM solves one FP32 factor may precondition
-constexpr int kReuseIterations = 150; // CG iterations allowed on a kept factor before refactoring
+constexpr int kReuseIterations = 60;  // CG iterations allowed on a kept factor before refactoring
 
 template <typename T>
 int solve_dense(pb_gpu_ctx* c, double rel, double abs_tol, int max_it, bool* converged, int* iterations,
@@ -487,11 +492,11 @@ int solve_dense(pb_gpu_ctx* c, double rel, double abs_tol, int max_it, bool* con
     DenseWork<T>& W = dwork<T>(c);
     const bool f32 = std::is_same<T, float>::value;
     int spent = 0;
-    if (f32 && c->f32_age >= 0 && c->f32_age < kMaxFactorAge) {
+    if (f32 && c->f32_age >= 0 && c->f32_age < kMaxFactorAge && !c->f32_stale) {
         // The reduced matrix changes little between LM iterations: the FP32 factor of an earlier
         // one still preconditions the CG on the current FP64 matrix.  A factorisation costs
-        // about as much as a few hundred CG iterations, so the kept factor is used until the
-        // CG needs more than kReuseIterations on it.
+        // about as much as a hundred CG iterations, so the kept factor is used until the CG
+        // needs more than kReuseIterations on it.
         const int cap = std::min(max_it, std::max(kReuseIterations, 4 * c->f32_base_iters));
         const int rc = dense_pcg<T>(c->sys, W, c->red.rhs, rel, abs_tol, cap, iterations, relres, converged,
                                     c->h_scratch + 40, c->stream, &c->launches);
@@ -689,6 +694,7 @@ int do_assemble(pb_gpu_ctx* c, double damping, int precision, double* cost, int*
 // The LM / Armijo driver (online branch of optimizePointsWithPlaMatrix).
 void lm_solve(pb_gpu_ctx* c, const pb_solve_options& op, pb_solve_report* rep) {
     c->f32_age = -1;  // every solve starts from a fresh factor: repeated solves run identically
+    c->f32_stale = false;
     const auto t0 = std::chrono::steady_clock::now();
     const HostModel& m = c->model;
     std::memset(rep, 0, sizeof(*rep));
@@ -827,6 +833,9 @@ void lm_solve(pb_gpu_ctx* c, const pb_solve_options& op, pb_solve_report* rep) {
                 if (accepted_slot >= 0) {
                     launch_accept(c->S[0], c->D[0], c->step_p, accepted_alpha, accepted_slot, c->stream);
                     c->launches += 1;
+                    // a large cost decrease means a large change of the reduced matrix: the next
+                    // solve refactors instead of trying the kept FP32 factor first
+                    c->f32_stale = current - cand > 1e-2 * current;
                     current = cand;
                     ++rep->accepted_steps;
                     damping /= 10.0;

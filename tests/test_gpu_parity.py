@@ -222,3 +222,26 @@ def test_mixed_solve_converges_to_the_oracle_fixed_point(name, make, opts):
     np.testing.assert_allclose(out["rms_before"], ref["rms_before"], rtol=1e-12)
     if ref["intrinsics"].size:
         np.testing.assert_allclose(out["intrinsics"], ref["intrinsics"], rtol=2e-5, atol=1e-7)
+
+
+@pytest.mark.parametrize("mixed", [False, True])
+def test_block_jacobi_pcg_solve_matches_oracle(mixed):
+    """The block-Jacobi PCG path (used above 16384 reduced unknowns), forced on the ring: the LM
+    solve with the PCG to the reference's 2e-10 relative residual reaches the oracle's solution."""
+    p = ring()
+    o = ring_options(mixed)
+    o.solver.maxIterations = 40
+    o.backend.linearSolver = 2
+    o_ref = ring_options(False)
+    o_ref.solver.maxIterations = 40
+    ref = O.Oracle(p, o_ref).solve()
+    ctx = gpu(p, o)
+    rep = ctx.solve()
+    out = ctx.download()
+    rr = ref["report"]
+    assert rep["status"] == rr["status"] == SolveStatus.Success
+    assert abs(rep["final_cost"] - rr["final_cost"]) / rr["final_cost"] < 1e-8
+    C_ref = ref["cameras"][:, 9:12]
+    scale = np.linalg.norm(C_ref - C_ref.mean(0), axis=1).max()
+    assert np.abs(out["cameras"][:, 9:12] - C_ref).max() / scale < 1e-6
+    assert np.array_equal(out["valid"], ref["valid"])
