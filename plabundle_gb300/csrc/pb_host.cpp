@@ -6,6 +6,7 @@
 #include <cstring>
 #include <limits>
 #include <numeric>
+#include <thread>
 
 #include "pb_internal.h"
 
@@ -16,6 +17,32 @@ namespace {
 constexpr double kInf = std::numeric_limits<double>::infinity();
 
 bool finite3(const double* v) { return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]); }
+
+// Host threads for a loop of n independent items: one per hardware thread, at most 32, and at
+// least 4096 items each.
+int host_threads(long long n) {
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const long long by_size = std::max(1LL, n / 4096);
+    return static_cast<int>(std::min<long long>(std::min<unsigned>(hw, 32u), by_size));
+}
+
+// f(i, begin, end) over `nthreads` contiguous ranges of [0, n); thread i gets range i.
+template <typename F>
+void parallel_ranges(int n, int nthreads, F f) {
+    if (nthreads <= 1) {
+        f(0, 0, n);
+        return;
+    }
+    std::vector<std::thread> pool;
+    pool.reserve(nthreads - 1);
+    for (int i = 1; i < nthreads; ++i)
+        pool.emplace_back([&, i] {
+            f(i, static_cast<int>(static_cast<long long>(n) * i / nthreads),
+              static_cast<int>(static_cast<long long>(n) * (i + 1) / nthreads));
+        });
+    f(0, 0, static_cast<int>(static_cast<long long>(n) / nthreads));
+    for (auto& th : pool) th.join();
+}
 
 double sanitized_weight(double w) { return std::isfinite(w) && w > 0.0 ? w : 0.0; }
 double sanitized_scale(double s) { return std::isfinite(s) && s > 0.0 ? s : 1.0; }
@@ -170,38 +197,63 @@ int build_host_model(const pb_problem_desc* pr, const pb_solve_options* op, Host
     std::vector<char> cam_has_residual(nc, 0), fixed_cam(nc, 0), fixed_trk(nt, 0);
     for (int c : m->fixed_cams) fixed_cam[c] = 1;
     for (int t : m->fixed_tracks) fixed_trk[t] = 1;
-    auto usable = [&](long long k) {
-        const int c = m->obs_cam[k];
-        return c >= 0 && c < nc && std::isfinite(m->obs_u[k]) && std::isfinite(m->obs_v[k]) &&
-               sanitized_weight(m->obs_weight[k]) > 0.0;
-    };
+    // usable observations (valid camera, finite pixel, positive weight), flagged once
+    std::vector<unsigned char> use(static_cast<size_t>(m->no), 0);
+    parallel_ranges(static_cast<int>(std::min<long long>(m->no, std::numeric_limits<int>::max())),
+                    host_threads(m->no), [&](int, int k0, int k1) {
+                        for (int k = k0; k < k1; ++k) {
+                            const int c = m->obs_cam[k];
+                            use[k] = c >= 0 && c < nc && std::isfinite(m->obs_u[k]) && std::isfinite(m->obs_v[k]) &&
+                                     sanitized_weight(m->obs_weight[k]) > 0.0;
+                        }
+                    });
+    auto usable = [&](long long k) { return use[k] != 0; };
     m->active_tracks = m->obs_count = m->rejected = 0;
-    for (int t = 0; t < nt; ++t) {
-        const double* X = &m->points_in[static_cast<size_t>(t) * 3];
-        if (!finite3(X)) continue;
-        int first = -1, count = 0;
-        bool second = false, positive = true;
-        double sq = 0.0;
-        for (long long k = m->offs[t]; k < m->offs[t + 1]; ++k) {
-            if (!usable(k)) continue;
-            const int c = m->obs_cam[k];
-            first = first < 0 ? c : first;
-            second = second || c != first;
-            double px[2];
-            if (!project(&m->cams_in[static_cast<size_t>(c) * kCamStride], X, px)) { positive = false; break; }
-            const double du = px[0] - m->obs_u[k], dv = px[1] - m->obs_v[k];
-            sq += sanitized_weight(m->obs_weight[k]) * (du * du + dv * dv);
-            ++count;
+    // The gate projects every observation: tracks are split over host threads, each thread
+    // keeps its own counts, and the counts are combined in thread order.
+    struct GateCounts {
+        int active = 0, obs = 0, rejected = 0;
+    };
+    auto gate = [&](int t0, int t1, GateCounts* gc) {
+        for (int t = t0; t < t1; ++t) {
+            const double* X = &m->points_in[static_cast<size_t>(t) * 3];
+            if (!finite3(X)) continue;
+            int first = -1, count = 0;
+            bool second = false, positive = true;
+            double sq = 0.0;
+            for (long long k = m->offs[t]; k < m->offs[t + 1]; ++k) {
+                if (!usable(k)) continue;
+                const int c = m->obs_cam[k];
+                first = first < 0 ? c : first;
+                second = second || c != first;
+                double px[2];
+                if (!project(&m->cams_in[static_cast<size_t>(c) * kCamStride], X, px)) { positive = false; break; }
+                const double du = px[0] - m->obs_u[k], dv = px[1] - m->obs_v[k];
+                sq += sanitized_weight(m->obs_weight[k]) * (du * du + dv * dv);
+                ++count;
+            }
+            const double rms = count > 0 ? std::sqrt(sq / (2.0 * count)) : kInf;
+            if (count < 2 || !second || !positive) continue;
+            if (op->max_initial_track_rms > 0.0 && rms > op->max_initial_track_rms) { ++gc->rejected; continue; }
+            m->active_track[t] = 1;
+            ++gc->active;
+            gc->obs += count;
         }
-        const double rms = count > 0 ? std::sqrt(sq / (2.0 * count)) : kInf;
-        if (count < 2 || !second || !positive) continue;
-        if (op->max_initial_track_rms > 0.0 && rms > op->max_initial_track_rms) { ++m->rejected; continue; }
-        m->active_track[t] = 1;
-        ++m->active_tracks;
-        m->obs_count += count;
-        for (long long k = m->offs[t]; k < m->offs[t + 1]; ++k)
-            if (usable(k)) cam_has_residual[m->obs_cam[k]] = 1;
+    };
+    {
+        const int nthreads = host_threads(nt);
+        std::vector<GateCounts> counts(nthreads);
+        parallel_ranges(nt, nthreads, [&](int i, int t0, int t1) { gate(t0, t1, &counts[i]); });
+        for (const GateCounts& gc : counts) {
+            m->active_tracks += gc.active;
+            m->obs_count += gc.obs;
+            m->rejected += gc.rejected;
+        }
     }
+    for (int t = 0; t < nt; ++t)
+        if (m->active_track[t])
+            for (long long k = m->offs[t]; k < m->offs[t + 1]; ++k)
+                if (usable(k)) cam_has_residual[m->obs_cam[k]] = 1;
     m->ncb = 0;
     if (op->refine_camera_pose)
         for (int c = 0; c < nc; ++c)
@@ -299,9 +351,15 @@ int build_host_model(const pb_problem_desc* pr, const pb_solve_options* op, Host
         const int P = m->P;
         std::vector<std::vector<int>> nbr(P);
         std::vector<int> tb;
+        // P x P seen-mask: each pair is recorded once however many tracks share it
+        std::vector<unsigned char> seen(static_cast<size_t>(P) * P, 0);
         auto connect = [&](int a, int b) {
             if (a < 0 || b < 0 || a == b) return;
-            nbr[std::min(a, b)].push_back(std::max(a, b));
+            const int lo = std::min(a, b), hi = std::max(a, b);
+            unsigned char& f = seen[static_cast<size_t>(lo) * P + hi];
+            if (f) return;
+            f = 1;
+            nbr[lo].push_back(hi);
         };
         for (int t = 0; t < nt; ++t) {
             if (!m->active_track[t]) continue;
@@ -372,25 +430,30 @@ int build_host_model(const pb_problem_desc* pr, const pb_solve_options* op, Host
 
     // --- processing order: active tracks sorted by their smallest pose block so that a chunk of
     // consecutive tracks touches few cameras; observations of each track kept in input order.
+    // The key is bounded (pose block, or nc + camera for cameras without one), so a stable
+    // counting sort gives the order of sorting (key, track index).
     {
-        std::vector<std::pair<long long, int>> key;
-        key.reserve(m->active_tracks);
+        const int nkeys = 2 * nc + 1;
+        std::vector<int> key(nt, -1), count(nkeys + 1, 0);
         for (int t = 0; t < nt; ++t) {
             if (!m->active_track[t]) continue;
-            int mn = std::numeric_limits<int>::max();
+            int mn = nkeys - 1;
             for (long long k = m->offs[t]; k < m->offs[t + 1]; ++k)
                 if (usable(k)) mn = std::min(mn, m->camera_block[m->obs_cam[k]] >= 0 ? m->camera_block[m->obs_cam[k]]
-                                                                                    : nc + m->obs_cam[k]);
-            key.emplace_back(static_cast<long long>(mn) * (static_cast<long long>(nt) + 1) + t, t);
+                                                                                     : nc + m->obs_cam[k]);
+            key[t] = mn;
+            ++count[mn + 1];
         }
-        std::sort(key.begin(), key.end());
-        m->trk_order.resize(key.size());
-        m->trk_obs_begin.assign(key.size() + 1, 0);
+        for (int i = 0; i < nkeys; ++i) count[i + 1] += count[i];
+        m->trk_order.assign(static_cast<size_t>(count[nkeys]), 0);
+        for (int t = 0; t < nt; ++t)
+            if (key[t] >= 0) m->trk_order[count[key[t]]++] = t;
+        const size_t ntp = m->trk_order.size();
+        m->trk_obs_begin.assign(ntp + 1, 0);
         m->p_obs_orig.clear();
         m->p_obs_orig.reserve(m->obs_count);
-        for (size_t i = 0; i < key.size(); ++i) {
-            const int t = key[i].second;
-            m->trk_order[i] = t;
+        for (size_t i = 0; i < ntp; ++i) {
+            const int t = m->trk_order[i];
             for (long long k = m->offs[t]; k < m->offs[t + 1]; ++k)
                 if (usable(k)) m->p_obs_orig.push_back(static_cast<int>(k));
             m->trk_obs_begin[i + 1] = static_cast<int>(m->p_obs_orig.size());
@@ -570,7 +633,7 @@ int build_chunks(HostModel* m, int precision, size_t smem_budget, std::string* e
         chunk_obs_start = obs_end;
     };
     pair_seen.assign(static_cast<size_t>(max_cams) * max_cams, 0);
-    std::vector<int> tcams;
+    std::vector<int> tcams, ol;
     std::vector<std::pair<int, int>> tpairs;
     for (int p = 0; p < ntp; ++p) {
         const int t = m->trk_order[p];
@@ -589,7 +652,7 @@ int build_chunks(HostModel* m, int precision, size_t smem_budget, std::string* e
                 ++new_cams;
                 return static_cast<int>(ccams.size() + tcams.size() - 1);
             };
-            std::vector<int> ol;
+            ol.clear();
             for (int o = o0; o < o1; ++o) {
                 const int c = m->obs_cam[m->p_obs_orig[o]];
                 ol.push_back(m->camera_block[c] >= 0 ? lidx(c) : -1);

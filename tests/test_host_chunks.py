@@ -23,7 +23,7 @@ SMEM_BUDGET = 227 * 1024 - 1024
 @pytest.fixture(scope="module")
 def probe(tmp_path_factory):
     out = str(tmp_path_factory.mktemp("probe") / "libhostprobe.so")
-    cmd = ["g++", "-std=c++17", "-O1", "-fPIC", "-shared", "-I", os.path.join(ROOT, "include"),
+    cmd = ["g++", "-std=c++17", "-O1", "-fPIC", "-shared", "-pthread", "-I", os.path.join(ROOT, "include"),
            os.path.join(HERE, "host_probe.cpp"), os.path.join(ROOT, "plabundle_gb300", "csrc", "pb_host.cpp"),
            "-o", out]
     subprocess.run(cmd, check=True, capture_output=True)
