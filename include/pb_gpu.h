@@ -243,6 +243,20 @@ pb_status pb_gpu_set_timing(pb_gpu_ctx* ctx, int32_t enable);
  * filled when timing is enabled. */
 pb_status pb_gpu_kernel_times(pb_gpu_ctx* ctx, double* out8);
 
+/* Batched solves of independent problems, e.g. local bundle-adjustment windows (no counterpart
+ * in the reference, which solves one problem per Solver::solve call).  Each problem is solved
+ * exactly as pb_gpu_solve_problem solves it, with the same options; n_workers host threads each
+ * own a context and its stream and take problems from a shared queue, so the kernels of
+ * different problems overlap on the device.  Per problem i: reports[i], and, when the pointer
+ * arrays and their entries are non-NULL, refined cameras / points / valid mask into
+ * cameras_out[i], points_out[i], valid_out[i], and the wall-clock time of its solve in
+ * latency_ms[i] (may be NULL).  Returns PB_OK, or the first failing status of any problem
+ * (all reports are still filled). */
+pb_status pb_gpu_solve_batch(int32_t device, int32_t n_problems, const pb_problem_desc* problems,
+                             const pb_solve_options* options, int32_t n_workers, pb_solve_report* reports,
+                             double* const* cameras_out, double* const* points_out, int8_t* const* valid_out,
+                             double* latency_ms);
+
 /* Allocation-free robust objective of caller-owned device arrays.  No counterpart in the
  * reference: it serves callers that keep their own cameras, points and observations in device
  * memory and may not allocate (a real-time loop whose device memory is reserved up front, where

@@ -16,6 +16,7 @@
 
 #include <cstdio>
 #include <cstdlib>
+#include <mutex>
 
 #include "pb_device.cuh"
 #include "pb_kernels.h"
@@ -594,11 +595,8 @@ template <typename T>
 int dense_factor(const PcgSystem<double>& sys, DenseWork<T>& W, double shift, cudaStream_t st, int* launches) {
     const int n = W.n, np = W.np, nt = W.nt;
     const size_t two_tiles = 2 * static_cast<size_t>(TS) * TP * sizeof(T);
-    static bool attrs[2] = {false, false};
-    if (!attrs[sizeof(T) == 8]) {
-        set_smem<T>(reinterpret_cast<const void*>(&k_potrf_coop<T>), two_tiles);
-        attrs[sizeof(T) == 8] = true;
-    }
+    static std::once_flag attrs;
+    std::call_once(attrs, [&] { set_smem<T>(reinterpret_cast<const void*>(&k_potrf_coop<T>), two_tiles); });
     int L = 0;
     cudaMemsetAsync(W.status, 0, sizeof(int), st);
     cudaMemsetAsync(W.A, 0, static_cast<size_t>(np) * np * sizeof(T), st);
@@ -622,7 +620,9 @@ int dense_factor(const PcgSystem<double>& sys, DenseWork<T>& W, double shift, cu
         int npv = np, ntv = nt;
         int* stv = W.status;
         void* args[] = {&A, &X, &Dv, &npv, &ntv, &stv};
-        if (cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(&k_potrf_coop<T>), dim3(W.fact_grid), dim3(256),
+        // one block per lower tile at most: small systems take a small grid
+        const int fgrid = std::max(1, std::min(W.fact_grid, nt * (nt + 1) / 2));
+        if (cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(&k_potrf_coop<T>), dim3(fgrid), dim3(256),
                                         args, two_tiles, st) != cudaSuccess)
             return -1;
         ++L;
@@ -646,7 +646,9 @@ int dense_pcg(const PcgSystem<double>& sys, DenseWork<T>& W, const double* b, do
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dense_cg<T>, kCgThreads, 0);
         W.coop_grid = std::max(1, std::min(per_sm, 2) * sms);
     }
-    const int grid = W.coop_grid;
+    // one warp per row of the triangular products: small systems (local windows) take a small
+    // grid and leave the rest of the device to concurrent work
+    const int grid = std::max(1, std::min(W.coop_grid, (W.n + kCgWarps - 1) / kCgWarps));
     PcgSystem<double> s = sys;
     const T* X = W.X;
     const T* XT = W.A;

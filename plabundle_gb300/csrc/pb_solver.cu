@@ -33,21 +33,44 @@ namespace {
 constexpr double kNaN = std::numeric_limits<double>::quiet_NaN();
 constexpr double kInfD = std::numeric_limits<double>::infinity();
 
+// Device memory of a context: slabs carved by a bump pointer (256-byte aligned).  release()
+// rewinds the slabs for the next problem instead of freeing them, so a context that solves one
+// problem after another (local-BA windows) stops calling cudaMalloc once its slabs are large
+// enough; free_all() returns the memory.  Buffers are not cleared: whatever must start at zero
+// is set explicitly by its user.
 struct DeviceArena {
-    std::vector<void*> blocks;
+    struct Slab {
+        char* base;
+        size_t size, used;
+    };
+    std::vector<Slab> slabs;
     size_t bytes = 0;
+    static constexpr size_t kAlign = 256, kMinSlab = size_t(8) << 20;
     template <typename T>
     T* alloc(size_t count) {
         if (count == 0) count = 1;
+        const size_t need = (count * sizeof(T) + kAlign - 1) & ~(kAlign - 1);
+        for (Slab& sl : slabs)
+            if (sl.size - sl.used >= need) {
+                T* p = reinterpret_cast<T*>(sl.base + sl.used);
+                sl.used += need;
+                bytes += need;
+                return p;
+            }
+        const size_t size = std::max(need, kMinSlab);
         void* p = nullptr;
-        if (cudaMalloc(&p, count * sizeof(T)) != cudaSuccess) throw std::bad_alloc();
-        blocks.push_back(p);
-        bytes += count * sizeof(T);
+        if (cudaMalloc(&p, size) != cudaSuccess) throw std::bad_alloc();
+        slabs.push_back({static_cast<char*>(p), size, need});
+        bytes += need;
         return static_cast<T*>(p);
     }
     void release() {
-        for (void* p : blocks) cudaFree(p);
-        blocks.clear();
+        for (Slab& sl : slabs) sl.used = 0;
+        bytes = 0;
+    }
+    void free_all() {
+        for (Slab& sl : slabs) cudaFree(sl.base);
+        slabs.clear();
         bytes = 0;
     }
 };
@@ -938,10 +961,10 @@ pb_status pb_gpu_destroy(pb_gpu_ctx* c) {
     if (!c) return PB_ERR_INVALID_ARGUMENT;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
-    c->arena.release();
-    c->parena[0].release();
-    c->parena[1].release();
-    c->darena.release();
+    c->arena.free_all();
+    c->parena[0].free_all();
+    c->parena[1].free_all();
+    c->darena.free_all();
     if (c->h_scratch) cudaFreeHost(c->h_scratch);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
@@ -1105,7 +1128,7 @@ pb_status pb_gpu_linearize_observations(pb_gpu_ctx* c, int32_t precision, double
         d2h(cost, dcost, no * sizeof(double));
         d2h(valid, dvalid, no);
         check(cudaStreamSynchronize(st), "linearize");
-        tmp.release();
+        tmp.free_all();
         return PB_OK;
     } catch (const std::exception& e) {
         return fail(c, PB_ERR_CUDA, e.what());

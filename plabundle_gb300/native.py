@@ -20,7 +20,7 @@ EXPORTED = [
     "pb_gpu_back_substitute", "pb_gpu_eval_cost", "pb_gpu_eval_cost_batch", "pb_gpu_apply_step", "pb_gpu_solve",
     "pb_gpu_download_state", "pb_gpu_solve_problem", "pb_gpu_request_cancel", "pb_gpu_get_stream",
     "pb_gpu_set_timing",
-    "pb_gpu_kernel_times", "pb_gpu_objective_noalloc",
+    "pb_gpu_kernel_times", "pb_gpu_objective_noalloc", "pb_gpu_solve_batch",
 ]
 
 
@@ -114,6 +114,7 @@ def load(build_if_missing: bool = False):
     L.pb_gpu_set_timing.argtypes = [vp, i32]
     L.pb_gpu_get_stream.argtypes = [vp, C.POINTER(vp)]
     L.pb_gpu_kernel_times.argtypes = [vp, vp]
+    L.pb_gpu_solve_batch.argtypes = [i32, i32, vp, C.POINTER(SolveOptionsC), i32, vp, vp, vp, vp, vp]
     L.pb_gpu_objective_noalloc.argtypes = [vp, i32, vp, i32, vp, vp, vp, vp, vp, i64, i32, dbl, vp,
                                            C.POINTER(dbl), C.POINTER(i64)]
     for name in EXPORTED:

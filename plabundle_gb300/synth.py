@@ -69,6 +69,23 @@ def project(cameras: np.ndarray, cam_idx: np.ndarray, X: np.ndarray):
     return np.stack([u, v], axis=1), valid
 
 
+def _project_one(cam: np.ndarray, X: np.ndarray):
+    """`project` of all points X [n, 3] with one camera record (no per-point gather)."""
+    R = cam[0:9].reshape(3, 3)
+    xc = (X - cam[9:12]) @ R
+    z = xc[:, 2]
+    valid = (-z if cam[23] != 0 else z) > 1e-9
+    zs = np.where(valid, z, 1.0)
+    x = xc[:, 0] / zs
+    y = xc[:, 1] / zs
+    r2 = x * x + y * y
+    k1, k2, k3, p1, p2 = cam[16:21]
+    radial = 1 + k1 * r2 + k2 * r2 * r2 + k3 * r2 ** 3
+    xd = x * radial + p1 * 2 * x * y + p2 * (r2 + 2 * x * x)
+    yd = y * radial + p1 * (r2 + 2 * y * y) + p2 * 2 * x * y
+    return np.stack([cam[21] * cam[12] * xd + cam[14], cam[22] * cam[13] * yd + cam[15]], axis=1), valid
+
+
 def rotation_from_axis_angle(w: np.ndarray) -> np.ndarray:
     th = np.linalg.norm(w)
     if th < 1e-15:
@@ -87,22 +104,40 @@ def perturb_cameras(cameras: np.ndarray, rng, rot_sigma: float, centre_sigma: fl
     return out
 
 
+def _choose_views_vectorized(visible_mask, rng, min_views, max_views):
+    """Per point, a uniformly random subset of min(k, visible) of its visible cameras with
+    k ~ U{min_views..max_views}, in camera order; vectorised over points (random keys, keep the
+    k smallest)."""
+    n_pts, n_c = visible_mask.shape
+    k = rng.integers(min_views, max_views + 1, n_pts)
+    keys = np.where(visible_mask, rng.random((n_pts, n_c)), np.inf)
+    rank = np.argsort(np.argsort(keys, axis=1), axis=1)
+    chosen = visible_mask & (rank < k[:, None])
+    counts = chosen.sum(1).astype(np.int64)
+    cam_idx = np.nonzero(chosen)[1].astype(np.int32)  # row-major: per point, cameras ascending
+    return counts, cam_idx
+
+
 def _assemble(cameras_true, cameras_init, X_true, X_init, visible_lists, rng, noise, outlier_frac,
-              min_views, max_views):
-    """Picks views per point, projects, adds noise and outliers; returns track-CSR arrays."""
+              min_views, max_views, visible_mask=None):
+    """Picks views per point, projects, adds noise and outliers; returns track-CSR arrays.
+    With `visible_mask` ([points, cameras] bool) the views are drawn vectorised."""
     n_pts = X_true.shape[0]
-    counts = np.zeros(n_pts, np.int64)
-    chosen = []
-    for t in range(n_pts):
-        vis = visible_lists[t]
-        k = int(rng.integers(min_views, max_views + 1))
-        if vis.size > k:
-            vis = np.sort(rng.choice(vis, size=k, replace=False))
-        chosen.append(vis)
-        counts[t] = vis.size
+    if visible_mask is not None:
+        counts, cam_idx = _choose_views_vectorized(visible_mask, rng, min_views, max_views)
+    else:
+        counts = np.zeros(n_pts, np.int64)
+        chosen = []
+        for t in range(n_pts):
+            vis = visible_lists[t]
+            k = int(rng.integers(min_views, max_views + 1))
+            if vis.size > k:
+                vis = np.sort(rng.choice(vis, size=k, replace=False))
+            chosen.append(vis)
+            counts[t] = vis.size
+        cam_idx = np.concatenate(chosen).astype(np.int32) if n_pts else np.zeros(0, np.int32)
     offsets = np.zeros(n_pts + 1, np.int64)
     np.cumsum(counts, out=offsets[1:])
-    cam_idx = np.concatenate(chosen).astype(np.int32) if n_pts else np.zeros(0, np.int32)
     pt_idx = np.repeat(np.arange(n_pts), counts)
     px, _ = project(cameras_true, cam_idx, X_true[pt_idx])
     px = px + rng.normal(0.0, noise, px.shape)
@@ -122,10 +157,19 @@ def _problem(cameras_init, X_init, offsets, cam_idx, px, **kw) -> Problem:
                    obs_scale=np.ones(n_obs), **kw).normalized()
 
 
-def _visible(cameras, X, margin=0.0):
-    """Per point, the sorted indices of the cameras that see it in front and in frame."""
+def _visible(cameras, X, margin=0.0, as_mask=False):
+    """Per point, the sorted indices of the cameras that see it in front and in frame (or the
+    [points, cameras] visibility mask with `as_mask`)."""
     n_c = cameras.shape[0]
-    lists = []
+    if as_mask:
+        # camera by camera: all points against one camera record, no per-pair gather
+        mask = np.zeros((X.shape[0], n_c), bool)
+        for c in range(n_c):
+            px, valid = _project_one(cameras[c], X)
+            mask[:, c] = valid & (px[:, 0] >= margin) & (px[:, 0] < cameras[c, 24] - margin) \
+                & (px[:, 1] >= margin) & (px[:, 1] < cameras[c, 25] - margin)
+        return mask
+    lists, masks = [], []
     chunk = max(1, 4_000_000 // max(1, n_c))
     for s in range(0, X.shape[0], chunk):
         Xs = X[s:s + chunk]
@@ -136,13 +180,21 @@ def _visible(cameras, X, margin=0.0):
         inside = valid & (px[:, 0] >= margin) & (px[:, 0] < cameras[ci, 24] - margin) \
             & (px[:, 1] >= margin) & (px[:, 1] < cameras[ci, 25] - margin)
         inside = inside.reshape(m, n_c)
-        lists.extend(np.nonzero(row)[0] for row in inside)
+        if as_mask:
+            masks.append(inside)
+        else:
+            lists.extend(np.nonzero(row)[0] for row in inside)
+    if as_mask:
+        return np.concatenate(masks) if masks else np.zeros((0, n_c), bool)
     return lists
 
 
 def ring_problem(seed: int = 7, n_cameras: int = 20, n_points: int = 2000, noise: float = 0.5,
                  outlier_frac: float = 0.02, rot_sigma: float = 0.01, centre_sigma: float = 0.05,
-                 point_sigma: float = 0.05, min_views: int = 3, max_views: int = 6) -> Problem:
+                 point_sigma: float = 0.05, min_views: int = 3, max_views: int = 6,
+                 vectorized_views: bool = False) -> Problem:
+    """The ring of cameras around a point cloud.  `vectorized_views` draws the views of all points
+    at once (same distribution, another random stream; used for large batches of windows)."""
     rng = np.random.default_rng(seed)
     cams = []
     for i in range(n_cameras):
@@ -153,8 +205,13 @@ def ring_problem(seed: int = 7, n_cameras: int = 20, n_points: int = 2000, noise
                                 width=4000.0, height=3000.0))
     cams = np.array(cams)
     X = rng.uniform(-2.0, 2.0, (n_points, 3))
-    vis = _visible(cams, X)
-    offsets, cam_idx, px = _assemble(cams, None, X, None, vis, rng, noise, outlier_frac, min_views, max_views)
+    if vectorized_views:
+        mask = _visible(cams, X, as_mask=True)
+        offsets, cam_idx, px = _assemble(cams, None, X, None, None, rng, noise, outlier_frac, min_views, max_views,
+                                         visible_mask=mask)
+    else:
+        vis = _visible(cams, X)
+        offsets, cam_idx, px = _assemble(cams, None, X, None, vis, rng, noise, outlier_frac, min_views, max_views)
     cams0 = perturb_cameras(cams, rng, rot_sigma, centre_sigma)
     X0 = X + rng.normal(0.0, point_sigma, X.shape)
     prob = _problem(cams0, X0, offsets, cam_idx, px)
@@ -263,7 +320,7 @@ def window_problems(n_windows: int = 256, seed: int = 1234, cameras=(10, 60), po
     for w in range(n_windows):
         nc = int(rng.integers(cameras[0], cameras[1] + 1))
         npt = int(rng.integers(points[0], points[1] + 1))
-        out.append(ring_problem(seed=seed * 1000 + w, n_cameras=nc, n_points=npt))
+        out.append(ring_problem(seed=seed * 1000 + w, n_cameras=nc, n_points=npt, vectorized_views=True))
     return out
 
 
