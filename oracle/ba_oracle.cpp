@@ -1683,3 +1683,361 @@ int32_t orc_solve(void* h, orc_report* rep, double* camsOut, double* ptsOut, int
 }
 
 }  // extern "C"
+
+// =================================================================================================
+// Implicit-differentiation reference (adjoint of the converged fixed point).
+//
+// Not a restatement of reference code (the reference has no adjoint): it is the independent CPU
+// check of the GPU backward pass.  Every observation's robust cost is written once more as a
+// function of local chart variables around a fixed state (the solver's own retractions:
+// rotation increment C2W' = D E(w)^T D C2W with E = Rx Ry Rz, world-frame centre increment or
+// the 2-DoF gauge tangent on the sphere |C - C_anchor| = baseline, point increment X + s(X) dX,
+// additive group intrinsics) and differentiated twice with hyper-dual numbers, which give exact
+// first and second derivatives (no truncation error).  The Python side assembles the sparse
+// Hessian from the per-observation blocks and solves it with a sparse direct factorisation.
+// =================================================================================================
+namespace orc {
+
+// Hyper-dual number v + a e1 + b e2 + ab e1 e2 (e1^2 = e2^2 = 0).
+struct HD {
+    double v = 0.0, a = 0.0, b = 0.0, ab = 0.0;
+    HD() = default;
+    HD(double x) : v(x) {}  // NOLINT: constants promote implicitly
+    HD(double x, double da, double db, double dab) : v(x), a(da), b(db), ab(dab) {}
+};
+inline HD operator+(const HD& x, const HD& y) { return {x.v + y.v, x.a + y.a, x.b + y.b, x.ab + y.ab}; }
+inline HD operator-(const HD& x, const HD& y) { return {x.v - y.v, x.a - y.a, x.b - y.b, x.ab - y.ab}; }
+inline HD operator-(const HD& x) { return {-x.v, -x.a, -x.b, -x.ab}; }
+inline HD operator*(const HD& x, const HD& y) {
+    return {x.v * y.v, x.v * y.a + x.a * y.v, x.v * y.b + x.b * y.v,
+            x.v * y.ab + x.a * y.b + x.b * y.a + x.ab * y.v};
+}
+// f(x) for a scalar function with value f0, first derivative f1 and second derivative f2 at x.v
+inline HD chain(const HD& x, double f0, double f1, double f2) {
+    return {f0, f1 * x.a, f1 * x.b, f1 * x.ab + f2 * x.a * x.b};
+}
+inline HD recip(const HD& x) {
+    const double i = 1.0 / x.v;
+    return chain(x, i, -i * i, 2.0 * i * i * i);
+}
+inline HD operator/(const HD& x, const HD& y) { return x * recip(y); }
+inline HD sqrt(const HD& x) {
+    const double s = std::sqrt(x.v);
+    return chain(x, s, 0.5 / s, -0.25 / (s * x.v));
+}
+inline HD sin(const HD& x) { return chain(x, std::sin(x.v), std::cos(x.v), -std::sin(x.v)); }
+inline HD cos(const HD& x) { return chain(x, std::cos(x.v), -std::sin(x.v), -std::cos(x.v)); }
+inline HD exp(const HD& x) {
+    const double e = std::exp(x.v);
+    return chain(x, e, e, e);
+}
+inline HD log1p(const HD& x) {
+    const double i = 1.0 / (1.0 + x.v);
+    return chain(x, std::log1p(x.v), i, -i * i);
+}
+inline double value(const HD& x) { return x.v; }
+inline double value(double x) { return x; }
+
+constexpr int kAdjMaxVars = 24;
+
+// Fixed data of one observation's chart and the positions of its variables in the local vector.
+struct ObsChart {
+    double R[9], C[3];           // camera state (camera-to-world rotation, centre)
+    double src[9];               // state intrinsics fx, fy, cx, cy, k1, k2, k3, p1, p2
+    double refcx, refcy, su, sv;
+    bool flip;
+    bool tangent;                // gauge scale camera: centre on the sphere around the anchor
+    double anchorC[3], e[3], Bw[6], baseline;
+    double X[3], s;              // point and its step scale (s = 1 for a fixed track)
+    double G[kP];                // group parameters (when the camera has a group)
+    bool en[kP];
+    double u, v, w;
+    int loss;
+    double scale;
+    // local variable positions (-1: absent)
+    int iw = -1, ic = -1, it = -1, ib = -1, ia = -1, ip = -1, iu = -1;
+    int ik[kP];
+};
+
+template <class S>
+S chartCost(const ObsChart& q, const S* z) {
+    // rotation: C2W' = T C2W, T[r][c] = sg[r] E[c][r] sg[c], E = Rx(w0) Ry(w1) Rz(w2)
+    const S w0 = z[q.iw], w1 = z[q.iw + 1], w2 = z[q.iw + 2];
+    const S sx = sin(w0), cx = cos(w0), sy = sin(w1), cy = cos(w1), sz = sin(w2), cz = cos(w2);
+    const S E[9] = {cy * cz, -(cy * sz), sy,
+                    sx * sy * cz + cx * sz, cx * cz - sx * sy * sz, -(sx * cy),
+                    sx * sz - cx * sy * cz, cx * sy * sz + sx * cz, cx * cy};
+    const double sg[3] = {1.0, -1.0, -1.0};
+    S Rn[9];
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) {
+            S acc(0.0);
+            for (int k = 0; k < 3; ++k) acc = acc + (sg[r] * sg[k]) * E[k * 3 + r] * q.R[k * 3 + c];
+            Rn[r * 3 + c] = acc;
+        }
+    S Cn[3];
+    if (q.tangent) {
+        S dir[3];
+        for (int i = 0; i < 3; ++i) dir[i] = q.e[i] + q.Bw[i] * z[q.it] + q.Bw[3 + i] * z[q.it + 1];
+        const S len = sqrt(dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2]);
+        const S bl = q.baseline + z[q.ib];
+        for (int i = 0; i < 3; ++i) Cn[i] = q.anchorC[i] + z[q.ia + i] + bl * dir[i] / len;
+    } else {
+        for (int i = 0; i < 3; ++i) Cn[i] = q.C[i] + z[q.ic + i];
+    }
+    S d[3];
+    for (int i = 0; i < 3; ++i) d[i] = (q.X[i] + (q.ip >= 0 ? q.s * z[q.ip + i] : S(0.0))) - Cn[i];
+    const S xc = Rn[0] * d[0] + Rn[3] * d[1] + Rn[6] * d[2];
+    const S yc = Rn[1] * d[0] + Rn[4] * d[1] + Rn[7] * d[2];
+    const S zc = Rn[2] * d[0] + Rn[5] * d[1] + Rn[8] * d[2];
+    const double fwd = q.flip ? -value(zc) : value(zc);
+    if (!(fwd > 1e-9)) throw InvalidProjection("behind the camera");
+    const S x = xc / zc, y = yc / zc;
+    auto par = [&](int p, double base) -> S { return q.ik[p] >= 0 ? S(base) + z[q.ik[p]] : S(base); };
+    const S fx = q.en[0] ? par(0, q.G[0]) : S(q.src[0]);
+    const S aspect = q.en[1] ? exp(par(1, q.G[1])) : S(q.src[0] > 1e-12 ? q.src[1] / q.src[0] : 1.0);
+    const S fy = fx * aspect;
+    const S ccx = q.en[2] ? par(2, q.G[2]) + q.refcx : S(q.src[2]);
+    const S ccy = q.en[3] ? par(3, q.G[3]) + q.refcy : S(q.src[3]);
+    S dist[5];
+    for (int p = 4; p < 9; ++p) dist[p - 4] = q.en[p] ? par(p, q.G[p]) : S(q.src[p]);
+    const S r2 = x * x + y * y;
+    const S radial = 1.0 + dist[0] * r2 + dist[1] * r2 * r2 + dist[2] * r2 * r2 * r2;
+    const S xy2 = 2.0 * x * y;
+    const S xd = x * radial + dist[3] * xy2 + dist[4] * (r2 + 2.0 * x * x);
+    const S yd = y * radial + dist[3] * (r2 + 2.0 * y * y) + dist[4] * xy2;
+    const S px = q.su * fx * xd + ccx, py = q.sv * fy * yd + ccy;
+    const S r0 = px - (q.iu >= 0 ? q.u + z[q.iu] : S(q.u));
+    const S r1 = py - (q.iu >= 0 ? q.v + z[q.iu + 1] : S(q.v));
+    const S sq = q.w * (r0 * r0 + r1 * r1);
+    if (!std::isfinite(value(sq)) || value(sq) < 0.0) throw InvalidProjection("non-finite residual");
+    if (q.loss == 0) return 0.5 * sq;
+    const double c2 = q.scale * q.scale;
+    if (q.loss == 1) return value(sq) <= c2 ? 0.5 * sq : q.scale * sqrt(sq) - 0.5 * c2;
+    return 0.5 * c2 * log1p(sq / c2);
+}
+
+}  // namespace orc
+
+extern "C" {
+
+// Replaces the state (cameras as published records, points, group parameters) so that the
+// adjoint is evaluated where another solver stopped.
+int32_t orc_set_state(void* h, const double* cams, const double* pts, const double* groups) {
+    using namespace orc;
+    auto* o = static_cast<Oracle*>(h);
+    for (size_t c = 0; c < o->state.cams.size(); ++c) o->state.cams[c] = loadCamera(cams + c * ORC_CAMERA_STRIDE);
+    for (size_t t = 0; t < o->nt(); ++t)
+        for (int a = 0; a < 3; ++a) o->state.points[t][a] = pts[t * 3 + a];
+    if (groups)
+        for (size_t g = 0; g < o->state.groups.size(); ++g)
+            for (int p = 0; p < kP; ++p) o->state.groups[g].params[p] = groups[g * kP + p];
+    return 0;
+}
+
+// Variable numbering of the adjoint: camera c -> [6c, 6c + 6) (rotation increment, centre
+// increment; the gauge scale camera's tangent coordinates in slots 3 and 4), track t ->
+// 6 nc + 3 t, group g parameter p -> 6 nc + 3 nt + kP g + p, the gauge baseline -> 6 nc + 3 nt +
+// kP ng, observation k (u, v) -> that + 1 + 2 k.  kind[id]: 0 unused, 1 solved for (free), 2 a
+// parameter of the problem (fixed cameras and tracks, the baseline, the observations).
+// geom (17 doubles): anchor, scale, baseline, e = C_scale - C_anchor (3), world tangent basis (6),
+// anchor centre (3), 0.
+int32_t orc_adjoint_layout(void* h, int64_t* n_vars, int8_t* kind, double* geom) {
+    using namespace orc;
+    auto* o = static_cast<Oracle*>(h);
+    const int64_t nc = static_cast<int64_t>(o->state.cams.size()), nt = static_cast<int64_t>(o->nt());
+    const int64_t ng = static_cast<int64_t>(o->state.groups.size()), no = static_cast<int64_t>(o->obs.size());
+    const int64_t base_g = 6 * nc + 3 * nt, id_b = base_g + kP * ng, base_o = id_b + 1;
+    *n_vars = base_o + 2 * no;
+    if (!kind) return 0;
+    std::fill(kind, kind + *n_vars, 0);
+    const Active& a = o->active;
+    std::vector<char> camUsed(nc, 0);
+    for (size_t t = 0; t < o->nt(); ++t) {
+        if (!a.activeTrack[t]) continue;
+        bool any = false;
+        for (int64_t k = o->offs[t]; k < o->offs[t + 1]; ++k) {
+            if (!obsUsable(o->obs[k], nc)) continue;
+            any = true;
+            camUsed[o->obs[k].cam] = 1;
+            kind[base_o + 2 * k] = kind[base_o + 2 * k + 1] = 2;
+        }
+        if (any)
+            for (int ax = 0; ax < 3; ++ax) kind[6 * nc + 3 * t + ax] = a.trackBlock[t] >= 0 ? 1 : 2;
+    }
+    for (int64_t c = 0; c < nc; ++c) {
+        if (!camUsed[c]) continue;
+        const bool free = a.cameraBlock[c] >= 0;
+        const bool tangent = free && usesGaugeTangent(*o, c);
+        for (int k = 0; k < 6; ++k) kind[6 * c + k] = free ? 1 : 2;
+        if (tangent) kind[6 * c + 5] = 0;
+    }
+    for (int64_t g = 0; g < ng; ++g)
+        for (int p = 0; p < kP; ++p)
+            if (o->state.groups[g].enabled[p]) kind[base_g + kP * g + p] = 1;
+    const bool gauge = o->gaugeScale >= 0 && a.cameraBlock[o->gaugeScale] >= 0 && usesGaugeTangent(*o, o->gaugeScale);
+    if (gauge) {
+        kind[id_b] = 2;
+        for (int k = 0; k < 6; ++k) kind[6 * o->gaugeAnchor + k] = 2;
+    }
+    if (geom) {
+        std::fill(geom, geom + 17, 0.0);
+        geom[0] = o->gaugeAnchor;
+        geom[1] = gauge ? o->gaugeScale : -1;
+        geom[2] = o->gaugeBaseline;
+        if (gauge) {
+            const auto& A = o->state.cams[o->gaugeAnchor].C;
+            const auto& Sc = o->state.cams[o->gaugeScale].C;
+            const auto basis = gaugeBasis(*o, o->state);
+            for (int i = 0; i < 3; ++i) geom[3 + i] = Sc[i] - A[i];
+            for (int p = 0; p < 2; ++p) {
+                const auto wb = targetCoords(basis[p].data());
+                for (int i = 0; i < 3; ++i) geom[6 + 3 * p + i] = wb[i];
+            }
+            for (int i = 0; i < 3; ++i) geom[12 + i] = A[i];
+        }
+    }
+    return 0;
+}
+
+// Per usable observation of an active track (in observation order, `count` of them): its local
+// variables' global ids (kAdjMaxVars, -1 padded), robust cost, gradient and Hessian (row-major
+// kAdjMaxVars^2) at state (+) z0, where z0 holds chart coordinates for every variable (NULL: 0).
+// prior (3 * ng * kP): Hessian invSigma^2, gradient and cost of the group-intrinsic priors
+// 0.5 (invSigma (theta - prior))^2 at the same state.  Returns 0, or 1 when an observation does
+// not project.
+int32_t orc_adjoint_local(void* h, const double* z0, int64_t* count, int32_t* ids, double* val, double* grad,
+                          double* hess, double* prior) {
+    using namespace orc;
+    auto* o = static_cast<Oracle*>(h);
+    const int64_t nc = static_cast<int64_t>(o->state.cams.size()), nt = static_cast<int64_t>(o->nt());
+    const int64_t ng = static_cast<int64_t>(o->state.groups.size());
+    const int64_t base_g = 6 * nc + 3 * nt, id_b = base_g + kP * ng, base_o = id_b + 1;
+    const Active& a = o->active;
+    std::vector<int64_t> list;
+    for (size_t t = 0; t < o->nt(); ++t) {
+        if (!a.activeTrack[t]) continue;
+        for (int64_t k = o->offs[t]; k < o->offs[t + 1]; ++k)
+            if (obsUsable(o->obs[k], nc)) list.push_back(k);
+    }
+    *count = static_cast<int64_t>(list.size());
+    if (prior)
+        for (int64_t g = 0; g < ng; ++g)
+            for (int p = 0; p < kP; ++p) {
+                const Group& G = o->state.groups[g];
+                const double w2 = G.enabled[p] ? G.invSigma[p] * G.invSigma[p] : 0.0;
+                const double d = G.params[p] + (z0 ? z0[base_g + kP * g + p] : 0.0) - G.prior[p];
+                prior[g * kP + p] = w2;                        // Hessian
+                prior[(ng + g) * kP + p] = w2 * d;             // gradient
+                prior[(2 * ng + g) * kP + p] = 0.5 * w2 * d * d;  // cost
+            }
+    if (!ids) return 0;
+    std::vector<int64_t> trackOf(o->obs.size(), -1);
+    for (size_t t = 0; t < o->nt(); ++t)
+        for (int64_t k = o->offs[t]; k < o->offs[t + 1]; ++k) trackOf[k] = static_cast<int64_t>(t);
+    const bool gauge = o->gaugeScale >= 0 && a.cameraBlock[o->gaugeScale] >= 0 && usesGaugeTangent(*o, o->gaugeScale);
+    std::array<std::array<double, 3>, 2> basis{};
+    if (gauge) basis = gaugeBasis(*o, o->state);
+    const auto& refs = o->refCams.empty() ? o->inputCams : o->refCams;
+    int bad = 0;
+#pragma omp parallel for schedule(dynamic, 64) num_threads(o->threads)
+    for (int64_t li = 0; li < static_cast<int64_t>(list.size()); ++li) {
+        const int64_t k = list[li];
+        const Obs& ob = o->obs[k];
+        const int64_t t = trackOf[k];
+        const int c = ob.cam;
+        const Camera& cam = o->state.cams[c];
+        ObsChart q{};
+        std::memcpy(q.R, cam.R, sizeof q.R);
+        std::memcpy(q.C, cam.C, sizeof q.C);
+        const double src[9] = {cam.fx, cam.fy, cam.cx, cam.cy, cam.k1, cam.k2, cam.k3, cam.p1, cam.p2};
+        std::memcpy(q.src, src, sizeof src);
+        q.refcx = refs[c].cx;
+        q.refcy = refs[c].cy;
+        q.su = cam.su;
+        q.sv = cam.sv;
+        q.flip = cam.flip;
+        q.tangent = gauge && c == o->gaugeScale;
+        int64_t gid[kAdjMaxVars];
+        int m = 0;
+        q.iw = m;
+        for (int i = 0; i < 3; ++i) gid[m++] = 6 * c + i;
+        if (q.tangent) {
+            const auto& A = o->state.cams[o->gaugeAnchor].C;
+            for (int i = 0; i < 3; ++i) {
+                q.anchorC[i] = A[i];
+                q.e[i] = cam.C[i] - A[i];
+            }
+            for (int p = 0; p < 2; ++p) {
+                const auto wb = targetCoords(basis[p].data());
+                for (int i = 0; i < 3; ++i) q.Bw[3 * p + i] = wb[i];
+            }
+            q.baseline = o->gaugeBaseline;
+            q.it = m;
+            gid[m++] = 6 * c + 3;
+            gid[m++] = 6 * c + 4;
+            q.ib = m;
+            gid[m++] = id_b;
+            q.ia = m;
+            for (int i = 0; i < 3; ++i) gid[m++] = 6 * o->gaugeAnchor + 3 + i;
+        } else {
+            q.ic = m;
+            for (int i = 0; i < 3; ++i) gid[m++] = 6 * c + 3 + i;
+        }
+        for (int i = 0; i < 3; ++i) q.X[i] = o->state.points[t][i];
+        q.s = a.trackBlock[t] >= 0 ? referencePointScale(q.X) : 1.0;
+        q.ip = m;
+        for (int i = 0; i < 3; ++i) gid[m++] = 6 * nc + 3 * t + i;
+        for (int p = 0; p < kP; ++p) q.ik[p] = -1;
+        const int g = o->state.groups.empty() ? -1 : a.calibGroupByCamera[c];
+        if (g >= 0) {
+            const Group& G = o->state.groups[g];
+            for (int p = 0; p < kP; ++p) {
+                q.G[p] = G.params[p];
+                q.en[p] = G.enabled[p];
+                if (G.enabled[p]) {
+                    q.ik[p] = m;
+                    gid[m++] = base_g + kP * g + p;
+                }
+            }
+        }
+        q.iu = m;
+        gid[m++] = base_o + 2 * k;
+        gid[m++] = base_o + 2 * k + 1;
+        const double ms = sanitizedScale(ob);
+        q.u = ob.u;
+        q.v = ob.v;
+        q.w = sanitizedWeight(ob) / (ms * ms);
+        q.loss = o->opt.robust_loss;
+        q.scale = o->opt.robust_loss_scale;
+        int32_t* oid = ids + li * kAdjMaxVars;
+        double* og = grad + li * kAdjMaxVars;
+        double* oh = hess + li * kAdjMaxVars * kAdjMaxVars;
+        for (int i = 0; i < kAdjMaxVars; ++i) {
+            oid[i] = i < m ? static_cast<int32_t>(gid[i]) : -1;
+            og[i] = 0.0;
+        }
+        std::fill(oh, oh + kAdjMaxVars * kAdjMaxVars, 0.0);
+        try {
+            HD z[kAdjMaxVars];
+            for (int i = 0; i < m; ++i) z[i] = HD(z0 ? z0[gid[i]] : 0.0);
+            for (int i = 0; i < m; ++i)
+                for (int j = i; j < m; ++j) {
+                    z[i].a = 1.0;
+                    z[j].b = 1.0;
+                    const HD f = chartCost(q, z);
+                    z[i].a = 0.0;
+                    z[j].b = 0.0;
+                    oh[i * kAdjMaxVars + j] = oh[j * kAdjMaxVars + i] = f.ab;
+                    if (j == i) og[i] = f.a;
+                    if (i == 0 && j == 0) val[li] = f.v;
+                }
+        } catch (const InvalidProjection&) {
+#pragma omp atomic write
+            bad = 1;
+        }
+    }
+    return bad;
+}
+
+}  // extern "C"

@@ -495,6 +495,12 @@ __global__ void k_accept(Shape S, DevPtrs D, const double* __restrict__ step_p, 
         double* ef = D.cams_eff + static_cast<size_t>(i) * kCamStride;
         for (int q = 0; q < 12; ++q) st[q] = tr[q];
         for (int q = 0; q < kCamStride; ++q) ef[q] = tr[q];
+        // the gauge tangent basis follows the accepted state (referenceGaugeTargetTangentBasis is
+        // evaluated on the current cameras, BundleAdjustPlaMatrixAssembly.cpp:69-99, :110, :205);
+        // read from the trial records, which this kernel does not write
+        if (i == S.gauge_scale && S.gauge_anchor >= 0 && S.gauge_baseline > 0.0)
+            gauge_basis(D.cams_trial + (static_cast<size_t>(a) * S.nc + S.gauge_anchor) * kCamStride + 9, tr + 9,
+                        D.gauge_basis + 6, D.gauge_basis);
     }
     if (i < S.ng * kGroupRec) D.groups[i] = D.groups_trial[static_cast<size_t>(a) * S.ng * kGroupRec + i];
     if (i < S.ntp && D.trk_block[i] >= 0) {
