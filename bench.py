@@ -34,12 +34,14 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="aerial", choices=["aerial", "ring", "windows"])
+    ap.add_argument("--workload", default="aerial", choices=["aerial", "ring", "windows", "adjoint"])
     ap.add_argument("--windows", type=int, default=256, help="local-BA windows of the windows workload")
     ap.add_argument("--workers", type=int, default=8, help="worker contexts of the windows workload")
     ap.add_argument("--cpu-iterations", type=int, default=2,
                     help="LM iterations of the bounded CPU sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--fd-obs", type=int, default=64,
+                    help="observations of the finite-difference check of the adjoint workload")
     return ap.parse_args()
 
 
@@ -240,6 +242,102 @@ def run_windows(args, rank, world, local_rank):
     print(json.dumps(line), flush=True)
 
 
+def run_adjoint(args, rank, world, local_rank):
+    """Backward pass of the converged 500-camera aerial solve (mixed precision): implicit
+    differentiation with the exact Hessian of L = sum_i |C_i - (C_i_true + N(0, 0.1 m))|^2 with
+    respect to every observation and initial pose.  value: device time of one pb_gpu_backward
+    (Hessian records, reduced system, solve, gradients; CUDA events on the context's stream);
+    e2e: the same call through the Python API with its host buffers (the loss gradient in,
+    dL/d(u, v) and dL/d(initial pose) out).  Then the central finite-difference check (h = 1e-3
+    px) on --fd-obs random observations: every perturbed solve restarts from the saved fixed
+    point and is re-converged with full Gauss-Newton steps."""
+    import numpy as np
+    import torch
+    from plabundle_gb300.adjoint import camera_centre_loss, polish
+    from plabundle_gb300.device import Gb300Context
+    from plabundle_gb300.problem import Precision
+
+    torch.cuda.set_device(local_rank)
+    prob, opts, cfg = workload("aerial")
+    opts.backend.enablePlaMatrixMixedPrecision = True
+    ctx = Gb300Context(local_rank)
+    assert ctx.upload(prob, opts) == 0
+    rep = ctx.solve()
+    polish(ctx, iterations=4, precision=Precision.Mixed)
+    d = ctx.download()
+    rng = np.random.default_rng(2024)
+    targets = prob.truth_cameras[:, 9:12] + rng.normal(0.0, 0.1, (prob.n_cameras, 3))
+    L, g = camera_centre_loss(d["cameras"], targets)
+    stream = torch.cuda.ExternalStream(ctx.stream_handle())
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    for _ in range(args.warmup):
+        out = ctx.backward(grad_cameras=g)
+    sampler = ClockSampler(local_rank)
+    sampler.start()
+    dev_ms, e2e_ms, reports = [], [], []
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        e0.record(stream)
+        out = ctx.backward(grad_cameras=g)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        e2e_ms.append(1e3 * (time.perf_counter() - t0))
+        dev_ms.append(e0.elapsed_time(e1))
+        reports.append(out["report"])
+    clocks = sampler.stop()
+    go = out["observations"]
+    # finite differences
+    ctx.save_state()
+    pick = rng.choice(np.nonzero(np.abs(go).sum(1) > 0)[0], args.fd_obs, replace=False)
+    h = 1e-3
+    fd = np.zeros((pick.size, 2))
+    t_fd = time.perf_counter()
+    for i, k in enumerate(pick):
+        for a in range(2):
+            vals = []
+            for sgn in (1.0, -1.0):
+                u, v = prob.obs_u[k], prob.obs_v[k]
+                ctx.set_observations([k], [u + sgn * h * (a == 0)], [v + sgn * h * (a == 1)])
+                ctx.restore_state()
+                polish(ctx, iterations=8, precision=Precision.Mixed)
+                vals.append(camera_centre_loss(ctx.download()["cameras"], targets)[0])
+                ctx.set_observations([k], [u], [v])
+            fd[i, a] = (vals[0] - vals[1]) / (2.0 * h)
+    t_fd = time.perf_counter() - t_fd
+    ctx.restore_state()
+    err = np.linalg.norm(go[pick] - fd) / np.linalg.norm(fd)
+    per_obs = np.linalg.norm(go[pick] - fd, axis=1) / np.maximum(np.linalg.norm(fd, axis=1), 1e-300)
+    last = reports[-1]
+    if rank != 0:
+        return
+    nobs = prob.n_obs
+    line = {"metric": "adjoint backward time (exact-Hessian implicit differentiation)",
+            "value": statistics.mean(dev_ms), "unit": "ms", "impl": "gb300", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.mean(dev_ms),
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64 Hessian records, f32 factor + f64 CG", "data": "synthetic (seeded)",
+            "config": dict(cfg, loss_of_solution="sum |C_i - (C_true + N(0, 0.1 m))|^2",
+                           l2="flushed between steps (256 MB write)", parallelism="replicas"),
+            "phases_ms": {k: last[k] for k in ("hessian_ms", "solve_ms", "gradient_ms", "total_ms")},
+            "adjoint_linear_iterations": last["linear_iterations"],
+            "adjoint_relative_residual": last["relative_residual"],
+            "forward_solve": {"status": rep["status"], "iterations": rep["iterations"]},
+            "loss": L,
+            "fd_check": {"observations": int(pick.size), "h_px": h, "relative_error": float(err),
+                         "per_observation_relative_error_median": float(np.median(per_obs)),
+                         "per_observation_relative_error_max": float(per_obs.max()),
+                         "seconds": t_fd},
+            "e2e": {"value": statistics.mean(e2e_ms), "unit": "ms", "h2d_bytes_per_step": int(g.nbytes),
+                    "d2h_bytes_per_step": int(16 * nobs + 48 * prob.n_cameras + 24 * prob.n_tracks)},
+            "gpu_launches": int(last["gpu_kernel_launches"]),
+            "clocks": clocks}
+    print(json.dumps(line), flush=True)
+
+
 def run_gb300(args, rank, world, local_rank):
     import ctypes as C
     import numpy as np
@@ -397,6 +495,9 @@ def main():
     if world > 1:
         import torch
         torch.distributed.init_process_group("nccl")
+    if args.workload == "adjoint":
+        run_adjoint(args, rank, world, local_rank)
+        return
     if args.workload == "windows":
         run_windows(args, rank, world, local_rank)
     else:

@@ -277,6 +277,54 @@ pb_status pb_gpu_solve_batch(int32_t device, int32_t n_problems, const pb_proble
  *     load the module): make it before any stream capture;
  *   - work is enqueued on `stream` (a cudaStream_t, NULL for the legacy default stream) and the
  *     call returns after that stream has finished it. */
+/* Device-side snapshot of the current state (poses, points, group intrinsics) and its restore
+ * (no counterpart in the reference).  Together with pb_gpu_set_observations they re-solve a
+ * problem after a measurement update from a known state without a new upload, e.g. the
+ * warm-started re-solves of a finite-difference check of pb_gpu_backward.  A new upload drops
+ * the snapshot. */
+pb_status pb_gpu_save_state(pb_gpu_ctx* ctx);
+pb_status pb_gpu_restore_state(pb_gpu_ctx* ctx);
+/* Replaces the measurements (u, v) of n observations, given by their original index, in the
+ * uploaded problem (no counterpart in the reference).  The gauge, the active-track gate and the
+ * intrinsic groups decided at upload are kept. */
+pb_status pb_gpu_set_observations(pb_gpu_ctx* ctx, int64_t n, const int64_t* index, const double* u, const double* v);
+
+/* Backward pass: implicit differentiation of the converged solve (no counterpart in the
+ * reference, which has no adjoint).  At the fixed point of the current state, for a scalar loss
+ * L of the refined state with partial derivatives
+ *   grad_cameras     n_cameras * 6: dL/d(final pose) as (rotation increment of the solver's pose
+ *                    retraction C2W' = D E(w)^T D C2W, E = Rx Ry Rz, D = diag(1,-1,-1); world
+ *                    centre), or NULL;
+ *   grad_points      n_tracks * 3: dL/d(final point), world, or NULL;
+ *   grad_intrinsics  n_groups * 13: dL/d(group parameter), or NULL;
+ * it solves H mu = dL/dz with H the exact Hessian of the robust objective (robust-loss second
+ * derivatives and residual curvature included) reduced over the points and solved by the same
+ * dense-Cholesky-preconditioned CG / block-Jacobi PCG as the forward solve, and returns
+ *   grad_observations     n_obs * 2: dL/d(u, v) (original order; 0 for unused observations);
+ *   grad_initial_cameras  n_cameras * 6: dL/d(initial pose) as (rotation increment, centre).
+ *                         Non-zero only through the gauge: fixed cameras (their final pose is
+ *                         the initial one) and the AutoAnchor baseline, which is taken from the
+ *                         initial centres of the anchor and scale cameras;
+ *   grad_initial_points   n_tracks * 3: dL/d(initial point), non-zero for fixed tracks only.
+ * Any output may be NULL.  The state must be a converged fixed point of the uploaded problem
+ * (after pb_gpu_solve); clamped intrinsics are treated as free.  The reduced-system buffers are
+ * reused, so a pb_gpu_linearize_schur is needed before the next pb_gpu_solve_reduced.  The
+ * reduced sums use FP64 atomics: results vary in the last bits from run to run. */
+typedef struct pb_adjoint_report {
+    int32_t status;                /* pb_status of the call */
+    int32_t linear_iterations;     /* CG / PCG iterations of the adjoint solve */
+    int32_t gpu_kernel_launches;
+    int32_t point_blocks_singular; /* 1 when a point block of the exact Hessian was singular */
+    double relative_residual;      /* |H mu - dL/dz| / |dL/dz| of the reduced solve */
+    double hessian_ms;             /* exact-Hessian records and the reduced system */
+    double solve_ms;
+    double gradient_ms;            /* back-substitution and the gradients */
+    double total_ms;
+} pb_adjoint_report;
+pb_status pb_gpu_backward(pb_gpu_ctx* ctx, const double* grad_cameras, const double* grad_points,
+                          const double* grad_intrinsics, double* grad_observations, double* grad_initial_cameras,
+                          double* grad_initial_points, pb_adjoint_report* report);
+
 #define PB_NOALLOC_MAX_OBS 4194304
 pb_status pb_gpu_objective_noalloc(const double* cameras, int32_t n_cameras, const double* points, int32_t n_points,
                                    const int32_t* obs_camera, const int32_t* obs_point, const double* obs_u,

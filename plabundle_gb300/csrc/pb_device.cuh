@@ -83,6 +83,25 @@ __device__ __forceinline__ bool robust_loss(double s, int loss, double scale, do
     return true;
 }
 
+// First and second derivatives d1 = rho'(s), d2 = rho''(s) of the robust cost of robust_loss
+// (the normal weight is 2 rho'(s)).  Used by the exact Hessian of the backward pass.
+__device__ __forceinline__ void robust_derivatives(double s, int loss, double scale, double& d1, double& d2) {
+    d1 = 0.5;
+    d2 = 0.0;
+    if (loss == 0) return;
+    const double c2 = scale * scale;
+    if (loss == 1) {
+        if (s <= c2) return;
+        const double n = sqrt(s);
+        d1 = 0.5 * scale / n;
+        d2 = -0.25 * scale / (n * s);
+        return;
+    }
+    const double q = 1.0 / (1.0 + s / c2);
+    d1 = 0.5 * q;
+    d2 = -0.5 * q * q / c2;
+}
+
 __device__ __forceinline__ double point_scale(double X0, double X1, double X2) {
     const double len = sqrt(X0 * X0 + X1 * X1 + X2 * X2) / 1000.0;
     if (!isfinite(len) || len == 0.0) return 1.0;

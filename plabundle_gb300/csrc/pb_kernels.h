@@ -137,6 +137,50 @@ int dense_pcg(const PcgSystem<double>& sys, DenseWork<T>& W, const double* b, do
               int max_it, int* iterations, double* relres, bool* converged, double* h_scal, cudaStream_t st,
               int* launches);
 
+// Backward pass (pb_adjoint.cu).  Per-observation record of the exact Hessian in the local chart
+// (pose 6 | point 3 | intrinsic columns ni): pose-pose (upper 6x6), pose-point (6x3), point-point
+// (upper 3x3), pose-intrinsic (6 x ni), point-intrinsic (3 x ni), intrinsic (upper ni x ni), the
+// FP64 Jacobian rows (2 x (9 + ni)), W2 = 2 rho' w I + 4 rho'' w^2 r r^T (3) and lam = 2 rho' w r (2).
+struct AdjLayout {
+    int ni = 0, stride = 0;
+    __host__ __device__ int hcc() const { return 0; }
+    __host__ __device__ int hcp() const { return 21; }
+    __host__ __device__ int hpp() const { return 39; }
+    __host__ __device__ int hck() const { return 45; }
+    __host__ __device__ int hpk() const { return 45 + 6 * ni; }
+    __host__ __device__ int hkk() const { return 45 + 9 * ni; }
+    __host__ __device__ int jac() const { return 45 + 9 * ni + ni * (ni + 1) / 2; }
+    __host__ __device__ int w2() const { return jac() + 2 * (9 + ni); }
+    static AdjLayout make(int n_int) {
+        AdjLayout L;
+        L.ni = n_int;
+        L.stride = L.w2() + 5;
+        return L;
+    }
+};
+constexpr int kAdjMaxStride = 68 + 11 * kMaxNI + kMaxNI * (kMaxNI + 1) / 2;
+
+struct AdjBuffers {
+    AdjLayout lay;
+    double* rec;            // nop * stride
+    double* vinv;           // ntp * 9 inverse point blocks
+    double* gpt;            // ntp * 3 dL/d(final point), world (processing order)
+    double* gcam;           // nc * 6 dL/d(final pose): rotation increment, world centre
+    double* gint;           // ng * kP dL/d(group parameters)
+    double* mu_p;           // ntp * 3 point part of the adjoint solution (point chart)
+    double* grad_obs;       // nop * 2 dL/d(u, v) (processing order)
+    double* grad_fixed_cam; // nc * 6 cross terms of fixed cameras (zeroed by the caller)
+    double* grad_fixed_pt;  // ntp * 3 cross terms of fixed tracks (world)
+    double* gauge;          // 4: cross terms of the anchor centre (3) and the gauge baseline (zeroed)
+    int* flags;             // bit 0: singular point block, bit 1: invalid projection, bit 2: pattern miss
+};
+
+void launch_adjoint_hessian(const Shape& S, const DevPtrs& D, const AdjBuffers& B, cudaStream_t st);
+void launch_adjoint_rhs(const Shape& S, const DevPtrs& D, const AdjBuffers& B, const RedOut<double>& R, cudaStream_t st);
+void launch_adjoint_schur(const Shape& S, const DevPtrs& D, const AdjBuffers& B, const RedOut<double>& R,
+                          cudaStream_t st);
+void launch_adjoint_gradient(const Shape& S, const DevPtrs& D, const AdjBuffers& B, const double* mu, cudaStream_t st);
+
 void to_double(const float* in, double* out, int n, cudaStream_t st);
 void to_double(const double* in, double* out, int n, cudaStream_t st);
 void to_float(const double* in, float* out, int n, cudaStream_t st);

@@ -156,6 +156,16 @@ struct pb_gpu_ctx {
     double kt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     int launches = 0;
     int solved = 0;
+    // backward pass (exact-Hessian records and outputs) and the state snapshot
+    DeviceArena aarena;
+    AdjBuffers adj{};
+    bool adj_ready = false;
+    DeviceArena sarena;
+    double* snap_cams = nullptr;
+    double* snap_points = nullptr;
+    double* snap_groups = nullptr;
+    bool snap_valid = false;
+    std::vector<long long> proc_of_obs;  // original observation -> processing index (-1: not processed)
 };
 
 namespace {
@@ -965,6 +975,8 @@ pb_status pb_gpu_destroy(pb_gpu_ctx* c) {
     c->parena[0].free_all();
     c->parena[1].free_all();
     c->darena.free_all();
+    c->aarena.free_all();
+    c->sarena.free_all();
     if (c->h_scratch) cudaFreeHost(c->h_scratch);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
@@ -1033,6 +1045,11 @@ pb_status pb_gpu_upload(pb_gpu_ctx* c, const pb_problem_desc* pr, const pb_solve
         c->structure_hash = c->model.structure_hash;
         c->uploaded = true;
         c->have_system = false;
+        c->aarena.release();
+        c->adj_ready = false;
+        c->sarena.release();
+        c->snap_valid = false;
+        c->proc_of_obs.clear();
         reset_state(c);
         check(cudaStreamSynchronize(c->stream), "upload");
         return PB_OK;
@@ -1364,6 +1381,275 @@ pb_status pb_gpu_set_timing(pb_gpu_ctx* c, int32_t enable) {
     if (!c) return PB_ERR_INVALID_ARGUMENT;
     c->timing = enable != 0;
     return PB_OK;
+}
+
+
+// ------------------------------------------------------------------ state snapshot, observations
+pb_status pb_gpu_save_state(pb_gpu_ctx* c) {
+    if (!c || !c->uploaded) return fail(c, PB_ERR_STATE, "no problem uploaded");
+    try {
+        const HostModel& m = c->model;
+        const DevPtrs& D = c->D[0];
+        const size_t nc = m.cams_in.size(), np = m.trk_order.size() * 3,
+                     ng = static_cast<size_t>(std::max(1, m.ng)) * kGroupRec;
+        if (!c->snap_cams) {
+            c->snap_cams = c->sarena.alloc<double>(nc);
+            c->snap_points = c->sarena.alloc<double>(np);
+            c->snap_groups = c->sarena.alloc<double>(ng);
+        }
+        cudaStream_t st = c->stream;
+        check(cudaMemcpyAsync(c->snap_cams, D.cams_state, nc * sizeof(double), cudaMemcpyDeviceToDevice, st), "D2D");
+        check(cudaMemcpyAsync(c->snap_points, D.points, np * sizeof(double), cudaMemcpyDeviceToDevice, st), "D2D");
+        check(cudaMemcpyAsync(c->snap_groups, D.groups, ng * sizeof(double), cudaMemcpyDeviceToDevice, st), "D2D");
+        check(cudaStreamSynchronize(st), "save_state");
+        c->snap_valid = true;
+        return PB_OK;
+    } catch (const std::exception& e) {
+        return fail(c, PB_ERR_CUDA, e.what());
+    }
+}
+
+pb_status pb_gpu_restore_state(pb_gpu_ctx* c) {
+    if (!c || !c->uploaded || !c->snap_valid) return fail(c, PB_ERR_STATE, "no saved state for this problem");
+    try {
+        const HostModel& m = c->model;
+        const DevPtrs& D = c->D[0];
+        const size_t nc = m.cams_in.size(), np = m.trk_order.size() * 3,
+                     ng = static_cast<size_t>(std::max(1, m.ng)) * kGroupRec;
+        cudaStream_t st = c->stream;
+        check(cudaMemcpyAsync(D.cams_state, c->snap_cams, nc * sizeof(double), cudaMemcpyDeviceToDevice, st), "D2D");
+        check(cudaMemcpyAsync(D.points, c->snap_points, np * sizeof(double), cudaMemcpyDeviceToDevice, st), "D2D");
+        check(cudaMemcpyAsync(D.groups, c->snap_groups, ng * sizeof(double), cudaMemcpyDeviceToDevice, st), "D2D");
+        launch_effective(c->S[0], D, st);
+        ++c->launches;
+        c->have_system = false;
+        check(cudaStreamSynchronize(st), "restore_state");
+        return PB_OK;
+    } catch (const std::exception& e) {
+        return fail(c, PB_ERR_CUDA, e.what());
+    }
+}
+
+pb_status pb_gpu_set_observations(pb_gpu_ctx* c, int64_t n, const int64_t* index, const double* u, const double* v) {
+    if (!c || !c->uploaded) return fail(c, PB_ERR_STATE, "no problem uploaded");
+    if (n < 0 || (n > 0 && (!index || !u || !v))) return fail(c, PB_ERR_INVALID_ARGUMENT, "invalid observation update");
+    try {
+        HostModel& m = c->model;
+        if (c->proc_of_obs.empty()) {
+            c->proc_of_obs.assign(static_cast<size_t>(m.no), -1);
+            for (size_t p = 0; p < m.p_obs_orig.size(); ++p) c->proc_of_obs[m.p_obs_orig[p]] = static_cast<long long>(p);
+        }
+        const DevPtrs& D = c->D[0];
+        cudaStream_t st = c->stream;
+        for (int64_t i = 0; i < n; ++i) {
+            const int64_t k = index[i];
+            if (k < 0 || k >= m.no || !std::isfinite(u[i]) || !std::isfinite(v[i]))
+                return fail(c, PB_ERR_INVALID_ARGUMENT, "observation index out of range or non-finite measurement");
+        }
+        for (int64_t i = 0; i < n; ++i) {
+            const int64_t k = index[i];
+            m.obs_u[k] = u[i];
+            m.obs_v[k] = v[i];
+            check(cudaMemcpyAsync(D.raw_u + k, &m.obs_u[k], sizeof(double), cudaMemcpyHostToDevice, st), "H2D");
+            check(cudaMemcpyAsync(D.raw_v + k, &m.obs_v[k], sizeof(double), cudaMemcpyHostToDevice, st), "H2D");
+            const long long p = c->proc_of_obs[k];
+            if (p >= 0) {
+                check(cudaMemcpyAsync(D.obs_u + p, &m.obs_u[k], sizeof(double), cudaMemcpyHostToDevice, st), "H2D");
+                check(cudaMemcpyAsync(D.obs_v + p, &m.obs_v[k], sizeof(double), cudaMemcpyHostToDevice, st), "H2D");
+            }
+        }
+        check(cudaStreamSynchronize(st), "set_observations");
+        c->have_system = false;
+        return PB_OK;
+    } catch (const std::exception& e) {
+        return fail(c, PB_ERR_CUDA, e.what());
+    }
+}
+
+// ------------------------------------------------------------------ backward pass
+pb_status pb_gpu_backward(pb_gpu_ctx* c, const double* grad_cameras, const double* grad_points,
+                          const double* grad_intrinsics, double* grad_observations, double* grad_initial_cameras,
+                          double* grad_initial_points, pb_adjoint_report* rep) {
+    if (!c || !c->uploaded) return fail(c, PB_ERR_STATE, "no problem uploaded");
+    if (rep) std::memset(rep, 0, sizeof(*rep));
+    try {
+        const HostModel& m = c->model;
+        const Shape& S = c->S[0];
+        const DevPtrs& D = c->D[0];
+        cudaStream_t st = c->stream;
+        const int nc = m.nc, ntp = S.ntp;
+        const long long nop = S.nop;
+        AdjBuffers& B = c->adj;
+        if (!c->adj_ready) {
+            DeviceArena& A = c->aarena;
+            B.lay = AdjLayout::make(S.ni);
+            B.rec = A.alloc<double>(static_cast<size_t>(std::max<long long>(1, nop)) * B.lay.stride);
+            B.vinv = A.alloc<double>(static_cast<size_t>(std::max(1, ntp)) * 9);
+            B.gpt = A.alloc<double>(static_cast<size_t>(std::max(1, ntp)) * 3);
+            B.gcam = A.alloc<double>(static_cast<size_t>(nc) * 6);
+            B.gint = A.alloc<double>(static_cast<size_t>(std::max(1, m.ng)) * kP);
+            B.mu_p = A.alloc<double>(static_cast<size_t>(std::max(1, ntp)) * 3);
+            B.grad_obs = A.alloc<double>(static_cast<size_t>(std::max<long long>(1, nop)) * 2);
+            B.grad_fixed_cam = A.alloc<double>(static_cast<size_t>(nc) * 6);
+            B.grad_fixed_pt = A.alloc<double>(static_cast<size_t>(std::max(1, ntp)) * 3);
+            B.gauge = A.alloc<double>(4);
+            B.flags = A.alloc<int>(1);
+            c->adj_ready = true;
+        }
+        // inputs: dL/d(final state) (processing order for points)
+        std::vector<double> gcam(static_cast<size_t>(nc) * 6, 0.0), gpt(static_cast<size_t>(std::max(1, ntp)) * 3, 0.0),
+            gint(static_cast<size_t>(std::max(1, m.ng)) * kP, 0.0);
+        if (grad_cameras) std::copy(grad_cameras, grad_cameras + gcam.size(), gcam.begin());
+        if (grad_points)
+            for (int p = 0; p < ntp; ++p)
+                for (int a = 0; a < 3; ++a) gpt[static_cast<size_t>(p) * 3 + a] = grad_points[static_cast<size_t>(m.trk_order[p]) * 3 + a];
+        if (grad_intrinsics && m.ng > 0) std::copy(grad_intrinsics, grad_intrinsics + static_cast<size_t>(m.ng) * kP, gint.begin());
+        for (double v : gcam)
+            if (!std::isfinite(v)) return fail(c, PB_ERR_INVALID_ARGUMENT, "non-finite camera gradient");
+        for (double v : gpt)
+            if (!std::isfinite(v)) return fail(c, PB_ERR_INVALID_ARGUMENT, "non-finite point gradient");
+        for (double v : gint)
+            if (!std::isfinite(v)) return fail(c, PB_ERR_INVALID_ARGUMENT, "non-finite intrinsic gradient");
+        check(cudaMemcpyAsync(B.gcam, gcam.data(), gcam.size() * sizeof(double), cudaMemcpyHostToDevice, st), "H2D");
+        check(cudaMemcpyAsync(B.gpt, gpt.data(), gpt.size() * sizeof(double), cudaMemcpyHostToDevice, st), "H2D");
+        check(cudaMemcpyAsync(B.gint, gint.data(), gint.size() * sizeof(double), cudaMemcpyHostToDevice, st), "H2D");
+        cudaEvent_t ev[4];
+        for (auto& e : ev) check(cudaEventCreate(&e), "event");
+        struct EvGuard {
+            cudaEvent_t* e;
+            ~EvGuard() { for (int i = 0; i < 4; ++i) cudaEventDestroy(e[i]); }
+        } guard{ev};
+        const int launches0 = c->launches;
+        check(cudaEventRecord(ev[0], st), "event");
+        // exact Hessian at the current state, reduced over the points
+        const int n = S.n;
+        RedOut<double>& R = c->red;
+        check(cudaMemsetAsync(R.vals, 0, static_cast<size_t>(std::max(1, S.nnzb)) * 36 * sizeof(double), st), "memset");
+        check(cudaMemsetAsync(R.border, 0, static_cast<size_t>(std::max(1, S.ncb)) * 6 * std::max(1, S.nb) * sizeof(double), st),
+              "memset");
+        check(cudaMemsetAsync(R.Cm, 0, static_cast<size_t>(std::max(1, S.nb * S.nb)) * sizeof(double), st), "memset");
+        check(cudaMemsetAsync(R.rhs, 0, static_cast<size_t>(std::max(1, n)) * sizeof(double), st), "memset");
+        check(cudaMemsetAsync(B.grad_fixed_cam, 0, static_cast<size_t>(nc) * 6 * sizeof(double), st), "memset");
+        check(cudaMemsetAsync(B.grad_fixed_pt, 0, static_cast<size_t>(std::max(1, ntp)) * 3 * sizeof(double), st), "memset");
+        check(cudaMemsetAsync(B.gauge, 0, 4 * sizeof(double), st), "memset");
+        check(cudaMemsetAsync(B.flags, 0, sizeof(int), st), "memset");
+        launch_effective(S, D, st);
+        launch_adjoint_hessian(S, D, B, st);
+        launch_adjoint_rhs(S, D, B, R, st);
+        launch_adjoint_schur(S, D, B, R, st);
+        c->launches += 5;
+        check(cudaGetLastError(), "adjoint launch");
+        check(cudaEventRecord(ev[1], st), "event");
+        int flags = 0;
+        check(cudaMemcpyAsync(&flags, B.flags, sizeof(int), cudaMemcpyDeviceToHost, st), "D2H");
+        check(cudaStreamSynchronize(st), "adjoint hessian");
+        c->have_system = false;  // the reduced buffers now hold the exact Hessian, not an LM system
+        if (rep) rep->point_blocks_singular = flags & 1;
+        if (flags & 2) return fail(c, PB_ERR_INVALID_PROJECTION, "an observation does not project at this state");
+        if (flags & 4) return fail(c, PB_ERR_STATE, "reduced pattern does not cover an observation pair");
+        if (flags & 1) return fail(c, PB_ERR_SINGULAR_BLOCK, "a point block of the exact Hessian is singular");
+        // solve H mu = dL/dz on the reduced system with the forward path's solvers
+        bool conv = false;
+        int it = 0;
+        double rr = 0.0;
+        const double rel = 1e-13, abs_tol = 1e-300;
+        const int max_it = std::max(400, 30 * m.P);
+        int rc;
+        c->f32_age = -1;
+        if (n > 16384) {
+            rc = solve_block_jacobi(c, rel, abs_tol, max_it, &conv, &it, &rr);
+        } else if (c->last_precision == PB_PRECISION_MIXED) {
+            rc = solve_dense<float>(c, rel, abs_tol, max_it, &conv, &it, &rr);
+        } else {
+            rc = solve_dense<double>(c, rel, abs_tol, max_it, &conv, &it, &rr);
+        }
+        c->f32_age = -1;  // the FP32 factor held now is the exact Hessian's, not an LM matrix's
+        if (rep) {
+            rep->linear_iterations = it;
+            rep->relative_residual = rr;
+        }
+        if (rc) return fail(c, PB_ERR_SINGULAR_BLOCK, "the exact Hessian is not positive definite (not a minimum?)");
+        check(cudaEventRecord(ev[2], st), "event");
+        launch_adjoint_gradient(S, D, B, c->step_c, st);
+        ++c->launches;
+        check(cudaGetLastError(), "adjoint gradient launch");
+        check(cudaEventRecord(ev[3], st), "event");
+        std::vector<double> gobs(static_cast<size_t>(std::max<long long>(1, nop)) * 2), gfc(static_cast<size_t>(nc) * 6),
+            gfp(static_cast<size_t>(std::max(1, ntp)) * 3), gauge(4), cams(m.cams_in.size());
+        check(cudaMemcpyAsync(gobs.data(), B.grad_obs, gobs.size() * sizeof(double), cudaMemcpyDeviceToHost, st), "D2H");
+        check(cudaMemcpyAsync(gfc.data(), B.grad_fixed_cam, gfc.size() * sizeof(double), cudaMemcpyDeviceToHost, st), "D2H");
+        check(cudaMemcpyAsync(gfp.data(), B.grad_fixed_pt, gfp.size() * sizeof(double), cudaMemcpyDeviceToHost, st), "D2H");
+        check(cudaMemcpyAsync(gauge.data(), B.gauge, 4 * sizeof(double), cudaMemcpyDeviceToHost, st), "D2H");
+        check(cudaMemcpyAsync(cams.data(), D.cams_state, cams.size() * sizeof(double), cudaMemcpyDeviceToHost, st), "D2H");
+        check(cudaMemcpyAsync(&flags, B.flags, sizeof(int), cudaMemcpyDeviceToHost, st), "D2H");
+        check(cudaStreamSynchronize(st), "adjoint gradient");
+        if (flags & 2) return fail(c, PB_ERR_INVALID_PROJECTION, "an observation does not project at this state");
+        if (grad_observations) {
+            std::fill(grad_observations, grad_observations + static_cast<size_t>(m.no) * 2, 0.0);
+            for (long long p = 0; p < nop; ++p) {
+                const long long k = m.p_obs_orig[p];
+                grad_observations[2 * k] = gobs[2 * p];
+                grad_observations[2 * k + 1] = gobs[2 * p + 1];
+            }
+        }
+        if (grad_initial_cameras) {
+            // fixed cameras: final pose = initial pose (direct term) plus the cross terms
+            std::fill(grad_initial_cameras, grad_initial_cameras + static_cast<size_t>(nc) * 6, 0.0);
+            for (int cam = 0; cam < nc; ++cam)
+                if (m.camera_block[cam] < 0)
+                    for (int a = 0; a < 6; ++a)
+                        grad_initial_cameras[cam * 6 + a] = gcam[static_cast<size_t>(cam) * 6 + a] + gfc[static_cast<size_t>(cam) * 6 + a];
+            // gauge: the scale camera's centre is anchor + b n(t), b = |C_scale^0 - C_anchor^0|
+            const int sc = m.gauge_scale, an = m.gauge_anchor;
+            if (sc >= 0 && an >= 0 && m.gauge_baseline > 0.0 && m.camera_block[sc] >= 0) {
+                double nv[3], e0[3], l = 0.0, l0 = 0.0;
+                for (int i = 0; i < 3; ++i) {
+                    nv[i] = cams[static_cast<size_t>(sc) * kCamStride + 9 + i] - cams[static_cast<size_t>(an) * kCamStride + 9 + i];
+                    e0[i] = m.cams_in[static_cast<size_t>(sc) * kCamStride + 9 + i] - m.cams_in[static_cast<size_t>(an) * kCamStride + 9 + i];
+                    l += nv[i] * nv[i];
+                    l0 += e0[i] * e0[i];
+                }
+                l = std::sqrt(l);
+                l0 = std::sqrt(l0);
+                const double* gs = &gcam[static_cast<size_t>(sc) * 6 + 3];
+                double db = gauge[3];
+                for (int i = 0; i < 3; ++i) db += gs[i] * nv[i] / l;
+                for (int i = 0; i < 3; ++i) {
+                    const double u0 = e0[i] / l0;
+                    grad_initial_cameras[an * 6 + 3 + i] += gauge[i] + gs[i] - db * u0;
+                    grad_initial_cameras[sc * 6 + 3 + i] += db * u0;
+                }
+            }
+        }
+        if (grad_initial_points) {
+            std::fill(grad_initial_points, grad_initial_points + static_cast<size_t>(m.nt) * 3, 0.0);
+            for (int p = 0; p < ntp; ++p) {
+                const int t = m.trk_order[p];
+                if (m.track_block[t] >= 0) continue;
+                for (int a = 0; a < 3; ++a)
+                    grad_initial_points[static_cast<size_t>(t) * 3 + a] =
+                        gfp[static_cast<size_t>(p) * 3 + a] + (grad_points ? grad_points[static_cast<size_t>(t) * 3 + a] : 0.0);
+            }
+        }
+        if (rep) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, ev[0], ev[1]);
+            rep->hessian_ms = ms;
+            cudaEventElapsedTime(&ms, ev[1], ev[2]);
+            rep->solve_ms = ms;
+            cudaEventElapsedTime(&ms, ev[2], ev[3]);
+            rep->gradient_ms = ms;
+            cudaEventElapsedTime(&ms, ev[0], ev[3]);
+            rep->total_ms = ms;
+            rep->gpu_kernel_launches = c->launches - launches0;
+            rep->status = PB_OK;
+        }
+        return PB_OK;
+    } catch (const std::bad_alloc&) {
+        return fail(c, PB_ERR_CUDA, "device allocation failed");
+    } catch (const std::exception& e) {
+        return fail(c, PB_ERR_CUDA, e.what());
+    }
 }
 
 }  // extern "C"

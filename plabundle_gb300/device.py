@@ -158,3 +158,37 @@ class Gb300Context:
                                                  rb.ctypes.data, ra.ctypes.data, intr.ctypes.data), "download")
         return {"cameras": cams, "points": pts, "valid": valid.astype(bool), "rms_before": rb, "rms_after": ra,
                 "intrinsics": intr[:ng]}
+
+    # ---- snapshot / measurement updates / backward pass -------------------------------------
+    def save_state(self):
+        self._check(self.L.pb_gpu_save_state(self.ctx), "save_state")
+
+    def restore_state(self):
+        self._check(self.L.pb_gpu_restore_state(self.ctx), "restore_state")
+
+    def set_observations(self, index, u, v):
+        idx = np.ascontiguousarray(index, np.int64)
+        uu = np.ascontiguousarray(u, np.float64)
+        vv = np.ascontiguousarray(v, np.float64)
+        self._check(self.L.pb_gpu_set_observations(self.ctx, idx.size, idx.ctypes.data, uu.ctypes.data, vv.ctypes.data),
+                    "set_observations")
+
+    def backward(self, grad_cameras=None, grad_points=None, grad_intrinsics=None):
+        """dL/d(observations), dL/d(initial poses), dL/d(initial points) of a scalar loss of the
+        converged state (pb_gpu_backward); the inputs are dL/d(final state) in the solver's chart."""
+        p = self.problem
+        def arr(a, shape):
+            return None if a is None else np.ascontiguousarray(np.broadcast_to(a, shape), np.float64)
+        gc = arr(grad_cameras, (p.n_cameras, 6))
+        gp = arr(grad_points, (p.n_tracks, 3))
+        ng = self.sizes()["intrinsic_blocks"]
+        gi = arr(grad_intrinsics, (max(1, ng), P)) if grad_intrinsics is not None else None
+        go = np.zeros((p.n_obs, 2))
+        gic = np.zeros((p.n_cameras, 6))
+        gip = np.zeros((p.n_tracks, 3))
+        rep = native.AdjointReportC()
+        ptr = lambda a: None if a is None else a.ctypes.data  # noqa: E731
+        self._check(self.L.pb_gpu_backward(self.ctx, ptr(gc), ptr(gp), ptr(gi), go.ctypes.data, gic.ctypes.data,
+                                           gip.ctypes.data, C.byref(rep)), "backward")
+        return {"observations": go, "initial_cameras": gic, "initial_points": gip, "report": rep.as_dict()}
+

@@ -21,6 +21,7 @@ EXPORTED = [
     "pb_gpu_download_state", "pb_gpu_solve_problem", "pb_gpu_request_cancel", "pb_gpu_get_stream",
     "pb_gpu_set_timing",
     "pb_gpu_kernel_times", "pb_gpu_objective_noalloc", "pb_gpu_solve_batch",
+    "pb_gpu_save_state", "pb_gpu_restore_state", "pb_gpu_set_observations", "pb_gpu_backward",
 ]
 
 
@@ -65,6 +66,16 @@ class SolveReportC(C.Structure):
 
 
 _lib = None
+
+
+class AdjointReportC(C.Structure):
+    _fields_ = [("status", C.c_int32), ("linear_iterations", C.c_int32), ("gpu_kernel_launches", C.c_int32),
+                ("point_blocks_singular", C.c_int32), ("relative_residual", C.c_double),
+                ("hessian_ms", C.c_double), ("solve_ms", C.c_double), ("gradient_ms", C.c_double),
+                ("total_ms", C.c_double)]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
 
 
 def library_path() -> str:
@@ -117,6 +128,10 @@ def load(build_if_missing: bool = False):
     L.pb_gpu_solve_batch.argtypes = [i32, i32, vp, C.POINTER(SolveOptionsC), i32, vp, vp, vp, vp, vp]
     L.pb_gpu_objective_noalloc.argtypes = [vp, i32, vp, i32, vp, vp, vp, vp, vp, i64, i32, dbl, vp,
                                            C.POINTER(dbl), C.POINTER(i64)]
+    L.pb_gpu_save_state.argtypes = [vp]
+    L.pb_gpu_restore_state.argtypes = [vp]
+    L.pb_gpu_set_observations.argtypes = [vp, i64, vp, vp, vp]
+    L.pb_gpu_backward.argtypes = [vp, vp, vp, vp, vp, vp, vp, C.POINTER(AdjointReportC)]
     for name in EXPORTED:
         if name not in ("pb_gpu_last_error", "pb_status_name"):
             getattr(L, name).restype = i32
