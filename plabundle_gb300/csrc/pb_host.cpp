@@ -493,43 +493,28 @@ size_t chunk_smem_bytes(int precision, int max_obs, int max_tracks, int ni, int 
     return s;
 }
 
-int build_chunks(HostModel* m, int precision, size_t smem_budget, std::string* err) {
-    ChunkSet& cs = m->chunks[precision];
-    // A chunk is bounded by its observations (one thread each, shared-memory records); cameras
-    // are chunk-local 8-bit indices (255 marks an observation without a pose block) and pairs
-    // only size the partial buffers.
-    // two CTAs per SM: at most half of the 228 KB of shared memory of an SM each, less the
-    // 1 KB the runtime reserves per CTA
-    const size_t per_cta = std::min(smem_budget, static_cast<size_t>(113 * 1024));
-    const int nb = m->ng * m->ni;
-    int max_obs = 256;
-    const int max_cams = 254;
-    const int max_pairs = 1 << 15;
-    // tracks of a chunk: per-track intrinsic sums in shared memory; a quarter of the observations
-    // (tracks of four or more views fill a chunk, shorter ones close it early)
-    auto tracks_for = [](int mo) { return std::max(8, mo / 4); };
-    while (chunk_smem_bytes(precision, max_obs, tracks_for(max_obs), m->ni, nb) > per_cta && max_obs > 32) max_obs -= 32;
-    const int max_tracks = tracks_for(max_obs);
-    if (chunk_smem_bytes(precision, max_obs, max_tracks, m->ni, nb) > per_cta) {
-        *err = "assembly chunk does not fit in shared memory";
-        return PB_SOLVE_UNSUPPORTED;
-    }
-    cs = ChunkSet{};
-    cs.max_obs = max_obs;
-    cs.max_cams = max_cams;
-    cs.max_pairs = max_pairs;
-    cs.max_tracks = max_tracks;
-    const int ntp = static_cast<int>(m->trk_order.size());
-    cs.obs_lcam.assign(m->p_obs_orig.size(), 255);
+namespace {
+
+struct ChunkLimits {
+    int max_obs, max_cams, max_pairs, max_tracks;
+};
+
+// Greedy chunk plan of the processing-order tracks [p_begin, p_range_end) into `cs` (a partial plan:
+// its begin arrays are local to it, obs_begin holds global observation indices).  obs_lcam is
+// the plan-wide per-observation array; this range writes only its own observations.
+int plan_range(const HostModel* m, const ChunkLimits& lim, int p_begin, int p_range_end, ChunkSet& cs,
+               std::vector<unsigned char>& obs_lcam, std::string* err) {
+    const int max_obs = lim.max_obs, max_cams = lim.max_cams, max_pairs = lim.max_pairs, max_tracks = lim.max_tracks;
+    const int obs_range_end = m->trk_obs_begin[p_range_end];
     std::vector<int> stamp(m->nc, -1), local(m->nc, -1);
     std::vector<unsigned char> pair_seen;  // max_cams * max_cams
     std::vector<int> ccams;                // cameras (with pose blocks) of the open chunk
     std::vector<std::pair<int, int>> cpairs;
     int chunk = 0;
-    int chunk_obs_start = 0;
-    int chunk_trk_start = 0;
+    int chunk_obs_start = m->trk_obs_begin[p_begin];
+    int chunk_trk_start = p_begin;
     std::vector<int> slot_of;                        // local pair (a, b) -> chunk slot
-    cs.obs_begin.push_back(0);
+    cs.obs_begin.push_back(chunk_obs_start);
     cs.slot_item_begin.push_back(0);
     cs.lcam_obs_begin.push_back(0);
     cs.cam_begin.push_back(0);
@@ -545,7 +530,7 @@ int build_chunks(HostModel* m, int precision, size_t smem_budget, std::string* e
         for (size_t i = 0; i < order.size(); ++i) remap[order[i]] = static_cast<int>(i);
         for (size_t i = 0; i < order.size(); ++i) cs.cams.push_back(ccams[order[i]]);
         for (int o = chunk_obs_start; o < obs_end; ++o)
-            if (cs.obs_lcam[o] != 255) cs.obs_lcam[o] = static_cast<unsigned char>(remap[cs.obs_lcam[o]]);
+            if (obs_lcam[o] != 255) obs_lcam[o] = static_cast<unsigned char>(remap[obs_lcam[o]]);
         std::vector<std::pair<int, int>> rp;
         rp.reserve(cpairs.size());
         for (auto& p : cpairs) {
@@ -567,7 +552,7 @@ int build_chunks(HostModel* m, int precision, size_t smem_budget, std::string* e
         // Two passes over the chunk's tracks: count the items of every slot, then place them.
         std::vector<int> cnt(rp.size() + 1, 0);
         int p_end = chunk_trk_start;
-        while (p_end < static_cast<int>(m->trk_order.size()) && m->trk_obs_begin[p_end] < obs_end) ++p_end;
+        while (p_end < p_range_end && m->trk_obs_begin[p_end] < obs_end) ++p_end;
         for (int pass = 0; pass < 2; ++pass) {
             auto emit = [&](int a, int b, unsigned short item) {
                 const int sl = slot_of[static_cast<size_t>(a) * ncl + b];
@@ -578,13 +563,13 @@ int build_chunks(HostModel* m, int precision, size_t smem_budget, std::string* e
                 const int o0 = m->trk_obs_begin[p], o1 = m->trk_obs_begin[p + 1];
                 const bool el = m->track_block[m->trk_order[p]] >= 0;
                 for (int i = o0; i < o1; ++i) {
-                    const int li = cs.obs_lcam[i];
+                    const int li = obs_lcam[i];
                     if (li == 255) continue;
                     const int ii = i - chunk_obs_start;
                     emit(li, li, static_cast<unsigned short>(ii | (ii << 8)));
                     if (!el) continue;
                     for (int j = i + 1; j < o1; ++j) {
-                        const int lj = cs.obs_lcam[j];
+                        const int lj = obs_lcam[j];
                         if (lj == 255) continue;
                         const int jj = j - chunk_obs_start;
                         if (li < lj) {
@@ -612,7 +597,7 @@ int build_chunks(HostModel* m, int precision, size_t smem_budget, std::string* e
         {
             std::vector<int> cc(static_cast<size_t>(ncl) + 1, 0);
             for (int o = chunk_obs_start; o < obs_end; ++o)
-                if (cs.obs_lcam[o] != 255) ++cc[cs.obs_lcam[o] + 1];
+                if (obs_lcam[o] != 255) ++cc[obs_lcam[o] + 1];
             const int base = static_cast<int>(cs.lcam_obs.size());
             cc[0] = base;
             for (int l = 0; l < ncl; ++l) {
@@ -621,7 +606,7 @@ int build_chunks(HostModel* m, int precision, size_t smem_budget, std::string* e
             }
             cs.lcam_obs.resize(static_cast<size_t>(cc[ncl]));
             for (int o = chunk_obs_start; o < obs_end; ++o)
-                if (cs.obs_lcam[o] != 255) cs.lcam_obs[cc[cs.obs_lcam[o]]++] = static_cast<unsigned char>(o - chunk_obs_start);
+                if (obs_lcam[o] != 255) cs.lcam_obs[cc[obs_lcam[o]]++] = static_cast<unsigned char>(o - chunk_obs_start);
         }
         cs.obs_begin.push_back(obs_end);
         cs.cam_begin.push_back(static_cast<int>(cs.cams.size()));
@@ -635,7 +620,7 @@ int build_chunks(HostModel* m, int precision, size_t smem_budget, std::string* e
     pair_seen.assign(static_cast<size_t>(max_cams) * max_cams, 0);
     std::vector<int> tcams, ol;
     std::vector<std::pair<int, int>> tpairs;
-    for (int p = 0; p < ntp; ++p) {
+    for (int p = p_begin; p < p_range_end; ++p) {
         const int t = m->trk_order[p];
         const int o0 = m->trk_obs_begin[p], o1 = m->trk_obs_begin[p + 1];
         const bool elim = m->track_block[t] >= 0;
@@ -698,13 +683,92 @@ int build_chunks(HostModel* m, int precision, size_t smem_budget, std::string* e
                 pair_seen[static_cast<size_t>(q.first) * max_cams + q.second] = 1;
                 cpairs.push_back(q);
             }
-            for (int i = 0; i < o1 - o0; ++i) cs.obs_lcam[o0 + i] = ol[i] < 0 ? 255 : static_cast<unsigned char>(ol[i]);
+            for (int i = 0; i < o1 - o0; ++i) obs_lcam[o0 + i] = ol[i] < 0 ? 255 : static_cast<unsigned char>(ol[i]);
             break;
         }
     }
-    if (chunk_obs_start < static_cast<int>(m->p_obs_orig.size()) || ntp == 0) {
+    if (chunk_obs_start < obs_range_end || p_range_end == p_begin) {
         for (auto& q : cpairs) pair_seen[static_cast<size_t>(q.first) * max_cams + q.second] = 0;
-        close_chunk(static_cast<int>(m->p_obs_orig.size()));
+        close_chunk(obs_range_end);
+    }
+    return 0;
+}
+
+}  // namespace
+
+// Chunk plan of the whole problem: fixed segments of the processing order (16 for problems of
+// 64k observations or more, else one) are planned concurrently and concatenated in order.  The
+// segment count does not depend on the host's thread count, so the plan - and the summation
+// order of the assembly - is the same on every machine.
+int build_chunks(HostModel* m, int precision, size_t smem_budget, std::string* err) {
+    ChunkSet& cs = m->chunks[precision];
+    // A chunk is bounded by its observations (one thread each, shared-memory records); cameras
+    // are chunk-local 8-bit indices (255 marks an observation without a pose block) and pairs
+    // only size the partial buffers.
+    // two CTAs per SM: at most half of the 228 KB of shared memory of an SM each, less the
+    // 1 KB the runtime reserves per CTA
+    const size_t per_cta = std::min(smem_budget, static_cast<size_t>(113 * 1024));
+    const int nb = m->ng * m->ni;
+    int max_obs = 256;
+    const int max_cams = 254;
+    const int max_pairs = 1 << 15;
+    // tracks of a chunk: per-track intrinsic sums in shared memory; a quarter of the observations
+    // (tracks of four or more views fill a chunk, shorter ones close it early)
+    auto tracks_for = [](int mo) { return std::max(8, mo / 4); };
+    while (chunk_smem_bytes(precision, max_obs, tracks_for(max_obs), m->ni, nb) > per_cta && max_obs > 32) max_obs -= 32;
+    const int max_tracks = tracks_for(max_obs);
+    if (chunk_smem_bytes(precision, max_obs, max_tracks, m->ni, nb) > per_cta) {
+        *err = "assembly chunk does not fit in shared memory";
+        return PB_SOLVE_UNSUPPORTED;
+    }
+    cs = ChunkSet{};
+    cs.max_obs = max_obs;
+    cs.max_cams = max_cams;
+    cs.max_pairs = max_pairs;
+    cs.max_tracks = max_tracks;
+    const ChunkLimits lim{max_obs, max_cams, max_pairs, max_tracks};
+    const int ntp = static_cast<int>(m->trk_order.size());
+    const long long nop = static_cast<long long>(m->p_obs_orig.size());
+    cs.obs_lcam.assign(static_cast<size_t>(nop), 255);
+    constexpr int kPlanSegments = 16;
+    const int nseg = nop >= 65536 && ntp >= kPlanSegments ? kPlanSegments : 1;
+    std::vector<int> seg(nseg + 1, 0);
+    seg[nseg] = ntp;
+    for (int k = 1; k < nseg; ++k) {
+        const long long target = nop * k / nseg;
+        const int* b = m->trk_obs_begin.data();
+        seg[k] = std::max(seg[k - 1], static_cast<int>(std::lower_bound(b, b + ntp, target) - b));
+    }
+    std::vector<ChunkSet> parts(nseg);
+    std::vector<int> rcs(nseg, 0);
+    std::vector<std::string> errs(nseg);
+    parallel_ranges(nseg, std::min(nseg, host_threads(nop)), [&](int, int k0, int k1) {
+        for (int k = k0; k < k1; ++k) rcs[k] = plan_range(m, lim, seg[k], seg[k + 1], parts[k], cs.obs_lcam, &errs[k]);
+    });
+    for (int k = 0; k < nseg; ++k)
+        if (rcs[k]) {
+            *err = errs[k];
+            return rcs[k];
+        }
+    // concatenate the segment plans
+    cs.obs_begin.push_back(0);
+    cs.cam_begin.push_back(0);
+    cs.pair_begin.push_back(0);
+    cs.slot_item_begin.push_back(0);
+    cs.lcam_obs_begin.push_back(0);
+    for (const ChunkSet& q : parts) {
+        const int cam0 = static_cast<int>(cs.cams.size()), pair0 = static_cast<int>(cs.pairs.size());
+        const int item0 = static_cast<int>(cs.slot_items.size()), lobs0 = static_cast<int>(cs.lcam_obs.size());
+        cs.obs_begin.insert(cs.obs_begin.end(), q.obs_begin.begin() + 1, q.obs_begin.end());
+        for (size_t i = 1; i < q.cam_begin.size(); ++i) cs.cam_begin.push_back(cam0 + q.cam_begin[i]);
+        for (size_t i = 1; i < q.pair_begin.size(); ++i) cs.pair_begin.push_back(pair0 + q.pair_begin[i]);
+        for (size_t i = 1; i < q.slot_item_begin.size(); ++i) cs.slot_item_begin.push_back(item0 + q.slot_item_begin[i]);
+        for (size_t i = 1; i < q.lcam_obs_begin.size(); ++i) cs.lcam_obs_begin.push_back(lobs0 + q.lcam_obs_begin[i]);
+        cs.cams.insert(cs.cams.end(), q.cams.begin(), q.cams.end());
+        cs.pairs.insert(cs.pairs.end(), q.pairs.begin(), q.pairs.end());
+        cs.pair_upper.insert(cs.pair_upper.end(), q.pair_upper.begin(), q.pair_upper.end());
+        cs.slot_items.insert(cs.slot_items.end(), q.slot_items.begin(), q.slot_items.end());
+        cs.lcam_obs.insert(cs.lcam_obs.end(), q.lcam_obs.begin(), q.lcam_obs.end());
     }
     // map each chunk pair to its upper pose block and build the reduce lists
     const int nupper = static_cast<int>(m->up_row.size());

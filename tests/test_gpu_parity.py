@@ -245,3 +245,31 @@ def test_block_jacobi_pcg_solve_matches_oracle(mixed):
     scale = np.linalg.norm(C_ref - C_ref.mean(0), axis=1).max()
     assert np.abs(out["cameras"][:, 9:12] - C_ref).max() / scale < 1e-6
     assert np.array_equal(out["valid"], ref["valid"])
+
+
+@pytest.mark.parametrize("name,make,opts", CASES)
+def test_parity_report_of_the_public_solve(name, make, opts):
+    """Solver.solve on the GPU (FP64) against the oracle, through the reference's outcome
+    comparison (plabundle_gb300/parity.py): id-keyed camera and track differences, identical
+    valid masks, matching termination status."""
+    from plabundle_gb300.parity import PhotoAlignmentComparisonTolerance, compare_outcomes, make_outcome
+    from plabundle_gb300.problem import QualitySummary, RefinedPoint, Result
+    from plabundle_gb300.solver import Solver
+    p = make()
+    o = opts(False)
+    got = Solver().solve(p, o)
+    ref = O.Oracle(p, opts()).solve()
+    rr = ref["report"]
+    oracle_result = Result(status=SolveStatus(rr["status"]), solutionUsable=bool(rr["solution_usable"]),
+                           quality=QualitySummary(meanRmsBefore=rr["mean_rms_before"], meanRmsAfter=rr["mean_rms_after"]),
+                           points=RefinedPoint(valid=ref["valid"], converged=True, point=ref["points"],
+                                               rmsBefore=ref["rms_before"], rmsAfter=ref["rms_after"], iterations=0),
+                           refinedCameras=ref["cameras"], backendMessage=got.backendMessage)
+    tol = PhotoAlignmentComparisonTolerance(rms=1e-6, cameraCenterMeters=1e-6, cameraRotationDegrees=1e-6,
+                                            pointMeters=1e-4)
+    c = compare_outcomes(make_outcome(oracle_result), make_outcome(got), tol)
+    assert c.comparable
+    assert c.validTrackMaskMismatchIds == []
+    assert c.terminationStatusMatches
+    assert c.equivalent, (c.maximumCameraCenterDifferenceMeters, c.maximumCameraRotationDifferenceDegrees,
+                          c.maximumPointDifferenceMeters, c.rmsAfterDifference)
