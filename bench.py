@@ -253,9 +253,8 @@ def run_adjoint(args, rank, world, local_rank):
     point and is re-converged with full Gauss-Newton steps."""
     import numpy as np
     import torch
-    from plabundle_gb300.adjoint import camera_centre_loss, polish
+    from plabundle_gb300.adjoint import camera_centre_loss, newton_polish
     from plabundle_gb300.device import Gb300Context
-    from plabundle_gb300.problem import Precision
 
     torch.cuda.set_device(local_rank)
     prob, opts, cfg = workload("aerial")
@@ -263,7 +262,7 @@ def run_adjoint(args, rank, world, local_rank):
     ctx = Gb300Context(local_rank)
     assert ctx.upload(prob, opts) == 0
     rep = ctx.solve()
-    polish(ctx, iterations=4, precision=Precision.Mixed)
+    trace = newton_polish(ctx, iterations=4)
     d = ctx.download()
     rng = np.random.default_rng(2024)
     targets = prob.truth_cameras[:, 9:12] + rng.normal(0.0, 0.1, (prob.n_cameras, 3))
@@ -303,7 +302,7 @@ def run_adjoint(args, rank, world, local_rank):
                 u, v = prob.obs_u[k], prob.obs_v[k]
                 ctx.set_observations([k], [u + sgn * h * (a == 0)], [v + sgn * h * (a == 1)])
                 ctx.restore_state()
-                polish(ctx, iterations=8, precision=Precision.Mixed)
+                newton_polish(ctx, iterations=3)
                 vals.append(camera_centre_loss(ctx.download()["cameras"], targets)[0])
                 ctx.set_observations([k], [u], [v])
             fd[i, a] = (vals[0] - vals[1]) / (2.0 * h)
@@ -325,7 +324,8 @@ def run_adjoint(args, rank, world, local_rank):
             "phases_ms": {k: last[k] for k in ("hessian_ms", "solve_ms", "gradient_ms", "total_ms")},
             "adjoint_linear_iterations": last["linear_iterations"],
             "adjoint_relative_residual": last["relative_residual"],
-            "forward_solve": {"status": rep["status"], "iterations": rep["iterations"]},
+            "forward_solve": {"status": rep["status"], "iterations": rep["iterations"],
+                              "newton_polish_gradient_norms": [gn for _, gn in trace]},
             "loss": L,
             "fd_check": {"observations": int(pick.size), "h_px": h, "relative_error": float(err),
                          "per_observation_relative_error_median": float(np.median(per_obs)),

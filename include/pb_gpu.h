@@ -325,6 +325,14 @@ pb_status pb_gpu_backward(pb_gpu_ctx* ctx, const double* grad_cameras, const dou
                           const double* grad_intrinsics, double* grad_observations, double* grad_initial_cameras,
                           double* grad_initial_points, pb_adjoint_report* report);
 
+/* One Newton step of the robust objective from the current state with the exact Hessian of the
+ * backward pass, applied without a line search (no counterpart in the reference).  For polishing
+ * a converged state to its fixed point well past the LM stopping rule, e.g. the re-converged
+ * solves of a finite-difference check; from a state far from a minimum the exact Hessian can be
+ * indefinite and the call fails with PB_ERR_SINGULAR_BLOCK.  step_max: largest |primary step
+ * component|; gradient_norm: |reduced gradient| at the state before the step (may be NULL). */
+pb_status pb_gpu_newton_step(pb_gpu_ctx* ctx, double* step_max, double* gradient_norm);
+
 #define PB_NOALLOC_MAX_OBS 4194304
 pb_status pb_gpu_objective_noalloc(const double* cameras, int32_t n_cameras, const double* points, int32_t n_points,
                                    const int32_t* obs_camera, const int32_t* obs_point, const double* obs_u,

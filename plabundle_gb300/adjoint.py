@@ -26,6 +26,21 @@ def camera_centre_loss(cameras: np.ndarray, targets: np.ndarray):
     return float((d * d).sum()), g
 
 
+def newton_polish(ctx, iterations: int = 6, tol: float = 0.0):
+    """Exact-Hessian Newton steps from a converged state (pb_gpu_newton_step): quadratic
+    convergence to the fixed point, where the Gauss-Newton steps of `polish` converge linearly
+    (slowly, when the robust loss's curvature makes the exact Hessian much smaller than
+    J^T W J).  The fixed point is the zero of the gradient either way.  Returns the list of
+    (largest step component, reduced gradient norm) per step."""
+    trace = []
+    for _ in range(iterations):
+        sm, gn = ctx.newton_step()
+        trace.append((sm, gn))
+        if tol > 0.0 and sm <= tol:
+            break
+    return trace
+
+
 def polish(ctx, iterations: int = 8, precision=Precision.Fp64, tol: float = 0.0):
     """Full Gauss-Newton steps (no damping, no line search) from the current state: converges
     to the same fixed point as the LM solve, past its stopping rule (step RMS 1e-6).  Returns the

@@ -11,23 +11,25 @@
 // drops them; at a Cauchy-weighted fixed point the rho'' term is of the same order as J^T w J).
 //
 //   k_adj_hessian   one thread per observation: FP64 Jacobian (linearize_obs), W2, and the
-//                   curvature lam^T d2 pi: second derivatives of the projection over the camera-
-//                   frame point and the intrinsics by hyper-dual numbers (exact), composed with
-//                   the analytic second derivatives of the camera-frame point in the chart
-//                   (rotation generators, gauge sphere); writes one record per observation.
-//   k_adj_rhs       dL/dz of the primary variables into the reduced right-hand side.
-//   k_adj_schur     one thread per track: point blocks V = sum H_pp, V^-1 (FP64), and the
-//                   eliminated terms -W V^-1 W^T scattered into the reduced system of the forward
-//                   path (pose CSR blocks, border, intrinsic block) with FP64 atomics; intrinsic
-//                   terms are first summed in shared memory per thread block.
-//   k_adj_finalize  priors (invSigma^2), empty diagonals, border transpose.
+//                   curvature lam^T d2 pi: analytic second derivatives of the projection over the
+//                   camera-frame point and the intrinsics, composed with the second derivatives
+//                   of the camera-frame point in the chart (rotation generators, gauge sphere);
+//                   writes one record per observation.
+//   k_adj_assemble  one CTA per chunk of the forward path's chunk plan: point blocks V = sum H_pp,
+//                   V^-1 (FP64), and the eliminated system -W V^-1 W^T plus the own terms, every
+//                   output element owned by one thread (fixed-order sums, no atomics), written
+//                   as FP64 chunk partials and summed by the forward reduce kernels into the
+//                   reduced system (pose CSR blocks, border, intrinsic block);
+//   k_adj_finalize  priors (invSigma^2), empty diagonals;
+//   k_adj_rhs       dL/dz of the primary variables added to the reduced right-hand side.
 //   (the reduced system is then solved by the forward path's dense Cholesky-preconditioned CG
 //    or block-Jacobi PCG)
 //   k_adj_gradient  one thread per track: point back-substitution mu_p = V^-1 (b_p - W^T mu_c),
 //                   dL/d(u, v) = W2 J mu per observation, cross terms of fixed cameras and
 //                   tracks, and the gauge terms (anchor centre, baseline) from the scale camera's
 //                   observations in the Euclidean centre chart.
-// The FP64 atomics make the reduced sums' order (and their last bits) vary from run to run.
+// Every sum of the reduced system and of dL/d(u, v) has a fixed order; only the initial-pose cross
+// terms of fixed cameras and of the gauge pair are accumulated with FP64 atomics.
 #include <cuda_runtime.h>
 
 #include "pb_kernels.h"
@@ -36,62 +38,102 @@ namespace pb {
 
 namespace {
 
-// ---------------------------------------------------------------- hyper-dual numbers
-// v + a e1 + b e2 + ab e1 e2 with e1^2 = e2^2 = 0: one evaluation gives f, df/dx_i, df/dx_j and
-// d2f/dx_i dx_j exactly.
-struct HD {
-    double v, a, b, ab;
-};
-__device__ __forceinline__ HD hd(double x) { return {x, 0.0, 0.0, 0.0}; }
-__device__ __forceinline__ HD operator+(HD x, HD y) { return {x.v + y.v, x.a + y.a, x.b + y.b, x.ab + y.ab}; }
-__device__ __forceinline__ HD operator*(HD x, HD y) {
-    return {x.v * y.v, fma(x.v, y.a, x.a * y.v), fma(x.v, y.b, x.b * y.v),
-            fma(x.v, y.ab, fma(x.a, y.b, fma(x.b, y.a, x.ab * y.v)))};
-}
-__device__ __forceinline__ HD operator*(double s, HD x) { return {s * x.v, s * x.a, s * x.b, s * x.ab}; }
-__device__ __forceinline__ HD operator+(double s, HD x) { return {s + x.v, x.a, x.b, x.ab}; }
-__device__ __forceinline__ HD hd_recip(HD x) {
-    const double i = 1.0 / x.v, i2 = i * i;
-    return {i, -i2 * x.a, -i2 * x.b, -i2 * x.ab + 2.0 * i2 * i * x.a * x.b};
-}
-__device__ __forceinline__ HD hd_exp(HD x) {
-    const double e = exp(x.v);
-    return {e, e * x.a, e * x.b, e * (x.ab + x.a * x.b)};
-}
-
-// lam^T pi(x_c + dx, kappa + dk) - the pixel projection weighted by lam - as a hyper-dual
-// function of the camera-frame point and the refined intrinsic columns (group chart: fx, log
-// aspect, cx, cy, k1, k2, k3, p1, p2 additive; fy = fx * aspect).
-__device__ __forceinline__ HD lam_pixel(const DCam& c, const HD* xv, const HD* kv, int ni, const int* cols,
-                                        double lam0, double lam1) {
-    HD fx = hd(c.fx), la = hd(0.0), cx = hd(c.cx), cy = hd(c.cy);
-    HD k1 = hd(c.k1), k2 = hd(c.k2), k3 = hd(c.k3), p1 = hd(c.p1), p2 = hd(c.p2);
-    for (int k = 0; k < ni; ++k) {
-        switch (cols[k]) {
-            case 0: fx = fx + kv[k]; break;
-            case 1: la = la + kv[k]; break;
-            case 2: cx = cx + kv[k]; break;
-            case 3: cy = cy + kv[k]; break;
-            case 4: k1 = k1 + kv[k]; break;
-            case 5: k2 = k2 + kv[k]; break;
-            case 6: k3 = k3 + kv[k]; break;
-            case 7: p1 = p1 + kv[k]; break;
-            case 8: p2 = p2 + kv[k]; break;
-            default: break;
-        }
-    }
+// Gradient gx (3) and Hessian Hm (M x M, M = 3 + ni, row-major) of lam^T pi(x_c, kappa) over the
+// camera-frame point x_c and the refined intrinsic columns kappa (group chart: fx, log aspect,
+// cx, cy, k1, k2, k3, p1, p2, additive; fy = fx * aspect).  Analytic: derivatives of the
+// distorted normalised point (xd, yd) over (x, y) = (X / Z, Y / Z), chained through the
+// perspective division; the intrinsics enter bilinearly (focal x distortion), so their own
+// block is non-zero only in the focal and aspect rows.
+__host__ __device__ __forceinline__ void lam_pixel_derivatives(const DCam& c, const double* xc, double lam0, double lam1, int ni,
+                                                      const int* cols, double* gx, double* Hm) {
+    const int M = 3 + ni;
+    const double iz = 1.0 / xc[2];
+    const double x = xc[0] * iz, y = xc[1] * iz;
+    const double r2 = x * x + y * y;
+    const double R = 1.0 + r2 * (c.k1 + r2 * (c.k2 + r2 * c.k3));
+    const double R1 = c.k1 + r2 * (2.0 * c.k2 + 3.0 * c.k3 * r2);
+    const double R2 = 2.0 * c.k2 + 6.0 * c.k3 * r2;
+    const double p1 = c.p1, p2 = c.p2;
+    const double yd = y * R + p1 * (r2 + 2.0 * y * y) + 2.0 * p2 * x * y;
+    const double xd_x = R + 2.0 * x * x * R1 + 2.0 * p1 * y + 6.0 * p2 * x;
+    const double xd_y = 2.0 * x * y * R1 + 2.0 * p1 * x + 2.0 * p2 * y;
+    const double yd_x = xd_y;
+    const double yd_y = R + 2.0 * y * y * R1 + 6.0 * p1 * y + 2.0 * p2 * x;
+    const double xd_xx = 6.0 * x * R1 + 4.0 * x * x * x * R2 + 6.0 * p2;
+    const double xd_xy = 2.0 * y * R1 + 4.0 * x * x * y * R2 + 2.0 * p1;
+    const double xd_yy = 2.0 * x * R1 + 4.0 * x * y * y * R2 + 2.0 * p2;
+    const double yd_xx = xd_xy;
+    const double yd_xy = xd_yy;
+    const double yd_yy = 6.0 * y * R1 + 4.0 * y * y * y * R2 + 6.0 * p1;
     const double aspect = c.fx > 0.0 ? c.fy / c.fx : 1.0;
-    const HD fy = fx * (aspect * hd_exp(la));
-    const HD iz = hd_recip(xv[2]);
-    const HD x = xv[0] * iz, y = xv[1] * iz;
-    const HD r2 = x * x + y * y;
-    const HD radial = 1.0 + r2 * (k1 + r2 * (k2 + r2 * k3));
-    const HD xy2 = 2.0 * (x * y);
-    const HD xd = x * radial + p1 * xy2 + p2 * (r2 + 2.0 * (x * x));
-    const HD yd = y * radial + p1 * (r2 + 2.0 * (y * y)) + p2 * xy2;
-    const HD pu = (c.su * fx) * xd + cx;
-    const HD pv = (c.sv * fy) * yd + cy;
-    return lam0 * pu + lam1 * pv;
+    const double al = lam0 * c.su * c.fx, be = lam1 * c.sv * c.fy;
+    const double Px = al * xd_x + be * yd_x, Py = al * xd_y + be * yd_y;
+    const double Pxx = al * xd_xx + be * yd_xx, Pxy = al * xd_xy + be * yd_xy, Pyy = al * xd_yy + be * yd_yy;
+    const double iz2 = iz * iz;
+    gx[0] = iz * Px;
+    gx[1] = iz * Py;
+    gx[2] = -iz * (x * Px + y * Py);
+    // J_n = iz [[1, 0, -x], [0, 1, -y]]; H = J_n^T P'' J_n + Px d2(x) + Py d2(y)
+    Hm[0 * M + 0] = iz2 * Pxx;
+    Hm[0 * M + 1] = Hm[1 * M + 0] = iz2 * Pxy;
+    Hm[1 * M + 1] = iz2 * Pyy;
+    Hm[0 * M + 2] = Hm[2 * M + 0] = -iz2 * (x * Pxx + y * Pxy + Px);
+    Hm[1 * M + 2] = Hm[2 * M + 1] = -iz2 * (x * Pxy + y * Pyy + Py);
+    Hm[2 * M + 2] = iz2 * (x * x * Pxx + 2.0 * x * y * Pxy + y * y * Pyy + 2.0 * (x * Px + y * Py));
+    // per intrinsic column: the (x, y)-gradient (kx, ky) of d(lam^T pi)/d kappa, and for the
+    // distortion columns the shape (shx, shy) = d(xd, yd)/d kappa that the focal and aspect rows
+    // multiply
+    double kx[kMaxNI], ky[kMaxNI], shx[kMaxNI], shy[kMaxNI];
+    for (int k = 0; k < ni; ++k) {
+        double dxd = 0.0, dyd = 0.0, dxd_x = 0.0, dxd_y = 0.0, dyd_x = 0.0, dyd_y = 0.0;
+        switch (cols[k]) {
+            case 0:  // fx (fy = fx * aspect follows)
+                kx[k] = lam0 * c.su * xd_x + lam1 * c.sv * aspect * yd_x;
+                ky[k] = lam0 * c.su * xd_y + lam1 * c.sv * aspect * yd_y;
+                shx[k] = shy[k] = 0.0;
+                continue;
+            case 1:  // log aspect: d fy = fy
+                kx[k] = be * yd_x;
+                ky[k] = be * yd_y;
+                shx[k] = shy[k] = 0.0;
+                continue;
+            case 4: dxd = x * r2; dyd = y * r2; dxd_x = r2 + 2.0 * x * x; dxd_y = 2.0 * x * y; dyd_x = dxd_y;
+                    dyd_y = r2 + 2.0 * y * y; break;
+            case 5: dxd = x * r2 * r2; dyd = y * r2 * r2; dxd_x = r2 * r2 + 4.0 * x * x * r2; dxd_y = 4.0 * x * y * r2;
+                    dyd_x = dxd_y; dyd_y = r2 * r2 + 4.0 * y * y * r2; break;
+            case 6: dxd = x * r2 * r2 * r2; dyd = y * r2 * r2 * r2; dxd_x = r2 * r2 * r2 + 6.0 * x * x * r2 * r2;
+                    dxd_y = 6.0 * x * y * r2 * r2; dyd_x = dxd_y; dyd_y = r2 * r2 * r2 + 6.0 * y * y * r2 * r2; break;
+            case 7: dxd = 2.0 * x * y; dyd = r2 + 2.0 * y * y; dxd_x = 2.0 * y; dxd_y = 2.0 * x; dyd_x = 2.0 * x;
+                    dyd_y = 6.0 * y; break;
+            case 8: dxd = r2 + 2.0 * x * x; dyd = 2.0 * x * y; dxd_x = 6.0 * x; dxd_y = 2.0 * y; dyd_x = 2.0 * y;
+                    dyd_y = 2.0 * x; break;
+            default: break;  // cx, cy: constant derivatives
+        }
+        kx[k] = al * dxd_x + be * dyd_x;
+        ky[k] = al * dxd_y + be * dyd_y;
+        shx[k] = dxd;
+        shy[k] = dyd;
+    }
+    // intrinsic-intrinsic block: only the focal and log-aspect rows are non-zero
+    for (int k = 0; k < ni; ++k)
+        for (int l = k; l < ni; ++l) {
+            const int ck = cols[k], cl = cols[l];
+            const int a = ck < cl ? ck : cl, b = ck < cl ? cl : ck;
+            const int kb = ck < cl ? l : k;  // the column of the larger index
+            double h = 0.0;
+            if (a == 0 && b == 1) h = lam1 * c.sv * aspect * yd;
+            else if (a == 1 && b == 1) h = be * yd;
+            else if (a == 0 && b >= 4) h = lam0 * c.su * shx[kb] + lam1 * c.sv * aspect * shy[kb];
+            else if (a == 1 && b >= 4) h = be * shy[kb];
+            Hm[(3 + k) * M + 3 + l] = Hm[(3 + l) * M + 3 + k] = h;
+        }
+    // point-intrinsic block: J_n^T (kx, ky)
+    for (int k = 0; k < ni; ++k) {
+        const double h0 = iz * kx[k], h1 = iz * ky[k], h2 = -iz * (x * kx[k] + y * ky[k]);
+        Hm[0 * M + 3 + k] = Hm[(3 + k) * M + 0] = h0;
+        Hm[1 * M + 3 + k] = Hm[(3 + k) * M + 1] = h1;
+        Hm[2 * M + 3 + k] = Hm[(3 + k) * M + 2] = h2;
+    }
 }
 
 __device__ __forceinline__ int sym6(int a, int b) { return a * 6 - a * (a - 1) / 2 + (b - a); }
@@ -124,19 +166,11 @@ __device__ bool adj_obs_hessian(const DCam& c, const double* X, double s, double
     const double d[3] = {X[0] - c.C[0], X[1] - c.C[1], X[2] - c.C[2]};
     double xc[3];
     for (int m = 0; m < 3; ++m) xc[m] = c.R[m] * d[0] + c.R[3 + m] * d[1] + c.R[6 + m] * d[2];
-    // second derivatives of lam^T pi over (x_c, kappa): M = 3 + ni hyper-dual passes per row
+    // second derivatives of lam^T pi over (x_c, kappa)
     const int M = 3 + ni;
     double gx[3];
     double Hm[(3 + kMaxNI) * (3 + kMaxNI)];
-    for (int i = 0; i < M; ++i)
-        for (int j = i; j < M; ++j) {
-            HD xv[3], kv[kMaxNI];
-            for (int m = 0; m < 3; ++m) xv[m] = {xc[m], i == m ? 1.0 : 0.0, j == m ? 1.0 : 0.0, 0.0};
-            for (int k = 0; k < ni; ++k) kv[k] = {0.0, i == 3 + k ? 1.0 : 0.0, j == 3 + k ? 1.0 : 0.0, 0.0};
-            const HD f = lam_pixel(c, xv, kv, ni, cols, lam0, lam1);
-            Hm[i * M + j] = Hm[j * M + i] = f.ab;
-            if (i == j && i < 3) gx[i] = f.a;
-        }
+    lam_pixel_derivatives(c, xc, lam0, lam1, ni, cols, gx, Hm);
     // camera-frame point Jacobian over (w0..2, centre 0..2, dX 0..2), columns of Jx[m][col]
     const double sg[3] = {1.0, -1.0, -1.0};
     double Jx[3][9];
@@ -270,8 +304,8 @@ __global__ void __launch_bounds__(128) k_adj_hessian(Shape S, DevPtrs D, AdjBuff
     }
 }
 
-// Reduced right-hand side: dL/dz of the primary variables (point terms are subtracted by the
-// Schur kernel).  One thread per camera, then one per intrinsic column.
+// dL/dz of the primary variables added to the reduced right-hand side (which holds the point
+// terms after the reduction).  One thread per camera, then one per intrinsic column.
 __global__ void k_adj_rhs(Shape S, DevPtrs D, AdjBuffers B, double* __restrict__ rhs) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t < S.nc) {
@@ -279,25 +313,24 @@ __global__ void k_adj_rhs(Shape S, DevPtrs D, AdjBuffers B, double* __restrict__
         if (b < 0) return;
         const double* g = B.gcam + static_cast<size_t>(t) * 6;
         double* r = rhs + 6 * b;
-        r[0] = g[0];
-        r[1] = g[1];
-        r[2] = g[2];
+        r[0] += g[0];
+        r[1] += g[1];
+        r[2] += g[2];
         if (is_tangent(S, t)) {
             const double* gb = D.gauge_basis;
-            r[3] = g[3] * gb[0] + g[4] * gb[1] + g[5] * gb[2];
-            r[4] = g[3] * gb[3] + g[4] * gb[4] + g[5] * gb[5];
-            r[5] = 0.0;
+            r[3] += g[3] * gb[0] + g[4] * gb[1] + g[5] * gb[2];
+            r[4] += g[3] * gb[3] + g[4] * gb[4] + g[5] * gb[5];
         } else {
-            r[3] = g[3];
-            r[4] = g[4];
-            r[5] = g[5];
+            r[3] += g[3];
+            r[4] += g[4];
+            r[5] += g[5];
         }
         return;
     }
     const int q = t - S.nc;
     if (q < S.nb) {
         const int g = q / S.ni, k = q - g * S.ni;
-        rhs[6 * S.ncb + q] = B.gint[static_cast<size_t>(g) * kP + S.int_cols[k]];
+        rhs[6 * S.ncb + q] += B.gint[static_cast<size_t>(g) * kP + S.int_cols[k]];
     }
 }
 
@@ -334,136 +367,281 @@ __device__ __forceinline__ bool sym3_inverse(const double* u, double* inv) {
     return true;
 }
 
-constexpr int kSchurThreads = 128;
-
-__global__ void __launch_bounds__(kSchurThreads) k_adj_schur(Shape S, DevPtrs D, AdjBuffers B, RedOut<double> R) {
-    extern __shared__ double s_k[];  // nb * nb intrinsic block, then nb rhs
-    const int nb = S.nb, ni = S.ni;
-    for (int i = threadIdx.x; i < nb * nb + nb; i += blockDim.x) s_k[i] = 0.0;
-    __syncthreads();
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    const AdjLayout& Lo = B.lay;
-    if (t < S.ntp) {
-        const int ob = D.trk_obs_begin[t], oe = D.trk_obs_begin[t + 1];
-        // own terms
-        for (int o = ob; o < oe; ++o) {
-            const double* rec = B.rec + static_cast<size_t>(o) * Lo.stride;
-            const int cam = D.obs_cam[o];
-            const int b = D.cam_block[cam], g = S.ng > 0 ? D.cam_group[cam] : -1;
-            if (b >= 0) {
-                double* blk = R.vals + static_cast<size_t>(D.diag_pos[b]) * 36;
-                const double* h = rec + Lo.hcc();
-                for (int a = 0; a < 6; ++a)
-                    for (int q = 0; q < 6; ++q) atomicAdd(blk + a * 6 + q, h[a <= q ? sym6(a, q) : sym6(q, a)]);
-                if (g >= 0) {
-                    const double* hk = rec + Lo.hck();
-                    for (int a = 0; a < 6; ++a)
-                        for (int k = 0; k < ni; ++k)
-                            atomicAdd(R.border + static_cast<size_t>(6 * b + a) * nb + g * ni + k, hk[a * ni + k]);
-                }
-            }
-            if (g >= 0) {
-                const double* hk = rec + Lo.hkk();
-                for (int k = 0; k < ni; ++k)
-                    for (int l = 0; l < ni; ++l)
-                        atomicAdd(s_k + (g * ni + k) * nb + g * ni + l, hk[k <= l ? symn(ni, k, l) : symn(ni, l, k)]);
-            }
+// Right-hand side of a track's point block: s(X) dL/dX (backward pass), or in Newton mode the
+// descent direction -grad F = -sum_o Jp_o^T lam_o over its observations (point chart).
+__device__ __forceinline__ void track_rhs(const Shape& S, const DevPtrs& D, const AdjBuffers& B, int trk, double* bp) {
+    if (B.newton) {
+        bp[0] = bp[1] = bp[2] = 0.0;
+        const int nl = 9 + S.ni;
+        for (int o = D.trk_obs_begin[trk]; o < D.trk_obs_begin[trk + 1]; ++o) {
+            const double* rec = B.rec + static_cast<size_t>(o) * B.lay.stride;
+            const double* J = rec + B.lay.jac();
+            const double l0 = rec[B.lay.w2() + 3], l1 = rec[B.lay.w2() + 4];
+            for (int i = 0; i < 3; ++i) bp[i] -= J[6 + i] * l0 + J[nl + 6 + i] * l1;
         }
-        if (D.trk_block[t] >= 0) {
+        return;
+    }
+    const double sp = D.pscale[trk];
+    for (int i = 0; i < 3; ++i) bp[i] = sp * B.gpt[static_cast<size_t>(trk) * 3 + i];
+}
+
+constexpr int kAdjThreads = 256;
+
+template <typename U>
+__device__ __forceinline__ U* carve(char*& ptr, size_t count) {
+    U* out = reinterpret_cast<U*>(ptr);
+    ptr += (count * sizeof(U) + 15) & ~static_cast<size_t>(15);
+    return out;
+}
+
+// Point elimination of the exact Hessian over the forward path's chunk plan: one CTA per chunk
+// of consecutive tracks, every output element owned by one thread that sums its terms over the
+// host-built item lists in a fixed order (deterministic, no atomics), written as FP64 chunk
+// partials in the layout of the forward assembly and summed by the forward reduce kernels:
+//   pose block (a, b):  sum_o H_cc(o) (own items)  -  sum_(oa, ob) Y_oa W_ob^T,  Y = W V^-1
+//   border (c, g):      sum_(o in c, g) H_ck(o)  -  sum_(o in c) Y_o K_(t(o), g)
+//   intrinsic (g, g'):  sum_(o in g) H_kk(o)  -  sum_t K_(t,g)^T V_t^-1 K_(t,g')
+//   rhs:                -sum_(o in c) Y_o b_t  and  -sum_t K_(t,g)^T V_t^-1 b_t
+// with W = H_cp (pose-point), K_(t,g) = sum over the track's observations of group g of H_pk,
+// V_t = sum H_pp and b_t = s(X) dL/dX of the track.
+__global__ void __launch_bounds__(kAdjThreads, 2)
+    k_adj_assemble(Shape S, DevPtrs D, AdjBuffers B, double* __restrict__ part_pair, double* __restrict__ part_cam,
+                   double* __restrict__ part_chunk) {
+    extern __shared__ __align__(16) char smem[];
+    const AdjLayout& Lo = B.lay;
+    const int chunk = blockIdx.x, tid = threadIdx.x;
+    const int MO = S.max_obs, MT = S.max_tracks;
+    const int ng = S.ng, ni = S.ni, nb = S.nb;
+    char* ptr = smem;
+    double* s_W = carve<double>(ptr, static_cast<size_t>(MO) * 18);     // H_cp per observation
+    double* s_Vi = carve<double>(ptr, static_cast<size_t>(MT) * 12);    // V^-1 (9) and q = V^-1 b (3) per track
+    double* s_K = carve<double>(ptr, static_cast<size_t>(MT) * nb * 3);  // K[(t, g*ni + c), j]
+    int* s_info = carve<int>(ptr, MO);                                  // group + 1 | elim << 4 | slot << 8
+    int* s_tfirst = carve<int>(ptr, MT + 1);
+    int* s_flag = carve<int>(ptr, 1);
+    const int obs0 = D.ch_obs_begin[chunk], nobs = D.ch_obs_begin[chunk + 1] - obs0;
+    const int trk0 = D.obs_trk[obs0];
+    const int ntc = D.obs_trk[obs0 + nobs - 1] - trk0 + 1;
+    if (tid == 0) s_flag[0] = ntc > MT ? 1 : 0;
+    __syncthreads();
+    if (s_flag[0]) {
+        if (tid == 0) atomicOr(B.flags, 4);
+        return;
+    }
+    // per observation: H_cp into shared memory, group / elimination / track slot
+    if (tid < nobs) {
+        const int o = obs0 + tid;
+        const double* rec = B.rec + static_cast<size_t>(o) * Lo.stride + Lo.hcp();
+        for (int i = 0; i < 18; ++i) s_W[tid * 18 + i] = rec[i];
+        const int cam = D.obs_cam[o], trk = D.obs_trk[o];
+        const int g = ng > 0 ? D.cam_group[cam] : -1;
+        const int elim = D.trk_block[trk] >= 0 ? 1 : 0;
+        const int slot = trk - trk0;
+        s_info[tid] = (g + 1) | (elim << 4) | (slot << 8);
+        if (o == D.trk_obs_begin[trk]) s_tfirst[slot] = tid;
+    }
+    if (tid == 0) s_tfirst[ntc] = nobs;
+    __syncthreads();
+    // per track: V^-1 and q (FP64), also kept for the gradient kernel
+    if (tid < ntc) {
+        const int trk = trk0 + tid;
+        double Vi[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, q[3] = {0, 0, 0};
+        if (D.trk_block[trk] >= 0) {
             double V[6] = {0, 0, 0, 0, 0, 0};
-            for (int o = ob; o < oe; ++o) {
+            for (int o = D.trk_obs_begin[trk]; o < D.trk_obs_begin[trk + 1]; ++o) {
                 const double* h = B.rec + static_cast<size_t>(o) * Lo.stride + Lo.hpp();
                 for (int i = 0; i < 6; ++i) V[i] += h[i];
             }
-            double Vi[9];
             if (!sym3_inverse(V, Vi)) {
                 atomicOr(B.flags, 1);
                 for (int i = 0; i < 9; ++i) Vi[i] = 0.0;
             }
-            for (int i = 0; i < 9; ++i) B.vinv[static_cast<size_t>(t) * 9 + i] = Vi[i];
-            // dL/d(point chart) = s(X) dL/dX
-            const double sp = D.pscale[t];
-            const double bp[3] = {sp * B.gpt[static_cast<size_t>(t) * 3], sp * B.gpt[static_cast<size_t>(t) * 3 + 1],
-                                  sp * B.gpt[static_cast<size_t>(t) * 3 + 2]};
-            double q[3];
+            double bp[3];
+            track_rhs(S, D, B, trk, bp);
             for (int i = 0; i < 3; ++i) q[i] = Vi[i * 3] * bp[0] + Vi[i * 3 + 1] * bp[1] + Vi[i * 3 + 2] * bp[2];
-            for (int o1 = ob; o1 < oe; ++o1) {
-                const double* rec1 = B.rec + static_cast<size_t>(o1) * Lo.stride;
-                const int cam1 = D.obs_cam[o1];
-                const int b1 = D.cam_block[cam1], g1 = S.ng > 0 ? D.cam_group[cam1] : -1;
-                const double* hcp1 = rec1 + Lo.hcp();
-                const double* hpk1 = rec1 + Lo.hpk();
-                // Y1 = Hcp1 V^-1 (6 x 3), K1 = Hpk1^T V^-1 (ni x 3)
-                double Y1[18], K1[3 * kMaxNI];
-                for (int a = 0; a < 6; ++a)
-                    for (int j = 0; j < 3; ++j)
-                        Y1[a * 3 + j] = hcp1[a * 3] * Vi[j] + hcp1[a * 3 + 1] * Vi[3 + j] + hcp1[a * 3 + 2] * Vi[6 + j];
-                for (int k = 0; k < ni; ++k)
-                    for (int j = 0; j < 3; ++j)
-                        K1[k * 3 + j] = hpk1[k] * Vi[j] + hpk1[ni + k] * Vi[3 + j] + hpk1[2 * ni + k] * Vi[6 + j];
-                if (b1 >= 0)
-                    for (int a = 0; a < 6; ++a)
-                        atomicAdd(R.rhs + 6 * b1 + a, -(hcp1[a * 3] * q[0] + hcp1[a * 3 + 1] * q[1] + hcp1[a * 3 + 2] * q[2]));
-                if (g1 >= 0)
-                    for (int k = 0; k < ni; ++k)
-                        atomicAdd(s_k + nb * nb + g1 * ni + k,
-                                  -(hpk1[k] * q[0] + hpk1[ni + k] * q[1] + hpk1[2 * ni + k] * q[2]));
-                for (int o2 = ob; o2 < oe; ++o2) {
-                    const double* rec2 = B.rec + static_cast<size_t>(o2) * Lo.stride;
-                    const int cam2 = D.obs_cam[o2];
-                    const int b2 = D.cam_block[cam2], g2 = S.ng > 0 ? D.cam_group[cam2] : -1;
-                    const double* hcp2 = rec2 + Lo.hcp();
-                    const double* hpk2 = rec2 + Lo.hpk();
-                    if (b1 >= 0 && b2 >= 0) {
-                        const int pos = csr_find(D, b1, b2);
-                        if (pos < 0) {
-                            atomicOr(B.flags, 4);
-                        } else {
-                            double* blk = R.vals + static_cast<size_t>(pos) * 36;
-                            for (int a = 0; a < 6; ++a)
-                                for (int q2 = 0; q2 < 6; ++q2)
-                                    atomicAdd(blk + a * 6 + q2, -(Y1[a * 3] * hcp2[q2 * 3] + Y1[a * 3 + 1] * hcp2[q2 * 3 + 1] +
-                                                                  Y1[a * 3 + 2] * hcp2[q2 * 3 + 2]));
-                        }
-                    }
-                    if (b1 >= 0 && g2 >= 0)
-                        for (int a = 0; a < 6; ++a)
-                            for (int k = 0; k < ni; ++k)
-                                atomicAdd(R.border + static_cast<size_t>(6 * b1 + a) * nb + g2 * ni + k,
-                                          -(Y1[a * 3] * hpk2[k] + Y1[a * 3 + 1] * hpk2[ni + k] + Y1[a * 3 + 2] * hpk2[2 * ni + k]));
-                    if (g1 >= 0 && g2 >= 0)
-                        for (int k = 0; k < ni; ++k)
-                            for (int l = 0; l < ni; ++l)
-                                atomicAdd(s_k + (g1 * ni + k) * nb + g2 * ni + l,
-                                          -(K1[k * 3] * hpk2[l] + K1[k * 3 + 1] * hpk2[ni + l] + K1[k * 3 + 2] * hpk2[2 * ni + l]));
-                }
+        }
+        for (int i = 0; i < 9; ++i) {
+            s_Vi[tid * 12 + i] = Vi[i];
+            B.vinv[static_cast<size_t>(trk) * 9 + i] = Vi[i];
+        }
+        for (int i = 0; i < 3; ++i) s_Vi[tid * 12 + 9 + i] = q[i];
+    }
+    // per track and group: K = sum of H_pk over the track's observations of the group
+    if (nb > 0) {
+        const int per = nb * 3;
+        for (int it = tid; it < ntc * per; it += blockDim.x) {
+            const int t = it / per, r = it - t * per;
+            const int gc = r / 3, j = r - gc * 3;
+            const int g = gc / ni, c = gc - g * ni;
+            double acc = 0.0;
+            for (int ob = s_tfirst[t]; ob < s_tfirst[t + 1]; ++ob) {
+                if ((s_info[ob] & 15) - 1 != g) continue;
+                acc += B.rec[static_cast<size_t>(obs0 + ob) * Lo.stride + Lo.hpk() + j * ni + c];
             }
+            s_K[it] = acc;
         }
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < nb * nb; i += blockDim.x)
-        if (s_k[i] != 0.0) atomicAdd(R.Cm + i, s_k[i]);
-    for (int i = threadIdx.x; i < nb; i += blockDim.x)
-        if (s_k[nb * nb + i] != 0.0) atomicAdd(R.rhs + 6 * S.ncb + i, s_k[nb * nb + i]);
+    // owner gathers
+    const int pair0 = D.ch_pair_begin[chunk], npairs = D.ch_pair_begin[chunk + 1] - pair0;
+    const int cam0 = D.ch_cam_begin[chunk], ncams = D.ch_cam_begin[chunk + 1] - cam0;
+    const int camrec = 12 + ng * 6 * ni;
+    const int crow = 2 + ng * ni;
+    const int chrec = nb * nb + 2 * nb;
+    const int w_pair = npairs * 6, w_cam = ncams * crow;
+    const int w_total = w_pair + w_cam + chrec;
+    // row x of Y_o = W_o V_t^-1
+    auto yrow = [&](int ob, int x, double* y) {
+        const int info = s_info[ob];
+        if (!((info >> 4) & 1)) {
+            y[0] = y[1] = y[2] = 0.0;
+            return;
+        }
+        const double* Vi = s_Vi + (info >> 8) * 12;
+        const double* w = s_W + ob * 18 + 3 * x;
+        for (int j = 0; j < 3; ++j) y[j] = w[0] * Vi[j] + w[1] * Vi[3 + j] + w[2] * Vi[6 + j];
+    };
+    for (int wk = tid; wk < w_total; wk += blockDim.x) {
+        if (wk < w_pair) {
+            const int sl = wk / 6, x = wk - sl * 6;
+            const int pk = D.ch_pairs[pair0 + sl];
+            const bool diag = (pk & 0xFFFF) == (pk >> 16);
+            double acc[6] = {0, 0, 0, 0, 0, 0};
+            const int i1 = D.slot_item_begin[pair0 + sl + 1];
+            for (int it = D.slot_item_begin[pair0 + sl]; it < i1; ++it) {
+                const unsigned item = D.slot_items[it];
+                const int oa = item & 0xFF, ob = item >> 8;
+                double y[3];
+                yrow(oa, x, y);
+                const double* wb = s_W + ob * 18;
+                if (oa == ob) {
+                    const double* h = B.rec + static_cast<size_t>(obs0 + oa) * Lo.stride + Lo.hcc();
+                    for (int q2 = 0; q2 < 6; ++q2) acc[q2] += h[x <= q2 ? sym6(x, q2) : sym6(q2, x)];
+                }
+                for (int q2 = 0; q2 < 6; ++q2) acc[q2] -= y[0] * wb[3 * q2] + y[1] * wb[3 * q2 + 1] + y[2] * wb[3 * q2 + 2];
+            }
+            double* out = part_pair + static_cast<size_t>(pair0 + sl) * 36;
+            for (int q2 = 0; q2 < 6; ++q2) {
+                if (!diag) {
+                    out[x * 6 + q2] = acc[q2];
+                } else if (q2 >= x) {
+                    out[x * 6 + q2] = acc[q2];
+                    out[q2 * 6 + x] = acc[q2];
+                }
+            }
+        } else if (wk < w_pair + w_cam) {
+            const int r = wk - w_pair;
+            const int l = r / crow, row = r - l * crow;
+            const int b0 = D.lcam_obs_begin[cam0 + l], b1 = D.lcam_obs_begin[cam0 + l + 1];
+            double* out = part_cam + static_cast<size_t>(cam0 + l) * camrec;
+            double acc[6] = {0, 0, 0, 0, 0, 0};
+            if (row == 0) {
+                // reduced right-hand side: -Y_o b_t = -W_o q_t, and in Newton mode the camera's
+                // own descent direction -J_c^T lam
+                for (int it = b0; it < b1; ++it) {
+                    const int ob = D.lcam_obs[it];
+                    const int info = s_info[ob];
+                    if (B.newton) {
+                        const double* rec = B.rec + static_cast<size_t>(obs0 + ob) * Lo.stride;
+                        const double* J = rec + Lo.jac();
+                        const double l0 = rec[Lo.w2() + 3], l1 = rec[Lo.w2() + 4];
+                        for (int a = 0; a < 6; ++a) acc[a] -= J[a] * l0 + J[9 + ni + a] * l1;
+                    }
+                    if (!((info >> 4) & 1)) continue;
+                    const double* q = s_Vi + (info >> 8) * 12 + 9;
+                    const double* w = s_W + ob * 18;
+                    for (int a = 0; a < 6; ++a) acc[a] -= w[3 * a] * q[0] + w[3 * a + 1] * q[1] + w[3 * a + 2] * q[2];
+                }
+                for (int a = 0; a < 6; ++a) out[a] = acc[a];
+            } else if (row == 1) {
+                for (int a = 0; a < 6; ++a) out[6 + a] = 0.0;
+            } else {
+                const int gc = row - 2, g = gc / ni, c2 = gc - g * ni;
+                for (int it = b0; it < b1; ++it) {
+                    const int ob = D.lcam_obs[it];
+                    const int info = s_info[ob];
+                    if ((info & 15) - 1 == g) {
+                        const double* h = B.rec + static_cast<size_t>(obs0 + ob) * Lo.stride + Lo.hck();
+                        for (int a = 0; a < 6; ++a) acc[a] += h[a * ni + c2];
+                    }
+                    if ((info >> 4) & 1) {
+                        const double* Kt = s_K + (static_cast<size_t>(info >> 8) * nb + gc) * 3;
+                        for (int a = 0; a < 6; ++a) {
+                            double y[3];
+                            yrow(ob, a, y);
+                            acc[a] -= y[0] * Kt[0] + y[1] * Kt[1] + y[2] * Kt[2];
+                        }
+                    }
+                }
+                for (int a = 0; a < 6; ++a) out[12 + (g * 6 + a) * ni + c2] = acc[a];
+            }
+        } else {
+            const int e = wk - w_pair - w_cam;
+            double* out = part_chunk + static_cast<size_t>(chunk) * chrec;
+            double acc = 0.0;
+            if (e < nb * nb) {
+                const int i = e / nb, j = e - i * nb;
+                if (i > j) continue;
+                const int g1 = i / ni, c1 = i - g1 * ni, g2 = j / ni, c2 = j - g2 * ni;
+                if (g1 == g2)
+                    for (int ob = 0; ob < nobs; ++ob) {
+                        if ((s_info[ob] & 15) - 1 != g1) continue;
+                        const double* h = B.rec + static_cast<size_t>(obs0 + ob) * Lo.stride + Lo.hkk();
+                        acc += h[c1 <= c2 ? symn(ni, c1, c2) : symn(ni, c2, c1)];
+                    }
+                for (int t = 0; t < ntc; ++t) {
+                    if (!((s_info[s_tfirst[t]] >> 4) & 1)) continue;
+                    const double* K1 = s_K + (static_cast<size_t>(t) * nb + i) * 3;
+                    const double* K2 = s_K + (static_cast<size_t>(t) * nb + j) * 3;
+                    const double* Vi = s_Vi + t * 12;
+                    for (int r = 0; r < 3; ++r)
+                        acc -= K1[r] * (Vi[r * 3] * K2[0] + Vi[r * 3 + 1] * K2[1] + Vi[r * 3 + 2] * K2[2]);
+                }
+                out[e] = acc;
+                if (i != j) out[j * nb + i] = acc;
+            } else if (e < nb * nb + nb) {
+                const int col = e - nb * nb;
+                if (B.newton) {
+                    const int g = col / ni, c = col - g * ni;
+                    for (int ob = 0; ob < nobs; ++ob) {
+                        if ((s_info[ob] & 15) - 1 != g) continue;
+                        const double* rec = B.rec + static_cast<size_t>(obs0 + ob) * Lo.stride;
+                        const double* J = rec + Lo.jac();
+                        acc -= J[9 + c] * rec[Lo.w2() + 3] + J[9 + ni + 9 + c] * rec[Lo.w2() + 4];
+                    }
+                }
+                for (int t = 0; t < ntc; ++t) {
+                    if (!((s_info[s_tfirst[t]] >> 4) & 1)) continue;
+                    const double* K1 = s_K + (static_cast<size_t>(t) * nb + col) * 3;
+                    const double* q = s_Vi + t * 12 + 9;
+                    acc -= K1[0] * q[0] + K1[1] * q[1] + K1[2] * q[2];
+                }
+                out[e] = acc;
+            } else {
+                out[e] = 0.0;
+            }
+        }
+    }
 }
 
-// Priors on the intrinsic diagonal (0.5 (invSigma (theta - prior))^2 has Hessian invSigma^2),
-// structurally empty diagonals set to 1 (their right-hand side is zero), border transpose.
-__global__ void k_adj_finalize(Shape S, DevPtrs D, RedOut<double> R) {
+// Priors on the intrinsic diagonal (0.5 (invSigma (theta - prior))^2 has Hessian invSigma^2) and
+// structurally empty diagonals set to 1 (their right-hand side is zero).
+__global__ void k_adj_finalize(Shape S, DevPtrs D, RedOut<double> R, int newton) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int nd = 6 * S.ncb;
     if (t < nd) {
         const int b = t / 6, a = t - b * 6;
         double* d = R.vals + static_cast<size_t>(D.diag_pos[b]) * 36 + a * 7;
         if (*d == 0.0) *d = 1.0;
-        for (int k = 0; k < S.nb; ++k)
-            R.border_t[static_cast<size_t>(k) * nd + t] = R.border[static_cast<size_t>(t) * S.nb + k];
     } else if (t < nd + S.nb) {
         const int q = t - nd, g = q / S.ni, k = q - g * S.ni;
-        const double w = D.groups[static_cast<size_t>(g) * kGroupRec + 2 * kP + S.int_cols[k]];
+        const double* G = D.groups + static_cast<size_t>(g) * kGroupRec;
+        const int p = S.int_cols[k];
+        const double w = G[2 * kP + p];
         double* d = R.Cm + static_cast<size_t>(q) * S.nb + q;
         const double v = *d + w * w;
         *d = v != 0.0 ? v : 1.0;
+        if (newton) R.rhs[nd + q] -= w * w * (G[p] - G[kP + p]);
     }
 }
 
@@ -479,7 +657,7 @@ __global__ void __launch_bounds__(128) k_adj_gradient(Shape S, DevPtrs D, AdjBuf
     double mp[3] = {0.0, 0.0, 0.0};
     if (free_pt) {
         double acc[3];
-        for (int i = 0; i < 3; ++i) acc[i] = D.pscale[t] * B.gpt[static_cast<size_t>(t) * 3 + i];
+        track_rhs(S, D, B, t, acc);
         for (int o = ob; o < oe; ++o) {
             const double* rec = B.rec + static_cast<size_t>(o) * Lo.stride;
             const int cam = D.obs_cam[o];
@@ -599,13 +777,25 @@ void launch_adjoint_rhs(const Shape& S, const DevPtrs& D, const AdjBuffers& B, c
     k_adj_rhs<<<(n + 127) / 128, 128, 0, st>>>(S, D, B, R.rhs);
 }
 
-void launch_adjoint_schur(const Shape& S, const DevPtrs& D, const AdjBuffers& B, const RedOut<double>& R,
-                          cudaStream_t st) {
-    if (S.ntp <= 0) return;
-    const size_t smem = static_cast<size_t>(S.nb * S.nb + S.nb) * sizeof(double);
-    k_adj_schur<<<(S.ntp + kSchurThreads - 1) / kSchurThreads, kSchurThreads, smem, st>>>(S, D, B, R);
+size_t adjoint_assemble_smem(const Shape& S) {
+    const auto up = [](size_t b) { return (b + 15) & ~static_cast<size_t>(15); };
+    return up(static_cast<size_t>(S.max_obs) * 18 * sizeof(double)) + up(static_cast<size_t>(S.max_tracks) * 12 * sizeof(double)) +
+           up(static_cast<size_t>(S.max_tracks) * S.nb * 3 * sizeof(double)) + up(static_cast<size_t>(S.max_obs) * sizeof(int)) +
+           up(static_cast<size_t>(S.max_tracks + 1) * sizeof(int)) + up(sizeof(int));
+}
+
+void launch_adjoint_schur(const Shape& S, const DevPtrs& D, const AdjBuffers& B, const AsmOut& part,
+                          const RedOut<double>& R, cudaStream_t st) {
+    if (S.nchunks > 0) {
+        const size_t smem = adjoint_assemble_smem(S);
+        cudaFuncSetAttribute(k_adj_assemble, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        k_adj_assemble<<<S.nchunks, kAdjThreads, smem, st>>>(S, D, B, static_cast<double*>(part.part_pair_v),
+                                                              static_cast<double*>(part.part_cam_v),
+                                                              static_cast<double*>(part.part_chunk_v));
+    }
+    launch_reduce_sums64(S, D, part, R, st);
     const int n = 6 * S.ncb + S.nb;
-    k_adj_finalize<<<(n + 127) / 128, 128, 0, st>>>(S, D, R);
+    k_adj_finalize<<<(n + 127) / 128, 128, 0, st>>>(S, D, R, B.newton);
 }
 
 void launch_adjoint_gradient(const Shape& S, const DevPtrs& D, const AdjBuffers& B, const double* mu, cudaStream_t st) {

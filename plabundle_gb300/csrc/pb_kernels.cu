@@ -609,6 +609,22 @@ void launch_reduce(const Shape& S, const DevPtrs& D, const AsmOut& O, const RedO
                                                   damping);
 }
 
+// The fixed-order sums of FP64 chunk partials of launch_reduce, without the damping and prior
+// finalisation (the backward pass finalises its exact Hessian itself).
+void launch_reduce_sums64(const Shape& S, const DevPtrs& D, const AsmOut& O, const RedOut<double>& R, cudaStream_t st) {
+    const AsmOutT<double> P = typed<double>(O);
+    const long long np = static_cast<long long>(S.nupper) * 36;
+    if (np > 0) k_reduce_pairs<double><<<static_cast<unsigned>((np + 255) / 256), 256, 0, st>>>(S, D, P.part_pair, R.vals);
+    const long long nc = static_cast<long long>(S.ncb) * (12 + S.ng * 6 * S.ni);
+    if (nc > 0)
+        k_reduce_cams<double><<<static_cast<unsigned>((nc + 255) / 256), 256, 0, st>>>(S, D, P.part_cam, R.rhs, R.direct,
+                                                                                       R.border, R.border_t);
+    const int chrec = S.nb * S.nb + 2 * S.nb;
+    const int tiles = (chrec + 31) / 32;
+    k_reduce_chunks<double><<<tiles + 1, 256, 0, st>>>(S, P.part_chunk, O.part_cost, O.part_flags, R.Cm, R.rhs + 6 * S.ncb,
+                                                       R.direct + 6 * S.ncb, R.result);
+}
+
 template <typename T>
 void launch_back_substitute(const Shape& S, const DevPtrs& D, const double* trk_data, const T* obs_rec, const double* step_c,
                             double* step_p, double* part, const double* direct64, double* out, cudaStream_t st) {

@@ -56,6 +56,7 @@ void launch_assemble(const Shape& S, const DevPtrs& D, const AsmOut& O, double d
 template <typename T>
 void launch_reduce(const Shape& S, const DevPtrs& D, const AsmOut& O, const RedOut<double>& R, double damping,
                    cudaStream_t st);
+void launch_reduce_sums64(const Shape& S, const DevPtrs& D, const AsmOut& O, const RedOut<double>& R, cudaStream_t st);
 template <typename T>
 void launch_back_substitute(const Shape& S, const DevPtrs& D, const double* trk_data, const T* obs_rec, const double* step_c,
                             double* step_p, double* part, const double* direct64, double* out, cudaStream_t st);
@@ -172,13 +173,18 @@ struct AdjBuffers {
     double* grad_fixed_cam; // nc * 6 cross terms of fixed cameras (zeroed by the caller)
     double* grad_fixed_pt;  // ntp * 3 cross terms of fixed tracks (world)
     double* gauge;          // 4: cross terms of the anchor centre (3) and the gauge baseline (zeroed)
+    AsmOut part;            // FP64 chunk partials of the point elimination
+    int newton;             // 1: right-hand side -grad F (a Newton step of the objective) instead of dL/dz
     int* flags;             // bit 0: singular point block, bit 1: invalid projection, bit 2: pattern miss
 };
 
 void launch_adjoint_hessian(const Shape& S, const DevPtrs& D, const AdjBuffers& B, cudaStream_t st);
 void launch_adjoint_rhs(const Shape& S, const DevPtrs& D, const AdjBuffers& B, const RedOut<double>& R, cudaStream_t st);
-void launch_adjoint_schur(const Shape& S, const DevPtrs& D, const AdjBuffers& B, const RedOut<double>& R,
-                          cudaStream_t st);
+size_t adjoint_assemble_smem(const Shape& S);
+// Point elimination into FP64 chunk partials (part: part_pair_v / part_cam_v / part_chunk_v as
+// double, part_cost / part_flags zero), their reduction into R, and the finalisation.
+void launch_adjoint_schur(const Shape& S, const DevPtrs& D, const AdjBuffers& B, const AsmOut& part,
+                          const RedOut<double>& R, cudaStream_t st);
 void launch_adjoint_gradient(const Shape& S, const DevPtrs& D, const AdjBuffers& B, const double* mu, cudaStream_t st);
 
 void to_double(const float* in, double* out, int n, cudaStream_t st);

@@ -160,6 +160,7 @@ struct pb_gpu_ctx {
     DeviceArena aarena;
     AdjBuffers adj{};
     bool adj_ready = false;
+    int adj_prec = 0;
     DeviceArena sarena;
     double* snap_cams = nullptr;
     double* snap_points = nullptr;
@@ -1467,35 +1468,154 @@ pb_status pb_gpu_set_observations(pb_gpu_ctx* c, int64_t n, const int64_t* index
 }
 
 // ------------------------------------------------------------------ backward pass
+}  // extern "C"
+
+namespace {
+
+// Exact-Hessian solve of the backward pass (newton == 0: H mu = dL/dz with dL/dz already in the
+// adjoint input buffers) or of a Newton step of the objective (newton == 1: H mu = -grad F).
+// Leaves mu in c->step_c (primary) and c->adj.mu_p (points), dL/d(u, v) and the cross terms in
+// the adjoint buffers.  ms[0..2]: Hessian, solve and gradient phases.
+pb_status adjoint_core(pb_gpu_ctx* c, int newton, pb_adjoint_report* rep, float* ms) {
+    const HostModel& m = c->model;
+    const int prec = c->adj_prec;
+    const Shape& S = c->S[prec];
+    const DevPtrs& D = c->D[prec];
+    cudaStream_t st = c->stream;
+    const int nc = m.nc, ntp = S.ntp;
+    AdjBuffers& B = c->adj;
+    B.newton = newton;
+    cudaEvent_t ev[4];
+    for (auto& e : ev) check(cudaEventCreate(&e), "event");
+    struct EvGuard {
+        cudaEvent_t* e;
+        ~EvGuard() { for (int i = 0; i < 4; ++i) cudaEventDestroy(e[i]); }
+    } guard{ev};
+    check(cudaEventRecord(ev[0], st), "event");
+    // exact Hessian at the current state, reduced over the points
+    const int n = S.n;
+    RedOut<double>& R = c->red;
+    check(cudaMemsetAsync(B.grad_fixed_cam, 0, static_cast<size_t>(nc) * 6 * sizeof(double), st), "memset");
+    check(cudaMemsetAsync(B.grad_fixed_pt, 0, static_cast<size_t>(std::max(1, ntp)) * 3 * sizeof(double), st), "memset");
+    check(cudaMemsetAsync(B.gauge, 0, 4 * sizeof(double), st), "memset");
+    check(cudaMemsetAsync(B.flags, 0, sizeof(int), st), "memset");
+    check(cudaMemsetAsync(B.mu_p, 0, static_cast<size_t>(std::max(1, ntp)) * 3 * sizeof(double), st), "memset");
+    launch_effective(S, D, st);
+    launch_adjoint_hessian(S, D, B, st);
+    launch_adjoint_schur(S, D, B, B.part, R, st);
+    launch_adjoint_rhs(S, D, B, R, st);
+    c->launches += 8;
+    check(cudaGetLastError(), "adjoint launch");
+    check(cudaEventRecord(ev[1], st), "event");
+    int flags = 0;
+    check(cudaMemcpyAsync(&flags, B.flags, sizeof(int), cudaMemcpyDeviceToHost, st), "D2H");
+    check(cudaStreamSynchronize(st), "adjoint hessian");
+    c->have_system = false;  // the reduced buffers now hold the exact Hessian, not an LM system
+    if (rep) rep->point_blocks_singular = flags & 1;
+    if (flags & 2) return fail(c, PB_ERR_INVALID_PROJECTION, "an observation does not project at this state");
+    if (flags & 4) return fail(c, PB_ERR_STATE, "reduced pattern does not cover an observation pair");
+    if (flags & 1) return fail(c, PB_ERR_SINGULAR_BLOCK, "a point block of the exact Hessian is singular");
+    // solve H mu = dL/dz on the reduced system with the forward path's solvers
+    bool conv = false;
+    int it = 0;
+    double rr = 0.0;
+    const double rel = 1e-13, abs_tol = 1e-300;
+    const int max_it = std::max(400, 30 * m.P);
+    int rc;
+    c->f32_age = -1;
+    if (n > 16384) {
+        rc = solve_block_jacobi(c, rel, abs_tol, max_it, &conv, &it, &rr);
+    } else if (c->last_precision == PB_PRECISION_MIXED) {
+        rc = solve_dense<float>(c, rel, abs_tol, max_it, &conv, &it, &rr);
+    } else {
+        rc = solve_dense<double>(c, rel, abs_tol, max_it, &conv, &it, &rr);
+    }
+    c->f32_age = -1;  // the FP32 factor held now is the exact Hessian's, not an LM matrix's
+    if (rep) {
+        rep->linear_iterations = it;
+        rep->relative_residual = rr;
+    }
+    if (rc) return fail(c, PB_ERR_SINGULAR_BLOCK, "the exact Hessian is not positive definite (not a minimum?)");
+    check(cudaEventRecord(ev[2], st), "event");
+    launch_adjoint_gradient(S, D, B, c->step_c, st);
+    ++c->launches;
+    check(cudaGetLastError(), "adjoint gradient launch");
+    check(cudaEventRecord(ev[3], st), "event");
+    cudaEventSynchronize(ev[3]);
+    cudaEventElapsedTime(&ms[0], ev[0], ev[1]);
+    cudaEventElapsedTime(&ms[1], ev[1], ev[2]);
+    cudaEventElapsedTime(&ms[2], ev[2], ev[3]);
+    return PB_OK;
+}
+
+// Allocates the adjoint buffers for the chunk plan of the arithmetic path last used.
+pb_status adjoint_prepare(pb_gpu_ctx* c) {
+    const HostModel& m = c->model;
+    // the point elimination runs over the chunk plan of the arithmetic path last used
+    const int prec = c->last_precision == PB_PRECISION_MIXED ? 1 : 0;
+    if (prec == 1) prepare_precision<float>(c, prec);
+    else prepare_precision<double>(c, prec);
+    const Shape& S = c->S[prec];
+    const DevPtrs& D = c->D[prec];
+    cudaStream_t st = c->stream;
+    const int nc = m.nc, ntp = S.ntp;
+    const long long nop = S.nop;
+    AdjBuffers& B = c->adj;
+    if (c->adj_ready && c->adj_prec != prec) {
+    c->aarena.release();
+    c->adj_ready = false;
+    }
+    if (!c->adj_ready) {
+    DeviceArena& A = c->aarena;
+    B.lay = AdjLayout::make(S.ni);
+    B.rec = A.alloc<double>(static_cast<size_t>(std::max<long long>(1, nop)) * B.lay.stride);
+    B.vinv = A.alloc<double>(static_cast<size_t>(std::max(1, ntp)) * 9);
+    B.gpt = A.alloc<double>(static_cast<size_t>(std::max(1, ntp)) * 3);
+    B.gcam = A.alloc<double>(static_cast<size_t>(nc) * 6);
+    B.gint = A.alloc<double>(static_cast<size_t>(std::max(1, m.ng)) * kP);
+    B.mu_p = A.alloc<double>(static_cast<size_t>(std::max(1, ntp)) * 3);
+    B.grad_obs = A.alloc<double>(static_cast<size_t>(std::max<long long>(1, nop)) * 2);
+    B.grad_fixed_cam = A.alloc<double>(static_cast<size_t>(nc) * 6);
+    B.grad_fixed_pt = A.alloc<double>(static_cast<size_t>(std::max(1, ntp)) * 3);
+    B.gauge = A.alloc<double>(4);
+    B.flags = A.alloc<int>(1);
+    const ChunkSet& cs = m.chunks[prec];
+    const int nch = std::max(1, S.nchunks);
+    B.part.part_pair_v = A.alloc<double>(std::max<size_t>(1, cs.n_pair_partials()) * 36);
+    B.part.part_cam_v = A.alloc<double>(std::max<size_t>(1, cs.n_cam_partials()) * (12 + S.ng * 6 * S.ni));
+    B.part.part_chunk_v = A.alloc<double>(static_cast<size_t>(nch) * std::max(1, S.nb * S.nb + 2 * S.nb));
+    B.part.part_cost = A.alloc<double>(nch);
+    B.part.part_flags = A.alloc<int>(nch);
+    check(cudaMemsetAsync(B.part.part_cost, 0, nch * sizeof(double), st), "memset");
+    check(cudaMemsetAsync(B.part.part_flags, 0, nch * sizeof(int), st), "memset");
+    if (adjoint_assemble_smem(S) > smem_budget(c->device))
+        return fail(c, PB_ERR_UNSUPPORTED, "adjoint chunk does not fit in shared memory");
+    c->adj_prec = prec;
+    c->adj_ready = true;
+    }
+    return PB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
 pb_status pb_gpu_backward(pb_gpu_ctx* c, const double* grad_cameras, const double* grad_points,
                           const double* grad_intrinsics, double* grad_observations, double* grad_initial_cameras,
                           double* grad_initial_points, pb_adjoint_report* rep) {
     if (!c || !c->uploaded) return fail(c, PB_ERR_STATE, "no problem uploaded");
     if (rep) std::memset(rep, 0, sizeof(*rep));
     try {
+        pb_status ps = adjoint_prepare(c);
+        if (ps != PB_OK) return ps;
         const HostModel& m = c->model;
-        const Shape& S = c->S[0];
-        const DevPtrs& D = c->D[0];
+        const int prec = c->adj_prec;
+        const Shape& S = c->S[prec];
+        const DevPtrs& D = c->D[prec];
         cudaStream_t st = c->stream;
         const int nc = m.nc, ntp = S.ntp;
         const long long nop = S.nop;
         AdjBuffers& B = c->adj;
-        if (!c->adj_ready) {
-            DeviceArena& A = c->aarena;
-            B.lay = AdjLayout::make(S.ni);
-            B.rec = A.alloc<double>(static_cast<size_t>(std::max<long long>(1, nop)) * B.lay.stride);
-            B.vinv = A.alloc<double>(static_cast<size_t>(std::max(1, ntp)) * 9);
-            B.gpt = A.alloc<double>(static_cast<size_t>(std::max(1, ntp)) * 3);
-            B.gcam = A.alloc<double>(static_cast<size_t>(nc) * 6);
-            B.gint = A.alloc<double>(static_cast<size_t>(std::max(1, m.ng)) * kP);
-            B.mu_p = A.alloc<double>(static_cast<size_t>(std::max(1, ntp)) * 3);
-            B.grad_obs = A.alloc<double>(static_cast<size_t>(std::max<long long>(1, nop)) * 2);
-            B.grad_fixed_cam = A.alloc<double>(static_cast<size_t>(nc) * 6);
-            B.grad_fixed_pt = A.alloc<double>(static_cast<size_t>(std::max(1, ntp)) * 3);
-            B.gauge = A.alloc<double>(4);
-            B.flags = A.alloc<int>(1);
-            c->adj_ready = true;
-        }
         // inputs: dL/d(final state) (processing order for points)
         std::vector<double> gcam(static_cast<size_t>(nc) * 6, 0.0), gpt(static_cast<size_t>(std::max(1, ntp)) * 3, 0.0),
             gint(static_cast<size_t>(std::max(1, m.ng)) * kP, 0.0);
@@ -1513,67 +1633,11 @@ pb_status pb_gpu_backward(pb_gpu_ctx* c, const double* grad_cameras, const doubl
         check(cudaMemcpyAsync(B.gcam, gcam.data(), gcam.size() * sizeof(double), cudaMemcpyHostToDevice, st), "H2D");
         check(cudaMemcpyAsync(B.gpt, gpt.data(), gpt.size() * sizeof(double), cudaMemcpyHostToDevice, st), "H2D");
         check(cudaMemcpyAsync(B.gint, gint.data(), gint.size() * sizeof(double), cudaMemcpyHostToDevice, st), "H2D");
-        cudaEvent_t ev[4];
-        for (auto& e : ev) check(cudaEventCreate(&e), "event");
-        struct EvGuard {
-            cudaEvent_t* e;
-            ~EvGuard() { for (int i = 0; i < 4; ++i) cudaEventDestroy(e[i]); }
-        } guard{ev};
         const int launches0 = c->launches;
-        check(cudaEventRecord(ev[0], st), "event");
-        // exact Hessian at the current state, reduced over the points
-        const int n = S.n;
-        RedOut<double>& R = c->red;
-        check(cudaMemsetAsync(R.vals, 0, static_cast<size_t>(std::max(1, S.nnzb)) * 36 * sizeof(double), st), "memset");
-        check(cudaMemsetAsync(R.border, 0, static_cast<size_t>(std::max(1, S.ncb)) * 6 * std::max(1, S.nb) * sizeof(double), st),
-              "memset");
-        check(cudaMemsetAsync(R.Cm, 0, static_cast<size_t>(std::max(1, S.nb * S.nb)) * sizeof(double), st), "memset");
-        check(cudaMemsetAsync(R.rhs, 0, static_cast<size_t>(std::max(1, n)) * sizeof(double), st), "memset");
-        check(cudaMemsetAsync(B.grad_fixed_cam, 0, static_cast<size_t>(nc) * 6 * sizeof(double), st), "memset");
-        check(cudaMemsetAsync(B.grad_fixed_pt, 0, static_cast<size_t>(std::max(1, ntp)) * 3 * sizeof(double), st), "memset");
-        check(cudaMemsetAsync(B.gauge, 0, 4 * sizeof(double), st), "memset");
-        check(cudaMemsetAsync(B.flags, 0, sizeof(int), st), "memset");
-        launch_effective(S, D, st);
-        launch_adjoint_hessian(S, D, B, st);
-        launch_adjoint_rhs(S, D, B, R, st);
-        launch_adjoint_schur(S, D, B, R, st);
-        c->launches += 5;
-        check(cudaGetLastError(), "adjoint launch");
-        check(cudaEventRecord(ev[1], st), "event");
+        float ms[3] = {0.f, 0.f, 0.f};
+        ps = adjoint_core(c, 0, rep, ms);
+        if (ps != PB_OK) return ps;
         int flags = 0;
-        check(cudaMemcpyAsync(&flags, B.flags, sizeof(int), cudaMemcpyDeviceToHost, st), "D2H");
-        check(cudaStreamSynchronize(st), "adjoint hessian");
-        c->have_system = false;  // the reduced buffers now hold the exact Hessian, not an LM system
-        if (rep) rep->point_blocks_singular = flags & 1;
-        if (flags & 2) return fail(c, PB_ERR_INVALID_PROJECTION, "an observation does not project at this state");
-        if (flags & 4) return fail(c, PB_ERR_STATE, "reduced pattern does not cover an observation pair");
-        if (flags & 1) return fail(c, PB_ERR_SINGULAR_BLOCK, "a point block of the exact Hessian is singular");
-        // solve H mu = dL/dz on the reduced system with the forward path's solvers
-        bool conv = false;
-        int it = 0;
-        double rr = 0.0;
-        const double rel = 1e-13, abs_tol = 1e-300;
-        const int max_it = std::max(400, 30 * m.P);
-        int rc;
-        c->f32_age = -1;
-        if (n > 16384) {
-            rc = solve_block_jacobi(c, rel, abs_tol, max_it, &conv, &it, &rr);
-        } else if (c->last_precision == PB_PRECISION_MIXED) {
-            rc = solve_dense<float>(c, rel, abs_tol, max_it, &conv, &it, &rr);
-        } else {
-            rc = solve_dense<double>(c, rel, abs_tol, max_it, &conv, &it, &rr);
-        }
-        c->f32_age = -1;  // the FP32 factor held now is the exact Hessian's, not an LM matrix's
-        if (rep) {
-            rep->linear_iterations = it;
-            rep->relative_residual = rr;
-        }
-        if (rc) return fail(c, PB_ERR_SINGULAR_BLOCK, "the exact Hessian is not positive definite (not a minimum?)");
-        check(cudaEventRecord(ev[2], st), "event");
-        launch_adjoint_gradient(S, D, B, c->step_c, st);
-        ++c->launches;
-        check(cudaGetLastError(), "adjoint gradient launch");
-        check(cudaEventRecord(ev[3], st), "event");
         std::vector<double> gobs(static_cast<size_t>(std::max<long long>(1, nop)) * 2), gfc(static_cast<size_t>(nc) * 6),
             gfp(static_cast<size_t>(std::max(1, ntp)) * 3), gauge(4), cams(m.cams_in.size());
         check(cudaMemcpyAsync(gobs.data(), B.grad_obs, gobs.size() * sizeof(double), cudaMemcpyDeviceToHost, st), "D2H");
@@ -1632,18 +1696,57 @@ pb_status pb_gpu_backward(pb_gpu_ctx* c, const double* grad_cameras, const doubl
             }
         }
         if (rep) {
-            float ms = 0.f;
-            cudaEventElapsedTime(&ms, ev[0], ev[1]);
-            rep->hessian_ms = ms;
-            cudaEventElapsedTime(&ms, ev[1], ev[2]);
-            rep->solve_ms = ms;
-            cudaEventElapsedTime(&ms, ev[2], ev[3]);
-            rep->gradient_ms = ms;
-            cudaEventElapsedTime(&ms, ev[0], ev[3]);
-            rep->total_ms = ms;
+            rep->hessian_ms = ms[0];
+            rep->solve_ms = ms[1];
+            rep->gradient_ms = ms[2];
+            rep->total_ms = static_cast<double>(ms[0]) + ms[1] + ms[2];
             rep->gpu_kernel_launches = c->launches - launches0;
             rep->status = PB_OK;
         }
+        return PB_OK;
+    } catch (const std::bad_alloc&) {
+        return fail(c, PB_ERR_CUDA, "device allocation failed");
+    } catch (const std::exception& e) {
+        return fail(c, PB_ERR_CUDA, e.what());
+    }
+}
+
+pb_status pb_gpu_newton_step(pb_gpu_ctx* c, double* step_max, double* gradient_norm) {
+    if (!c || !c->uploaded) return fail(c, PB_ERR_STATE, "no problem uploaded");
+    try {
+        pb_status ps = adjoint_prepare(c);
+        if (ps != PB_OK) return ps;
+        const int prec = c->adj_prec;
+        const Shape& S = c->S[prec];
+        const DevPtrs& D = c->D[prec];
+        cudaStream_t st = c->stream;
+        AdjBuffers& B = c->adj;
+        check(cudaMemsetAsync(B.gcam, 0, static_cast<size_t>(S.nc) * 6 * sizeof(double), st), "memset");
+        check(cudaMemsetAsync(B.gint, 0, static_cast<size_t>(std::max(1, S.ng)) * kP * sizeof(double), st), "memset");
+        float ms[3];
+        ps = adjoint_core(c, 1, nullptr, ms);
+        if (ps != PB_OK) return ps;
+        // |reduced -grad F| before the step, then state (+) step (no line search: a polish of a
+        // converged state)
+        std::vector<double> g(static_cast<size_t>(std::max(1, S.n))), step(g.size());
+        check(cudaMemcpyAsync(g.data(), c->red.rhs, S.n * sizeof(double), cudaMemcpyDeviceToHost, st), "D2H");
+        check(cudaMemcpyAsync(step.data(), c->step_c, S.n * sizeof(double), cudaMemcpyDeviceToHost, st), "D2H");
+        check(cudaMemcpyAsync(c->step_p, B.mu_p, static_cast<size_t>(std::max(1, S.ntp)) * 3 * sizeof(double),
+                              cudaMemcpyDeviceToDevice, st), "D2D");
+        const double alpha = 1.0;
+        double cst = 0.0;
+        eval_costs(c, &alpha, 1, 1, &cst);
+        launch_accept(S, D, c->step_p, alpha, 0, st);
+        c->launches += 1;
+        check(cudaStreamSynchronize(st), "newton step");
+        c->have_system = false;
+        double gn = 0.0, sm = 0.0;
+        for (int i = 0; i < S.n; ++i) {
+            gn += g[i] * g[i];
+            sm = std::max(sm, std::fabs(step[i]));
+        }
+        if (gradient_norm) *gradient_norm = std::sqrt(gn);
+        if (step_max) *step_max = sm;
         return PB_OK;
     } catch (const std::bad_alloc&) {
         return fail(c, PB_ERR_CUDA, "device allocation failed");

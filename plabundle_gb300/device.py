@@ -192,3 +192,11 @@ class Gb300Context:
                                            gip.ctypes.data, C.byref(rep)), "backward")
         return {"observations": go, "initial_cameras": gic, "initial_points": gip, "report": rep.as_dict()}
 
+    def newton_step(self):
+        """One exact-Hessian Newton step from the current state (pb_gpu_newton_step); returns
+        (largest primary step component, reduced gradient norm before the step)."""
+        sm = C.c_double(0)
+        gn = C.c_double(0)
+        self._check(self.L.pb_gpu_newton_step(self.ctx, C.byref(sm), C.byref(gn)), "newton_step")
+        return sm.value, gn.value
+

@@ -22,6 +22,7 @@ EXPORTED = [
     "pb_gpu_set_timing",
     "pb_gpu_kernel_times", "pb_gpu_objective_noalloc", "pb_gpu_solve_batch",
     "pb_gpu_save_state", "pb_gpu_restore_state", "pb_gpu_set_observations", "pb_gpu_backward",
+    "pb_gpu_newton_step",
 ]
 
 
@@ -132,6 +133,7 @@ def load(build_if_missing: bool = False):
     L.pb_gpu_restore_state.argtypes = [vp]
     L.pb_gpu_set_observations.argtypes = [vp, i64, vp, vp, vp]
     L.pb_gpu_backward.argtypes = [vp, vp, vp, vp, vp, vp, vp, C.POINTER(AdjointReportC)]
+    L.pb_gpu_newton_step.argtypes = [vp, C.POINTER(dbl), C.POINTER(dbl)]
     for name in EXPORTED:
         if name not in ("pb_gpu_last_error", "pb_status_name"):
             getattr(L, name).restype = i32
