@@ -188,17 +188,17 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
         double Ri[6] = {0, 0, 0, 0, 0, 0}, q[3] = {0, 0, 0};
         bool singular = !(fabs(det) > 1e-15) || !isfinite(det);
         if (!singular) {
-            const double R00 = sqrt(V[0]);
-            const double R10 = V[1] / R00, R20 = V[2] / R00;
+            // Cholesky through reciprocal square roots (no FP64 division on the critical path)
+            const double i00 = rsqrt(V[0]);
+            const double R10 = V[1] * i00, R20 = V[2] * i00;
             const double a11 = V[3] - R10 * R10;
-            const double R11 = sqrt(a11);
-            const double R21 = (V[4] - R20 * R10) / R11;
+            const double i11 = rsqrt(a11);
+            const double R21 = (V[4] - R20 * R10) * i11;
             const double a22 = V[5] - R20 * R20 - R21 * R21;
-            const double R22 = sqrt(a22);
-            if (!(V[0] > 0.0) || !(a11 > 0.0) || !(a22 > 0.0) || !isfinite(R22)) {
+            const double i22 = rsqrt(a22);
+            if (!(V[0] > 0.0) || !(a11 > 0.0) || !(a22 > 0.0) || !isfinite(i22)) {
                 singular = true;
             } else {
-                const double i00 = 1.0 / R00, i11 = 1.0 / R11, i22 = 1.0 / R22;
                 const double i10 = -R10 * i00 * i11;
                 const double i21 = -R21 * i11 * i22;
                 const double i20 = -(R20 * i00 + R21 * i10) * i22;
@@ -299,7 +299,7 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
     const int crow = 2 + ng * ni;  // rows of a camera record: rhs, direct rhs, border (g, c)
     const int chrec = nb * nb + 2 * nb;
     const int w_pair = npairs * 6, w_cam = ncams * crow;
-    const int w_total = w_pair + w_cam + chrec;
+    const int w_total = w_pair + w_cam;
     for (int wk = tid; wk < w_total; wk += blockDim.x) {
         if (wk < w_pair) {
             // row x of the pose block of chunk pair slot s
@@ -404,17 +404,23 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
 #pragma unroll
                 for (int a = 0; a < 6; ++a) out[12 + (g * 6 + a) * ni + c2] = acc[a].part();
             }
-        } else {
-            // intrinsic block entry (i, j), i <= j, or an intrinsic gradient entry
-            const int e = wk - w_pair - w_cam;
-            P* out = O.part_chunk + static_cast<size_t>(chunk) * chrec;
+        }
+    }
+    // Intrinsic block entries (i, j), i <= j, and intrinsic gradient entries: one warp per entry,
+    // its lanes striding over the chunk's observations and tracks, then a fixed shuffle tree (the
+    // entries sum over every observation of the chunk, so a thread per entry would be the
+    // chunk's critical path).  Warps that finish their rows above start here at once.
+    {
+        P* out = O.part_chunk + static_cast<size_t>(chunk) * chrec;
+        const int nwarps = static_cast<int>(blockDim.x >> 5);
+        for (int e = wid; e < chrec; e += nwarps) {
             Acc<T> acc;
             if (e < nb * nb) {
                 const int i = e / nb, j = e - i * nb;
                 if (i > j) continue;
                 const int g1 = i / ni, c1 = i - g1 * ni, g2 = j / ni, c2 = j - g2 * ni;
                 if (g1 == g2) {
-                    for (int ob = 0; ob < nobs; ++ob) {
+                    for (int ob = lane; ob < nobs; ob += 32) {
                         if (info_group(s_info[ob]) != g1) continue;
                         const T* A = s_A + static_cast<size_t>(ob) * 2 * nA;
                         const VT w = s_M[static_cast<size_t>(ob) * 6 + 5];
@@ -423,7 +429,7 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
                     }
                 }
                 const int need = (1 << g1) | (1 << g2);
-                for (int t = 0; t < ntc; ++t) {
+                for (int t = lane; t < ntc; t += 32) {
                     if ((s_tmask[t] & need) != need) continue;
                     const VT* K1 = s_K + (static_cast<size_t>(t) * nb + i) * 3;
                     const VT* K2 = s_K + (static_cast<size_t>(t) * nb + j) * 3;
@@ -431,14 +437,17 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
                     acc_fma(acc, -K1[1], K2[1]);
                     acc_fma(acc, -K1[2], K2[2]);
                 }
-                out[e] = acc.part();
-                if (i != j) out[j * nb + i] = acc.part();
+                warp_merge(acc);
+                if (lane == 0) {
+                    out[e] = acc.part();
+                    if (i != j) out[j * nb + i] = acc.part();
+                }
             } else {
                 const int idx = e - nb * nb;
                 const bool reduced = idx < nb;
                 const int col = reduced ? idx : idx - nb;
                 const int g = col / ni, c = col - g * ni;
-                for (int ob = 0; ob < nobs; ++ob) {
+                for (int ob = lane; ob < nobs; ob += 32) {
                     if (info_group(s_info[ob]) != g) continue;
                     acc.add(s_D[static_cast<size_t>(ob) * nA + 6 + c]);
                     if (reduced) {
@@ -448,7 +457,8 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
                         acc_fma(acc, A[nA + 6 + c], -M[4]);
                     }
                 }
-                out[e] = acc.part();
+                warp_merge(acc);
+                if (lane == 0) out[e] = acc.part();
             }
         }
     }

@@ -388,6 +388,20 @@ __device__ __forceinline__ void acc_fma(Acc<float>& acc, float a, ff b) {
 }
 __device__ __forceinline__ void acc_fma(Acc<double>& acc, double a, double b) { acc.s = fma(a, b, acc.s); }
 
+// Sum of the accumulators of a warp into lane 0 by a fixed shuffle tree (deterministic order).
+__device__ __forceinline__ void warp_merge(Acc<double>& acc) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc.s += __shfl_down_sync(0xffffffffu, acc.s, o);
+}
+__device__ __forceinline__ void warp_merge(Acc<float>& acc) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float h = __shfl_down_sync(0xffffffffu, acc.hi, o);
+        const float l = __shfl_down_sync(0xffffffffu, acc.lo, o);
+        acc.merge_part(make_float2(h, l));
+    }
+}
+
 // exact product of two floats as a float-float
 __device__ __forceinline__ ff two_prod(float a, float b) {
     const float p = __fmul_rn(a, b);

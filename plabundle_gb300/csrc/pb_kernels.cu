@@ -667,6 +667,142 @@ void launch_strict_rms(const Shape& S, const DevPtrs& D, const double* cams, con
     k_strict_rms<<<(nt + 255) / 256, 256, 0, st>>>(S, D, cams, init_points, proc_of_track, use_state, nt, out);
 }
 
+// ---------------------------------------------------------------- quality finalisation
+// finalizeBundleAdjustResult (BundleAdjustQuality.cpp:403-502) on the device: the strict RMS
+// after the solve of every active track, the filter threshold max(filterMaxReprojError,
+// filterSigmaFactor * median of the finite RMS values), the valid mask and the mean RMS of the
+// kept tracks.  The median is an exact order statistic (radix select over the bit patterns of
+// the non-negative doubles, which order like their values), the mean of the two middle values
+// for an even count, as the host's finite median.
+
+constexpr int kQualityThreads = 1024;
+
+__device__ __forceinline__ bool quality_candidate(const signed char* active, const double* rms, int t) {
+    return active[t] && isfinite(rms[t]);
+}
+
+// k-th smallest (0-based) candidate value, by eight 8-bit radix passes; all threads take part
+__device__ double quality_select(int nt, const signed char* active, const double* rms, unsigned long long k,
+                                 unsigned int* hist, unsigned long long* s_prefix, unsigned long long* s_rank) {
+    unsigned long long prefix = 0ull, mask = 0ull;
+    if (threadIdx.x == 0) *s_rank = k;
+    for (int pass = 0; pass < 8; ++pass) {
+        const int shift = 56 - 8 * pass;
+        for (int i = threadIdx.x; i < 256; i += blockDim.x) hist[i] = 0u;
+        __syncthreads();
+        for (int t = threadIdx.x; t < nt; t += blockDim.x) {
+            if (!quality_candidate(active, rms, t)) continue;
+            const unsigned long long bits = static_cast<unsigned long long>(__double_as_longlong(rms[t]));
+            if ((bits & mask) == prefix) atomicAdd(&hist[(bits >> shift) & 255ull], 1u);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned long long r = *s_rank, before = 0ull;
+            int b = 0;
+            for (; b < 255; ++b) {
+                if (before + hist[b] > r) break;
+                before += hist[b];
+            }
+            *s_rank = r - before;
+            *s_prefix = prefix | (static_cast<unsigned long long>(b) << shift);
+        }
+        __syncthreads();
+        prefix = *s_prefix;
+        mask |= 255ull << shift;
+        __syncthreads();
+    }
+    return __longlong_as_double(static_cast<long long>(prefix));
+}
+
+// one CTA: out[0] = threshold, out[1] = candidate count
+__global__ void __launch_bounds__(kQualityThreads) k_quality_threshold(int nt, const signed char* __restrict__ active,
+                                                                       const double* __restrict__ rms, int enable,
+                                                                       double max_err, double sigma,
+                                                                       double* __restrict__ out) {
+    __shared__ unsigned int hist[256];
+    __shared__ unsigned long long s_prefix, s_rank;
+    __shared__ int s_count[kQualityThreads / 32];
+    int cnt = 0;
+    for (int t = threadIdx.x; t < nt; t += blockDim.x) cnt += quality_candidate(active, rms, t) ? 1 : 0;
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    if ((threadIdx.x & 31) == 0) s_count[threadIdx.x >> 5] = cnt;
+    __syncthreads();
+    long long n = 0;
+    for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w) n += s_count[w];
+    double thr = __longlong_as_double(0x7ff0000000000000ll);
+    if (enable) {
+        thr = isfinite(max_err) && max_err >= 0.0 ? max_err : 0.0;
+        if (n > 0 && isfinite(sigma) && sigma > 0.0) {
+            const unsigned long long h = static_cast<unsigned long long>(n / 2);
+            const double upper = quality_select(nt, active, rms, h, hist, &s_prefix, &s_rank);
+            double med = upper;
+            if ((n & 1) == 0) med = 0.5 * (quality_select(nt, active, rms, h - 1, hist, &s_prefix, &s_rank) + upper);
+            thr = fmax(thr, sigma * med);
+        }
+    }
+    if (threadIdx.x == 0) {
+        out[0] = thr;
+        out[1] = static_cast<double>(n);
+    }
+}
+
+// valid mask and per-block partials (kept, sum RMS before, sum RMS after)
+__global__ void __launch_bounds__(256) k_quality_filter(int nt, const signed char* __restrict__ active,
+                                                        const double* __restrict__ rms_before,
+                                                        const double* __restrict__ rms_after,
+                                                        const double* __restrict__ thr_in, signed char* __restrict__ valid,
+                                                        double* __restrict__ part) {
+    __shared__ double s[3][8];
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    double k = 0.0, b = 0.0, a = 0.0;
+    if (t < nt) {
+        const double thr = thr_in[0];
+        const bool v = quality_candidate(active, rms_after, t) && !(rms_after[t] > thr);
+        valid[t] = v ? 1 : 0;
+        if (v) {
+            k = 1.0;
+            b = rms_before[t];
+            a = rms_after[t];
+        }
+    }
+    const double w[3] = {warp_sum(k), warp_sum(b), warp_sum(a)};
+    if ((threadIdx.x & 31) == 0)
+        for (int i = 0; i < 3; ++i) s[i][threadIdx.x >> 5] = w[i];
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        double acc = 0.0;
+        for (int i = 0; i < 8; ++i) acc += s[threadIdx.x][i];
+        part[static_cast<size_t>(blockIdx.x) * 3 + threadIdx.x] = acc;
+    }
+}
+
+// fixed-order sums of the block partials into out[2..4]
+__global__ void k_quality_sums(int nblocks, const double* __restrict__ part, double* __restrict__ out) {
+    __shared__ double s[3][256];
+    for (int i = 0; i < 3; ++i) {
+        double acc = 0.0;
+        for (int b = threadIdx.x; b < nblocks; b += blockDim.x) acc += part[static_cast<size_t>(b) * 3 + i];
+        s[i][threadIdx.x] = acc;
+    }
+    __syncthreads();
+    for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+        if (threadIdx.x < st)
+            for (int i = 0; i < 3; ++i) s[i][threadIdx.x] += s[i][threadIdx.x + st];
+        __syncthreads();
+    }
+    if (threadIdx.x < 3) out[2 + threadIdx.x] = s[threadIdx.x][0];
+}
+
+size_t quality_part_size(int nt) { return static_cast<size_t>(std::max(1, (nt + 255) / 256)) * 3; }
+
+void launch_quality(int nt, const signed char* active, const double* rms_before, const double* rms_after, int enable,
+                    double max_err, double sigma, signed char* valid, double* part, double* out, cudaStream_t st) {
+    k_quality_threshold<<<1, kQualityThreads, 0, st>>>(nt, active, rms_after, enable, max_err, sigma, out);
+    const int nblk = std::max(1, (nt + 255) / 256);
+    k_quality_filter<<<nblk, 256, 0, st>>>(nt, active, rms_before, rms_after, out, valid, part);
+    k_quality_sums<<<1, 256, 0, st>>>(nblk, part, out);
+}
+
 
 template void launch_reduce<float>(const Shape&, const DevPtrs&, const AsmOut&, const RedOut<double>&, double,
                                    cudaStream_t);

@@ -71,6 +71,12 @@ void launch_cost(const Shape& S, const DevPtrs& D, const double* step_c, const d
 void launch_accept(const Shape& S, const DevPtrs& D, const double* step_p, double alpha, int a, cudaStream_t st);
 void launch_strict_rms(const Shape& S, const DevPtrs& D, const double* cams, const double* init_points,
                        const int* proc_of_track, int use_state, int nt, double* out, cudaStream_t st);
+// Quality finalisation on the device (finalizeBundleAdjustResult): out[0] filter threshold,
+// out[1] candidate tracks, out[2] kept tracks, out[3] / out[4] sums of the kept tracks' RMS before
+// / after; valid[nt] the valid mask.  part: quality_part_size(nt) doubles.
+size_t quality_part_size(int nt);
+void launch_quality(int nt, const signed char* active, const double* rms_before, const double* rms_after, int enable,
+                    double max_err, double sigma, signed char* valid, double* part, double* out, cudaStream_t st);
 
 // PCG (pb_pcg.cu)
 template <typename T>

@@ -140,6 +140,11 @@ struct pb_gpu_ctx {
     int* pre_status = nullptr;
     double* rms_before_d = nullptr;
     double* rms_after_d = nullptr;
+    signed char* active_d = nullptr;   // nt: active-track mask
+    signed char* valid_d = nullptr;    // nt: valid mask of the last solve
+    double* quality_part = nullptr;
+    double* quality_out = nullptr;     // threshold, candidates, kept, sum RMS before / after
+    bool quality_host_stale = false;   // valid / rms_after live on the device only
     double* init_points_all = nullptr;
     int* proc_of_track = nullptr;
     // pinned host scratch
@@ -324,6 +329,11 @@ void upload_structure(pb_gpu_ctx* c) {
     c->pre_status = A.alloc<int>(1);
     c->rms_before_d = A.alloc<double>(nt);
     c->rms_after_d = A.alloc<double>(nt);
+    c->active_d = upload_new(A, m.active_track, st);
+    c->valid_d = A.alloc<signed char>(nt);
+    c->quality_part = A.alloc<double>(quality_part_size(nt));
+    c->quality_out = A.alloc<double>(5);
+    c->quality_host_stale = false;
     // reduced system (FP64) and the block-Jacobi PCG buffers
     c->red.vals = A.alloc<double>(static_cast<size_t>(std::max(1, S.nnzb)) * 36);
     c->red.border = A.alloc<double>(static_cast<size_t>(std::max(1, S.ncb)) * 6 * std::max(1, S.nb));
@@ -675,39 +685,18 @@ void reset_state(pb_gpu_ctx* c) {
 void finalize_quality(pb_gpu_ctx* c, const pb_solve_options& op, pb_solve_report* rep) {
     const HostModel& m = c->model;
     const int nt = m.nt;
-    launch_strict_rms(c->S[0], c->D[0], c->D[0].cams_eff, c->init_points_all, c->proc_of_track, 1, nt, c->rms_after_d,
-                      c->stream);
-    c->launches += 1;
-    c->rms_after.assign(nt, 0.0);
-    check(cudaMemcpyAsync(c->rms_after.data(), c->rms_after_d, nt * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "D2H");
-    check(cudaStreamSynchronize(c->stream), "quality");
-    // finalizeBundleAdjustResult (BundleAdjustQuality.cpp:403-502)
-    c->valid.assign(nt, 0);
-    std::vector<double> cand;
-    for (int t = 0; t < nt; ++t) {
-        if (!m.active_track[t]) {
-            c->rms_after[t] = kInfD;
-            continue;
-        }
-        c->valid[t] = std::isfinite(c->rms_after[t]) ? 1 : 0;
-        if (c->valid[t]) cand.push_back(c->rms_after[t]);
-    }
-    double thr = kInfD;
-    if (op.enable_point_filter) {
-        thr = std::isfinite(op.filter_max_reproj_error) && op.filter_max_reproj_error >= 0 ? op.filter_max_reproj_error : 0.0;
-        if (!cand.empty() && std::isfinite(op.filter_sigma_factor) && op.filter_sigma_factor > 0.0)
-            thr = std::max(thr, op.filter_sigma_factor * finite_median(cand, 0.0));
-    }
-    double sb = 0.0, sa = 0.0;
-    int kept = 0;
-    for (int t = 0; t < nt; ++t) {
-        if (c->valid[t] && c->rms_after[t] > thr) c->valid[t] = 0;
-        if (c->valid[t]) {
-            ++kept;
-            sb += c->rms_before[t];
-            sa += c->rms_after[t];
-        }
-    }
+    cudaStream_t st = c->stream;
+    // finalizeBundleAdjustResult (BundleAdjustQuality.cpp:403-502): strict RMS, filter threshold,
+    // valid mask and means on the device; five numbers come back
+    launch_strict_rms(c->S[0], c->D[0], c->D[0].cams_eff, c->init_points_all, c->proc_of_track, 1, nt, c->rms_after_d, st);
+    launch_quality(nt, c->active_d, c->rms_before_d, c->rms_after_d, op.enable_point_filter, op.filter_max_reproj_error,
+                   op.filter_sigma_factor, c->valid_d, c->quality_part, c->quality_out, st);
+    c->launches += 4;
+    check(cudaMemcpyAsync(c->h_scratch, c->quality_out, 5 * sizeof(double), cudaMemcpyDeviceToHost, st), "D2H");
+    check(cudaStreamSynchronize(st), "quality");
+    c->quality_host_stale = true;
+    const double thr = c->h_scratch[0], kept_d = c->h_scratch[2], sb = c->h_scratch[3], sa = c->h_scratch[4];
+    const int kept = static_cast<int>(kept_d);
     rep->filter_threshold = thr;
     rep->optimized_tracks = kept;
     rep->mean_rms_before = kept ? sb / kept : kInfD;
@@ -717,6 +706,17 @@ void finalize_quality(pb_gpu_ctx* c, const pb_solve_options& op, pb_solve_report
         rep->status = PB_SOLVE_NUMERICAL_FAILURE;
         rep->solution_usable = 0;
     }
+}
+
+// The valid mask and strict RMS after the last solve, fetched from the device on first use.
+void fetch_quality(pb_gpu_ctx* c) {
+    if (!c->quality_host_stale) return;
+    const int nt = c->model.nt;
+    c->valid.assign(nt, 0);
+    c->rms_after.assign(nt, 0.0);
+    check(cudaMemcpy(c->valid.data(), c->valid_d, nt * sizeof(signed char), cudaMemcpyDeviceToHost), "D2H");
+    check(cudaMemcpy(c->rms_after.data(), c->rms_after_d, nt * sizeof(double), cudaMemcpyDeviceToHost), "D2H");
+    c->quality_host_stale = false;
 }
 
 int do_assemble(pb_gpu_ctx* c, double damping, int precision, double* cost, int* flags) {
@@ -1328,6 +1328,7 @@ pb_status pb_gpu_download_state(pb_gpu_ctx* c, double* cams, double* pts, int8_t
             for (size_t p = 0; p < m.trk_order.size(); ++p)
                 for (int a = 0; a < 3; ++a) pts[static_cast<size_t>(m.trk_order[p]) * 3 + a] = sp[p * 3 + a];
         }
+        if (valid || ra) fetch_quality(c);
         for (int t = 0; t < m.nt; ++t) {
             if (valid) valid[t] = c->solved && static_cast<size_t>(t) < c->valid.size() ? c->valid[t] : 0;
             if (rb) rb[t] = static_cast<size_t>(t) < c->rms_before.size() ? c->rms_before[t] : kNaN;
