@@ -58,16 +58,21 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const int MO = S.max_obs, MT = S.max_tracks;
     const int ng = S.ng, ni = S.ni, nb = S.nb, nA = 6 + ni;
+    // per-observation records are padded to an odd number of 4- or 8-byte words, so that the
+    // lanes of a warp reading the same field of consecutive observations hit distinct banks
+    const int sA = chunk_stride(2 * nA), sG = chunk_stride(18), sY = chunk_stride(6), sM = chunk_stride(6),
+              sD = chunk_stride(nA);
     char* ptr = smem;
     double* s_V = carve<double>(ptr, static_cast<size_t>(MO) * 9);
-    T* s_A = carve<T>(ptr, static_cast<size_t>(MO) * 2 * nA);
-    VT* s_G = carve<VT>(ptr, static_cast<size_t>(MO) * 18);
-    VT* s_Y = carve<VT>(ptr, static_cast<size_t>(MO) * 6);
-    VT* s_M = carve<VT>(ptr, static_cast<size_t>(MO) * 6);
-    VT* s_D = carve<VT>(ptr, static_cast<size_t>(MO) * nA);
+    T* s_A = carve<T>(ptr, static_cast<size_t>(MO) * sA);
+    VT* s_G = carve<VT>(ptr, static_cast<size_t>(MO) * sG);
+    VT* s_Y = carve<VT>(ptr, static_cast<size_t>(MO) * sY);
+    VT* s_M = carve<VT>(ptr, static_cast<size_t>(MO) * sM);
+    VT* s_D = carve<VT>(ptr, static_cast<size_t>(MO) * sD);
     int* s_info = carve<int>(ptr, MO);
     int* s_trk = carve<int>(ptr, MO);
-    VT* s_K = carve<VT>(ptr, static_cast<size_t>(MT) * nb * 3);
+    const int sK = chunk_stride(nb * 3);  // per-track K record (odd: lanes over tracks hit distinct banks)
+    VT* s_K = carve<VT>(ptr, static_cast<size_t>(MT) * sK);
     int* s_tfirst = carve<int>(ptr, MT + 1);
     int* s_tmask = carve<int>(ptr, MT);  // calibration groups present in each chunk track
     double* s_misc = carve<double>(ptr, 40);
@@ -106,7 +111,7 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
             cost = L.cost;
         }
         s_info[tid] = (ok ? kOk : 0) | (elim ? kElim : 0) | ((grp + 1) << 2);
-        T* A = s_A + static_cast<size_t>(tid) * 2 * nA;
+        T* A = s_A + static_cast<size_t>(tid) * sA;
         for (int a = 0; a < 6; ++a) {
             A[a] = ok ? L.Jc[a] : T(0);
             A[nA + a] = ok ? L.Jc[6 + a] : T(0);
@@ -116,7 +121,7 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
             A[nA + 6 + a] = ok ? L.Ji[kMaxNI + a] : T(0);
         }
         // the observation's gradient -J^T w r (FP64): pose and intrinsic columns
-        VT* Dg = s_D + static_cast<size_t>(tid) * nA;
+        VT* Dg = s_D + static_cast<size_t>(tid) * sD;
         for (int a = 0; a < 6; ++a) Dg[a] = ok ? Val::make(grad[a]) : Val::zero();
         for (int a = 0; a < ni; ++a) Dg[6 + a] = ok ? Val::make(grad[9 + a]) : Val::zero();
         double* V = s_V + static_cast<size_t>(tid) * 9;
@@ -224,9 +229,9 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
     // G = J_pose^T Y (values: float-float on the FP32 path; zero for tracks not eliminated)
     if (active) {
         if (!start) s_trk[tid] = s_trk[first];
-        VT* G = s_G + static_cast<size_t>(tid) * 18;
-        VT* Ys = s_Y + static_cast<size_t>(tid) * 6;
-        VT* Mo = s_M + static_cast<size_t>(tid) * 6;
+        VT* G = s_G + static_cast<size_t>(tid) * sG;
+        VT* Ys = s_Y + static_cast<size_t>(tid) * sY;
+        VT* Mo = s_M + static_cast<size_t>(tid) * sM;
         if (ok) {
             const double w = L.wd;
             double Y[2][3] = {{0, 0, 0}, {0, 0, 0}}, q[3] = {0, 0, 0};
@@ -252,7 +257,7 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
                 y[i] = Val::make(Y[i / 3][i % 3]);
                 Ys[i] = y[i];
             }
-            const T* A = s_A + static_cast<size_t>(tid) * 2 * nA;
+            const T* A = s_A + static_cast<size_t>(tid) * sA;
             // back-substitution record of the observation: A rows, then Y
             T* rec = O.obs_rec + static_cast<size_t>(o) * (2 * nA + 6);
             for (int i = 0; i < 2 * nA; ++i) rec[i] = A[i];
@@ -283,11 +288,11 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
             VT acc = Val::zero();
             for (int ob = s_tfirst[t]; ob < s_tfirst[t + 1]; ++ob) {
                 if (info_group(s_info[ob]) != g) continue;
-                const T* A = s_A + static_cast<size_t>(ob) * 2 * nA;
-                const VT* Y = s_Y + static_cast<size_t>(ob) * 6;
+                const T* A = s_A + static_cast<size_t>(ob) * sA;
+                const VT* Y = s_Y + static_cast<size_t>(ob) * sY;
                 acc = acc + (A[6 + c] * Y[kk] + A[nA + 6 + c] * Y[3 + kk]);
             }
-            s_K[it] = acc;
+            s_K[static_cast<size_t>(t) * sK + r] = acc;
         }
         __syncthreads();
     }
@@ -313,8 +318,8 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
                 const int oa = item & 0xFF, ob = item >> 8;
                 if (oa == ob) {
                     // own term: row x of J^T M J
-                    const T* A = s_A + static_cast<size_t>(oa) * 2 * nA;
-                    const VT* M = s_M + static_cast<size_t>(oa) * 6;
+                    const T* A = s_A + static_cast<size_t>(oa) * sA;
+                    const VT* M = s_M + static_cast<size_t>(oa) * sM;
                     const T ax0 = A[x], ax1 = A[nA + x];
                     const VT u0 = ax0 * M[0] + ax1 * M[1];
                     const VT u1 = ax0 * M[1] + ax1 * M[2];
@@ -324,8 +329,8 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
                         acc_fma(acc[y], A[nA + y], u1);
                     }
                 } else {
-                    const VT* Ga = s_G + static_cast<size_t>(oa) * 18 + 3 * x;
-                    const VT* Gb = s_G + static_cast<size_t>(ob) * 18;
+                    const VT* Ga = s_G + static_cast<size_t>(oa) * sG + 3 * x;
+                    const VT* Gb = s_G + static_cast<size_t>(ob) * sG;
                     const VT g0 = -Ga[0], g1 = -Ga[1], g2 = -Ga[2];
 #pragma unroll
                     for (int y = 0; y < 6; ++y) {
@@ -356,12 +361,12 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
                 // gradient -J_pose^T w r (the point term with the rounded Jacobian)
                 for (int it = b0; it < b1; ++it) {
                     const int ob = D.lcam_obs[it];
-                    const VT* Dg = s_D + static_cast<size_t>(ob) * nA;
+                    const VT* Dg = s_D + static_cast<size_t>(ob) * sD;
 #pragma unroll
                     for (int a = 0; a < 6; ++a) acc[a].add(Dg[a]);
                     if (row == 0) {
-                        const T* A = s_A + static_cast<size_t>(ob) * 2 * nA;
-                        const VT* M = s_M + static_cast<size_t>(ob) * 6;
+                        const T* A = s_A + static_cast<size_t>(ob) * sA;
+                        const VT* M = s_M + static_cast<size_t>(ob) * sM;
                         const VT m0 = -M[3], m1 = -M[4];
 #pragma unroll
                         for (int a = 0; a < 6; ++a) {
@@ -378,9 +383,9 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
                 for (int it = b0; it < b1; ++it) {
                     const int ob = D.lcam_obs[it];
                     const int info = s_info[ob];
-                    const T* A = s_A + static_cast<size_t>(ob) * 2 * nA;
+                    const T* A = s_A + static_cast<size_t>(ob) * sA;
                     if (info_group(info) == g) {
-                        const VT w = s_M[static_cast<size_t>(ob) * 6 + 5];
+                        const VT w = s_M[static_cast<size_t>(ob) * sM + 5];
                         const VT u0 = A[6 + c2] * w, u1 = A[nA + 6 + c2] * w;
 #pragma unroll
                         for (int a = 0; a < 6; ++a) {
@@ -390,9 +395,9 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
                     }
                     const int ts = trk_slot(s_trk[ob]);
                     if ((info & kElim) && ts < ntc && ((s_tmask[ts] >> g) & 1)) {
-                        const VT* Kt = s_K + (static_cast<size_t>(ts) * nb + gc) * 3;
+                        const VT* Kt = s_K + static_cast<size_t>(ts) * sK + gc * 3;
                         const VT k0 = -Kt[0], k1 = -Kt[1], k2 = -Kt[2];
-                        const VT* Go = s_G + static_cast<size_t>(ob) * 18;
+                        const VT* Go = s_G + static_cast<size_t>(ob) * sG;
 #pragma unroll
                         for (int a = 0; a < 6; ++a) {
                             acc_fma(acc[a], Go[3 * a], k0);
@@ -422,8 +427,8 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
                 if (g1 == g2) {
                     for (int ob = lane; ob < nobs; ob += 32) {
                         if (info_group(s_info[ob]) != g1) continue;
-                        const T* A = s_A + static_cast<size_t>(ob) * 2 * nA;
-                        const VT w = s_M[static_cast<size_t>(ob) * 6 + 5];
+                        const T* A = s_A + static_cast<size_t>(ob) * sA;
+                        const VT w = s_M[static_cast<size_t>(ob) * sM + 5];
                         acc_fma(acc, w, two_prod(A[6 + c1], A[6 + c2]));
                         acc_fma(acc, w, two_prod(A[nA + 6 + c1], A[nA + 6 + c2]));
                     }
@@ -431,8 +436,8 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
                 const int need = (1 << g1) | (1 << g2);
                 for (int t = lane; t < ntc; t += 32) {
                     if ((s_tmask[t] & need) != need) continue;
-                    const VT* K1 = s_K + (static_cast<size_t>(t) * nb + i) * 3;
-                    const VT* K2 = s_K + (static_cast<size_t>(t) * nb + j) * 3;
+                    const VT* K1 = s_K + static_cast<size_t>(t) * sK + i * 3;
+                    const VT* K2 = s_K + static_cast<size_t>(t) * sK + j * 3;
                     acc_fma(acc, -K1[0], K2[0]);
                     acc_fma(acc, -K1[1], K2[1]);
                     acc_fma(acc, -K1[2], K2[2]);
@@ -449,10 +454,10 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
                 const int g = col / ni, c = col - g * ni;
                 for (int ob = lane; ob < nobs; ob += 32) {
                     if (info_group(s_info[ob]) != g) continue;
-                    acc.add(s_D[static_cast<size_t>(ob) * nA + 6 + c]);
+                    acc.add(s_D[static_cast<size_t>(ob) * sD + 6 + c]);
                     if (reduced) {
-                        const T* A = s_A + static_cast<size_t>(ob) * 2 * nA;
-                        const VT* M = s_M + static_cast<size_t>(ob) * 6;
+                        const T* A = s_A + static_cast<size_t>(ob) * sA;
+                        const VT* M = s_M + static_cast<size_t>(ob) * sM;
                         acc_fma(acc, A[6 + c], -M[3]);
                         acc_fma(acc, A[nA + 6 + c], -M[4]);
                     }

@@ -479,14 +479,15 @@ size_t chunk_smem_bytes(int precision, int max_obs, int max_tracks, int ni, int 
     const size_t mo = static_cast<size_t>(max_obs), mt = static_cast<size_t>(max_tracks);
     auto al = [](size_t v) { return (v + 15) & ~static_cast<size_t>(15); };
     size_t s = 0;
-    s += al(mo * 9 * 8);        // point normal equations per observation, then the track factor (FP64)
-    s += al(mo * 2 * nA * ts);  // A_o = [J_pose | J_intrinsic]
-    s += al(mo * 18 * vs);      // G_o = J_pose^T Y_o
-    s += al(mo * 6 * vs);       // Y_o
-    s += al(mo * 6 * vs);       // M_o, Y_o q, w
-    s += al(mo * nA * vs);      // gradient -J^T w r of the pose and intrinsic columns
+    auto st = [](size_t words) { return static_cast<size_t>(chunk_stride(static_cast<int>(words))); };
+    s += al(mo * 9 * 8);            // point normal equations per observation, then the track factor (FP64)
+    s += al(mo * st(2 * nA) * ts);  // A_o = [J_pose | J_intrinsic]
+    s += al(mo * st(18) * vs);      // G_o = J_pose^T Y_o
+    s += al(mo * st(6) * vs);       // Y_o
+    s += al(mo * st(6) * vs);       // M_o, Y_o q, w
+    s += al(mo * st(nA) * vs);      // gradient -J^T w r of the pose and intrinsic columns
     s += al(mo * 4) * 2;        // observation flags, track records
-    s += al(mt * static_cast<size_t>(nb) * 3 * vs);  // per-track K
+    s += al(mt * st(static_cast<size_t>(nb) * 3) * vs);  // per-track K
     s += al((mt + 1) * 4);      // track starts
     s += al(mt * 4);            // calibration groups present per track
     s += al(40 * 8);            // warp partial costs and track counts, flags

@@ -147,6 +147,15 @@ struct HostModel {
     long long structure_hash = 0;
 };
 
+// Per-observation record stride of the assembly's shared-memory arrays: the field count rounded
+// up to an odd number of words (bank-conflict-free strided access by the lanes of a warp).
+#if defined(__CUDACC__)
+#define PB_HOST_DEVICE __host__ __device__
+#else
+#define PB_HOST_DEVICE
+#endif
+inline PB_HOST_DEVICE int chunk_stride(int words) { return words | 1; }
+
 // pb_host.cpp
 int build_host_model(const pb_problem_desc* pr, const pb_solve_options* op, HostModel* m, std::string* err);
 int build_chunks(HostModel* m, int precision, size_t smem_budget, std::string* err);
