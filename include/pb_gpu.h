@@ -91,6 +91,14 @@ typedef struct pb_problem_desc {
     const int32_t* fixed_tracks;
     const int32_t* calibration_group_ids;      /* n_cameras or NULL: Problem::cameraCalibrationGroupIds */
     const double* intrinsic_reference_cameras; /* n_cameras * 32 or NULL */
+    /* Control-point constraints of the tracks (Track::controlPointConstraints,
+     * ControlPointConstraint, include/plabundle/constraints.h:73-87, :127-133): n_control_points
+     * entries; control_point_track[i] the track index; control_point_data[15 * i]: target point (3),
+     * sigmaMeters, weight, uncertainty (0 isotropic sigma, 1 covariance, 2 square-root
+     * information), uncertaintyMatrix (9, row-major).  May be 0 / NULL. */
+    int32_t n_control_points;
+    const int32_t* control_point_track;
+    const double* control_point_data;
 } pb_problem_desc;
 
 /* SolveOptions (include/plabundle/options.h:58-187) as flat fields. */
@@ -118,6 +126,8 @@ typedef struct pb_solve_options {
     int32_t preconditioner_cluster_size; /* BackendOptions::plaMatrixPreconditionerClusterSize (1) */
     int32_t linear_solver;             /* 0 auto, 1 dense-Cholesky-preconditioned CG, 2 block-Jacobi PCG */
     double calibration[32];            /* CalibrationOptions numeric fields (27 used) */
+    double control_point_weight;       /* ConstraintOptions::controlPointWeight (1) */
+    double control_point_huber_delta;  /* ConstraintOptions::controlPointHuberDeltaMeters (0.2) */
 } pb_solve_options;
 
 /* PlaMatrixDiagnostics (include/plabundle/result.h:91-128) + QualitySummary fields. */

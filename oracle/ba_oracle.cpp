@@ -16,6 +16,7 @@
 #include <cstring>
 #include <limits>
 #include <memory>
+#include <set>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -314,8 +315,18 @@ struct Oracle {
     double lastCost = 0.0;
     bool lastSingular = false;
 
+    // control points: per track, the linearisable constraints as J = sqrt(weight) W and target P
+    struct ControlPoint {
+        double J[9];
+        double P[3];
+    };
+    std::vector<std::vector<ControlPoint>> controlPoints;
+    std::vector<std::array<double, 3>> gaugeTargets;  // valid targets of tracks with usable observations
+    bool hasControlPoints = false;
+
     size_t nt() const { return offs.size() - 1; }
-    bool refParam() const { return true; }
+    // useReferencePointParameterization (BundleAdjustPlaMatrixAssembly.cpp:24-30)
+    bool refParam() const { return !hasControlPoints; }
 };
 
 bool isCameraFixed(const Oracle& o, int cam) {
@@ -323,8 +334,160 @@ bool isCameraFixed(const Oracle& o, int cam) {
 }
 bool isTrackFixed(const Oracle& o, int t) { return std::binary_search(o.fixedTracks.begin(), o.fixedTracks.end(), t); }
 
-// Gauge normalisation for image-only problems: validateAndNormalizeBundleAdjustOptions
-// (BundleAdjustValidation.cpp:772-893) with no pose priors, control points or scale bars.
+// Cholesky factor of a 3x3 covariance / information matrix with the checks of
+// control_point.cpp:34-85 (finite; symmetric to 1e-10 max(1, running max|a|); pivots L_jj^2
+// above 1e-12 max(1, max|a|)).
+bool controlPointCholesky(const double* a, double L[3][3]) {
+    double mx = 0.0;
+    for (int i = 0; i < 9; ++i) {
+        const int r = i / 3, c = i % 3;
+        const double v = a[r * 3 + c], t = a[c * 3 + r];
+        if (!std::isfinite(v) || !std::isfinite(t)) return false;
+        mx = std::max({mx, std::fabs(v), std::fabs(t)});
+        if (std::fabs(v - t) > 1.0e-10 * std::max(1.0, mx)) return false;
+    }
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) L[r][c] = 0.0;
+    for (int c = 0; c < 3; ++c) {
+        for (int r = c; r < 3; ++r) {
+            double v = a[r * 3 + c];
+            for (int k = 0; k < c; ++k) v -= L[r][k] * L[c][k];
+            if (r == c) {
+                if (!(v > 0.0)) return false;
+                L[c][c] = std::sqrt(v);
+            } else {
+                L[r][c] = v / L[c][c];
+            }
+        }
+    }
+    const double threshold = std::max(1.0, mx) * 1.0e-12;
+    for (int d = 0; d < 3; ++d)
+        if (!(L[d][d] * L[d][d] > threshold) || !std::isfinite(L[d][d] * L[d][d])) return false;
+    return true;
+}
+
+// makeControlPointWhitening (control_point.cpp:91-165) and validateControlPointConstraint
+// (:205-220): the whitening W with W^T W the information of the target.  rec: target (3),
+// sigma, weight, kind, matrix (9).
+bool controlPointWhitening(const double* rec, double W[9]) {
+    for (int a = 0; a < 3; ++a)
+        if (!std::isfinite(rec[a])) return false;
+    if (!std::isfinite(rec[4]) || rec[4] <= 0.0) return false;
+    const int kind = static_cast<int>(rec[5]);
+    const double* m = rec + 6;
+    std::fill(W, W + 9, 0.0);
+    if (kind == 0) {
+        if (!std::isfinite(rec[3]) || rec[3] <= 0.0) return false;
+        W[0] = W[4] = W[8] = 1.0 / rec[3];
+        return true;
+    }
+    double L[3][3];
+    if (kind == 1) {
+        if (!controlPointCholesky(m, L)) return false;
+        // W = L^-1 column by column (forward substitution of L w = e_c)
+        for (int c = 0; c < 3; ++c)
+            for (int r = 0; r < 3; ++r) {
+                double v = r == c ? 1.0 : 0.0;
+                for (int k = 0; k < r; ++k) v -= L[r][k] * W[k * 3 + c];
+                W[r * 3 + c] = v / L[r][r];
+            }
+        return true;
+    }
+    if (kind == 2) {
+        for (int i = 0; i < 9; ++i)
+            if (!std::isfinite(m[i])) return false;
+        double info[9];
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) info[r * 3 + c] = m[r] * m[c] + m[3 + r] * m[3 + c] + m[6 + r] * m[6 + c];
+        if (!controlPointCholesky(info, L)) return false;
+        std::copy(m, m + 9, W);
+        return true;
+    }
+    return false;
+}
+
+// Control points of the problem: Problem validation rejects an invalid constraint
+// (problem.cpp:253-260); linearizeControlPoint (BundleAdjustPlaMatrixConstraints.cpp:90-116)
+// skips one whose weight controlPointWeight * weight is not positive.  The gauge targets are the
+// valid constraints of tracks seen by two distinct cameras (BundleAdjustValidation.cpp:94-106,
+// :147-236).
+int loadControlPoints(Oracle& o, const orc_problem* pr) {
+    o.controlPoints.assign(o.nt(), {});
+    o.gaugeTargets.clear();
+    o.hasControlPoints = pr->n_control_points > 0;
+    if (!o.hasControlPoints) return 0;
+    if (!pr->control_point_track || !pr->control_point_data) return InvalidInput;
+    const double cw = o.opt.control_point_weight;
+    if (!std::isfinite(cw) || cw < 0.0 || !std::isfinite(o.opt.control_point_huber_delta) ||
+        o.opt.control_point_huber_delta <= 0.0)
+        return InvalidInput;
+    for (int i = 0; i < pr->n_control_points; ++i) {
+        const int t = pr->control_point_track[i];
+        if (t < 0 || t >= static_cast<int>(o.nt())) return InvalidInput;
+        const double* rec = pr->control_point_data + static_cast<size_t>(i) * 15;
+        double W[9];
+        if (!controlPointWhitening(rec, W)) return InvalidInput;
+        std::set<int> cams;
+        for (int64_t k = o.offs[t]; k < o.offs[t + 1]; ++k) {
+            const Obs& ob = o.obs[k];
+            if (ob.cam >= 0 && std::isfinite(ob.u) && std::isfinite(ob.v) && std::isfinite(ob.w) && ob.w > 0.0)
+                cams.insert(ob.cam);
+        }
+        if (cams.size() >= 2) o.gaugeTargets.push_back({rec[0], rec[1], rec[2]});
+        const double weight = cw * rec[4];
+        if (!(weight > 0.0)) continue;
+        Oracle::ControlPoint cp;
+        const double sw = std::sqrt(weight);
+        for (int k = 0; k < 9; ++k) cp.J[k] = sw * W[k];
+        for (int a = 0; a < 3; ++a) cp.P[a] = rec[a];
+        o.controlPoints[t].push_back(cp);
+    }
+    return 0;
+}
+
+// linearizeControlPoint + finishRobust (BundleAdjustPlaMatrixConstraints.cpp:17-29, :90-116):
+// r = J (X - P), Huber of |r|^2 with the control-point delta.  False when not finite (skipped).
+bool controlPointResidual(const Oracle& o, const Oracle::ControlPoint& cp, const double* X, double r[3],
+                          RobustEval* rb) {
+    const double d[3] = {X[0] - cp.P[0], X[1] - cp.P[1], X[2] - cp.P[2]};
+    for (int a = 0; a < 3; ++a) r[a] = cp.J[a * 3] * d[0] + cp.J[a * 3 + 1] * d[1] + cp.J[a * 3 + 2] * d[2];
+    if (!robustLoss(r[0] * r[0] + r[1] * r[1] + r[2] * r[2], 1, o.opt.control_point_huber_delta, rb)) return false;
+    return std::isfinite(rb->cost) && std::isfinite(rb->weight);
+}
+
+// hasCompleteControlPointGauge (BundleAdjustValidation.cpp:181-236): three targets, pairwise
+// apart, not collinear.
+bool completeControlPointGauge(const Oracle& o) {
+    const auto& p = o.gaugeTargets;
+    for (size_t i = 0; i < p.size(); ++i)
+        for (size_t j = i + 1; j < p.size(); ++j) {
+            const double u[3] = {p[j][0] - p[i][0], p[j][1] - p[i][1], p[j][2] - p[i][2]};
+            const double uu = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
+            if (uu <= 1.0e-16) continue;
+            for (size_t k = j + 1; k < p.size(); ++k) {
+                const double v[3] = {p[k][0] - p[i][0], p[k][1] - p[i][1], p[k][2] - p[i][2]};
+                const double vv = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+                const double x[3] = {u[1] * v[2] - u[2] * v[1], u[2] * v[0] - u[0] * v[2], u[0] * v[1] - u[1] * v[0]};
+                if (vv > 1.0e-16 && x[0] * x[0] + x[1] * x[1] + x[2] * x[2] > 1.0e-12 * uu * vv) return true;
+            }
+        }
+    return false;
+}
+
+// hasControlPointBaselineToFixedCamera (BundleAdjustValidation.cpp:147-179).
+bool controlPointBaseline(const Oracle& o, const std::vector<int>& fixedSet) {
+    for (const auto& t : o.gaugeTargets)
+        for (int f : fixedSet) {
+            const double* c = o.inputCams[f].C;
+            if (!std::isfinite(c[0]) || !std::isfinite(c[1]) || !std::isfinite(c[2])) continue;
+            const double d2 = (t[0] - c[0]) * (t[0] - c[0]) + (t[1] - c[1]) * (t[1] - c[1]) + (t[2] - c[2]) * (t[2] - c[2]);
+            if (d2 > 1.0e-16) return true;
+        }
+    return false;
+}
+
+// Gauge normalisation: validateAndNormalizeBundleAdjustOptions
+// (BundleAdjustValidation.cpp:772-893) with control points and no pose priors or scale bars.
 int normalizeGauge(Oracle& o) {
     const auto& opt = o.opt;
     std::vector<int> sorted = o.fixedCams;
@@ -349,12 +512,19 @@ int normalizeGauge(Oracle& o) {
     }
     if (!opt.refine_camera_pose || opt.gauge_policy == 2 || o.inputCams.empty()) return 0;
     std::vector<int> fixedSet = sorted;
-    if (opt.gauge_policy == 1) return fixedSet.size() >= 2 ? 0 : Unsupported;
+    const bool absolutePose = completeControlPointGauge(o);
+    bool absoluteScale = absolutePose || controlPointBaseline(o, fixedSet);
+    if (opt.gauge_policy == 1)
+        return (absolutePose && absoluteScale) || fixedSet.size() >= 2 || (fixedSet.size() == 1 && absoluteScale)
+                   ? 0
+                   : Unsupported;
+    if (absolutePose && absoluteScale) return 0;
     if (fixedSet.empty()) {
         o.fixedCams.push_back(0);
         fixedSet.push_back(0);
+        absoluteScale = absoluteScale || controlPointBaseline(o, fixedSet);
     }
-    if (fixedSet.size() < 2) {
+    if (!absoluteScale && fixedSet.size() < 2) {
         const int anchor = *std::min_element(fixedSet.begin(), fixedSet.end());
         const double* a = o.inputCams[anchor].C;
         int best = -1;
@@ -917,6 +1087,21 @@ void build(Oracle& o, double damping, double* costOut, bool* singularOut) {
                     accumulateDirect(tm, L, acc);
                     if (elim) accumulatePoint(tm, L, pw);
                 }
+                // control points (linearizeTrack, BundleAdjustPlaMatrixReferenceSchur.cpp:331-346) and
+                // accumulatePointOnlyConstraint (:241-260)
+                for (const auto& cp : o.controlPoints[t]) {
+                    double r[3];
+                    RobustEval rb;
+                    if (!controlPointResidual(o, cp, o.state.points[t].data(), r, &rb)) continue;
+                    cost += rb.cost;
+                    if (!elim) continue;
+                    for (int c = 0; c < kE; ++c)
+                        for (int row = 0; row < 3; ++row) {
+                            const double jv = cp.J[row * 3 + c];
+                            pw.rhs[c] -= rb.weight * jv * r[row];
+                            for (int oth = 0; oth < kE; ++oth) pw.V[c * kE + oth] += rb.weight * jv * cp.J[row * 3 + oth];
+                        }
+                }
                 if (elim && !eliminatePoint(damping, pw, acc, &o.backSub[t])) pSingular[th] = 1;
             }
             pCost[th] = cost;
@@ -1200,6 +1385,36 @@ void applyPoseStep(Camera& cam, const double* d) {
     cam.C[2] += d[5];
 }
 
+// The plain parameterisation's pose delta (CameraState::applyDeltaPose,
+// BundleAdjustPlaMatrixAssembly.cpp:1134-1136).  The camera library that defines it is not part
+// of the reference tree; its first-order form is fixed by the plain rotation columns
+// Jw x (X - C) (BundleAdjustPlaMatrixProjection.cpp:208-214), a world-frame rotation vector
+// left-multiplied on camera-to-world.  Restated as C2W' = Exp(w) C2W with the exponential summed
+// as a power series of the skew matrix (to 1e-20 relative), and C' = C + dC.
+void applyPlainPoseStep(Camera& cam, const double* d) {
+    const double K[9] = {0.0, -d[2], d[1], d[2], 0.0, -d[0], -d[1], d[0], 0.0};
+    double E[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1}, term[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+    for (int n = 1; n < 60; ++n) {
+        double nt[9];
+        double mx = 0.0;
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) {
+                double v = 0.0;
+                for (int k = 0; k < 3; ++k) v += term[r * 3 + k] * K[k * 3 + c];
+                nt[r * 3 + c] = v / n;
+                mx = std::max(mx, std::fabs(nt[r * 3 + c]));
+            }
+        std::memcpy(term, nt, sizeof(term));
+        for (int i = 0; i < 9; ++i) E[i] += term[i];
+        if (mx < 1e-20) break;
+    }
+    double R[9];
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) R[r * 3 + c] = E[r * 3] * cam.R[c] + E[r * 3 + 1] * cam.R[3 + c] + E[r * 3 + 2] * cam.R[6 + c];
+    std::memcpy(cam.R, R, sizeof(R));
+    for (int a = 0; a < 3; ++a) cam.C[a] += d[3 + a];
+}
+
 // applyReferenceGaugeTangentStep (BundleAdjustPlaMatrixAssembly.cpp:101-128).
 std::array<double, 3> gaugeTangentStep(const Oracle& o, const State& s, double a, double b) {
     const auto origin = targetCoords(s.cams[o.gaugeAnchor].C);
@@ -1217,17 +1432,21 @@ std::array<double, 3> gaugeTangentStep(const Oracle& o, const State& s, double a
     return targetCoords(out);
 }
 
-// applyStep (BundleAdjustPlaMatrixAssembly.cpp:1111-1247) with the reference point
-// parameterisation, applyIntrinsicStep (BundleAdjustPlaMatrixModel.cpp:248-269).
+// applyStep (BundleAdjustPlaMatrixAssembly.cpp:1111-1247) in the reference point
+// parameterisation or the plain one (control points), applyIntrinsicStep
+// (BundleAdjustPlaMatrixModel.cpp:248-269).
 State applyStep(const Oracle& o, const State& s, const std::vector<double>& ps, const std::vector<double>& es,
                 double alpha) {
     State n = s;
+    const bool ref = o.refParam();
     for (size_t c = 0; c < n.cams.size(); ++c) {
         const int b = o.active.cameraBlock[c];
         if (b < 0) continue;
         double d[6];
         for (int i = 0; i < 6; ++i) d[i] = alpha * ps[static_cast<size_t>(b) * kP + i];
-        if (usesGaugeTangent(o, c)) {
+        if (!ref) {
+            applyPlainPoseStep(n.cams[c], d);
+        } else if (usesGaugeTangent(o, c)) {
             const auto centre = gaugeTangentStep(o, n, d[3], d[4]);
             const double rd[6] = {d[0], d[1], d[2], 0, 0, 0};
             applyPoseStep(n.cams[c], rd);
@@ -1247,14 +1466,14 @@ State applyStep(const Oracle& o, const State& s, const std::vector<double>& ps, 
     for (size_t t = 0; t < n.points.size(); ++t) {
         const int eb = o.active.trackBlock[t];
         if (eb < 0) continue;
-        const double sc = referencePointScale(s.points[t].data());
+        const double sc = ref ? referencePointScale(s.points[t].data()) : 1.0;
         for (int a = 0; a < 3; ++a) n.points[t][a] += sc * alpha * es[static_cast<size_t>(eb) * 3 + a];
     }
     return n;
 }
 
-// evaluateObjective (BundleAdjustPlaMatrixAssembly.cpp:1010-1019): image costs of the active
-// tracks plus intrinsic priors; an invalid projection makes the cost +inf
+// evaluateObjective (BundleAdjustPlaMatrixAssembly.cpp:1010-1019): image and control-point
+// costs of the active tracks (:674-690) plus intrinsic priors; an invalid projection makes the cost +inf
 // (BundleAdjustPlaMatrix.cpp:42-58).
 double objective(const Oracle& o, const State& s) {
     const int T = std::max(1, std::min<int>(o.threads, static_cast<int>(o.nt())));
@@ -1282,6 +1501,12 @@ double objective(const Oracle& o, const State& s) {
                     break;
                 }
                 cost += rb.cost;
+            }
+            if (bad[th]) break;
+            for (const auto& cp : o.controlPoints[t]) {
+                double r[3];
+                RobustEval rb;
+                if (controlPointResidual(o, cp, s.points[t].data(), r, &rb)) cost += rb.cost;
             }
         }
         part[th] = cost;
@@ -1375,6 +1600,7 @@ void* orc_create(const orc_problem* pr, const orc_options* op, int32_t* status) 
 #endif
     int st = 0;
     if (o->inputCams.empty() || o->nt() == 0) st = InvalidInput;
+    if (!st) st = loadControlPoints(*o, pr);
     if (!st) st = normalizeGauge(*o);
     if (!st) {
         prepareActive(*o);
@@ -1389,6 +1615,8 @@ void* orc_create(const orc_problem* pr, const orc_options* op, int32_t* status) 
 
 void orc_destroy(void* h) { delete static_cast<Oracle*>(h); }
 
+int32_t orc_control_point_whitening(const double* record, double* W) { return controlPointWhitening(record, W) ? 1 : 0; }
+
 int32_t orc_info(void* h, int32_t* counts, double* baseline) {
     auto* o = static_cast<Oracle*>(h);
     counts[0] = o->active.primaryBlockCount;
@@ -1401,6 +1629,9 @@ int32_t orc_info(void* h, int32_t* counts, double* baseline) {
     counts[7] = static_cast<int32_t>(o->pairs.size());
     counts[8] = o->gaugeAnchor;
     counts[9] = o->gaugeScale;
+    counts[10] = static_cast<int32_t>(o->fixedCams.size());
+    counts[11] = o->fixedCams.empty() ? -1 : o->fixedCams.front();
+    counts[12] = o->refParam() ? 1 : 0;
     *baseline = o->gaugeBaseline;
     return 0;
 }
@@ -1429,7 +1660,7 @@ int32_t orc_linearize_observations(void* h, double* res, double* jp, double* jpo
             const Camera cam = effectiveCamera(*o, o->state, ob.cam);
             Lin L;
             if (!linearize(cam, activeIntrinsics(*o, ob.cam), o->state.points[t].data(), ob, o->opt.robust_loss,
-                           o->opt.robust_loss_scale, true, &L))
+                           o->opt.robust_loss_scale, o->refParam(), &L))
                 continue;
             valid[k] = 1;
             std::memcpy(res + 2 * k, L.r, sizeof(L.r));
@@ -1845,6 +2076,7 @@ int32_t orc_set_state(void* h, const double* cams, const double* pts, const doub
 int32_t orc_adjoint_layout(void* h, int64_t* n_vars, int8_t* kind, double* geom) {
     using namespace orc;
     auto* o = static_cast<Oracle*>(h);
+    if (!o->refParam()) return 2;  // the adjoint charts are those of image-only problems
     const int64_t nc = static_cast<int64_t>(o->state.cams.size()), nt = static_cast<int64_t>(o->nt());
     const int64_t ng = static_cast<int64_t>(o->state.groups.size()), no = static_cast<int64_t>(o->obs.size());
     const int64_t base_g = 6 * nc + 3 * nt, id_b = base_g + kP * ng, base_o = id_b + 1;
@@ -1910,6 +2142,7 @@ int32_t orc_adjoint_local(void* h, const double* z0, int64_t* count, int32_t* id
                           double* hess, double* prior) {
     using namespace orc;
     auto* o = static_cast<Oracle*>(h);
+    if (!o->refParam()) return 2;  // the adjoint charts are those of image-only problems
     const int64_t nc = static_cast<int64_t>(o->state.cams.size()), nt = static_cast<int64_t>(o->nt());
     const int64_t ng = static_cast<int64_t>(o->state.groups.size());
     const int64_t base_g = 6 * nc + 3 * nt, id_b = base_g + kP * ng, base_o = id_b + 1;

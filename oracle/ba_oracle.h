@@ -49,6 +49,12 @@ typedef struct orc_problem {
     const int32_t* fixed_tracks;
     const int32_t* calibration_group_ids; /* n_cameras or NULL */
     const double* intrinsic_reference_cameras; /* n_cameras * 32 or NULL */
+    /* control points (Track::controlPointConstraints): track index and 15 doubles each --
+     * target (3), sigmaMeters, weight, uncertainty kind (0 sigma, 1 covariance, 2 sqrt
+     * information), matrix (9, row-major) */
+    int32_t n_control_points;
+    const int32_t* control_point_track;
+    const double* control_point_data;
 } orc_problem;
 
 typedef struct orc_options {
@@ -73,6 +79,8 @@ typedef struct orc_options {
     double linear_relative_tolerance;
     double linear_absolute_tolerance;
     double calibration[32];         /* CalibrationOptions numeric fields, see ORC_CAL_* */
+    double control_point_weight;    /* ConstraintOptions::controlPointWeight */
+    double control_point_huber_delta; /* ConstraintOptions::controlPointHuberDeltaMeters */
 } orc_options;
 
 typedef struct orc_report {
@@ -101,9 +109,13 @@ typedef struct orc_report {
 
 void* orc_create(const orc_problem* problem, const orc_options* options, int32_t* status);
 void orc_destroy(void* handle);
+/* validateControlPointConstraint + makeControlPointWhitening of one 15-double control-point
+ * record: 1 and the whitening W (row-major 3x3) when valid, else 0. */
+int32_t orc_control_point_whitening(const double* record, double* W);
 /* counts: [primary, camera_blocks, intrinsic_blocks, track_blocks, active_tracks,
  *          observation_count, rejected_initial_tracks, n_pairs(after first build),
- *          gauge_anchor, gauge_scale] */
+ *          gauge_anchor, gauge_scale, fixed_cameras, first fixed camera (-1: none),
+ *          reference point parameterisation (1) or plain (0)] */
 int32_t orc_info(void* handle, int32_t* counts, double* gauge_baseline);
 int32_t orc_active(void* handle, int8_t* active_track, int32_t* camera_block, int32_t* intrinsic_block,
                    int32_t* track_block);

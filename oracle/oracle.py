@@ -25,7 +25,9 @@ class OrcProblem(C.Structure):
                 ("obs_camera", C.c_void_p), ("obs_u", C.c_void_p), ("obs_v", C.c_void_p),
                 ("obs_weight", C.c_void_p), ("obs_scale", C.c_void_p), ("n_fixed_cameras", C.c_int32),
                 ("fixed_cameras", C.c_void_p), ("n_fixed_tracks", C.c_int32), ("fixed_tracks", C.c_void_p),
-                ("calibration_group_ids", C.c_void_p), ("intrinsic_reference_cameras", C.c_void_p)]
+                ("calibration_group_ids", C.c_void_p), ("intrinsic_reference_cameras", C.c_void_p),
+                ("n_control_points", C.c_int32), ("control_point_track", C.c_void_p),
+                ("control_point_data", C.c_void_p)]
 
 
 class OrcOptions(C.Structure):
@@ -38,7 +40,8 @@ class OrcOptions(C.Structure):
                 ("gauge_baseline", C.c_double), ("intrinsic_mask", C.c_uint32), ("num_threads", C.c_int32),
                 ("linear_solver", C.c_int32), ("max_linear_iterations", C.c_int32),
                 ("linear_relative_tolerance", C.c_double), ("linear_absolute_tolerance", C.c_double),
-                ("calibration", C.c_double * 32)]
+                ("calibration", C.c_double * 32), ("control_point_weight", C.c_double),
+                ("control_point_huber_delta", C.c_double)]
 
 
 class OrcReport(C.Structure):
@@ -79,6 +82,8 @@ def lib():
         L.orc_cost.restype = C.c_double
         L.orc_cost.argtypes = [C.c_void_p]
         L.orc_solve.argtypes = [C.c_void_p, C.POINTER(OrcReport)] + [C.c_void_p] * 6
+        L.orc_control_point_whitening.argtypes = [C.c_void_p, C.c_void_p]
+        L.orc_control_point_whitening.restype = C.c_int32
         _lib = L
     return _lib
 
@@ -109,7 +114,25 @@ def make_options(options, num_threads: int = 0, linear_solver: int = 0) -> OrcOp
     o.linear_absolute_tolerance = 1.0e-12
     for i, v in enumerate(cal.numeric_block()):
         o.calibration[i] = v
+    o.control_point_weight = options.constraints.controlPointWeight
+    o.control_point_huber_delta = options.constraints.controlPointHuberDeltaMeters
     return o
+
+
+def control_point_whitening(record):
+    """(valid, W 3x3) of one ControlPointConstraint record (15 doubles)."""
+    rec = np.ascontiguousarray(record, np.float64)
+    W = np.zeros(9)
+    ok = lib().orc_control_point_whitening(rec.ctypes.data, W.ctypes.data)
+    return bool(ok), W.reshape(3, 3)
+
+
+def control_points(problem):
+    """(track int32 [n], records float64 [n, 15]) of Problem.controlPoints."""
+    cps = getattr(problem, "controlPoints", None) or []
+    track = np.ascontiguousarray([t for t, _ in cps], np.int32)
+    data = np.ascontiguousarray(np.array([c.record() for _, c in cps], np.float64).reshape(-1, 15))
+    return track, data
 
 
 class Oracle:
@@ -121,11 +144,13 @@ class Oracle:
                       p.obs_scale]
         fixed_c = np.ascontiguousarray(p.fixedCameraIndices, np.int32)
         fixed_t = np.ascontiguousarray(p.fixedTrackIndices, np.int32)
-        self._keep += [fixed_c, fixed_t, p.cameraCalibrationGroupIds, p.sharedIntrinsicReferenceCameras]
+        cp_t, cp_d = control_points(p)
+        self._keep += [fixed_c, fixed_t, p.cameraCalibrationGroupIds, p.sharedIntrinsicReferenceCameras, cp_t, cp_d]
         self.desc = OrcProblem(p.n_cameras, _ptr(p.cameras), p.n_tracks, _ptr(p.track_offsets), _ptr(p.points),
                                p.n_obs, _ptr(p.obs_camera), _ptr(p.obs_u), _ptr(p.obs_v), _ptr(p.obs_weight),
                                _ptr(p.obs_scale), fixed_c.size, _ptr(fixed_c), fixed_t.size, _ptr(fixed_t),
-                               _ptr(p.cameraCalibrationGroupIds), _ptr(p.sharedIntrinsicReferenceCameras))
+                               _ptr(p.cameraCalibrationGroupIds), _ptr(p.sharedIntrinsicReferenceCameras),
+                               cp_t.size, _ptr(cp_t) if cp_t.size else None, _ptr(cp_d) if cp_t.size else None)
         self.opts = make_options(options, num_threads, linear_solver)
         g = p.gauge
         self.opts.gauge_policy = int(g.policy)
@@ -152,7 +177,8 @@ class Oracle:
         base = C.c_double(0)
         lib().orc_info(self.h, _ptr(counts), C.byref(base))
         keys = ["primary", "camera_blocks", "intrinsic_blocks", "track_blocks", "active_tracks",
-                "observation_count", "rejected_initial_tracks", "n_pairs", "gauge_anchor", "gauge_scale"]
+                "observation_count", "rejected_initial_tracks", "n_pairs", "gauge_anchor", "gauge_scale",
+                "fixed_cameras", "first_fixed_camera", "ref_param"]
         d = {k: int(v) for k, v in zip(keys, counts)}
         d["gauge_baseline"] = base.value
         return d

@@ -154,7 +154,7 @@ __device__ bool adj_obs_hessian(const DCam& c, const double* X, double s, double
                                 double lscale, bool tangent, const double* gb, const double* nvec, double baseline,
                                 int ni, const int* cols, const AdjLayout& Lo, double* rec) {
     Lin<double> L;
-    if (!linearize_obs<double>(c, X[0], X[1], X[2], s, u, v, wobs, loss, lscale, tangent, gb, ni, cols, true, L))
+    if (!linearize_obs<double>(c, X[0], X[1], X[2], s, u, v, wobs, loss, lscale, tangent, false, gb, ni, cols, true, L))
         return false;
     const double r0 = L.rd0, r1 = L.rd1;
     double d1, d2;

@@ -75,6 +75,7 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
     VT* s_K = carve<VT>(ptr, static_cast<size_t>(MT) * sK);
     int* s_tfirst = carve<int>(ptr, MT + 1);
     int* s_tmask = carve<int>(ptr, MT);  // calibration groups present in each chunk track
+    double* s_cpc = carve<double>(ptr, MT);  // control-point cost of each chunk track
     double* s_misc = carve<double>(ptr, 40);
     int* s_flags = reinterpret_cast<int*>(s_misc + 32);
     int* s_wcount = reinterpret_cast<int*>(s_misc + 34);
@@ -104,7 +105,7 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
         const double* X = D.points + static_cast<size_t>(trk) * 3;
         const bool tangent = cam == S.gauge_scale && S.gauge_anchor >= 0 && S.gauge_baseline > 0.0;
         ok = linearize_obs<T>(c, X[0], X[1], X[2], D.pscale[trk], D.obs_u[o], D.obs_v[o], D.obs_w[o], S.loss,
-                              S.loss_scale, tangent, D.gauge_basis, ni, S.int_cols, true, L, grad);
+                              S.loss_scale, tangent, !S.ref_param, D.gauge_basis, ni, S.int_cols, true, L, grad);
         if (!ok) {
             atomicOr(s_flags, 2);
         } else {
@@ -177,8 +178,30 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
         }
     }
     if (tid == 0 && ntc <= MT) s_tfirst[ntc] = nobs;
+    // control points of the track (linearizeTrack, BundleAdjustPlaMatrixReferenceSchur.cpp:331-346):
+    // their cost always, their point terms when the point is eliminated
+    double cpV[6] = {0, 0, 0, 0, 0, 0}, cpg[3] = {0, 0, 0};
+    if (start && S.ncp > 0) {
+        const int trk = D.obs_trk[o];
+        const double* X = D.points + static_cast<size_t>(trk) * 3;
+        double cc_sum = 0.0;
+        for (int q = D.trk_cp_begin[trk]; q < D.trk_cp_begin[trk + 1]; ++q) {
+            const double* rec = D.cp_rec + static_cast<size_t>(q) * 12;
+            double r[3], cc, cw;
+            if (!cp_eval(rec, X[0], X[1], X[2], S.cp_huber, r, cc, cw)) continue;  // not finite: skipped
+            cc_sum += cc;
+            // accumulatePointOnlyConstraint (:241-260): V += w J^T J, g -= w J^T r, J = sqrt(weight) W
+            int e = 0;
+            for (int a = 0; a < 3; ++a) {
+                for (int b = a; b < 3; ++b)
+                    cpV[e++] += cw * (rec[a] * rec[b] + rec[3 + a] * rec[3 + b] + rec[6 + a] * rec[6 + b]);
+                cpg[a] -= cw * (rec[a] * r[0] + rec[3 + a] * r[1] + rec[6 + a] * r[2]);
+            }
+        }
+        if (slot < MT) s_cpc[slot] = cc_sum;
+    }
     if (start && elim) {
-        double V[6] = {0, 0, 0, 0, 0, 0}, rhs[3] = {0, 0, 0};
+        double V[6] = {cpV[0], cpV[1], cpV[2], cpV[3], cpV[4], cpV[5]}, rhs[3] = {cpg[0], cpg[1], cpg[2]};
         for (int j = 0; j < k; ++j) {
             const double* v = s_V + static_cast<size_t>(first + j) * 9;
             for (int i = 0; i < 6; ++i) V[i] += v[i];
@@ -470,6 +493,8 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
     if (tid == 0) {
         double c = 0.0;
         for (int w = 0; w < static_cast<int>((blockDim.x + 31) >> 5); ++w) c += s_misc[w];
+        if (S.ncp > 0)
+            for (int t = 0; t < ntc; ++t) c += s_cpc[t];
         O.part_cost[chunk] = c;
         O.part_flags[chunk] = s_flags[0];
     }

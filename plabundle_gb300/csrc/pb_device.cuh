@@ -7,6 +7,9 @@
 //   rotation increment  C2W' = D E(w)^T D C2W, D = diag(1,-1,-1), E = Rx Ry Rz
 //   centre increment    C' = C + dC (world frame), or the 2-DoF gauge tangent for the scale camera
 //   point increment     X' = X + s(X) dX, s(X) = (|X|/1000) / atan(|X|/1000)
+// and, for problems with control points, the plain parameterisation (:208-214): rotation columns
+// Jw x (X - C) of a world-frame rotation vector, C2W' = Exp(w) C2W, and X' = X + dX.  The two
+// rotation charts agree to first order up to the sign of the first component.
 // The projection, residual and robust cost are always evaluated in FP64; the Jacobians are
 // produced in the arithmetic type T of the kernel (float on the mixed path).
 #pragma once
@@ -102,6 +105,30 @@ __device__ __forceinline__ void robust_derivatives(double s, int loss, double sc
     d2 = -0.5 * q * q / c2;
 }
 
+// Control-point residual of a track point (linearizeControlPoint,
+// BundleAdjustPlaMatrixConstraints.cpp:90-116): r = sqrt(weight) W (X - P) from a record
+// [sqrt(weight) W (9, row-major), P (3)], Huber on |r|^2 with the control-point delta
+// (finishRobust, :17-29).  False when the cost is not finite.
+__device__ __forceinline__ bool cp_eval(const double* __restrict__ rec, double X0, double X1, double X2, double delta,
+                                        double* r, double& cost, double& weight) {
+    const double d0 = X0 - rec[9], d1 = X1 - rec[10], d2 = X2 - rec[11];
+    for (int a = 0; a < 3; ++a) r[a] = rec[a * 3] * d0 + rec[a * 3 + 1] * d1 + rec[a * 3 + 2] * d2;
+    const double sq = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+    double c = 0.0, w = 0.0;
+    if (!isfinite(sq)) return false;
+    if (sq <= delta * delta) {
+        c = 0.5 * sq;
+        w = 1.0;
+    } else {
+        const double n = sqrt(sq);
+        c = delta * n - 0.5 * delta * delta;
+        w = delta / n;
+    }
+    cost = c;
+    weight = w;
+    return isfinite(c) && isfinite(w);
+}
+
 __device__ __forceinline__ double point_scale(double X0, double X1, double X2) {
     const double len = sqrt(X0 * X0 + X1 * X1 + X2 * X2) / 1000.0;
     if (!isfinite(len) || len == 0.0) return 1.0;
@@ -142,7 +169,8 @@ __device__ __forceinline__ void intrinsic_column(int col, U x, U y, U r2, U xd, 
 }
 
 // Linearises one observation; s64 is the point step scale s(X) of its track.  `tangent` selects the gauge tangent centre columns (basis: two
-// world-frame directions in gb[0..5]).  Returns false on an invalid projection or loss.
+// world-frame directions in gb[0..5]); `plain` the rotation columns of the plain parameterisation.
+// Returns false on an invalid projection or loss.
 // With `grad`, also writes the observation's gradient -J^T w r in FP64: pose [0, 6), point
 // [6, 9), intrinsic columns [9, 9 + ni).  On the FP64 path it comes from the FP64 Jacobian; on
 // the FP32 path from the FP64 projection through v = R (dpi/dx_c)^T (w r), so that the gradient
@@ -150,8 +178,9 @@ __device__ __forceinline__ void intrinsic_column(int col, U x, U y, U r2, U xd, 
 template <typename T>
 __device__ __forceinline__ bool linearize_obs(const DCam& c, double X0, double X1, double X2, double s64, double u,
                                               double v, double wobs, int loss, double lscale, bool tangent,
-                                              const double* __restrict__ gb, int ni, const int* __restrict__ cols,
-                                              bool want_jacobian, Lin<T>& L, double* grad = nullptr) {
+                                              bool plain, const double* __restrict__ gb, int ni,
+                                              const int* __restrict__ cols, bool want_jacobian, Lin<T>& L,
+                                              double* grad = nullptr) {
     Proj p;
     if (!project64(c, X0, X1, X2, p)) return false;
     const double r0 = p.px - u, r1 = p.py - v;
@@ -185,6 +214,7 @@ __device__ __forceinline__ bool linearize_obs(const DCam& c, double X0, double X
     for (int i = 0; i < 9; ++i) R[i] = static_cast<T>(c.R[i]);
     const T d0 = static_cast<T>(p.d0), d1 = static_cast<T>(p.d1), d2 = static_cast<T>(p.d2);
     const T s = static_cast<T>(s64);
+    const T rs0 = plain ? T(-1) : T(1);
 #pragma unroll
     for (int pa = 0; pa < 2; ++pa) {
         // world point Jacobian: dpi/dXw = dpi/dxc * R^T
@@ -192,7 +222,7 @@ __device__ __forceinline__ bool linearize_obs(const DCam& c, double X0, double X
         const T jw1 = dc[pa * 3 + 0] * R[3] + dc[pa * 3 + 1] * R[4] + dc[pa * 3 + 2] * R[5];
         const T jw2 = dc[pa * 3 + 0] * R[6] + dc[pa * 3 + 1] * R[7] + dc[pa * 3 + 2] * R[8];
         // rotation columns of the target parameterisation: s_k * Jw (e_k x d), s = (1,-1,-1)
-        L.Jc[pa * 6 + 0] = jw2 * d1 - jw1 * d2;
+        L.Jc[pa * 6 + 0] = rs0 * (jw2 * d1 - jw1 * d2);
         L.Jc[pa * 6 + 1] = jw2 * d0 - jw0 * d2;
         L.Jc[pa * 6 + 2] = jw0 * d1 - jw1 * d0;
         if (tangent) {
@@ -238,7 +268,7 @@ __device__ __forceinline__ bool linearize_obs(const DCam& c, double X0, double X
             const double v0 = c.R[0] * tx + c.R[1] * ty + c.R[2] * tz;
             const double v1 = c.R[3] * tx + c.R[4] * ty + c.R[5] * tz;
             const double v2 = c.R[6] * tx + c.R[7] * ty + c.R[8] * tz;
-            grad[0] = -(v2 * p.d1 - v1 * p.d2);
+            grad[0] = plain ? v2 * p.d1 - v1 * p.d2 : -(v2 * p.d1 - v1 * p.d2);
             grad[1] = -(v2 * p.d0 - v0 * p.d2);
             grad[2] = -(v0 * p.d1 - v1 * p.d0);
             if (tangent) {

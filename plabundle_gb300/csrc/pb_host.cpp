@@ -86,6 +86,89 @@ void camera_parameter_block(const double* cam, double* p) {
     for (int i = 2; i < 9; ++i) p[i] = cam[12 + i];
 }
 
+// Lower Cholesky factor of a symmetric positive definite 3x3 matrix with the checks of the
+// control-point uncertainty factorisation (control_point.cpp:34-85): finite, symmetric to
+// 1e-10 max(1, max|a|), every pivot above 1e-12 max(1, max|a|).
+bool cp_cholesky(const double* a, double* L) {
+    double maximum = 0.0;
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) {
+            const double v = a[r * 3 + c], t = a[c * 3 + r];
+            if (!std::isfinite(v) || !std::isfinite(t)) return false;
+            maximum = std::max(maximum, std::max(std::fabs(v), std::fabs(t)));
+            if (std::fabs(v - t) > 1.0e-10 * std::max(1.0, maximum)) return false;
+        }
+    const double threshold = std::max(1.0, maximum) * 1.0e-12;
+    for (int i = 0; i < 9; ++i) L[i] = 0.0;
+    for (int j = 0; j < 3; ++j) {
+        double d = a[j * 3 + j];
+        for (int k = 0; k < j; ++k) d -= L[j * 3 + k] * L[j * 3 + k];
+        if (!(d > 0.0) || !std::isfinite(d)) return false;
+        const double ljj = std::sqrt(d);
+        L[j * 3 + j] = ljj;
+        for (int i = j + 1; i < 3; ++i) {
+            double v = a[i * 3 + j];
+            for (int k = 0; k < j; ++k) v -= L[i * 3 + k] * L[j * 3 + k];
+            L[i * 3 + j] = v / ljj;
+        }
+    }
+    for (int j = 0; j < 3; ++j)
+        if (!(L[j * 3 + j] * L[j * 3 + j] > threshold)) return false;
+    return true;
+}
+
+// makeControlPointWhitening (control_point.cpp:91-158): isotropic sigma -> I / sigma;
+// covariance C = L L^T -> L^-1; square-root information W (W^T W positive definite) -> W.
+// data: point (3), sigma, weight, kind, matrix (9).
+bool cp_whitening(const double* data, double* W) {
+    const int kind = static_cast<int>(data[5]);
+    const double* mat = data + 6;
+    for (int i = 0; i < 9; ++i) W[i] = 0.0;
+    if (kind == 0) {
+        const double sigma = data[3];
+        if (!std::isfinite(sigma) || sigma <= 0.0) return false;
+        for (int a = 0; a < 3; ++a) W[a * 3 + a] = 1.0 / sigma;
+        return true;
+    }
+    if (kind == 1) {
+        double L[9];
+        if (!cp_cholesky(mat, L)) return false;
+        // inverse of the lower triangle
+        for (int i = 0; i < 3; ++i) {
+            W[i * 3 + i] = 1.0 / L[i * 3 + i];
+            for (int j = 0; j < i; ++j) {
+                double v = 0.0;
+                for (int k = j; k < i; ++k) v -= L[i * 3 + k] * W[k * 3 + j];
+                W[i * 3 + j] = v / L[i * 3 + i];
+            }
+        }
+        return true;
+    }
+    if (kind == 2) {
+        for (int i = 0; i < 9; ++i)
+            if (!std::isfinite(mat[i])) return false;
+        double info[9], L[9];
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) {
+                double v = 0.0;
+                for (int k = 0; k < 3; ++k) v += mat[k * 3 + r] * mat[k * 3 + c];
+                info[r * 3 + c] = v;
+            }
+        if (!cp_cholesky(info, L)) return false;
+        for (int i = 0; i < 9; ++i) W[i] = mat[i];
+        return true;
+    }
+    return false;
+}
+
+// validateControlPointConstraint (control_point.cpp:205-220)
+bool cp_valid(const double* data, double* W) {
+    for (int a = 0; a < 3; ++a)
+        if (!std::isfinite(data[a])) return false;
+    if (!std::isfinite(data[4]) || data[4] <= 0.0) return false;
+    return cp_whitening(data, W);
+}
+
 int build_host_model(const pb_problem_desc* pr, const pb_solve_options* op, HostModel* m, std::string* err) {
     if (!pr || !op) { *err = "null problem or options"; return PB_SOLVE_INVALID_INPUT; }
     if (pr->n_cameras <= 0 || pr->n_tracks <= 0 || !pr->cameras || !pr->track_offsets || !pr->points) {
@@ -138,6 +221,85 @@ int build_host_model(const pb_problem_desc* pr, const pb_solve_options* op, Host
         return PB_SOLVE_UNSUPPORTED;
     }
 
+    // --- control points (Track::controlPointConstraints): any constraint switches the problem to
+    // the plain parameterisation (enableControlPointConstraints, Conversion.cpp:106;
+    // useReferencePointParameterization, BundleAdjustPlaMatrixAssembly.cpp:24-30); a constraint
+    // whose weight is not positive does not linearise and is skipped (linearizeControlPoint,
+    // BundleAdjustPlaMatrixConstraints.cpp:90-116)
+    m->cp_track.clear();
+    m->cp_rec.clear();
+    m->ref_param = pr->n_control_points <= 0;
+    m->cp_huber = op->control_point_huber_delta;
+    std::vector<double> cp_points;  // valid targets of tracks with usable observations
+    std::vector<char> cp_usable_track;
+    if (pr->n_control_points > 0) {
+        if (!pr->control_point_track || !pr->control_point_data) { *err = "control-point arrays missing"; return PB_SOLVE_INVALID_INPUT; }
+        if (!std::isfinite(op->control_point_weight) || op->control_point_weight < 0.0 ||
+            !std::isfinite(op->control_point_huber_delta) || op->control_point_huber_delta <= 0.0) {
+            *err = "control-point weight must be finite and non-negative and its Huber delta finite and positive";
+            return PB_SOLVE_INVALID_INPUT;
+        }
+        // hasUsableTrackObservations (BundleAdjustValidation.cpp:94-106): two distinct cameras
+        cp_usable_track.assign(m->nt, 0);
+        for (int t = 0; t < m->nt; ++t) {
+            int first = -1;
+            for (long long k = m->offs[t]; k < m->offs[t + 1]; ++k) {
+                const int c = m->obs_cam[k];
+                if (c < 0 || !std::isfinite(m->obs_u[k]) || !std::isfinite(m->obs_v[k]) || !std::isfinite(m->obs_weight[k]) ||
+                    !(m->obs_weight[k] > 0.0))
+                    continue;
+                if (first < 0) first = c;
+                else if (c != first) { cp_usable_track[t] = 1; break; }
+            }
+        }
+        for (int i = 0; i < pr->n_control_points; ++i) {
+            const int t = pr->control_point_track[i];
+            if (t < 0 || t >= m->nt) { *err = "control-point track index out of range"; return PB_SOLVE_INVALID_INPUT; }
+            const double* d = pr->control_point_data + static_cast<size_t>(i) * 15;
+            // validateProblem rejects the whole problem (problem.cpp:253-260)
+            double W[9];
+            if (!cp_valid(d, W)) { *err = "track contains an invalid control-point constraint"; return PB_SOLVE_INVALID_INPUT; }
+            if (cp_usable_track[t]) cp_points.insert(cp_points.end(), d, d + 3);
+            const double wgt = op->control_point_weight * d[4];
+            if (!(wgt > 0.0)) continue;
+            const double sw = std::sqrt(wgt);
+            m->cp_track.push_back(t);
+            for (int k = 0; k < 9; ++k) m->cp_rec.push_back(sw * W[k]);
+            m->cp_rec.insert(m->cp_rec.end(), d, d + 3);
+        }
+    }
+    // hasCompleteControlPointGauge (BundleAdjustValidation.cpp:181-236): three non-collinear targets
+    bool cp_complete = false;
+    {
+        const size_t np = cp_points.size() / 3;
+        for (size_t a = 0; a < np && !cp_complete; ++a)
+            for (size_t b = a + 1; b < np && !cp_complete; ++b) {
+                const double ab[3] = {cp_points[b * 3] - cp_points[a * 3], cp_points[b * 3 + 1] - cp_points[a * 3 + 1],
+                                      cp_points[b * 3 + 2] - cp_points[a * 3 + 2]};
+                const double ab2 = ab[0] * ab[0] + ab[1] * ab[1] + ab[2] * ab[2];
+                if (ab2 <= 1.0e-16) continue;
+                for (size_t c = b + 1; c < np; ++c) {
+                    const double ac[3] = {cp_points[c * 3] - cp_points[a * 3], cp_points[c * 3 + 1] - cp_points[a * 3 + 1],
+                                          cp_points[c * 3 + 2] - cp_points[a * 3 + 2]};
+                    const double ac2 = ac[0] * ac[0] + ac[1] * ac[1] + ac[2] * ac[2];
+                    const double x[3] = {ab[1] * ac[2] - ab[2] * ac[1], ab[2] * ac[0] - ab[0] * ac[2], ab[0] * ac[1] - ab[1] * ac[0]};
+                    const double x2 = x[0] * x[0] + x[1] * x[1] + x[2] * x[2];
+                    if (ac2 > 1.0e-16 && x2 > 1.0e-12 * ab2 * ac2) { cp_complete = true; break; }
+                }
+            }
+    }
+    // hasControlPointBaselineToFixedCamera (BundleAdjustValidation.cpp:147-179)
+    auto cp_baseline_to = [&](const std::vector<int>& fixed) {
+        for (size_t i = 0; i < cp_points.size() / 3; ++i)
+            for (int f : fixed) {
+                const double* c = &m->cams_in[static_cast<size_t>(f) * kCamStride + 9];
+                if (!std::isfinite(c[0]) || !std::isfinite(c[1]) || !std::isfinite(c[2])) continue;
+                const double dx = cp_points[i * 3] - c[0], dy = cp_points[i * 3 + 1] - c[1], dz = cp_points[i * 3 + 2] - c[2];
+                if (dx * dx + dy * dy + dz * dz > 1.0e-16) return true;
+            }
+        return false;
+    };
+
     // --- gauge (validateAndNormalizeBundleAdjustOptions, BundleAdjustValidation.cpp:772-893)
     {
         std::vector<int> fc = m->fixed_cams;
@@ -162,11 +324,19 @@ int build_host_model(const pb_problem_desc* pr, const pb_solve_options* op, Host
             if (i && m->fixed_tracks[i] == m->fixed_tracks[i - 1]) { *err = "duplicate fixed track index"; return PB_SOLVE_INVALID_INPUT; }
         }
         if (op->refine_camera_pose && op->gauge_policy != 2) {
+            // absolute pose and scale from three non-collinear control points; scale alone from
+            // a control point away from a fixed camera (:826-835)
+            bool abs_scale = cp_complete || cp_baseline_to(fc);
             if (op->gauge_policy == 1) {
-                if (fc.size() < 2) { *err = "incomplete gauge: two fixed cameras are required"; return PB_SOLVE_UNSUPPORTED; }
-            } else {
-                if (fc.empty()) { m->fixed_cams.push_back(0); fc.push_back(0); }
-                if (fc.size() < 2) {
+                const bool complete = (cp_complete && abs_scale) || fc.size() >= 2 || (fc.size() == 1 && abs_scale);
+                if (!complete) { *err = "incomplete gauge: two fixed cameras, or a fixed camera and an absolute scale, are required"; return PB_SOLVE_UNSUPPORTED; }
+            } else if (!cp_complete) {
+                if (fc.empty()) {
+                    m->fixed_cams.push_back(0);
+                    fc.push_back(0);
+                    abs_scale = abs_scale || cp_baseline_to(fc);
+                }
+                if (!abs_scale && fc.size() < 2) {
                     const int anchor = fc[0];
                     const double* a = &m->cams_in[static_cast<size_t>(anchor) * kCamStride + 9];
                     int best = -1;
@@ -459,6 +629,24 @@ int build_host_model(const pb_problem_desc* pr, const pb_solve_options* op, Host
             m->trk_obs_begin[i + 1] = static_cast<int>(m->p_obs_orig.size());
         }
     }
+    // control points of the processed tracks, in processing order
+    {
+        const size_t ntp = m->trk_order.size();
+        std::vector<int> proc(nt, -1);
+        for (size_t i = 0; i < ntp; ++i) proc[m->trk_order[i]] = static_cast<int>(i);
+        std::vector<int> cnt(ntp + 1, 0);
+        for (int t : m->cp_track)
+            if (proc[t] >= 0) ++cnt[proc[t] + 1];
+        for (size_t i = 0; i < ntp; ++i) cnt[i + 1] += cnt[i];
+        m->trk_cp_begin = cnt;
+        m->cp_proc.assign(static_cast<size_t>(cnt[ntp]) * 12, 0.0);
+        std::vector<int> fill(cnt.begin(), cnt.end() - 1);
+        for (size_t i = 0; i < m->cp_track.size(); ++i) {
+            const int p = proc[m->cp_track[i]];
+            if (p < 0) continue;
+            std::copy(&m->cp_rec[i * 12], &m->cp_rec[i * 12] + 12, &m->cp_proc[static_cast<size_t>(fill[p]++) * 12]);
+        }
+    }
     // structure hash for pattern reuse
     {
         unsigned long long h = 1469598103934665603ull;
@@ -490,6 +678,7 @@ size_t chunk_smem_bytes(int precision, int max_obs, int max_tracks, int ni, int 
     s += al(mt * st(static_cast<size_t>(nb) * 3) * vs);  // per-track K
     s += al((mt + 1) * 4);      // track starts
     s += al(mt * 4);            // calibration groups present per track
+    s += al(mt * 8);            // control-point cost per track
     s += al(40 * 8);            // warp partial costs and track counts, flags
     return s;
 }

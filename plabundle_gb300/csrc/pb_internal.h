@@ -36,6 +36,12 @@ struct Shape {
     double gauge_baseline;
     int int_cols[kMaxNI];
     int max_obs, max_cams, max_pairs, max_tracks;  // chunk limits of the active chunk set
+    // 1: the reference point parameterisation of image-only problems (point steps X + s(X) dX,
+    // Euler target rotation steps); 0: plain X + dX and world-frame rotation-vector steps
+    // (useReferencePointParameterization, BundleAdjustPlaMatrixAssembly.cpp:24-30)
+    int ref_param;
+    int ncp;             // control-point constraints of processed tracks
+    double cp_huber;     // Huber delta of the control-point residuals (m)
 };
 
 struct DevPtrs {
@@ -57,6 +63,8 @@ struct DevPtrs {
     double* points;       // ntp * 3
     double* points0;      // ntp * 3
     double* pscale;       // ntp: point step scale s(X) of the current points
+    int* trk_cp_begin;    // ntp + 1: control points of each processed track
+    double* cp_rec;       // 12 per control point: whitening sqrt(weight) W (row-major), target P
     // observations (processing order)
     int* obs_cam;
     double* obs_u;
@@ -123,6 +131,15 @@ struct HostModel {
     std::vector<int> obs_cam;
     std::vector<double> obs_u, obs_v, obs_weight, obs_scale;
     std::vector<int> fixed_cams, fixed_tracks, group_ids;
+    // control points (valid constraints only): per original track, the whitened residual
+    // sqrt(weight) W (X - P) as W (9, scaled) and P (3); ref_param == false when any exists
+    // (the reference point parameterisation applies to image-only problems)
+    std::vector<int> cp_track;
+    std::vector<double> cp_rec;   // 12 per constraint
+    std::vector<int> trk_cp_begin;  // processed tracks + 1
+    std::vector<double> cp_proc;    // 12 per constraint of a processed track, processing order
+    double cp_huber = 0.2;
+    bool ref_param = true;
     int gauge_anchor = -1, gauge_scale = -1;
     double gauge_baseline = 0.0;
     int loss = 0;
@@ -158,6 +175,9 @@ inline PB_HOST_DEVICE int chunk_stride(int words) { return words | 1; }
 
 // pb_host.cpp
 int build_host_model(const pb_problem_desc* pr, const pb_solve_options* op, HostModel* m, std::string* err);
+// validateControlPointConstraint + makeControlPointWhitening (control_point.cpp:91-220) of one
+// 15-double control-point record; W receives the whitening matrix (row-major).
+bool cp_valid(const double* data, double* W);
 int build_chunks(HostModel* m, int precision, size_t smem_budget, std::string* err);
 size_t chunk_smem_bytes(int precision, int max_obs, int max_tracks, int ni, int nb);
 double finite_median(std::vector<double> v, double fallback);

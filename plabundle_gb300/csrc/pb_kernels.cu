@@ -183,7 +183,7 @@ __global__ void k_effective(Shape S, DevPtrs D) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c < S.ntp) {
         const double* X = D.points + static_cast<size_t>(c) * 3;
-        D.pscale[c] = point_scale(X[0], X[1], X[2]);
+        D.pscale[c] = S.ref_param ? point_scale(X[0], X[1], X[2]) : 1.0;
     }
     if (c < S.nc) {
         const double* G = S.ng > 0 ? D.groups + static_cast<size_t>(D.cam_group[c]) * kGroupRec : nullptr;
@@ -197,8 +197,9 @@ __global__ void k_effective(Shape S, DevPtrs D) {
 }
 
 // Trial states for a batch of step lengths: pose retraction (applyReferenceCameraPoseStep,
-// BundleAdjustPlaMatrixAssembly.cpp:130-179; gauge tangent step :101-128) and clamped intrinsic
-// update (applyIntrinsicStep, BundleAdjustPlaMatrixModel.cpp:248-269).
+// BundleAdjustPlaMatrixAssembly.cpp:130-179; gauge tangent step :101-128; the plain
+// parameterisation's pose delta :1134-1136) and clamped intrinsic update (applyIntrinsicStep,
+// BundleAdjustPlaMatrixModel.cpp:248-269).
 __global__ void k_trial_cameras(Shape S, DevPtrs D, const double* __restrict__ step_c, const double* __restrict__ alphas,
                                 int n_alpha) {
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
@@ -233,7 +234,35 @@ __global__ void k_trial_cameras(Shape S, DevPtrs D, const double* __restrict__ s
     const double* st = D.cams_state + static_cast<size_t>(c) * kCamStride;
     for (int i = 0; i < kCamStride; ++i) pose[i] = st[i];
     const int b = D.cam_block[c];
-    if (b >= 0) {
+    if (b >= 0 && !S.ref_param) {
+        // plain parameterisation: the camera's own pose delta (CameraState::applyDeltaPose,
+        // BundleAdjustPlaMatrixAssembly.cpp:1134-1136), C2W' = Exp(alpha w) C2W by Rodrigues'
+        // formula and C' = C + alpha dC for every refined camera, the gauge scale camera's
+        // tangent coordinates included
+        const double* d = step_c + 6 * b;
+        const double w0 = alpha * d[0], w1 = alpha * d[1], w2 = alpha * d[2];
+        const double th2 = w0 * w0 + w1 * w1 + w2 * w2;
+        double A, B;
+        if (th2 < 1e-16) {
+            A = 1.0 - th2 / 6.0;
+            B = 0.5 - th2 / 24.0;
+        } else {
+            const double th = sqrt(th2), sh = sin(0.5 * th);
+            A = sin(th) / th;
+            B = 2.0 * sh * sh / th2;  // (1 - cos th) / th^2 without the cancellation
+        }
+        const double K[9] = {0.0, -w2, w1, w2, 0.0, -w0, -w1, w0, 0.0};
+        double E[9];
+        for (int r = 0; r < 3; ++r)
+            for (int q = 0; q < 3; ++q) {
+                const double kk = K[r * 3] * K[q] + K[r * 3 + 1] * K[3 + q] + K[r * 3 + 2] * K[6 + q];
+                E[r * 3 + q] = (r == q ? 1.0 : 0.0) + A * K[r * 3 + q] + B * kk;
+            }
+        for (int r = 0; r < 3; ++r)
+            for (int q = 0; q < 3; ++q)
+                pose[r * 3 + q] = E[r * 3] * st[q] + E[r * 3 + 1] * st[3 + q] + E[r * 3 + 2] * st[6 + q];
+        for (int i = 0; i < 3; ++i) pose[9 + i] = st[9 + i] + alpha * d[3 + i];
+    } else if (b >= 0) {
         const double* d = step_c + 6 * b;
         const double dx = alpha * d[0], dy = alpha * d[1], dz = alpha * d[2];
         double sx, cx, sy, cy, sz, cz;
@@ -319,6 +348,14 @@ __global__ void __launch_bounds__(256) k_cost_batch(Shape S, DevPtrs D, const do
             if (good) {
                 const double r0 = p.px - u, r1 = p.py - v;
                 good = robust_loss(w * (r0 * r0 + r1 * r1), S.loss, S.loss_scale, cost, rw) && isfinite(cost);
+            }
+            if (good && S.ncp > 0 && o == D.trk_obs_begin[trk]) {
+                // the track's control points, once per track (its first observation's thread); a
+                // term that is not finite is skipped (BundleAdjustPlaMatrixAssembly.cpp:674-690)
+                for (int q = D.trk_cp_begin[trk]; q < D.trk_cp_begin[trk + 1]; ++q) {
+                    double r[3], cc, cw;
+                    if (cp_eval(D.cp_rec + static_cast<size_t>(q) * 12, X0, X1, X2, S.cp_huber, r, cc, cw)) cost += cc;
+                }
             }
             if (!good) atomicOr(&s_bad[a], 1);
             else c[a] = cost;
@@ -509,7 +546,7 @@ __global__ void k_accept(Shape S, DevPtrs D, const double* __restrict__ step_p, 
         X[0] += f * step_p[static_cast<size_t>(i) * 3 + 0];
         X[1] += f * step_p[static_cast<size_t>(i) * 3 + 1];
         X[2] += f * step_p[static_cast<size_t>(i) * 3 + 2];
-        D.pscale[i] = point_scale(X[0], X[1], X[2]);
+        D.pscale[i] = S.ref_param ? point_scale(X[0], X[1], X[2]) : 1.0;
     }
 }
 
@@ -565,7 +602,7 @@ __global__ void k_linearize_export(Shape S, DevPtrs D, double* __restrict__ res,
     const bool tangent = cam == S.gauge_scale && S.gauge_anchor >= 0 && S.gauge_baseline > 0.0;
     Lin<T> L;
     const bool ok = linearize_obs<T>(c, X[0], X[1], X[2], D.pscale[trk], D.obs_u[o], D.obs_v[o], D.obs_w[o], S.loss,
-                                     S.loss_scale, tangent, D.gauge_basis, S.ni, S.int_cols, true, L);
+                                     S.loss_scale, tangent, !S.ref_param, D.gauge_basis, S.ni, S.int_cols, true, L);
     valid[k] = ok ? 1 : 0;
     if (!ok) return;
     res[2 * k] = static_cast<double>(L.r0);

@@ -230,6 +230,9 @@ void upload_structure(pb_gpu_ctx* c) {
     S.gauge_scale = m.gauge_scale;
     S.gauge_baseline = m.gauge_baseline;
     for (int i = 0; i < kMaxNI; ++i) S.int_cols[i] = i < m.ni ? m.int_cols[i] : 0;
+    S.ref_param = m.ref_param ? 1 : 0;
+    S.ncp = static_cast<int>(m.cp_proc.size() / 12);
+    S.cp_huber = m.cp_huber;
 
     D.cams_input = upload_new(A, m.cams_in, st);
     D.cams_ref = upload_new(A, m.cams_ref, st);
@@ -262,6 +265,14 @@ void upload_structure(pb_gpu_ctx* c) {
     D.points0 = upload_new(A, pts, st);
     D.points = A.alloc<double>(pts.size());
     D.pscale = A.alloc<double>(std::max<size_t>(1, pts.size() / 3));
+    {
+        std::vector<int> cpb = m.trk_cp_begin;
+        if (cpb.empty()) cpb.assign(static_cast<size_t>(ntp) + 1, 0);
+        D.trk_cp_begin = upload_new(A, cpb, st);
+        std::vector<double> cpr = m.cp_proc;
+        if (cpr.empty()) cpr.assign(12, 0.0);
+        D.cp_rec = upload_new(A, cpr, st);
+    }
     // observations in processing order
     std::vector<int> ocam(nop), otrk(nop);
     std::vector<double> ou(nop), ov(nop), ow(nop);
@@ -1552,6 +1563,10 @@ pb_status adjoint_core(pb_gpu_ctx* c, int newton, pb_adjoint_report* rep, float*
 // Allocates the adjoint buffers for the chunk plan of the arithmetic path last used.
 pb_status adjoint_prepare(pb_gpu_ctx* c) {
     const HostModel& m = c->model;
+    // the exact Hessian is written for the Euler target rotation chart and the scaled point chart
+    // of image-only problems; control points switch the solve to the plain parameterisation
+    if (!m.ref_param)
+        return fail(c, PB_ERR_UNSUPPORTED, "the backward pass covers image-only problems (no control points)");
     // the point elimination runs over the chunk plan of the arithmetic path last used
     const int prec = c->last_precision == PB_PRECISION_MIXED ? 1 : 0;
     if (prec == 1) prepare_precision<float>(c, prec);

@@ -36,7 +36,9 @@ class ProblemDesc(C.Structure):
                 ("obs_camera", C.c_void_p), ("obs_u", C.c_void_p), ("obs_v", C.c_void_p),
                 ("obs_weight", C.c_void_p), ("obs_scale", C.c_void_p), ("n_fixed_cameras", C.c_int32),
                 ("fixed_cameras", C.c_void_p), ("n_fixed_tracks", C.c_int32), ("fixed_tracks", C.c_void_p),
-                ("calibration_group_ids", C.c_void_p), ("intrinsic_reference_cameras", C.c_void_p)]
+                ("calibration_group_ids", C.c_void_p), ("intrinsic_reference_cameras", C.c_void_p),
+                ("n_control_points", C.c_int32), ("control_point_track", C.c_void_p),
+                ("control_point_data", C.c_void_p)]
 
 
 class SolveOptionsC(C.Structure):
@@ -50,7 +52,8 @@ class SolveOptionsC(C.Structure):
                 ("max_linear_iterations", C.c_int32), ("linear_relative_tolerance", C.c_double),
                 ("linear_absolute_tolerance", C.c_double), ("refinement_sweeps", C.c_int32),
                 ("preconditioner_cluster_size", C.c_int32), ("linear_solver", C.c_int32),
-                ("calibration", C.c_double * 32)]
+                ("calibration", C.c_double * 32), ("control_point_weight", C.c_double),
+                ("control_point_huber_delta", C.c_double)]
 
 
 class SolveReportC(C.Structure):
@@ -150,12 +153,21 @@ def problem_desc(problem):
     p = problem.normalized()
     fixed_c = np.ascontiguousarray(p.fixedCameraIndices, np.int32)
     fixed_t = np.ascontiguousarray(p.fixedTrackIndices, np.int32)
-    keep = [p, fixed_c, fixed_t]
+    cp_track, cp_data = control_point_arrays(p)
+    keep = [p, fixed_c, fixed_t, cp_track, cp_data]
     desc = ProblemDesc(p.n_cameras, _ptr(p.cameras), p.n_tracks, _ptr(p.track_offsets), _ptr(p.points), p.n_obs,
                        _ptr(p.obs_camera), _ptr(p.obs_u), _ptr(p.obs_v), _ptr(p.obs_weight), _ptr(p.obs_scale),
                        fixed_c.size, _ptr(fixed_c), fixed_t.size, _ptr(fixed_t), _ptr(p.cameraCalibrationGroupIds),
-                       _ptr(p.sharedIntrinsicReferenceCameras))
+                       _ptr(p.sharedIntrinsicReferenceCameras), cp_track.size, _ptr(cp_track), _ptr(cp_data))
     return desc, keep
+
+
+def control_point_arrays(problem):
+    """(track indices int32 [n], records float64 [n, 15]) of the problem's control points."""
+    cps = getattr(problem, "controlPoints", None) or []
+    track = np.ascontiguousarray([t for t, _ in cps], np.int32)
+    data = np.ascontiguousarray(np.array([c.record() for _, c in cps], np.float64).reshape(-1, 15))
+    return track, data
 
 
 def solve_options(options, problem=None) -> SolveOptionsC:
@@ -187,6 +199,9 @@ def solve_options(options, problem=None) -> SolveOptionsC:
     o.linear_solver = int(b.linearSolver)
     for i, v in enumerate(cal.numeric_block()):
         o.calibration[i] = v
+    con = getattr(options, "constraints", None)
+    o.control_point_weight = con.controlPointWeight if con is not None else 1.0
+    o.control_point_huber_delta = con.controlPointHuberDeltaMeters if con is not None else 0.2
     return o
 
 

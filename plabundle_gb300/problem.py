@@ -21,7 +21,7 @@ from __future__ import annotations
 import dataclasses
 import enum
 from dataclasses import dataclass, field
-from typing import List, Optional
+from typing import List, Optional, Sequence, Tuple
 
 import numpy as np
 
@@ -109,12 +109,38 @@ class Gauge:
     referenceBaseline: float = 0.0
 
 
+class ControlPointUncertainty(enum.IntEnum):
+    """ControlPointConstraint::Uncertainty (include/plabundle/constraints.h:79-84)."""
+
+    IsotropicSigma = 0
+    Covariance = 1
+    SqrtInformation = 2
+
+
+@dataclass
+class ControlPointConstraint:
+    """ControlPointConstraint (include/plabundle/constraints.h:73-87): the target of a track's
+    point in the solver frame with its uncertainty."""
+
+    point: Sequence[float] = (0.0, 0.0, 0.0)
+    sigmaMeters: float = 1.0
+    weight: float = 1.0
+    uncertainty: ControlPointUncertainty = ControlPointUncertainty.IsotropicSigma
+    uncertaintyMatrix: Sequence[float] = (0.0,) * 9   # row-major covariance (m^2) or sqrt information (1/m)
+
+    def record(self) -> np.ndarray:
+        return np.array(list(self.point) + [self.sigmaMeters, self.weight, float(int(self.uncertainty))] +
+                        list(self.uncertaintyMatrix), np.float64)
+
+
 @dataclass
 class Problem:
     """plabundle::Problem (include/plabundle/problem.h:37-54) for frame cameras.
 
-    Rigs, laser and survey constraints are not carried: the GB300 backend covers the
-    image-only online reduced-Schur path.
+    Rigs, laser planes, scale bars and pose priors are not carried: the GB300 backend covers the
+    online reduced-Schur path, whose only survey term is the control point
+    (canUseReferenceOnlineSchur, BundleAdjustPlaMatrixReferenceSchur.cpp:667-673).  Control
+    points are the (track, ControlPointConstraint) pairs of Track::controlPointConstraints.
     """
 
     cameras: np.ndarray                 # [n_cameras, 32] float64
@@ -130,6 +156,7 @@ class Problem:
     cameraCalibrationGroupIds: Optional[np.ndarray] = None   # [n_cameras] int32
     sharedIntrinsicReferenceCameras: Optional[np.ndarray] = None  # [n_cameras, 32]
     gauge: Gauge = field(default_factory=Gauge)
+    controlPoints: List[Tuple[int, ControlPointConstraint]] = field(default_factory=list)
 
     @property
     def n_cameras(self) -> int:
@@ -307,10 +334,19 @@ class QualityGateOptions:
 
 
 @dataclass
+class ConstraintOptions:
+    """ConstraintOptions (include/plabundle/options.h:122-135): the control-point fields."""
+
+    controlPointWeight: float = 1.0
+    controlPointHuberDeltaMeters: float = 0.2
+
+
+@dataclass
 class SolveOptions:
     """include/plabundle/options.h:180-187."""
 
     solver: SolverControlOptions = field(default_factory=SolverControlOptions)
+    constraints: ConstraintOptions = field(default_factory=ConstraintOptions)
     calibration: CalibrationOptions = field(default_factory=CalibrationOptions)
     backend: BackendOptions = field(default_factory=BackendOptions)
     quality: QualityGateOptions = field(default_factory=QualityGateOptions)
@@ -357,7 +393,7 @@ class PlaMatrixDiagnostics:
 
 @dataclass
 class QualitySummary:
-    """include/plabundle/result.h:50-89 (image-only fields)."""
+    """include/plabundle/result.h:50-89 (image and control-point fields)."""
 
     totalTracks: int = 0
     optimizedTracks: int = 0
@@ -367,6 +403,9 @@ class QualitySummary:
     refinedCameraCount: int = 0
     refinedCalibrationGroupCount: int = 0
     filterThreshold: float = 0.0
+    controlPointConstraintCount: int = 0
+    controlPointRmsBeforeMeters: float = 0.0
+    controlPointRmsAfterMeters: float = 0.0
 
 
 @dataclass

@@ -10,6 +10,7 @@ from __future__ import annotations
 
 import ctypes as C
 import math
+from typing import Optional
 
 import numpy as np
 
@@ -77,8 +78,64 @@ def validate_problem(problem: Problem) -> str:
     return ""
 
 
-def result_fails_quality_gate(result: Result, options: SolveOptions) -> str:
-    """resultFailsQualityGate for image-only problems (src/solver.cpp:123-210)."""
+def control_point_rms_uncertainty(problem: Problem, options: SolveOptions) -> float:
+    """The control-point entry of constraintRmsUncertainty (src/solver.cpp:50-95):
+    sqrt(mean over valid constraints of |W^-1|_F^2 / (controlPointWeight * weight))
+    (controlPointRmsUncertaintyMeters, src/control_point.cpp:167-200)."""
+    var, n = 0.0, 0
+    for _, c in problem.controlPoints:
+        W = control_point_whitening(c)
+        if W is None:
+            continue
+        d = np.linalg.det(W)
+        if not np.isfinite(d) or abs(d) <= 1e-18:
+            continue
+        u2 = float((np.linalg.inv(W) ** 2).sum())
+        var += u2 / (options.constraints.controlPointWeight * c.weight)
+        n += 1
+    return math.sqrt(var / n) if n else 0.0
+
+
+def control_point_whitening(c) -> Optional[np.ndarray]:
+    """makeControlPointWhitening (src/control_point.cpp:91-165) for the statistics: None when the
+    constraint does not validate."""
+    from .problem import ControlPointUncertainty
+    if not np.all(np.isfinite(c.point)) or not (np.isfinite(c.weight) and c.weight > 0):
+        return None
+    M = np.asarray(c.uncertaintyMatrix, np.float64).reshape(3, 3)
+    if c.uncertainty == ControlPointUncertainty.IsotropicSigma:
+        return np.eye(3) / c.sigmaMeters if np.isfinite(c.sigmaMeters) and c.sigmaMeters > 0 else None
+    A = M if c.uncertainty == ControlPointUncertainty.Covariance else M.T @ M
+    if not np.all(np.isfinite(A)) or not np.allclose(A, A.T, rtol=0, atol=1e-10 * max(1.0, np.abs(A).max())):
+        return None
+    try:
+        L = np.linalg.cholesky(A)
+    except np.linalg.LinAlgError:
+        return None
+    if np.any(np.diag(L) ** 2 <= 1e-12 * max(1.0, np.abs(A).max())):
+        return None
+    return np.linalg.inv(L) if c.uncertainty == ControlPointUncertainty.Covariance else M
+
+
+def control_point_stats(problem: Problem, points: Optional[np.ndarray], valid: np.ndarray):
+    """computeControlPointStats (src/internal/BundleAdjustQuality.cpp:179-211): count and RMS of
+    |X - P| over the constraints of the tracks valid in the result, X the initial point (before)
+    or the refined one (after)."""
+    X = problem.points if points is None else points
+    s, n = 0.0, 0
+    for t, c in problem.controlPoints:
+        if not valid[t]:
+            continue
+        d2 = float(((np.asarray(X[t]) - np.asarray(c.point)) ** 2).sum())
+        if not np.isfinite(d2):
+            continue
+        s += d2
+        n += 1
+    return n, (math.sqrt(s / n) if n else 0.0)
+
+
+def result_fails_quality_gate(result: Result, options: SolveOptions, problem: Optional[Problem] = None) -> str:
+    """resultFailsQualityGate (src/solver.cpp:123-210) for image and control-point terms."""
     q = options.quality
     if not q.enabled:
         return ""
@@ -95,6 +152,14 @@ def result_fails_quality_gate(result: Result, options: SolveOptions) -> str:
             return "quality gate rejected excessive reprojection RMS growth"
         if qs.meanRmsBefore <= 1e-12 and qs.meanRmsAfter > 1e-9:
             return "quality gate rejected growth from a zero-residual input"
+    # constraintRmsPassesQualityGate (src/internal/BundleAdjustQuality.cpp:504-540)
+    if problem is not None and qs.controlPointConstraintCount > 0:
+        unc = control_point_rms_uncertainty(problem, options)
+        before, after = qs.controlPointRmsBeforeMeters, qs.controlPointRmsAfterMeters
+        if not (math.isfinite(before) and math.isfinite(after) and math.isfinite(unc)) or unc < 0:
+            return "quality gate rejected invalid control-point constraint RMS or uncertainty"
+        if after > max(1.0, q.maxAcceptedConstraintRmsGrowth) * max(before, unc):
+            return "quality gate rejected control-point constraint RMS growth beyond the uncertainty threshold"
     return ""
 
 
@@ -172,8 +237,13 @@ class Solver:
             backSubstitutionSeconds=r["back_substitution_ms"] / 1e3, schurPatternBuilds=r["pattern_builds"],
             schurPatternReuses=r["pattern_reuses"], mixedPrecisionUsed=bool(copts.precision == 1),
             refinementSweeps=r["refinement_sweeps"], deviceName=f"cuda:{ws.device}")
+        if problem.controlPoints:
+            v = result.points.valid
+            result.quality.controlPointConstraintCount, result.quality.controlPointRmsBeforeMeters = \
+                control_point_stats(problem, None, v)
+            _, result.quality.controlPointRmsAfterMeters = control_point_stats(problem, pts, v)
         result.report = r
-        gate = result_fails_quality_gate(result, options)
+        gate = result_fails_quality_gate(result, options, problem)
         if gate:
             result.qualityGateRejected = True
             result.qualityGateMessage = gate

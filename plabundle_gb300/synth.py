@@ -20,7 +20,8 @@ from __future__ import annotations
 
 import numpy as np
 
-from .problem import CAMERA_STRIDE, Gauge, GaugePolicy, Problem
+from .problem import (CAMERA_STRIDE, ControlPointConstraint, ControlPointUncertainty, Gauge, GaugePolicy,
+                      Problem)
 
 
 def look_at_rotation(centre: np.ndarray, target: np.ndarray, up=(0.0, 0.0, 1.0)) -> np.ndarray:
@@ -327,3 +328,35 @@ def window_problems(n_windows: int = 256, seed: int = 1234, cameras=(10, 60), po
 def with_gauge(problem: Problem, policy=GaugePolicy.AutoAnchor) -> Problem:
     problem.gauge = Gauge(policy=policy)
     return problem
+
+
+def with_control_points(problem: Problem, n: int = 12, sigma: float = 0.02, seed: int = 0,
+                        kinds=(0, 1, 2), weights=(1.0, 0.5, 2.0)) -> Problem:
+    """Survey control points on `n` tracks seen by two distinct cameras: the true point plus
+    Gaussian noise (0.1 sigma on every other target, so that both Huber branches occur), with
+    the uncertainty cycling through isotropic sigma, a correlated covariance and the matching
+    upper-triangular square-root information (kinds 0, 1, 2)."""
+    rng = np.random.default_rng(seed)
+    off = np.asarray(problem.track_offsets)
+    cams = np.asarray(problem.obs_camera)
+    eligible = [t for t in range(problem.n_tracks) if np.unique(cams[off[t]:off[t + 1]]).size >= 2]
+    pick = np.sort(rng.choice(np.array(eligible), size=min(n, len(eligible)), replace=False))
+    truth = getattr(problem, "truth_points", None)
+    truth = problem.points if truth is None else truth
+    cps = []
+    for i, t in enumerate(pick):
+        scale = sigma * (0.1 if i % 2 else 1.0)
+        target = truth[t] + rng.normal(0.0, scale, 3)
+        kind = kinds[i % len(kinds)]
+        B = rng.normal(0.0, 0.4, (3, 3))
+        cov = sigma * sigma * (np.eye(3) + B @ B.T)
+        c = ControlPointConstraint(point=tuple(target), sigmaMeters=sigma, weight=weights[i % len(weights)],
+                                   uncertainty=ControlPointUncertainty(kind))
+        if kind == 1:
+            c.uncertaintyMatrix = tuple(cov.reshape(9))
+        elif kind == 2:
+            c.uncertaintyMatrix = tuple(np.linalg.cholesky(np.linalg.inv(cov)).T.reshape(9))
+        cps.append((int(t), c))
+    problem.controlPoints = cps
+    return problem
+

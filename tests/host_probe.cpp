@@ -153,3 +153,29 @@ extern "C" int probe_chunks(const pb_problem_desc* pr, const pb_solve_options* o
     }
     return 0;
 }
+
+// Host model of a problem: status, message, and the gauge the host settled on.
+// out_i: [status, ref_param, n_fixed_cams, gauge_anchor, gauge_scale, n_control_points kept,
+//         camera_blocks]; fixed: the fixed cameras (n_cameras capacity); out_d: [gauge_baseline]
+extern "C" int probe_model(const pb_problem_desc* pr, const pb_solve_options* op, int* out_i, int* fixed,
+                           double* out_d) {
+    using namespace pb;
+    HostModel m;
+    std::string err;
+    const int rc = build_host_model(pr, op, &m, &err);
+    g_msg = err;
+    out_i[0] = rc;
+    if (rc) return rc;
+    out_i[1] = m.ref_param ? 1 : 0;
+    out_i[2] = static_cast<int>(m.fixed_cams.size());
+    out_i[3] = m.gauge_anchor;
+    out_i[4] = m.gauge_scale;
+    out_i[5] = static_cast<int>(m.cp_track.size());
+    out_i[6] = m.ncb;
+    for (size_t i = 0; i < m.fixed_cams.size(); ++i) fixed[i] = m.fixed_cams[i];
+    out_d[0] = m.gauge_baseline;
+    return 0;
+}
+
+// The host's control-point validation and whitening of one record.
+extern "C" int probe_cp_whitening(const double* rec, double* W) { return pb::cp_valid(rec, W) ? 1 : 0; }

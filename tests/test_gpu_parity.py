@@ -62,7 +62,19 @@ def index_map(ctx, orc):
     return np.array(idx)
 
 
-CASES = [("ring", ring, ring_options), ("aerial", aerial, aerial_options)]
+def ring_gcp():
+    """The ring with ten survey targets (sigma 2 cm, the three uncertainty forms): complete
+    control-point gauge, plain parameterisation, Huber control-point terms in both branches."""
+    return synth.with_control_points(ring(), n=10, seed=2)
+
+
+def aerial_gcp():
+    """The aerial block with 16 ground control points and shared intrinsics refined."""
+    return synth.with_control_points(aerial(), n=16, seed=4)
+
+
+CASES = [("ring", ring, ring_options), ("aerial", aerial, aerial_options), ("ring_gcp", ring_gcp, ring_options),
+         ("aerial_gcp", aerial_gcp, aerial_options)]
 
 
 @pytest.mark.parametrize("name,make,opts", CASES)
@@ -275,3 +287,20 @@ def test_parity_report_of_the_public_solve(name, make, opts):
     assert c.terminationStatusMatches
     assert c.equivalent, (c.maximumCameraCenterDifferenceMeters, c.maximumCameraRotationDifferenceDegrees,
                           c.maximumPointDifferenceMeters, c.rmsAfterDifference)
+    if p.controlPoints:
+        # control-point statistics of the result (BundleAdjustQuality.cpp:179-211, :282-289)
+        q = got.quality
+        assert q.controlPointConstraintCount == sum(1 for t, _ in p.controlPoints if ref["valid"][t])
+        assert q.controlPointRmsAfterMeters < q.controlPointRmsBeforeMeters
+        assert not got.qualityGateRejected
+
+
+def test_backward_pass_rejects_control_point_problems():
+    """The exact-Hessian adjoint is written for the charts of image-only problems; a problem with
+    control points (plain parameterisation) is refused with an unsupported status."""
+    p = ring_gcp()
+    ctx = gpu(p, ring_options())
+    ctx.solve()
+    g = np.zeros((p.n_cameras, 6))
+    with pytest.raises(RuntimeError, match="image-only"):
+        ctx.backward(grad_cameras=g)

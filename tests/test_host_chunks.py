@@ -21,18 +21,8 @@ SMEM_BUDGET = 227 * 1024 - 1024
 
 
 @pytest.fixture(scope="module")
-def probe(tmp_path_factory):
-    out = str(tmp_path_factory.mktemp("probe") / "libhostprobe.so")
-    cmd = ["g++", "-std=c++17", "-O1", "-fPIC", "-shared", "-pthread", "-I", os.path.join(ROOT, "include"),
-           os.path.join(HERE, "host_probe.cpp"), os.path.join(ROOT, "plabundle_gb300", "csrc", "pb_host.cpp"),
-           "-o", out]
-    subprocess.run(cmd, check=True, capture_output=True)
-    L = C.CDLL(out)
-    L.probe_chunks.argtypes = [C.POINTER(native.ProblemDesc), C.POINTER(native.SolveOptionsC), C.c_int,
-                               C.c_size_t, C.POINTER(C.c_longlong)]
-    L.probe_chunks.restype = C.c_int
-    L.probe_message.restype = C.c_char_p
-    return L
+def probe(host_probe):
+    return host_probe
 
 
 def run_probe(L, problem, options, precision):
