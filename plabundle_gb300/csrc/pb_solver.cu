@@ -616,12 +616,21 @@ int solve_block_jacobi(pb_gpu_ctx* c, double rel, double abs_tol, int max_it, bo
     return 0;
 }
 
+// Automatic choice of the reduced solver: the dense-factor preconditioned CG while the factor
+// fits comfortably (FP32 factor and inverse: 2 n^2 x 4 B, 8.6 GB at n = 32768; the FP64 path's
+// factor costs 2n^3/3 FP64 flops every iteration, so it stops at n = 16384), block-Jacobi PCG
+// beyond.  Both solve to the same relative residual; the preconditioner only sets the iteration
+// count (block-Jacobi needs thousands per LM iteration on a 3 000-camera block).
+bool dense_solver_fits(int n, int precision) { return n <= (precision == PB_PRECISION_MIXED ? 32768 : 16384); }
+
 int solve_reduced(pb_gpu_ctx* c, const pb_solve_options& op, bool* converged, int* iterations, double* relres,
                   int* sweeps) {
     const double rel = op.linear_relative_tolerance > 0 ? op.linear_relative_tolerance : 2.0e-10;
     const double abs_tol = op.linear_absolute_tolerance > 0 ? op.linear_absolute_tolerance : 1.0e-12;
     const int max_it = op.max_linear_iterations > 0 ? op.max_linear_iterations : std::max(200, 30 * c->model.P);
-    const int solver = (op.linear_solver == 1 || op.linear_solver == 2) ? op.linear_solver : (c->S[0].n <= 16384 ? 1 : 2);
+    const int solver = (op.linear_solver == 1 || op.linear_solver == 2)
+                           ? op.linear_solver
+                           : (dense_solver_fits(c->S[0].n, c->last_precision) ? 1 : 2);
     c->last_solver = solver;
     *converged = false;
     *iterations = 0;
@@ -1535,7 +1544,7 @@ pb_status adjoint_core(pb_gpu_ctx* c, int newton, pb_adjoint_report* rep, float*
     const int max_it = std::max(400, 30 * m.P);
     int rc;
     c->f32_age = -1;
-    if (n > 16384) {
+    if (!dense_solver_fits(n, c->last_precision)) {
         rc = solve_block_jacobi(c, rel, abs_tol, max_it, &conv, &it, &rr);
     } else if (c->last_precision == PB_PRECISION_MIXED) {
         rc = solve_dense<float>(c, rel, abs_tol, max_it, &conv, &it, &rr);
