@@ -34,7 +34,8 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="aerial", choices=["aerial", "aerial_gcp", "ring", "windows", "adjoint"])
+    ap.add_argument("--workload", default="aerial",
+                    choices=["aerial", "aerial_gcp", "aerial3000_gcp", "ring", "windows", "adjoint"])
     ap.add_argument("--windows", type=int, default=256, help="local-BA windows of the windows workload")
     ap.add_argument("--workers", type=int, default=8, help="worker contexts of the windows workload")
     ap.add_argument("--cpu-iterations", type=int, default=2,
@@ -62,8 +63,13 @@ def workload(name):
     from plabundle_gb300 import synth
     from plabundle_gb300.problem import ImageRobustLoss, SolveOptions
     opts = SolveOptions()
-    if name in ("aerial", "aerial_gcp"):
-        prob = synth.aerial_grid_problem(seed=11)
+    if name in ("aerial", "aerial_gcp", "aerial3000_gcp"):
+        if name == "aerial3000_gcp":
+            # the 3 000-camera block of the large survey configuration (60 x 50 nadir grid,
+            # 1.5 M points, ~10 M observations) without rigs or scale bars
+            prob = synth.aerial_grid_problem(seed=21, n_along=60, n_lines=50, n_points=1_500_000)
+        else:
+            prob = synth.aerial_grid_problem(seed=11)
         opts.solver.imageRobustLoss = ImageRobustLoss.Cauchy
         opts.solver.imageRobustLossScalePixels = 1.5
         opts.calibration.refineSharedFocalLength = True
@@ -71,15 +77,16 @@ def workload(name):
         opts.calibration.refineSharedRadialDistortion = True
         # time to converge: the solve runs until the reference's stopping rule (step RMS <= 1e-6)
         opts.solver.maxIterations = 200
-        cfg = {"workload": "aerial_grid_500cam_200kpt", "cameras": prob.n_cameras, "tracks": prob.n_tracks,
+        cfg = {"workload": "aerial_grid_%dcam_%dkpt" % (prob.n_cameras, round(prob.n_tracks / 1000)),
+               "cameras": prob.n_cameras, "tracks": prob.n_tracks,
                "observations": prob.n_obs, "calibration_groups": 2, "loss": "cauchy_1.5px",
                "refined_intrinsics": "f, cx, cy, k1, k2, k3, p1, p2",
                "max_lm_iterations": opts.solver.maxIterations, "stopping": "step RMS <= 1e-6 (converged)"}
-        if name == "aerial_gcp":
+        if name in ("aerial_gcp", "aerial3000_gcp"):
             # 40 ground control points on tracks seen by two cameras (2 cm, three uncertainty forms):
             # complete control-point gauge, plain parameterisation
             synth.with_control_points(prob, n=40, sigma=0.02, seed=3)
-            cfg.update(workload="aerial_grid_500cam_200kpt_40gcp", control_points=len(prob.controlPoints))
+            cfg.update(workload=cfg["workload"] + "_40gcp", control_points=len(prob.controlPoints))
     else:
         prob = synth.ring_problem(seed=7)
         opts.solver.imageRobustLoss = ImageRobustLoss.Huber

@@ -3,16 +3,19 @@
 //
 // One CTA of 256 threads per chunk of consecutive tracks (host-built: at most max_obs <= 256
 // observations and max_tracks tracks), one thread per observation in phases A-C:
-//   A. linearise the observation: FP64 residual, robust weight and cost; Jacobians A = [J_pose |
-//      J_intr] and Jp in T (FP32 on the mixed path);
+//   A. linearise the observation: residual, robust weight and gradient in FP64 with the cost on
+//      the FP64 path, in float-float without the cost on the mixed path (FP64 runs at a small
+//      fraction of the FP32 rate on this part; the LM takes the mixed path's FP64 cost from the
+//      line search); Jacobians A = [J_pose | J_intr] and Jp in T (FP32 on the mixed path);
 //   B. per track, V = sum w Jp^T Jp and the point gradient in FP64 and the factor V = R R^T
 //      (the 3x3 point block inverse of BundleAdjustPlaMatrixReferenceSchur.cpp:350-490);
 //   C. per observation, in FP64: Y = w Jp R^-T (2x3), the reduced weight M = w I - Y Y^T and Y q
 //      (q = R^-1 g_p); then G = J_pose^T Y.  The matrix derives from the rounded Jacobians only,
 //      so it is the exact Schur complement of one consistently perturbed linearisation (the
 //      FP32 rounding of a Jacobian perturbs the weakest mode of S by ~eps*sqrt(cond), rounding
-//      S itself by eps*cond).  The gradient g = -J^T w r is FP64-accurate (see linearize_obs):
-//      the rounded Jacobians shape the step, never the fixed point;
+//      S itself by eps*cond).  The gradient g = -J^T w r does not carry the Jacobians' rounding
+//      (FP64 or float-float, see linearize_obs / linearize_obs_ff): the rounded Jacobians shape
+//      the step, never the fixed point;
 //   K. per track and calibration group, K = sum over the group's observations of J_intr^T Y;
 //   D. every output element of the chunk is owned by one thread, which gathers its terms in a
 //      fixed order into compensated accumulators and writes the chunk partial once:
@@ -26,6 +29,8 @@
 // residuals, two-sum accumulation): ~44 significant bits on the FP32 pipe, enough for reduced
 // matrices of condition ~1e9, where FP32 products alone leave the weakest modes indefinite.
 #include <cuda_runtime.h>
+
+#include <type_traits>
 
 #include "pb_device.cuh"
 #include "pb_kernels.h"
@@ -63,7 +68,7 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
     const int sA = chunk_stride(2 * nA), sG = chunk_stride(18), sY = chunk_stride(6), sM = chunk_stride(6),
               sD = chunk_stride(nA);
     char* ptr = smem;
-    double* s_V = carve<double>(ptr, static_cast<size_t>(MO) * 9);
+    double* s_V = carve<double>(ptr, static_cast<size_t>(MO) * 9);  // point normal terms, then the track factor
     T* s_A = carve<T>(ptr, static_cast<size_t>(MO) * sA);
     VT* s_G = carve<VT>(ptr, static_cast<size_t>(MO) * sG);
     VT* s_Y = carve<VT>(ptr, static_cast<size_t>(MO) * sY);
@@ -90,8 +95,67 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
     Lin<T> L;
     double grad[9 + kMaxNI];
     double cost = 0.0;
+    double w64 = 0.0;  // normal weight (FP64 value of the float-float weight on the mixed path)
+    T jpT[6];          // point Jacobian of the arithmetic type
     int first = 0, k = 0;
     bool elim = false, ok = false;
+    constexpr bool kMixed = std::is_same<T, float>::value;
+    if constexpr (kMixed) {
+    if (active) {
+        // mixed path: float-float linearisation (no cost: the LM takes it from the line search)
+        const int cam = D.obs_cam[o];
+        const int trk = D.obs_trk[o];
+        const int tb0 = D.trk_obs_begin[trk];
+        first = tb0 - obs0;
+        k = D.trk_obs_begin[trk + 1] - tb0;
+        elim = D.trk_block[trk] >= 0;
+        const int grp = ng > 0 ? D.cam_group[cam] : -1;
+        const bool tangent = cam == S.gauge_scale && S.gauge_anchor >= 0 && S.gauge_baseline > 0.0;
+        const float2* of = D.obs_ff + static_cast<size_t>(o) * 3;
+        LinFF F;
+        ok = linearize_obs_ff(D.cams_ff + static_cast<size_t>(cam) * kCamFF, D.points_ff + static_cast<size_t>(trk) * 3,
+                              ffl(D.pscale_ff[trk]), ffl(of[0]), ffl(of[1]), ffl(of[2]), S.loss,
+                              ff{S.loss_scale_hi, S.loss_scale_lo}, tangent, !S.ref_param, D.gauge_basis, ni,
+                              S.int_cols, F);
+        if (!ok) atomicOr(s_flags, 2);
+        s_info[tid] = (ok ? kOk : 0) | (elim ? kElim : 0) | ((grp + 1) << 2);
+        T* A = s_A + static_cast<size_t>(tid) * sA;
+        for (int a = 0; a < 6; ++a) {
+            A[a] = ok ? F.Jc[a] : T(0);
+            A[nA + a] = ok ? F.Jc[6 + a] : T(0);
+        }
+        for (int a = 0; a < ni; ++a) {
+            A[6 + a] = ok ? F.Ji[a] : T(0);
+            A[nA + 6 + a] = ok ? F.Ji[kMaxNI + a] : T(0);
+        }
+        VT* Dg = s_D + static_cast<size_t>(tid) * sD;
+        {
+            for (int a = 0; a < 6; ++a) Dg[a] = ok ? F.g[a] : Val::zero();
+            for (int a = 0; a < ni; ++a) Dg[6 + a] = ok ? F.g[9 + a] : Val::zero();
+            // the point block, its factor and the projector of phases B and C stay in FP64: the
+            // reduced weight M = w I - Y Y^T cancels to a small fraction of w, and the weakest modes
+            // of the reduced matrix need its FP64 rounding
+            double* V = s_V + static_cast<size_t>(tid) * 9;
+            w64 = static_cast<double>(F.w.hi) + static_cast<double>(F.w.lo);
+            for (int i = 0; i < 6; ++i) jpT[i] = F.Jp[i];
+            if (elim && ok) {
+                // V_o = w Jp^T Jp from the rounded Jacobian and the point gradient
+                const double w = w64;
+                const double j0 = F.Jp[0], j1 = F.Jp[1], j2 = F.Jp[2], j3 = F.Jp[3], j4 = F.Jp[4], j5 = F.Jp[5];
+                V[0] = w * (j0 * j0 + j3 * j3);
+                V[1] = w * (j0 * j1 + j3 * j4);
+                V[2] = w * (j0 * j2 + j3 * j5);
+                V[3] = w * (j1 * j1 + j4 * j4);
+                V[4] = w * (j1 * j2 + j4 * j5);
+                V[5] = w * (j2 * j2 + j5 * j5);
+                for (int i = 0; i < 3; ++i)
+                    V[6 + i] = static_cast<double>(F.g[6 + i].hi) + static_cast<double>(F.g[6 + i].lo);
+            } else {
+                for (int i = 0; i < 9; ++i) V[i] = 0.0;
+            }
+        }
+    }
+    } else {
     if (active) {
         const int cam = D.obs_cam[o];
         const int trk = D.obs_trk[o];
@@ -126,8 +190,11 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
         for (int a = 0; a < 6; ++a) Dg[a] = ok ? Val::make(grad[a]) : Val::zero();
         for (int a = 0; a < ni; ++a) Dg[6 + a] = ok ? Val::make(grad[9 + a]) : Val::zero();
         double* V = s_V + static_cast<size_t>(tid) * 9;
+        if constexpr (!kMixed) {
+        w64 = L.wd;
+        for (int i = 0; i < 6; ++i) jpT[i] = L.Jp[i];
         if (elim && ok) {
-            // V_o = w Jp^T Jp from the (rounded) Jacobian and the point gradient, in FP64
+            // V_o = w Jp^T Jp from the Jacobian and the point gradient, in FP64
             const double w = L.wd;
             const double j0 = L.Jp[0], j1 = L.Jp[1], j2 = L.Jp[2], j3 = L.Jp[3], j4 = L.Jp[4], j5 = L.Jp[5];
             V[0] = w * (j0 * j0 + j3 * j3);
@@ -142,6 +209,8 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
         } else {
             for (int i = 0; i < 9; ++i) V[i] = 0.0;
         }
+        }
+    }
     }
     // chunk-local track slots: rank of each track's first observation among the chunk's
     // track starts (all lanes of every warp take part: blockDim is a multiple of 32)
@@ -256,35 +325,39 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
         VT* Ys = s_Y + static_cast<size_t>(tid) * sY;
         VT* Mo = s_M + static_cast<size_t>(tid) * sM;
         if (ok) {
-            const double w = L.wd;
-            double Y[2][3] = {{0, 0, 0}, {0, 0, 0}}, q[3] = {0, 0, 0};
-            if (elim) {
-                const double* st = s_V + static_cast<size_t>(first) * 9;
-                const double i00 = st[0], i10 = st[1], i11 = st[2], i20 = st[3], i21 = st[4], i22 = st[5];
-                q[0] = st[6]; q[1] = st[7]; q[2] = st[8];
-                for (int pa = 0; pa < 2; ++pa) {
-                    const double p0 = L.Jp[pa * 3], p1 = L.Jp[pa * 3 + 1], p2 = L.Jp[pa * 3 + 2];
-                    Y[pa][0] = w * (i00 * p0);
-                    Y[pa][1] = w * (i10 * p0 + i11 * p1);
-                    Y[pa][2] = w * (i20 * p0 + i21 * p1 + i22 * p2);
-                }
-            }
-            Mo[0] = Val::make(w - (Y[0][0] * Y[0][0] + Y[0][1] * Y[0][1] + Y[0][2] * Y[0][2]));
-            Mo[1] = Val::make(-(Y[0][0] * Y[1][0] + Y[0][1] * Y[1][1] + Y[0][2] * Y[1][2]));
-            Mo[2] = Val::make(w - (Y[1][0] * Y[1][0] + Y[1][1] * Y[1][1] + Y[1][2] * Y[1][2]));
-            Mo[3] = Val::make(Y[0][0] * q[0] + Y[0][1] * q[1] + Y[0][2] * q[2]);
-            Mo[4] = Val::make(Y[1][0] * q[0] + Y[1][1] * q[1] + Y[1][2] * q[2]);
-            Mo[5] = Val::make(w);
             VT y[6];
-            for (int i = 0; i < 6; ++i) {
-                y[i] = Val::make(Y[i / 3][i % 3]);
-                Ys[i] = y[i];
+            {
+                // FP64 from the rounded Jacobian and the weight of phase A
+                const double w = w64;
+                double Y[2][3] = {{0, 0, 0}, {0, 0, 0}}, q[3] = {0, 0, 0};
+                if (elim) {
+                    const double* st = s_V + static_cast<size_t>(first) * 9;
+                    const double i00 = st[0], i10 = st[1], i11 = st[2], i20 = st[3], i21 = st[4], i22 = st[5];
+                    q[0] = st[6]; q[1] = st[7]; q[2] = st[8];
+                    for (int pa = 0; pa < 2; ++pa) {
+                        const double p0 = jpT[pa * 3], p1 = jpT[pa * 3 + 1], p2 = jpT[pa * 3 + 2];
+                        Y[pa][0] = w * (i00 * p0);
+                        Y[pa][1] = w * (i10 * p0 + i11 * p1);
+                        Y[pa][2] = w * (i20 * p0 + i21 * p1 + i22 * p2);
+                    }
+                }
+                Mo[0] = Val::make(w - (Y[0][0] * Y[0][0] + Y[0][1] * Y[0][1] + Y[0][2] * Y[0][2]));
+                Mo[1] = Val::make(-(Y[0][0] * Y[1][0] + Y[0][1] * Y[1][1] + Y[0][2] * Y[1][2]));
+                Mo[2] = Val::make(w - (Y[1][0] * Y[1][0] + Y[1][1] * Y[1][1] + Y[1][2] * Y[1][2]));
+                Mo[3] = Val::make(Y[0][0] * q[0] + Y[0][1] * q[1] + Y[0][2] * q[2]);
+                Mo[4] = Val::make(Y[1][0] * q[0] + Y[1][1] * q[1] + Y[1][2] * q[2]);
+                Mo[5] = Val::make(w);
+                for (int i = 0; i < 6; ++i) y[i] = Val::make(Y[i / 3][i % 3]);
             }
+            for (int i = 0; i < 6; ++i) Ys[i] = y[i];
             const T* A = s_A + static_cast<size_t>(tid) * sA;
             // back-substitution record of the observation: A rows, then Y
             T* rec = O.obs_rec + static_cast<size_t>(o) * (2 * nA + 6);
             for (int i = 0; i < 2 * nA; ++i) rec[i] = A[i];
-            for (int i = 0; i < 6; ++i) rec[2 * nA + i] = static_cast<T>(Y[i / 3][i % 3]);
+            for (int i = 0; i < 6; ++i) {
+                if constexpr (kMixed) rec[2 * nA + i] = y[i].hi;  // RN of the FP64 value
+                else rec[2 * nA + i] = y[i];
+            }
             for (int a = 0; a < 6; ++a) {
                 const T ja0 = A[a], ja1 = A[nA + a];
                 G[a * 3 + 0] = ja0 * y[0] + ja1 * y[3];
@@ -300,7 +373,6 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
         }
     }
     __syncthreads();
-
     // ---- K: per track and group, K[(g, c), k] = sum_(o in track, group g) (J_intr^T Y)[c, k]
     if (nb > 0) {
         const int per = nb * 3;

@@ -450,4 +450,201 @@ __device__ __forceinline__ float warp_sum(float v) {
     return v;
 }
 
+// ---------------------------------------------------------------- float-float linearisation
+// The mixed path's linearisation in float-float arithmetic.  FP64 runs at a small fraction of the
+// FP32 rate on this part, and the projection, robust weight and gradient of every observation
+// were the FP64-bound share of the assembly.  Here they run on the FP32 pipe with ~44 significant
+// bits: the residual keeps ~1e-10 px absolute accuracy, enough for the gradient that decides the
+// fixed point.  The reciprocal and reciprocal square root take one Newton-Raphson step from the
+// FP32 hardware approximation, with the correction term evaluated in float-float (the
+// double-word division scheme of Joldes, Muller and Popescu, "Tight and rigorous error bounds for
+// basic building blocks of double-word arithmetic", ACM TOMS 2017).  Inputs are float-float
+// copies of the effective cameras, points, point scales and observations, written when the FP64
+// state changes.
+
+__host__ __device__ __forceinline__ float2 ff_pack(double d) {
+    const float h = static_cast<float>(d);
+    return make_float2(h, static_cast<float>(d - static_cast<double>(h)));
+}
+__device__ __forceinline__ ff ffl(float2 v) { return {v.x, v.y}; }
+__device__ __forceinline__ ff ff_sub(ff a, ff b) { return a + (-b); }
+__device__ __forceinline__ ff ff_twice(ff a) { return {2.f * a.hi, 2.f * a.lo}; }  // exact
+__device__ __forceinline__ ff ff_one() { return {1.f, 0.f}; }
+__device__ __forceinline__ bool ff_le(ff a, ff b) { return a.hi < b.hi || (a.hi == b.hi && a.lo <= b.lo); }
+
+// 1 / a: r = RN(1 / a.hi), then r + r (1 - a r) with the residual 1 - a r in float-float.
+__device__ __forceinline__ ff ff_recip(ff a) {
+    const float r = __frcp_rn(a.hi);
+    const ff e = ff_sub(ff_one(), r * a);
+    return ff_norm(r, __fmul_rn(r, e.hi));
+}
+// 1 / sqrt(a), a > 0: y = rsqrt(a.hi), then y + y (1 - a y^2) / 2 with the residual in float-float.
+__device__ __forceinline__ ff ff_rsqrt(ff a) {
+    const float y = rsqrtf(a.hi);
+    const ff e = ff_sub(ff_one(), a * two_prod(y, y));
+    return ff_norm(y, __fmul_rn(0.5f * y, e.hi));
+}
+
+// Float-float camera record: R (9), C (3), fx, fy, cx, cy, k1, k2, k3, p1, p2 (11), then the
+// signs su, sv and the depth flip as plain floats.
+constexpr int kCamFF = 24;
+__host__ __device__ __forceinline__ void camera_ff(const double* c, float2* out) {
+    for (int i = 0; i < 21; ++i) out[i] = ff_pack(c[i]);
+    out[21] = make_float2(c[21] < 0.0 ? -1.f : 1.f, 0.f);
+    out[22] = make_float2(c[22] < 0.0 ? -1.f : 1.f, 0.f);
+    out[23] = make_float2(c[23] != 0.0 ? 1.f : 0.f, 0.f);
+}
+
+struct LinFF {
+    float Jc[12];          // 2x6 pose Jacobian (FP32)
+    float Jp[6];           // 2x3 point Jacobian, scaled (FP32)
+    float Ji[2 * kMaxNI];  // 2 x ni intrinsic Jacobian (FP32)
+    ff r0, r1, w;          // residual and normal weight
+    ff g[9 + kMaxNI];      // -J^T w r: pose [0, 6), point [6, 9), intrinsic [9, 9 + ni)
+};
+
+// Intrinsic Jacobian column `col` (as intrinsic_column) in float-float.
+__device__ __forceinline__ void intrinsic_column_ff(int col, ff x, ff y, ff r2, ff xd, ff yd, float su, float sv,
+                                                    ff sfx, ff sfy, ff aspect, ff& ju, ff& jv) {
+    const ff z = {0.f, 0.f};
+    ju = z;
+    jv = z;
+    switch (col) {
+        case 0: ju = su * xd; jv = (sv * yd) * aspect; break;
+        case 1: jv = sfy * yd; break;
+        case 2: ju = ff_one(); break;
+        case 3: jv = ff_one(); break;
+        case 4: ju = sfx * (x * r2); jv = sfy * (y * r2); break;
+        case 5: { const ff r4 = r2 * r2; ju = sfx * (x * r4); jv = sfy * (y * r4); break; }
+        case 6: { const ff r6 = r2 * r2 * r2; ju = sfx * (x * r6); jv = sfy * (y * r6); break; }
+        case 7: ju = sfx * ff_twice(x * y); jv = sfy * (r2 + ff_twice(y * y)); break;
+        case 8: ju = sfx * (r2 + ff_twice(x * x)); jv = sfy * ff_twice(x * y); break;
+        default: break;
+    }
+}
+
+// linearize_obs of the mixed path (same Jacobian columns, same robust weight), with the
+// gradient -J^T w r in float-float and no cost.  cam: kCamFF values; X: the point; s: its step
+// scale; gb: the FP64 gauge tangent basis (read for the tangent camera only).
+__device__ __forceinline__ bool linearize_obs_ff(const float2* __restrict__ cam, const float2* __restrict__ X, ff s,
+                                                 ff u, ff v, ff wobs, int loss, ff lscale, bool tangent, bool plain,
+                                                 const double* __restrict__ gb, int ni, const int* __restrict__ cols,
+                                                 LinFF& L) {
+    ff R[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) R[i] = ffl(cam[i]);
+    const ff d0 = ff_sub(ffl(X[0]), ffl(cam[9])), d1 = ff_sub(ffl(X[1]), ffl(cam[10])),
+             d2 = ff_sub(ffl(X[2]), ffl(cam[11]));
+    const ff xc = R[0] * d0 + R[3] * d1 + R[6] * d2;
+    const ff yc = R[1] * d0 + R[4] * d1 + R[7] * d2;
+    const ff zc = R[2] * d0 + R[5] * d1 + R[8] * d2;
+    const float fwd = cam[23].x != 0.f ? -(zc.hi + zc.lo) : zc.hi + zc.lo;
+    if (!(fwd > 1e-9f)) return false;
+    const ff iz = ff_recip(zc);
+    const ff x = xc * iz, y = yc * iz;
+    const ff r2 = x * x + y * y;
+    const ff k1 = ffl(cam[16]), k2 = ffl(cam[17]), k3 = ffl(cam[18]), p1 = ffl(cam[19]), p2 = ffl(cam[20]);
+    const ff radial = ff_one() + r2 * (k1 + r2 * (k2 + r2 * k3));
+    const ff xy2 = ff_twice(x * y);
+    const ff xd = x * radial + p1 * xy2 + p2 * (r2 + ff_twice(x * x));
+    const ff yd = y * radial + p1 * (r2 + ff_twice(y * y)) + p2 * xy2;
+    const float su = cam[21].x, sv = cam[22].x;
+    const ff fx = ffl(cam[12]), fy = ffl(cam[13]);
+    const ff sfx = su * fx, sfy = sv * fy;
+    const ff px = sfx * xd + ffl(cam[14]);
+    const ff py = sfy * yd + ffl(cam[15]);
+    if (!isfinite(px.hi) || !isfinite(py.hi)) return false;
+    const ff r0 = ff_sub(px, u), r1 = ff_sub(py, v);
+    // evaluateImageRobustLoss weight (BundleAdjustPlaMatrixProjection.cpp:75-109)
+    const ff sq = wobs * (r0 * r0 + r1 * r1);
+    if (!(sq.hi >= 0.f) || !isfinite(sq.hi)) return false;
+    ff rw = ff_one();
+    if (loss == 1) {
+        if (!ff_le(sq, lscale * lscale)) rw = lscale * ff_rsqrt(sq);
+    } else if (loss == 2) {
+        const ff c2 = lscale * lscale;
+        rw = c2 * ff_recip(c2 + sq);
+    }
+    const ff w = wobs * rw;
+    if (!isfinite(w.hi)) return false;
+    L.r0 = r0;
+    L.r1 = r1;
+    L.w = w;
+    // FP32 Jacobians from the leading parts (the formulas of linearize_obs)
+    const float fx_ = x.hi, fy_ = y.hi, fr2 = r2.hi, frad = radial.hi;
+    const float fk1 = k1.hi, fk2 = k2.hi, fk3 = k3.hi, fp1 = p1.hi, fp2 = p2.hi;
+    const float fsfx = sfx.hi, fsfy = sfy.hi, fiz = iz.hi;
+    const float dr = fk1 + fr2 * (2.f * fk2 + 3.f * fk3 * fr2);
+    const float dxd_dx = frad + 2.f * fx_ * fx_ * dr + 2.f * fp1 * fy_ + 6.f * fp2 * fx_;
+    const float dxd_dy = 2.f * fx_ * fy_ * dr + 2.f * fp1 * fx_ + 2.f * fp2 * fy_;
+    const float dyd_dy = frad + 2.f * fy_ * fy_ * dr + 6.f * fp1 * fy_ + 2.f * fp2 * fx_;
+    const float du_dx = fsfx * dxd_dx, du_dy = fsfx * dxd_dy, dv_dx = fsfy * dxd_dy, dv_dy = fsfy * dyd_dy;
+    const float dc[6] = {du_dx * fiz, du_dy * fiz, -(du_dx * fx_ + du_dy * fy_) * fiz,
+                         dv_dx * fiz, dv_dy * fiz, -(dv_dx * fx_ + dv_dy * fy_) * fiz};
+    const float fd0 = d0.hi, fd1 = d1.hi, fd2 = d2.hi, fs = s.hi;
+    const float rs0 = plain ? -1.f : 1.f;
+#pragma unroll
+    for (int pa = 0; pa < 2; ++pa) {
+        const float jw0 = dc[pa * 3] * R[0].hi + dc[pa * 3 + 1] * R[1].hi + dc[pa * 3 + 2] * R[2].hi;
+        const float jw1 = dc[pa * 3] * R[3].hi + dc[pa * 3 + 1] * R[4].hi + dc[pa * 3 + 2] * R[5].hi;
+        const float jw2 = dc[pa * 3] * R[6].hi + dc[pa * 3 + 1] * R[7].hi + dc[pa * 3 + 2] * R[8].hi;
+        L.Jc[pa * 6 + 0] = rs0 * (jw2 * fd1 - jw1 * fd2);
+        L.Jc[pa * 6 + 1] = jw2 * fd0 - jw0 * fd2;
+        L.Jc[pa * 6 + 2] = jw0 * fd1 - jw1 * fd0;
+        if (tangent) {
+            L.Jc[pa * 6 + 3] = -(jw0 * static_cast<float>(gb[0]) + jw1 * static_cast<float>(gb[1]) +
+                                 jw2 * static_cast<float>(gb[2]));
+            L.Jc[pa * 6 + 4] = -(jw0 * static_cast<float>(gb[3]) + jw1 * static_cast<float>(gb[4]) +
+                                 jw2 * static_cast<float>(gb[5]));
+            L.Jc[pa * 6 + 5] = 0.f;
+        } else {
+            L.Jc[pa * 6 + 3] = -jw0;
+            L.Jc[pa * 6 + 4] = -jw1;
+            L.Jc[pa * 6 + 5] = -jw2;
+        }
+        L.Jp[pa * 3 + 0] = jw0 * fs;
+        L.Jp[pa * 3 + 1] = jw1 * fs;
+        L.Jp[pa * 3 + 2] = jw2 * fs;
+    }
+    const ff aspect = fx.hi > 0.f ? fy * ff_recip(fx) : ff_one();
+    for (int k = 0; k < ni; ++k)
+        intrinsic_column<float>(cols[k], fx_, fy_, fr2, xd.hi, yd.hi, su, sv, fsfx, fsfy, aspect.hi, L.Ji[k],
+                                L.Ji[kMaxNI + k]);
+    // gradient -J^T (w r) through v = R (dpi/dx_c)^T (w r), in float-float
+    const ff wr0 = w * r0, wr1 = w * r1;
+    const ff gdr = k1 + r2 * (ff_twice(k2) + 3.f * (k3 * r2));
+    const ff gxx = radial + ff_twice(x * x) * gdr + ff_twice(p1 * y) + 6.f * (p2 * x);
+    const ff gxy = ff_twice(x * y) * gdr + ff_twice(p1 * x) + ff_twice(p2 * y);
+    const ff gyy = radial + ff_twice(y * y) * gdr + 6.f * (p1 * y) + ff_twice(p2 * x);
+    const ff a0 = sfx * wr0, a1 = sfy * wr1;
+    const ff tx = (a0 * gxx + a1 * gxy) * iz;
+    const ff ty = (a0 * gxy + a1 * gyy) * iz;
+    const ff tz = -(tx * x + ty * y);
+    const ff v0 = R[0] * tx + R[1] * ty + R[2] * tz;
+    const ff v1 = R[3] * tx + R[4] * ty + R[5] * tz;
+    const ff v2 = R[6] * tx + R[7] * ty + R[8] * tz;
+    const ff g0 = ff_sub(v2 * d1, v1 * d2);
+    L.g[0] = plain ? g0 : -g0;
+    L.g[1] = -ff_sub(v2 * d0, v0 * d2);
+    L.g[2] = -ff_sub(v0 * d1, v1 * d0);
+    if (tangent) {
+        L.g[3] = v0 * ff_make(gb[0]) + v1 * ff_make(gb[1]) + v2 * ff_make(gb[2]);
+        L.g[4] = v0 * ff_make(gb[3]) + v1 * ff_make(gb[4]) + v2 * ff_make(gb[5]);
+        L.g[5] = {0.f, 0.f};
+    } else {
+        L.g[3] = v0;
+        L.g[4] = v1;
+        L.g[5] = v2;
+    }
+    L.g[6] = -(s * v0);
+    L.g[7] = -(s * v1);
+    L.g[8] = -(s * v2);
+    for (int k = 0; k < ni; ++k) {
+        ff ju, jv;
+        intrinsic_column_ff(cols[k], x, y, r2, xd, yd, su, sv, sfx, sfy, aspect, ju, jv);
+        L.g[9 + k] = -(ju * wr0 + jv * wr1);
+    }
+    return true;
+}
+
 }  // namespace pb

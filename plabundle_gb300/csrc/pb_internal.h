@@ -42,7 +42,18 @@ struct Shape {
     int ref_param;
     int ncp;             // control-point constraints of processed tracks
     double cp_huber;     // Huber delta of the control-point residuals (m)
+    float loss_scale_hi, loss_scale_lo;  // loss_scale as float-float (mixed-path linearisation)
 };
+
+// float-float pair (hi, lo) of device state copies: CUDA's float2 in device code, a struct of the
+// same layout for the host-only compilation of this header
+#if defined(__CUDACC__)
+using ff2 = float2;
+#else
+struct alignas(8) ff2 {
+    float x, y;
+};
+#endif
 
 struct DevPtrs {
     // cameras
@@ -65,6 +76,12 @@ struct DevPtrs {
     double* pscale;       // ntp: point step scale s(X) of the current points
     int* trk_cp_begin;    // ntp + 1: control points of each processed track
     double* cp_rec;       // 12 per control point: whitening sqrt(weight) W (row-major), target P
+    // float-float copies of the state read by the mixed-path linearisation, written with the
+    // FP64 state (k_effective, k_accept)
+    ff2* cams_ff;      // nc * kCamFF: effective cameras
+    ff2* points_ff;    // ntp * 3
+    ff2* pscale_ff;    // ntp
+    ff2* obs_ff;       // nop * 3: u, v, weight (processing order)
     // observations (processing order)
     int* obs_cam;
     double* obs_u;

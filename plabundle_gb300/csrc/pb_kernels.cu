@@ -7,6 +7,8 @@
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "pb_device.cuh"
 #include "pb_kernels.h"
 
@@ -183,12 +185,17 @@ __global__ void k_effective(Shape S, DevPtrs D) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c < S.ntp) {
         const double* X = D.points + static_cast<size_t>(c) * 3;
-        D.pscale[c] = S.ref_param ? point_scale(X[0], X[1], X[2]) : 1.0;
+        const double sc = S.ref_param ? point_scale(X[0], X[1], X[2]) : 1.0;
+        D.pscale[c] = sc;
+        D.pscale_ff[c] = ff_pack(sc);
+        for (int a = 0; a < 3; ++a) D.points_ff[static_cast<size_t>(c) * 3 + a] = ff_pack(X[a]);
     }
     if (c < S.nc) {
         const double* G = S.ng > 0 ? D.groups + static_cast<size_t>(D.cam_group[c]) * kGroupRec : nullptr;
+        double* ef = D.cams_eff + static_cast<size_t>(c) * kCamStride;
         group_camera(D.cams_state + static_cast<size_t>(c) * kCamStride, D.cams_ref + static_cast<size_t>(c) * kCamStride,
-                     G, D.cams_eff + static_cast<size_t>(c) * kCamStride);
+                     G, ef);
+        camera_ff(ef, D.cams_ff + static_cast<size_t>(c) * kCamFF);
     }
     if (c == 0 && S.gauge_anchor >= 0 && S.gauge_scale >= 0 && S.gauge_baseline > 0.0)
         gauge_basis(D.cams_state + static_cast<size_t>(S.gauge_anchor) * kCamStride + 9,
@@ -532,6 +539,7 @@ __global__ void k_accept(Shape S, DevPtrs D, const double* __restrict__ step_p, 
         double* ef = D.cams_eff + static_cast<size_t>(i) * kCamStride;
         for (int q = 0; q < 12; ++q) st[q] = tr[q];
         for (int q = 0; q < kCamStride; ++q) ef[q] = tr[q];
+        camera_ff(tr, D.cams_ff + static_cast<size_t>(i) * kCamFF);
         // the gauge tangent basis follows the accepted state (referenceGaugeTargetTangentBasis is
         // evaluated on the current cameras, BundleAdjustPlaMatrixAssembly.cpp:69-99, :110, :205);
         // read from the trial records, which this kernel does not write
@@ -546,7 +554,10 @@ __global__ void k_accept(Shape S, DevPtrs D, const double* __restrict__ step_p, 
         X[0] += f * step_p[static_cast<size_t>(i) * 3 + 0];
         X[1] += f * step_p[static_cast<size_t>(i) * 3 + 1];
         X[2] += f * step_p[static_cast<size_t>(i) * 3 + 2];
-        D.pscale[i] = S.ref_param ? point_scale(X[0], X[1], X[2]) : 1.0;
+        const double sc = S.ref_param ? point_scale(X[0], X[1], X[2]) : 1.0;
+        D.pscale[i] = sc;
+        D.pscale_ff[i] = ff_pack(sc);
+        for (int q = 0; q < 3; ++q) D.points_ff[static_cast<size_t>(i) * 3 + q] = ff_pack(X[q]);
     }
 }
 
@@ -617,6 +628,29 @@ __global__ void k_linearize_export(Shape S, DevPtrs D, double* __restrict__ res,
         for (int i = 0; i < S.ni; ++i) ji[2 * kP * k + r * kP + S.int_cols[i]] = static_cast<double>(L.Ji[r * kMaxNI + i]);
     nw[k] = static_cast<double>(L.w);
     cost[k] = L.cost;
+    if constexpr (std::is_same<T, float>::value) {
+        // the mixed path linearises in float-float (the assembly's phase A); its residual,
+        // Jacobians and weight replace the FP64 ones, the cost stays the FP64 one
+        const ff2* of = D.obs_ff + static_cast<size_t>(o) * 3;
+        LinFF F;
+        const bool okf = linearize_obs_ff(D.cams_ff + static_cast<size_t>(cam) * kCamFF,
+                                          D.points_ff + static_cast<size_t>(trk) * 3, ffl(D.pscale_ff[trk]),
+                                          ffl(of[0]), ffl(of[1]), ffl(of[2]), S.loss,
+                                          ff{S.loss_scale_hi, S.loss_scale_lo}, tangent, !S.ref_param, D.gauge_basis,
+                                          S.ni, S.int_cols, F);
+        valid[k] = okf ? 1 : 0;
+        if (!okf) return;
+        res[2 * k] = static_cast<double>(F.r0.hi) + static_cast<double>(F.r0.lo);
+        res[2 * k + 1] = static_cast<double>(F.r1.hi) + static_cast<double>(F.r1.lo);
+        for (int i = 0; i < 6; ++i) jp[6 * k + i] = static_cast<double>(F.Jp[i]);
+        if (D.cam_block[cam] >= 0)
+            for (int r = 0; r < 2; ++r)
+                for (int i = 0; i < 6; ++i) jpose[2 * kP * k + r * kP + i] = static_cast<double>(F.Jc[r * 6 + i]);
+        for (int r = 0; r < 2; ++r)
+            for (int i = 0; i < S.ni; ++i)
+                ji[2 * kP * k + r * kP + S.int_cols[i]] = static_cast<double>(F.Ji[r * kMaxNI + i]);
+        nw[k] = static_cast<double>(F.w.hi) + static_cast<double>(F.w.lo);
+    }
 }
 
 // ---------------------------------------------------------------- launchers

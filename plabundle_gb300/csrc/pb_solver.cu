@@ -233,11 +233,17 @@ void upload_structure(pb_gpu_ctx* c) {
     S.ref_param = m.ref_param ? 1 : 0;
     S.ncp = static_cast<int>(m.cp_proc.size() / 12);
     S.cp_huber = m.cp_huber;
+    {
+        const float2 ls = ff_pack(m.loss_scale);
+        S.loss_scale_hi = ls.x;
+        S.loss_scale_lo = ls.y;
+    }
 
     D.cams_input = upload_new(A, m.cams_in, st);
     D.cams_ref = upload_new(A, m.cams_ref, st);
     D.cams_state = A.alloc<double>(m.cams_in.size());
     D.cams_eff = A.alloc<double>(m.cams_in.size());
+    D.cams_ff = A.alloc<float2>(static_cast<size_t>(nc) * kCamFF);
     D.cams_trial = A.alloc<double>(static_cast<size_t>(kMaxAlpha) * m.cams_in.size());
     D.cam_block = upload_new(A, m.camera_block, st);
     std::vector<int> grp(nc, -1);
@@ -265,6 +271,8 @@ void upload_structure(pb_gpu_ctx* c) {
     D.points0 = upload_new(A, pts, st);
     D.points = A.alloc<double>(pts.size());
     D.pscale = A.alloc<double>(std::max<size_t>(1, pts.size() / 3));
+    D.points_ff = A.alloc<float2>(std::max<size_t>(3, pts.size()));
+    D.pscale_ff = A.alloc<float2>(std::max<size_t>(1, pts.size() / 3));
     {
         std::vector<int> cpb = m.trk_cp_begin;
         if (cpb.empty()) cpb.assign(static_cast<size_t>(ntp) + 1, 0);
@@ -291,6 +299,15 @@ void upload_structure(pb_gpu_ctx* c) {
     D.obs_u = upload_new(A, ou, st);
     D.obs_v = upload_new(A, ov, st);
     D.obs_w = upload_new(A, ow, st);
+    {
+        std::vector<float2> off(static_cast<size_t>(std::max<long long>(1, nop)) * 3, make_float2(0.f, 0.f));
+        for (long long o = 0; o < nop; ++o) {
+            off[static_cast<size_t>(o) * 3] = ff_pack(ou[o]);
+            off[static_cast<size_t>(o) * 3 + 1] = ff_pack(ov[o]);
+            off[static_cast<size_t>(o) * 3 + 2] = ff_pack(ow[o]);
+        }
+        D.obs_ff = upload_new(A, off, st);
+    }
     D.obs_trk = upload_new(A, otrk, st);
     D.obs_orig = upload_new(A, m.p_obs_orig, st);
     // pose CSR
@@ -789,13 +806,17 @@ void lm_solve(pb_gpu_ctx* c, const pb_solve_options& op, pb_solve_report* rep) {
     auto ms = [](std::chrono::steady_clock::time_point a, std::chrono::steady_clock::time_point b) {
         return std::chrono::duration<double, std::milli>(b - a).count();
     };
+    // The mixed-path assembly computes no cost (its linearisation is float-float): the FP64 cost
+    // of the state comes from the cost kernel, here for the initial state and afterwards from the
+    // line search that accepted the state.
+    const bool cost_from_assembly = precision != PB_PRECISION_MIXED;
     try {
-        if (converged) {
+        if (converged || !cost_from_assembly) {
             double cst;
             eval_costs(c, nullptr, 1, 0, &cst);
             current = cst;
             rep->initial_cost = current;
-            ++rep->objective_evaluations;
+            if (converged) ++rep->objective_evaluations;
         }
         const int budget = std::max(1, op.max_iterations);
         bool terminate = false;
@@ -813,8 +834,10 @@ void lm_solve(pb_gpu_ctx* c, const pb_solve_options& op, pb_solve_report* rep) {
                 if (flags & 2) throw std::runtime_error("online Schur linearisation produced an invalid projection");
                 ++rep->linearizations;
                 ++rep->objective_evaluations;
-                current = cost;
-                if (rep->linearizations == 1) rep->initial_cost = current;
+                if (cost_from_assembly) {
+                    current = cost;
+                    if (rep->linearizations == 1) rep->initial_cost = current;
+                }
                 if (flags & 1) {
                     ++iterations;
                     ++rep->rejected_steps;
@@ -1180,6 +1203,7 @@ pb_status pb_gpu_linearize_schur(pb_gpu_ctx* c, double lambda, int32_t precision
         double cst;
         int flags;
         do_assemble(c, lambda, precision == PB_PRECISION_MIXED ? PB_PRECISION_MIXED : PB_PRECISION_FP64, &cst, &flags);
+        if (precision == PB_PRECISION_MIXED) eval_costs(c, nullptr, 1, 0, &cst);  // no cost in the mixed assembly
         if (cost) *cost = cst;
         if (singular) *singular = flags & 1;
         if (flags & 2) return fail(c, PB_ERR_INVALID_PROJECTION, "invalid projection during linearisation");
@@ -1468,6 +1492,7 @@ pb_status pb_gpu_set_observations(pb_gpu_ctx* c, int64_t n, const int64_t* index
             if (k < 0 || k >= m.no || !std::isfinite(u[i]) || !std::isfinite(v[i]))
                 return fail(c, PB_ERR_INVALID_ARGUMENT, "observation index out of range or non-finite measurement");
         }
+        std::vector<float2> uv_ff(static_cast<size_t>(n) * 2);  // lives until the synchronisation below
         for (int64_t i = 0; i < n; ++i) {
             const int64_t k = index[i];
             m.obs_u[k] = u[i];
@@ -1478,6 +1503,10 @@ pb_status pb_gpu_set_observations(pb_gpu_ctx* c, int64_t n, const int64_t* index
             if (p >= 0) {
                 check(cudaMemcpyAsync(D.obs_u + p, &m.obs_u[k], sizeof(double), cudaMemcpyHostToDevice, st), "H2D");
                 check(cudaMemcpyAsync(D.obs_v + p, &m.obs_v[k], sizeof(double), cudaMemcpyHostToDevice, st), "H2D");
+                uv_ff[2 * i] = ff_pack(m.obs_u[k]);
+                uv_ff[2 * i + 1] = ff_pack(m.obs_v[k]);
+                check(cudaMemcpyAsync(D.obs_ff + 3 * p, &uv_ff[2 * i], 2 * sizeof(float2), cudaMemcpyHostToDevice, st),
+                      "H2D");
             }
         }
         check(cudaStreamSynchronize(st), "set_observations");
