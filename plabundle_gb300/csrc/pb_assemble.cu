@@ -102,7 +102,8 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
     constexpr bool kMixed = std::is_same<T, float>::value;
     if constexpr (kMixed) {
     if (active) {
-        // mixed path: float-float linearisation (no cost: the LM takes it from the line search)
+        // mixed path: FP64 projection, float-float weight and gradient (no cost: the LM takes it
+        // from the line search)
         const int cam = D.obs_cam[o];
         const int trk = D.obs_trk[o];
         const int tb0 = D.trk_obs_begin[trk];
@@ -111,10 +112,14 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
         elim = D.trk_block[trk] >= 0;
         const int grp = ng > 0 ? D.cam_group[cam] : -1;
         const bool tangent = cam == S.gauge_scale && S.gauge_anchor >= 0 && S.gauge_baseline > 0.0;
-        const float2* of = D.obs_ff + static_cast<size_t>(o) * 3;
+        DCam c;
+        load_cam(D.cams_eff + static_cast<size_t>(cam) * kCamStride, c);
+        const double* X = D.points + static_cast<size_t>(trk) * 3;
+        Proj pr;
         LinFF F;
-        ok = linearize_obs_ff(D.cams_ff + static_cast<size_t>(cam) * kCamFF, D.points_ff + static_cast<size_t>(trk) * 3,
-                              ffl(D.pscale_ff[trk]), ffl(of[0]), ffl(of[1]), ffl(of[2]), S.loss,
+        ok = project64(c, X[0], X[1], X[2], pr) &&
+             linearize_obs_ff(pr, D.obs_u[o], D.obs_v[o], D.cams_ff + static_cast<size_t>(cam) * kCamFF,
+                              ffl(D.pscale_ff[trk]), ffl(D.obs_ff[static_cast<size_t>(o) * 3 + 2]), S.loss,
                               ff{S.loss_scale_hi, S.loss_scale_lo}, tangent, !S.ref_param, D.gauge_basis, ni,
                               S.int_cols, F);
         if (!ok) atomicOr(s_flags, 2);

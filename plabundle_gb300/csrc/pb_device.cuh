@@ -451,16 +451,17 @@ __device__ __forceinline__ float warp_sum(float v) {
 }
 
 // ---------------------------------------------------------------- float-float linearisation
-// The mixed path's linearisation in float-float arithmetic.  FP64 runs at a small fraction of the
-// FP32 rate on this part, and the projection, robust weight and gradient of every observation
-// were the FP64-bound share of the assembly.  Here they run on the FP32 pipe with ~44 significant
-// bits: the residual keeps ~1e-10 px absolute accuracy, enough for the gradient that decides the
-// fixed point.  The reciprocal and reciprocal square root take one Newton-Raphson step from the
-// FP32 hardware approximation, with the correction term evaluated in float-float (the
-// double-word division scheme of Joldes, Muller and Popescu, "Tight and rigorous error bounds for
-// basic building blocks of double-word arithmetic", ACM TOMS 2017).  Inputs are float-float
-// copies of the effective cameras, points, point scales and observations, written when the FP64
-// state changes.
+// The mixed path's robust weight and gradient in float-float arithmetic.  FP64 runs at a small
+// fraction of the FP32 rate on this part, and the robust weight, the cost and the gradient chain
+// of every observation were most of the FP64 work of the assembly.  The projection and residual
+// stay FP64; the rest runs on the FP32 pipe with ~44 significant bits.  (A float-float projection
+// was measured too: its ~3e-10 px residual error put a noise floor into the reduced right-hand
+// side near convergence and cost ~30% more CG iterations than it saved.)  The reciprocal and
+// reciprocal square root take one Newton-Raphson step from the FP32 hardware approximation, with
+// the correction term evaluated in float-float (the double-word division scheme of Joldes,
+// Muller and Popescu, "Tight and rigorous error bounds for basic building blocks of double-word
+// arithmetic", ACM TOMS 2017).  Inputs are float-float copies of the effective cameras, point
+// scales and observation weights, written when the FP64 state changes.
 
 __host__ __device__ __forceinline__ float2 ff_pack(double d) {
     const float h = static_cast<float>(d);
@@ -523,38 +524,29 @@ __device__ __forceinline__ void intrinsic_column_ff(int col, ff x, ff y, ff r2, 
     }
 }
 
-// linearize_obs of the mixed path (same Jacobian columns, same robust weight), with the
-// gradient -J^T w r in float-float and no cost.  cam: kCamFF values; X: the point; s: its step
-// scale; gb: the FP64 gauge tangent basis (read for the tangent camera only).
-__device__ __forceinline__ bool linearize_obs_ff(const float2* __restrict__ cam, const float2* __restrict__ X, ff s,
-                                                 ff u, ff v, ff wobs, int loss, ff lscale, bool tangent, bool plain,
+// linearize_obs of the mixed path (same Jacobian columns, same robust weight).  The projection
+// and residual stay FP64 (p: project64 of the observation): the residual is a small difference
+// of pixel coordinates, and its absolute accuracy sets the noise floor of the gradient near
+// convergence, where the reduced right-hand side shrinks towards it.  Everything after the
+// residual -- the robust weight and the gradient -J^T w r -- runs in float-float, and the cost is
+// not evaluated.  cam: the camera's float-float record (kCamFF values); s: the point's step scale;
+// wobs: the observation weight; gb: the FP64 gauge tangent basis (read for the tangent camera only).
+__device__ __forceinline__ bool linearize_obs_ff(const Proj& p, double u, double v, const float2* __restrict__ cam,
+                                                 ff s, ff wobs, int loss, ff lscale, bool tangent, bool plain,
                                                  const double* __restrict__ gb, int ni, const int* __restrict__ cols,
                                                  LinFF& L) {
     ff R[9];
 #pragma unroll
     for (int i = 0; i < 9; ++i) R[i] = ffl(cam[i]);
-    const ff d0 = ff_sub(ffl(X[0]), ffl(cam[9])), d1 = ff_sub(ffl(X[1]), ffl(cam[10])),
-             d2 = ff_sub(ffl(X[2]), ffl(cam[11]));
-    const ff xc = R[0] * d0 + R[3] * d1 + R[6] * d2;
-    const ff yc = R[1] * d0 + R[4] * d1 + R[7] * d2;
-    const ff zc = R[2] * d0 + R[5] * d1 + R[8] * d2;
-    const float fwd = cam[23].x != 0.f ? -(zc.hi + zc.lo) : zc.hi + zc.lo;
-    if (!(fwd > 1e-9f)) return false;
-    const ff iz = ff_recip(zc);
-    const ff x = xc * iz, y = yc * iz;
-    const ff r2 = x * x + y * y;
+    const ff d0 = ff_make(p.d0), d1 = ff_make(p.d1), d2 = ff_make(p.d2);
+    const ff iz = ff_make(p.iz);
+    const ff x = ff_make(p.x), y = ff_make(p.y), r2 = ff_make(p.r2), radial = ff_make(p.radial);
+    const ff xd = ff_make(p.xd), yd = ff_make(p.yd);
     const ff k1 = ffl(cam[16]), k2 = ffl(cam[17]), k3 = ffl(cam[18]), p1 = ffl(cam[19]), p2 = ffl(cam[20]);
-    const ff radial = ff_one() + r2 * (k1 + r2 * (k2 + r2 * k3));
-    const ff xy2 = ff_twice(x * y);
-    const ff xd = x * radial + p1 * xy2 + p2 * (r2 + ff_twice(x * x));
-    const ff yd = y * radial + p1 * (r2 + ff_twice(y * y)) + p2 * xy2;
     const float su = cam[21].x, sv = cam[22].x;
     const ff fx = ffl(cam[12]), fy = ffl(cam[13]);
     const ff sfx = su * fx, sfy = sv * fy;
-    const ff px = sfx * xd + ffl(cam[14]);
-    const ff py = sfy * yd + ffl(cam[15]);
-    if (!isfinite(px.hi) || !isfinite(py.hi)) return false;
-    const ff r0 = ff_sub(px, u), r1 = ff_sub(py, v);
+    const ff r0 = ff_make(p.px - u), r1 = ff_make(p.py - v);
     // evaluateImageRobustLoss weight (BundleAdjustPlaMatrixProjection.cpp:75-109)
     const ff sq = wobs * (r0 * r0 + r1 * r1);
     if (!(sq.hi >= 0.f) || !isfinite(sq.hi)) return false;

@@ -76,12 +76,11 @@ struct DevPtrs {
     double* pscale;       // ntp: point step scale s(X) of the current points
     int* trk_cp_begin;    // ntp + 1: control points of each processed track
     double* cp_rec;       // 12 per control point: whitening sqrt(weight) W (row-major), target P
-    // float-float copies of the state read by the mixed-path linearisation, written with the
-    // FP64 state (k_effective, k_accept)
+    // float-float copies read by the mixed-path weight and gradient, written with the FP64 state
+    // (k_effective, k_accept) and the observations
     ff2* cams_ff;      // nc * kCamFF: effective cameras
-    ff2* points_ff;    // ntp * 3
     ff2* pscale_ff;    // ntp
-    ff2* obs_ff;       // nop * 3: u, v, weight (processing order)
+    ff2* obs_ff;       // nop * 3: u, v, weight (processing order; the weight is read)
     // observations (processing order)
     int* obs_cam;
     double* obs_u;

@@ -188,7 +188,6 @@ __global__ void k_effective(Shape S, DevPtrs D) {
         const double sc = S.ref_param ? point_scale(X[0], X[1], X[2]) : 1.0;
         D.pscale[c] = sc;
         D.pscale_ff[c] = ff_pack(sc);
-        for (int a = 0; a < 3; ++a) D.points_ff[static_cast<size_t>(c) * 3 + a] = ff_pack(X[a]);
     }
     if (c < S.nc) {
         const double* G = S.ng > 0 ? D.groups + static_cast<size_t>(D.cam_group[c]) * kGroupRec : nullptr;
@@ -557,7 +556,6 @@ __global__ void k_accept(Shape S, DevPtrs D, const double* __restrict__ step_p, 
         const double sc = S.ref_param ? point_scale(X[0], X[1], X[2]) : 1.0;
         D.pscale[i] = sc;
         D.pscale_ff[i] = ff_pack(sc);
-        for (int q = 0; q < 3; ++q) D.points_ff[static_cast<size_t>(i) * 3 + q] = ff_pack(X[q]);
     }
 }
 
@@ -629,13 +627,13 @@ __global__ void k_linearize_export(Shape S, DevPtrs D, double* __restrict__ res,
     nw[k] = static_cast<double>(L.w);
     cost[k] = L.cost;
     if constexpr (std::is_same<T, float>::value) {
-        // the mixed path linearises in float-float (the assembly's phase A); its residual,
-        // Jacobians and weight replace the FP64 ones, the cost stays the FP64 one
-        const ff2* of = D.obs_ff + static_cast<size_t>(o) * 3;
+        // the mixed path's weight and gradient chain are float-float (the assembly's phase A);
+        // its residual, Jacobians and weight replace the FP64 ones, the cost stays the FP64 one
+        Proj pr;
         LinFF F;
-        const bool okf = linearize_obs_ff(D.cams_ff + static_cast<size_t>(cam) * kCamFF,
-                                          D.points_ff + static_cast<size_t>(trk) * 3, ffl(D.pscale_ff[trk]),
-                                          ffl(of[0]), ffl(of[1]), ffl(of[2]), S.loss,
+        const bool okf = project64(c, X[0], X[1], X[2], pr) &&
+                         linearize_obs_ff(pr, D.obs_u[o], D.obs_v[o], D.cams_ff + static_cast<size_t>(cam) * kCamFF,
+                                          ffl(D.pscale_ff[trk]), ffl(D.obs_ff[static_cast<size_t>(o) * 3 + 2]), S.loss,
                                           ff{S.loss_scale_hi, S.loss_scale_lo}, tangent, !S.ref_param, D.gauge_basis,
                                           S.ni, S.int_cols, F);
         valid[k] = okf ? 1 : 0;

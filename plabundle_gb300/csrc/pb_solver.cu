@@ -271,7 +271,6 @@ void upload_structure(pb_gpu_ctx* c) {
     D.points0 = upload_new(A, pts, st);
     D.points = A.alloc<double>(pts.size());
     D.pscale = A.alloc<double>(std::max<size_t>(1, pts.size() / 3));
-    D.points_ff = A.alloc<float2>(std::max<size_t>(3, pts.size()));
     D.pscale_ff = A.alloc<float2>(std::max<size_t>(1, pts.size() / 3));
     {
         std::vector<int> cpb = m.trk_cp_begin;
@@ -783,9 +782,12 @@ void lm_solve(pb_gpu_ctx* c, const pb_solve_options& op, pb_solve_report* rep) {
         c->error = "invalid image robust loss";
         return;
     }
+    const float2 ls = ff_pack(op.robust_loss_scale);
     for (int p = 0; p < 2; ++p) {
         c->S[p].loss = op.robust_loss;
         c->S[p].loss_scale = op.robust_loss_scale;
+        c->S[p].loss_scale_hi = ls.x;
+        c->S[p].loss_scale_lo = ls.y;
     }
     reset_state(c);
     if (m.obs_count == 0) {
