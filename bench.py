@@ -56,7 +56,7 @@ ITERATIONS_TO_CONVERGE = {"aerial": 81, "ring": 20}
 # dram__bytes_write.sum of an ncu capture on the 250-camera / 100k-point aerial grid
 # (663 659 observations; profiles/k_assemble_aerial250.md).  The chunk plan is the same at 500
 # cameras, so the traffic scales with the observations.
-ASSEMBLY_DRAM_BYTES_PER_OBS = (30.759680e6 + 255.699456e6) / 663659
+ASSEMBLY_DRAM_BYTES_PER_OBS = (39.366400e6 + 253.288704e6) / 663659
 
 
 def workload(name):

@@ -206,10 +206,10 @@ pb_status pb_gpu_linearize_schur(pb_gpu_ctx* ctx, double lambda, int32_t precisi
 pb_status pb_gpu_get_reduced(pb_gpu_ctx* ctx, double* dense_matrix, double* rhs, double* direct_rhs);
 
 /* Kernel (c): solve of the damped reduced system (solveDampedSchurComplement, call site
- * BundleAdjustPlaMatrix.cpp:311-357).  Up to 16384 unknowns: conjugate gradients on the FP64
- * matrix preconditioned by a dense Cholesky factor of the Jacobi-scaled matrix (FP32 factor on
- * the mixed path, FP64 on the FP64 path); larger systems: block-Jacobi PCG.  One cooperative
- * kernel per solve. */
+ * BundleAdjustPlaMatrix.cpp:311-357).  Up to 32768 unknowns on the mixed path (16384 on the
+ * FP64 path): conjugate gradients on the FP64 matrix preconditioned by a dense Cholesky factor
+ * of the Jacobi-scaled matrix (FP32 factor on the mixed path, FP64 on the FP64 path); larger
+ * systems: block-Jacobi PCG.  One cooperative kernel per solve. */
 pb_status pb_gpu_solve_reduced(pb_gpu_ctx* ctx, double* step, int32_t* converged, int32_t* iterations,
                                double* relative_residual);
 
