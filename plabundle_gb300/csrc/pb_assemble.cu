@@ -119,7 +119,7 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
         LinFF F;
         ok = project64(c, X[0], X[1], X[2], pr) &&
              linearize_obs_ff(pr, D.obs_u[o], D.obs_v[o], D.cams_ff + static_cast<size_t>(cam) * kCamFF,
-                              ffl(D.pscale_ff[trk]), ffl(D.obs_ff[static_cast<size_t>(o) * 3 + 2]), S.loss,
+                              ffl(D.pscale_ff[trk]), ffl(D.obs_w_ff[o]), S.loss,
                               ff{S.loss_scale_hi, S.loss_scale_lo}, tangent, !S.ref_param, D.gauge_basis, ni,
                               S.int_cols, F);
         if (!ok) atomicOr(s_flags, 2);

@@ -519,42 +519,58 @@ int build_host_model(const pb_problem_desc* pr, const pb_solve_options* op, Host
     // (prepareOffDiagonalTopology, BundleAdjustPlaMatrixReferenceSchur.cpp:568-659)
     {
         const int P = m->P;
-        std::vector<std::vector<int>> nbr(P);
-        std::vector<int> tb;
-        // P x P seen-mask: each pair is recorded once however many tracks share it
-        std::vector<unsigned char> seen(static_cast<size_t>(P) * P, 0);
-        auto connect = [&](int a, int b) {
-            if (a < 0 || b < 0 || a == b) return;
-            const int lo = std::min(a, b), hi = std::max(a, b);
-            unsigned char& f = seen[static_cast<size_t>(lo) * P + hi];
-            if (f) return;
-            f = 1;
-            nbr[lo].push_back(hi);
-        };
-        for (int t = 0; t < nt; ++t) {
-            if (!m->active_track[t]) continue;
-            tb.clear();
-            for (long long k = m->offs[t]; k < m->offs[t + 1]; ++k) {
-                if (!usable(k)) continue;
-                const int c = m->obs_cam[k];
-                connect(m->camera_block[c], m->intrinsic_block[c]);
-                if (m->track_block[t] >= 0) {
-                    if (m->camera_block[c] >= 0) tb.push_back(m->camera_block[c]);
-                    if (m->intrinsic_block[c] >= 0) tb.push_back(m->intrinsic_block[c]);
+        // Upper pairs (lo, hi) as bits lo * P + hi of a P x P bitset.  Tracks are split over host
+        // threads, each with its own bitset (a pair is recorded once however many tracks share
+        // it); the bitsets are OR-ed and read out row-major, which is the sorted, deduplicated
+        // pair list.
+        const size_t words = (static_cast<size_t>(P) * P + 63) / 64;
+        const int nthreads = host_threads(nt);
+        std::vector<std::vector<unsigned long long>> bits(nthreads, std::vector<unsigned long long>(words, 0ull));
+        parallel_ranges(nt, nthreads, [&](int i, int t0, int t1) {
+            unsigned long long* mask = bits[i].data();
+            auto connect = [&](int a, int b) {
+                if (a < 0 || b < 0 || a == b) return;
+                const size_t bit = static_cast<size_t>(std::min(a, b)) * P + std::max(a, b);
+                mask[bit >> 6] |= 1ull << (bit & 63);
+            };
+            std::vector<int> tb;
+            for (int t = t0; t < t1; ++t) {
+                if (!m->active_track[t]) continue;
+                tb.clear();
+                for (long long k = m->offs[t]; k < m->offs[t + 1]; ++k) {
+                    if (!usable(k)) continue;
+                    const int c = m->obs_cam[k];
+                    connect(m->camera_block[c], m->intrinsic_block[c]);
+                    if (m->track_block[t] >= 0) {
+                        if (m->camera_block[c] >= 0) tb.push_back(m->camera_block[c]);
+                        if (m->intrinsic_block[c] >= 0) tb.push_back(m->intrinsic_block[c]);
+                    }
                 }
+                if (m->track_block[t] < 0) continue;
+                std::sort(tb.begin(), tb.end());
+                tb.erase(std::unique(tb.begin(), tb.end()), tb.end());
+                for (size_t l = 0; l < tb.size(); ++l)
+                    for (size_t r = l + 1; r < tb.size(); ++r) connect(tb[l], tb[r]);
             }
-            if (m->track_block[t] < 0) continue;
-            std::sort(tb.begin(), tb.end());
-            tb.erase(std::unique(tb.begin(), tb.end()), tb.end());
-            for (size_t l = 0; l < tb.size(); ++l)
-                for (size_t r = l + 1; r < tb.size(); ++r) connect(tb[l], tb[r]);
-        }
+        });
+        std::vector<unsigned long long>& all = bits[0];
+        for (int i = 1; i < nthreads; ++i)
+            for (size_t w = 0; w < words; ++w) all[w] |= bits[i][w];
         m->pairs.clear();
         for (int r = 0; r < P; ++r) {
-            auto& v = nbr[r];
-            std::sort(v.begin(), v.end());
-            v.erase(std::unique(v.begin(), v.end()), v.end());
-            for (int c : v) m->pairs.emplace_back(r, c);
+            const size_t b0 = static_cast<size_t>(r) * P + r + 1, b1 = static_cast<size_t>(r + 1) * P;
+            for (size_t b = b0; b < b1;) {
+                const size_t w = b >> 6;
+                unsigned long long v = all[w] >> (b & 63);
+                if (!v) {
+                    b = (w + 1) << 6;
+                    continue;
+                }
+                const size_t hit = b + static_cast<size_t>(__builtin_ctzll(v));
+                if (hit >= b1) break;
+                m->pairs.emplace_back(r, static_cast<int>(hit - static_cast<size_t>(r) * P));
+                b = hit + 1;
+            }
         }
         // pose CSR (both triangles), diagonal always present
         const int nb = m->ncb;
@@ -604,30 +620,42 @@ int build_host_model(const pb_problem_desc* pr, const pb_solve_options* op, Host
     // counting sort gives the order of sorting (key, track index).
     {
         const int nkeys = 2 * nc + 1;
-        std::vector<int> key(nt, -1), count(nkeys + 1, 0);
-        for (int t = 0; t < nt; ++t) {
-            if (!m->active_track[t]) continue;
-            int mn = nkeys - 1;
-            for (long long k = m->offs[t]; k < m->offs[t + 1]; ++k)
-                if (usable(k)) mn = std::min(mn, m->camera_block[m->obs_cam[k]] >= 0 ? m->camera_block[m->obs_cam[k]]
-                                                                                     : nc + m->obs_cam[k]);
-            key[t] = mn;
-            ++count[mn + 1];
-        }
+        // keys and usable-observation counts per track (threads over tracks), then the counting
+        // sort and the observation ranges in processing order, filled by threads over ranges
+        std::vector<int> key(nt, -1), nuse(nt, 0), count(nkeys + 1, 0);
+        const int nthreads = host_threads(m->no);
+        parallel_ranges(nt, nthreads, [&](int, int t0, int t1) {
+            for (int t = t0; t < t1; ++t) {
+                if (!m->active_track[t]) continue;
+                int mn = nkeys - 1, cnt = 0;
+                for (long long k = m->offs[t]; k < m->offs[t + 1]; ++k)
+                    if (usable(k)) {
+                        const int c = m->obs_cam[k];
+                        mn = std::min(mn, m->camera_block[c] >= 0 ? m->camera_block[c] : nc + c);
+                        ++cnt;
+                    }
+                key[t] = mn;
+                nuse[t] = cnt;
+            }
+        });
+        for (int t = 0; t < nt; ++t)
+            if (key[t] >= 0) ++count[key[t] + 1];
         for (int i = 0; i < nkeys; ++i) count[i + 1] += count[i];
         m->trk_order.assign(static_cast<size_t>(count[nkeys]), 0);
         for (int t = 0; t < nt; ++t)
             if (key[t] >= 0) m->trk_order[count[key[t]]++] = t;
         const size_t ntp = m->trk_order.size();
         m->trk_obs_begin.assign(ntp + 1, 0);
-        m->p_obs_orig.clear();
-        m->p_obs_orig.reserve(m->obs_count);
-        for (size_t i = 0; i < ntp; ++i) {
-            const int t = m->trk_order[i];
-            for (long long k = m->offs[t]; k < m->offs[t + 1]; ++k)
-                if (usable(k)) m->p_obs_orig.push_back(static_cast<int>(k));
-            m->trk_obs_begin[i + 1] = static_cast<int>(m->p_obs_orig.size());
-        }
+        for (size_t i = 0; i < ntp; ++i) m->trk_obs_begin[i + 1] = m->trk_obs_begin[i] + nuse[m->trk_order[i]];
+        m->p_obs_orig.assign(static_cast<size_t>(m->trk_obs_begin[ntp]), 0);
+        parallel_ranges(static_cast<int>(ntp), nthreads, [&](int, int i0, int i1) {
+            for (int i = i0; i < i1; ++i) {
+                const int t = m->trk_order[i];
+                int pos = m->trk_obs_begin[i];
+                for (long long k = m->offs[t]; k < m->offs[t + 1]; ++k)
+                    if (usable(k)) m->p_obs_orig[pos++] = static_cast<int>(k);
+            }
+        });
     }
     // control points of the processed tracks, in processing order
     {

@@ -80,7 +80,7 @@ struct DevPtrs {
     // (k_effective, k_accept) and the observations
     ff2* cams_ff;      // nc * kCamFF: effective cameras
     ff2* pscale_ff;    // ntp
-    ff2* obs_ff;       // nop * 3: u, v, weight (processing order; the weight is read)
+    ff2* obs_w_ff;     // nop: observation weight (processing order)
     // observations (processing order)
     int* obs_cam;
     double* obs_u;

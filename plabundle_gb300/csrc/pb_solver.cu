@@ -299,13 +299,9 @@ void upload_structure(pb_gpu_ctx* c) {
     D.obs_v = upload_new(A, ov, st);
     D.obs_w = upload_new(A, ow, st);
     {
-        std::vector<float2> off(static_cast<size_t>(std::max<long long>(1, nop)) * 3, make_float2(0.f, 0.f));
-        for (long long o = 0; o < nop; ++o) {
-            off[static_cast<size_t>(o) * 3] = ff_pack(ou[o]);
-            off[static_cast<size_t>(o) * 3 + 1] = ff_pack(ov[o]);
-            off[static_cast<size_t>(o) * 3 + 2] = ff_pack(ow[o]);
-        }
-        D.obs_ff = upload_new(A, off, st);
+        std::vector<float2> wff(static_cast<size_t>(std::max<long long>(1, nop)), make_float2(0.f, 0.f));
+        for (long long o = 0; o < nop; ++o) wff[static_cast<size_t>(o)] = ff_pack(ow[o]);
+        D.obs_w_ff = upload_new(A, wff, st);
     }
     D.obs_trk = upload_new(A, otrk, st);
     D.obs_orig = upload_new(A, m.p_obs_orig, st);
@@ -1494,7 +1490,6 @@ pb_status pb_gpu_set_observations(pb_gpu_ctx* c, int64_t n, const int64_t* index
             if (k < 0 || k >= m.no || !std::isfinite(u[i]) || !std::isfinite(v[i]))
                 return fail(c, PB_ERR_INVALID_ARGUMENT, "observation index out of range or non-finite measurement");
         }
-        std::vector<float2> uv_ff(static_cast<size_t>(n) * 2);  // lives until the synchronisation below
         for (int64_t i = 0; i < n; ++i) {
             const int64_t k = index[i];
             m.obs_u[k] = u[i];
@@ -1505,10 +1500,6 @@ pb_status pb_gpu_set_observations(pb_gpu_ctx* c, int64_t n, const int64_t* index
             if (p >= 0) {
                 check(cudaMemcpyAsync(D.obs_u + p, &m.obs_u[k], sizeof(double), cudaMemcpyHostToDevice, st), "H2D");
                 check(cudaMemcpyAsync(D.obs_v + p, &m.obs_v[k], sizeof(double), cudaMemcpyHostToDevice, st), "H2D");
-                uv_ff[2 * i] = ff_pack(m.obs_u[k]);
-                uv_ff[2 * i + 1] = ff_pack(m.obs_v[k]);
-                check(cudaMemcpyAsync(D.obs_ff + 3 * p, &uv_ff[2 * i], 2 * sizeof(float2), cudaMemcpyHostToDevice, st),
-                      "H2D");
             }
         }
         check(cudaStreamSynchronize(st), "set_observations");
