@@ -549,8 +549,14 @@ void ensure_dense(pb_gpu_ctx* c) {
     c->dense_ready[idx] = true;
 }
 
-constexpr int kMaxFactorAge = 10;     // LM solves one FP32 factor may precondition
+constexpr int kMaxFactorAge = 10;     // LM solves one FP32 factor may precondition (at n <= 3000)
 constexpr int kReuseIterations = 60;  // CG iterations allowed on a kept factor before refactoring
+
+// A factorisation costs ~n^3 and a CG iteration ~n^2: at n = 3016 one factorisation costs about
+// 95 CG iterations, at n = 18016 several hundred.  The age limit of a kept factor therefore grows
+// with n (a size rule, not a timing rule, so that repeated solves stay identical); the cap on the
+// CG iterations of a reuse still refactors as soon as the kept factor preconditions badly.
+int max_factor_age(int n) { return std::max(kMaxFactorAge, n / 300); }
 
 template <typename T>
 int solve_dense(pb_gpu_ctx* c, double rel, double abs_tol, int max_it, bool* converged, int* iterations,
@@ -559,7 +565,7 @@ int solve_dense(pb_gpu_ctx* c, double rel, double abs_tol, int max_it, bool* con
     DenseWork<T>& W = dwork<T>(c);
     const bool f32 = std::is_same<T, float>::value;
     int spent = 0;
-    if (f32 && c->f32_age >= 0 && c->f32_age < kMaxFactorAge && !c->f32_stale) {
+    if (f32 && c->f32_age >= 0 && c->f32_age < max_factor_age(c->S[0].n) && !c->f32_stale) {
         // The reduced matrix changes little between LM iterations: the FP32 factor of an earlier
         // one still preconditions the CG on the current FP64 matrix.  A factorisation costs
         // about as much as a hundred CG iterations, so the kept factor is used until the CG
