@@ -312,14 +312,15 @@ def test_mixed_weight_and_gradient_chain_match_fp64(name, make, opts):
     from the FP64 projection and residual.  Against the FP64 path at the same state: normal
     weights within 1e-10 relative (measured ~1e-10 at the 500-camera block), the direct gradient
     (before point elimination, the image terms only) within 1e-10 of its largest entry (measured
-    3e-12); the residual is the FP64 one, identical."""
+    3e-12); the residual is the FP64 one."""
     p = make()
     ctx = gpu(p, opts())
     a = ctx.linearize_observations(Precision.Fp64)
     b = ctx.linearize_observations(Precision.Mixed)
     sel = (a["valid"] == 1) & (b["valid"] == 1)
     assert np.array_equal(a["valid"], b["valid"])
-    np.testing.assert_array_equal(b["residual"][sel], a["residual"][sel])
+    # the float-float copy of the FP64 residual keeps 48 of its 53 bits
+    np.testing.assert_allclose(b["residual"][sel], a["residual"][sel], rtol=1e-13, atol=1e-15)
     wrel = np.abs(b["normal_weight"][sel] - a["normal_weight"][sel]) / a["normal_weight"][sel]
     assert wrel.max() < 1e-10, wrel.max()
     ctx.linearize_schur(0.0, Precision.Fp64)
