@@ -1043,7 +1043,11 @@ pb_status pb_gpu_upload(pb_gpu_ctx* c, const pb_problem_desc* pr, const pb_solve
         std::string err;
         c->shift32 = 1e-7;
         c->f32_age = -1;
+        // opt-in trace (PB_GPU_TRACE=1): host model and device upload times
+        static const bool trace = std::getenv("PB_GPU_TRACE") != nullptr;
+        const auto t_start = std::chrono::steady_clock::now();
         const int rc = build_host_model(pr, op, &m, &err);
+        const auto t_model = std::chrono::steady_clock::now();
         if (rc) {
             c->uploaded = false;
             return fail(c, rc == PB_SOLVE_UNSUPPORTED ? PB_ERR_UNSUPPORTED : PB_ERR_INVALID_ARGUMENT, err);
@@ -1100,6 +1104,13 @@ pb_status pb_gpu_upload(pb_gpu_ctx* c, const pb_problem_desc* pr, const pb_solve
         c->proc_of_obs.clear();
         reset_state(c);
         check(cudaStreamSynchronize(c->stream), "upload");
+        if (trace) {
+            const auto t_end = std::chrono::steady_clock::now();
+            std::fprintf(stderr, "PB_GPU_UPLOAD host_model_ms=%.2f device_upload_ms=%.2f reuse=%d\n",
+                         std::chrono::duration<double, std::milli>(t_model - t_start).count(),
+                         std::chrono::duration<double, std::milli>(t_end - t_model).count(),
+                         c->pattern_reuses > 0 ? 1 : 0);
+        }
         return PB_OK;
     } catch (const std::bad_alloc&) {
         c->uploaded = false;

@@ -319,8 +319,10 @@ def test_mixed_weight_and_gradient_chain_match_fp64(name, make, opts):
     b = ctx.linearize_observations(Precision.Mixed)
     sel = (a["valid"] == 1) & (b["valid"] == 1)
     assert np.array_equal(a["valid"], b["valid"])
-    # the float-float copy of the FP64 residual keeps 48 of its 53 bits
-    np.testing.assert_allclose(b["residual"][sel], a["residual"][sel], rtol=1e-13, atol=1e-15)
+    # the FP64 residual, to a few ulps of the pixel coordinate (the compiler contracts the
+    # projection into FMAs differently at different call sites) and the 48 bits of its
+    # float-float copy
+    np.testing.assert_allclose(b["residual"][sel], a["residual"][sel], rtol=1e-13, atol=2e-12)
     wrel = np.abs(b["normal_weight"][sel] - a["normal_weight"][sel]) / a["normal_weight"][sel]
     assert wrel.max() < 1e-10, wrel.max()
     ctx.linearize_schur(0.0, Precision.Fp64)
