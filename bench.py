@@ -156,6 +156,24 @@ def cpu_cores():
     return os.cpu_count() or 1
 
 
+def max_over_ranks(value: float, world: int) -> float:
+    """The largest value over the ranks of the job (a job's time is its slowest rank's); the
+    process group's own device (NCCL: the current GPU, gloo: the host)."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def window_seed(rank: int) -> int:
+    """Seed of a rank's set of local-BA windows: every rank solves its own windows (weak scaling)."""
+    return 1234 + rank
+
+
 def cpu_sample(prob, opts, iterations, full_iterations):
     """Oracle (CPU FP64 restatement, all host threads) on `iterations` LM iterations of the
     workload, scaled to `full_iterations` iterations (ms per full solve)."""
@@ -218,7 +236,7 @@ def run_windows(args, rank, world, local_rank):
     from plabundle_gb300.batch import solve_batch
     from plabundle_gb300.problem import ImageRobustLoss, SolveOptions
 
-    wins = synth.window_problems(n_windows=args.windows, seed=1234 + rank)
+    wins = synth.window_problems(n_windows=args.windows, seed=window_seed(rank))
     torch.cuda.set_device(local_rank)
     o = SolveOptions()
     o.solver.imageRobustLoss = ImageRobustLoss.Huber
@@ -228,10 +246,15 @@ def run_windows(args, rank, world, local_rank):
     solve_batch(wins[:2 * args.workers], o, n_workers=args.workers, device=local_rank)  # warm-up
     rates, lats = [], None
     for _ in range(max(1, args.steps)):
+        # whole-job rate: every rank's windows over the slowest rank's time
+        if world > 1:
+            torch.distributed.barrier()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         res, lat = solve_batch(wins, o, n_workers=args.workers, device=local_rank)
-        rates.append(len(wins) / (time.perf_counter() - t0))
+        torch.cuda.synchronize()
+        dt = max_over_ranks(time.perf_counter() - t0, world)
+        rates.append(world * len(wins) / dt)
         lats = lat
     t0 = time.perf_counter()
     res1, lat1 = solve_batch(wins, o, n_workers=1, device=local_rank)
@@ -243,7 +266,7 @@ def run_windows(args, rank, world, local_rank):
     line = {"metric": "local-BA windows per second (batched)", "value": statistics.mean(rates), "unit": "windows/s",
             "impl": "gb300", "n_gpus": world, "steps": args.steps, "warmup": 1, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64 (mixed)", "data": "synthetic (seeded)",
-            "config": {"workload": f"{len(wins)} ring windows, 10-60 cameras, 1k-20k points",
+            "config": {"workload": f"{len(wins)} ring windows per GPU, 10-60 cameras, 1k-20k points",
                        "observations": int(sum(p.n_obs for p in wins)), "workers": args.workers,
                        "max_lm_iterations": 20, "loss": "huber_1.5px"},
             "latency_ms": {"p50": float(np.percentile(lats, 50)), "p99": float(np.percentile(lats, 99))},
@@ -391,11 +414,7 @@ def run_gb300(args, rank, world, local_rank):
     if world > 1:
         torch.distributed.barrier()
     clocks = sampler.stop()
-    ms_mixed = statistics.mean(t_mixed)
-    if world > 1:
-        t = torch.tensor([ms_mixed], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_mixed = float(t.item())
+    ms_mixed = max_over_ranks(statistics.mean(t_mixed), world)
     out_mixed = ctx.download()
     launches = sum(r["gpu_kernel_launches"] for r in reps_mixed)
 
