@@ -48,9 +48,9 @@ def parse_args():
 
 # LM iterations a converged solve of each workload takes.  The FP64 GPU path reproduces the
 # oracle's trajectory iteration for iteration (tests/test_gpu_parity.py), and on the 500-camera
-# aerial grid it converges in 81 iterations (GB300 measurement), so the CPU samples of the
+# aerial grid it converges in 82 iterations (GB300 measurement), so the CPU samples of the
 # reference arm are scaled to these counts.
-ITERATIONS_TO_CONVERGE = {"aerial": 81, "ring": 20}
+ITERATIONS_TO_CONVERGE = {"aerial": 82, "aerial_gcp": 21, "aerial3000_gcp": 27, "ring": 20}
 
 # DRAM traffic of one k_assemble<float> launch per observation: dram__bytes_read.sum +
 # dram__bytes_write.sum of an ncu capture on the 250-camera / 100k-point aerial grid
