@@ -123,7 +123,8 @@ typedef struct pb_solve_options {
     double linear_relative_tolerance;  /* 0: 2e-10 (online Schur path) */
     double linear_absolute_tolerance;  /* 0: 1e-12 */
     int32_t refinement_sweeps;         /* block-Jacobi mixed path: 1..3 refinement sweeps (unused by dense CG) */
-    int32_t preconditioner_cluster_size; /* BackendOptions::plaMatrixPreconditionerClusterSize (1) */
+    int32_t preconditioner_cluster_size; /* BackendOptions::plaMatrixPreconditionerClusterSize (1..16;
+                                          * accepted, the solution does not depend on it) */
     int32_t linear_solver;             /* 0 auto, 1 dense-Cholesky-preconditioned CG, 2 block-Jacobi PCG */
     double calibration[32];            /* CalibrationOptions numeric fields (27 used) */
     double control_point_weight;       /* ConstraintOptions::controlPointWeight (1) */

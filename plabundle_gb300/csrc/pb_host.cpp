@@ -216,9 +216,13 @@ int build_host_model(const pb_problem_desc* pr, const pb_solve_options* op, Host
     }
     m->loss = op->robust_loss;
     m->loss_scale = op->robust_loss_scale;
-    if (op->preconditioner_cluster_size > 1) {
-        *err = "only block-Jacobi cluster size 1 is implemented by the GB300 backend";
-        return PB_SOLVE_UNSUPPORTED;
+    // BackendOptions::plaMatrixPreconditionerClusterSize (validateOptions: 1..16) selects how the
+    // reference's block-Jacobi PCG groups blocks.  It changes the iteration count, not the solution
+    // (the CG runs to the same relative residual): the dense-factor preconditioner here subsumes
+    // any grouping, and the block-Jacobi PCG used beyond its size limit keeps single blocks.
+    if (op->preconditioner_cluster_size < 1 || op->preconditioner_cluster_size > 16) {
+        *err = "preconditioner cluster size must lie in [1, 16]";
+        return PB_SOLVE_INVALID_INPUT;
     }
 
     // --- control points (Track::controlPointConstraints): any constraint switches the problem to

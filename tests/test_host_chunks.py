@@ -105,3 +105,20 @@ def test_chunks_of_the_500_camera_workload_are_consistent(probe):
     assert nch * max_obs >= nobs
     # chunks are filled: on average at least 3/4 of max_obs observations
     assert nobs / nch > 0.75 * max_obs
+
+
+def test_preconditioner_cluster_sizes_are_accepted(probe):
+    """BackendOptions::plaMatrixPreconditionerClusterSize 1..16 is valid (validateOptions) and
+    leaves the solution unchanged: the host accepts it; 0 and 17 are invalid input."""
+    import numpy as np
+    p = synth.ring_problem(seed=3, n_cameras=8, n_points=200)
+    for size, status in ((1, 0), (4, 0), (16, 0), (0, 4), (17, 4)):
+        o = SolveOptions()
+        o.backend.plaMatrixPreconditionerClusterSize = size
+        desc, keep = native.problem_desc(p)
+        copts = native.solve_options(o, p)
+        out_i = np.zeros(8, np.int32)
+        fixed = np.zeros(p.n_cameras + 2, np.int32)
+        out_d = np.zeros(2)
+        probe.probe_model(C.byref(desc), C.byref(copts), out_i.ctypes.data, fixed.ctypes.data, out_d.ctypes.data)
+        assert out_i[0] == status, (size, out_i[0])
