@@ -16,7 +16,7 @@ import numpy as np
 
 from . import native
 from .problem import (Backend, GaugePolicy, PlaMatrixDiagnostics, Problem, QualitySummary, RefinedPoint, Result,
-                      SolveOptions, SolveStatus, summarize_problem)
+                      SolveOptions, SolveStatus, backend_name, summarize_problem)
 
 
 class SolverWorkspace:
@@ -181,8 +181,18 @@ class Solver:
     def solve(self, problem: Problem, options: SolveOptions | None = None,
               workspace: SolverWorkspace | None = None) -> Result:
         options = options or SolveOptions()
+        requested = options.backend.requested
+        if requested not in (Backend.Auto, Backend.Gb300):
+            # explicit backend that this build does not provide (src/solver.cpp:450-467); there is
+            # no CPU fallback to run instead
+            result = Result(requestedBackend=requested, usedBackend=requested, usedGpu=False,
+                            status=SolveStatus.BackendUnavailable, solutionUsable=False,
+                            backendMessage=f"backend {backend_name(requested)} is not provided by the GB300 build",
+                            backendSelectionReason="explicit_backend")
+            result.observationCount = summarize_problem(problem)["observationCount"]
+            return result
         ws = workspace or SolverWorkspace(options.backend.plaMatrixDevice)
-        result = Result(requestedBackend=options.backend.requested, usedBackend=Backend.Gb300)
+        result = Result(requestedBackend=requested, usedBackend=Backend.Gb300)
         result.observationCount = summarize_problem(problem)["observationCount"]
         err = validate_options(options) or validate_problem(problem)
         if err:
@@ -250,8 +260,10 @@ class Solver:
             result.solutionUsable = False
             if result.status in (SolveStatus.Success, SolveStatus.NoConvergence):
                 result.status = SolveStatus.NumericalFailure
-            result.backendSelectionReason = "explicit_backend; quality_gate_rejected"
+            how = "explicit_backend" if requested == Backend.Gb300 else "auto_selected_gb300"
+            result.backendSelectionReason = how + "; quality_gate_rejected"
         else:
-            result.backendSelectionReason = "explicit_backend; quality_gate_passed" if options.quality.enabled \
-                else "explicit_backend; quality_gate_disabled"
+            how = "explicit_backend" if requested == Backend.Gb300 else "auto_selected_gb300"
+            result.backendSelectionReason = how + ("; quality_gate_passed" if options.quality.enabled
+                                                   else "; quality_gate_disabled")
         return result

@@ -289,3 +289,16 @@ def test_quality_statistics_whitening_agrees_with_the_oracle():
     expect = np.sqrt(np.mean([(np.linalg.inv(O.control_point_whitening(c.record())[1]) ** 2).sum() / c.weight
                               for _, c in p.controlPoints]))
     assert abs(control_point_rms_uncertainty(p, o) - expect) < 1e-12 * expect
+
+
+def test_unavailable_backend_is_reported_without_running():
+    """An explicit backend this build does not provide: BackendUnavailable, no solution, no GPU
+    work (src/solver.cpp:450-467; the build has no CPU fallback to run instead)."""
+    from plabundle_gb300.problem import Backend
+    from plabundle_gb300.solver import Solver
+    o = SolveOptions()
+    o.backend.requested = Backend.PlaMatrixCpu
+    r = Solver().solve(base_ring(), o)
+    assert r.status == SolveStatus.BackendUnavailable
+    assert not r.solutionUsable and r.usedBackend == Backend.PlaMatrixCpu
+    assert "not provided" in r.backendMessage
