@@ -710,6 +710,25 @@ void launch_linearize_export(const Shape& S, const DevPtrs& D, double* res, doub
                                                                                        valid);
 }
 
+__global__ void k_gather_obs(long long nop, int ntp, DevPtrs D) {
+    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < nop) {
+        const int k = D.obs_orig[i];
+        D.obs_cam[i] = D.raw_cam[k];
+        D.obs_u[i] = D.raw_u[k];
+        D.obs_v[i] = D.raw_v[k];
+        D.obs_w[i] = D.raw_w[k];
+        D.obs_w_ff[i] = ff_pack(D.raw_w[k]);
+    }
+    if (i < ntp)
+        for (int o = D.trk_obs_begin[i]; o < D.trk_obs_begin[i + 1]; ++o) D.obs_trk[o] = static_cast<int>(i);
+}
+
+void launch_gather_obs(long long nop, int ntp, const DevPtrs& D, cudaStream_t st) {
+    const long long n = std::max<long long>(std::max<long long>(nop, ntp), 1);
+    k_gather_obs<<<static_cast<unsigned>((n + 255) / 256), 256, 0, st>>>(nop, ntp, D);
+}
+
 void launch_effective(const Shape& S, const DevPtrs& D, cudaStream_t st) {
     const int n = std::max(std::max(S.nc, S.ntp), 1);
     k_effective<<<(n + 127) / 128, 128, 0, st>>>(S, D);

@@ -57,6 +57,10 @@ template <typename T>
 void launch_reduce(const Shape& S, const DevPtrs& D, const AsmOut& O, const RedOut<double>& R, double damping,
                    cudaStream_t st);
 void launch_reduce_sums64(const Shape& S, const DevPtrs& D, const AsmOut& O, const RedOut<double>& R, cudaStream_t st);
+// Observations in processing order (cam, u, v, weight and its float-float copy, track) gathered
+// from the original-order arrays through obs_orig and trk_obs_begin.
+void launch_gather_obs(long long nop, int ntp, const DevPtrs& D, cudaStream_t st);
+
 template <typename T>
 void launch_back_substitute(const Shape& S, const DevPtrs& D, const double* trk_data, const T* obs_rec, const double* step_c,
                             double* step_p, double* part, const double* direct64, double* out, cudaStream_t st);

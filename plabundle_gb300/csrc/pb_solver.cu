@@ -280,38 +280,8 @@ void upload_structure(pb_gpu_ctx* c) {
         if (cpr.empty()) cpr.assign(12, 0.0);
         D.cp_rec = upload_new(A, cpr, st);
     }
-    // observations in processing order
-    std::vector<int> ocam(nop), otrk(nop);
-    std::vector<double> ou(nop), ov(nop), ow(nop);
-    for (int p = 0; p < ntp; ++p)
-        for (int o = m.trk_obs_begin[p]; o < m.trk_obs_begin[p + 1]; ++o) otrk[o] = p;
-    for (long long o = 0; o < nop; ++o) {
-        const int k = m.p_obs_orig[o];
-        ocam[o] = m.obs_cam[k];
-        ou[o] = m.obs_u[k];
-        ov[o] = m.obs_v[k];
-        const double w = std::isfinite(m.obs_weight[k]) && m.obs_weight[k] > 0 ? m.obs_weight[k] : 0.0;
-        const double s = std::isfinite(m.obs_scale[k]) && m.obs_scale[k] > 0 ? m.obs_scale[k] : 1.0;
-        ow[o] = w / (s * s);
-    }
-    D.obs_cam = upload_new(A, ocam, st);
-    D.obs_u = upload_new(A, ou, st);
-    D.obs_v = upload_new(A, ov, st);
-    D.obs_w = upload_new(A, ow, st);
-    {
-        std::vector<float2> wff(static_cast<size_t>(std::max<long long>(1, nop)), make_float2(0.f, 0.f));
-        for (long long o = 0; o < nop; ++o) wff[static_cast<size_t>(o)] = ff_pack(ow[o]);
-        D.obs_w_ff = upload_new(A, wff, st);
-    }
-    D.obs_trk = upload_new(A, otrk, st);
-    D.obs_orig = upload_new(A, m.p_obs_orig, st);
-    // pose CSR
-    D.row_ptr = upload_new(A, m.row_ptr, st);
-    D.col_idx = upload_new(A, m.col_idx, st);
-    D.diag_pos = upload_new(A, m.diag_pos, st);
-    D.up_csr = upload_new(A, m.up_csr, st);
-    D.up_csr_t = upload_new(A, m.up_csr_t, st);
-    // raw observations for the strict RMS
+    // observations: the original-order arrays (strict RMS) are uploaded once, and the
+    // processing-order arrays are gathered from them on the device
     std::vector<int> rbad(m.no, 0);
     std::vector<double> rw(m.no, 0.0);
     for (long long k = 0; k < m.no; ++k) {
@@ -329,6 +299,22 @@ void upload_structure(pb_gpu_ctx* c) {
     D.raw_v = upload_new(A, m.obs_v, st);
     D.raw_w = upload_new(A, rw, st);
     D.raw_bad = upload_new(A, rbad, st);
+    D.obs_orig = upload_new(A, m.p_obs_orig, st);
+    D.obs_cam = A.alloc<int>(static_cast<size_t>(std::max<long long>(1, nop)));
+    D.obs_u = A.alloc<double>(static_cast<size_t>(std::max<long long>(1, nop)));
+    D.obs_v = A.alloc<double>(static_cast<size_t>(std::max<long long>(1, nop)));
+    D.obs_w = A.alloc<double>(static_cast<size_t>(std::max<long long>(1, nop)));
+    D.obs_w_ff = A.alloc<float2>(static_cast<size_t>(std::max<long long>(1, nop)));
+    D.obs_trk = A.alloc<int>(static_cast<size_t>(std::max<long long>(1, nop)));
+    launch_gather_obs(nop, ntp, D, st);
+    check(cudaGetLastError(), "gather launch");
+    // pose CSR
+    D.row_ptr = upload_new(A, m.row_ptr, st);
+    D.col_idx = upload_new(A, m.col_idx, st);
+    D.diag_pos = upload_new(A, m.diag_pos, st);
+    D.up_csr = upload_new(A, m.up_csr, st);
+    D.up_csr_t = upload_new(A, m.up_csr_t, st);
+    // initial points of every track for the strict RMS before
     c->init_points_all = upload_new(A, m.points_in, st);
     std::vector<int> pot(nt, -1);
     for (int p = 0; p < ntp; ++p) pot[m.trk_order[p]] = p;
