@@ -101,40 +101,39 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
     bool elim = false, ok = false;
     constexpr bool kMixed = std::is_same<T, float>::value;
     if constexpr (kMixed) {
-    if (active) {
-        // mixed path: FP64 projection, float-float weight and gradient (no cost: the LM takes it
-        // from the line search)
-        const int cam = D.obs_cam[o];
-        const int trk = D.obs_trk[o];
-        const int tb0 = D.trk_obs_begin[trk];
-        first = tb0 - obs0;
-        k = D.trk_obs_begin[trk + 1] - tb0;
-        elim = D.trk_block[trk] >= 0;
-        const int grp = ng > 0 ? D.cam_group[cam] : -1;
-        const bool tangent = cam == S.gauge_scale && S.gauge_anchor >= 0 && S.gauge_baseline > 0.0;
-        DCam c;
-        load_cam(D.cams_eff + static_cast<size_t>(cam) * kCamStride, c);
-        const double* X = D.points + static_cast<size_t>(trk) * 3;
-        Proj pr;
-        LinFF F;
-        ok = project64(c, X[0], X[1], X[2], pr) &&
-             linearize_obs_ff(pr, D.obs_u[o], D.obs_v[o], D.cams_ff + static_cast<size_t>(cam) * kCamFF,
-                              ffl(D.pscale_ff[trk]), ffl(D.obs_w_ff[o]), S.loss,
-                              ff{S.loss_scale_hi, S.loss_scale_lo}, tangent, !S.ref_param, D.gauge_basis, ni,
-                              S.int_cols, F);
-        if (!ok) atomicOr(s_flags, 2);
-        s_info[tid] = (ok ? kOk : 0) | (elim ? kElim : 0) | ((grp + 1) << 2);
-        T* A = s_A + static_cast<size_t>(tid) * sA;
-        for (int a = 0; a < 6; ++a) {
-            A[a] = ok ? F.Jc[a] : T(0);
-            A[nA + a] = ok ? F.Jc[6 + a] : T(0);
-        }
-        for (int a = 0; a < ni; ++a) {
-            A[6 + a] = ok ? F.Ji[a] : T(0);
-            A[nA + 6 + a] = ok ? F.Ji[kMaxNI + a] : T(0);
-        }
-        VT* Dg = s_D + static_cast<size_t>(tid) * sD;
-        {
+        if (active) {
+            // mixed path: FP64 projection, float-float weight and gradient (no cost: the LM takes it
+            // from the line search)
+            const int cam = D.obs_cam[o];
+            const int trk = D.obs_trk[o];
+            const int tb0 = D.trk_obs_begin[trk];
+            first = tb0 - obs0;
+            k = D.trk_obs_begin[trk + 1] - tb0;
+            elim = D.trk_block[trk] >= 0;
+            const int grp = ng > 0 ? D.cam_group[cam] : -1;
+            const bool tangent = cam == S.gauge_scale && S.gauge_anchor >= 0 && S.gauge_baseline > 0.0;
+            DCam c;
+            load_cam(D.cams_eff + static_cast<size_t>(cam) * kCamStride, c);
+            const double* X = D.points + static_cast<size_t>(trk) * 3;
+            Proj pr;
+            LinFF F;
+            ok = project64(c, X[0], X[1], X[2], pr) &&
+                 linearize_obs_ff(pr, D.obs_u[o], D.obs_v[o], D.cams_ff + static_cast<size_t>(cam) * kCamFF,
+                                  ffl(D.pscale_ff[trk]), ffl(D.obs_w_ff[o]), S.loss,
+                                  ff{S.loss_scale_hi, S.loss_scale_lo}, tangent, !S.ref_param, D.gauge_basis, ni,
+                                  S.int_cols, F);
+            if (!ok) atomicOr(s_flags, 2);
+            s_info[tid] = (ok ? kOk : 0) | (elim ? kElim : 0) | ((grp + 1) << 2);
+            T* A = s_A + static_cast<size_t>(tid) * sA;
+            for (int a = 0; a < 6; ++a) {
+                A[a] = ok ? F.Jc[a] : T(0);
+                A[nA + a] = ok ? F.Jc[6 + a] : T(0);
+            }
+            for (int a = 0; a < ni; ++a) {
+                A[6 + a] = ok ? F.Ji[a] : T(0);
+                A[nA + 6 + a] = ok ? F.Ji[kMaxNI + a] : T(0);
+            }
+            VT* Dg = s_D + static_cast<size_t>(tid) * sD;
             for (int a = 0; a < 6; ++a) Dg[a] = ok ? F.g[a] : Val::zero();
             for (int a = 0; a < ni; ++a) Dg[6 + a] = ok ? F.g[9 + a] : Val::zero();
             // the point block, its factor and the projector of phases B and C stay in FP64: the
@@ -159,63 +158,60 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
                 for (int i = 0; i < 9; ++i) V[i] = 0.0;
             }
         }
-    }
     } else {
-    if (active) {
-        const int cam = D.obs_cam[o];
-        const int trk = D.obs_trk[o];
-        const int tb0 = D.trk_obs_begin[trk];
-        first = tb0 - obs0;
-        k = D.trk_obs_begin[trk + 1] - tb0;
-        elim = D.trk_block[trk] >= 0;
-        const int grp = ng > 0 ? D.cam_group[cam] : -1;
-        DCam c;
-        load_cam(D.cams_eff + static_cast<size_t>(cam) * kCamStride, c);
-        const double* X = D.points + static_cast<size_t>(trk) * 3;
-        const bool tangent = cam == S.gauge_scale && S.gauge_anchor >= 0 && S.gauge_baseline > 0.0;
-        ok = linearize_obs<T>(c, X[0], X[1], X[2], D.pscale[trk], D.obs_u[o], D.obs_v[o], D.obs_w[o], S.loss,
-                              S.loss_scale, tangent, !S.ref_param, D.gauge_basis, ni, S.int_cols, true, L, grad);
-        if (!ok) {
-            atomicOr(s_flags, 2);
-        } else {
-            cost = L.cost;
+        if (active) {
+            const int cam = D.obs_cam[o];
+            const int trk = D.obs_trk[o];
+            const int tb0 = D.trk_obs_begin[trk];
+            first = tb0 - obs0;
+            k = D.trk_obs_begin[trk + 1] - tb0;
+            elim = D.trk_block[trk] >= 0;
+            const int grp = ng > 0 ? D.cam_group[cam] : -1;
+            DCam c;
+            load_cam(D.cams_eff + static_cast<size_t>(cam) * kCamStride, c);
+            const double* X = D.points + static_cast<size_t>(trk) * 3;
+            const bool tangent = cam == S.gauge_scale && S.gauge_anchor >= 0 && S.gauge_baseline > 0.0;
+            ok = linearize_obs<T>(c, X[0], X[1], X[2], D.pscale[trk], D.obs_u[o], D.obs_v[o], D.obs_w[o], S.loss,
+                                  S.loss_scale, tangent, !S.ref_param, D.gauge_basis, ni, S.int_cols, true, L, grad);
+            if (!ok) {
+                atomicOr(s_flags, 2);
+            } else {
+                cost = L.cost;
+            }
+            s_info[tid] = (ok ? kOk : 0) | (elim ? kElim : 0) | ((grp + 1) << 2);
+            T* A = s_A + static_cast<size_t>(tid) * sA;
+            for (int a = 0; a < 6; ++a) {
+                A[a] = ok ? L.Jc[a] : T(0);
+                A[nA + a] = ok ? L.Jc[6 + a] : T(0);
+            }
+            for (int a = 0; a < ni; ++a) {
+                A[6 + a] = ok ? L.Ji[a] : T(0);
+                A[nA + 6 + a] = ok ? L.Ji[kMaxNI + a] : T(0);
+            }
+            // the observation's gradient -J^T w r (FP64): pose and intrinsic columns
+            VT* Dg = s_D + static_cast<size_t>(tid) * sD;
+            for (int a = 0; a < 6; ++a) Dg[a] = ok ? Val::make(grad[a]) : Val::zero();
+            for (int a = 0; a < ni; ++a) Dg[6 + a] = ok ? Val::make(grad[9 + a]) : Val::zero();
+            double* V = s_V + static_cast<size_t>(tid) * 9;
+            w64 = L.wd;
+            for (int i = 0; i < 6; ++i) jpT[i] = L.Jp[i];
+            if (elim && ok) {
+                // V_o = w Jp^T Jp from the Jacobian and the point gradient, in FP64
+                const double w = L.wd;
+                const double j0 = L.Jp[0], j1 = L.Jp[1], j2 = L.Jp[2], j3 = L.Jp[3], j4 = L.Jp[4], j5 = L.Jp[5];
+                V[0] = w * (j0 * j0 + j3 * j3);
+                V[1] = w * (j0 * j1 + j3 * j4);
+                V[2] = w * (j0 * j2 + j3 * j5);
+                V[3] = w * (j1 * j1 + j4 * j4);
+                V[4] = w * (j1 * j2 + j4 * j5);
+                V[5] = w * (j2 * j2 + j5 * j5);
+                V[6] = grad[6];
+                V[7] = grad[7];
+                V[8] = grad[8];
+            } else {
+                for (int i = 0; i < 9; ++i) V[i] = 0.0;
+            }
         }
-        s_info[tid] = (ok ? kOk : 0) | (elim ? kElim : 0) | ((grp + 1) << 2);
-        T* A = s_A + static_cast<size_t>(tid) * sA;
-        for (int a = 0; a < 6; ++a) {
-            A[a] = ok ? L.Jc[a] : T(0);
-            A[nA + a] = ok ? L.Jc[6 + a] : T(0);
-        }
-        for (int a = 0; a < ni; ++a) {
-            A[6 + a] = ok ? L.Ji[a] : T(0);
-            A[nA + 6 + a] = ok ? L.Ji[kMaxNI + a] : T(0);
-        }
-        // the observation's gradient -J^T w r (FP64): pose and intrinsic columns
-        VT* Dg = s_D + static_cast<size_t>(tid) * sD;
-        for (int a = 0; a < 6; ++a) Dg[a] = ok ? Val::make(grad[a]) : Val::zero();
-        for (int a = 0; a < ni; ++a) Dg[6 + a] = ok ? Val::make(grad[9 + a]) : Val::zero();
-        double* V = s_V + static_cast<size_t>(tid) * 9;
-        if constexpr (!kMixed) {
-        w64 = L.wd;
-        for (int i = 0; i < 6; ++i) jpT[i] = L.Jp[i];
-        if (elim && ok) {
-            // V_o = w Jp^T Jp from the Jacobian and the point gradient, in FP64
-            const double w = L.wd;
-            const double j0 = L.Jp[0], j1 = L.Jp[1], j2 = L.Jp[2], j3 = L.Jp[3], j4 = L.Jp[4], j5 = L.Jp[5];
-            V[0] = w * (j0 * j0 + j3 * j3);
-            V[1] = w * (j0 * j1 + j3 * j4);
-            V[2] = w * (j0 * j2 + j3 * j5);
-            V[3] = w * (j1 * j1 + j4 * j4);
-            V[4] = w * (j1 * j2 + j4 * j5);
-            V[5] = w * (j2 * j2 + j5 * j5);
-            V[6] = grad[6];
-            V[7] = grad[7];
-            V[8] = grad[8];
-        } else {
-            for (int i = 0; i < 9; ++i) V[i] = 0.0;
-        }
-        }
-    }
     }
     // chunk-local track slots: rank of each track's first observation among the chunk's
     // track starts (all lanes of every warp take part: blockDim is a multiple of 32)
