@@ -248,11 +248,21 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
         }
     }
     if (tid == 0 && ntc <= MT) s_tfirst[ntc] = nobs;
+    __syncthreads();
+    // Per track, one thread: track slot t goes to lane t / 4 of warp t % 4 (warps 4-7 for slots
+    // 128 and up), so that the FP64 work of the chunk's tracks runs on a few warps spread over
+    // the four sub-partitions rather than on scattered lanes of every warp.
+    const int tslot = (wid >> 2) * 128 + lane * 4 + (wid & 3);
+    const bool tact = tslot < ntc;
+    const int tfirst = tact ? s_tfirst[tslot] : 0;
+    const int tk = tact ? s_tfirst[tslot + 1] - tfirst : 0;
+    const int tobs = obs0 + tfirst;
+    const bool telim = tact && (s_info[tfirst] & kElim);
     // control points of the track (linearizeTrack, BundleAdjustPlaMatrixReferenceSchur.cpp:331-346):
     // their cost always, their point terms when the point is eliminated
     double cpV[6] = {0, 0, 0, 0, 0, 0}, cpg[3] = {0, 0, 0};
-    if (start && S.ncp > 0) {
-        const int trk = D.obs_trk[o];
+    if (tact && S.ncp > 0) {
+        const int trk = D.obs_trk[tobs];
         const double* X = D.points + static_cast<size_t>(trk) * 3;
         double cc_sum = 0.0;
         for (int q = D.trk_cp_begin[trk]; q < D.trk_cp_begin[trk + 1]; ++q) {
@@ -268,12 +278,12 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
                 cpg[a] -= cw * (rec[a] * r[0] + rec[3 + a] * r[1] + rec[6 + a] * r[2]);
             }
         }
-        if (slot < MT) s_cpc[slot] = cc_sum;
+        s_cpc[tslot] = cc_sum;
     }
-    if (start && elim) {
+    if (telim) {
         double V[6] = {cpV[0], cpV[1], cpV[2], cpV[3], cpV[4], cpV[5]}, rhs[3] = {cpg[0], cpg[1], cpg[2]};
-        for (int j = 0; j < k; ++j) {
-            const double* v = s_V + static_cast<size_t>(first + j) * 9;
+        for (int j = 0; j < tk; ++j) {
+            const double* v = s_V + static_cast<size_t>(tfirst + j) * 9;
             for (int i = 0; i < 6; ++i) V[i] += v[i];
             for (int i = 0; i < 3; ++i) rhs[i] += v[6 + i];
         }
@@ -307,8 +317,8 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
             }
         }
         if (singular) atomicOr(s_flags, 1);
-        double* st = s_V + static_cast<size_t>(first) * 9;
-        double* gt = O.trk_data + static_cast<size_t>(D.obs_trk[o]) * kTrackRec;
+        double* st = s_V + static_cast<size_t>(tfirst) * 9;
+        double* gt = O.trk_data + static_cast<size_t>(D.obs_trk[tobs]) * kTrackRec;
         for (int i = 0; i < 6; ++i) { st[i] = Ri[i]; gt[i] = Ri[i]; }
         for (int i = 0; i < 3; ++i) {
             st[6 + i] = q[i];
