@@ -56,7 +56,7 @@ ITERATIONS_TO_CONVERGE = {"aerial": 82, "aerial_gcp": 21, "aerial3000_gcp": 27, 
 # dram__bytes_write.sum of an ncu capture on the 250-camera / 100k-point aerial grid
 # (663 659 observations; profiles/k_assemble_aerial250.md).  The chunk plan is the same at 500
 # cameras, so the traffic scales with the observations.
-ASSEMBLY_DRAM_BYTES_PER_OBS = (39.366400e6 + 253.288704e6) / 663659
+ASSEMBLY_DRAM_BYTES_PER_OBS = (30.970112e6 + 251.056128e6) / 663659
 
 
 def workload(name):
