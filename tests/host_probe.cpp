@@ -155,8 +155,9 @@ extern "C" int probe_chunks(const pb_problem_desc* pr, const pb_solve_options* o
 }
 
 // Host model of a problem: status, message, and the gauge the host settled on.
-// out_i: [status, ref_param, n_fixed_cams, gauge_anchor, gauge_scale, n_control_points kept,
-//         camera_blocks]; fixed: the fixed cameras (n_cameras capacity); out_d: [gauge_baseline]
+// out_i (11 ints): [status, ref_param, n_fixed_cams, gauge_anchor, gauge_scale, n_control_points
+//         kept, camera_blocks, active_tracks, observations, rejected tracks, track_blocks];
+// fixed: the fixed cameras (n_cameras capacity); out_d: [gauge_baseline]
 extern "C" int probe_model(const pb_problem_desc* pr, const pb_solve_options* op, int* out_i, int* fixed,
                            double* out_d) {
     using namespace pb;
@@ -172,6 +173,10 @@ extern "C" int probe_model(const pb_problem_desc* pr, const pb_solve_options* op
     out_i[4] = m.gauge_scale;
     out_i[5] = static_cast<int>(m.cp_track.size());
     out_i[6] = m.ncb;
+    out_i[7] = m.active_tracks;
+    out_i[8] = m.obs_count;
+    out_i[9] = m.rejected;
+    out_i[10] = m.ntb;
     for (size_t i = 0; i < m.fixed_cams.size(); ++i) fixed[i] = m.fixed_cams[i];
     out_d[0] = m.gauge_baseline;
     return 0;

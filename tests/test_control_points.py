@@ -89,14 +89,15 @@ def ring_options():
 def host_model(probe, problem, options):
     desc, keep = native.problem_desc(problem)
     o = native.solve_options(options, problem)
-    out_i = np.zeros(8, np.int32)
+    out_i = np.zeros(12, np.int32)
     fixed = np.zeros(problem.n_cameras + 2, np.int32)
     out_d = np.zeros(2)
     probe.probe_model(C.byref(desc), C.byref(o), out_i.ctypes.data, fixed.ctypes.data, out_d.ctypes.data)
     del keep
     return {"status": int(out_i[0]), "ref_param": int(out_i[1]), "fixed_cameras": int(out_i[2]),
             "gauge_anchor": int(out_i[3]), "gauge_scale": int(out_i[4]), "kept": int(out_i[5]),
-            "camera_blocks": int(out_i[6]), "first_fixed": int(fixed[0]) if out_i[2] else -1,
+            "camera_blocks": int(out_i[6]), "active_tracks": int(out_i[7]), "observation_count": int(out_i[8]),
+            "rejected_initial_tracks": int(out_i[9]), "track_blocks": int(out_i[10]), "first_fixed": int(fixed[0]) if out_i[2] else -1,
             "gauge_baseline": float(out_d[0])}
 
 

@@ -117,7 +117,7 @@ def test_preconditioner_cluster_sizes_are_accepted(probe):
         o.backend.plaMatrixPreconditionerClusterSize = size
         desc, keep = native.problem_desc(p)
         copts = native.solve_options(o, p)
-        out_i = np.zeros(8, np.int32)
+        out_i = np.zeros(12, np.int32)
         fixed = np.zeros(p.n_cameras + 2, np.int32)
         out_d = np.zeros(2)
         probe.probe_model(C.byref(desc), C.byref(copts), out_i.ctypes.data, fixed.ctypes.data, out_d.ctypes.data)
