@@ -52,6 +52,33 @@ def fixed_gauge():
     return p
 
 
+def ragged():
+    """Ragged tracks: five empty tracks (repeated offsets), twenty tracks cut to one observation
+    (inactive) and twenty cut to two (the minimum of an active track)."""
+    p = ring(seed=11)
+    off = np.asarray(p.track_offsets, np.int64)
+    keep, offsets, points = [], [0], []
+    for t in range(p.n_tracks):
+        obs = list(range(off[t], off[t + 1]))
+        if t < 20:
+            obs = obs[:1]
+        elif t < 40:
+            obs = obs[:2]
+        if t % 60 == 0:
+            offsets.append(offsets[-1])
+            points.append(p.points[t])
+        keep += obs
+        offsets.append(offsets[-1] + len(obs))
+        points.append(p.points[t])
+    k = np.array(keep)
+    p.track_offsets = np.array(offsets, np.int64)
+    p.points = np.array(points, float)
+    p.obs_camera = np.asarray(p.obs_camera, np.int32)[k]
+    for name in ("obs_u", "obs_v", "obs_weight", "obs_scale"):
+        setattr(p, name, np.asarray(getattr(p, name), float)[k])
+    return p
+
+
 def no_usable_observation():
     p = ring()
     p.obs_weight = np.zeros(p.n_obs)
@@ -65,4 +92,5 @@ CASES = [
     ("least_squares", ring, lambda: options(ImageRobustLoss.LeastSquares)),
     ("cauchy", ring, lambda: options(ImageRobustLoss.Cauchy)),
     ("initial_rms_gate", lambda: ring(seed=9), lambda: options(max_initial_rms=40.0)),
+    ("ragged_tracks", ragged, lambda: options()),
 ]

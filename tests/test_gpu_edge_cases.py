@@ -1,8 +1,9 @@
 """Edge cases of the input on the GPU path against the oracle (FP64, the full LM solve through the
 C ABI): unusable observations (non-finite pixels, camera indices out of range, zero, negative or
 infinite weights, non-positive measurement scales), fixed tracks and cameras under an explicit
-gauge, the least-squares and Cauchy losses, the initial-RMS track gate, and a problem with no
-usable observation.  The FP64 path follows the oracle's LM trajectory iteration for iteration."""
+gauge, the least-squares and Cauchy losses, the initial-RMS track gate, ragged tracks (empty and
+single-observation tracks), and a problem with no usable observation.  The FP64 path follows the oracle's LM trajectory iteration for iteration; the
+mixed path reaches the oracle's fixed point."""
 import numpy as np
 import pytest
 
@@ -44,3 +45,31 @@ def test_no_usable_observation_is_invalid_input():
     assert ctx.upload(p, options()) == 0, ctx.L.pb_gpu_last_error(ctx.ctx)
     assert ctx.sizes()["observation_count"] == 0
     assert ctx.solve()["status"] == SolveStatus.InvalidInput
+
+
+# every case whose FP64 solve converges within 80 iterations (the fixed-track case does not: its
+# fixed points keep the noise of their initial triangulation)
+MIXED = [c for c in CASES if c[0] != "fixed_tracks_and_cameras"]
+
+
+@pytest.mark.parametrize("name,make,opts", MIXED, ids=[c[0] for c in MIXED])
+def test_mixed_edge_case_solve_reaches_the_oracle_fixed_point(name, make, opts):
+    """Mixed path (float-float weights and gradient, FP32 Jacobians, FP64 residual and cost) on the
+    same inputs: 1e-6 relative final cost, 1e-5 relative camera-centre error, identical inliers."""
+    p = make()
+    o_ref, o_mix = opts(), opts()
+    o_mix.backend.enablePlaMatrixMixedPrecision = True
+    o_ref.solver.maxIterations = o_mix.solver.maxIterations = 80
+    ref = O.Oracle(p, o_ref).solve()
+    assert ref["report"]["status"] == SolveStatus.Success
+    ctx = Gb300Context(0)
+    assert ctx.upload(p, o_mix) == 0, ctx.L.pb_gpu_last_error(ctx.ctx)
+    rep = ctx.solve()
+    out = ctx.download()
+    assert rep["status"] == SolveStatus.Success
+    rr = ref["report"]
+    assert abs(rep["final_cost"] - rr["final_cost"]) <= 1e-6 * rr["final_cost"]
+    C_ref = ref["cameras"][:, 9:12]
+    scale = np.linalg.norm(C_ref - C_ref.mean(0), axis=1).max()
+    assert np.abs(out["cameras"][:, 9:12] - C_ref).max() / scale < 1e-5
+    assert np.array_equal(out["valid"], ref["valid"])
