@@ -503,8 +503,8 @@ def run_gb300(args, rank, world, local_rank):
                      "algorithmic_bytes_per_launch": asm_bytes, "avg_launch_ms": asm_ms,
                      "peak_kind": f"{peak_kind} copy bandwidth",
                      "note": "issue-bound, not HBM-bound: float-float products on the FP32 pipe; ncu on the "
-                             "250-camera case: 51% of issue slots, FMA pipe 34%, FP64 pipe 23% of peak, "
-                             "DRAM 2.5% (profiles/k_assemble_aerial250.md)"},
+                             "250-camera case: 51% of issue slots, FMA pipe 34%, FP64 pipe 21% of peak, "
+                             "DRAM 2.4% (profiles/k_assemble_aerial250.md)"},
         "kernel_ms_per_solve": {k: v for k, v in kt.items()},
         "solve_breakdown_ms": {k: rep_t[k] for k in ("assembly_ms", "linear_ms", "back_substitution_ms",
                                                      "objective_ms", "total_ms")},
