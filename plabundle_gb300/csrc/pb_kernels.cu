@@ -14,61 +14,81 @@
 
 namespace pb {
 
+// The three fixed-order sums below are independent of one another and each is latency-bound on
+// a small grid (the chunk-record sum has one CTA per 32 record entries), so one launch runs them
+// side by side over block ranges [pose pairs | cameras | chunk records + cost].  Each keeps the
+// summation order of its own loop; the loads of a loop are issued ahead of its merge chain.
+template <typename T>
+struct ReduceArgs {
+    using part_t = typename Acc<T>::part_type;
+    const part_t* part_pair;
+    const part_t* part_cam;
+    const part_t* part_chunk;
+    const double* part_cost;
+    const int* part_flags;
+    double *vals, *rhs, *direct, *border, *border_t, *Cm, *result;
+    unsigned pair_blocks, cam_blocks;
+};
+
 // Sum of the chunk partials of every upper pose block, written to both CSR orientations.
 template <typename T>
-__global__ void k_reduce_pairs(Shape S, DevPtrs D, const typename Acc<T>::part_type* __restrict__ part_pair,
-                               double* __restrict__ vals) {
-    const long long idx = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void reduce_pairs(const Shape& S, const DevPtrs& D, const ReduceArgs<T>& R, unsigned blk) {
+    const long long idx = static_cast<long long>(blk) * blockDim.x + threadIdx.x;
     if (idx >= static_cast<long long>(S.nupper) * 36) return;
     const int u = static_cast<int>(idx / 36), e = static_cast<int>(idx - static_cast<long long>(u) * 36);
     Acc<T> acc;
-    for (int c = D.up_contrib_begin[u]; c < D.up_contrib_begin[u + 1]; ++c)
-        acc.merge_part(part_pair[static_cast<size_t>(D.up_contrib[c]) * 36 + e]);
+    const int c1 = D.up_contrib_begin[u + 1];
+#pragma unroll 4
+    for (int c = D.up_contrib_begin[u]; c < c1; ++c)
+        acc.merge_part(R.part_pair[static_cast<size_t>(D.up_contrib[c]) * 36 + e]);
     const double v = acc.value64();
-    vals[static_cast<size_t>(D.up_csr[u]) * 36 + e] = v;
+    R.vals[static_cast<size_t>(D.up_csr[u]) * 36 + e] = v;
     const int t = D.up_csr_t[u];
-    if (t >= 0) vals[static_cast<size_t>(t) * 36 + (e % 6) * 6 + e / 6] = v;
+    if (t >= 0) R.vals[static_cast<size_t>(t) * 36 + (e % 6) * 6 + e / 6] = v;
 }
 
 // Sum of the per-camera partials: rhs, direct rhs and the intrinsic border rows.
 template <typename T>
-__global__ void k_reduce_cams(Shape S, DevPtrs D, const typename Acc<T>::part_type* __restrict__ part_cam,
-                              double* __restrict__ rhs, double* __restrict__ direct, double* __restrict__ border,
-                              double* __restrict__ border_t) {
+__device__ __forceinline__ void reduce_cams(const Shape& S, const DevPtrs& D, const ReduceArgs<T>& R, unsigned blk) {
     const int camrec = 12 + S.ng * 6 * S.ni;
-    const long long idx = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const long long idx = static_cast<long long>(blk) * blockDim.x + threadIdx.x;
     if (idx >= static_cast<long long>(S.ncb) * camrec) return;
     const int i = static_cast<int>(idx / camrec), e = static_cast<int>(idx - static_cast<long long>(i) * camrec);
     Acc<T> acc;
-    for (int c = D.cam_contrib_begin[i]; c < D.cam_contrib_begin[i + 1]; ++c)
-        acc.merge_part(part_cam[static_cast<size_t>(D.cam_contrib[c]) * camrec + e]);
+    const int c1 = D.cam_contrib_begin[i + 1];
+#pragma unroll 4
+    for (int c = D.cam_contrib_begin[i]; c < c1; ++c)
+        acc.merge_part(R.part_cam[static_cast<size_t>(D.cam_contrib[c]) * camrec + e]);
     const double v = acc.value64();
-    if (e < 6) rhs[i * 6 + e] = v;
-    else if (e < 12) direct[i * 6 + e - 6] = v;
+    if (e < 6) R.rhs[i * 6 + e] = v;
+    else if (e < 12) R.direct[i * 6 + e - 6] = v;
     else {
         const int f = e - 12;  // (g * 6 + a) * ni + c
         const int g = f / (6 * S.ni), rem = f - g * 6 * S.ni, a = rem / S.ni, c = rem - a * S.ni;
-        border[(static_cast<size_t>(i) * 6 + a) * S.nb + g * S.ni + c] = v;
-        border_t[static_cast<size_t>(g * S.ni + c) * 6 * S.ncb + i * 6 + a] = v;
+        R.border[(static_cast<size_t>(i) * 6 + a) * S.nb + g * S.ni + c] = v;
+        R.border_t[static_cast<size_t>(g * S.ni + c) * 6 * S.ncb + i * 6 + a] = v;
     }
 }
 
 // Chunk-level sums (intrinsic block, intrinsic rhs): one CTA per 32 record entries, its warps
-// striding over the chunks, merged in warp order.  The last CTA sums the costs and flags.
+// striding over the chunks, merged in warp order.  The block after the last tile sums the costs
+// and flags.
 template <typename T>
-__global__ void k_reduce_chunks(Shape S, const typename Acc<T>::part_type* __restrict__ part_chunk,
-                                const double* __restrict__ part_cost, const int* __restrict__ part_flags,
-                                double* __restrict__ Cm, double* __restrict__ rhs_b, double* __restrict__ direct_b,
-                                double* __restrict__ result) {
+__device__ __forceinline__ void reduce_chunks(const Shape& S, const ReduceArgs<T>& R, unsigned blk) {
     const int nb = S.nb, chrec = nb * nb + 2 * nb;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int tiles = (chrec + 31) / 32;
-    if (static_cast<int>(blockIdx.x) < tiles) {
+    double* Cm = R.Cm;
+    double* rhs_b = R.rhs + 6 * S.ncb;
+    double* direct_b = R.direct + 6 * S.ncb;
+    if (static_cast<int>(blk) < tiles) {
         __shared__ typename Acc<T>::part_type s_acc[8][32];
-        const int e = blockIdx.x * 32 + lane;
+        const int e = blk * 32 + lane;
         Acc<T> acc;
-        if (e < chrec)
-            for (int c = wid; c < S.nchunks; c += nw) acc.merge_part(part_chunk[static_cast<size_t>(c) * chrec + e]);
+        if (e < chrec) {
+#pragma unroll 4
+            for (int c = wid; c < S.nchunks; c += nw) acc.merge_part(R.part_chunk[static_cast<size_t>(c) * chrec + e]);
+        }
         s_acc[wid][lane] = acc.part();
         __syncthreads();
         if (wid == 0 && e < chrec) {
@@ -86,8 +106,8 @@ __global__ void k_reduce_chunks(Shape S, const typename Acc<T>::part_type* __res
     double c = 0.0;
     int f = 0;
     for (int i = threadIdx.x; i < S.nchunks; i += blockDim.x) {
-        c += part_cost[i];
-        f |= part_flags[i];
+        c += R.part_cost[i];
+        f |= R.part_flags[i];
     }
     s_cost[threadIdx.x] = c;
     s_flag[threadIdx.x] = f;
@@ -100,9 +120,19 @@ __global__ void k_reduce_chunks(Shape S, const typename Acc<T>::part_type* __res
         __syncthreads();
     }
     if (threadIdx.x == 0) {
-        result[0] = s_cost[0];
-        result[1] = static_cast<double>(s_flag[0]);
+        R.result[0] = s_cost[0];
+        R.result[1] = static_cast<double>(s_flag[0]);
     }
+}
+
+// 256 threads per block (the chunk-record sum's warp count and cost buffers assume it); the block
+// range decides the sum, uniformly per block.
+template <typename T>
+__global__ void __launch_bounds__(256) k_reduce_sums(Shape S, DevPtrs D, ReduceArgs<T> R) {
+    const unsigned b = blockIdx.x;
+    if (b < R.pair_blocks) reduce_pairs<T>(S, D, R, b);
+    else if (b < R.pair_blocks + R.cam_blocks) reduce_cams<T>(S, D, R, b - R.pair_blocks);
+    else reduce_chunks<T>(S, R, b - R.pair_blocks - R.cam_blocks);
 }
 
 // Intrinsic priors (assembleReferencePriors, ...ReferenceSchur.cpp:492-536) and
@@ -660,19 +690,34 @@ static AsmOutT<T> typed(const AsmOut& o) {
 }
 
 template <typename T>
+void launch_reduce_sums(const Shape& S, const DevPtrs& D, const AsmOut& O, const RedOut<double>& R, cudaStream_t st) {
+    const AsmOutT<T> P = typed<T>(O);
+    ReduceArgs<T> A;
+    A.part_pair = P.part_pair;
+    A.part_cam = P.part_cam;
+    A.part_chunk = P.part_chunk;
+    A.part_cost = O.part_cost;
+    A.part_flags = O.part_flags;
+    A.vals = R.vals;
+    A.rhs = R.rhs;
+    A.direct = R.direct;
+    A.border = R.border;
+    A.border_t = R.border_t;
+    A.Cm = R.Cm;
+    A.result = R.result;
+    const long long np = static_cast<long long>(S.nupper) * 36;
+    const long long nc = static_cast<long long>(S.ncb) * (12 + S.ng * 6 * S.ni);
+    A.pair_blocks = static_cast<unsigned>((np + 255) / 256);
+    A.cam_blocks = static_cast<unsigned>((nc + 255) / 256);
+    const int chrec = S.nb * S.nb + 2 * S.nb;
+    const unsigned chunk_blocks = static_cast<unsigned>((chrec + 31) / 32) + 1;
+    k_reduce_sums<T><<<A.pair_blocks + A.cam_blocks + chunk_blocks, 256, 0, st>>>(S, D, A);
+}
+
+template <typename T>
 void launch_reduce(const Shape& S, const DevPtrs& D, const AsmOut& O, const RedOut<double>& R, double damping,
                    cudaStream_t st) {
-    const AsmOutT<T> P = typed<T>(O);
-    const long long np = static_cast<long long>(S.nupper) * 36;
-    if (np > 0) k_reduce_pairs<T><<<static_cast<unsigned>((np + 255) / 256), 256, 0, st>>>(S, D, P.part_pair, R.vals);
-    const long long nc = static_cast<long long>(S.ncb) * (12 + S.ng * 6 * S.ni);
-    if (nc > 0)
-        k_reduce_cams<T><<<static_cast<unsigned>((nc + 255) / 256), 256, 0, st>>>(S, D, P.part_cam, R.rhs, R.direct,
-                                                                                  R.border, R.border_t);
-    const int chrec = S.nb * S.nb + 2 * S.nb;
-    const int tiles = (chrec + 31) / 32;
-    k_reduce_chunks<T><<<tiles + 1, 256, 0, st>>>(S, P.part_chunk, O.part_cost, O.part_flags, R.Cm, R.rhs + 6 * S.ncb,
-                                                  R.direct + 6 * S.ncb, R.result);
+    launch_reduce_sums<T>(S, D, O, R, st);
     const int nf = std::max(S.ncb * 6, 1);
     k_finalize<<<(nf + 255) / 256, 256, 0, st>>>(S, D, R.vals, R.Cm, R.rhs + 6 * S.ncb, R.direct + 6 * S.ncb, R.result,
                                                   damping);
@@ -681,17 +726,7 @@ void launch_reduce(const Shape& S, const DevPtrs& D, const AsmOut& O, const RedO
 // The fixed-order sums of FP64 chunk partials of launch_reduce, without the damping and prior
 // finalisation (the backward pass finalises its exact Hessian itself).
 void launch_reduce_sums64(const Shape& S, const DevPtrs& D, const AsmOut& O, const RedOut<double>& R, cudaStream_t st) {
-    const AsmOutT<double> P = typed<double>(O);
-    const long long np = static_cast<long long>(S.nupper) * 36;
-    if (np > 0) k_reduce_pairs<double><<<static_cast<unsigned>((np + 255) / 256), 256, 0, st>>>(S, D, P.part_pair, R.vals);
-    const long long nc = static_cast<long long>(S.ncb) * (12 + S.ng * 6 * S.ni);
-    if (nc > 0)
-        k_reduce_cams<double><<<static_cast<unsigned>((nc + 255) / 256), 256, 0, st>>>(S, D, P.part_cam, R.rhs, R.direct,
-                                                                                       R.border, R.border_t);
-    const int chrec = S.nb * S.nb + 2 * S.nb;
-    const int tiles = (chrec + 31) / 32;
-    k_reduce_chunks<double><<<tiles + 1, 256, 0, st>>>(S, P.part_chunk, O.part_cost, O.part_flags, R.Cm, R.rhs + 6 * S.ncb,
-                                                       R.direct + 6 * S.ncb, R.result);
+    launch_reduce_sums<double>(S, D, O, R, st);
 }
 
 template <typename T>

@@ -479,7 +479,7 @@ void assemble(pb_gpu_ctx* c, double damping, int precision, double* cost, int* f
     {
         Timer t(c, 3);
         launch_reduce<T>(S, D, B.out, c->red, damping, c->stream);
-        c->launches += 4;
+        c->launches += 2;  // k_reduce_sums, k_finalize
     }
     check(cudaGetLastError(), "assemble launch");
     check(cudaMemcpyAsync(c->h_scratch, c->red.result, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "D2H");
@@ -1550,7 +1550,7 @@ pb_status adjoint_core(pb_gpu_ctx* c, int newton, pb_adjoint_report* rep, float*
     launch_adjoint_hessian(S, D, B, st);
     launch_adjoint_schur(S, D, B, B.part, R, st);
     launch_adjoint_rhs(S, D, B, R, st);
-    c->launches += 8;
+    c->launches += 6;
     check(cudaGetLastError(), "adjoint launch");
     check(cudaEventRecord(ev[1], st), "event");
     int flags = 0;
