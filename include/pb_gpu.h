@@ -129,6 +129,10 @@ typedef struct pb_solve_options {
     double calibration[32];            /* CalibrationOptions numeric fields (27 used) */
     double control_point_weight;       /* ConstraintOptions::controlPointWeight (1) */
     double control_point_huber_delta;  /* ConstraintOptions::controlPointHuberDeltaMeters (0.2) */
+    int32_t factor_reuse;              /* dense-factor reuse across LM iterations: 0 default (the mixed
+                                        * path keeps its FP32 factor while it preconditions well, the
+                                        * FP64 path refactors every iteration), 1 keep on both paths,
+                                        * 2 refactor every iteration on both paths */
 } pb_solve_options;
 
 /* PlaMatrixDiagnostics (include/plabundle/result.h:91-128) + QualitySummary fields. */
@@ -268,26 +272,6 @@ pb_status pb_gpu_solve_batch(int32_t device, int32_t n_problems, const pb_proble
                              double* const* cameras_out, double* const* points_out, int8_t* const* valid_out,
                              double* latency_ms);
 
-/* Allocation-free robust objective of caller-owned device arrays.  No counterpart in the
- * reference: it serves callers that keep their own cameras, points and observations in device
- * memory and may not allocate (a real-time loop whose device memory is reserved up front, where
- * a cudaMalloc or cudaFree would synchronise the device and stall its other streams), and that
- * cannot create a context (pb_gpu_create / pb_gpu_upload allocate).  It is the line-search cost
- * kernel with its per-block partials in one fixed file-scope device array:
- *   - cameras: n_cameras * PB_CAMERA_STRIDE records (effective intrinsics), points: n_points * 3,
- *     observations: camera index, point index, u, v and w = weight / measurementScale^2; all
- *     device pointers, read only;
- *   - cost (host): sum of the robust costs of the observations that project validly;
- *     invalid_projections (host, may be NULL): how many did not (behind the camera, non-finite);
- *   - at most PB_NOALLOC_MAX_OBS observations, else PB_ERR_BOUNDS before any launch; a camera or
- *     point index out of range is skipped on the device and reported as PB_ERR_BOUNDS;
- *   - the scratch array is shared by all calls on a device: calls that overlap in time on one
- *     device race, so callers serialise them; nothing in it has to start at zero (every element
- *     read is written earlier in the same call);
- *   - the first call on a device resolves the array's address (cudaGetSymbolAddress, which may
- *     load the module): make it before any stream capture;
- *   - work is enqueued on `stream` (a cudaStream_t, NULL for the legacy default stream) and the
- *     call returns after that stream has finished it. */
 /* Device-side snapshot of the current state (poses, points, group intrinsics) and its restore
  * (no counterpart in the reference).  Together with pb_gpu_set_observations they re-solve a
  * problem after a measurement update from a known state without a new upload, e.g. the
@@ -320,7 +304,9 @@ pb_status pb_gpu_set_observations(pb_gpu_ctx* ctx, int64_t n, const int64_t* ind
  * Any output may be NULL.  The state must be a converged fixed point of the uploaded problem
  * (after pb_gpu_solve); clamped intrinsics are treated as free.  The reduced-system buffers are
  * reused, so a pb_gpu_linearize_schur is needed before the next pb_gpu_solve_reduced.  The
- * reduced sums use FP64 atomics: results vary in the last bits from run to run. */
+ * reduced system is summed in a fixed order without atomics; only the few gauge and fixed-
+ * camera cross terms of the gradients use FP64 atomics, so those entries of
+ * grad_initial_cameras / grad_initial_points may vary in the last bits from run to run. */
 typedef struct pb_adjoint_report {
     int32_t status;                /* pb_status of the call */
     int32_t linear_iterations;     /* CG / PCG iterations of the adjoint solve */
@@ -344,6 +330,30 @@ pb_status pb_gpu_backward(pb_gpu_ctx* ctx, const double* grad_cameras, const dou
  * component|; gradient_norm: |reduced gradient| at the state before the step (may be NULL). */
 pb_status pb_gpu_newton_step(pb_gpu_ctx* ctx, double* step_max, double* gradient_norm);
 
+/* Allocation-free robust objective of caller-owned device arrays.  No counterpart in the
+ * reference: it serves callers that keep their own cameras, points and observations in device
+ * memory and may not allocate (a real-time loop whose device memory is reserved up front, where
+ * a cudaMalloc or cudaFree would synchronise the device and stall its other streams), and that
+ * cannot create a context (pb_gpu_create / pb_gpu_upload allocate).  It is the line-search cost
+ * kernel with its per-block partials in one fixed file-scope device array:
+ *   - cameras: n_cameras * PB_CAMERA_STRIDE records (effective intrinsics), points: n_points * 3,
+ *     observations: camera index, point index, u, v and w = weight / measurementScale^2; all
+ *     device pointers, read only;
+ *   - cost (host): sum of the robust costs of the observations that project validly;
+ *     invalid_projections (host, may be NULL): how many did not (behind the camera, non-finite);
+ *   - at most PB_NOALLOC_MAX_OBS observations, else PB_ERR_BOUNDS before any launch; a camera or
+ *     point index out of range is skipped on the device and reported as PB_ERR_BOUNDS;
+ *   - the scratch array is shared by all calls on a device: calls that overlap in time on one
+ *     device race, so callers serialise them; nothing in it has to start at zero (every element
+ *     read is written earlier in the same call);
+ *   - the first call on a device resolves the array's address (cudaGetSymbolAddress, which may
+ *     load the module), so that first call should come before any stream capture; the address
+ *     is kept for the life of the process, so the call must not be used across a
+ *     cudaDeviceReset of that device;
+ *   - work is enqueued on `stream` (a cudaStream_t, NULL for the legacy default stream); the call
+ *     copies its three totals back and synchronises `stream` before it returns;
+ *   - an error already pending on the calling thread (cudaPeekAtLastError) is left in place and
+ *     the call returns PB_ERR_CUDA without launching. */
 #define PB_NOALLOC_MAX_OBS 4194304
 pb_status pb_gpu_objective_noalloc(const double* cameras, int32_t n_cameras, const double* points, int32_t n_points,
                                    const int32_t* obs_camera, const int32_t* obs_point, const double* obs_u,

@@ -31,7 +31,7 @@ def _nvcc() -> str:
 
 
 def _flags(verbose_ptxas: bool) -> list:
-    f = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-Xcompiler", "-pthread",
+    f = ["-O3", "-std=c++20", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-Xcompiler", "-pthread",
          "-I", os.path.join(ROOT, "include")] + ARCH
     if verbose_ptxas:
         f += ["-Xptxas", "-v"]

@@ -459,7 +459,7 @@ __global__ void __launch_bounds__(256) k_back_substitute(Shape S, DevPtrs D, con
                                                          double* __restrict__ step_p, double* __restrict__ part) {
     // Point steps dp = V^-1 (g_p - W^T dc) = R^-T (q - sum_o Y_o^T A_o dc) from the records the
     // assembly kept (A = [J_pose | J_intr] rows and Y = w Jp R^-T of every observation), with
-    // FP64 accumulation (backSubstituteReferencePoints, ...ReferenceSchur.cpp:538-590).
+    // FP64 accumulation (recoverReferencePointSteps, BundleAdjustPlaMatrixReferenceSchur.cpp:982-1082).
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int nA = 6 + S.ni, stride = 2 * nA + 6;
     double dd = 0.0, ss = 0.0;

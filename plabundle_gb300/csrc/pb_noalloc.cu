@@ -14,7 +14,11 @@
 //   - the array is shared by all callers on a device: calls that overlap in time on one device
 //     race; callers serialise them (one stream, or host-side ordering);
 //   - the array's device address is resolved with cudaGetSymbolAddress on the first call on each
-//     device (that call may load the module); make the first call before capturing a stream.
+//     device (that call may load the module), so that first call should come before any stream
+//     capture; the address is kept for the life of the process (not valid across a
+//     cudaDeviceReset);
+//   - an error already pending on the calling thread is left for its owner: the call returns
+//     PB_ERR_CUDA without launching, and every status it reads afterwards is its own.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -126,6 +130,8 @@ extern "C" pb_status pb_gpu_objective_noalloc(const double* cameras, int32_t n_c
         if (invalid_projections) *invalid_projections = 0;
         return PB_OK;
     }
+    // an error pending from earlier work on this thread is not this call's: leave it in place
+    if (cudaPeekAtLastError() != cudaSuccess) return PB_ERR_CUDA;
     double* scratch = noalloc_scratch();
     if (!scratch) return PB_ERR_CUDA;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
@@ -133,6 +139,7 @@ extern "C" pb_status pb_gpu_objective_noalloc(const double* cameras, int32_t n_c
     k_objective_part<<<nblocks, kNoAllocThreads, 0, st>>>(cameras, n_cameras, points, n_points, obs_camera, obs_point,
                                                           obs_u, obs_v, obs_w, static_cast<long long>(n_obs),
                                                           robust_loss, robust_loss_scale, scratch);
+    if (cudaGetLastError() != cudaSuccess) return PB_ERR_CUDA;
     k_objective_final<<<1, kNoAllocThreads, 0, st>>>(nblocks, scratch);
     if (cudaGetLastError() != cudaSuccess) return PB_ERR_CUDA;
     double totals[3] = {0.0, 0.0, 0.0};

@@ -22,7 +22,7 @@ def host_probe(tmp_path_factory):
     from plabundle_gb300 import native
     here = os.path.dirname(os.path.abspath(__file__))
     out = str(tmp_path_factory.mktemp("probe") / "libhostprobe.so")
-    cmd = ["g++", "-std=c++17", "-O1", "-fPIC", "-shared", "-pthread", "-I", os.path.join(ROOT, "include"),
+    cmd = ["g++", "-std=c++20", "-O1", "-fPIC", "-shared", "-pthread", "-I", os.path.join(ROOT, "include"),
            os.path.join(here, "host_probe.cpp"), os.path.join(ROOT, "plabundle_gb300", "csrc", "pb_host.cpp"),
            "-o", out]
     subprocess.run(cmd, check=True, capture_output=True)
