@@ -46,17 +46,42 @@ def parse_args():
     return ap.parse_args()
 
 
-# LM iterations a converged solve of each workload takes.  The FP64 GPU path reproduces the
-# oracle's trajectory iteration for iteration (tests/test_gpu_parity.py), and on the 500-camera
-# aerial grid it converges in 82 iterations (GB300 measurement), so the CPU samples of the
-# reference arm are scaled to these counts.
-ITERATIONS_TO_CONVERGE = {"aerial": 82, "aerial_gcp": 21, "aerial3000_gcp": 27, "ring": 20}
+# LM iterations of a converged CPU solve of the large workloads, which a bounded CPU sample is
+# scaled to.  The 500-camera grid uses the oracle's own converged solve, measured when its fixture
+# was generated (tests/golden/aerial_500cam_200kpt_oracle.npz: 36 iterations); the control-point
+# workloads have no CPU fixture and use the iteration counts of the FP64 GPU path on them.  The
+# 20-camera ring is solved in full on the CPU (a fraction of a second), with no scaling.
+FP64_GPU_ITERATIONS = {"aerial_gcp": 21, "aerial3000_gcp": 27}
+
+
+def converged_iterations(workload_name):
+    """(LM iterations of a converged CPU solve, where the count comes from), or (None, ...) for a
+    workload that the CPU solves in full."""
+    if workload_name == "ring":
+        return None, "full solve"
+    if workload_name == "aerial":
+        m = measured_converged_cpu_solve(workload_name)
+        if m is not None:
+            return m["iterations"], "the oracle's converged solve of the committed fixture"
+    return FP64_GPU_ITERATIONS.get(workload_name, 36), "the FP64 GPU path's converged solve"
 
 # DRAM traffic of one k_assemble<float> launch per observation: dram__bytes_read.sum +
 # dram__bytes_write.sum of an ncu capture on the 250-camera / 100k-point aerial grid
 # (663 659 observations; profiles/k_assemble_aerial250.md).  The chunk plan is the same at 500
 # cameras, so the traffic scales with the observations.
 ASSEMBLY_DRAM_BYTES_PER_OBS = (30.970112e6 + 251.056128e6) / 663659
+# Warp instructions of one k_assemble<float> launch per observation (smsp__inst_executed.sum of the
+# same capture).
+ASSEMBLY_INST_PER_OBS = 902579227 / 663659
+SMS = 152  # streaming multiprocessors of a GB300
+
+# What the mixed path keeps in FP64 (everything else of the assembly and the CG preconditioner is
+# FP32 or float-float on the FP32 pipe).
+MIXED_FP64_SPLIT = ("projection and residual; 3x3 point blocks, their factor and the per-observation "
+                    "projector (phases B and C of the assembly); point back-substitution; the reduced matrix "
+                    "and vectors of the CG (FP64 SpMV), the cost, gain ratio and line search; FP32: Jacobians, "
+                    "the dense preconditioner factor; float-float: robust weight, gradient chain, all Schur "
+                    "products and sums")
 
 
 def workload(name):
@@ -176,20 +201,32 @@ def window_seed(rank: int) -> int:
 
 def cpu_sample(prob, opts, iterations, full_iterations):
     """Oracle (CPU FP64 restatement, all host threads) on `iterations` LM iterations of the
-    workload, scaled to `full_iterations` iterations (ms per full solve)."""
+    workload, scaled to `full_iterations` iterations (ms per full solve); with
+    `full_iterations` None, the whole solve under the workload's own budget, unscaled."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     import copy
     o2 = copy.deepcopy(opts)
-    o2.solver.maxIterations = iterations
+    if full_iterations is not None:
+        o2.solver.maxIterations = iterations
     orc = O.Oracle(prob, o2, num_threads=cpu_cores())
     t = time.perf_counter()
     r = orc.solve()
     dt = time.perf_counter() - t
     it = max(1, r["report"]["iterations"])
     per_it = dt / it
+    if full_iterations is None:
+        return dt * 1e3, {"sample_iterations": it, "sample_seconds": dt, "per_iteration_ms": per_it * 1e3}
     return per_it * full_iterations * 1e3, {"sample_iterations": it, "sample_seconds": dt,
                                            "per_iteration_ms": per_it * 1e3}
+
+
+def cpu_sample_text(info, full_it, source):
+    if full_it is None:
+        return (f"the complete converged solve ({info['sample_iterations']} LM iterations, "
+                f"{info['sample_seconds']:.2f} s); CPU FP64 restatement of the reference with OpenMP")
+    return (f"{info['sample_iterations']} LM iterations of the workload ({info['sample_seconds']:.1f} s), "
+            f"scaled to the {full_it} iterations of {source}; CPU FP64 restatement of the reference with OpenMP")
 
 
 def problem_bytes(prob):
@@ -202,11 +239,27 @@ def problem_bytes(prob):
     return h2d, d2h
 
 
+def measured_converged_cpu_solve(workload_name):
+    """Wall time of one complete converged CPU FP64 solve of the 500-camera workload, measured when
+    its committed fixture was generated (a cross-check of the sampled CPU baseline), or None."""
+    if workload_name != "aerial":
+        return None
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    import make_c1_fixture as FX
+    fx = FX.load_fixture()
+    if fx is None:
+        return None
+    m = fx[0]
+    return {"seconds": m["wall_seconds"], "threads": m["threads"], "cpu": m["cpu"], "machine": m["machine"],
+            "iterations": m["report"]["iterations"], "status": m["report"]["status"],
+            "source": "tests/golden/aerial_500cam_200kpt_oracle.npz (make_c1_fixture.py)"}
+
+
 def run_reference(args, rank):
     if rank != 0:
         return
     prob, opts, cfg = workload(args.workload)
-    full_it = ITERATIONS_TO_CONVERGE[args.workload]
+    full_it, source = converged_iterations(args.workload)
     vals = []
     for i in range(args.warmup + args.steps):
         ms, info = cpu_sample(prob, opts, args.cpu_iterations, full_it)
@@ -218,9 +271,8 @@ def run_reference(args, rank):
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
             "config": cfg,
             "cpu_baseline": {"value": v, "unit": "ms", "cores": cpu_cores(), "kind": "port",
-                             "sample": f"{info['sample_iterations']} LM iterations of the workload per step, "
-                                       f"scaled to the {full_it} iterations of a converged solve (CPU FP64 "
-                                       f"restatement of the reference, OpenMP)"},
+                             "sample": "per step: " + cpu_sample_text(info, full_it, source),
+                             "converged_solve_measured": measured_converged_cpu_solve(args.workload)},
             "e2e": {"value": v, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -418,13 +470,18 @@ def run_gb300(args, rank, world, local_rank):
     out_mixed = ctx.download()
     launches = sum(r["gpu_kernel_launches"] for r in reps_mixed)
 
-    # FP64 GPU path (same kernels in double precision)
-    opts64 = opts
-    opts64.backend.enablePlaMatrixMixedPrecision = False
+    # FP64 GPU paths (same kernels in double precision): the trajectory-parity arm refactors the
+    # FP64 dense preconditioner every LM iteration; the like-for-like arm keeps it across LM
+    # iterations under the mixed path's reuse policy (pb_solve_options.factor_reuse = 1)
     ctx.copts.precision = 0
     t_64, reps_64 = timed_solves(max(1, args.steps // 2), 1)
     out_64 = ctx.download()
     ms_64 = statistics.mean(t_64)
+    ctx.copts.factor_reuse = 1
+    t_64r, reps_64r = timed_solves(max(1, args.steps // 2), 1)
+    out_64r = ctx.download()
+    ms_64r = statistics.mean(t_64r)
+    ctx.copts.factor_reuse = 0
     ctx.copts.precision = 1
 
     # per-kernel device times of one mixed solve (CUDA events on the context stream)
@@ -432,6 +489,7 @@ def run_gb300(args, rank, world, local_rank):
     rep_t = ctx.solve()
     kt = ctx.kernel_times()
     ctx.set_timing(False)
+    out_t = ctx.download()
 
     s = ctx.sizes()
     p = ctx.problem
@@ -442,12 +500,30 @@ def run_gb300(args, rank, world, local_rank):
     # system written (pose blocks both triangles, border, rhs and direct rhs in FP32).
     nnzb = 2 * s["n_pairs"] + s["camera_blocks"]
     red_bytes = 4 * (36 * nnzb + 6 * s["camera_blocks"] * (s["dim"] - 6 * s["camera_blocks"]) + 2 * s["dim"])
-    asm_bytes = 37 * nop + (24 + 8 + 48) * ntp + red_bytes
+    ni = s["ni"]
+    asm_bytes = (37 + 4 * (2 * (6 + ni) + 6)) * nop + (24 + 8 + 96) * ntp + red_bytes
     asm_ms = kt["assemble_ms"] / max(1, kt["assemble_launches"])
     peak, peak_kind = measured_peaks()
     achieved = asm_bytes / (asm_ms * 1e-3) / 1e9 if asm_ms > 0 else None
+    # issue roofline: warp instructions of one launch (per observation, from the committed ncu
+    # capture) over the CUDA-event time, against 4 issue slots per SM per cycle at the sampled clock
+    sm_mhz = clocks.get("sm_mhz") or 2070.0
+    issue_peak = 4 * SMS * sm_mhz * 1e-3  # G warp instructions / s
+    issue_achieved = ASSEMBLY_INST_PER_OBS * nop / (asm_ms * 1e-3) / 1e9 if asm_ms > 0 else None
+    # CG (k_dense_cg): bytes one iteration reads -- the FP64 reduced matrix (pose blocks, both
+    # border orientations, intrinsic block), the FP32 triangular factor X and X^T (lower triangles
+    # of the padded dimension), and eight FP64 vectors; served from L2 after the first iteration
+    n = s["dim"]
+    npad = 64 * ((n + 63) // 64)
+    cg_iter_bytes = (8 * (36 * nnzb + 2 * 6 * s["camera_blocks"] * (n - 6 * s["camera_blocks"])
+                          + (n - 6 * s["camera_blocks"]) ** 2)
+                     + 2 * 4 * npad * (npad + 64) // 2 + 8 * 8 * n)
+    cg_ms = kt["pcg_ms"]
+    cg_iters = rep_t["linear_iterations"]
+    cg_gbs = cg_iter_bytes * cg_iters / (cg_ms * 1e-3) / 1e9 if cg_ms > 0 else None
 
-    # end to end through the C ABI with host buffers (upload + solve + download)
+    # first call of a fresh context (host planning, chunk plan and device pattern built, device
+    # memory allocated) beside the warm end-to-end calls below
     desc, keep = native.problem_desc(prob)
     copts = native.solve_options(opts, prob)
     copts.precision = 1
@@ -458,6 +534,15 @@ def run_gb300(args, rank, world, local_rank):
     rb = np.zeros(pp.n_tracks)
     ra = np.zeros(pp.n_tracks)
     rep = native.SolveReportC()
+    cold_ctx = Gb300Context(local_rank)
+    flush.fill_(1.0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    st = cold_ctx.L.pb_gpu_solve_problem(cold_ctx.ctx, C.byref(desc), C.byref(copts), C.byref(rep), cams.ctypes.data,
+                                         pts.ctypes.data, valid.ctypes.data, rb.ctypes.data, ra.ctypes.data)
+    cold_ms = (time.perf_counter() - t0) * 1e3
+    assert st == 0
+    cold_ctx.close()
     e2e = []
     for i in range(args.warmup + args.steps):
         flush.fill_(1.0)
@@ -477,14 +562,33 @@ def run_gb300(args, rank, world, local_rank):
     C64 = out_64["cameras"][:, 9:12]
     scale = np.linalg.norm(C64 - C64.mean(0), axis=1).max()
     cam_err = float(np.abs(out_mixed["cameras"][:, 9:12] - C64).max() / scale)
+    f_r = reps_64r[-1]["final_cost"]
+    cam_err_r = float(np.abs(out_64r["cameras"][:, 9:12] - C64).max() / scale)
+
+    # accuracy of the mixed path against the CPU FP64 oracle's converged solve of the same problem
+    # (committed fixture; compared only when the generator reproduces the fixture's problem)
+    vs_oracle = None
+    if args.workload == "aerial":
+        sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+        import make_c1_fixture as FX
+        fx = FX.load_fixture()
+        if fx is None:
+            vs_oracle = {"unavailable": "fixture absent"}
+        elif not FX.digests_match(fx[0], prob):
+            vs_oracle = {"unavailable": "generator does not reproduce the fixture's problem (digest differs)"}
+        else:
+            vs_oracle = FX.compare(fx[0], fx[1], out_t["cameras"], out_t["intrinsics"], out_t["valid"],
+                                   out_t["rms_after"], out_t["points"], rep_t["final_cost"], rep_t["filter_threshold"])
+            vs_oracle["oracle_cpu_solve_seconds"] = fx[0]["wall_seconds"]
+            vs_oracle["oracle_cpu"] = f"{fx[0]['threads']} threads, {fx[0]['cpu']} ({fx[0]['machine']})"
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        cpu_ms, info = cpu_sample(prob, opts, args.cpu_iterations, reps_64[-1]["iterations"])
+        full_it, source = converged_iterations(args.workload)
+        cpu_ms, info = cpu_sample(prob, opts, args.cpu_iterations, full_it)
         cpu = {"value": cpu_ms, "unit": "ms", "cores": cpu_cores(), "kind": "port",
-               "sample": f"{info['sample_iterations']} LM iterations of the workload "
-                         f"({info['sample_seconds']:.1f} s), scaled to the {reps_64[-1]['iterations']} iterations "
-                         f"of the FP64 solve; CPU FP64 restatement of the reference with OpenMP"}
+               "sample": cpu_sample_text(info, full_it, source),
+               "converged_solve_measured": measured_converged_cpu_solve(args.workload)}
     if rank != 0:
         return
     line = {
@@ -492,24 +596,43 @@ def run_gb300(args, rank, world, local_rank):
         "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64 (mixed)", "data": "synthetic (seeded)",
         "config": dict(cfg, l2="flushed between steps (256 MB write)", parallelism="replicas"),
-        "fp64_path_ms_per_step": ms_64, "speedup_vs_fp64_path": ms_64 / ms_mixed,
+        "fp64_path_ms_per_step": ms_64, "fp64_reuse_path_ms_per_step": ms_64r,
+        "speedup_vs_fp64_path": min(ms_64, ms_64r) / ms_mixed,
+        "speedup_vs_fp64_refactor_path": ms_64 / ms_mixed,
         "mixed_vs_fp64": {"final_cost_rel_diff": abs(f_m - f_d) / f_d, "camera_centre_rel_err": cam_err,
                           "mixed_iterations": reps_mixed[-1]["iterations"], "fp64_iterations": reps_64[-1]["iterations"],
-                          "mixed_status": reps_mixed[-1]["status"], "fp64_status": reps_64[-1]["status"]},
-        "roofline": {"kernel": "k_assemble<float> (linearise + online point Schur)", "bound": "hbm",
-                     "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": (achieved / peak) if achieved else None,
+                          "mixed_status": reps_mixed[-1]["status"], "fp64_status": reps_64[-1]["status"],
+                          "fp64_reuse_vs_fp64": {"final_cost_rel_diff": abs(f_r - f_d) / f_d,
+                                                 "camera_centre_rel_err": cam_err_r,
+                                                 "iterations": reps_64r[-1]["iterations"],
+                                                 "status": reps_64r[-1]["status"]}},
+        "mixed_vs_oracle": vs_oracle,
+        "fp64_on_mixed_path": MIXED_FP64_SPLIT,
+        "roofline": {"kernel": "k_assemble<float> (linearise + online point Schur)", "bound": "issue",
+                     "achieved": issue_achieved, "peak": issue_peak, "unit": "G warp-instructions/s",
+                     "frac": (issue_achieved / issue_peak) if issue_achieved else None,
                      "traffic": ASSEMBLY_DRAM_BYTES_PER_OBS * nop,
-                     "algorithmic_bytes_per_launch": asm_bytes, "avg_launch_ms": asm_ms,
-                     "peak_kind": f"{peak_kind} copy bandwidth",
-                     "note": "issue-bound, not HBM-bound: float-float products on the FP32 pipe; ncu on the "
-                             "250-camera case: 51% of issue slots, FMA pipe 34%, FP64 pipe 21% of peak, "
-                             "DRAM 2.4% (profiles/k_assemble_aerial250.md)"},
+                     "avg_launch_ms": asm_ms,
+                     "peak_kind": f"4 issue slots per SM per cycle x {SMS} SMs at the sampled {sm_mhz:.0f} MHz",
+                     "instructions_per_launch": ASSEMBLY_INST_PER_OBS * nop,
+                     "hbm": {"achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": (achieved / peak) if achieved else None,
+                             "algorithmic_bytes_per_launch": asm_bytes, "peak_kind": f"{peak_kind} copy bandwidth"},
+                     "note": "issue-bound, not HBM-bound: float-float products on the FP32 pipe; warp instructions "
+                             "per observation and traffic per observation from the ncu capture of the 250-camera "
+                             "case (profiles/k_assemble_aerial250.md), scaled by the observations of a launch"},
+        "pcg": {"kernel": "k_dense_cg<float> (FP64 matrix, FP32 dense-factor preconditioner)",
+                "iterations_per_solve": cg_iters, "device_ms_per_solve": cg_ms,
+                "us_per_iteration": 1e3 * cg_ms / cg_iters if cg_iters else None,
+                "bytes_per_iteration": cg_iter_bytes, "achieved": cg_gbs, "peak": peak, "unit": "GB/s",
+                "frac": (cg_gbs / peak) if cg_gbs else None, "served_from": "L2 (129 MB) after the first iteration",
+                "note": "latency-bound: four grid barriers per iteration"},
         "kernel_ms_per_solve": {k: v for k, v in kt.items()},
         "solve_breakdown_ms": {k: rep_t[k] for k in ("assembly_ms", "linear_ms", "back_substitution_ms",
                                                      "objective_ms", "total_ms")},
         "linear_iterations": reps_mixed[-1]["linear_iterations"],
-        "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "cold_first_call_ms": cold_ms},
         "gpu_launches": launches,
         "clocks": clocks,
     }

@@ -133,6 +133,11 @@ typedef struct pb_solve_options {
                                         * path keeps its FP32 factor while it preconditions well, the
                                         * FP64 path refactors every iteration), 1 keep on both paths,
                                         * 2 refactor every iteration on both paths */
+    int32_t general_path;              /* 1: the general path (SolverControlOptions::useReferenceOnlineSchur
+                                        * = false): undamped equations per linearisation, damped Schur
+                                        * solve to 1e-12, finite-difference directional decrease, retry
+                                        * with ten times the damping at the same state; 0: the online
+                                        * reference path */
 } pb_solve_options;
 
 /* PlaMatrixDiagnostics (include/plabundle/result.h:91-128) + QualitySummary fields. */
@@ -329,6 +334,115 @@ pb_status pb_gpu_backward(pb_gpu_ctx* ctx, const double* grad_cameras, const dou
  * indefinite and the call fails with PB_ERR_SINGULAR_BLOCK.  step_max: largest |primary step
  * component|; gradient_norm: |reduced gradient| at the state before the step (may be NULL). */
 pb_status pb_gpu_newton_step(pb_gpu_ctx* ctx, double* step_max, double* gradient_norm);
+
+/* ---- Internal block-Schur interface: the general (non-online) path's linear solve ----------
+ *
+ * pb_bne is plamatrix::internal::BlockNormalEquations<double> (PlaMatrix is absent from the
+ * reference tree; its interface is restated from the reference's use sites): block normal
+ * equations H x = -g with primary blocks of primary_block_size columns (13 in the reference,
+ * src/internal/BundleAdjustPlaMatrixProblem.h:41) and eliminated blocks of 3 (points).  A
+ * residual block r (rows) with Jacobians J_b and weight w adds H_bc += w J_b^T J_c and
+ * g_b += w J_b^T r for every pair of its blocks.  A container is filled by one thread at a time;
+ * per-thread shards are merged, as the reference's OpenMP assembly does
+ * (src/internal/BundleAdjustPlaMatrixAssembly.cpp:843-912).  Jacobians are row-major,
+ * rows x block size.  Host-side only: no call below touches the GPU. */
+#define PB_BNE_MAX_PRIMARY_BLOCK_SIZE 16
+typedef struct pb_bne pb_bne;
+/* BlockNormalEquations<double>(primaryBlocks, eliminatedBlocks, primaryBlockSize, eliminatedBlockSize)
+ * (BundleAdjustPlaMatrixAssembly.cpp:856-857); eliminated_block_size must be 3. */
+pb_status pb_bne_create(int32_t primary_blocks, int32_t eliminated_blocks, int32_t primary_block_size,
+                        int32_t eliminated_block_size, pb_bne** out);
+pb_status pb_bne_destroy(pb_bne* eq);
+/* clearValues (BundleAdjustPlaMatrixAssembly.cpp:861): zeroes every value, keeps the pattern. */
+pb_status pb_bne_clear_values(pb_bne* eq);
+/* [primaryBlockCount, eliminatedBlockCount, primaryBlockSize, eliminatedBlockSize, stored upper
+ * primary pairs, stored primary-eliminated couplings] (BundleAdjustPlaMatrixAssembly.cpp:851-854). */
+pb_status pb_bne_sizes(const pb_bne* eq, int32_t* sizes6);
+/* addResidualBlocks(primary, primaryJacobians, n, eliminated, eliminatedJacobian, residual, rows,
+ * weight) (BundleAdjustPlaMatrixAssembly.cpp:413-421); eliminated < 0: no eliminated block. */
+pb_status pb_bne_add_residual_blocks(pb_bne* eq, const int32_t* primary, const double* const* primary_jacobians,
+                                     int32_t n_primary, int32_t eliminated, const double* eliminated_jacobian,
+                                     const double* residual, int32_t rows, double weight);
+/* addPrimaryResidualBlocks (BundleAdjustPlaMatrixAssembly.cpp:431-437, AssemblySurvey.cpp:35-40). */
+pb_status pb_bne_add_primary_residual_blocks(pb_bne* eq, const int32_t* primary, const double* const* primary_jacobians,
+                                             int32_t n_primary, const double* residual, int32_t rows, double weight);
+/* addPrimaryResidualBlock(block, J, r, rows[, w]) (BundleAdjustPlaMatrixAssembly.cpp:373,
+ * AssemblySurvey.cpp:80-84: the priors, weight 1). */
+pb_status pb_bne_add_primary_residual_block(pb_bne* eq, int32_t block, const double* jacobian, const double* residual,
+                                            int32_t rows, double weight);
+/* addEliminatedResidualBlock (BundleAdjustPlaMatrixAssembly.cpp:376-377, :423-428). */
+pb_status pb_bne_add_eliminated_residual_block(pb_bne* eq, int32_t block, const double* jacobian,
+                                               const double* residual, int32_t rows, double weight);
+/* addResidualBlock: one primary and one eliminated block. */
+pb_status pb_bne_add_residual_block(pb_bne* eq, int32_t primary, const double* primary_jacobian, int32_t eliminated,
+                                    const double* eliminated_jacobian, const double* residual, int32_t rows,
+                                    double weight);
+/* addPrimaryGradientBlock / addPrimaryHessianBlock(row, col, block)
+ * (BundleAdjustPlaMatrixReferenceSchur.cpp:911-926); a block below the diagonal (row > col) is
+ * stored as the transpose of its upper mirror. */
+pb_status pb_bne_add_primary_gradient_block(pb_bne* eq, int32_t block, const double* gradient);
+pb_status pb_bne_add_primary_hessian_block(pb_bne* eq, int32_t row_block, int32_t col_block, const double* block);
+/* finalizePrimaryDiagonal(scale, add) (BundleAdjustPlaMatrixReferenceSchur.cpp:930): non-zero
+ * primary diagonal entries are multiplied by scale, zero ones are set to add. */
+pb_status pb_bne_finalize_primary_diagonal(pb_bne* eq, double scale, double add);
+/* mergeFrom / mergeEliminatedShardFrom(shard, offset) (BundleAdjustPlaMatrixAssembly.cpp:899-912):
+ * adds every value of the other container; a shard's eliminated block k is block offset + k. */
+pb_status pb_bne_merge_from(pb_bne* eq, const pb_bne* other);
+pb_status pb_bne_merge_eliminated_shard_from(pb_bne* eq, const pb_bne* shard, int32_t eliminated_offset);
+/* Dense copy (any pointer may be NULL): primary matrix (P*pb)^2 with both triangles, primary
+ * gradient, eliminated blocks (E*9), eliminated gradient (E*3), couplings: (eliminated, primary)
+ * index pairs and pb x 3 blocks in storage order (sizes[5] of them). */
+pb_status pb_bne_export(const pb_bne* eq, double* primary_matrix, double* primary_gradient, double* eliminated_blocks,
+                        double* eliminated_gradient, int32_t* coupling_index, double* couplings);
+
+/* SchurComplementSolverOptions (BundleAdjustPlaMatrix.cpp:317-340). */
+typedef struct pb_schur_options {
+    int32_t max_iterations;              /* maxIterations; 0: max(200, 30 * primary blocks) */
+    double relative_tolerance;           /* relativeTolerance; 0: 1e-12 (the general path's) */
+    double absolute_tolerance;           /* absoluteTolerance; 0: 1e-12 */
+    int32_t preconditioner_cluster_size; /* accepted (1..16); the dense-factor preconditioner subsumes any grouping */
+    int32_t use_initial_guess;           /* useInitialGuess: primary_step holds the start vector on entry */
+    int32_t use_mixed_precision;         /* useMixedPrecision: FP32 factor preconditioning the FP64 CG */
+} pb_schur_options;
+
+/* SchurComplementSolverReport (BundleAdjustPlaMatrix.cpp:372-399). */
+typedef struct pb_schur_report {
+    int32_t converged;
+    int32_t iterations;
+    int32_t schur_pattern_reused;
+    int32_t schur_assembly_on_device;
+    int32_t mixed_precision_used;
+    int32_t symbolic_analysis_reused;
+    int32_t eliminated_singular;         /* an eliminated block was singular after damping */
+    double relative_residual;            /* |b - S x| / |b| of the damped reduced system (residual check) */
+    double small_block_inverse_ms;
+    double schur_accumulation_ms;
+    double schur_assembly_ms;
+    double cholesky_factorization_ms;
+    double triangular_solve_ms;          /* the preconditioned CG */
+    double linear_solve_ms;
+    double back_substitution_ms;
+    double total_ms;
+    char preconditioner_name[64];
+    char device_name[64];
+} pb_schur_report;
+
+/* solveDampedSchurComplement(equations, damping, options, workspace, &primary, &eliminated)
+ * (call sites src/internal/BundleAdjustPlaMatrix.cpp:349-357, src/linescan_plamatrix.cpp:147-158)
+ * on the context's device and stream: damping scales the diagonals of the primary and eliminated
+ * blocks by (1 + damping) (a zero primary diagonal entry becomes 1); the eliminated blocks are
+ * Schur-eliminated, the reduced system is solved by CG preconditioned with a dense Cholesky factor
+ * (FP64, or FP32 with use_mixed_precision) to the tolerances, and the eliminated steps are
+ * back-substituted.  primary_step: P * primary_block_size, eliminated_step: E * 3 (host).  A
+ * singular eliminated block or a reduced system that is not positive definite returns
+ * PB_ERR_SINGULAR_BLOCK with a "numerically SPD (positive definite)" message, which the reference
+ * driver treats as a retryable breakdown (BundleAdjustPlaMatrix.cpp:34-40); a system that did not
+ * reach the tolerance returns PB_OK with report->converged = 0.  The pattern is reused while the
+ * container's structure is unchanged (report->schur_pattern_reused).  Reduced dimension up to
+ * 16384 (32768 with use_mixed_precision), else PB_ERR_UNSUPPORTED. */
+pb_status pb_gpu_solve_damped_schur(pb_gpu_ctx* ctx, const pb_bne* equations, double damping,
+                                    const pb_schur_options* options, double* primary_step, double* eliminated_step,
+                                    pb_schur_report* report);
 
 /* Allocation-free robust objective of caller-owned device arrays.  No counterpart in the
  * reference: it serves callers that keep their own cameras, points and observations in device

@@ -15,6 +15,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <limits>
+#include <map>
 #include <memory>
 #include <set>
 #include <stdexcept>
@@ -292,6 +293,8 @@ struct BackSub {
     std::vector<std::array<double, kP * kE>> cross;
 };
 
+struct GeneralEquations;
+
 struct Oracle {
     std::vector<Camera> inputCams, refCams;
     std::vector<std::array<double, 3>> initialPoints;
@@ -323,6 +326,9 @@ struct Oracle {
     std::vector<std::vector<ControlPoint>> controlPoints;
     std::vector<std::array<double, 3>> gaugeTargets;  // valid targets of tracks with usable observations
     bool hasControlPoints = false;
+
+    // block normal equations of the general path (orc_general_build)
+    std::shared_ptr<GeneralEquations> general;
 
     size_t nt() const { return offs.size() - 1; }
     // useReferencePointParameterization (BundleAdjustPlaMatrixAssembly.cpp:24-30)
@@ -1239,24 +1245,60 @@ void solveLinear(const Oracle& o, std::vector<double>& x, bool* converged, int* 
     const double bn = std::sqrt(dot(b, b));
     const double tol = std::max(o.opt.linear_relative_tolerance * bn, o.opt.linear_absolute_tolerance);
     int solver = o.opt.linear_solver;
-    if (solver == 0) solver = n <= 2600 ? 1 : 2;
+    if (solver == 0) {
+        // a direct solve while the live unknowns fit a dense factor (the reference's CPU backends
+        // are direct: dense or sparse Cholesky, BundleAdjustPlaMatrixRuntime.cpp:18-55); the
+        // padding columns of the 13-wide blocks carry a unit diagonal (finalizePrimaryDiagonal)
+        size_t live = 0;
+        for (int blk = 0; blk < P; ++blk)
+            for (int p = 0; p < kP; ++p) live += o.diag[static_cast<size_t>(blk) * kP * kP + p * kP + p] != 1.0;
+        solver = live <= 8000 ? 1 : 2;
+    }
     x.assign(n, 0.0);
     *iterations = 0;
     if (solver == 1) {
         std::vector<double> A;
         denseReduced(o, A, n);
-        std::vector<double> Acopy = A;
-        if (!cholesky(A, n)) throw LinearFailure("dense Schur matrix is not numerically SPD (positive definite)");
-        x = b;
-        cholSolve(A, n, x);
-        std::vector<double> r(n, 0.0);
+        // the factor runs over the live rows: a padding row is decoupled (zero off-diagonal, unit
+        // diagonal, zero right-hand side) and its step is zero
+        std::vector<size_t> live;
         for (size_t i = 0; i < n; ++i) {
-            double v = b[i];
-            for (size_t j = 0; j < n; ++j) v -= Acopy[i * n + j] * x[j];
-            r[i] = v;
+            bool pad = A[i * n + i] == 1.0 && b[i] == 0.0;
+            for (size_t j = 0; j < n && pad; ++j) pad = j == i || A[i * n + j] == 0.0;
+            if (!pad) live.push_back(i);
         }
-        *converged = std::sqrt(dot(r, r)) <= tol;
-        *iterations = 1;
+        const size_t m = live.size();
+        std::vector<double> Ac(m * m), bc(m);
+        for (size_t i = 0; i < m; ++i) {
+            bc[i] = b[live[i]];
+            for (size_t j = 0; j < m; ++j) Ac[i * m + j] = A[live[i] * n + live[j]];
+        }
+        std::vector<double> L = Ac;
+        if (!cholesky(L, m)) throw LinearFailure("dense Schur matrix is not numerically SPD (positive definite)");
+        std::vector<double> xc = bc;
+        cholSolve(L, m, xc);
+        // direct solve with iterative refinement against the FP64 residual (the reference's direct
+        // path keeps a post-solve residual check "after refinement", BundleAdjustPlaMatrix.cpp:
+        // 321-330): up to three correction sweeps while |b - S x| exceeds the tolerance
+        std::vector<double> res(m);
+        double rn = 0.0;
+        int sweeps = 0;
+        for (;;) {
+#pragma omp parallel for if (m > 512)
+            for (size_t i = 0; i < m; ++i) {
+                double v = bc[i];
+                for (size_t j = 0; j < m; ++j) v -= Ac[i * m + j] * xc[j];
+                res[i] = v;
+            }
+            rn = std::sqrt(dot(res, res));
+            if (rn <= tol || sweeps == 3) break;
+            cholSolve(L, m, res);
+            for (size_t i = 0; i < m; ++i) xc[i] += res[i];
+            ++sweeps;
+        }
+        for (size_t i = 0; i < m; ++i) x[live[i]] = xc[i];
+        *converged = rn <= tol;
+        *iterations = 1 + sweeps;
         return;
     }
     // block-Jacobi preconditioner: Cholesky of each 13x13 diagonal block
@@ -1291,7 +1333,16 @@ void solveLinear(const Oracle& o, std::vector<double>& x, bool* converged, int* 
         }
         ++it;
         rn = std::sqrt(dot(r, r));
-        if (rn <= tol) { *converged = true; break; }
+        if (rn <= tol) {
+            // post-solve check of the true residual b - S x (the recursive residual can fall below
+            // its FP64 floor near convergence)
+            std::vector<double> sx(n);
+            spmv(o, x, sx);
+            double tr = 0.0;
+            for (size_t i = 0; i < n; ++i) tr += (b[i] - sx[i]) * (b[i] - sx[i]);
+            *converged = std::sqrt(tr) <= tol;
+            break;
+        }
         precond(r, z);
         const double rzn = dot(r, z);
         const double beta = rzn / rz;
@@ -1567,6 +1618,342 @@ std::vector<Camera> publishCameras(const Oracle& o, const State& s) {
     return out;
 }
 
+// ---- General (non-online) path ----------------------------------------------------------------
+// The reference's default path (useReferenceOnlineSchur = false, include/plabundle/options.h:65):
+// buildNormalEquations assembles undamped block normal equations once per linearisation
+// (BundleAdjustPlaMatrixAssembly.cpp:586-939) and solveDampedSchurComplement (PlaMatrix, absent
+// from the tree) eliminates the points and solves (call site BundleAdjustPlaMatrix.cpp:311-357).
+//
+// BlockNormalEquations<double> restated from its use sites: a residual block r with Jacobians J_b
+// (rows x block size) and weight w adds H_bc += w J_b^T J_c and g_b += w J_b^T r over all pairs of
+// its blocks.  Primary blocks are 13 wide, eliminated blocks 3.
+struct GeneralEquations {
+    int P = 0, E = 0;
+    std::vector<double> diag, gp, hee, ge;                    // P*13*13, P*13, E*9, E*3
+    std::map<std::pair<int, int>, std::vector<double>> off;  // (row < col) -> 13 x 13
+    std::map<std::pair<int, int>, std::vector<double>> cpl;  // (eliminated, primary) -> 13 x 3
+    void reset(int p, int e) {
+        P = p;
+        E = e;
+        diag.assign(static_cast<size_t>(P) * kP * kP, 0.0);
+        gp.assign(static_cast<size_t>(P) * kP, 0.0);
+        hee.assign(static_cast<size_t>(E) * 9, 0.0);
+        ge.assign(static_cast<size_t>(E) * 3, 0.0);
+        off.clear();
+        cpl.clear();
+    }
+    // addResidualBlocks(primary, Jp, n, eliminated, Je, r, rows, w) (...Assembly.cpp:413-421);
+    // eliminated < 0: addPrimaryResidualBlocks; n == 0: addEliminatedResidualBlock.  Every ordered
+    // pair of terms (a, b) adds J_a^T J_b to block (prim a, prim b); the stored upper block takes
+    // the pairs with prim a < prim b, the diagonal block those with prim a == prim b.
+    void addResidualBlocks(const int* prim, const double* const* Jp, int n, int elim, const double* Je,
+                           const double* r, int rows, double w) {
+        for (int a = 0; a < n; ++a) {
+            for (int i = 0; i < kP; ++i) {
+                double s = 0.0;
+                for (int k = 0; k < rows; ++k) s += Jp[a][k * kP + i] * r[k];
+                gp[static_cast<size_t>(prim[a]) * kP + i] += w * s;
+            }
+            for (int b = 0; b < n; ++b) {
+                if (prim[a] > prim[b]) continue;
+                double* dst;
+                if (prim[a] == prim[b]) {
+                    dst = diag.data() + static_cast<size_t>(prim[a]) * kP * kP;
+                } else {
+                    auto& blk = off[{prim[a], prim[b]}];
+                    if (blk.empty()) blk.assign(kP * kP, 0.0);
+                    dst = blk.data();
+                }
+                for (int i = 0; i < kP; ++i)
+                    for (int j = 0; j < kP; ++j) {
+                        double s = 0.0;
+                        for (int k = 0; k < rows; ++k) s += Jp[a][k * kP + i] * Jp[b][k * kP + j];
+                        dst[i * kP + j] += w * s;
+                    }
+            }
+            if (elim >= 0) {
+                auto& blk = cpl[{elim, prim[a]}];
+                if (blk.empty()) blk.assign(kP * kE, 0.0);
+                for (int i = 0; i < kP; ++i)
+                    for (int j = 0; j < kE; ++j) {
+                        double s = 0.0;
+                        for (int k = 0; k < rows; ++k) s += Jp[a][k * kP + i] * Je[k * kE + j];
+                        blk[i * kE + j] += w * s;
+                    }
+            }
+        }
+        if (elim >= 0) {
+            for (int i = 0; i < kE; ++i) {
+                double s = 0.0;
+                for (int k = 0; k < rows; ++k) s += Je[k * kE + i] * r[k];
+                ge[static_cast<size_t>(elim) * 3 + i] += w * s;
+                for (int j = 0; j < kE; ++j) {
+                    double h = 0.0;
+                    for (int k = 0; k < rows; ++k) h += Je[k * kE + i] * Je[k * kE + j];
+                    hee[static_cast<size_t>(elim) * 9 + i * 3 + j] += w * h;
+                }
+            }
+        }
+    }
+};
+
+// buildNormalEquations (BundleAdjustPlaMatrixAssembly.cpp:586-939) at the current state for frame
+// cameras: every usable observation of an active track through addObservation (:381-440): its
+// primary terms (camera pose block, intrinsic group block) and the track's eliminated point;
+// control points through addPointResidual (:356-380, :663-672); the intrinsic priors through
+// assemblePrimaryPriors (AssemblySurvey.cpp:43-91, weight 1).  Returns the linearised cost.
+double buildGeneral(Oracle& o, GeneralEquations& q) {
+    q.reset(o.active.primaryBlockCount, o.active.trackBlockCount);
+    const bool ref = o.refParam();
+    double cost = 0.0;
+    for (size_t t = 0; t < o.nt(); ++t) {
+        if (!o.active.activeTrack[t]) continue;
+        const int elim = o.active.trackBlock[t];
+        for (int64_t k = o.offs[t]; k < o.offs[t + 1]; ++k) {
+            const Obs& ob = o.obs[k];
+            if (!obsUsable(ob, o.state.cams.size())) continue;
+            const Camera cam = effectiveCamera(o, o.state, ob.cam);
+            Lin L;
+            if (!linearize(cam, activeIntrinsics(o, ob.cam), o.state.points[t].data(), ob, o.opt.robust_loss,
+                           o.opt.robust_loss_scale, ref, &L))
+                throw InvalidProjection("linearisation produced an invalid projection");
+            cost += L.cost;
+            const Terms tm = primaryTerms(o, o.state, ob.cam, L);
+            const double* jp[2] = {tm.J[0], tm.J[1]};
+            q.addResidualBlocks(tm.blocks, jp, tm.count, elim, L.Jp, L.r, 2, L.nw);
+        }
+        for (const auto& cp : o.controlPoints[t]) {
+            double r[3];
+            RobustEval rb;
+            if (!controlPointResidual(o, cp, o.state.points[t].data(), r, &rb)) continue;
+            cost += rb.cost;
+            if (elim >= 0) q.addResidualBlocks(nullptr, nullptr, 0, elim, cp.J, r, 3, rb.weight);
+        }
+    }
+    for (size_t g = 0; g < o.state.groups.size(); ++g) {
+        const Group& gr = o.state.groups[g];
+        const int block = o.active.cameraBlockCount + static_cast<int>(g);
+        std::vector<double> J(kP * kP, 0.0), r(kP, 0.0);
+        for (int p = 0; p < kP; ++p) {
+            if (!gr.enabled[p]) continue;
+            r[p] = gr.invSigma[p] * (gr.params[p] - gr.prior[p]);
+            J[p * kP + p] = gr.invSigma[p];
+            cost += 0.5 * r[p] * r[p];
+        }
+        const double* jp[1] = {J.data()};
+        q.addResidualBlocks(&block, jp, 1, -1, nullptr, r.data(), kP, 1.0);
+    }
+    return cost;
+}
+
+// solveDampedSchurComplement restated (PlaMatrix is absent; the damping form is the online path's,
+// BundleAdjustPlaMatrixReferenceSchur.cpp:362-365, :930): primary and eliminated diagonals times
+// (1 + damping), a zero primary diagonal entry set to 1; S = H_pp - sum W V^-1 W^T,
+// b = -g_p + sum W V^-1 g_e; dense FP64 Cholesky; y_e = V^-1 (-g_e - W^T x).  `converged`: the
+// residual |b - S x| is within max(tol |b|, 1e-12).
+void solveGeneralDamped(const GeneralEquations& q, double damping, double tol, std::vector<double>& x,
+                        std::vector<double>& y, bool* converged) {
+    const size_t n = static_cast<size_t>(q.P) * kP;
+    std::vector<double> S(n * n, 0.0), b(n);
+    for (int blk = 0; blk < q.P; ++blk)
+        for (int i = 0; i < kP; ++i)
+            for (int j = 0; j < kP; ++j) {
+                double v = q.diag[static_cast<size_t>(blk) * kP * kP + i * kP + j];
+                if (i == j) v = v != 0.0 ? v * (1.0 + damping) : 1.0;
+                S[(static_cast<size_t>(blk) * kP + i) * n + static_cast<size_t>(blk) * kP + j] = v;
+            }
+    for (const auto& kv : q.off) {
+        const size_t r0 = static_cast<size_t>(kv.first.first) * kP, c0 = static_cast<size_t>(kv.first.second) * kP;
+        for (int i = 0; i < kP; ++i)
+            for (int j = 0; j < kP; ++j) {
+                S[(r0 + i) * n + c0 + j] = kv.second[i * kP + j];
+                S[(c0 + j) * n + r0 + i] = kv.second[i * kP + j];
+            }
+    }
+    for (size_t i = 0; i < n; ++i) b[i] = -q.gp[i];
+    std::vector<std::array<double, 9>> inv(q.E);
+    for (int e = 0; e < q.E; ++e) {
+        double V[9];
+        for (int i = 0; i < 9; ++i) V[i] = q.hee[static_cast<size_t>(e) * 9 + i];
+        for (int d = 0; d < 3; ++d) V[d * 4] *= 1.0 + damping;
+        if (!inverse3x3(V, inv[e].data(), 1.0e-15)) throw LinearFailure("eliminated block is not numerically SPD");
+    }
+    // couplings of each eliminated block (the map is ordered by eliminated block)
+    auto it = q.cpl.begin();
+    while (it != q.cpl.end()) {
+        const int e = it->first.first;
+        std::vector<std::pair<int, const std::vector<double>*>> ws;
+        while (it != q.cpl.end() && it->first.first == e) {
+            ws.push_back({it->first.second, &it->second});
+            ++it;
+        }
+        const auto& iv = inv[e];
+        std::vector<std::vector<double>> Y(ws.size(), std::vector<double>(kP * kE, 0.0));
+        for (size_t a = 0; a < ws.size(); ++a)
+            for (int i = 0; i < kP; ++i)
+                for (int k = 0; k < kE; ++k)
+                    for (int m = 0; m < kE; ++m) Y[a][i * kE + k] += (*ws[a].second)[i * kE + m] * iv[m * 3 + k];
+        for (size_t a = 0; a < ws.size(); ++a) {
+            const size_t ra = static_cast<size_t>(ws[a].first) * kP;
+            for (int i = 0; i < kP; ++i)
+                for (int k = 0; k < kE; ++k) b[ra + i] += Y[a][i * kE + k] * q.ge[static_cast<size_t>(e) * 3 + k];
+            for (size_t c = 0; c < ws.size(); ++c) {
+                const size_t rc = static_cast<size_t>(ws[c].first) * kP;
+                for (int i = 0; i < kP; ++i)
+                    for (int j = 0; j < kP; ++j) {
+                        double h = 0.0;
+                        for (int k = 0; k < kE; ++k) h += Y[a][i * kE + k] * (*ws[c].second)[j * kE + k];
+                        S[(ra + i) * n + rc + j] -= h;
+                    }
+            }
+        }
+    }
+    std::vector<double> L = S;
+    if (!cholesky(L, n)) throw LinearFailure("dense Schur matrix is not numerically SPD (positive definite)");
+    x = b;
+    cholSolve(L, n, x);
+    // iterative refinement against the FP64 residual, up to three sweeps (as the online path's
+    // direct solve)
+    double bn = 0.0;
+    for (size_t i = 0; i < n; ++i) bn += b[i] * b[i];
+    const double limit = std::max(tol * std::sqrt(bn), 1.0e-12);
+    std::vector<double> res(n);
+    double rn = 0.0;
+    for (int sweep = 0;; ++sweep) {
+        rn = 0.0;
+        for (size_t i = 0; i < n; ++i) {
+            double v = b[i];
+            for (size_t j = 0; j < n; ++j) v -= S[i * n + j] * x[j];
+            res[i] = v;
+            rn += v * v;
+        }
+        if (std::sqrt(rn) <= limit || sweep == 3) break;
+        cholSolve(L, n, res);
+        for (size_t i = 0; i < n; ++i) x[i] += res[i];
+    }
+    *converged = std::sqrt(rn) <= limit;
+    std::vector<double> r(static_cast<size_t>(q.E) * 3);
+    for (int e = 0; e < q.E; ++e)
+        for (int k = 0; k < 3; ++k) r[static_cast<size_t>(e) * 3 + k] = -q.ge[static_cast<size_t>(e) * 3 + k];
+    for (const auto& kv : q.cpl) {
+        const int e = kv.first.first;
+        const size_t ra = static_cast<size_t>(kv.first.second) * kP;
+        for (int k = 0; k < kE; ++k)
+            for (int i = 0; i < kP; ++i) r[static_cast<size_t>(e) * 3 + k] -= kv.second[i * kE + k] * x[ra + i];
+    }
+    y.assign(static_cast<size_t>(q.E) * 3, 0.0);
+    for (int e = 0; e < q.E; ++e)
+        for (int k = 0; k < 3; ++k) {
+            double v = 0.0;
+            for (int m = 0; m < 3; ++m) v += inv[e][k * 3 + m] * r[static_cast<size_t>(e) * 3 + m];
+            y[static_cast<size_t>(e) * 3 + k] = v;
+        }
+}
+
+// The general branch of optimizePointsWithPlaMatrix (BundleAdjustPlaMatrix.cpp:236-542 with
+// use_reference_online_schur false): one buildNormalEquations per accepted state, damped solves
+// to 1e-12 (retried with ten times the damping at the same state when short of the tolerance or
+// rejected), convergence when the step RMS is at most 1e-6 before a line search, a forward-
+// difference directional decrease (step 1e-4), Armijo with the general path's limit, and the
+// last (smallest) trial accepted when it lowers the cost.  A solver breakdown is a numerical
+// failure.
+void solveGeneralPath(Oracle* o, orc_report* rep, double* current_out, int* iterations_out, bool* converged_out,
+                      bool* failed_out) {
+    const Active& a = o->active;
+    const int T = std::max(1, std::min<int>(o->threads, static_cast<int>(o->nt())));
+    trackBoundaries(*o, T);
+    double current = std::numeric_limits<double>::quiet_NaN(), damping = 0.0;
+    int iterations = 0;
+    bool converged = a.primaryBlockCount == 0 && a.trackBlockCount == 0;
+    bool failed = false;
+    GeneralEquations q;
+    std::vector<double> ps, es;
+    const double tol = o->opt.linear_relative_tolerance > 0 ? o->opt.linear_relative_tolerance : 1.0e-12;
+    try {
+        if (converged) {
+            current = objective(*o, o->state);
+            rep->initial_cost = current;
+            ++rep->objective_evaluations;
+        }
+        const int budget = std::max(1, o->opt.max_iterations);
+        while (iterations < budget && !converged) {
+            const auto ta = std::chrono::steady_clock::now();
+            current = buildGeneral(*o, q);
+            rep->assembly_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - ta).count();
+            ++rep->linearizations;
+            ++rep->objective_evaluations;
+            if (rep->linearizations == 1) rep->initial_cost = current;
+            bool relinearize = false;
+            while (iterations < budget && !converged && !relinearize) {
+                bool lconv = false;
+                const auto tl = std::chrono::steady_clock::now();
+                solveGeneralDamped(q, damping, tol, ps, es, &lconv);
+                rep->linear_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - tl).count();
+                rep->linear_iterations += 1;
+                ++iterations;
+                if (!lconv) {
+                    ++rep->rejected_steps;
+                    damping = damping == 0.0 ? 1e-3 : damping * 10.0;
+                    continue;
+                }
+                double rg = 0.0, rp = 0.0;
+                stepRms(*o, ps, es, &rg, &rp);
+                if (rg <= 1e-6 && rp <= 1e-6) {
+                    converged = true;
+                    continue;
+                }
+                double dd = 0.0;
+                {
+                    const double h = 1.0e-4;
+                    const State fs = applyStep(*o, o->state, ps, es, h);
+                    const double fd = objective(*o, fs);
+                    ++rep->objective_evaluations;
+                    if (std::isfinite(fd) && fd < current) dd = (current - fd) / h;
+                }
+                double cand = kInf, alpha = 1.0, tried = 1.0;
+                bool armijo = false;
+                State cs;
+                for (int ls = 0; ls < o->opt.line_search_steps; ++ls) {
+                    cs = applyStep(*o, o->state, ps, es, alpha);
+                    cand = objective(*o, cs);
+                    tried = alpha;
+                    ++rep->objective_evaluations;
+                    const double limit = dd > 0.0 ? current - o->opt.armijo_coefficient * alpha * dd : current;
+                    if (std::isfinite(cand) && cand <= limit && cand < current) {
+                        armijo = true;
+                        break;
+                    }
+                    alpha *= 0.5;
+                }
+                (void)armijo;
+                const bool accept = std::isfinite(cand) && cand < current;
+                if (std::getenv("PB_GPU_TRACE"))
+                    std::fprintf(stderr,
+                                 "ORACLE_TRACE general it=%d cost=%.15e lambda=%.3e dd=%.6e rms_global=%.3e "
+                                 "rms_point=%.3e alpha=%.6g cand=%.15e accepted=%d\n",
+                                 iterations, current, damping, dd, rg, rp, tried, cand, accept ? 1 : 0);
+                if (accept) {
+                    o->state = std::move(cs);
+                    current = cand;
+                    ++rep->accepted_steps;
+                    damping /= 10.0;
+                    converged = tried * rg <= 1e-6 && tried * rp <= 1e-6;
+                    relinearize = !converged;
+                } else {
+                    ++rep->rejected_steps;
+                    damping = damping == 0.0 ? 1e-3 : damping * 10.0;
+                }
+            }
+        }
+    } catch (const std::exception&) {
+        failed = true;
+    }
+    *current_out = current;
+    *iterations_out = iterations;
+    *converged_out = converged;
+    *failed_out = failed;
+}
+
 }  // namespace orc
 
 using namespace orc;
@@ -1736,6 +2123,72 @@ double orc_cost(void* h) {
     return objective(*o, o->state);
 }
 
+int32_t orc_general_build(void* h, double* cost, int32_t* counts) {
+    auto* o = static_cast<Oracle*>(h);
+    try {
+        const int T = std::max(1, std::min<int>(o->threads, static_cast<int>(o->nt())));
+        trackBoundaries(*o, T);
+        if (!o->general) o->general = std::make_shared<GeneralEquations>();
+        *cost = buildGeneral(*o, *o->general);
+        counts[0] = o->general->P;
+        counts[1] = o->general->E;
+        counts[2] = static_cast<int32_t>(o->general->cpl.size());
+        return 0;
+    } catch (const std::exception&) {
+        return NumericalFailure;
+    }
+}
+
+int32_t orc_general_export(void* h, double* primary_matrix, double* gp, double* hee, double* ge, int32_t* cpl_index,
+                           double* cpl) {
+    auto* o = static_cast<Oracle*>(h);
+    if (!o->general) return InvalidInput;
+    const GeneralEquations& q = *o->general;
+    const size_t n = static_cast<size_t>(q.P) * kP;
+    std::fill(primary_matrix, primary_matrix + n * n, 0.0);
+    for (int b = 0; b < q.P; ++b)
+        for (int i = 0; i < kP; ++i)
+            for (int j = 0; j < kP; ++j)
+                primary_matrix[(static_cast<size_t>(b) * kP + i) * n + static_cast<size_t>(b) * kP + j] =
+                    q.diag[static_cast<size_t>(b) * kP * kP + i * kP + j];
+    for (const auto& kv : q.off) {
+        const size_t r0 = static_cast<size_t>(kv.first.first) * kP, c0 = static_cast<size_t>(kv.first.second) * kP;
+        for (int i = 0; i < kP; ++i)
+            for (int j = 0; j < kP; ++j) {
+                primary_matrix[(r0 + i) * n + c0 + j] = kv.second[i * kP + j];
+                primary_matrix[(c0 + j) * n + r0 + i] = kv.second[i * kP + j];
+            }
+    }
+    std::copy(q.gp.begin(), q.gp.end(), gp);
+    std::copy(q.hee.begin(), q.hee.end(), hee);
+    std::copy(q.ge.begin(), q.ge.end(), ge);
+    size_t k = 0;
+    for (const auto& kv : q.cpl) {
+        cpl_index[2 * k] = kv.first.first;
+        cpl_index[2 * k + 1] = kv.first.second;
+        std::copy(kv.second.begin(), kv.second.end(), cpl + k * kP * kE);
+        ++k;
+    }
+    return 0;
+}
+
+int32_t orc_general_solve(void* h, double damping, double tolerance, double* primary, double* eliminated,
+                          int32_t* converged) {
+    auto* o = static_cast<Oracle*>(h);
+    if (!o->general) return InvalidInput;
+    try {
+        std::vector<double> x, y;
+        bool cv = false;
+        solveGeneralDamped(*o->general, damping, tolerance, x, y, &cv);
+        std::copy(x.begin(), x.end(), primary);
+        std::copy(y.begin(), y.end(), eliminated);
+        *converged = cv;
+        return 0;
+    } catch (const std::exception&) {
+        return NumericalFailure;
+    }
+}
+
 // optimizePointsWithPlaMatrix, online reduced-Schur branch (BundleAdjustPlaMatrix.cpp:162-631),
 // followed by finalizeBundleAdjustResult (BundleAdjustQuality.cpp:403-502).
 int32_t orc_solve(void* h, orc_report* rep, double* camsOut, double* ptsOut, int8_t* validOut, double* rmsBefore,
@@ -1759,6 +2212,9 @@ int32_t orc_solve(void* h, orc_report* rep, double* camsOut, double* ptsOut, int
     bool converged = a.primaryBlockCount == 0 && a.trackBlockCount == 0;
     bool failed = false;
     std::vector<double> ps, es;
+    if (o->opt.general_path) {
+        solveGeneralPath(o, rep, &current, &iterations, &converged, &failed);
+    } else
     try {
         if (converged) {
             current = objective(*o, o->state);

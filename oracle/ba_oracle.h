@@ -1,5 +1,6 @@
 /*
- * ba_oracle.h -- CPU FP64 restatement of plabundle's reduced-Schur bundle adjustment.
+ * ba_oracle.h -- CPU FP64 restatement of plabundle's reduced-Schur bundle adjustment: the online
+ * reduced-Schur path and the general path (block normal equations + damped Schur solve).
  *
  * TEST INFRASTRUCTURE ONLY.  Only tests/, __graft_entry__.smoke() and bench.py's
  * cpu_baseline leg (and `bench.py --impl reference`) may load this library; the
@@ -81,6 +82,7 @@ typedef struct orc_options {
     double calibration[32];         /* CalibrationOptions numeric fields, see ORC_CAL_* */
     double control_point_weight;    /* ConstraintOptions::controlPointWeight */
     double control_point_huber_delta; /* ConstraintOptions::controlPointHuberDeltaMeters */
+    int32_t general_path;           /* 1: the general path (useReferenceOnlineSchur = false) */
 } orc_options;
 
 typedef struct orc_report {
@@ -133,6 +135,17 @@ int32_t orc_solve_linear(void* handle, double* primary_step, int32_t* converged,
 int32_t orc_back_substitute(void* handle, const double* primary_step, double* eliminated_step,
                             double* directional_decrease, int32_t* success);
 double orc_cost(void* handle);
+/* General path: buildNormalEquations at the current state into the handle's block normal
+ * equations; counts: [primary blocks, eliminated blocks, couplings]. */
+int32_t orc_general_build(void* handle, double* cost, int32_t* counts);
+/* Dense primary matrix ((13 P)^2, both triangles), primary gradient (13 P), eliminated blocks (9 E),
+ * eliminated gradient (3 E), couplings (eliminated, primary) and 13x3 blocks in (eliminated,
+ * primary) order. */
+int32_t orc_general_export(void* handle, double* primary_matrix, double* primary_gradient, double* eliminated_blocks,
+                           double* eliminated_gradient, int32_t* coupling_index, double* couplings);
+/* solveDampedSchurComplement restated on the built equations (dense FP64). */
+int32_t orc_general_solve(void* handle, double damping, double tolerance, double* primary_step,
+                          double* eliminated_step, int32_t* converged);
 /* Full solve from the initial state. */
 int32_t orc_solve(void* handle, orc_report* report, double* cameras_out, double* points_out, int8_t* valid_out,
                   double* rms_before, double* rms_after, double* intrinsics_out);

@@ -41,7 +41,7 @@ class OrcOptions(C.Structure):
                 ("linear_solver", C.c_int32), ("max_linear_iterations", C.c_int32),
                 ("linear_relative_tolerance", C.c_double), ("linear_absolute_tolerance", C.c_double),
                 ("calibration", C.c_double * 32), ("control_point_weight", C.c_double),
-                ("control_point_huber_delta", C.c_double)]
+                ("control_point_huber_delta", C.c_double), ("general_path", C.c_int32)]
 
 
 class OrcReport(C.Structure):
@@ -82,6 +82,10 @@ def lib():
         L.orc_cost.restype = C.c_double
         L.orc_cost.argtypes = [C.c_void_p]
         L.orc_solve.argtypes = [C.c_void_p, C.POINTER(OrcReport)] + [C.c_void_p] * 6
+        L.orc_general_build.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.c_void_p]
+        L.orc_general_export.argtypes = [C.c_void_p] + [C.c_void_p] * 6
+        L.orc_general_solve.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_void_p, C.c_void_p,
+                                        C.POINTER(C.c_int32)]
         L.orc_control_point_whitening.argtypes = [C.c_void_p, C.c_void_p]
         L.orc_control_point_whitening.restype = C.c_int32
         _lib = L
@@ -110,7 +114,9 @@ def make_options(options, num_threads: int = 0, linear_solver: int = 0) -> OrcOp
     o.num_threads = num_threads or s.numThreads
     o.linear_solver = linear_solver
     o.max_linear_iterations = options.backend.maxLinearIterations
-    o.linear_relative_tolerance = 2.0e-10
+    # the reference's tolerances: 2e-10 online, 1e-12 on the general path (BundleAdjustPlaMatrix.cpp:321-330)
+    o.general_path = 0 if s.useReferenceOnlineSchur else 1
+    o.linear_relative_tolerance = 2.0e-10 if s.useReferenceOnlineSchur else 1.0e-12
     o.linear_absolute_tolerance = 1.0e-12
     for i, v in enumerate(cal.numeric_block()):
         o.calibration[i] = v
@@ -254,6 +260,30 @@ class Oracle:
 
     def cost(self):
         return lib().orc_cost(self.h)
+
+    def general_equations(self):
+        """Block normal equations of the general path at the current state (buildNormalEquations):
+        dense primary matrix, primary gradient, eliminated blocks and gradient, couplings."""
+        cost = C.c_double(0)
+        counts = np.zeros(3, np.int32)
+        if lib().orc_general_build(self.h, C.byref(cost), _ptr(counts)) != 0:
+            raise RuntimeError("oracle general build failed")
+        P, E, nc = (int(v) for v in counts)
+        n = P * _P
+        out = {"cost": cost.value, "H": np.zeros((n, n)), "g": np.zeros(n), "Hee": np.zeros((E, 3, 3)),
+               "ge": np.zeros((E, 3)), "coupling_index": np.zeros((nc, 2), np.int32), "W": np.zeros((nc, _P, 3))}
+        lib().orc_general_export(self.h, *(_ptr(out[k]) for k in ("H", "g", "Hee", "ge", "coupling_index", "W")))
+        return out
+
+    def general_solve(self, damping, tolerance=1e-12):
+        """solveDampedSchurComplement restated on the equations of the last general_equations()."""
+        info = self.info()
+        x = np.zeros(info["primary"] * _P)
+        y = np.zeros(info["track_blocks"] * 3)
+        cv = C.c_int32(0)
+        if lib().orc_general_solve(self.h, damping, tolerance, _ptr(x), _ptr(y), C.byref(cv)) != 0:
+            raise RuntimeError("oracle general solve failed (not numerically SPD)")
+        return x, y, bool(cv.value)
 
     def solve(self):
         p = self.problem

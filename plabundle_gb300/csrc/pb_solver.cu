@@ -116,7 +116,8 @@ struct pb_gpu_ctx {
     DenseWork<float> dw32;
     DenseWork<double> dw64;
     double shift32 = 1e-7;  // last FP32 factor shift that factorised
-    int f32_age = -1;       // LM solves served by the current FP32 factor (-1: none)
+    int f32_age = -1;       // LM solves served by the current kept dense factor (-1: none)
+    int factor_reuse = 0;   // pb_solve_options.factor_reuse of the running solve
     bool f32_stale = false; // the last accepted step changed the cost by more than 1 %
     int f32_base_iters = 0; // CG iterations of the first solve with that factor
     bool dense_ready[2] = {false, false};
@@ -172,6 +173,8 @@ struct pb_gpu_ctx {
     double* snap_groups = nullptr;
     bool snap_valid = false;
     std::vector<long long> proc_of_obs;  // original observation -> processing index (-1: not processed)
+    // damped Schur solves of host block normal equations (pb_gpu_solve_damped_schur)
+    SchurWork* schur = nullptr;
 };
 
 namespace {
@@ -424,6 +427,8 @@ void prepare_precision(pb_gpu_ctx* c, int precision) {
     D.slot_items = upload_new(A, cs.slot_items, st);
     D.lcam_obs_begin = upload_new(A, cs.lcam_obs_begin, st);
     D.lcam_obs = upload_new(A, cs.lcam_obs, st);
+    D.warp_task_begin = upload_new(A, cs.warp_task_begin, st);
+    D.task_list = upload_new(A, cs.task_list, st);
     const int camrec = 12 + S.ng * 6 * S.ni, chrec = S.nb * S.nb + 2 * S.nb;
     // chunk partials: accumulator pairs of the assembly (float2 on the FP32 path, double on FP64)
     using PT = typename Acc<T>::part_type;
@@ -550,8 +555,11 @@ int solve_dense(pb_gpu_ctx* c, double rel, double abs_tol, int max_it, bool* con
     ensure_dense<T>(c);
     DenseWork<T>& W = dwork<T>(c);
     const bool f32 = std::is_same<T, float>::value;
+    // factor reuse across LM iterations: the mixed path's default; the FP64 path on request
+    // (pb_solve_options.factor_reuse), which gives an FP64 arm with the mixed path's policy
+    const bool reuse = f32 ? c->factor_reuse != 2 : c->factor_reuse == 1;
     int spent = 0;
-    if (f32 && c->f32_age >= 0 && c->f32_age < max_factor_age(c->S[0].n) && !c->f32_stale) {
+    if (reuse && c->f32_age >= 0 && c->f32_age < max_factor_age(c->S[0].n) && !c->f32_stale) {
         // The reduced matrix changes little between LM iterations: the FP32 factor of an earlier
         // one still preconditions the CG on the current FP64 matrix.  A factorisation costs
         // about as much as a hundred CG iterations, so the kept factor is used until the CG
@@ -585,7 +593,7 @@ int solve_dense(pb_gpu_ctx* c, double rel, double abs_tol, int max_it, bool* con
     const int rc = dense_pcg<T>(c->sys, W, c->red.rhs, rel, abs_tol, max_it, iterations, relres, converged,
                                 c->h_scratch + 40, c->stream, &c->launches);
     if (rc < 0) throw CudaError(std::string("dense CG failed: ") + cudaGetErrorString(cudaGetLastError()));
-    if (f32) {
+    if (reuse) {
         c->f32_age = rc == 0 ? 1 : -1;
         c->f32_base_iters = *iterations;
     }
@@ -629,7 +637,10 @@ bool dense_solver_fits(int n, int precision) { return n <= (precision == PB_PREC
 
 int solve_reduced(pb_gpu_ctx* c, const pb_solve_options& op, bool* converged, int* iterations, double* relres,
                   int* sweeps) {
-    const double rel = op.linear_relative_tolerance > 0 ? op.linear_relative_tolerance : 2.0e-10;
+    // the reference's tolerances: 2e-10 on the online path, 1e-12 on the general path
+    // (BundleAdjustPlaMatrix.cpp:321-330)
+    const double rel = op.linear_relative_tolerance > 0 ? op.linear_relative_tolerance
+                                                         : (op.general_path ? 1.0e-12 : 2.0e-10);
     const double abs_tol = op.linear_absolute_tolerance > 0 ? op.linear_absolute_tolerance : 1.0e-12;
     const int max_it = op.max_linear_iterations > 0 ? op.max_linear_iterations : std::max(200, 30 * c->model.P);
     const int solver = (op.linear_solver == 1 || op.linear_solver == 2)
@@ -649,6 +660,19 @@ int solve_reduced(pb_gpu_ctx* c, const pb_solve_options& op, bool* converged, in
         *sweeps = *iterations;  // FP64-residual corrections of the FP32 factor
     } else {
         rc = solve_dense<double>(c, rel, abs_tol, max_it, converged, iterations, relres);
+    }
+    if (rc == 0 && *converged) {
+        // Post-solve residual check on the FP64 reduced system: the CG stops on its recursive
+        // residual, which near convergence can fall below the FP64 floor of the true residual
+        // |b - S x|.  The reference guards its direct factorisation the same way and, on a miss,
+        // retries the step with more damping (BundleAdjustPlaMatrix.cpp:321-330, :402-408).
+        residual64<double>(c->sys, c->red.rhs, c->step_c, c->r64, c->res_out, c->stream);
+        c->launches += 2;
+        check(cudaMemcpyAsync(c->h_scratch, c->res_out, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "D2H");
+        check(cudaStreamSynchronize(c->stream), "residual check");
+        const double rn = c->h_scratch[0], bn = c->h_scratch[1];
+        *relres = bn > 0.0 ? rn / bn : rn;
+        if (!(rn <= std::max(rel * bn, abs_tol))) *converged = false;
     }
     return rc;
 }
@@ -753,6 +777,7 @@ int do_assemble(pb_gpu_ctx* c, double damping, int precision, double* cost, int*
 void lm_solve(pb_gpu_ctx* c, const pb_solve_options& op, pb_solve_report* rep) {
     c->f32_age = -1;  // every solve starts from a fresh factor: repeated solves run identically
     c->f32_stale = false;
+    c->factor_reuse = (op.factor_reuse >= 0 && op.factor_reuse <= 2) ? op.factor_reuse : 0;
     const auto t0 = std::chrono::steady_clock::now();
     const HostModel& m = c->model;
     std::memset(rep, 0, sizeof(*rep));
@@ -946,6 +971,220 @@ void lm_solve(pb_gpu_ctx* c, const pb_solve_options& op, pb_solve_report* rep) {
     c->solved = 1;
 }
 
+// The general (non-online) branch of optimizePointsWithPlaMatrix (BundleAdjustPlaMatrix.cpp:
+// 236-542 with use_reference_online_schur false).  The reference builds the undamped block normal
+// equations once per linearisation and hands them, with the current damping, to
+// solveDampedSchurComplement; a rejected step retries the same equations with ten times the
+// damping.  Here the damped Schur complement of the equations at the current state is formed by
+// the fused assembly kernel, which linearises and eliminates in one pass: for image and
+// control-point terms the damped Schur complement of H (primary and point diagonals scaled by
+// 1 + damping) is exactly what the online assembly computes with that damping, so a retry re-runs
+// the kernel at the unchanged state.  The driver differs from the online branch in:
+//   - relative linear tolerance 1e-12;
+//   - a step whose RMS (global and point) is at most 1e-6 ends the solve before any line search;
+//   - the directional decrease is the finite difference (f(x) - f(x + 1e-4 d)) / 1e-4 of the
+//     objective along the step (0 when that trial is not lower);
+//   - Armijo accepts at cost <= f - c alpha dd (cost < f alone when dd is 0); when no step length
+//     passes, the last (smallest) trial is still accepted if it lowers the cost;
+//   - a rejected step (or a linear solve short of its tolerance) multiplies the damping by ten and
+//     solves again at the same state; a solver breakdown is a numerical failure of the solve.
+void lm_solve_general(pb_gpu_ctx* c, const pb_solve_options& op, pb_solve_report* rep) {
+    c->f32_age = -1;
+    c->f32_stale = false;
+    c->factor_reuse = (op.factor_reuse >= 0 && op.factor_reuse <= 2) ? op.factor_reuse : 0;
+    const auto t0 = std::chrono::steady_clock::now();
+    const HostModel& m = c->model;
+    std::memset(rep, 0, sizeof(*rep));
+    for (double& v : c->kt) v = 0.0;
+    c->launches = 0;
+    rep->active_tracks = m.active_tracks;
+    rep->observation_count = m.obs_count;
+    rep->rejected_initial_tracks = m.rejected;
+    rep->camera_blocks = m.ncb;
+    rep->intrinsic_blocks = m.ng;
+    rep->pattern_builds = c->pattern_builds;
+    rep->pattern_reuses = c->pattern_reuses;
+    if (!(op.robust_loss >= 0 && op.robust_loss <= 2 && std::isfinite(op.robust_loss_scale) && op.robust_loss_scale > 0)) {
+        rep->status = PB_SOLVE_INVALID_INPUT;
+        c->error = "invalid image robust loss";
+        return;
+    }
+    const float2 ls = ff_pack(op.robust_loss_scale);
+    for (int p = 0; p < 2; ++p) {
+        c->S[p].loss = op.robust_loss;
+        c->S[p].loss_scale = op.robust_loss_scale;
+        c->S[p].loss_scale_hi = ls.x;
+        c->S[p].loss_scale_lo = ls.y;
+    }
+    reset_state(c);
+    if (m.obs_count == 0) {
+        rep->status = PB_SOLVE_INVALID_INPUT;
+        return;
+    }
+    const int precision = op.precision == PB_PRECISION_MIXED ? PB_PRECISION_MIXED : PB_PRECISION_FP64;
+    const bool trace = std::getenv("PB_GPU_TRACE") != nullptr;
+    double current = kNaN, damping = 0.0;
+    int iterations = 0;
+    bool converged = m.P == 0 && m.ntb == 0;
+    bool failed = false, cancelled = false;
+    const double n_global = static_cast<double>(6 * m.ncb + m.ng * m.ni);
+    const double n_point = 3.0 * m.ntb;
+    auto t_asm = 0.0, t_lin = 0.0, t_bs = 0.0, t_obj = 0.0;
+    auto now = [] { return std::chrono::steady_clock::now(); };
+    auto ms = [](std::chrono::steady_clock::time_point a, std::chrono::steady_clock::time_point b) {
+        return std::chrono::duration<double, std::milli>(b - a).count();
+    };
+    const bool cost_from_assembly = precision != PB_PRECISION_MIXED;
+    try {
+        if (converged || !cost_from_assembly) {
+            double cst;
+            eval_costs(c, nullptr, 1, 0, &cst);
+            current = cst;
+            rep->initial_cost = current;
+            if (converged) ++rep->objective_evaluations;
+        }
+        const int budget = std::max(1, op.max_iterations);
+        while (iterations < budget && !converged) {
+            if (c->cancel) { cancelled = true; break; }
+            // buildNormalEquations: one linearisation and objective evaluation per state
+            ++rep->linearizations;
+            ++rep->objective_evaluations;
+            bool linearized = false;
+            bool relinearize = false;
+            while (iterations < budget && !converged && !relinearize) {
+                if (c->cancel) { cancelled = true; break; }
+                double cost;
+                int flags;
+                auto ta = now();
+                do_assemble(c, damping, precision, &cost, &flags);
+                t_asm += ms(ta, now());
+                if (flags & 4) throw std::runtime_error("assembly chunk table inconsistent (bounds check)");
+                if (flags & 2) throw std::runtime_error("linearisation produced an invalid projection");
+                if (cost_from_assembly && !linearized) {
+                    current = cost;
+                    if (rep->linearizations == 1) rep->initial_cost = current;
+                }
+                linearized = true;
+                if (flags & 1) throw std::runtime_error("eliminated point block is not numerically SPD (positive definite)");
+                bool lconv = false;
+                int lit = 0, sweeps = 0;
+                double relres = 0.0;
+                auto tl = now();
+                const int lrc = solve_reduced(c, op, &lconv, &lit, &relres, &sweeps);
+                t_lin += ms(tl, now());
+                if (lrc) throw std::runtime_error("reduced system is not numerically SPD (positive definite)");
+                rep->linear_iterations += lit;
+                rep->refinement_sweeps += sweeps;
+                ++iterations;
+                if (!lconv) {
+                    ++rep->rejected_steps;
+                    damping = damping == 0.0 ? 1e-3 : damping * 10.0;
+                    continue;
+                }
+                double dd_bs, psq, csq;
+                auto tb = now();
+                back_substitute(c, &dd_bs, &psq, &csq);
+                t_bs += ms(tb, now());
+                const double rg = n_global > 0 ? std::sqrt(csq / n_global) : 0.0;
+                const double rp = n_point > 0 ? std::sqrt(psq / n_point) : 0.0;
+                if (rg <= 1e-6 && rp <= 1e-6) {
+                    converged = true;
+                    continue;
+                }
+                auto tc = now();
+                // directional decrease by a forward difference of the objective along the step
+                double dd = 0.0;
+                {
+                    const double h = 1.0e-4;
+                    double fd;
+                    eval_costs(c, &h, 1, 1, &fd);
+                    ++rep->objective_evaluations;
+                    if (std::isfinite(fd) && fd < current) dd = (current - fd) / h;
+                }
+                double cand = kInfD, alpha = 1.0;
+                int accepted_slot = -1;
+                double accepted_alpha = 1.0;
+                int last_slot = -1;
+                int k0 = 0;
+                while (k0 < op.line_search_steps && accepted_slot < 0) {
+                    const int nbatch = std::min(k0 == 0 ? 1 : kMaxAlpha, op.line_search_steps - k0);
+                    double al[kMaxAlpha], costs[kMaxAlpha];
+                    for (int i = 0; i < nbatch; ++i) al[i] = std::ldexp(1.0, -(k0 + i));
+                    eval_costs(c, al, nbatch, 1, costs);
+                    for (int i = 0; i < nbatch; ++i) {
+                        ++rep->objective_evaluations;
+                        cand = costs[i];
+                        alpha = al[i];
+                        last_slot = i;
+                        const double limit = dd > 0.0 ? current - op.armijo_coefficient * alpha * dd : current;
+                        if (std::isfinite(cand) && cand <= limit && cand < current) {
+                            accepted_slot = i;
+                            accepted_alpha = alpha;
+                            break;
+                        }
+                    }
+                    k0 += nbatch;
+                }
+                t_obj += ms(tc, now());
+                // the last trial evaluated (the smallest step length) is accepted when it lowers
+                // the cost even without the Armijo condition
+                const bool accept = std::isfinite(cand) && cand < current;
+                if (accept && accepted_slot < 0) {
+                    accepted_slot = last_slot;
+                    accepted_alpha = alpha;
+                }
+                if (trace)
+                    std::fprintf(stderr,
+                                 "PB_GPU_TRACE general it=%d precision=%d cost=%.15e lambda=%.3e lin_it=%d relres=%.3e "
+                                 "dd=%.6e rms_global=%.3e rms_point=%.3e alpha=%.6g cand=%.15e accepted=%d\n",
+                                 iterations, precision, current, damping, lit, relres, dd, rg, rp, accepted_alpha, cand,
+                                 accept ? 1 : 0);
+                if (accept) {
+                    launch_accept(c->S[0], c->D[0], c->step_p, accepted_alpha, accepted_slot, c->stream);
+                    c->launches += 1;
+                    c->f32_stale = current - cand > 1e-2 * current;
+                    current = cand;
+                    ++rep->accepted_steps;
+                    damping /= 10.0;
+                    converged = accepted_alpha * rg <= 1e-6 && accepted_alpha * rp <= 1e-6;
+                    relinearize = !converged;
+                } else {
+                    ++rep->rejected_steps;
+                    damping = damping == 0.0 ? 1e-3 : damping * 10.0;
+                }
+            }
+        }
+        check(cudaStreamSynchronize(c->stream), "solve");
+    } catch (const CudaError&) {
+        throw;
+    } catch (const std::exception& e) {
+        failed = true;
+        c->error = e.what();
+    }
+    rep->iterations = iterations;
+    rep->final_cost = current;
+    rep->assembly_ms = t_asm;
+    rep->linear_ms = t_lin;
+    rep->back_substitution_ms = t_bs;
+    rep->objective_ms = t_obj;
+    if (cancelled) {
+        reset_state(c);
+        check(cudaStreamSynchronize(c->stream), "reset");
+        rep->status = PB_SOLVE_CANCELLED;
+        rep->solution_usable = 0;
+    } else if (failed) {
+        rep->status = PB_SOLVE_NUMERICAL_FAILURE;
+        rep->solution_usable = 0;
+    } else {
+        rep->status = converged ? PB_SOLVE_SUCCESS : PB_SOLVE_NO_CONVERGENCE;
+        rep->solution_usable = std::isfinite(current) ? 1 : 0;
+        finalize_quality(c, op, rep);
+    }
+    rep->gpu_kernel_launches = c->launches;
+    rep->total_ms = ms(t0, now());
+    c->solved = 1;
+}
+
 pb_status fail(pb_gpu_ctx* c, pb_status s, const std::string& msg) {
     if (c) c->error = msg;
     return s;
@@ -1011,6 +1250,7 @@ pb_status pb_gpu_destroy(pb_gpu_ctx* c) {
     c->darena.free_all();
     c->aarena.free_all();
     c->sarena.free_all();
+    schur_work_destroy(c->schur);
     if (c->h_scratch) cudaFreeHost(c->h_scratch);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
@@ -1060,6 +1300,7 @@ pb_status pb_gpu_upload(pb_gpu_ctx* c, const pb_problem_desc* pr, const pb_solve
                 dst.cam_contrib_begin = src.cam_contrib_begin; dst.cam_contrib = src.cam_contrib; dst.obs_lcam = src.obs_lcam;
                 dst.slot_item_begin = src.slot_item_begin; dst.slot_items = src.slot_items;
                 dst.lcam_obs_begin = src.lcam_obs_begin; dst.lcam_obs = src.lcam_obs;
+                dst.warp_task_begin = src.warp_task_begin; dst.task_list = src.task_list;
                 sd.nchunks = ss.nchunks; sd.max_obs = ss.max_obs; sd.max_cams = ss.max_cams; sd.max_pairs = ss.max_pairs; sd.max_tracks = ss.max_tracks;
             };
             keep_chunks(c->D[0], d0, c->S[0], s0);
@@ -1351,7 +1592,8 @@ pb_status pb_gpu_solve(pb_gpu_ctx* c, const pb_solve_options* op, pb_solve_repor
     try {
         cudaSetDevice(c->device);
         c->error.clear();
-        lm_solve(c, *op, rep);
+        if (op->general_path) lm_solve_general(c, *op, rep);
+        else lm_solve(c, *op, rep);
         return PB_OK;
     } catch (const std::exception& e) {
         rep->status = PB_SOLVE_NUMERICAL_FAILURE;
@@ -1753,6 +1995,27 @@ pb_status pb_gpu_backward(pb_gpu_ctx* c, const double* grad_cameras, const doubl
             rep->gpu_kernel_launches = c->launches - launches0;
             rep->status = PB_OK;
         }
+        return PB_OK;
+    } catch (const std::bad_alloc&) {
+        return fail(c, PB_ERR_CUDA, "device allocation failed");
+    } catch (const std::exception& e) {
+        return fail(c, PB_ERR_CUDA, e.what());
+    }
+}
+
+pb_status pb_gpu_solve_damped_schur(pb_gpu_ctx* c, const pb_bne* eq, double damping, const pb_schur_options* options,
+                                    double* primary_step, double* eliminated_step, pb_schur_report* report) {
+    if (!c || !eq || !options || !report) return fail(c, PB_ERR_INVALID_ARGUMENT, "null argument");
+    if (!(damping >= 0.0) || !std::isfinite(damping)) return fail(c, PB_ERR_INVALID_ARGUMENT, "invalid damping");
+    if (options->preconditioner_cluster_size < 0 || options->preconditioner_cluster_size > 16)
+        return fail(c, PB_ERR_INVALID_ARGUMENT, "preconditioner cluster size outside 1..16");
+    try {
+        cudaSetDevice(c->device);
+        if (!c->schur) c->schur = schur_work_create();
+        std::string err;
+        const int st = schur_solve(c->schur, c->device, c->stream, eq, damping, *options, primary_step, eliminated_step,
+                                   report, &err);
+        if (st != PB_OK) return fail(c, static_cast<pb_status>(st), err);
         return PB_OK;
     } catch (const std::bad_alloc&) {
         return fail(c, PB_ERR_CUDA, "device allocation failed");

@@ -23,6 +23,11 @@ EXPORTED = [
     "pb_gpu_kernel_times", "pb_gpu_objective_noalloc", "pb_gpu_solve_batch",
     "pb_gpu_save_state", "pb_gpu_restore_state", "pb_gpu_set_observations", "pb_gpu_backward",
     "pb_gpu_newton_step",
+    "pb_bne_create", "pb_bne_destroy", "pb_bne_clear_values", "pb_bne_sizes", "pb_bne_add_residual_blocks",
+    "pb_bne_add_primary_residual_blocks", "pb_bne_add_primary_residual_block",
+    "pb_bne_add_eliminated_residual_block", "pb_bne_add_residual_block", "pb_bne_add_primary_gradient_block",
+    "pb_bne_add_primary_hessian_block", "pb_bne_finalize_primary_diagonal", "pb_bne_merge_from",
+    "pb_bne_merge_eliminated_shard_from", "pb_bne_export", "pb_gpu_solve_damped_schur",
 ]
 
 
@@ -53,7 +58,8 @@ class SolveOptionsC(C.Structure):
                 ("linear_absolute_tolerance", C.c_double), ("refinement_sweeps", C.c_int32),
                 ("preconditioner_cluster_size", C.c_int32), ("linear_solver", C.c_int32),
                 ("calibration", C.c_double * 32), ("control_point_weight", C.c_double),
-                ("control_point_huber_delta", C.c_double)]
+                ("control_point_huber_delta", C.c_double), ("factor_reuse", C.c_int32),
+                ("general_path", C.c_int32)]
 
 
 class SolveReportC(C.Structure):
@@ -80,6 +86,27 @@ class AdjointReportC(C.Structure):
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class SchurOptionsC(C.Structure):
+    _fields_ = [("max_iterations", C.c_int32), ("relative_tolerance", C.c_double),
+                ("absolute_tolerance", C.c_double), ("preconditioner_cluster_size", C.c_int32),
+                ("use_initial_guess", C.c_int32), ("use_mixed_precision", C.c_int32)]
+
+
+class SchurReportC(C.Structure):
+    _fields_ = [(n, C.c_int32) for n in (
+        "converged", "iterations", "schur_pattern_reused", "schur_assembly_on_device", "mixed_precision_used",
+        "symbolic_analysis_reused", "eliminated_singular")] + [(n, C.c_double) for n in (
+            "relative_residual", "small_block_inverse_ms", "schur_accumulation_ms", "schur_assembly_ms",
+            "cholesky_factorization_ms", "triangular_solve_ms", "linear_solve_ms", "back_substitution_ms",
+            "total_ms")] + [("preconditioner_name", C.c_char * 64), ("device_name", C.c_char * 64)]
+
+    def as_dict(self):
+        d = {name: getattr(self, name) for name, _ in self._fields_}
+        for k in ("preconditioner_name", "device_name"):
+            d[k] = d[k].decode()
+        return d
 
 
 def library_path() -> str:
@@ -137,6 +164,22 @@ def load(build_if_missing: bool = False):
     L.pb_gpu_set_observations.argtypes = [vp, i64, vp, vp, vp]
     L.pb_gpu_backward.argtypes = [vp, vp, vp, vp, vp, vp, vp, C.POINTER(AdjointReportC)]
     L.pb_gpu_newton_step.argtypes = [vp, C.POINTER(dbl), C.POINTER(dbl)]
+    L.pb_bne_create.argtypes = [i32, i32, i32, i32, C.POINTER(vp)]
+    L.pb_bne_destroy.argtypes = [vp]
+    L.pb_bne_clear_values.argtypes = [vp]
+    L.pb_bne_sizes.argtypes = [vp, vp]
+    L.pb_bne_add_residual_blocks.argtypes = [vp, vp, vp, i32, i32, vp, vp, i32, dbl]
+    L.pb_bne_add_primary_residual_blocks.argtypes = [vp, vp, vp, i32, vp, i32, dbl]
+    L.pb_bne_add_primary_residual_block.argtypes = [vp, i32, vp, vp, i32, dbl]
+    L.pb_bne_add_eliminated_residual_block.argtypes = [vp, i32, vp, vp, i32, dbl]
+    L.pb_bne_add_residual_block.argtypes = [vp, i32, vp, i32, vp, vp, i32, dbl]
+    L.pb_bne_add_primary_gradient_block.argtypes = [vp, i32, vp]
+    L.pb_bne_add_primary_hessian_block.argtypes = [vp, i32, i32, vp]
+    L.pb_bne_finalize_primary_diagonal.argtypes = [vp, dbl, dbl]
+    L.pb_bne_merge_from.argtypes = [vp, vp]
+    L.pb_bne_merge_eliminated_shard_from.argtypes = [vp, vp, i32]
+    L.pb_bne_export.argtypes = [vp] + [vp] * 6
+    L.pb_gpu_solve_damped_schur.argtypes = [vp, vp, dbl, C.POINTER(SchurOptionsC), vp, vp, C.POINTER(SchurReportC)]
     for name in EXPORTED:
         if name not in ("pb_gpu_last_error", "pb_status_name"):
             getattr(L, name).restype = i32
@@ -192,7 +235,8 @@ def solve_options(options, problem=None) -> SolveOptionsC:
     o.intrinsic_mask = intrinsic_mask(cal)
     o.precision = int(Precision.Mixed if b.enablePlaMatrixMixedPrecision else Precision.Fp64)
     o.max_linear_iterations = b.maxLinearIterations
-    o.linear_relative_tolerance = 2.0e-10
+    # 0: the reference's tolerance of the path (2e-10 online, 1e-12 general)
+    o.linear_relative_tolerance = 0.0
     o.linear_absolute_tolerance = 1.0e-12
     o.refinement_sweeps = b.refinementSweeps
     o.preconditioner_cluster_size = b.plaMatrixPreconditionerClusterSize
@@ -202,6 +246,8 @@ def solve_options(options, problem=None) -> SolveOptionsC:
     con = getattr(options, "constraints", None)
     o.control_point_weight = con.controlPointWeight if con is not None else 1.0
     o.control_point_huber_delta = con.controlPointHuberDeltaMeters if con is not None else 0.2
+    o.factor_reuse = int(getattr(b, "factorReuse", 0))
+    o.general_path = 0 if s.useReferenceOnlineSchur else 1
     return o
 
 

@@ -206,6 +206,8 @@ class SolverControlOptions:
     imageRobustLossScalePixels: float = 1.0
     referenceArmijoCoefficient: float = 1.0e-3
     referenceLineSearchSteps: int = 34
+    # True: the online reduced-Schur path; False: the general path (the reference's default is
+    # False; this backend defaults to the online path, its headline path)
     useReferenceOnlineSchur: bool = True
     enablePointFilter: bool = True
     filterMaxReprojError: float = 2.5
@@ -321,6 +323,9 @@ class BackendOptions:
     refinementSweeps: int = 3
     maxLinearIterations: int = 0
     linearSolver: int = 0   # 0 auto, 1 dense-Cholesky-preconditioned CG, 2 block-Jacobi PCG
+    # dense-factor reuse across LM iterations: 0 default (mixed path keeps its FP32 factor, FP64
+    # path refactors every iteration), 1 keep on both paths, 2 refactor on both paths
+    factorReuse: int = 0
 
 
 @dataclass
