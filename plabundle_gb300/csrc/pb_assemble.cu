@@ -18,7 +18,8 @@
 //      the step, never the fixed point;
 //   K. per track and calibration group, K = sum over the group's observations of J_intr^T Y;
 //   D. every output element of the chunk is owned by one thread, which gathers its terms in a
-//      fixed order into compensated accumulators and writes the chunk partial once:
+//      fixed order into compensated accumulators and writes the chunk partial once (which
+//      thread owns which row is a host-built schedule that balances the warps' loads):
 //        pose block (a, b):  sum_o J^T M J (own terms)  -  sum_(o != o') G_o G_o'^T
 //        border (c, g):      sum_(o in c, g) w J_pose^T J_intr  -  sum_(o in c) G_o K_(t(o), g)^T
 //        intrinsic (g, g'):  sum_(o in g) w J_intr^T J_intr  -  sum_t K_(t,g) K_(t,g')^T
@@ -410,8 +411,12 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
     const int crow = 2 + ng * ni;  // rows of a camera record: rhs, direct rhs, border (g, c)
     const int chrec = nb * nb + 2 * nb;
     const int w_pair = npairs * 6, w_cam = ncams * crow;
-    const int w_total = w_pair + w_cam;
-    for (int wk = tid; wk < w_total; wk += blockDim.x) {
+    // host-built schedule (schedule_owner_tasks, pb_host.cpp): this warp's rounds of 32 tasks,
+    // dealt to the warps by longest processing time
+    const int task_end = D.warp_task_begin[chunk * kAssembleWarps + wid + 1];
+    for (int pos = D.warp_task_begin[chunk * kAssembleWarps + wid] + lane; pos < task_end; pos += 32) {
+        const int wk = D.task_list[pos];
+        if (wk == kNoTask) continue;
         if (wk < w_pair) {
             // row x of the pose block of chunk pair slot s
             const int s = wk / 6, x = wk - s * 6;
@@ -593,6 +598,7 @@ static AsmOutT<T> typed_out(const AsmOut& o) {
 // 256 threads per chunk whatever its observation count (at most 256): threads beyond the chunk's
 // observations idle in phases A-C and take their share of the gathers of phase D.
 constexpr int kAssembleThreads = 256;
+static_assert(kAssembleThreads == 32 * kAssembleWarps, "the owner-gather schedule is planned for 8 warps");
 
 template <typename T>
 void launch_assemble(const Shape& S, const DevPtrs& D, const AsmOut& O, double damping, size_t smem, cudaStream_t st) {

@@ -718,8 +718,124 @@ size_t chunk_smem_bytes(int precision, int max_obs, int max_tracks, int ni, int 
 namespace {
 
 struct ChunkLimits {
-    int max_obs, max_cams, max_pairs, max_tracks;
+    int max_obs, max_cams, max_pairs, max_tracks, precision;
 };
+
+// Owner-gather schedule of one chunk (phase D of the assembly kernel).  The chunk's tasks are
+// the rows of its pose pair blocks (6 per pair slot: task id 6 s + x) followed by its camera rows
+// (2 + ng ni per chunk camera: rhs, direct rhs, border columns).  A task's cost is estimated from
+// the terms its owner thread sums (compensated multiply-adds: 18 per own term and 20 per coupling
+// of a pose row; per observation 20 / 8 for the two gradient rows, and for a border row 2, plus
+// 12 for a direct term and 18 for a coupling through the track's intrinsic sums K).  The tasks are
+// cut into rounds of 32 (one per warp lane) and the rounds are dealt to the kAssembleWarps warps
+// by longest processing time: each round, costed by its longest task, goes to the warp with the
+// least load so far.
+//   - FP32 path: the rounds keep the natural task order.  Neighbouring lanes then own rows of the
+//     same pair block or camera and read the same observation records (shared-memory broadcasts);
+//     sorting by cost broke that and was measured slower (3.49 against 2.82 ms per 500-camera
+//     launch).
+//   - FP64 path: the FP64 pipe executes every lane slot of a warp instruction whether the lane is
+//     active or not, so the rounds are built from whole pair blocks and cameras sorted by
+//     decreasing cost (lanes of a round then run loops of similar length): 7.16 against 7.77 ms.
+// The schedule only decides which thread owns a task: every output is still summed by one thread
+// in the order of its item list, so results do not depend on it.
+void schedule_owner_tasks(const HostModel* m, int precision, int chunk_obs_start, int obs_end, int p_first, int p_end,
+                          const std::vector<unsigned char>& obs_lcam, ChunkSet& cs, int slot0, int nslots,
+                          int lcam0, int ncl) {
+    const int ng = m->ng, ni = m->ni;
+    const int crow = 2 + ng * ni;
+    const int nobs = obs_end - chunk_obs_start;
+    // calibration group and eliminated flag of every chunk observation, groups present per track
+    std::vector<int> grp(nobs, -1), tmask(nobs, 0);
+    std::vector<char> elim(nobs, 0);
+    for (int p = p_first; p < p_end; ++p) {
+        const int o0 = m->trk_obs_begin[p], o1 = m->trk_obs_begin[p + 1];
+        const bool el = m->track_block[m->trk_order[p]] >= 0;
+        int mask = 0;
+        for (int o = o0; o < o1; ++o) {
+            const int g = ng > 0 ? m->calib_group[m->obs_cam[m->p_obs_orig[o]]] : -1;
+            grp[o - chunk_obs_start] = g;
+            if (g >= 0) mask |= 1 << g;
+        }
+        for (int o = o0; o < o1; ++o) {
+            tmask[o - chunk_obs_start] = mask;
+            elim[o - chunk_obs_start] = el ? 1 : 0;
+        }
+    }
+    const int ntask = 6 * nslots + crow * ncl;
+    std::vector<std::pair<long long, int>> cost(ntask);
+    for (int sl = 0; sl < nslots; ++sl) {
+        long long c = 0;
+        for (int it = cs.slot_item_begin[slot0 + sl]; it < cs.slot_item_begin[slot0 + sl + 1]; ++it) {
+            const unsigned item = cs.slot_items[it];
+            c += (item & 0xFF) == (item >> 8) ? 18 : 20;
+        }
+        for (int x = 0; x < 6; ++x) cost[6 * sl + x] = {c, 6 * sl + x};
+    }
+    for (int l = 0; l < ncl; ++l) {
+        const int b0 = cs.lcam_obs_begin[lcam0 + l], b1 = cs.lcam_obs_begin[lcam0 + l + 1];
+        for (int row = 0; row < crow; ++row) {
+            long long c = 0;
+            if (row < 2) {
+                c = static_cast<long long>(b1 - b0) * (row == 0 ? 20 : 8);
+            } else {
+                const int g = (row - 2) / ni;
+                for (int it = b0; it < b1; ++it) {
+                    const int ob = cs.lcam_obs[it];
+                    c += 2 + (grp[ob] == g ? 12 : 0) + (elim[ob] && ((tmask[ob] >> g) & 1) ? 18 : 0);
+                }
+            }
+            const int id = 6 * nslots + l * crow + row;
+            cost[id] = {c, id};
+        }
+    }
+    if (precision == PB_PRECISION_FP64) {
+        // whole pair blocks (6 rows) and cameras (crow rows) by decreasing longest row, ties by
+        // position (a deterministic plan); rows inside a group keep their order
+        std::vector<std::pair<long long, int>> groups;
+        groups.reserve(static_cast<size_t>(nslots) + ncl);
+        for (int sl = 0; sl < nslots; ++sl) groups.push_back({cost[6 * sl].first, sl});
+        for (int l = 0; l < ncl; ++l) {
+            long long mx = 0;
+            for (int row = 0; row < crow; ++row) mx = std::max(mx, cost[6 * nslots + l * crow + row].first);
+            groups.push_back({mx, nslots + l});
+        }
+        std::stable_sort(groups.begin(), groups.end(), [](const auto& a, const auto& b) { return a.first > b.first; });
+        std::vector<std::pair<long long, int>> order;
+        order.reserve(cost.size());
+        for (const auto& g : groups) {
+            if (g.second < nslots) {
+                for (int x = 0; x < 6; ++x) order.push_back(cost[6 * g.second + x]);
+            } else {
+                const int l = g.second - nslots;
+                for (int row = 0; row < crow; ++row) order.push_back(cost[6 * nslots + l * crow + row]);
+            }
+        }
+        cost.swap(order);
+    }
+    const int nrounds = (ntask + 31) / 32;
+    std::vector<std::vector<int>> warp_rounds(kAssembleWarps);
+    std::vector<long long> load(kAssembleWarps, 0);
+    for (int r = 0; r < nrounds; ++r) {
+        long long rc = 0;
+        for (int k = 32 * r; k < std::min(ntask, 32 * r + 32); ++k) rc = std::max(rc, cost[k].first);
+        const int w = static_cast<int>(std::min_element(load.begin(), load.end()) - load.begin());
+        load[w] += rc;
+        warp_rounds[w].push_back(r);
+    }
+    const int base = static_cast<int>(cs.task_list.size());
+    int pos = base;
+    for (int w = 0; w < kAssembleWarps; ++w) {
+        cs.warp_task_begin.push_back(pos);
+        for (int r : warp_rounds[w]) {
+            for (int lane = 0; lane < 32; ++lane) {
+                const int k = 32 * r + lane;
+                cs.task_list.push_back(k < ntask ? static_cast<unsigned short>(cost[k].second) : kNoTask);
+            }
+            pos += 32;
+        }
+    }
+}
 
 // Greedy chunk plan of the processing-order tracks [p_begin, p_range_end) into `cs` (a partial plan:
 // its begin arrays are local to it, obs_begin holds global observation indices).  obs_lcam is
@@ -773,6 +889,7 @@ int plan_range(const HostModel* m, const ChunkLimits& lim, int p_begin, int p_ra
         // with oa on the lower chunk camera (both orientations when they share a camera).
         // Two passes over the chunk's tracks: count the items of every slot, then place them.
         std::vector<int> cnt(rp.size() + 1, 0);
+        const int p_first = chunk_trk_start;
         int p_end = chunk_trk_start;
         while (p_end < p_range_end && m->trk_obs_begin[p_end] < obs_end) ++p_end;
         for (int pass = 0; pass < 2; ++pass) {
@@ -830,6 +947,8 @@ int plan_range(const HostModel* m, const ChunkLimits& lim, int p_begin, int p_ra
             for (int o = chunk_obs_start; o < obs_end; ++o)
                 if (obs_lcam[o] != 255) cs.lcam_obs[cc[obs_lcam[o]]++] = static_cast<unsigned char>(o - chunk_obs_start);
         }
+        schedule_owner_tasks(m, lim.precision, chunk_obs_start, obs_end, p_first, p_end, obs_lcam, cs, cs.pair_begin.back(),
+                             static_cast<int>(rp.size()), cs.cam_begin.back(), ncl);
         cs.obs_begin.push_back(obs_end);
         cs.cam_begin.push_back(static_cast<int>(cs.cams.size()));
         cs.pair_begin.push_back(static_cast<int>(cs.pairs.size()));
@@ -933,7 +1052,8 @@ int build_chunks(HostModel* m, int precision, size_t smem_budget, std::string* e
     const int nb = m->ng * m->ni;
     int max_obs = 256;
     const int max_cams = 254;
-    const int max_pairs = 1 << 15;
+    // pair slots of a chunk: its owner-gather task ids (6 per slot plus the camera rows) are 16-bit
+    const int max_pairs = 8192;
     // tracks of a chunk: per-track intrinsic sums in shared memory; a quarter of the observations
     // (tracks of four or more views fill a chunk, shorter ones close it early)
     auto tracks_for = [](int mo) { return std::max(8, mo / 4); };
@@ -948,7 +1068,7 @@ int build_chunks(HostModel* m, int precision, size_t smem_budget, std::string* e
     cs.max_cams = max_cams;
     cs.max_pairs = max_pairs;
     cs.max_tracks = max_tracks;
-    const ChunkLimits lim{max_obs, max_cams, max_pairs, max_tracks};
+    const ChunkLimits lim{max_obs, max_cams, max_pairs, max_tracks, precision};
     const int ntp = static_cast<int>(m->trk_order.size());
     const long long nop = static_cast<long long>(m->p_obs_orig.size());
     cs.obs_lcam.assign(static_cast<size_t>(nop), 255);
@@ -991,7 +1111,11 @@ int build_chunks(HostModel* m, int precision, size_t smem_budget, std::string* e
         cs.pair_upper.insert(cs.pair_upper.end(), q.pair_upper.begin(), q.pair_upper.end());
         cs.slot_items.insert(cs.slot_items.end(), q.slot_items.begin(), q.slot_items.end());
         cs.lcam_obs.insert(cs.lcam_obs.end(), q.lcam_obs.begin(), q.lcam_obs.end());
+        const int task0 = static_cast<int>(cs.task_list.size());
+        for (int v : q.warp_task_begin) cs.warp_task_begin.push_back(task0 + v);
+        cs.task_list.insert(cs.task_list.end(), q.task_list.begin(), q.task_list.end());
     }
+    cs.warp_task_begin.push_back(static_cast<int>(cs.task_list.size()));
     // map each chunk pair to its upper pose block and build the reduce lists
     const int nupper = static_cast<int>(m->up_row.size());
     // upper index lookup per row: sorted by col

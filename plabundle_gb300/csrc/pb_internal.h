@@ -16,6 +16,8 @@ constexpr int kMaxGroups = 4;           // calibration groups held in the dense 
 constexpr int kMaxNB = kMaxGroups * kMaxNI;
 constexpr int kGroupRec = 6 * kP;       // params, prior, invSigma, lower, upper, enabled
 constexpr int kTrackRec = 12;           // L (upper 3x3: 6), q (3), rhs (3)
+constexpr int kAssembleWarps = 8;       // warps of an assembly CTA (256 threads)
+constexpr unsigned short kNoTask = 0xFFFF;  // idle lane of an owner-gather round
 
 // Device-side descriptors passed by value to kernels.
 struct Shape {
@@ -99,6 +101,10 @@ struct DevPtrs {
     unsigned short* slot_items;  // oa | ob << 8 (chunk-local observations); oa == ob: own term
     int* lcam_obs_begin;  // chunk cameras + 1: observations of each chunk camera
     unsigned char* lcam_obs;     // chunk-local observation indices
+    // owner-gather schedule: per chunk and warp, the first entry of the warp's task rounds
+    // (kAssembleWarps per chunk + 1); rounds of 32 task ids, kNoTask for an idle lane
+    int* warp_task_begin;
+    unsigned short* task_list;
     // reduce lists
     int* up_contrib_begin;  // nupper + 1
     int* up_contrib;        // partial pair slots
@@ -134,6 +140,9 @@ struct ChunkSet {
     std::vector<unsigned short> slot_items;
     std::vector<unsigned char> lcam_obs;
     std::vector<int> up_contrib_begin, up_contrib, cam_contrib_begin, cam_contrib;
+    // owner-gather schedule of phase D of the assembly (see schedule_owner_tasks in pb_host.cpp)
+    std::vector<int> warp_task_begin;
+    std::vector<unsigned short> task_list;
     size_t n_pair_partials() const { return pairs.size(); }
     size_t n_cam_partials() const { return cams.size(); }
     int n() const { return static_cast<int>(obs_begin.empty() ? 0 : obs_begin.size() - 1); }

@@ -8,7 +8,8 @@
 //     observation on the diagonal slot, one coupling per pair of observations of an eliminated
 //     track (lower chunk camera first; both orientations when the two share a camera);
 //   - every chunk camera lists exactly its observations, in order;
-//   - every chunk pair is reduced into the upper pose block of its two cameras, exactly once.
+//   - every chunk pair is reduced into the upper pose block of its two cameras, exactly once;
+//   - the owner-gather schedule holds every task of a chunk exactly once, in rounds of 32.
 // Returns 0 when all hold, else a nonzero code with a message.
 #include <algorithm>
 #include <cstdio>
@@ -139,7 +140,27 @@ extern "C" int probe_chunks(const pb_problem_desc* pr, const pb_solve_options* o
             for (int k = cs.cam_contrib_begin[blk]; k < cs.cam_contrib_begin[blk + 1]; ++k) hits += cs.cam_contrib[k] == c0 + l;
             if (hits != 1) return fail("chunk camera not reduced exactly once");
         }
+        // owner-gather schedule: every task of the chunk exactly once, rounds of 32 per warp
+        {
+            const int ntask = 6 * (cs.pair_begin[c + 1] - cs.pair_begin[c]) + (2 + m.ng * m.ni) * ncl;
+            std::vector<int> seen(static_cast<size_t>(ntask), 0);
+            for (int w = 0; w < kAssembleWarps; ++w) {
+                const int b = cs.warp_task_begin[c * kAssembleWarps + w], e = cs.warp_task_begin[c * kAssembleWarps + w + 1];
+                if (e < b || (e - b) % 32 != 0) return fail("warp task range not made of rounds of 32");
+                for (int k = b; k < e; ++k) {
+                    const int id = cs.task_list[k];
+                    if (id == kNoTask) continue;
+                    if (id >= ntask) return fail("task id outside the chunk");
+                    ++seen[id];
+                }
+            }
+            for (int v : seen)
+                if (v != 1) return fail("owner-gather task not scheduled exactly once");
+        }
     }
+    if (static_cast<int>(cs.warp_task_begin.size()) != nch * kAssembleWarps + 1 ||
+        cs.warp_task_begin.back() != static_cast<int>(cs.task_list.size()))
+        return fail("warp task table size");
     for (int v : slot_seen)
         if (!v) return fail("pair slot outside every chunk");
     if (stats) {
