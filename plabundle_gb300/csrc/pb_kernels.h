@@ -197,6 +197,13 @@ void launch_adjoint_schur(const Shape& S, const DevPtrs& D, const AdjBuffers& B,
                           const RedOut<double>& R, cudaStream_t st);
 void launch_adjoint_gradient(const Shape& S, const DevPtrs& D, const AdjBuffers& B, const double* mu, cudaStream_t st);
 
+// Damped Schur solves of host block normal equations (pb_schur.cu).
+struct SchurWork;
+SchurWork* schur_work_create();
+void schur_work_destroy(SchurWork* w);
+int schur_solve(SchurWork* w, int device, cudaStream_t st, const pb_bne* eq, double damping, const pb_schur_options& op,
+                double* primary_step, double* eliminated_step, pb_schur_report* report, std::string* err);
+
 void to_double(const float* in, double* out, int n, cudaStream_t st);
 void to_double(const double* in, double* out, int n, cudaStream_t st);
 void to_float(const double* in, float* out, int n, cudaStream_t st);
