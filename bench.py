@@ -69,10 +69,10 @@ def converged_iterations(workload_name):
 # dram__bytes_write.sum of an ncu capture on the 250-camera / 100k-point aerial grid
 # (663 659 observations; profiles/k_assemble_aerial250.md).  The chunk plan is the same at 500
 # cameras, so the traffic scales with the observations.
-ASSEMBLY_DRAM_BYTES_PER_OBS = (30.970112e6 + 251.056128e6) / 663659
+ASSEMBLY_DRAM_BYTES_PER_OBS = (38.476032e6 + 253.275904e6) / 663659
 # Warp instructions of one k_assemble<float> launch per observation (smsp__inst_executed.sum of the
 # same capture).
-ASSEMBLY_INST_PER_OBS = 902579227 / 663659
+ASSEMBLY_INST_PER_OBS = 903541636 / 663659
 SMS = 152  # streaming multiprocessors of a GB300
 
 # What the mixed path keeps in FP64 (everything else of the assembly and the CG preconditioner is
@@ -574,8 +574,9 @@ def run_gb300(args, rank, world, local_rank):
         fx = FX.load_fixture()
         if fx is None:
             vs_oracle = {"unavailable": "fixture absent"}
-        elif not FX.digests_match(fx[0], prob):
-            vs_oracle = {"unavailable": "generator does not reproduce the fixture's problem (digest differs)"}
+        elif FX.problem_mismatch(fx[0], fx[1], prob):
+            vs_oracle = {"unavailable": "generator does not reproduce the fixture's problem: "
+                                        + FX.problem_mismatch(fx[0], fx[1], prob)}
         else:
             vs_oracle = FX.compare(fx[0], fx[1], out_t["cameras"], out_t["intrinsics"], out_t["valid"],
                                    out_t["rms_after"], out_t["points"], rep_t["final_cost"], rep_t["filter_threshold"])

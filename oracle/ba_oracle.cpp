@@ -1297,7 +1297,7 @@ void solveLinear(const Oracle& o, std::vector<double>& x, bool* converged, int* 
             ++sweeps;
         }
         for (size_t i = 0; i < m; ++i) x[live[i]] = xc[i];
-        *converged = rn <= tol;
+        *converged = rn <= tol || !o.opt.residual_gate;
         *iterations = 1 + sweeps;
         return;
     }
@@ -1340,7 +1340,7 @@ void solveLinear(const Oracle& o, std::vector<double>& x, bool* converged, int* 
             spmv(o, x, sx);
             double tr = 0.0;
             for (size_t i = 0; i < n; ++i) tr += (b[i] - sx[i]) * (b[i] - sx[i]);
-            *converged = std::sqrt(tr) <= tol;
+            *converged = std::sqrt(tr) <= tol || !o.opt.residual_gate;
             break;
         }
         precond(r, z);
@@ -1751,7 +1751,7 @@ double buildGeneral(Oracle& o, GeneralEquations& q) {
 // (1 + damping), a zero primary diagonal entry set to 1; S = H_pp - sum W V^-1 W^T,
 // b = -g_p + sum W V^-1 g_e; dense FP64 Cholesky; y_e = V^-1 (-g_e - W^T x).  `converged`: the
 // residual |b - S x| is within max(tol |b|, 1e-12).
-void solveGeneralDamped(const GeneralEquations& q, double damping, double tol, std::vector<double>& x,
+void solveGeneralDamped(const GeneralEquations& q, double damping, double tol, bool gate, std::vector<double>& x,
                         std::vector<double>& y, bool* converged) {
     const size_t n = static_cast<size_t>(q.P) * kP;
     std::vector<double> S(n * n, 0.0), b(n);
@@ -1831,7 +1831,7 @@ void solveGeneralDamped(const GeneralEquations& q, double damping, double tol, s
         cholSolve(L, n, res);
         for (size_t i = 0; i < n; ++i) x[i] += res[i];
     }
-    *converged = std::sqrt(rn) <= limit;
+    *converged = std::sqrt(rn) <= limit || !gate;
     std::vector<double> r(static_cast<size_t>(q.E) * 3);
     for (int e = 0; e < q.E; ++e)
         for (int k = 0; k < 3; ++k) r[static_cast<size_t>(e) * 3 + k] = -q.ge[static_cast<size_t>(e) * 3 + k];
@@ -1887,7 +1887,7 @@ void solveGeneralPath(Oracle* o, orc_report* rep, double* current_out, int* iter
             while (iterations < budget && !converged && !relinearize) {
                 bool lconv = false;
                 const auto tl = std::chrono::steady_clock::now();
-                solveGeneralDamped(q, damping, tol, ps, es, &lconv);
+                solveGeneralDamped(q, damping, tol, o->opt.residual_gate != 0, ps, es, &lconv);
                 rep->linear_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - tl).count();
                 rep->linear_iterations += 1;
                 ++iterations;
@@ -2179,7 +2179,7 @@ int32_t orc_general_solve(void* h, double damping, double tolerance, double* pri
     try {
         std::vector<double> x, y;
         bool cv = false;
-        solveGeneralDamped(*o->general, damping, tolerance, x, y, &cv);
+        solveGeneralDamped(*o->general, damping, tolerance, o->opt.residual_gate != 0, x, y, &cv);
         std::copy(x.begin(), x.end(), primary);
         std::copy(y.begin(), y.end(), eliminated);
         *converged = cv;

@@ -83,6 +83,13 @@ typedef struct orc_options {
     double control_point_weight;    /* ConstraintOptions::controlPointWeight */
     double control_point_huber_delta; /* ConstraintOptions::controlPointHuberDeltaMeters */
     int32_t general_path;           /* 1: the general path (useReferenceOnlineSchur = false) */
+    /* 1: a linear solve counts as converged only when its true residual |b - S x| passes the
+     * tolerance (the reference's post-solve check of its direct CPU path); 0: the refined direct
+     * solution (or the PCG on its recursive residual) is accepted, as a CG solver that stops on
+     * its recursive residual does.  Near a fixed point of an ill-conditioned problem the true
+     * residual sits at the FP64 floor, where 1 rejects the step and ends the solve on a damped
+     * step. */
+    int32_t residual_gate;
 } orc_options;
 
 typedef struct orc_report {

@@ -41,7 +41,8 @@ class OrcOptions(C.Structure):
                 ("linear_solver", C.c_int32), ("max_linear_iterations", C.c_int32),
                 ("linear_relative_tolerance", C.c_double), ("linear_absolute_tolerance", C.c_double),
                 ("calibration", C.c_double * 32), ("control_point_weight", C.c_double),
-                ("control_point_huber_delta", C.c_double), ("general_path", C.c_int32)]
+                ("control_point_huber_delta", C.c_double), ("general_path", C.c_int32),
+                ("residual_gate", C.c_int32)]
 
 
 class OrcReport(C.Structure):
@@ -96,7 +97,7 @@ def _ptr(a):
     return None if a is None else a.ctypes.data
 
 
-def make_options(options, num_threads: int = 0, linear_solver: int = 0) -> OrcOptions:
+def make_options(options, num_threads: int = 0, linear_solver: int = 0, residual_gate: bool = True) -> OrcOptions:
     from plabundle_gb300.problem import intrinsic_mask
     s, cal = options.solver, options.calibration
     o = OrcOptions()
@@ -116,6 +117,7 @@ def make_options(options, num_threads: int = 0, linear_solver: int = 0) -> OrcOp
     o.max_linear_iterations = options.backend.maxLinearIterations
     # the reference's tolerances: 2e-10 online, 1e-12 on the general path (BundleAdjustPlaMatrix.cpp:321-330)
     o.general_path = 0 if s.useReferenceOnlineSchur else 1
+    o.residual_gate = 1 if residual_gate else 0
     o.linear_relative_tolerance = 2.0e-10 if s.useReferenceOnlineSchur else 1.0e-12
     o.linear_absolute_tolerance = 1.0e-12
     for i, v in enumerate(cal.numeric_block()):
@@ -144,7 +146,7 @@ def control_points(problem):
 class Oracle:
     """One oracle instance over a problem (holds the active problem and the reduced system)."""
 
-    def __init__(self, problem, options, num_threads: int = 0, linear_solver: int = 0):
+    def __init__(self, problem, options, num_threads: int = 0, linear_solver: int = 0, residual_gate: bool = True):
         self.problem = p = problem.normalized()
         self._keep = [p.cameras, p.points, p.track_offsets, p.obs_camera, p.obs_u, p.obs_v, p.obs_weight,
                       p.obs_scale]
@@ -157,7 +159,7 @@ class Oracle:
                                _ptr(p.obs_scale), fixed_c.size, _ptr(fixed_c), fixed_t.size, _ptr(fixed_t),
                                _ptr(p.cameraCalibrationGroupIds), _ptr(p.sharedIntrinsicReferenceCameras),
                                cp_t.size, _ptr(cp_t) if cp_t.size else None, _ptr(cp_d) if cp_t.size else None)
-        self.opts = make_options(options, num_threads, linear_solver)
+        self.opts = make_options(options, num_threads, linear_solver, residual_gate)
         g = p.gauge
         self.opts.gauge_policy = int(g.policy)
         self.opts.gauge_anchor_camera = g.referenceAnchorCameraIndex

@@ -661,19 +661,6 @@ int solve_reduced(pb_gpu_ctx* c, const pb_solve_options& op, bool* converged, in
     } else {
         rc = solve_dense<double>(c, rel, abs_tol, max_it, converged, iterations, relres);
     }
-    if (rc == 0 && *converged) {
-        // Post-solve residual check on the FP64 reduced system: the CG stops on its recursive
-        // residual, which near convergence can fall below the FP64 floor of the true residual
-        // |b - S x|.  The reference guards its direct factorisation the same way and, on a miss,
-        // retries the step with more damping (BundleAdjustPlaMatrix.cpp:321-330, :402-408).
-        residual64<double>(c->sys, c->red.rhs, c->step_c, c->r64, c->res_out, c->stream);
-        c->launches += 2;
-        check(cudaMemcpyAsync(c->h_scratch, c->res_out, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "D2H");
-        check(cudaStreamSynchronize(c->stream), "residual check");
-        const double rn = c->h_scratch[0], bn = c->h_scratch[1];
-        *relres = bn > 0.0 ? rn / bn : rn;
-        if (!(rn <= std::max(rel * bn, abs_tol))) *converged = false;
-    }
     return rc;
 }
 

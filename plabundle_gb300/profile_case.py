@@ -2,6 +2,7 @@
 
     python -m plabundle_gb300.profile_case --workload aerial500 --precision mixed --iterations 3
     python -m plabundle_gb300.profile_case --workload aerial250 --precision mixed --iterations 3
+    python -m plabundle_gb300.profile_case --workload aerial250 --precision mixed --iterations 3 --linear-solver 2
 
 `aerial500` is the 500-camera / 200k-point aerial grid of the benchmark (Cauchy 1.5 px, two
 calibration groups refining f, cx, cy, k1-k3, p1, p2); `aerial250` the same generator at half
@@ -41,9 +42,12 @@ def main():
     ap.add_argument("--workload", default="aerial250", choices=["aerial250", "aerial500"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--iterations", type=int, default=3)
+    ap.add_argument("--linear-solver", type=int, default=0, choices=[0, 1, 2],
+                    help="0 automatic, 1 dense-factor-preconditioned CG, 2 block-Jacobi PCG")
     a = ap.parse_args()
     mixed = a.precision == "mixed"
     p, o = workload(a.workload, mixed, 1)
+    o.backend.linearSolver = a.linear_solver
     warm = Gb300Context(0)
     assert warm.upload(p, o) == 0
     warm.solve()
