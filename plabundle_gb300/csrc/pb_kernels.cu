@@ -453,40 +453,56 @@ __global__ void k_cost_final(Shape S, DevPtrs D, const double* __restrict__ part
 
 // Back-substitution (recoverReferencePointSteps, ...ReferenceSchur.cpp:982-1082), one thread per
 // track:  dp = R^-T (q - R^-1 u),  u = sum_o w J_p^T (J_o dc).
+// Per observation o of an eliminated track: the term Y_o^T A_o dc (3 values) of its track's sum,
+// one thread per observation (records read by consecutive lanes, FP64 accumulation).
 template <typename T>
+__global__ void __launch_bounds__(256) k_backsub_terms(Shape S, DevPtrs D, const T* __restrict__ obs_rec,
+                                                       const double* __restrict__ step_c, double* __restrict__ terms) {
+    const long long o = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (o >= S.nop) return;
+    const int nA = 6 + S.ni, stride = 2 * nA + 6;
+    const int cam = D.obs_cam[o];
+    const T* rec = obs_rec + static_cast<size_t>(o) * stride;
+    double e0 = 0.0, e1 = 0.0;
+    const int b = D.cam_block[cam];
+    if (b >= 0)
+        for (int a = 0; a < 6; ++a) {
+            const double dcv = step_c[6 * b + a];
+            e0 = fma(static_cast<double>(rec[a]), dcv, e0);
+            e1 = fma(static_cast<double>(rec[nA + a]), dcv, e1);
+        }
+    const int g = S.ng > 0 ? D.cam_group[cam] : -1;
+    if (g >= 0)
+        for (int a = 0; a < S.ni; ++a) {
+            const double dcv = step_c[6 * S.ncb + g * S.ni + a];
+            e0 = fma(static_cast<double>(rec[6 + a]), dcv, e0);
+            e1 = fma(static_cast<double>(rec[nA + 6 + a]), dcv, e1);
+        }
+    const T* Y = rec + 2 * nA;
+    double* u = terms + static_cast<size_t>(o) * 3;
+    u[0] = static_cast<double>(Y[0]) * e0 + static_cast<double>(Y[3]) * e1;
+    u[1] = static_cast<double>(Y[1]) * e0 + static_cast<double>(Y[4]) * e1;
+    u[2] = static_cast<double>(Y[2]) * e0 + static_cast<double>(Y[5]) * e1;
+}
+
+// track:  dp = R^-T (q - R^-1 u),  u = sum_o w J_p^T (J_o dc).
 __global__ void __launch_bounds__(256) k_back_substitute(Shape S, DevPtrs D, const double* __restrict__ trk_data,
-                                                         const T* __restrict__ obs_rec, const double* __restrict__ step_c,
+                                                         const double* __restrict__ terms,
                                                          double* __restrict__ step_p, double* __restrict__ part) {
     // Point steps dp = V^-1 (g_p - W^T dc) = R^-T (q - sum_o Y_o^T A_o dc) from the records the
     // assembly kept (A = [J_pose | J_intr] rows and Y = w Jp R^-T of every observation), with
     // FP64 accumulation (recoverReferencePointSteps, BundleAdjustPlaMatrixReferenceSchur.cpp:982-1082).
+    // The per-observation terms come from k_backsub_terms and are summed here in observation order,
+    // the order of a single-thread loop over the track.
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    const int nA = 6 + S.ni, stride = 2 * nA + 6;
     double dd = 0.0, ss = 0.0;
     if (t < S.ntp && D.trk_block[t] >= 0) {
         double u0 = 0.0, u1 = 0.0, u2 = 0.0;
         for (int o = D.trk_obs_begin[t]; o < D.trk_obs_begin[t + 1]; ++o) {
-            const int cam = D.obs_cam[o];
-            const T* rec = obs_rec + static_cast<size_t>(o) * stride;
-            double e0 = 0.0, e1 = 0.0;
-            const int b = D.cam_block[cam];
-            if (b >= 0)
-                for (int a = 0; a < 6; ++a) {
-                    const double dcv = step_c[6 * b + a];
-                    e0 = fma(static_cast<double>(rec[a]), dcv, e0);
-                    e1 = fma(static_cast<double>(rec[nA + a]), dcv, e1);
-                }
-            const int g = S.ng > 0 ? D.cam_group[cam] : -1;
-            if (g >= 0)
-                for (int a = 0; a < S.ni; ++a) {
-                    const double dcv = step_c[6 * S.ncb + g * S.ni + a];
-                    e0 = fma(static_cast<double>(rec[6 + a]), dcv, e0);
-                    e1 = fma(static_cast<double>(rec[nA + 6 + a]), dcv, e1);
-                }
-            const T* Y = rec + 2 * nA;
-            u0 += static_cast<double>(Y[0]) * e0 + static_cast<double>(Y[3]) * e1;
-            u1 += static_cast<double>(Y[1]) * e0 + static_cast<double>(Y[4]) * e1;
-            u2 += static_cast<double>(Y[2]) * e0 + static_cast<double>(Y[5]) * e1;
+            const double* u = terms + static_cast<size_t>(o) * 3;
+            u0 += u[0];
+            u1 += u[1];
+            u2 += u[2];
         }
         const double* td = trk_data + static_cast<size_t>(t) * kTrackRec;
         const double i00 = td[0], i10 = td[1], i11 = td[2], i20 = td[3], i21 = td[4], i22 = td[5];
@@ -731,9 +747,12 @@ void launch_reduce_sums64(const Shape& S, const DevPtrs& D, const AsmOut& O, con
 
 template <typename T>
 void launch_back_substitute(const Shape& S, const DevPtrs& D, const double* trk_data, const T* obs_rec, const double* step_c,
-                            double* step_p, double* part, const double* direct64, double* out, cudaStream_t st) {
+                            double* step_p, double* terms, double* part, const double* direct64, double* out,
+                            cudaStream_t st) {
     const int nblk = std::max(1, (S.ntp + 255) / 256);
-    k_back_substitute<T><<<nblk, 256, 0, st>>>(S, D, trk_data, obs_rec, step_c, step_p, part);
+    if (S.nop > 0)
+        k_backsub_terms<T><<<static_cast<unsigned>((S.nop + 255) / 256), 256, 0, st>>>(S, D, obs_rec, step_c, terms);
+    k_back_substitute<<<nblk, 256, 0, st>>>(S, D, trk_data, terms, step_p, part);
     k_backsub_final<<<1, 256, 0, st>>>(S, D, part, nblk, step_c, direct64, out);
 }
 
@@ -932,9 +951,9 @@ template void launch_reduce<float>(const Shape&, const DevPtrs&, const AsmOut&, 
 template void launch_reduce<double>(const Shape&, const DevPtrs&, const AsmOut&, const RedOut<double>&, double,
                                     cudaStream_t);
 template void launch_back_substitute<float>(const Shape&, const DevPtrs&, const double*, const float*, const double*,
-                                            double*, double*, const double*, double*, cudaStream_t);
+                                            double*, double*, double*, const double*, double*, cudaStream_t);
 template void launch_back_substitute<double>(const Shape&, const DevPtrs&, const double*, const double*, const double*,
-                                             double*, double*, const double*, double*, cudaStream_t);
+                                             double*, double*, double*, const double*, double*, cudaStream_t);
 template void launch_linearize_export<float>(const Shape&, const DevPtrs&, double*, double*, double*, double*, double*,
                                              double*, signed char*, cudaStream_t);
 template void launch_linearize_export<double>(const Shape&, const DevPtrs&, double*, double*, double*, double*,

@@ -61,9 +61,11 @@ void launch_reduce_sums64(const Shape& S, const DevPtrs& D, const AsmOut& O, con
 // from the original-order arrays through obs_orig and trk_obs_begin.
 void launch_gather_obs(long long nop, int ntp, const DevPtrs& D, cudaStream_t st);
 
+// terms: processed observations * 3 doubles (per-observation terms, summed per track in order)
 template <typename T>
 void launch_back_substitute(const Shape& S, const DevPtrs& D, const double* trk_data, const T* obs_rec, const double* step_c,
-                            double* step_p, double* part, const double* direct64, double* out, cudaStream_t st);
+                            double* step_p, double* terms, double* part, const double* direct64, double* out,
+                            cudaStream_t st);
 template <typename T>
 void launch_linearize_export(const Shape& S, const DevPtrs& D, double* res, double* jp, double* jpose, double* ji,
                              double* nw, double* cost, signed char* valid, cudaStream_t st);

@@ -132,6 +132,7 @@ struct pb_gpu_ctx {
     double* r64 = nullptr;
     double* res_out = nullptr;
     double* bs_part = nullptr;
+    double* bs_terms = nullptr;  // per processed observation: its term of the point back-substitution
     double* bs_out = nullptr;
     double* cost_part = nullptr;
     double* cost_out = nullptr;
@@ -332,6 +333,7 @@ void upload_structure(pb_gpu_ctx* c) {
     c->res_out = A.alloc<double>(2 + static_cast<size_t>(std::max(1, (m.ncb + 7) / 8)) * kMaxNB);
     const int bs_blocks = std::max(1, (ntp + 255) / 256);
     c->bs_part = A.alloc<double>(2 * static_cast<size_t>(bs_blocks));
+    c->bs_terms = A.alloc<double>(3 * static_cast<size_t>(std::max<long long>(1, nop)));
     c->bs_out = A.alloc<double>(4);
     const long long cost_blocks = std::max<long long>(1, (nop + 255) / 256);
     c->cost_part = A.alloc<double>(static_cast<size_t>(cost_blocks) * kMaxAlpha * 2);
@@ -671,12 +673,12 @@ void back_substitute(pb_gpu_ctx* c, double* dd, double* point_sq, double* cam_sq
     if (precision == PB_PRECISION_FP64)
         launch_back_substitute<double>(S, D, static_cast<const double*>(c->p64.out.trk_data_v),
                                        static_cast<const double*>(c->p64.out.obs_rec_v), c->step_c, c->step_p,
-                                       c->bs_part, c->direct64, c->bs_out, c->stream);
+                                       c->bs_terms, c->bs_part, c->direct64, c->bs_out, c->stream);
     else
         launch_back_substitute<float>(S, D, static_cast<const double*>(c->p32.out.trk_data_v),
-                                      static_cast<const float*>(c->p32.out.obs_rec_v), c->step_c, c->step_p, c->bs_part,
-                                      c->direct64, c->bs_out, c->stream);
-    c->launches += 2;
+                                      static_cast<const float*>(c->p32.out.obs_rec_v), c->step_c, c->step_p, c->bs_terms,
+                                      c->bs_part, c->direct64, c->bs_out, c->stream);
+    c->launches += 3;
     check(cudaGetLastError(), "back-substitution launch");
     check(cudaMemcpyAsync(c->h_scratch, c->bs_out, 3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "D2H");
     check(cudaStreamSynchronize(c->stream), "back-substitution");
