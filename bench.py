@@ -37,7 +37,8 @@ def parse_args():
     ap.add_argument("--workload", default="aerial",
                     choices=["aerial", "aerial_gcp", "aerial3000_gcp", "ring", "windows", "adjoint"])
     ap.add_argument("--windows", type=int, default=256, help="local-BA windows of the windows workload")
-    ap.add_argument("--workers", type=int, default=8, help="worker contexts of the windows workload")
+    ap.add_argument("--workers", type=int, default=0,
+                    help="worker contexts of the windows workload (0: chosen by the batch autotuner)")
     ap.add_argument("--cpu-iterations", type=int, default=2,
                     help="LM iterations of the bounded CPU sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -285,7 +286,7 @@ def run_windows(args, rank, world, local_rank):
     import numpy as np
     import torch
     from plabundle_gb300 import synth
-    from plabundle_gb300.batch import solve_batch
+    from plabundle_gb300.batch import solve_batch, tune_workers
     from plabundle_gb300.problem import ImageRobustLoss, SolveOptions
 
     wins = synth.window_problems(n_windows=args.windows, seed=window_seed(rank))
@@ -295,7 +296,12 @@ def run_windows(args, rank, world, local_rank):
     o.solver.imageRobustLossScalePixels = 1.5
     o.solver.maxIterations = 20
     o.backend.enablePlaMatrixMixedPrecision = True
-    solve_batch(wins[:2 * args.workers], o, n_workers=args.workers, device=local_rank)  # warm-up
+    # worker count: the batch's autotuner on a sample of this rank's windows (--workers 0), or as given
+    tuned = None
+    workers = args.workers
+    if workers <= 0:
+        workers, tuned = tune_workers(wins, o, device=local_rank)
+    solve_batch(wins[:2 * workers], o, n_workers=workers, device=local_rank)  # warm-up
     rates, lats = [], None
     for _ in range(max(1, args.steps)):
         # whole-job rate: every rank's windows over the slowest rank's time
@@ -303,7 +309,7 @@ def run_windows(args, rank, world, local_rank):
             torch.distributed.barrier()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        res, lat = solve_batch(wins, o, n_workers=args.workers, device=local_rank)
+        res, lat = solve_batch(wins, o, n_workers=workers, device=local_rank)
         torch.cuda.synchronize()
         dt = max_over_ranks(time.perf_counter() - t0, world)
         rates.append(world * len(wins) / dt)
@@ -319,7 +325,8 @@ def run_windows(args, rank, world, local_rank):
             "impl": "gb300", "n_gpus": world, "steps": args.steps, "warmup": 1, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64 (mixed)", "data": "synthetic (seeded)",
             "config": {"workload": f"{len(wins)} ring windows per GPU, 10-60 cameras, 1k-20k points",
-                       "observations": int(sum(p.n_obs for p in wins)), "workers": args.workers,
+                       "observations": int(sum(p.n_obs for p in wins)), "workers": workers,
+                       "workers_tuned": tuned,
                        "max_lm_iterations": 20, "loss": "huber_1.5px"},
             "latency_ms": {"p50": float(np.percentile(lats, 50)), "p99": float(np.percentile(lats, 99))},
             "one_at_a_time": {"windows_per_s": seq_rate, "latency_p50_ms": float(np.percentile(lat1, 50)),

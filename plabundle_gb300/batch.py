@@ -1,10 +1,17 @@
 """Batched solves of independent problems (local bundle-adjustment windows) through
 pb_gpu_solve_batch: every problem is solved as `Solver.solve` would solve it, with worker
-contexts on their own streams so that the windows overlap on the device."""
+contexts on their own streams so that the windows overlap on the device.
+
+`tune_workers` is the batch's autotuner: the number of worker contexts sets how the host
+planning of the windows and their kernels overlap, and the best count depends on the host's
+cores, the device and the window sizes, so it is chosen by measured throughput on a sample of
+the caller's own windows.  Results do not depend on the count (every window is solved exactly as
+alone)."""
 from __future__ import annotations
 
 import ctypes as C
-from typing import List, Sequence
+import time
+from typing import Dict, List, Sequence, Tuple
 
 import numpy as np
 
@@ -44,3 +51,22 @@ def solve_batch(problems: Sequence[Problem], options: SolveOptions, n_workers: i
         results.append(r)
     del keep
     return results, latency
+
+
+def tune_workers(problems: Sequence[Problem], options: SolveOptions, device: int = 0,
+                 candidates: Sequence[int] = (4, 6, 8, 12, 16), sample: int = 48,
+                 repeats: int = 2) -> Tuple[int, Dict[int, float]]:
+    """Worker count with the highest measured throughput (problems per second) on the first
+    `sample` problems, best of `repeats` timed batches per candidate after one untimed batch
+    (device memory, module loading).  Returns (best count, {count: problems per second})."""
+    sub = list(problems[:max(1, min(sample, len(problems)))])
+    solve_batch(sub[:max(candidates)], options, n_workers=max(candidates), device=device)
+    rates: Dict[int, float] = {}
+    for w in candidates:
+        best = 0.0
+        for _ in range(max(1, repeats)):
+            t0 = time.perf_counter()
+            solve_batch(sub, options, n_workers=w, device=device)
+            best = max(best, len(sub) / (time.perf_counter() - t0))
+        rates[int(w)] = best
+    return max(rates, key=rates.get), rates

@@ -5,8 +5,9 @@
 // solved exactly as pb_gpu_solve_problem solves it) and gets the windows onto the device
 // together: n_workers host threads each own a context with its own stream and take problems from
 // a shared queue, so the kernels of different windows overlap on the GPU, their host-side
-// planning overlaps on the CPU, and a context's device memory is reused from one window to the
-// next (slab arena).  The cooperative solvers size their grids to the window.
+// planning overlaps on the CPU (each worker's planning threads capped at the host cores divided
+// by the workers), and a context's device memory is reused from one window to the next (slab
+// arena).  The cooperative solvers size their grids to the window.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -15,7 +16,7 @@
 #include <thread>
 #include <vector>
 
-#include "../../include/pb_gpu.h"
+#include "pb_internal.h"
 
 extern "C" pb_status pb_gpu_solve_batch(int32_t device, int32_t n_problems, const pb_problem_desc* problems,
                                         const pb_solve_options* options, int32_t n_workers, pb_solve_report* reports,
@@ -31,11 +32,15 @@ extern "C" pb_status pb_gpu_solve_batch(int32_t device, int32_t n_problems, cons
         int expected = PB_OK;
         if (st != PB_OK) first_error.compare_exchange_strong(expected, st);
     };
+    // the workers share the host cores for their planning (the plan does not depend on it)
+    const int cap = std::max(1, static_cast<int>(std::max(1u, std::thread::hardware_concurrency())) / workers);
     auto work = [&]() {
+        pb::set_host_thread_cap(cap);
         pb_gpu_ctx* ctx = nullptr;
         const pb_status cs = pb_gpu_create(device, &ctx);
         if (cs != PB_OK) {
             note(cs);
+            pb::set_host_thread_cap(0);
             return;
         }
         for (int i = next.fetch_add(1); i < n_problems; i = next.fetch_add(1)) {
@@ -49,6 +54,7 @@ extern "C" pb_status pb_gpu_solve_batch(int32_t device, int32_t n_problems, cons
             note(st);
         }
         pb_gpu_destroy(ctx);
+        pb::set_host_thread_cap(0);
     };
     std::vector<std::thread> pool;
     pool.reserve(workers - 1);

@@ -20,10 +20,16 @@ bool finite3(const double* v) { return std::isfinite(v[0]) && std::isfinite(v[1]
 
 // Host threads for a loop of n independent items: one per hardware thread, at most 32, and at
 // least 4096 items each.
+// Cap on the planning threads of the calling thread (0: none), set by pb_gpu_solve_batch so that
+// its concurrent workers share the host cores instead of each spawning a full set.
+thread_local int g_host_thread_cap = 0;
+
 int host_threads(long long n) {
     const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
     const long long by_size = std::max(1LL, n / 4096);
-    return static_cast<int>(std::min<long long>(std::min<unsigned>(hw, 32u), by_size));
+    long long t = std::min<long long>(std::min<unsigned>(hw, 32u), by_size);
+    if (g_host_thread_cap > 0) t = std::min<long long>(t, g_host_thread_cap);
+    return static_cast<int>(t);
 }
 
 // f(i, begin, end) over `nthreads` contiguous ranges of [0, n); thread i gets range i.
@@ -66,6 +72,8 @@ bool project(const double* cam, const double* X, double* px) {
 }
 
 }  // namespace
+
+void set_host_thread_cap(int cap) { g_host_thread_cap = cap > 0 ? cap : 0; }
 
 double finite_median(std::vector<double> v, double fallback) {
     v.erase(std::remove_if(v.begin(), v.end(), [](double a) { return !std::isfinite(a); }), v.end());
@@ -746,8 +754,13 @@ void schedule_owner_tasks(const HostModel* m, int precision, int chunk_obs_start
     const int crow = 2 + ng * ni;
     const int nobs = obs_end - chunk_obs_start;
     // calibration group and eliminated flag of every chunk observation, groups present per track
-    std::vector<int> grp(nobs, -1), tmask(nobs, 0);
-    std::vector<char> elim(nobs, 0);
+    // (per-thread buffers: the planner calls this once per chunk)
+    thread_local std::vector<int> grp, tmask;
+    thread_local std::vector<char> elim;
+    thread_local std::vector<std::pair<long long, int>> cost;
+    grp.assign(nobs, -1);
+    tmask.assign(nobs, 0);
+    elim.assign(nobs, 0);
     for (int p = p_first; p < p_end; ++p) {
         const int o0 = m->trk_obs_begin[p], o1 = m->trk_obs_begin[p + 1];
         const bool el = m->track_block[m->trk_order[p]] >= 0;
@@ -763,7 +776,7 @@ void schedule_owner_tasks(const HostModel* m, int precision, int chunk_obs_start
         }
     }
     const int ntask = 6 * nslots + crow * ncl;
-    std::vector<std::pair<long long, int>> cost(ntask);
+    cost.resize(ntask);
     for (int sl = 0; sl < nslots; ++sl) {
         long long c = 0;
         for (int it = cs.slot_item_begin[slot0 + sl]; it < cs.slot_item_begin[slot0 + sl + 1]; ++it) {
@@ -814,20 +827,22 @@ void schedule_owner_tasks(const HostModel* m, int precision, int chunk_obs_start
         cost.swap(order);
     }
     const int nrounds = (ntask + 31) / 32;
-    std::vector<std::vector<int>> warp_rounds(kAssembleWarps);
-    std::vector<long long> load(kAssembleWarps, 0);
+    thread_local std::vector<int> owner;
+    owner.assign(nrounds, 0);
+    long long load[kAssembleWarps] = {};
     for (int r = 0; r < nrounds; ++r) {
         long long rc = 0;
         for (int k = 32 * r; k < std::min(ntask, 32 * r + 32); ++k) rc = std::max(rc, cost[k].first);
-        const int w = static_cast<int>(std::min_element(load.begin(), load.end()) - load.begin());
+        const int w = static_cast<int>(std::min_element(load, load + kAssembleWarps) - load);
         load[w] += rc;
-        warp_rounds[w].push_back(r);
+        owner[r] = w;
     }
-    const int base = static_cast<int>(cs.task_list.size());
-    int pos = base;
+    int pos = static_cast<int>(cs.task_list.size());
+    cs.task_list.reserve(cs.task_list.size() + 32 * static_cast<size_t>(nrounds));
     for (int w = 0; w < kAssembleWarps; ++w) {
         cs.warp_task_begin.push_back(pos);
-        for (int r : warp_rounds[w]) {
+        for (int r = 0; r < nrounds; ++r) {
+            if (owner[r] != w) continue;
             for (int lane = 0; lane < 32; ++lane) {
                 const int k = 32 * r + lane;
                 cs.task_list.push_back(k < ntask ? static_cast<unsigned short>(cost[k].second) : kNoTask);

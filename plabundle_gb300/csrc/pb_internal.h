@@ -206,6 +206,9 @@ bool cp_valid(const double* data, double* W);
 int build_chunks(HostModel* m, int precision, size_t smem_budget, std::string* err);
 size_t chunk_smem_bytes(int precision, int max_obs, int max_tracks, int ni, int nb);
 double finite_median(std::vector<double> v, double fallback);
+// Largest number of threads the host planning of the calling thread may use (0: no cap).  The
+// plan and every result are the same for any cap.
+void set_host_thread_cap(int cap);
 void camera_parameter_block(const double* cam, double* p);
 
 }  // namespace pb
