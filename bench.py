@@ -44,6 +44,8 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--fd-obs", type=int, default=64,
                     help="observations of the finite-difference check of the adjoint workload")
+    ap.add_argument("--no-secondary", action="store_true",
+                    help="leave out the windows and backward-pass records of the default 1-GPU run")
     return ap.parse_args()
 
 
@@ -85,12 +87,16 @@ MIXED_FP64_SPLIT = ("projection and residual; 3x3 point blocks, their factor and
                     "products and sums")
 
 
-def workload(name):
+def workload(name, problem=None):
+    """(problem, options, config) of a named workload; `problem`: the 500-camera grid when the
+    caller has generated it already (the generator is seeded, so it is the same problem)."""
     from plabundle_gb300 import synth
     from plabundle_gb300.problem import ImageRobustLoss, SolveOptions
     opts = SolveOptions()
     if name in ("aerial", "aerial_gcp", "aerial3000_gcp"):
-        if name == "aerial3000_gcp":
+        if name == "aerial" and problem is not None:
+            prob = problem
+        elif name == "aerial3000_gcp":
             # the 3 000-camera block of the large survey configuration (60 x 50 nadir grid,
             # 1.5 M points, ~10 M observations) without rigs or scale bars
             prob = synth.aerial_grid_problem(seed=21, n_along=60, n_lines=50, n_points=1_500_000)
@@ -279,17 +285,24 @@ def run_reference(args, rank):
 
 
 def run_windows(args, rank, world, local_rank):
+    line = measure_windows(args.windows, args.workers, args.steps, rank, world, local_rank)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def measure_windows(n_windows, workers, steps, rank, world, local_rank):
     """Batched local BA: independent ring windows (10-60 cameras, 1k-20k points, each generated
     like the 20-camera ring with its own seed), mixed precision, 20 LM iterations, solved through
-    pb_gpu_solve_batch with `--workers` contexts, against the same windows one at a time.  Host
-    wall clock (the batch spans several streams); inputs start in host memory."""
+    pb_gpu_solve_batch with `workers` contexts (0: chosen by the batch autotuner), against the same
+    windows one at a time.  Host wall clock (the batch spans several streams); inputs start in host
+    memory.  Returns the bench line (rank 0; None on the other ranks)."""
     import numpy as np
     import torch
     from plabundle_gb300 import synth
     from plabundle_gb300.batch import solve_batch, tune_workers
     from plabundle_gb300.problem import ImageRobustLoss, SolveOptions
 
-    wins = synth.window_problems(n_windows=args.windows, seed=window_seed(rank))
+    wins = synth.window_problems(n_windows=n_windows, seed=window_seed(rank))
     torch.cuda.set_device(local_rank)
     o = SolveOptions()
     o.solver.imageRobustLoss = ImageRobustLoss.Huber
@@ -298,12 +311,11 @@ def run_windows(args, rank, world, local_rank):
     o.backend.enablePlaMatrixMixedPrecision = True
     # worker count: the batch's autotuner on a sample of this rank's windows (--workers 0), or as given
     tuned = None
-    workers = args.workers
     if workers <= 0:
         workers, tuned = tune_workers(wins, o, device=local_rank)
     solve_batch(wins[:2 * workers], o, n_workers=workers, device=local_rank)  # warm-up
     rates, lats = [], None
-    for _ in range(max(1, args.steps)):
+    for _ in range(max(1, steps)):
         # whole-job rate: every rank's windows over the slowest rank's time
         if world > 1:
             torch.distributed.barrier()
@@ -320,9 +332,9 @@ def run_windows(args, rank, world, local_rank):
     ok = sum(1 for r in res if r["status"] in (1, 2))
     same = sum(1 for a, b in zip(res, res1) if a["final_cost"] == b["final_cost"])
     if rank != 0:
-        return
-    line = {"metric": "local-BA windows per second (batched)", "value": statistics.mean(rates), "unit": "windows/s",
-            "impl": "gb300", "n_gpus": world, "steps": args.steps, "warmup": 1, "higher_is_better": True,
+        return None
+    return {"metric": "local-BA windows per second (batched)", "value": statistics.mean(rates), "unit": "windows/s",
+            "impl": "gb300", "n_gpus": world, "steps": steps, "warmup": 1, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64 (mixed)", "data": "synthetic (seeded)",
             "config": {"workload": f"{len(wins)} ring windows per GPU, 10-60 cameras, 1k-20k points",
                        "observations": int(sum(p.n_obs for p in wins)), "workers": workers,
@@ -333,10 +345,15 @@ def run_windows(args, rank, world, local_rank):
                               "latency_p99_ms": float(np.percentile(lat1, 99))},
             "speedup_vs_one_at_a_time": statistics.mean(rates) / seq_rate,
             "solved": ok, "identical_to_one_at_a_time": same}
-    print(json.dumps(line), flush=True)
 
 
 def run_adjoint(args, rank, world, local_rank):
+    line = measure_adjoint(args.steps, args.warmup, args.fd_obs, rank, world, local_rank)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def measure_adjoint(steps, warmup, fd_obs, rank, world, local_rank, problem=None):
     """Backward pass of the converged 500-camera aerial solve (mixed precision): implicit
     differentiation with the exact Hessian of L = sum_i |C_i - (C_i_true + N(0, 0.1 m))|^2 with
     respect to every observation and initial pose.  value: device time of one pb_gpu_backward
@@ -344,14 +361,15 @@ def run_adjoint(args, rank, world, local_rank):
     e2e: the same call through the Python API with its host buffers (the loss gradient in,
     dL/d(u, v) and dL/d(initial pose) out).  Then the central finite-difference check (h = 1e-3
     px) on --fd-obs random observations: every perturbed solve restarts from the saved fixed
-    point and is re-converged with full Gauss-Newton steps."""
+    point and is re-converged with full Gauss-Newton steps.  `problem`: the 500-camera grid when
+    the caller has generated it already.  Returns the bench line (rank 0; None on the others)."""
     import numpy as np
     import torch
     from plabundle_gb300.adjoint import camera_centre_loss, newton_polish
     from plabundle_gb300.device import Gb300Context
 
     torch.cuda.set_device(local_rank)
-    prob, opts, cfg = workload("aerial")
+    prob, opts, cfg = workload("aerial", problem)
     opts.backend.enablePlaMatrixMixedPrecision = True
     ctx = Gb300Context(local_rank)
     assert ctx.upload(prob, opts) == 0
@@ -363,12 +381,12 @@ def run_adjoint(args, rank, world, local_rank):
     L, g = camera_centre_loss(d["cameras"], targets)
     stream = torch.cuda.ExternalStream(ctx.stream_handle())
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         out = ctx.backward(grad_cameras=g)
     sampler = ClockSampler(local_rank)
     sampler.start()
     dev_ms, e2e_ms, reports = [], [], []
-    for _ in range(args.steps):
+    for _ in range(steps):
         flush.fill_(1.0)
         torch.cuda.synchronize()
         e0 = torch.cuda.Event(enable_timing=True)
@@ -385,7 +403,7 @@ def run_adjoint(args, rank, world, local_rank):
     go = out["observations"]
     # finite differences
     ctx.save_state()
-    pick = rng.choice(np.nonzero(np.abs(go).sum(1) > 0)[0], args.fd_obs, replace=False)
+    pick = rng.choice(np.nonzero(np.abs(go).sum(1) > 0)[0], fd_obs, replace=False)
     h = 1e-3
     fd = np.zeros((pick.size, 2))
     t_fd = time.perf_counter()
@@ -405,12 +423,13 @@ def run_adjoint(args, rank, world, local_rank):
     err = np.linalg.norm(go[pick] - fd) / np.linalg.norm(fd)
     per_obs = np.linalg.norm(go[pick] - fd, axis=1) / np.maximum(np.linalg.norm(fd, axis=1), 1e-300)
     last = reports[-1]
+    ctx.close()
     if rank != 0:
-        return
+        return None
     nobs = prob.n_obs
-    line = {"metric": "adjoint backward time (exact-Hessian implicit differentiation)",
+    return {"metric": "adjoint backward time (exact-Hessian implicit differentiation)",
             "value": statistics.mean(dev_ms), "unit": "ms", "impl": "gb300", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.mean(dev_ms),
+            "steps": steps, "warmup": warmup, "ms_per_step": statistics.mean(dev_ms),
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64 Hessian records, f32 factor + f64 CG", "data": "synthetic (seeded)",
             "config": dict(cfg, loss_of_solution="sum |C_i - (C_true + N(0, 0.1 m))|^2",
@@ -429,7 +448,6 @@ def run_adjoint(args, rank, world, local_rank):
                     "d2h_bytes_per_step": int(16 * nobs + 48 * prob.n_cameras + 24 * prob.n_tracks)},
             "gpu_launches": int(last["gpu_kernel_launches"]),
             "clocks": clocks}
-    print(json.dumps(line), flush=True)
 
 
 def run_gb300(args, rank, world, local_rank):
@@ -646,7 +664,26 @@ def run_gb300(args, rank, world, local_rank):
     }
     if cpu:
         line["cpu_baseline"] = cpu
+    if args.workload == "aerial" and world == 1 and not args.no_secondary:
+        # the two other workloads of the path, measured after the headline's timed region in the
+        # same run: 256 batched local-BA windows and the backward pass of this converged solve
+        ctx.close()
+        line["secondary"] = secondary_records(prob, local_rank)
     print(json.dumps(line), flush=True)
+
+
+def secondary_records(prob, local_rank):
+    """Compact records of the windows and backward-pass workloads (their own bench lines, with
+    fewer timed repetitions: 2 timed batches of the 256 windows; 3 backward passes after 3 warm-up
+    passes and a 16-observation finite-difference check)."""
+    out = {}
+    t0 = time.perf_counter()
+    out["windows"] = measure_windows(256, 0, 2, 0, 1, local_rank)
+    out["windows"]["wall_seconds"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    out["adjoint"] = measure_adjoint(3, 3, 16, 0, 1, local_rank, problem=prob)
+    out["adjoint"]["wall_seconds"] = time.perf_counter() - t0
+    return out
 
 
 def main():

@@ -632,6 +632,11 @@ int dense_factor(const PcgSystem<double>& sys, DenseWork<T>& W, double shift, cu
     int status = 0;
     cudaMemcpyAsync(&status, W.status, sizeof(int), cudaMemcpyDeviceToHost, st);
     if (cudaStreamSynchronize(st) != cudaSuccess) return -1;
+    // opt-in trace (PB_GPU_TRACE=1): one line per factorisation
+    static const bool trace = std::getenv("PB_GPU_TRACE") != nullptr;
+    if (trace)
+        std::fprintf(stderr, "PB_GPU_FACTOR precision=%d n=%d shift=%.3e status=%d\n", sizeof(T) == 4 ? 1 : 0, n, shift,
+                     status);
     return status;
 }
 
