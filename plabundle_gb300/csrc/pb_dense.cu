@@ -172,6 +172,17 @@ __device__ __forceinline__ int owned_elements(int* ii, int* ll) {
 }
 
 // Block 0 of step k: L_kk (written to A_kk, zeros above the diagonal) and D_k = L_kk^-1.
+//
+// The factorisation is the unscaled right-looking elimination (after step j, column j holds
+// d_j * L_:j): every lower element (i, l) receives a_il -= a_ij a_lj / d_j for j < l in increasing
+// j.  It runs in four panels of 16 columns so that the block synchronises 12 times instead of once
+// per column: warp 0 eliminates the panel's 16 x 16 diagonal block on its own (warp barriers) and
+// records 1 / d_j, then the rows below take the panel's steps in registers (16 lanes per row, the
+// row's pivot entries by shuffle), then every thread applies the panel's 16 steps, in order, to
+// its elements of the trailing block.  Each element sees the same updates in the same order as a
+// column-by-column elimination.  The inverse R = L^-1 (R = I, R_ic -= L_ij R_jc / L_jj for
+// i > j >= c, then R_ic / L_ii) is independent per column: four lanes own a column (rows split
+// mod 4, held in registers) and pass row j between them by shuffle, with no block barrier.
 template <typename T>
 __device__ void diag_factor_inverse(T* __restrict__ A, T* __restrict__ Dinv, int np, int k, T* sA, T* sB,
                                     int* __restrict__ status) {
@@ -179,19 +190,65 @@ __device__ void diag_factor_inverse(T* __restrict__ A, T* __restrict__ Dinv, int
     tile_load<T, false>(Akk, np, sA);
     int ii[9], ll[9];
     owned_elements(ii, ll);
-    // unscaled right-looking elimination: after step j, column j holds d_j * L_:j
-    for (int j = 0; j < TS; ++j) {
-        __syncthreads();
-        const T d = sA[j * TP + j];
-        if (!(d > T(0))) {
-            if (threadIdx.x == 0) atomicOr(status, 2);
-        }
-        const T inv = d > T(0) ? T(1) / d : T(0);
-#pragma unroll
-        for (int s = 0; s < 9; ++s)
-            if (ll[s] > j) sA[ii[s] * TP + ll[s]] -= sA[ii[s] * TP + j] * sA[ll[s] * TP + j] * inv;
-    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __shared__ T s_inv[TS];  // 1 / d_j of the elimination, then 1 / L_jj of the inverse
+    constexpr int PW = 16;   // panel width
     __syncthreads();
+    for (int c0 = 0; c0 < TS; c0 += PW) {
+        // (a) the panel's diagonal block, warp 0: elements (c0 + ri, c0 + rl), 1 <= rl <= ri < 16
+        if (warp == 0) {
+            int ri[4], rl[4];
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+                const int e = lane + 32 * t;  // 120 elements
+                int r = 1;
+                while (r * (r + 1) / 2 <= e) ++r;  // e < r (r + 1) / 2: row r, column e - r (r - 1) / 2 + 1
+                ri[t] = e < 120 ? r : -1;
+                rl[t] = e < 120 ? e - r * (r - 1) / 2 + 1 : 0x7fff;
+            }
+            for (int j = c0; j < c0 + PW; ++j) {
+                __syncwarp();
+                const T d = sA[j * TP + j];
+                if (!(d > T(0))) {
+                    if (lane == 0) atomicOr(status, 2);
+                }
+                const T inv = d > T(0) ? T(1) / d : T(0);
+                if (lane == 0) s_inv[j] = inv;
+                const int rj = j - c0;
+#pragma unroll
+                for (int t = 0; t < 4; ++t)
+                    if (rl[t] > rj && ri[t] >= 0) {
+                        const int i = c0 + ri[t], l = c0 + rl[t];
+                        sA[i * TP + l] -= sA[i * TP + j] * sA[l * TP + j] * inv;
+                    }
+            }
+        }
+        __syncthreads();
+        // (b) rows below the diagonal block, panel columns: two rows per warp, a lane per column
+        const int nbelow = TS - c0 - PW;
+        for (int task = warp; task < nbelow / 2; task += static_cast<int>(blockDim.x >> 5)) {
+            const int i = c0 + PW + 2 * task + (lane >> 4), l = c0 + (lane & 15);
+            T a = sA[i * TP + l];
+#pragma unroll
+            for (int j = c0; j < c0 + PW; ++j) {
+                const T aij = __shfl_sync(0xffffffffu, a, (lane & 16) | (j - c0));
+                if (l > j) a -= aij * sA[l * TP + j] * s_inv[j];
+            }
+            sA[i * TP + l] = a;
+        }
+        __syncthreads();
+        // (c) the trailing block: elements (i, l), c0 + 16 <= l <= i < 64, the panel's steps in order
+        const int m = nbelow, ntrail = m * (m + 1) / 2;
+        for (int e = threadIdx.x; e < ntrail; e += blockDim.x) {
+            const int t = tri_row(e);
+            const int i = c0 + PW + t, l = c0 + PW + (e - t * (t + 1) / 2);
+            T a = sA[i * TP + l];
+#pragma unroll
+            for (int j = c0; j < c0 + PW; ++j) a -= sA[i * TP + j] * sA[l * TP + j] * s_inv[j];
+            sA[i * TP + l] = a;
+        }
+        __syncthreads();
+    }
     T v[9];
 #pragma unroll
     for (int s = 0; s < 9; ++s) {
@@ -206,16 +263,33 @@ __device__ void diag_factor_inverse(T* __restrict__ A, T* __restrict__ Dinv, int
         if (ii[s] < 0) continue;
         sA[ii[s] * TP + ll[s]] = v[s];
         if (ii[s] != ll[s]) sA[ll[s] * TP + ii[s]] = T(0);
-        sB[ii[s] * TP + ll[s]] = ii[s] == ll[s] ? T(1) : T(0);  // R = I (lower part)
-        if (ii[s] != ll[s]) sB[ll[s] * TP + ii[s]] = T(0);
     }
-    // inverse: right-looking on R = I, one barrier per column: R_ic -= L_ij R_jc / L_jj
-    for (int j = 0; j < TS; ++j) {
-        __syncthreads();
-        const T inv = T(1) / sA[j * TP + j];
+    __syncthreads();
+    // 1 / L_jj once per row for the inverse
+    if (threadIdx.x < TS) s_inv[threadIdx.x] = T(1) / sA[threadIdx.x * TP + threadIdx.x];
+    __syncthreads();
+    {
+        // column c = 8 warp + lane / 4; this lane holds rows i = part + 4 q
+        const int c = 8 * warp + (lane >> 2), part = lane & 3;
+        T r[TS / 4];
 #pragma unroll
-        for (int s = 0; s < 9; ++s)
-            if (ii[s] > j && ll[s] <= j) sB[ii[s] * TP + ll[s]] -= sA[ii[s] * TP + j] * sB[j * TP + ll[s]] * inv;
+        for (int q = 0; q < TS / 4; ++q) r[q] = part + 4 * q == c ? T(1) : T(0);
+#pragma unroll
+        for (int j = 0; j < TS; ++j) {
+            // row j of the column, final from the steps before j, from the lane that holds it
+            const T rj = __shfl_sync(0xffffffffu, r[j >> 2], (lane & ~3) | (j & 3));
+            if (8 * warp <= j) {  // some column of this warp has c <= j
+                const T inv = s_inv[j];
+#pragma unroll
+                for (int q = 0; q < TS / 4; ++q) {
+                    if (4 * q + 3 <= j) continue;  // every row of this slot is <= j
+                    const int i = part + 4 * q;
+                    if (i > j && c <= j) r[q] -= sA[i * TP + j] * rj * inv;
+                }
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < TS / 4; ++q) sB[(part + 4 * q) * TP + c] = r[q];
     }
     __syncthreads();
 #pragma unroll
