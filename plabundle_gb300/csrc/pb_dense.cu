@@ -174,8 +174,8 @@ __device__ __forceinline__ int owned_elements(int* ii, int* ll) {
 // Block 0 of step k: L_kk (written to A_kk, zeros above the diagonal) and D_k = L_kk^-1.
 //
 // The factorisation is the unscaled right-looking elimination (after step j, column j holds
-// d_j * L_:j): every lower element (i, l) receives a_il -= a_ij a_lj / d_j for j < l in increasing
-// j.  It runs in four panels of 16 columns so that the block synchronises 12 times instead of once
+// d_j * L_:j): every lower element (i, l) receives a_il = fma(-(a_ij a_lj), 1 / d_j, a_il) for
+// j < l in increasing j (one rounding of the product, one of the update, in every phase).  It runs in four panels of 16 columns so that the block synchronises 12 times instead of once
 // per column: warp 0 eliminates the panel's 16 x 16 diagonal block on its own (warp barriers) and
 // records 1 / d_j, then the rows below take the panel's steps in registers (16 lanes per row, the
 // row's pivot entries by shuffle), then every thread applies the panel's 16 steps, in order, to
@@ -195,14 +195,18 @@ __device__ void diag_factor_inverse(T* __restrict__ A, T* __restrict__ Dinv, int
     constexpr int PW = 16;   // panel width
     __syncthreads();
     for (int c0 = 0; c0 < TS; c0 += PW) {
-        // (a) the panel's diagonal block, warp 0: elements (c0 + ri, c0 + rl), 1 <= rl <= ri < 16
-        if (warp == 0) {
+        // (a) the panel's diagonal block, warp 0.  FP32: in registers, lane r holds columns 0-7 of
+        // row c0 + r, lane r + 16 its columns 8-15, and pivot entries reach the other lanes by
+        // shuffle.  FP64: in shared memory, each lane updating its own few of the block's 120
+        // elements, which issues a quarter of the FP64 instructions of the register form (every
+        // lane of that form steps through every column).
+        if (warp == 0 && sizeof(T) == 8) {
             int ri[4], rl[4];
 #pragma unroll
             for (int t = 0; t < 4; ++t) {
-                const int e = lane + 32 * t;  // 120 elements
+                const int e = lane + 32 * t;  // e < 120: row r, column e - r (r - 1) / 2 + 1
                 int r = 1;
-                while (r * (r + 1) / 2 <= e) ++r;  // e < r (r + 1) / 2: row r, column e - r (r - 1) / 2 + 1
+                while (r * (r + 1) / 2 <= e) ++r;
                 ri[t] = e < 120 ? r : -1;
                 rl[t] = e < 120 ? e - r * (r - 1) / 2 + 1 : 0x7fff;
             }
@@ -219,9 +223,34 @@ __device__ void diag_factor_inverse(T* __restrict__ A, T* __restrict__ Dinv, int
                 for (int t = 0; t < 4; ++t)
                     if (rl[t] > rj && ri[t] >= 0) {
                         const int i = c0 + ri[t], l = c0 + rl[t];
-                        sA[i * TP + l] -= sA[i * TP + j] * sA[l * TP + j] * inv;
+                        sA[i * TP + l] = fma(-(sA[i * TP + j] * sA[l * TP + j]), inv, sA[i * TP + l]);
                     }
             }
+            __syncwarp();
+        } else if (warp == 0) {
+            const int ri = lane & 15, half = lane >> 4;
+            T a[PW / 2];
+#pragma unroll
+            for (int q = 0; q < PW / 2; ++q) a[q] = sA[(c0 + ri) * TP + c0 + 8 * half + q];
+#pragma unroll
+            for (int rj = 0; rj < PW; ++rj) {
+                const int hj = rj >> 3;  // half holding column rj
+                const T d = __shfl_sync(0xffffffffu, a[rj & 7], rj + 16 * hj);
+                if (!(d > T(0))) {
+                    if (lane == 0) atomicOr(status, 2);
+                }
+                const T inv = d > T(0) ? T(1) / d : T(0);
+                if (lane == 0) s_inv[c0 + rj] = inv;
+                const T aij = __shfl_sync(0xffffffffu, a[rj & 7], ri + 16 * hj);
+#pragma unroll
+                for (int rl = 1; rl < PW; ++rl) {
+                    if (rl <= rj) continue;
+                    const T alj = __shfl_sync(0xffffffffu, a[rj & 7], rl + 16 * hj);
+                    if (half == (rl >> 3) && ri >= rl) a[rl & 7] = fma(-(aij * alj), inv, a[rl & 7]);
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < PW / 2; ++q) sA[(c0 + ri) * TP + c0 + 8 * half + q] = a[q];
         }
         __syncthreads();
         // (b) rows below the diagonal block, panel columns: two rows per warp, a lane per column
@@ -232,7 +261,7 @@ __device__ void diag_factor_inverse(T* __restrict__ A, T* __restrict__ Dinv, int
 #pragma unroll
             for (int j = c0; j < c0 + PW; ++j) {
                 const T aij = __shfl_sync(0xffffffffu, a, (lane & 16) | (j - c0));
-                if (l > j) a -= aij * sA[l * TP + j] * s_inv[j];
+                if (l > j) a = fma(-(aij * sA[l * TP + j]), s_inv[j], a);
             }
             sA[i * TP + l] = a;
         }
@@ -244,7 +273,7 @@ __device__ void diag_factor_inverse(T* __restrict__ A, T* __restrict__ Dinv, int
             const int i = c0 + PW + t, l = c0 + PW + (e - t * (t + 1) / 2);
             T a = sA[i * TP + l];
 #pragma unroll
-            for (int j = c0; j < c0 + PW; ++j) a -= sA[i * TP + j] * sA[l * TP + j] * s_inv[j];
+            for (int j = c0; j < c0 + PW; ++j) a = fma(-(sA[i * TP + j] * sA[l * TP + j]), s_inv[j], a);
             sA[i * TP + l] = a;
         }
         __syncthreads();
@@ -284,7 +313,7 @@ __device__ void diag_factor_inverse(T* __restrict__ A, T* __restrict__ Dinv, int
                 for (int q = 0; q < TS / 4; ++q) {
                     if (4 * q + 3 <= j) continue;  // every row of this slot is <= j
                     const int i = part + 4 * q;
-                    if (i > j && c <= j) r[q] -= sA[i * TP + j] * rj * inv;
+                    if (i > j && c <= j) r[q] = fma(-(sA[i * TP + j] * rj), inv, r[q]);
                 }
             }
         }
@@ -417,9 +446,15 @@ __global__ void __launch_bounds__(256) k_potrf_coop(T* __restrict__ A, T* __rest
 
 // ---- conjugate gradients on the FP64 reduced matrix, preconditioner D X^T X D (X = L^-1).
 // One cooperative persistent kernel runs the whole solve; per iteration four phases separated
-// by grid barriers: (1) the direction update fused with the block-CSR SpMV (q = S z + beta q, a
-// warp per pose block row or border row), (2) the x / r updates, (3) w = X D r and (4)
-// z = D X^T w (a warp per row).
+// by grid barriers: (1) the direction update fused with the block-CSR SpMV, (2) the x / r
+// updates, (3) w = X D r and (4) z = D X^T w (a warp per row).  Grid-wide sums: p.q after (1),
+// r.r after (2), r.z after (4).  (Reading r.r together with r.z after (4), one sum fewer, measured
+// slower at 500 cameras: 82.7 against 79.0 ms of CG per solve.)
+// FP64 arithmetic issues at 1/64 of the FP32 rate on this part: an SM sub-partition retires one
+// warp-wide FP64 instruction about every 64 cycles.  The phases are therefore shaped by their
+// FP64 instructions per sub-partition rather than by bytes: the SpMV runs as short work items (32
+// pose blocks, or 256 entries of a border row, per warp) whose partial sums the owners of the
+// rows add in a fixed order, and the dot-product reductions do their FP64 adds on four warps.
 // Dot products go through per-block partials that every block sums in the same fixed order, so
 // all blocks take the same convergence / breakdown decision and no result depends on timing.
 namespace {
@@ -428,33 +463,84 @@ constexpr int kCgWarps = kCgThreads / 32;
 constexpr int kCgPart = 4;  // partial slots per block
 }  // namespace
 
-// Block sum of v (all threads), written by thread 0 to *dst.
-__device__ __forceinline__ void block_partial(double v, double* s_red, double* dst) {
-    v = warp_sum(v);
+// Block sum of v (all threads), written by thread 0 to *dst: warps 0-3 (one per sub-partition)
+// each add 64 of the values, thread 0 the four sums.  Every caller passes a grid barrier before
+// s_vals / s_q are written again.
+__device__ __forceinline__ void block_partial(double v, double* s_vals, double* s_q, double* dst) {
+    s_vals[threadIdx.x] = v;
+    __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane == 0) s_red[warp] = v;
+    if (warp < 4) {
+        double t = s_vals[64 * warp + lane] + s_vals[64 * warp + 32 + lane];
+        t = warp_sum(t);
+        if (lane == 0) s_q[warp] = t;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) *dst = (s_q[0] + s_q[1]) + (s_q[2] + s_q[3]);
+}
+
+// Sums over blocks of partial slots `slot` and `slot + 1` (TWO) or `slot` alone, identical in
+// every block: warps 0-3 each add a quarter of the blocks' partials (lane l: every 32nd), thread 0
+// the four sums, broadcast through s_tot (a grid barrier separates two uses of one slot).
+template <bool TWO>
+__device__ __forceinline__ void grid_totals(const double* part, int slot, double* s_q, double* s_tot) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int G = static_cast<int>(gridDim.x);
+    if (warp < 4) {
+        const int k0 = G * warp / 4, k1 = G * (warp + 1) / 4;
+        double t0 = 0.0, t1 = 0.0;
+#pragma unroll 4
+        for (int k = k0 + lane; k < k1; k += 32) {
+            t0 += part[k * kCgPart + slot];
+            if (TWO) t1 += part[k * kCgPart + slot + 1];
+        }
+        t0 = warp_sum(t0);
+        if (TWO) t1 = warp_sum(t1);
+        if (lane == 0) {
+            s_q[4 + warp] = t0;
+            if (TWO) s_q[8 + warp] = t1;
+        }
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
-        double t = 0.0;
-        for (int w = 0; w < kCgWarps; ++w) t += s_red[w];
-        *dst = t;
+        s_tot[slot] = (s_q[4] + s_q[5]) + (s_q[6] + s_q[7]);
+        if (TWO) s_tot[slot + 1] = (s_q[8] + s_q[9]) + (s_q[10] + s_q[11]);
     }
     __syncthreads();
 }
 
-// Sum over blocks of partial slot `slot`, identical in every block: every thread loads at most
-// a couple of partials at once (no dependent load chain), then a fixed shuffle and warp order.
-__device__ __forceinline__ double grid_total(const double* part, int slot, double* s_red) {
-    double v = 0.0;
-    for (int k = threadIdx.x; k < static_cast<int>(gridDim.x); k += blockDim.x) v += part[k * kCgPart + slot];
-    v = warp_sum(v);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    __syncthreads();
-    if (lane == 0) s_red[warp] = v;
-    __syncthreads();
-    double t = 0.0;
-    for (int w = 0; w < kCgWarps; ++w) t += s_red[w];
-    __syncthreads();
+// Warp sums of eight per-lane values with nine FP64 adds: a transposing butterfly in which, at
+// each of the first three levels, a lane keeps half of its values and adds its partner's share of
+// them.  The total of value x ends in lanes 4x .. 4x + 3 (all four hold the same bits).
+__device__ __forceinline__ double warp_sum8(double (&a)[8]) {
+    const int lane = threadIdx.x & 31;
+    {
+        const bool up = lane & 16;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const double send = up ? a[j] : a[4 + j];
+            const double keep = up ? a[4 + j] : a[j];
+            a[j] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+        }
+    }
+    {
+        const bool up = lane & 8;
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            const double send = up ? a[j] : a[2 + j];
+            const double keep = up ? a[2 + j] : a[j];
+            a[j] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+        }
+    }
+    double t;
+    {
+        const bool up = lane & 4;
+        const double send = up ? a[0] : a[1];
+        const double keep = up ? a[1] : a[0];
+        t = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+    }
+    t += __shfl_xor_sync(0xffffffffu, t, 2);
+    t += __shfl_xor_sync(0xffffffffu, t, 1);
     return t;
 }
 
@@ -494,25 +580,35 @@ __device__ __forceinline__ double tri_rows(const T* __restrict__ M, int np, int 
     return contrib;
 }
 
-// Direction update fused with the SpMV: p = z + beta p_old, written by each row's owner to p_new,
-// and q = S p with the neighbours' entries of p formed on the fly by the same expression (so
-// bitwise equal to what their owners write), over the pose block rows and the border rows (a
-// warp per row).  On the first iteration (beta == 0) p = z exactly, whatever p_old holds.
-// Returns this thread's share of p.q.
+// Direction update fused with the SpMV: p = z + beta p_old, written to p_new by the first work
+// item of each row, and the partial products of S p, with the entries of p formed on the fly by
+// the same expression (so bitwise equal to p_new).  On the first iteration (beta == 0) p = z
+// exactly, whatever p_old holds.  Work items, one warp each, in the warp-major order that spreads
+// consecutive items over the blocks: segment s < pose_seg of pose block row r (its blocks
+// 32 s .. 32 s + 31, a lane per block; the border columns with segment 0), then segment
+// s < border_seg of border row c (a contiguous 256-entry share of its pose and intrinsic
+// columns).  Item sums go to qpart: pose item (r, s) at 6 (r pose_seg + s), border item (c, s)
+// at 6 ncb pose_seg + c border_seg + s; q is their sum over s, formed in order where q is read.
+// Returns this thread's share of p.q = sum over items of p_i (item sum)_i.
 __device__ __forceinline__ double spmv_update(const PcgSystem<double>& sys, const double* __restrict__ z,
                                               double beta, const double* __restrict__ p_old,
-                                              double* __restrict__ p_new, double* __restrict__ q) {
+                                              double* __restrict__ p_new, double* __restrict__ qpart, int pose_seg,
+                                              int border_seg) {
     const int lane = threadIdx.x & 31;
-    // warp-major row order: consecutive rows go to different blocks (SMs)
+    // warp-major item order: consecutive items go to different blocks (SMs)
     const int gw = (threadIdx.x >> 5) * gridDim.x + blockIdx.x, nw = gridDim.x * kCgWarps;
-    const int nb = sys.nb, n6 = 6 * sys.ncb;
+    const int nb = sys.nb, n6 = 6 * sys.ncb, nrow = n6 + nb;
+    const int npose = sys.ncb * pose_seg;
     const bool first = beta == 0.0;
     auto pv = [&](int i) { return first ? z[i] : fma(beta, p_old[i], z[i]); };
     double pq = 0.0;
-    for (int r = gw; r < sys.ncb + nb; r += nw) {
-        if (r < sys.ncb) {
-            double acc[6] = {0, 0, 0, 0, 0, 0};
-            for (int e = sys.row_ptr[r] + lane; e < sys.row_ptr[r + 1]; e += 32) {
+    for (int t = gw; t < npose + nb * border_seg; t += nw) {
+        if (t < npose) {
+            const int r = t / pose_seg, sg = t - r * pose_seg;
+            const int e0 = sys.row_ptr[r] + 32 * sg, e1 = sys.row_ptr[r + 1];
+            double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            const int e = e0 + lane;
+            if (e < e1) {
                 const int j = sys.col_idx[e];
                 const double* A = sys.vals + static_cast<size_t>(e) * 36;
                 double pj[6];
@@ -523,38 +619,37 @@ __device__ __forceinline__ double spmv_update(const PcgSystem<double>& sys, cons
 #pragma unroll
                     for (int c = 0; c < 6; ++c) acc[a] = fma(A[a * 6 + c], pj[c], acc[a]);
             }
-            const double* Bi = sys.border + static_cast<size_t>(r) * 6 * nb;
-            for (int c = lane; c < nb; c += 32) {
-                const double pc = pv(n6 + c);
+            if (sg == 0) {
+                const double* Bi = sys.border + static_cast<size_t>(r) * 6 * nb;
+                for (int c = lane; c < nb; c += 32) {
+                    const double pc = pv(n6 + c);
 #pragma unroll
-                for (int a = 0; a < 6; ++a) acc[a] = fma(Bi[a * nb + c], pc, acc[a]);
+                    for (int a = 0; a < 6; ++a) acc[a] = fma(Bi[a * nb + c], pc, acc[a]);
+                }
             }
-#pragma unroll
-            for (int a = 0; a < 6; ++a) acc[a] = warp_sum(acc[a]);
-            if (lane < 6) {
-                double v = acc[0];
-#pragma unroll
-                for (int a = 1; a < 6; ++a)
-                    if (lane == a) v = acc[a];
-                const int i = 6 * r + lane;
+            const double v = warp_sum8(acc);
+            const int x = lane >> 2;
+            if ((lane & 3) == 0 && x < 6) {
+                const int i = 6 * r + x;
                 const double pi = pv(i);
-                q[i] = v;
-                p_new[i] = pi;
+                qpart[6 * t + x] = v;
+                if (sg == 0) p_new[i] = pi;
                 pq += pi * v;
             }
         } else {
-            const int c = r - sys.ncb;
-            double v = 0.0;
+            const int u = t - npose, c = u / border_seg, sg = u - c * border_seg;
+            const int k0 = min(nrow, 256 * sg), k1 = min(nrow, 256 * (sg + 1));
             const double* Bc = sys.border_t + static_cast<size_t>(c) * n6;
+            const double* Cc = sys.Cm + static_cast<size_t>(c) * nb;
+            double v = 0.0;
 #pragma unroll 4
-            for (int k = lane; k < n6; k += 32) v = fma(Bc[k], pv(k), v);
-            for (int d = lane; d < nb; d += 32) v = fma(sys.Cm[c * nb + d], pv(n6 + d), v);
+            for (int k = k0 + lane; k < k1; k += 32) v = fma(k < n6 ? Bc[k] : Cc[k - n6], pv(k), v);
             v = warp_sum(v);
             if (lane == 0) {
                 const int i = n6 + c;
                 const double pi = pv(i);
-                q[i] = v;
-                p_new[i] = pi;
+                qpart[6 * npose + u] = v;
+                if (sg == 0) p_new[i] = pi;
                 pq += pi * v;
             }
         }
@@ -564,18 +659,20 @@ __device__ __forceinline__ double spmv_update(const PcgSystem<double>& sys, cons
 
 // out: [0] iterations, [1] relative residual, [2] converged, [3] status (1: breakdown)
 template <typename T>
-__global__ void __launch_bounds__(kCgThreads) k_dense_cg(PcgSystem<double> sys, const T* __restrict__ X,
+__global__ void __launch_bounds__(kCgThreads, 2) k_dense_cg(PcgSystem<double> sys, const T* __restrict__ X,
                                                          const T* __restrict__ XT, int np,
                                                          const double* __restrict__ dscale,
                                                          const double* __restrict__ b, double* __restrict__ x,
                                                          double* __restrict__ r, double* __restrict__ z,
                                                          double* __restrict__ p, double* __restrict__ p2,
-                                                         double* __restrict__ q, T* __restrict__ u,
-                                                         T* __restrict__ w, double* __restrict__ part,
-                                                         double* __restrict__ out, double rel_tol, double abs_tol,
-                                                         int max_it) {
+                                                         double* __restrict__ qpart, int pose_seg, int border_seg,
+                                                         T* __restrict__ u, T* __restrict__ w,
+                                                         double* __restrict__ part, double* __restrict__ out,
+                                                         double rel_tol, double abs_tol, int max_it) {
     cgk::grid_group grid = cgk::this_grid();
-    __shared__ double s_red[kCgWarps + 1];
+    __shared__ double s_vals[kCgThreads];
+    __shared__ double s_q[12];
+    __shared__ double s_tot[kCgPart];
     const int n = 6 * sys.ncb + sys.nb;
     const int gt = blockIdx.x * blockDim.x + threadIdx.x, nt = gridDim.x * blockDim.x;
     double* mypart = part + static_cast<size_t>(blockIdx.x) * kCgPart;
@@ -587,14 +684,15 @@ __global__ void __launch_bounds__(kCgThreads) k_dense_cg(PcgSystem<double> sys, 
         u[i] = static_cast<T>(dscale[i] * b[i]);
         bb += b[i] * b[i];
     }
-    block_partial(bb, s_red, mypart + 0);
+    block_partial(bb, s_vals, s_q, mypart + 0);
     grid.sync();
     tri_rows<T, true>(X, np, n, u, w, nullptr, nullptr, nullptr);
     grid.sync();
-    block_partial(tri_rows<T, false>(XT, np, n, w, nullptr, z, dscale, b), s_red, mypart + 1);
+    block_partial(tri_rows<T, false>(XT, np, n, w, nullptr, z, dscale, b), s_vals, s_q, mypart + 1);
     grid.sync();
-    const double bnorm = sqrt(grid_total(part, 0, s_red));
-    double rz = grid_total(part, 1, s_red);
+    grid_totals<true>(part, 0, s_q, s_tot);
+    const double bnorm = sqrt(s_tot[0]);
+    double rz = s_tot[1];
     const double tol = fmax(rel_tol * bnorm, abs_tol);
     double rn = bnorm, beta = 0.0;
     int it = 0, status = 0;
@@ -602,32 +700,46 @@ __global__ void __launch_bounds__(kCgThreads) k_dense_cg(PcgSystem<double> sys, 
     double* p_old = p2;
     double* p_cur = p;
     while (!converged && it < max_it) {
-        // p = z + beta p, q = S p (the direction buffers alternate)
+        // p = z + beta p and the partial products of S p (the direction buffers alternate)
         {
             double* t = p_old;
             p_old = p_cur;
             p_cur = t;
         }
-        block_partial(spmv_update(sys, z, beta, p_old, p_cur, q), s_red, mypart + 2);
+        block_partial(spmv_update(sys, z, beta, p_old, p_cur, qpart, pose_seg, border_seg), s_vals, s_q, mypart + 2);
         grid.sync();
-        const double pq = grid_total(part, 2, s_red);
+        grid_totals<false>(part, 2, s_q, s_tot);
+        const double pq = s_tot[2];
         if (!(pq > 0.0) || !isfinite(pq) || !isfinite(rz)) {
             status = 1;
             break;
         }
         const double alpha = rz / pq;
         double rr = 0.0;
+        const int n6 = 6 * sys.ncb;
         for (int i = gt; i < n; i += nt) {
             x[i] = fma(alpha, p_cur[i], x[i]);
-            const double rv = fma(-alpha, q[i], r[i]);
+            // (S p)_i: the row's item sums in order
+            double qi;
+            if (i < n6) {
+                const double* qs = qpart + 6 * (i / 6) * pose_seg + i % 6;
+                qi = qs[0];
+                for (int sg = 1; sg < pose_seg; ++sg) qi += qs[6 * sg];
+            } else {
+                const double* qs = qpart + 6 * sys.ncb * pose_seg + (i - n6) * border_seg;
+                qi = qs[0];
+                for (int sg = 1; sg < border_seg; ++sg) qi += qs[sg];
+            }
+            const double rv = fma(-alpha, qi, r[i]);
             r[i] = rv;
             u[i] = static_cast<T>(dscale[i] * rv);
             rr += rv * rv;
         }
-        block_partial(rr, s_red, mypart + 0);
+        block_partial(rr, s_vals, s_q, mypart + 0);
         grid.sync();
         ++it;
-        rn = sqrt(grid_total(part, 0, s_red));
+        grid_totals<false>(part, 0, s_q, s_tot);
+        rn = sqrt(s_tot[0]);
         if (!isfinite(rn)) {
             status = 1;
             break;
@@ -636,12 +748,12 @@ __global__ void __launch_bounds__(kCgThreads) k_dense_cg(PcgSystem<double> sys, 
             converged = true;
             break;
         }
-        // z = D X^T X D r
         tri_rows<T, true>(X, np, n, u, w, nullptr, nullptr, nullptr);
         grid.sync();
-        block_partial(tri_rows<T, false>(XT, np, n, w, nullptr, z, dscale, r), s_red, mypart + 1);
+        block_partial(tri_rows<T, false>(XT, np, n, w, nullptr, z, dscale, r), s_vals, s_q, mypart + 1);
         grid.sync();
-        const double rz_new = grid_total(part, 1, s_red);
+        grid_totals<false>(part, 1, s_q, s_tot);
+        const double rz_new = s_tot[1];
         beta = rz_new / rz;
         rz = rz_new;
     }
@@ -735,8 +847,9 @@ int dense_pcg(const PcgSystem<double>& sys, DenseWork<T>& W, const double* b, do
     const double* dscale = W.dscale;
     double rt = rel_tol, at = abs_tol;
     int mi = max_it;
-    void* args[] = {&s, &X, &XT, &np, &dscale, &b, &W.x, &W.r, &W.z, &W.p, &W.w, &W.q, &W.ut, &W.wt, &W.part,
-                    &W.scal, &rt, &at, &mi};
+    int ps = W.pose_seg, bs = W.border_seg;
+    void* args[] = {&s, &X, &XT, &np, &dscale, &b, &W.x, &W.r, &W.z, &W.p, &W.w, &W.qpart, &ps, &bs, &W.ut, &W.wt,
+                    &W.part, &W.scal, &rt, &at, &mi};
     const cudaError_t e = cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(&k_dense_cg<T>), dim3(grid),
                                                       dim3(kCgThreads), args, 0, st);
     if (e != cudaSuccess) return -1;

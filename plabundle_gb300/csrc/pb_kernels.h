@@ -130,6 +130,10 @@ struct DenseWork {
     double* dscale = nullptr;
     int* status = nullptr;
     double *x = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr, *w = nullptr;
+    // SpMV work items of the CG: pose_seg per pose block row (32 blocks each), border_seg per border
+    // row (256 entries each); qpart holds their sums (6 ncb pose_seg + nb border_seg doubles)
+    int pose_seg = 0, border_seg = 0;
+    double* qpart = nullptr;
     T *ut = nullptr, *wt = nullptr;  // scaled residual and X D r in the factor's type
     double* part = nullptr;  // per-block partials of the cooperative CG (grid * 4)
     double* scal = nullptr;

@@ -264,6 +264,10 @@ void ensure_dense(SchurWork* w, int device) {
     W.z = w->dense.alloc<double>(W.n);
     W.p = w->dense.alloc<double>(W.n);
     W.q = w->dense.alloc<double>(W.n);
+    // SpMV work items of the CG: every row is a border row here, 256 entries per item
+    W.pose_seg = 0;
+    W.border_seg = (W.n + 255) / 256;
+    W.qpart = w->dense.alloc<double>(static_cast<size_t>(W.n) * W.border_seg);
     W.w = w->dense.alloc<double>(W.n);
     W.ut = w->dense.alloc<T>(W.np);
     W.wt = w->dense.alloc<T>(W.np);

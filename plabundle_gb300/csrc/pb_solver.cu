@@ -528,6 +528,16 @@ void ensure_dense(pb_gpu_ctx* c) {
     W.z = A.alloc<double>(W.n);
     W.p = A.alloc<double>(W.n);
     W.q = A.alloc<double>(W.n);
+    {
+        // SpMV work items of the CG: 32 pose blocks per item (the longest block row sets the
+        // items per row), 256 entries of a border row per item
+        int longest = 0;
+        for (int r = 0; r < S.ncb; ++r) longest = std::max(longest, c->model.row_ptr[r + 1] - c->model.row_ptr[r]);
+        W.pose_seg = S.ncb > 0 ? std::max(1, (longest + 31) / 32) : 0;
+        W.border_seg = S.nb > 0 ? (S.n + 255) / 256 : 0;
+        W.qpart = A.alloc<double>(std::max<size_t>(1, 6 * static_cast<size_t>(S.ncb) * W.pose_seg +
+                                                          static_cast<size_t>(S.nb) * W.border_seg));
+    }
     W.w = A.alloc<double>(W.n);
     W.ut = A.alloc<T>(W.np);
     W.wt = A.alloc<T>(W.np);
