@@ -99,6 +99,15 @@ typedef struct pb_problem_desc {
     int32_t n_control_points;
     const int32_t* control_point_track;
     const double* control_point_data;
+    /* Scale-bar constraints (Problem::scaleBarConstraints, ScaleBarConstraint,
+     * include/plabundle/constraints.h:93-101): n_scale_bars entries; scale_bar_tracks[2 * i] and
+     * [2 * i + 1] the two track indices; scale_bar_data[3 * i]: measuredDistanceMeters,
+     * sigmaMeters, weight.  Their tracks become primary point blocks (prepareActiveProblem,
+     * BundleAdjustPlaMatrixProblem.cpp:235-266) and the problem is solved on the general path.
+     * May be 0 / NULL. */
+    int32_t n_scale_bars;
+    const int32_t* scale_bar_tracks;
+    const double* scale_bar_data;
 } pb_problem_desc;
 
 /* SolveOptions (include/plabundle/options.h:58-187) as flat fields. */
@@ -137,7 +146,11 @@ typedef struct pb_solve_options {
                                         * = false): undamped equations per linearisation, damped Schur
                                         * solve to 1e-12, finite-difference directional decrease, retry
                                         * with ten times the damping at the same state; 0: the online
-                                        * reference path */
+                                        * reference path (a problem with scale bars always takes the
+                                        * general path, as canUseReferenceOnlineSchur decides,
+                                        * BundleAdjustPlaMatrixReferenceSchur.cpp:667-673) */
+    double scale_bar_weight;           /* ConstraintOptions::scaleBarWeight (1) */
+    double scale_bar_huber_delta;      /* ConstraintOptions::scaleBarHuberDeltaMeters (0.2) */
 } pb_solve_options;
 
 /* PlaMatrixDiagnostics (include/plabundle/result.h:91-128) + QualitySummary fields. */
@@ -171,6 +184,8 @@ typedef struct pb_solve_report {
     double back_substitution_ms;
     double objective_ms;
     double total_ms;
+    int32_t promoted_point_blocks;     /* tracks of scale bars solved as primary point blocks */
+    int32_t general_path_used;         /* 1 when the solve ran on the general path */
 } pb_solve_report;
 
 /* Context lifetime (SolverWorkspace construction / clear()). */

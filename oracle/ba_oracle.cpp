@@ -271,7 +271,9 @@ struct Group {
 struct Active {
     std::vector<char> activeTrack;
     std::vector<int> cameraBlock, intrinsicBlockByCamera, calibGroupByCamera, trackBlock;
+    std::vector<int> trackPrimaryBlock;  // scale-bar tracks promoted to primary point blocks, else -1
     int primaryBlockCount = 0, cameraBlockCount = 0, intrinsicBlockCount = 0, trackBlockCount = 0;
+    int promotedTrackBlockCount = 0;
     int activeTrackCount = 0, observationCount = 0, rejectedInitialTracks = 0;
 };
 
@@ -326,13 +328,19 @@ struct Oracle {
     std::vector<std::vector<ControlPoint>> controlPoints;
     std::vector<std::array<double, 3>> gaugeTargets;  // valid targets of tracks with usable observations
     bool hasControlPoints = false;
+    // scale bars: tracks, measured distance and residual scale sqrt(weight) / sigma
+    struct ScaleBar {
+        int a, b;
+        double length, scale, weight;
+    };
+    std::vector<ScaleBar> scaleBars;
 
     // block normal equations of the general path (orc_general_build)
     std::shared_ptr<GeneralEquations> general;
 
     size_t nt() const { return offs.size() - 1; }
     // useReferencePointParameterization (BundleAdjustPlaMatrixAssembly.cpp:24-30)
-    bool refParam() const { return !hasControlPoints; }
+    bool refParam() const { return !hasControlPoints && scaleBars.empty(); }
 };
 
 bool isCameraFixed(const Oracle& o, int cam) {
@@ -417,6 +425,42 @@ bool controlPointWhitening(const double* rec, double W[9]) {
 // skips one whose weight controlPointWeight * weight is not positive.  The gauge targets are the
 // valid constraints of tracks seen by two distinct cameras (BundleAdjustValidation.cpp:94-106,
 // :147-236).
+// Scale bars: validateProblem (problem.cpp:342-355) rejects an invalid bar; linearizeScaleBar
+// (BundleAdjustPlaMatrixConstraints.cpp:118-153) uses weight = scaleBarWeight * weight and the
+// residual scale sqrt(weight) / max(1e-9, sigma).
+int loadScaleBars(Oracle& o, const orc_problem* pr) {
+    o.scaleBars.clear();
+    if (pr->n_scale_bars <= 0) return 0;
+    if (!pr->scale_bar_tracks || !pr->scale_bar_data) return InvalidInput;
+    if (!std::isfinite(o.opt.scale_bar_weight) || !(o.opt.scale_bar_weight > 0.0) ||
+        !std::isfinite(o.opt.scale_bar_huber_delta) || o.opt.scale_bar_huber_delta < 0.0)
+        return InvalidInput;
+    const int nt = static_cast<int>(o.nt());
+    for (int i = 0; i < pr->n_scale_bars; ++i) {
+        const int a = pr->scale_bar_tracks[2 * i], b = pr->scale_bar_tracks[2 * i + 1];
+        const double* d = pr->scale_bar_data + static_cast<size_t>(i) * 3;
+        if (a < 0 || b < 0 || a == b || a >= nt || b >= nt || !std::isfinite(d[0]) || !(d[0] > 0.0) ||
+            !std::isfinite(d[1]) || !(d[1] > 0.0) || !std::isfinite(d[2]) || !(d[2] > 0.0))
+            return InvalidInput;
+        const double w = o.opt.scale_bar_weight * d[2];
+        o.scaleBars.push_back({a, b, d[0], std::sqrt(w) / std::max(1e-9, d[1]), w});
+    }
+    return 0;
+}
+
+// linearizeScaleBar with finishRobust's Huber loss: r = s (|Xa - Xb| - L), dr/dXa = s (Xa - Xb) /
+// |Xa - Xb| = -dr/dXb; false when the points coincide.
+bool scaleBarResidual(const Oracle& o, const Oracle::ScaleBar& sb, const double* Xa, const double* Xb, double* r,
+                      double J[3], RobustEval* rb) {
+    const double d[3] = {Xa[0] - Xb[0], Xa[1] - Xb[1], Xa[2] - Xb[2]};
+    const double dist = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    if (!(dist > 1e-12)) return false;
+    *r = sb.scale * (dist - sb.length);
+    for (int a = 0; a < 3; ++a) J[a] = sb.scale * d[a] / dist;
+    if (!robustLoss((*r) * (*r), 1, o.opt.scale_bar_huber_delta, rb)) return false;
+    return std::isfinite(rb->cost) && std::isfinite(rb->weight);
+}
+
 int loadControlPoints(Oracle& o, const orc_problem* pr) {
     o.controlPoints.assign(o.nt(), {});
     o.gaugeTargets.clear();
@@ -519,7 +563,8 @@ int normalizeGauge(Oracle& o) {
     if (!opt.refine_camera_pose || opt.gauge_policy == 2 || o.inputCams.empty()) return 0;
     std::vector<int> fixedSet = sorted;
     const bool absolutePose = completeControlPointGauge(o);
-    bool absoluteScale = absolutePose || controlPointBaseline(o, fixedSet);
+    // hasUsableScaleBar (BundleAdjustValidation.cpp:242-259): every loaded bar is usable
+    bool absoluteScale = absolutePose || !o.scaleBars.empty() || controlPointBaseline(o, fixedSet);
     if (opt.gauge_policy == 1)
         return (absolutePose && absoluteScale) || fixedSet.size() >= 2 || (fixedSet.size() == 1 && absoluteScale)
                    ? 0
@@ -618,9 +663,21 @@ void prepareActive(Oracle& o) {
         for (size_t c = 0; c < nc; ++c) a.intrinsicBlockByCamera[c] = a.primaryBlockCount + a.calibGroupByCamera[c];
         a.primaryBlockCount += a.intrinsicBlockCount;
     }
+    // scale-bar tracks become primary point blocks (BundleAdjustPlaMatrixProblem.cpp:235-266)
+    std::vector<char> promote(nt, 0);
+    for (const auto& sb : o.scaleBars)
+        for (int t : {sb.a, sb.b})
+            if (a.activeTrack[t] && !isTrackFixed(o, t)) promote[t] = 1;
+    a.trackPrimaryBlock.assign(nt, -1);
+    a.promotedTrackBlockCount = 0;
     for (size_t t = 0; t < nt; ++t) {
         if (!a.activeTrack[t] || isTrackFixed(o, static_cast<int>(t))) continue;
-        a.trackBlock[t] = a.trackBlockCount++;
+        if (promote[t]) {
+            a.trackPrimaryBlock[t] = a.primaryBlockCount++;
+            ++a.promotedTrackBlockCount;
+        } else {
+            a.trackBlock[t] = a.trackBlockCount++;
+        }
     }
 }
 
@@ -1397,6 +1454,11 @@ void stepRms(const Oracle& o, const std::vector<double>& ps, const std::vector<d
             }
     }
     for (size_t t = 0; t < o.nt(); ++t) {
+        const int pb = o.active.trackPrimaryBlock.empty() ? -1 : o.active.trackPrimaryBlock[t];
+        if (pb >= 0) {
+            for (int i = 0; i < 3; ++i) ss += ps[static_cast<size_t>(pb) * kP + i] * ps[static_cast<size_t>(pb) * kP + i];
+            sd += 3;
+        }
         const int eb = o.active.trackBlock[t];
         if (eb < 0) continue;
         for (int i = 0; i < 3; ++i) ss += es[eb * 3 + i] * es[eb * 3 + i];
@@ -1515,6 +1577,12 @@ State applyStep(const Oracle& o, const State& s, const std::vector<double>& ps, 
             if (gr.enabled[p]) gr.params[p] = std::clamp(gr.params[p] + alpha * ps[off + p], gr.lower[p], gr.upper[p]);
     }
     for (size_t t = 0; t < n.points.size(); ++t) {
+        const int pb = o.active.trackPrimaryBlock.empty() ? -1 : o.active.trackPrimaryBlock[t];
+        if (pb >= 0) {
+            // a promoted point: the primary step (the plain parameterisation)
+            for (int a = 0; a < 3; ++a) n.points[t][a] += alpha * ps[static_cast<size_t>(pb) * kP + a];
+            continue;
+        }
         const int eb = o.active.trackBlock[t];
         if (eb < 0) continue;
         const double sc = ref ? referencePointScale(s.points[t].data()) : 1.0;
@@ -1567,7 +1635,15 @@ double objective(const Oracle& o, const State& s) {
         if (bad[th]) return kInf;
         cost += part[th];
     }
-    return cost + priorCost(o, s);
+    cost += priorCost(o, s);
+    // assembleScaleBars (BundleAdjustPlaMatrixAssemblySurvey.cpp:131-186): bars of active tracks
+    for (const auto& sb : o.scaleBars) {
+        if (!o.active.activeTrack[sb.a] || !o.active.activeTrack[sb.b]) continue;
+        double r, J[3];
+        RobustEval rb;
+        if (scaleBarResidual(o, sb, s.points[sb.a].data(), s.points[sb.b].data(), &r, J, &rb)) cost += rb.cost;
+    }
+    return cost;
 }
 
 // strictTrackRms (BundleAdjustQuality.cpp:302-364).
@@ -1709,6 +1785,7 @@ double buildGeneral(Oracle& o, GeneralEquations& q) {
     for (size_t t = 0; t < o.nt(); ++t) {
         if (!o.active.activeTrack[t]) continue;
         const int elim = o.active.trackBlock[t];
+        const int prim = o.active.trackPrimaryBlock[t];
         for (int64_t k = o.offs[t]; k < o.offs[t + 1]; ++k) {
             const Obs& ob = o.obs[k];
             if (!obsUsable(ob, o.state.cams.size())) continue;
@@ -1719,16 +1796,60 @@ double buildGeneral(Oracle& o, GeneralEquations& q) {
                 throw InvalidProjection("linearisation produced an invalid projection");
             cost += L.cost;
             const Terms tm = primaryTerms(o, o.state, ob.cam, L);
-            const double* jp[2] = {tm.J[0], tm.J[1]};
-            q.addResidualBlocks(tm.blocks, jp, tm.count, elim, L.Jp, L.r, 2, L.nw);
+            int blocks[3] = {tm.blocks[0], tm.blocks[1], -1};
+            const double* jp[3] = {tm.J[0], tm.J[1], nullptr};
+            int count = tm.count;
+            double Jpp[2 * kP] = {0};
+            if (prim >= 0) {
+                // addObservation's point primary term: the point Jacobian padded to 13 columns
+                for (int k = 0; k < 2; ++k)
+                    for (int c = 0; c < 3; ++c) Jpp[k * kP + c] = L.Jp[k * kE + c];
+                blocks[count] = prim;
+                jp[count++] = Jpp;
+            }
+            q.addResidualBlocks(blocks, jp, count, elim, L.Jp, L.r, 2, L.nw);
         }
         for (const auto& cp : o.controlPoints[t]) {
             double r[3];
             RobustEval rb;
             if (!controlPointResidual(o, cp, o.state.points[t].data(), r, &rb)) continue;
             cost += rb.cost;
-            if (elim >= 0) q.addResidualBlocks(nullptr, nullptr, 0, elim, cp.J, r, 3, rb.weight);
+            if (elim >= 0) {
+                q.addResidualBlocks(nullptr, nullptr, 0, elim, cp.J, r, 3, rb.weight);
+            } else if (prim >= 0) {
+                // addPointResidual on a primary point block (BundleAdjustPlaMatrixAssembly.cpp:356-380)
+                double Jc[3 * kP] = {0};
+                for (int k = 0; k < 3; ++k)
+                    for (int c = 0; c < 3; ++c) Jc[k * kP + c] = cp.J[k * 3 + c];
+                const double* jc[1] = {Jc};
+                q.addResidualBlocks(&prim, jc, 1, -1, nullptr, r, 3, rb.weight);
+            }
         }
+    }
+    // assembleScaleBars (BundleAdjustPlaMatrixAssemblySurvey.cpp:131-186)
+    for (const auto& sb : o.scaleBars) {
+        if (!o.active.activeTrack[sb.a] || !o.active.activeTrack[sb.b]) continue;
+        double r, J[3];
+        RobustEval rb;
+        if (!scaleBarResidual(o, sb, o.state.points[sb.a].data(), o.state.points[sb.b].data(), &r, J, &rb)) continue;
+        cost += rb.cost;
+        double Ja[kP] = {0}, Jb[kP] = {0};
+        for (int c = 0; c < 3; ++c) {
+            Ja[c] = J[c];
+            Jb[c] = -J[c];
+        }
+        int blocks[2];
+        const double* jp[2];
+        int count = 0;
+        if (o.active.trackPrimaryBlock[sb.a] >= 0) {
+            blocks[count] = o.active.trackPrimaryBlock[sb.a];
+            jp[count++] = Ja;
+        }
+        if (o.active.trackPrimaryBlock[sb.b] >= 0) {
+            blocks[count] = o.active.trackPrimaryBlock[sb.b];
+            jp[count++] = Jb;
+        }
+        if (count > 0) q.addResidualBlocks(blocks, jp, count, -1, nullptr, &r, 1, rb.weight);
     }
     for (size_t g = 0; g < o.state.groups.size(); ++g) {
         const Group& gr = o.state.groups[g];
@@ -1988,6 +2109,9 @@ void* orc_create(const orc_problem* pr, const orc_options* op, int32_t* status) 
     int st = 0;
     if (o->inputCams.empty() || o->nt() == 0) st = InvalidInput;
     if (!st) st = loadControlPoints(*o, pr);
+    if (!st) st = loadScaleBars(*o, pr);
+    // a problem with scale bars has no online path (canUseReferenceOnlineSchur)
+    if (!st && !o->scaleBars.empty()) o->opt.general_path = 1;
     if (!st) st = normalizeGauge(*o);
     if (!st) {
         prepareActive(*o);

@@ -56,6 +56,12 @@ typedef struct orc_problem {
     int32_t n_control_points;
     const int32_t* control_point_track;
     const double* control_point_data;
+    /* scale bars (Problem::scaleBarConstraints): two track indices and (measuredDistanceMeters,
+     * sigmaMeters, weight) each; their active, non-fixed tracks become primary point blocks and
+     * the problem is solved on the general path */
+    int32_t n_scale_bars;
+    const int32_t* scale_bar_tracks;
+    const double* scale_bar_data;
 } orc_problem;
 
 typedef struct orc_options {
@@ -90,6 +96,8 @@ typedef struct orc_options {
      * residual sits at the FP64 floor, where 1 rejects the step and ends the solve on a damped
      * step. */
     int32_t residual_gate;
+    double scale_bar_weight;        /* ConstraintOptions::scaleBarWeight */
+    double scale_bar_huber_delta;   /* ConstraintOptions::scaleBarHuberDeltaMeters */
 } orc_options;
 
 typedef struct orc_report {

@@ -27,7 +27,8 @@ class OrcProblem(C.Structure):
                 ("fixed_cameras", C.c_void_p), ("n_fixed_tracks", C.c_int32), ("fixed_tracks", C.c_void_p),
                 ("calibration_group_ids", C.c_void_p), ("intrinsic_reference_cameras", C.c_void_p),
                 ("n_control_points", C.c_int32), ("control_point_track", C.c_void_p),
-                ("control_point_data", C.c_void_p)]
+                ("control_point_data", C.c_void_p), ("n_scale_bars", C.c_int32), ("scale_bar_tracks", C.c_void_p),
+                ("scale_bar_data", C.c_void_p)]
 
 
 class OrcOptions(C.Structure):
@@ -42,7 +43,8 @@ class OrcOptions(C.Structure):
                 ("linear_relative_tolerance", C.c_double), ("linear_absolute_tolerance", C.c_double),
                 ("calibration", C.c_double * 32), ("control_point_weight", C.c_double),
                 ("control_point_huber_delta", C.c_double), ("general_path", C.c_int32),
-                ("residual_gate", C.c_int32)]
+                ("residual_gate", C.c_int32), ("scale_bar_weight", C.c_double),
+                ("scale_bar_huber_delta", C.c_double)]
 
 
 class OrcReport(C.Structure):
@@ -124,6 +126,8 @@ def make_options(options, num_threads: int = 0, linear_solver: int = 0, residual
         o.calibration[i] = v
     o.control_point_weight = options.constraints.controlPointWeight
     o.control_point_huber_delta = options.constraints.controlPointHuberDeltaMeters
+    o.scale_bar_weight = getattr(options.constraints, "scaleBarWeight", 1.0)
+    o.scale_bar_huber_delta = getattr(options.constraints, "scaleBarHuberDeltaMeters", 0.2)
     return o
 
 
@@ -133,6 +137,16 @@ def control_point_whitening(record):
     W = np.zeros(9)
     ok = lib().orc_control_point_whitening(rec.ctypes.data, W.ctypes.data)
     return bool(ok), W.reshape(3, 3)
+
+
+def scale_bars(problem):
+    """(tracks int32 [n, 2], records float64 [n, 3]: distance, sigma, weight) of the problem's
+    scale bars."""
+    bars = getattr(problem, "scaleBarConstraints", None) or []
+    tracks = np.ascontiguousarray(np.array([(b.trackIndexA, b.trackIndexB) for b in bars], np.int32).reshape(-1, 2))
+    data = np.ascontiguousarray(np.array([(b.measuredDistanceMeters, b.sigmaMeters, b.weight) for b in bars],
+                                         np.float64).reshape(-1, 3))
+    return tracks, data
 
 
 def control_points(problem):
@@ -153,12 +167,16 @@ class Oracle:
         fixed_c = np.ascontiguousarray(p.fixedCameraIndices, np.int32)
         fixed_t = np.ascontiguousarray(p.fixedTrackIndices, np.int32)
         cp_t, cp_d = control_points(p)
-        self._keep += [fixed_c, fixed_t, p.cameraCalibrationGroupIds, p.sharedIntrinsicReferenceCameras, cp_t, cp_d]
+        sb_t, sb_d = scale_bars(p)
+        self._keep += [fixed_c, fixed_t, p.cameraCalibrationGroupIds, p.sharedIntrinsicReferenceCameras, cp_t, cp_d,
+                       sb_t, sb_d]
         self.desc = OrcProblem(p.n_cameras, _ptr(p.cameras), p.n_tracks, _ptr(p.track_offsets), _ptr(p.points),
                                p.n_obs, _ptr(p.obs_camera), _ptr(p.obs_u), _ptr(p.obs_v), _ptr(p.obs_weight),
                                _ptr(p.obs_scale), fixed_c.size, _ptr(fixed_c), fixed_t.size, _ptr(fixed_t),
                                _ptr(p.cameraCalibrationGroupIds), _ptr(p.sharedIntrinsicReferenceCameras),
-                               cp_t.size, _ptr(cp_t) if cp_t.size else None, _ptr(cp_d) if cp_t.size else None)
+                               cp_t.size, _ptr(cp_t) if cp_t.size else None, _ptr(cp_d) if cp_t.size else None,
+                               sb_d.shape[0], _ptr(sb_t) if sb_d.shape[0] else None,
+                               _ptr(sb_d) if sb_d.shape[0] else None)
         self.opts = make_options(options, num_threads, linear_solver, residual_gate)
         g = p.gauge
         self.opts.gauge_policy = int(g.policy)

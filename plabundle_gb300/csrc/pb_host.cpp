@@ -280,6 +280,41 @@ int build_host_model(const pb_problem_desc* pr, const pb_solve_options* op, Host
             m->cp_rec.insert(m->cp_rec.end(), d, d + 3);
         }
     }
+    // --- scale bars (Problem::scaleBarConstraints): validateProblem rejects an invalid bar
+    // (problem.cpp:342-355); any bar gives the problem an absolute scale (hasUsableScaleBar,
+    // BundleAdjustValidation.cpp:242-259), switches to the plain parameterisation and to the
+    // general path (useReferencePointParameterization, BundleAdjustPlaMatrixAssembly.cpp:24-30;
+    // canUseReferenceOnlineSchur, BundleAdjustPlaMatrixReferenceSchur.cpp:667-673)
+    m->bar_tracks.clear();
+    m->bar_data.clear();
+    m->bar_weight = op->scale_bar_weight;
+    m->bar_huber = op->scale_bar_huber_delta;
+    m->force_general = false;
+    if (pr->n_scale_bars < 0) { *err = "scale-bar count must be non-negative"; return PB_SOLVE_INVALID_INPUT; }
+    if (pr->n_scale_bars > 0) {
+        if (!pr->scale_bar_tracks || !pr->scale_bar_data) { *err = "scale-bar arrays missing"; return PB_SOLVE_INVALID_INPUT; }
+        if (!std::isfinite(op->scale_bar_weight) || !(op->scale_bar_weight > 0.0) ||
+            !std::isfinite(op->scale_bar_huber_delta) || op->scale_bar_huber_delta < 0.0) {
+            *err = "scale-bar weight must be finite and positive and its Huber delta finite and non-negative";
+            return PB_SOLVE_INVALID_INPUT;
+        }
+        for (int i = 0; i < pr->n_scale_bars; ++i) {
+            const int a = pr->scale_bar_tracks[2 * i], b = pr->scale_bar_tracks[2 * i + 1];
+            const double* d = pr->scale_bar_data + static_cast<size_t>(i) * 3;
+            if (a < 0 || b < 0 || a == b || a >= m->nt || b >= m->nt || !std::isfinite(d[0]) || !(d[0] > 0.0) ||
+                !std::isfinite(d[1]) || !(d[1] > 0.0) || !std::isfinite(d[2]) || !(d[2] > 0.0)) {
+                *err = "problem contains an invalid scale-bar constraint";
+                return PB_SOLVE_INVALID_INPUT;
+            }
+            m->bar_tracks.push_back(a);
+            m->bar_tracks.push_back(b);
+            m->bar_data.insert(m->bar_data.end(), d, d + 3);
+        }
+        m->ref_param = false;
+        m->force_general = true;
+    }
+    const bool bar_scale = !m->bar_tracks.empty();
+
     // hasCompleteControlPointGauge (BundleAdjustValidation.cpp:181-236): three non-collinear targets
     bool cp_complete = false;
     {
@@ -338,7 +373,7 @@ int build_host_model(const pb_problem_desc* pr, const pb_solve_options* op, Host
         if (op->refine_camera_pose && op->gauge_policy != 2) {
             // absolute pose and scale from three non-collinear control points; scale alone from
             // a control point away from a fixed camera (:826-835)
-            bool abs_scale = cp_complete || cp_baseline_to(fc);
+            bool abs_scale = cp_complete || bar_scale || cp_baseline_to(fc);
             if (op->gauge_policy == 1) {
                 const bool complete = (cp_complete && abs_scale) || fc.size() >= 2 || (fc.size() == 1 && abs_scale);
                 if (!complete) { *err = "incomplete gauge: two fixed cameras, or a fixed camera and an absolute scale, are required"; return PB_SOLVE_UNSUPPORTED; }
@@ -461,9 +496,27 @@ int build_host_model(const pb_problem_desc* pr, const pb_solve_options* op, Host
             if ((op->intrinsic_mask >> p) & 1u) m->int_cols[m->ni++] = p;
         if (m->ng > kMaxGroups) { *err = "more calibration groups than the dense intrinsic border holds (4)"; return PB_SOLVE_UNSUPPORTED; }
     }
+    // the active, non-fixed tracks of scale bars become primary point blocks, numbered after the
+    // intrinsic groups in track order; the others are eliminated
+    std::vector<char> promote(nt, 0);
+    for (size_t i = 0; i < m->bar_tracks.size(); ++i) {
+        const int t = m->bar_tracks[i];
+        if (m->active_track[t] && !fixed_trk[t]) promote[t] = 1;
+    }
     m->ntb = 0;
-    for (int t = 0; t < nt; ++t)
-        if (m->active_track[t] && !fixed_trk[t]) m->track_block[t] = m->ntb++;
+    m->npr = 0;
+    m->prom_track.clear();
+    m->track_prom.assign(nt, -1);
+    for (int t = 0; t < nt; ++t) {
+        if (!m->active_track[t] || fixed_trk[t]) continue;
+        if (promote[t]) {
+            m->track_prom[t] = m->npr++;
+            m->prom_track.push_back(t);
+        } else {
+            m->track_block[t] = m->ntb++;
+        }
+    }
+    m->P += m->npr;
 
     // --- intrinsic groups (initializeIntrinsicGroups, BundleAdjustPlaMatrixModel.cpp:84-231)
     m->groups.assign(m->ng, HostGroup{});

@@ -44,6 +44,9 @@ struct Shape {
     int ref_param;
     int ncp;             // control-point constraints of processed tracks
     double cp_huber;     // Huber delta of the control-point residuals (m)
+    int npr;             // tracks promoted to primary point blocks (scale bars)
+    int nbar;            // scale bars
+    double bar_huber;    // Huber delta of the scale-bar residuals (m)
     float loss_scale_hi, loss_scale_lo;  // loss_scale as float-float (mixed-path linearisation)
 };
 
@@ -72,6 +75,11 @@ struct DevPtrs {
     // tracks (processing order)
     int* trk_obs_begin;   // ntp + 1
     int* trk_block;       // ntp
+    int* trk_free;        // ntp: 1 when the point moves (eliminated or promoted), else 0
+    int* trk_prom;        // ntp: promoted index (scale bars), or -1
+    int* prom_proc;       // npr: processing index of each promoted track
+    int* bar_pidx;        // 2 per scale bar: processing indices of its tracks, -1 when not processed
+    double* bar_par;      // 2 per scale bar: measured distance, residual scale sqrt(weight) / sigma
     int* trk_orig;        // ntp
     double* points;       // ntp * 3
     double* points0;      // ntp * 3
@@ -165,6 +173,16 @@ struct HostModel {
     std::vector<double> cp_proc;    // 12 per constraint of a processed track, processing order
     double cp_huber = 0.2;
     bool ref_param = true;
+    // scale bars (Problem::scaleBarConstraints): two original track indices and (distance, sigma,
+    // weight) per bar; the active, non-fixed tracks of the bars become primary point blocks,
+    // promoted index k in track order (prepareActiveProblem, BundleAdjustPlaMatrixProblem.cpp:235-266)
+    std::vector<int> bar_tracks;
+    std::vector<double> bar_data;
+    double bar_weight = 1.0, bar_huber = 0.2;
+    std::vector<int> prom_track;  // promoted index -> original track
+    std::vector<int> track_prom;  // original track -> promoted index, or -1
+    int npr = 0;
+    bool force_general = false;   // scale bars: the online path is not available
     int gauge_anchor = -1, gauge_scale = -1;
     double gauge_baseline = 0.0;
     int loss = 0;

@@ -363,7 +363,7 @@ __global__ void __launch_bounds__(256) k_cost_batch(Shape S, DevPtrs D, const do
         const int cam = D.obs_cam[o], trk = D.obs_trk[o];
         const double* X = D.points + static_cast<size_t>(trk) * 3;
         const double u = D.obs_u[o], v = D.obs_v[o], w = D.obs_w[o];
-        const bool moves = use_trial && D.trk_block[trk] >= 0;
+        const bool moves = use_trial && D.trk_free[trk];
         const double s = moves ? D.pscale[trk] : 0.0;
         const double* dp = moves ? step_p + static_cast<size_t>(trk) * 3 : nullptr;
         for (int a = 0; a < n_alpha; ++a) {
@@ -593,7 +593,7 @@ __global__ void k_accept(Shape S, DevPtrs D, const double* __restrict__ step_p, 
                         D.gauge_basis + 6, D.gauge_basis);
     }
     if (i < S.ng * kGroupRec) D.groups[i] = D.groups_trial[static_cast<size_t>(a) * S.ng * kGroupRec + i];
-    if (i < S.ntp && D.trk_block[i] >= 0) {
+    if (i < S.ntp && D.trk_free[i]) {
         double* X = D.points + static_cast<size_t>(i) * 3;
         const double f = D.pscale[i] * alpha;
         X[0] += f * step_p[static_cast<size_t>(i) * 3 + 0];

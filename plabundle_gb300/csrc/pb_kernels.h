@@ -51,6 +51,16 @@ struct RedOut {
     double* result;
 };
 
+// Reduced system extended by the primary point blocks of scale-bar tracks (pb_survey.cu): border
+// columns and Cm rows nb .. nb + 3 npr - 1 hold the promoted points.
+struct ExtSys {
+    double* border;    // 6 ncb x nbx
+    double* border_t;  // nbx x 6 ncb
+    double* Cm;        // nbx x nbx
+    double* rhs;       // nx
+    int nbx, nx;       // nb + 3 npr, n + 3 npr
+};
+
 template <typename T>
 void launch_assemble(const Shape& S, const DevPtrs& D, const AsmOut& O, double damping, size_t smem, cudaStream_t st);
 template <typename T>
@@ -75,6 +85,16 @@ void launch_effective(const Shape& S, const DevPtrs& D, cudaStream_t st);
 void launch_cost(const Shape& S, const DevPtrs& D, const double* step_c, const double* step_p, const double* alphas,
                  int n_alpha, int use_trial, double* part, double* out, cudaStream_t st);
 void launch_accept(const Shape& S, const DevPtrs& D, const double* step_p, double alpha, int a, cudaStream_t st);
+// Scale bars (pb_survey.cu): the extended system of the current state (`flags` bit 2: a promoted
+// observation did not project; `bar_cost`: the bars' robust cost), the split of its solution into
+// the camera / intrinsic step and the promoted point steps (`out`: their squared sum), and the
+// bars' cost of the trial states or of the current state.
+void launch_extend_system(const Shape& S, const DevPtrs& D, const RedOut<double>& R, const ExtSys& X, double damping,
+                          int* flags, double* bar_cost, cudaStream_t st);
+void launch_ext_step(const Shape& S, const DevPtrs& D, const double* xsol, double* step_c, double* step_p, double* out,
+                     cudaStream_t st);
+void launch_bar_cost(const Shape& S, const DevPtrs& D, const double* step_p, const double* alphas, int n_alpha,
+                     int use_trial, double* out, cudaStream_t st);
 void launch_strict_rms(const Shape& S, const DevPtrs& D, const double* cams, const double* init_points,
                        const int* proc_of_track, int use_state, int nt, double* out, cudaStream_t st);
 // Quality finalisation on the device (finalizeBundleAdjustResult): out[0] filter threshold,

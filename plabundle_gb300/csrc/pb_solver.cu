@@ -176,6 +176,12 @@ struct pb_gpu_ctx {
     std::vector<long long> proc_of_obs;  // original observation -> processing index (-1: not processed)
     // damped Schur solves of host block normal equations (pb_gpu_solve_damped_schur)
     SchurWork* schur = nullptr;
+    // scale bars: the reduced system extended by the promoted points (pb_survey.cu)
+    bool ext_on = false;
+    ExtSys ext{};
+    PcgSystem<double> sysx{};
+    int* ext_flags = nullptr;
+    double* bar_d = nullptr;  // bar cost of the current state, then of the trial states
 };
 
 namespace {
@@ -237,6 +243,9 @@ void upload_structure(pb_gpu_ctx* c) {
     S.ref_param = m.ref_param ? 1 : 0;
     S.ncp = static_cast<int>(m.cp_proc.size() / 12);
     S.cp_huber = m.cp_huber;
+    S.npr = m.npr;
+    S.nbar = static_cast<int>(m.bar_tracks.size() / 2);
+    S.bar_huber = m.bar_huber;
     {
         const float2 ls = ff_pack(m.loss_scale);
         S.loss_scale_hi = ls.x;
@@ -271,6 +280,36 @@ void upload_structure(pb_gpu_ctx* c) {
     }
     D.trk_obs_begin = upload_new(A, m.trk_obs_begin, st);
     D.trk_block = upload_new(A, tblock, st);
+    {
+        // points that move (eliminated or promoted) and the scale-bar records in processing order
+        std::vector<int> tfree(ntp), tprom(ntp, -1), pproc(std::max(1, m.npr), 0);
+        std::vector<int> pot_h(nt, -1);
+        for (int p = 0; p < ntp; ++p) {
+            const int t = m.trk_order[p];
+            pot_h[t] = p;
+            tprom[p] = m.track_prom.empty() ? -1 : m.track_prom[t];
+            tfree[p] = (m.track_block[t] >= 0 || tprom[p] >= 0) ? 1 : 0;
+            if (tprom[p] >= 0) pproc[tprom[p]] = p;
+        }
+        D.trk_free = upload_new(A, tfree, st);
+        D.trk_prom = upload_new(A, tprom, st);
+        D.prom_proc = upload_new(A, pproc, st);
+        const int nbar = static_cast<int>(m.bar_tracks.size() / 2);
+        std::vector<int> bp(std::max(1, 2 * nbar), -1);
+        std::vector<double> bpar(std::max(1, 2 * nbar), 0.0);
+        for (int i = 0; i < nbar; ++i) {
+            for (int e = 0; e < 2; ++e) {
+                const int t = m.bar_tracks[2 * i + e];
+                bp[2 * i + e] = m.active_track[t] ? pot_h[t] : -1;
+            }
+            // linearizeScaleBar: weight = scaleBarWeight * weight, residual scale sqrt(weight) / sigma
+            const double* d = &m.bar_data[static_cast<size_t>(i) * 3];
+            bpar[2 * i] = d[0];
+            bpar[2 * i + 1] = std::sqrt(m.bar_weight * d[2]) / std::max(1e-9, d[1]);
+        }
+        D.bar_pidx = upload_new(A, bp, st);
+        D.bar_par = upload_new(A, bpar, st);
+    }
     D.trk_orig = upload_new(A, torig, st);
     D.points0 = upload_new(A, pts, st);
     D.points = A.alloc<double>(pts.size());
@@ -378,6 +417,23 @@ void upload_structure(pb_gpu_ctx* c) {
     sy.Cinv = A.alloc<double>(static_cast<size_t>(std::max(1, S.ng)) * kMaxNI * kMaxNI);
     c->pcg_x = A.alloc<double>(std::max(1, n));
     c->pcg_work = A.alloc<double>(static_cast<size_t>(std::max(1, n)) * 4);
+    c->ext_on = S.nbar > 0;
+    if (c->ext_on) {
+        ExtSys& X = c->ext;
+        X.nbx = S.nb + 3 * S.npr;
+        X.nx = n + 3 * S.npr;
+        X.border = A.alloc<double>(static_cast<size_t>(std::max(1, 6 * S.ncb)) * std::max(1, X.nbx));
+        X.border_t = A.alloc<double>(static_cast<size_t>(std::max(1, 6 * S.ncb)) * std::max(1, X.nbx));
+        X.Cm = A.alloc<double>(static_cast<size_t>(std::max(1, X.nbx)) * std::max(1, X.nbx));
+        X.rhs = A.alloc<double>(std::max(1, X.nx));
+        c->sysx = sy;
+        c->sysx.nb = X.nbx;
+        c->sysx.border = X.border;
+        c->sysx.border_t = X.border_t;
+        c->sysx.Cm = X.Cm;
+        c->ext_flags = A.alloc<int>(1);
+        c->bar_d = A.alloc<double>(kMaxAlpha + 2);  // [0] current, [1 .. kMaxAlpha] trials, then the step sum
+    }
     c->pcg_grid = pcg_grid_size<double>(S.ncb);
     c->S[0] = c->S[1] = S;
     c->D[0] = c->D[1] = D;
@@ -452,6 +508,7 @@ void ensure_pcg_partials(pb_gpu_ctx* c) {
 }
 
 void set_assemble_smem(int precision, size_t bytes);
+double extend_system(pb_gpu_ctx* c, double damping);
 
 struct Timer {
     pb_gpu_ctx* c;
@@ -495,6 +552,9 @@ void assemble(pb_gpu_ctx* c, double damping, int precision, double* cost, int* f
     *flags = static_cast<int>(c->h_scratch[1]);
     c->last_precision = precision;
     c->have_system = true;
+    // scale bars: every assembly extends the reduced system by the promoted points and adds the
+    // bars' cost, so that every solve of this context sees the extended system
+    if (c->ext_on && !(*flags & 6)) *cost += extend_system(c, damping);
 }
 
 // Reduced solve.  Returns 0 ok, 1 breakdown / not positive definite (retried by the LM driver
@@ -514,8 +574,10 @@ void ensure_dense(pb_gpu_ctx* c) {
     DenseWork<T>& W = dwork<T>(c);
     const Shape& S = c->S[0];
     DeviceArena& A = c->darena;
-    W.n = S.n;
-    W.nt = std::max(1, (S.n + 63) / 64);
+    // the system solved: the reduced one, or its extension by promoted points (scale bars)
+    const int nsol = c->ext_on ? c->ext.nx : S.n, nbsol = c->ext_on ? c->ext.nbx : S.nb;
+    W.n = nsol;
+    W.nt = std::max(1, (nsol + 63) / 64);
     W.np = W.nt * 64;
     W.nnzb = S.nnzb;
     W.A = A.alloc<T>(static_cast<size_t>(W.np) * W.np);
@@ -534,9 +596,9 @@ void ensure_dense(pb_gpu_ctx* c) {
         int longest = 0;
         for (int r = 0; r < S.ncb; ++r) longest = std::max(longest, c->model.row_ptr[r + 1] - c->model.row_ptr[r]);
         W.pose_seg = S.ncb > 0 ? std::max(1, (longest + 31) / 32) : 0;
-        W.border_seg = S.nb > 0 ? (S.n + 255) / 256 : 0;
+        W.border_seg = nbsol > 0 ? (nsol + 255) / 256 : 0;
         W.qpart = A.alloc<double>(std::max<size_t>(1, 6 * static_cast<size_t>(S.ncb) * W.pose_seg +
-                                                          static_cast<size_t>(S.nb) * W.border_seg));
+                                                          static_cast<size_t>(nbsol) * W.border_seg));
     }
     W.w = A.alloc<double>(W.n);
     W.ut = A.alloc<T>(W.np);
@@ -567,6 +629,8 @@ int solve_dense(pb_gpu_ctx* c, double rel, double abs_tol, int max_it, bool* con
     ensure_dense<T>(c);
     DenseWork<T>& W = dwork<T>(c);
     const bool f32 = std::is_same<T, float>::value;
+    const PcgSystem<double>& sys = c->ext_on ? c->sysx : c->sys;
+    const double* rhs = c->ext_on ? c->ext.rhs : c->red.rhs;
     // factor reuse across LM iterations: the mixed path's default; the FP64 path on request
     // (pb_solve_options.factor_reuse), which gives an FP64 arm with the mixed path's policy
     const bool reuse = f32 ? c->factor_reuse != 2 : c->factor_reuse == 1;
@@ -577,8 +641,8 @@ int solve_dense(pb_gpu_ctx* c, double rel, double abs_tol, int max_it, bool* con
         // about as much as a hundred CG iterations, so the kept factor is used until the CG
         // needs more than kReuseIterations on it.
         const int cap = std::min(max_it, std::max(kReuseIterations, 4 * c->f32_base_iters));
-        const int rc = dense_pcg<T>(c->sys, W, c->red.rhs, rel, abs_tol, cap, iterations, relres, converged,
-                                    c->h_scratch + 40, c->stream, &c->launches);
+        const int rc = dense_pcg<T>(sys, W, rhs, rel, abs_tol, cap, iterations, relres, converged, c->h_scratch + 40,
+                                    c->stream, &c->launches);
         if (rc < 0) throw CudaError(std::string("dense CG failed: ") + cudaGetErrorString(cudaGetLastError()));
         if (rc == 0 && *converged) {
             ++c->f32_age;
@@ -595,15 +659,15 @@ int solve_dense(pb_gpu_ctx* c, double rel, double abs_tol, int max_it, bool* con
     double shift = f32 ? c->shift32 : 0.0;
     int st = 0;
     for (int attempt = 0; attempt < 6; ++attempt) {
-        st = dense_factor<T>(c->sys, W, shift, c->stream, &c->launches);
+        st = dense_factor<T>(sys, W, shift, c->stream, &c->launches);
         if (st < 0) throw CudaError(std::string("dense factorisation failed: ") + cudaGetErrorString(cudaGetLastError()));
         if (st == 0 || (st & 1)) break;
         shift = shift == 0.0 ? 1e-9 : shift * 10.0;
     }
     if (st) return 1;
     if (f32) c->shift32 = shift;
-    const int rc = dense_pcg<T>(c->sys, W, c->red.rhs, rel, abs_tol, max_it, iterations, relres, converged,
-                                c->h_scratch + 40, c->stream, &c->launches);
+    const int rc = dense_pcg<T>(sys, W, rhs, rel, abs_tol, max_it, iterations, relres, converged, c->h_scratch + 40,
+                                c->stream, &c->launches);
     if (rc < 0) throw CudaError(std::string("dense CG failed: ") + cudaGetErrorString(cudaGetLastError()));
     if (reuse) {
         c->f32_age = rc == 0 ? 1 : -1;
@@ -655,9 +719,16 @@ int solve_reduced(pb_gpu_ctx* c, const pb_solve_options& op, bool* converged, in
                                                          : (op.general_path ? 1.0e-12 : 2.0e-10);
     const double abs_tol = op.linear_absolute_tolerance > 0 ? op.linear_absolute_tolerance : 1.0e-12;
     const int max_it = op.max_linear_iterations > 0 ? op.max_linear_iterations : std::max(200, 30 * c->model.P);
-    const int solver = (op.linear_solver == 1 || op.linear_solver == 2)
-                           ? op.linear_solver
-                           : (dense_solver_fits(c->S[0].n, c->last_precision) ? 1 : 2);
+    int solver = (op.linear_solver == 1 || op.linear_solver == 2)
+                     ? op.linear_solver
+                     : (dense_solver_fits(c->S[0].n, c->last_precision) ? 1 : 2);
+    if (c->ext_on) {
+        // the promoted points live in the dense border: the dense-factor CG solves the extension
+        if (!dense_solver_fits(c->ext.nx, c->last_precision))
+            throw std::runtime_error("scale bars need the dense reduced solver, and the reduced dimension exceeds its limit "
+                                     "(32 768 mixed, 16 384 FP64)");
+        solver = 1;
+    }
     c->last_solver = solver;
     *converged = false;
     *iterations = 0;
@@ -708,11 +779,50 @@ void eval_costs(pb_gpu_ctx* c, const double* alphas, int n, int use_trial, doubl
         Timer t(c, 2);
         launch_cost(S, D, c->step_c, c->step_p, c->alphas_d, n, use_trial, c->cost_part, c->cost_out, c->stream);
         c->launches += use_trial ? 3 : 2;
+        if (c->ext_on) {
+            launch_bar_cost(S, D, c->step_p, c->alphas_d, n, use_trial, c->bar_d + 1, c->stream);
+            c->launches += 1;
+        }
     }
     check(cudaGetLastError(), "cost launch");
     check(cudaMemcpyAsync(c->h_scratch, c->cost_out, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "D2H");
+    if (c->ext_on)
+        check(cudaMemcpyAsync(c->h_scratch + 8, c->bar_d + 1, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream),
+              "D2H");
     check(cudaStreamSynchronize(c->stream), "cost");
     std::memcpy(out, c->h_scratch, n * sizeof(double));
+    // the scale bars' robust cost (assembleScaleBars, BundleAdjustPlaMatrixAssemblySurvey.cpp:131-186)
+    if (c->ext_on)
+        for (int i = 0; i < n; ++i) out[i] += c->h_scratch[8 + i];
+}
+
+// Scale bars: the reduced system of the last assembly extended by the promoted points; returns
+// the bars' cost at the current state.
+double extend_system(pb_gpu_ctx* c, double damping) {
+    const Shape& S = c->S[0];
+    check(cudaMemsetAsync(c->ext_flags, 0, sizeof(int), c->stream), "memset");
+    launch_extend_system(S, c->D[0], c->red, c->ext, damping, c->ext_flags, c->bar_d, c->stream);
+    c->launches += S.npr > 0 ? 4 : 3;
+    check(cudaGetLastError(), "extension launch");
+    check(cudaMemcpyAsync(c->h_scratch, c->bar_d, sizeof(double), cudaMemcpyDeviceToHost, c->stream), "D2H");
+    check(cudaMemcpyAsync(c->h_scratch + 1, c->ext_flags, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "D2H");
+    check(cudaStreamSynchronize(c->stream), "extension");
+    int flags = 0;
+    std::memcpy(&flags, c->h_scratch + 1, sizeof(int));
+    if (flags & 2) throw std::runtime_error("linearisation produced an invalid projection");
+    return c->h_scratch[0];
+}
+
+// Scale bars: the promoted points' steps of the last extended solve into the point steps;
+// returns their squared sum.
+double promoted_steps(pb_gpu_ctx* c) {
+    const double* xsol = c->last_precision == PB_PRECISION_MIXED ? c->dw32.x : c->dw64.x;
+    launch_ext_step(c->S[0], c->D[0], xsol, c->step_c, c->step_p, c->bar_d + kMaxAlpha + 1, c->stream);
+    c->launches += 1;
+    check(cudaGetLastError(), "promoted step launch");
+    check(cudaMemcpyAsync(c->h_scratch, c->bar_d + kMaxAlpha + 1, sizeof(double), cudaMemcpyDeviceToHost, c->stream), "D2H");
+    check(cudaStreamSynchronize(c->stream), "promoted steps");
+    return c->h_scratch[0];
 }
 
 void reset_state(pb_gpu_ctx* c) {
@@ -1000,6 +1110,8 @@ void lm_solve_general(pb_gpu_ctx* c, const pb_solve_options& op, pb_solve_report
     rep->observation_count = m.obs_count;
     rep->rejected_initial_tracks = m.rejected;
     rep->camera_blocks = m.ncb;
+    rep->promoted_point_blocks = m.npr;
+    rep->general_path_used = 1;
     rep->intrinsic_blocks = m.ng;
     rep->pattern_builds = c->pattern_builds;
     rep->pattern_reuses = c->pattern_reuses;
@@ -1024,10 +1136,10 @@ void lm_solve_general(pb_gpu_ctx* c, const pb_solve_options& op, pb_solve_report
     const bool trace = std::getenv("PB_GPU_TRACE") != nullptr;
     double current = kNaN, damping = 0.0;
     int iterations = 0;
-    bool converged = m.P == 0 && m.ntb == 0;
+    bool converged = m.P == 0 && m.ntb == 0 && m.npr == 0;
     bool failed = false, cancelled = false;
     const double n_global = static_cast<double>(6 * m.ncb + m.ng * m.ni);
-    const double n_point = 3.0 * m.ntb;
+    const double n_point = 3.0 * (m.ntb + m.npr);
     auto t_asm = 0.0, t_lin = 0.0, t_bs = 0.0, t_obj = 0.0;
     auto now = [] { return std::chrono::steady_clock::now(); };
     auto ms = [](std::chrono::steady_clock::time_point a, std::chrono::steady_clock::time_point b) {
@@ -1083,6 +1195,7 @@ void lm_solve_general(pb_gpu_ctx* c, const pb_solve_options& op, pb_solve_report
                 double dd_bs, psq, csq;
                 auto tb = now();
                 back_substitute(c, &dd_bs, &psq, &csq);
+                if (c->ext_on) psq += promoted_steps(c);
                 t_bs += ms(tb, now());
                 const double rg = n_global > 0 ? std::sqrt(csq / n_global) : 0.0;
                 const double rp = n_point > 0 ? std::sqrt(psq / n_point) : 0.0;
@@ -1591,7 +1704,9 @@ pb_status pb_gpu_solve(pb_gpu_ctx* c, const pb_solve_options* op, pb_solve_repor
     try {
         cudaSetDevice(c->device);
         c->error.clear();
-        if (op->general_path) lm_solve_general(c, *op, rep);
+        // a problem with scale bars has no online path (canUseReferenceOnlineSchur,
+        // BundleAdjustPlaMatrixReferenceSchur.cpp:667-673)
+        if (op->general_path || c->model.force_general) lm_solve_general(c, *op, rep);
         else lm_solve(c, *op, rep);
         return PB_OK;
     } catch (const std::exception& e) {
@@ -1841,7 +1956,7 @@ pb_status adjoint_prepare(pb_gpu_ctx* c) {
     // the exact Hessian is written for the Euler target rotation chart and the scaled point chart
     // of image-only problems; control points switch the solve to the plain parameterisation
     if (!m.ref_param)
-        return fail(c, PB_ERR_UNSUPPORTED, "the backward pass covers image-only problems (no control points)");
+        return fail(c, PB_ERR_UNSUPPORTED, "the backward pass covers image-only problems (no control points or scale bars)");
     // the point elimination runs over the chunk plan of the arithmetic path last used
     const int prec = c->last_precision == PB_PRECISION_MIXED ? 1 : 0;
     if (prec == 1) prepare_precision<float>(c, prec);

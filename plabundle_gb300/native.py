@@ -43,7 +43,8 @@ class ProblemDesc(C.Structure):
                 ("fixed_cameras", C.c_void_p), ("n_fixed_tracks", C.c_int32), ("fixed_tracks", C.c_void_p),
                 ("calibration_group_ids", C.c_void_p), ("intrinsic_reference_cameras", C.c_void_p),
                 ("n_control_points", C.c_int32), ("control_point_track", C.c_void_p),
-                ("control_point_data", C.c_void_p)]
+                ("control_point_data", C.c_void_p), ("n_scale_bars", C.c_int32), ("scale_bar_tracks", C.c_void_p),
+                ("scale_bar_data", C.c_void_p)]
 
 
 class SolveOptionsC(C.Structure):
@@ -59,7 +60,8 @@ class SolveOptionsC(C.Structure):
                 ("preconditioner_cluster_size", C.c_int32), ("linear_solver", C.c_int32),
                 ("calibration", C.c_double * 32), ("control_point_weight", C.c_double),
                 ("control_point_huber_delta", C.c_double), ("factor_reuse", C.c_int32),
-                ("general_path", C.c_int32)]
+                ("general_path", C.c_int32), ("scale_bar_weight", C.c_double),
+                ("scale_bar_huber_delta", C.c_double)]
 
 
 class SolveReportC(C.Structure):
@@ -69,7 +71,8 @@ class SolveReportC(C.Structure):
         "rejected_initial_tracks", "optimized_tracks", "camera_blocks", "intrinsic_blocks", "pattern_builds",
         "pattern_reuses", "gpu_kernel_launches")] + [(n, C.c_double) for n in (
             "initial_cost", "final_cost", "mean_rms_before", "mean_rms_after", "valid_track_ratio",
-            "filter_threshold", "assembly_ms", "linear_ms", "back_substitution_ms", "objective_ms", "total_ms")]
+            "filter_threshold", "assembly_ms", "linear_ms", "back_substitution_ms", "objective_ms", "total_ms")] + [
+        (n, C.c_int32) for n in ("promoted_point_blocks", "general_path_used")]
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -197,12 +200,24 @@ def problem_desc(problem):
     fixed_c = np.ascontiguousarray(p.fixedCameraIndices, np.int32)
     fixed_t = np.ascontiguousarray(p.fixedTrackIndices, np.int32)
     cp_track, cp_data = control_point_arrays(p)
-    keep = [p, fixed_c, fixed_t, cp_track, cp_data]
+    sb_tracks, sb_data = scale_bar_arrays(p)
+    keep = [p, fixed_c, fixed_t, cp_track, cp_data, sb_tracks, sb_data]
     desc = ProblemDesc(p.n_cameras, _ptr(p.cameras), p.n_tracks, _ptr(p.track_offsets), _ptr(p.points), p.n_obs,
                        _ptr(p.obs_camera), _ptr(p.obs_u), _ptr(p.obs_v), _ptr(p.obs_weight), _ptr(p.obs_scale),
                        fixed_c.size, _ptr(fixed_c), fixed_t.size, _ptr(fixed_t), _ptr(p.cameraCalibrationGroupIds),
-                       _ptr(p.sharedIntrinsicReferenceCameras), cp_track.size, _ptr(cp_track), _ptr(cp_data))
+                       _ptr(p.sharedIntrinsicReferenceCameras), cp_track.size, _ptr(cp_track), _ptr(cp_data),
+                       sb_data.shape[0], _ptr(sb_tracks), _ptr(sb_data))
     return desc, keep
+
+
+def scale_bar_arrays(problem):
+    """(track pairs int32 [n, 2], records float64 [n, 3]: distance, sigma, weight) of the problem's
+    scale bars."""
+    bars = getattr(problem, "scaleBarConstraints", None) or []
+    tracks = np.ascontiguousarray(np.array([(b.trackIndexA, b.trackIndexB) for b in bars], np.int32).reshape(-1, 2))
+    data = np.ascontiguousarray(np.array([(b.measuredDistanceMeters, b.sigmaMeters, b.weight) for b in bars],
+                                         np.float64).reshape(-1, 3))
+    return tracks, data
 
 
 def control_point_arrays(problem):
@@ -248,6 +263,8 @@ def solve_options(options, problem=None) -> SolveOptionsC:
     o.control_point_huber_delta = con.controlPointHuberDeltaMeters if con is not None else 0.2
     o.factor_reuse = int(getattr(b, "factorReuse", 0))
     o.general_path = 0 if s.useReferenceOnlineSchur else 1
+    o.scale_bar_weight = con.scaleBarWeight if con is not None else 1.0
+    o.scale_bar_huber_delta = con.scaleBarHuberDeltaMeters if con is not None else 0.2
     return o
 
 

@@ -134,13 +134,27 @@ class ControlPointConstraint:
 
 
 @dataclass
+class ScaleBarConstraint:
+    """ScaleBarConstraint (include/plabundle/constraints.h:93-101): the measured distance between
+    the points of two tracks."""
+
+    trackIndexA: int = -1
+    trackIndexB: int = -1
+    measuredDistanceMeters: float = 0.0
+    sigmaMeters: float = 1.0
+    weight: float = 1.0
+    sourceIndex: int = -1
+
+
+@dataclass
 class Problem:
     """plabundle::Problem (include/plabundle/problem.h:37-54) for frame cameras.
 
-    Rigs, laser planes, scale bars and pose priors are not carried: the GB300 backend covers the
-    online reduced-Schur path, whose only survey term is the control point
-    (canUseReferenceOnlineSchur, BundleAdjustPlaMatrixReferenceSchur.cpp:667-673).  Control
-    points are the (track, ControlPointConstraint) pairs of Track::controlPointConstraints.
+    Control points are the (track, ControlPointConstraint) pairs of Track::controlPointConstraints;
+    scale bars are Problem::scaleBarConstraints (their tracks become primary point blocks and the
+    problem is solved on the general path, canUseReferenceOnlineSchur,
+    BundleAdjustPlaMatrixReferenceSchur.cpp:667-673).  Rigs, laser planes and ranges, pose priors
+    and the camera-plane constraint are not carried.
     """
 
     cameras: np.ndarray                 # [n_cameras, 32] float64
@@ -157,6 +171,7 @@ class Problem:
     sharedIntrinsicReferenceCameras: Optional[np.ndarray] = None  # [n_cameras, 32]
     gauge: Gauge = field(default_factory=Gauge)
     controlPoints: List[Tuple[int, ControlPointConstraint]] = field(default_factory=list)
+    scaleBarConstraints: List[ScaleBarConstraint] = field(default_factory=list)
 
     @property
     def n_cameras(self) -> int:
@@ -340,10 +355,13 @@ class QualityGateOptions:
 
 @dataclass
 class ConstraintOptions:
-    """ConstraintOptions (include/plabundle/options.h:122-135): the control-point fields."""
+    """ConstraintOptions (include/plabundle/options.h:122-135): the control-point and scale-bar
+    fields."""
 
     controlPointWeight: float = 1.0
     controlPointHuberDeltaMeters: float = 0.2
+    scaleBarWeight: float = 1.0
+    scaleBarHuberDeltaMeters: float = 0.2
 
 
 @dataclass
@@ -411,6 +429,9 @@ class QualitySummary:
     controlPointConstraintCount: int = 0
     controlPointRmsBeforeMeters: float = 0.0
     controlPointRmsAfterMeters: float = 0.0
+    scaleBarConstraintCount: int = 0
+    scaleBarRmsBeforeMeters: float = 0.0
+    scaleBarRmsAfterMeters: float = 0.0
 
 
 @dataclass

@@ -134,6 +134,47 @@ def control_point_stats(problem: Problem, points: Optional[np.ndarray], valid: n
     return n, (math.sqrt(s / n) if n else 0.0)
 
 
+def scale_bar_rms_uncertainty(problem: Problem, options: SolveOptions) -> float:
+    """sqrt(mean over the bars of sigma^2 / (scaleBarWeight * weight)) (constraintRmsUncertainty,
+    src/solver.cpp:84-88)."""
+    bars = problem.scaleBarConstraints
+    var = sum(b.sigmaMeters ** 2 / (options.constraints.scaleBarWeight * b.weight) for b in bars)
+    return math.sqrt(var / len(bars)) if bars else 0.0
+
+
+def scale_bar_stats(problem: Problem, points: Optional[np.ndarray], valid: np.ndarray):
+    """computeScaleBarStats (src/internal/BundleAdjustQuality.cpp:213-259): count and RMS of
+    |X_a - X_b| - measured distance over the usable bars whose two tracks are valid in the result,
+    the initial points (before) or the refined ones (after)."""
+    X = problem.points if points is None else points
+    s, n = 0.0, 0
+    for b in problem.scaleBarConstraints:
+        a, c = b.trackIndexA, b.trackIndexB
+        if a < 0 or c < 0 or a == c or a >= problem.n_tracks or c >= problem.n_tracks:
+            continue
+        if not (math.isfinite(b.measuredDistanceMeters) and b.measuredDistanceMeters > 0):
+            continue
+        if not (valid[a] and valid[c]):
+            continue
+        r = float(np.linalg.norm(np.asarray(X[a]) - np.asarray(X[c]))) - b.measuredDistanceMeters
+        if not math.isfinite(r):
+            continue
+        s += r * r
+        n += 1
+    return n, (math.sqrt(s / n) if n else 0.0)
+
+
+def constraint_gate(count: int, before: float, after: float, growth: float, unc: float, what: str) -> str:
+    """constraintRmsPassesQualityGate (src/internal/BundleAdjustQuality.cpp:504-540)."""
+    if count <= 0:
+        return ""
+    if not (math.isfinite(before) and math.isfinite(after) and math.isfinite(unc)) or unc < 0:
+        return f"quality gate rejected invalid {what} RMS or uncertainty"
+    if after > max(1.0, growth) * max(before, unc):
+        return f"quality gate rejected {what} RMS growth beyond the uncertainty threshold"
+    return ""
+
+
 def result_fails_quality_gate(result: Result, options: SolveOptions, problem: Optional[Problem] = None) -> str:
     """resultFailsQualityGate (src/solver.cpp:123-210) for image and control-point terms."""
     q = options.quality
@@ -160,6 +201,12 @@ def result_fails_quality_gate(result: Result, options: SolveOptions, problem: Op
             return "quality gate rejected invalid control-point constraint RMS or uncertainty"
         if after > max(1.0, q.maxAcceptedConstraintRmsGrowth) * max(before, unc):
             return "quality gate rejected control-point constraint RMS growth beyond the uncertainty threshold"
+    if problem is not None and qs.scaleBarConstraintCount > 0:
+        msg = constraint_gate(qs.scaleBarConstraintCount, qs.scaleBarRmsBeforeMeters, qs.scaleBarRmsAfterMeters,
+                              q.maxAcceptedConstraintRmsGrowth, scale_bar_rms_uncertainty(problem, options),
+                              "scale-bar constraint")
+        if msg:
+            return msg
     return ""
 
 
@@ -252,6 +299,11 @@ class Solver:
             result.quality.controlPointConstraintCount, result.quality.controlPointRmsBeforeMeters = \
                 control_point_stats(problem, None, v)
             _, result.quality.controlPointRmsAfterMeters = control_point_stats(problem, pts, v)
+        if problem.scaleBarConstraints:
+            v = result.points.valid
+            result.quality.scaleBarConstraintCount, result.quality.scaleBarRmsBeforeMeters = \
+                scale_bar_stats(problem, None, v)
+            _, result.quality.scaleBarRmsAfterMeters = scale_bar_stats(problem, pts, v)
         result.report = r
         gate = result_fails_quality_gate(result, options, problem)
         if gate:

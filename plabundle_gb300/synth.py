@@ -330,6 +330,41 @@ def with_gauge(problem: Problem, policy=GaugePolicy.AutoAnchor) -> Problem:
     return problem
 
 
+def with_scale_bars(problem: Problem, n: int = 10, sigma: float = 0.005, seed: int = 0,
+                    max_length: float = 20.0, weights=(1.0, 0.5, 2.0)) -> Problem:
+    """Scale bars between `n` disjoint pairs of tracks seen by two distinct cameras, their true
+    points at most `max_length` apart (the closest candidate to a random track): measured
+    distance = true distance + N(0, sigma), sigma and the weights cycling as given."""
+    from .problem import ScaleBarConstraint
+    rng = np.random.default_rng(seed)
+    off = np.asarray(problem.track_offsets)
+    cams = np.asarray(problem.obs_camera)
+    truth = getattr(problem, "truth_points", None)
+    truth = problem.points if truth is None else truth
+    eligible = np.array([t for t in range(problem.n_tracks) if np.unique(cams[off[t]:off[t + 1]]).size >= 2])
+    used = set()
+    bars = []
+    for t in rng.permutation(eligible):
+        if len(bars) >= n:
+            break
+        if t in used:
+            continue
+        d = np.linalg.norm(truth[eligible] - truth[t], axis=1)
+        order = np.argsort(d)
+        for j in order[1:]:
+            u = int(eligible[j])
+            if u in used or u == t or d[j] <= 0.5 or d[j] > max_length:
+                continue
+            used.update((int(t), u))
+            length = float(np.linalg.norm(truth[u] - truth[t])) + rng.normal(0.0, sigma)
+            bars.append(ScaleBarConstraint(trackIndexA=int(t), trackIndexB=u, measuredDistanceMeters=length,
+                                           sigmaMeters=sigma, weight=weights[len(bars) % len(weights)],
+                                           sourceIndex=len(bars)))
+            break
+    problem.scaleBarConstraints = bars
+    return problem
+
+
 def with_control_points(problem: Problem, n: int = 12, sigma: float = 0.02, seed: int = 0,
                         kinds=(0, 1, 2), weights=(1.0, 0.5, 2.0)) -> Problem:
     """Survey control points on `n` tracks seen by two distinct cameras: the true point plus
