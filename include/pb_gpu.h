@@ -108,6 +108,31 @@ typedef struct pb_problem_desc {
     int32_t n_scale_bars;
     const int32_t* scale_bar_tracks;
     const double* scale_bar_data;
+    /* Rig topology (Problem::rig, placamera::RigTopology, include/plabundle/problem.h:52; the
+     * reference's README "Rig BA"): captures hold a rig-to-world rotation and the rig centre in
+     * world coordinates, sensors a camera-to-rig rotation and the camera centre in rig
+     * coordinates, and every camera is bound to one capture and one sensor of the same rig
+     * (RigCameraBinding, resolved to indices by the caller).
+     *   rig_captures[12 * k]: rigToWorldRotation (9, row-major), rigCenterInWorld (3);
+     *   rig_capture_info[2 * k]: rigId, fixedPose (0/1);
+     *   rig_sensors[12 * s]: cameraToRigRotation (9, row-major), cameraCenterInRig (3);
+     *   rig_sensor_info[2 * s]: rigId, fixedExtrinsic (0/1);
+     *   rig_camera_capture / rig_camera_sensor: n_cameras indices.
+     * The composed camera is R = R_rig R_sensor, C = C_rig + R_rig c_sensor; the poses passed in
+     * `cameras` are replaced by the composition (runConcreteBackend, src/solver.cpp:282).  Every
+     * rig needs at least one fixed sensor.  The pose blocks are then one per non-fixed capture
+     * followed by one per non-fixed sensor (prepareActiveProblem,
+     * BundleAdjustPlaMatrixProblem.cpp:156-199) and the problem uses the plain parameterisation
+     * (useReferencePointParameterization, BundleAdjustPlaMatrixAssembly.cpp:24-30).
+     * n_rig_captures == 0: no rig. */
+    int32_t n_rig_captures;
+    const double* rig_captures;
+    const int32_t* rig_capture_info;
+    int32_t n_rig_sensors;
+    const double* rig_sensors;
+    const int32_t* rig_sensor_info;
+    const int32_t* rig_camera_capture;
+    const int32_t* rig_camera_sensor;
 } pb_problem_desc;
 
 /* SolveOptions (include/plabundle/options.h:58-187) as flat fields. */
@@ -186,6 +211,8 @@ typedef struct pb_solve_report {
     double total_ms;
     int32_t promoted_point_blocks;     /* tracks of scale bars solved as primary point blocks */
     int32_t general_path_used;         /* 1 when the solve ran on the general path */
+    int32_t rig_capture_blocks;        /* ActiveProblem::rigCaptureBlockCount (0 without a rig) */
+    int32_t rig_sensor_blocks;         /* ActiveProblem::rigSensorBlockCount */
 } pb_solve_report;
 
 /* Context lifetime (SolverWorkspace construction / clear()). */
@@ -256,6 +283,15 @@ pb_status pb_gpu_solve(pb_gpu_ctx* ctx, const pb_solve_options* options, pb_solv
  * strict RMS before/after, intrinsic group parameters (n_groups * 13). Any pointer may be NULL. */
 pb_status pb_gpu_download_state(pb_gpu_ctx* ctx, double* cameras, double* points, int8_t* valid,
                                 double* rms_before, double* rms_after, double* intrinsics);
+
+/* Rig problems: the current capture and sensor parameters (Result::refinedRig,
+ * include/plabundle/result.h:149), 12 doubles each in the layout of pb_problem_desc's
+ * rig_captures / rig_sensors, and the pose block of every capture and sensor (-1: fixed or without
+ * residuals; ActiveProblem::rigCaptureBlockByCamera / rigSensorBlockByCamera,
+ * BundleAdjustPlaMatrixProblem.h:13-39, per capture / sensor instead of per camera).  Any pointer
+ * may be NULL.  PB_ERR_STATE when the uploaded problem has no rig. */
+pb_status pb_gpu_get_rig(pb_gpu_ctx* ctx, double* captures, double* sensors, int32_t* capture_block,
+                         int32_t* sensor_block);
 
 /* One call: upload + solve + download (the path a caller of Solver::solve takes). */
 pb_status pb_gpu_solve_problem(pb_gpu_ctx* ctx, const pb_problem_desc* problem, const pb_solve_options* options,

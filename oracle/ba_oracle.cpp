@@ -272,15 +272,26 @@ struct Active {
     std::vector<char> activeTrack;
     std::vector<int> cameraBlock, intrinsicBlockByCamera, calibGroupByCamera, trackBlock;
     std::vector<int> trackPrimaryBlock;  // scale-bar tracks promoted to primary point blocks, else -1
+    // rigs (BundleAdjustPlaMatrixProblem.h:13-39): per camera, the capture / sensor index and block
+    std::vector<int> rigCaptureIndexByCamera, rigSensorIndexByCamera, rigCaptureBlockByCamera, rigSensorBlockByCamera;
+    int rigCaptureBlockCount = 0, rigSensorBlockCount = 0;
     int primaryBlockCount = 0, cameraBlockCount = 0, intrinsicBlockCount = 0, trackBlockCount = 0;
     int promotedTrackBlockCount = 0;
     int activeTrackCount = 0, observationCount = 0, rejectedInitialTracks = 0;
+};
+
+// A rig capture (rig-to-world rotation, rig centre) or sensor (camera-to-rig rotation, camera centre
+// in the rig): a rotation R (row-major) and a centre C.
+struct RigPose {
+    double R[9];
+    double C[3];
 };
 
 struct State {
     std::vector<Camera> cams;
     std::vector<std::array<double, 3>> points;
     std::vector<Group> groups;
+    std::vector<RigPose> captures, sensors;  // rig problems
 };
 
 struct OffDiagSlot {
@@ -338,9 +349,15 @@ struct Oracle {
     // block normal equations of the general path (orc_general_build)
     std::shared_ptr<GeneralEquations> general;
 
+    // rig topology: input captures and sensors, (rigId, fixed flag) of each, per-camera binding
+    bool hasRig = false;
+    std::vector<RigPose> inputCaptures, inputSensors;
+    std::vector<int> captureInfo, sensorInfo;
+    std::vector<int> cameraCapture, cameraSensor;
+
     size_t nt() const { return offs.size() - 1; }
     // useReferencePointParameterization (BundleAdjustPlaMatrixAssembly.cpp:24-30)
-    bool refParam() const { return !hasControlPoints && scaleBars.empty(); }
+    bool refParam() const { return !hasControlPoints && scaleBars.empty() && !hasRig; }
 };
 
 bool isCameraFixed(const Oracle& o, int cam) {
@@ -643,9 +660,43 @@ void prepareActive(Oracle& o) {
         for (int64_t k = o.offs[t]; k < o.offs[t + 1]; ++k)
             if (obsUsable(o.obs[k], nc)) camHasResidual[o.obs[k].cam] = 1;
     }
-    if (o.opt.refine_camera_pose) {
+    a.rigCaptureIndexByCamera.assign(nc, -1);
+    a.rigSensorIndexByCamera.assign(nc, -1);
+    a.rigCaptureBlockByCamera.assign(nc, -1);
+    a.rigSensorBlockByCamera.assign(nc, -1);
+    if (o.hasRig) {
+        a.rigCaptureIndexByCamera = o.cameraCapture;
+        a.rigSensorIndexByCamera = o.cameraSensor;
+    }
+    if (o.opt.refine_camera_pose && !o.hasRig) {
         for (size_t c = 0; c < nc; ++c)
             if (camHasResidual[c] && !isCameraFixed(o, static_cast<int>(c))) a.cameraBlock[c] = a.cameraBlockCount++;
+    } else if (o.opt.refine_camera_pose) {
+        // BundleAdjustPlaMatrixProblem.cpp:156-199
+        const size_t ncap = o.inputCaptures.size(), nsen = o.inputSensors.size();
+        std::vector<int> captureBlocks(ncap, -1), sensorBlocks(nsen, -1);
+        for (size_t k = 0; k < ncap; ++k) {
+            bool hasResidual = false;
+            bool fixed = o.captureInfo[2 * k + 1] != 0;
+            for (size_t c = 0; c < nc; ++c)
+                if (a.rigCaptureIndexByCamera[c] == static_cast<int>(k)) {
+                    hasResidual = hasResidual || camHasResidual[c];
+                    fixed = fixed || isCameraFixed(o, static_cast<int>(c)) || o.gaugeScale == static_cast<int>(c);
+                }
+            if (hasResidual && !fixed) captureBlocks[k] = a.rigCaptureBlockCount++;
+        }
+        for (size_t sI = 0; sI < nsen; ++sI) {
+            bool hasResidual = false;
+            for (size_t c = 0; c < nc; ++c)
+                hasResidual = hasResidual || (a.rigSensorIndexByCamera[c] == static_cast<int>(sI) && camHasResidual[c]);
+            if (hasResidual && !o.sensorInfo[2 * sI + 1])
+                sensorBlocks[sI] = a.rigCaptureBlockCount + a.rigSensorBlockCount++;
+        }
+        for (size_t c = 0; c < nc; ++c) {
+            a.rigCaptureBlockByCamera[c] = captureBlocks[static_cast<size_t>(a.rigCaptureIndexByCamera[c])];
+            a.rigSensorBlockByCamera[c] = sensorBlocks[static_cast<size_t>(a.rigSensorIndexByCamera[c])];
+        }
+        a.cameraBlockCount = a.rigCaptureBlockCount + a.rigSensorBlockCount;
     }
     a.primaryBlockCount = a.cameraBlockCount;
     if (hasSharedIntrinsics(o)) {
@@ -782,7 +833,8 @@ std::array<bool, kP> activeIntrinsics(const Oracle& o, size_t c) {
 
 bool usesGaugeTangent(const Oracle& o, size_t c) {
     const int nc = static_cast<int>(o.inputCams.size());
-    return o.gaugeAnchor >= 0 && o.gaugeScale >= 0 && o.gaugeAnchor < nc && o.gaugeScale < nc &&
+    // a rig camera never takes the tangent (constrained_center, BundleAdjustPlaMatrixAssembly.cpp:204)
+    return !o.hasRig && o.gaugeAnchor >= 0 && o.gaugeScale >= 0 && o.gaugeAnchor < nc && o.gaugeScale < nc &&
            c == static_cast<size_t>(o.gaugeScale) && std::isfinite(o.gaugeBaseline) && o.gaugeBaseline > 0.0;
 }
 
@@ -811,17 +863,64 @@ std::array<std::array<double, 3>, 2> gaugeBasis(const Oracle& o, const State& s)
     return {cross3(unit, second), second};
 }
 
-// cameraPosePrimaryTerms + observationPrimaryTerms (BundleAdjustPlaMatrixAssembly.cpp:186-342)
-// for non-rig cameras.
+// cameraPosePrimaryTerms + observationPrimaryTerms (BundleAdjustPlaMatrixAssembly.cpp:186-342).
+// A rig camera's Jacobian is chained to its capture block (rotation column a: J_rot[a] +
+// J_ctr (e_a x L) with the lever L = R_rig c_sensor; centre columns J_ctr) and its sensor block
+// (columns J_rot R_rig[:, a] and J_ctr R_rig[:, a]) (:207-284); its intrinsic block follows.
 struct Terms {
-    int blocks[2];
-    double J[2][2 * kP];
+    int blocks[3];
+    double J[3][2 * kP];
     int count = 0;
 };
 
 Terms primaryTerms(const Oracle& o, const State& s, size_t c, const Lin& L) {
     Terms t;
     std::memset(t.J, 0, sizeof(t.J));
+    if (o.hasRig) {
+        const int ki = o.active.rigCaptureIndexByCamera[c], si = o.active.rigSensorIndexByCamera[c];
+        if (ki >= 0 && si >= 0) {
+            const RigPose& cap = s.captures[static_cast<size_t>(ki)];
+            const RigPose& sen = s.sensors[static_cast<size_t>(si)];
+            double lever[3] = {0, 0, 0};
+            for (int w = 0; w < 3; ++w)
+                for (int r = 0; r < 3; ++r) lever[w] += cap.R[w * 3 + r] * sen.C[r];
+            const int kb = o.active.rigCaptureBlockByCamera[c], sb = o.active.rigSensorBlockByCamera[c];
+            if (kb >= 0) {
+                double* J = t.J[t.count];
+                for (int row = 0; row < 2; ++row) {
+                    const double* cr = L.Jc + row * 6;
+                    for (int ax = 0; ax < 3; ++ax) {
+                        double cd[3] = {0, 0, 0};
+                        cd[(ax + 1) % 3] = -lever[(ax + 2) % 3];
+                        cd[(ax + 2) % 3] = lever[(ax + 1) % 3];
+                        J[row * kP + ax] = cr[ax];
+                        for (int w = 0; w < 3; ++w) J[row * kP + ax] += cr[3 + w] * cd[w];
+                        J[row * kP + 3 + ax] = cr[3 + ax];
+                    }
+                }
+                t.blocks[t.count++] = kb;
+            }
+            if (sb >= 0) {
+                double* J = t.J[t.count];
+                for (int row = 0; row < 2; ++row) {
+                    const double* cr = L.Jc + row * 6;
+                    for (int ax = 0; ax < 3; ++ax)
+                        for (int w = 0; w < 3; ++w) {
+                            const double basis = cap.R[w * 3 + ax];
+                            J[row * kP + ax] += cr[w] * basis;
+                            J[row * kP + 3 + ax] += cr[3 + w] * basis;
+                        }
+                }
+                t.blocks[t.count++] = sb;
+            }
+        }
+        const int ib = o.active.intrinsicBlockByCamera[c];
+        if (ib >= 0) {
+            std::memcpy(t.J[t.count], L.Ji, sizeof(L.Ji));
+            t.blocks[t.count++] = ib;
+        }
+        return t;
+    }
     const int cb = o.active.cameraBlock[c];
     if (cb >= 0) {
         const bool tangent = usesGaugeTangent(o, c);
@@ -851,7 +950,7 @@ Terms primaryTerms(const Oracle& o, const State& s, size_t c, const Lin& L) {
     return t;
 }
 
-// prepareOffDiagonalTopology (BundleAdjustPlaMatrixReferenceSchur.cpp:568-659), without rig blocks.
+// prepareOffDiagonalTopology (BundleAdjustPlaMatrixReferenceSchur.cpp:568-659).
 void prepareTopology(Oracle& o) {
     if (o.topologyReady) return;
     const int P = o.active.primaryBlockCount;
@@ -869,8 +968,10 @@ void prepareTopology(Oracle& o) {
         for (int64_t k = o.offs[t]; k < o.offs[t + 1]; ++k) {
             const Obs& ob = o.obs[k];
             if (!obsUsable(ob, o.inputCams.size())) continue;
-            const int b[2] = {o.active.cameraBlock[ob.cam], o.active.intrinsicBlockByCamera[ob.cam]};
-            connect(b[0], b[1]);
+            const int b[4] = {o.active.cameraBlock[ob.cam], o.active.rigCaptureBlockByCamera[ob.cam],
+                              o.active.rigSensorBlockByCamera[ob.cam], o.active.intrinsicBlockByCamera[ob.cam]};
+            for (int l = 0; l < 4; ++l)
+                for (int r = l + 1; r < 4; ++r) connect(b[l], b[r]);
             if (o.active.trackBlock[t] >= 0)
                 for (int v : b)
                     if (v >= 0) tb.push_back(v);
@@ -982,8 +1083,8 @@ struct Accumulator {
 
 // accumulateObservationPrimaryTerms (BundleAdjustPlaMatrixReferenceSchur.cpp:140-193).
 void accumulateDirect(const Terms& t, const Lin& L, Accumulator& acc) {
-    int act[2][kP];
-    int na[2] = {0, 0};
+    int act[3][kP];
+    int na[3] = {0, 0, 0};
     for (int k = 0; k < t.count; ++k) {
         for (int p = 0; p < kP; ++p) {
             const double jx = t.J[k][p], jy = t.J[k][kP + p];
@@ -1548,11 +1649,52 @@ std::array<double, 3> gaugeTangentStep(const Oracle& o, const State& s, double a
 // applyStep (BundleAdjustPlaMatrixAssembly.cpp:1111-1247) in the reference point
 // parameterisation or the plain one (control points), applyIntrinsicStep
 // (BundleAdjustPlaMatrixModel.cpp:248-269).
+// Rig step (BundleAdjustPlaMatrixAssembly.cpp:1152-1209): placamera::applyPoseDelta on every
+// capture and sensor with a block (the plain pose delta, applyPlainPoseStep), then the cameras
+// composed again.
+void composeRigCamera(const RigPose& cap, const RigPose& sen, Camera& cam) {
+    for (int r = 0; r < 3; ++r)
+        for (int q = 0; q < 3; ++q)
+            cam.R[r * 3 + q] = cap.R[r * 3] * sen.R[q] + cap.R[r * 3 + 1] * sen.R[3 + q] + cap.R[r * 3 + 2] * sen.R[6 + q];
+    for (int r = 0; r < 3; ++r)
+        cam.C[r] = cap.C[r] + cap.R[r * 3] * sen.C[0] + cap.R[r * 3 + 1] * sen.C[1] + cap.R[r * 3 + 2] * sen.C[2];
+}
+
+void applyRigPoseStep(RigPose& p, const double* d) {
+    Camera tmp{};
+    std::memcpy(tmp.R, p.R, sizeof(p.R));
+    std::memcpy(tmp.C, p.C, sizeof(p.C));
+    applyPlainPoseStep(tmp, d);
+    std::memcpy(p.R, tmp.R, sizeof(p.R));
+    std::memcpy(p.C, tmp.C, sizeof(p.C));
+}
+
 State applyStep(const Oracle& o, const State& s, const std::vector<double>& ps, const std::vector<double>& es,
                 double alpha) {
     State n = s;
     const bool ref = o.refParam();
-    for (size_t c = 0; c < n.cams.size(); ++c) {
+    if (o.hasRig) {
+        const Active& a = o.active;
+        auto blockOf = [&](const std::vector<int>& index, const std::vector<int>& blocks, size_t i) {
+            for (size_t c = 0; c < index.size(); ++c)
+                if (index[c] == static_cast<int>(i)) return blocks[c];
+            return -1;
+        };
+        auto step = [&](RigPose& p, int block) {
+            if (block < 0) return;
+            double d[6];
+            for (int i = 0; i < 6; ++i) d[i] = alpha * ps[static_cast<size_t>(block) * kP + i];
+            applyRigPoseStep(p, d);
+        };
+        for (size_t k = 0; k < n.captures.size(); ++k)
+            step(n.captures[k], blockOf(a.rigCaptureIndexByCamera, a.rigCaptureBlockByCamera, k));
+        for (size_t si = 0; si < n.sensors.size(); ++si)
+            step(n.sensors[si], blockOf(a.rigSensorIndexByCamera, a.rigSensorBlockByCamera, si));
+        for (size_t c = 0; c < n.cams.size(); ++c)
+            composeRigCamera(n.captures[static_cast<size_t>(o.cameraCapture[c])],
+                             n.sensors[static_cast<size_t>(o.cameraSensor[c])], n.cams[c]);
+    }
+    for (size_t c = 0; c < n.cams.size() && !o.hasRig; ++c) {
         const int b = o.active.cameraBlock[c];
         if (b < 0) continue;
         double d[6];
@@ -1796,8 +1938,8 @@ double buildGeneral(Oracle& o, GeneralEquations& q) {
                 throw InvalidProjection("linearisation produced an invalid projection");
             cost += L.cost;
             const Terms tm = primaryTerms(o, o.state, ob.cam, L);
-            int blocks[3] = {tm.blocks[0], tm.blocks[1], -1};
-            const double* jp[3] = {tm.J[0], tm.J[1], nullptr};
+            int blocks[4] = {tm.blocks[0], tm.blocks[1], tm.blocks[2], -1};
+            const double* jp[4] = {tm.J[0], tm.J[1], tm.J[2], nullptr};
             int count = tm.count;
             double Jpp[2 * kP] = {0};
             if (prim >= 0) {
@@ -2081,6 +2223,72 @@ using namespace orc;
 
 extern "C" {
 
+// Rig topology (Problem::rig): composeRigCameras replaces every camera's pose by the composition of
+// its capture and sensor, R = R_rig R_sensor and C = C_rig + R_rig c_sensor (runConcreteBackend,
+// src/solver.cpp:282; the composition is stated in the reference's README, "Rig BA"); without
+// explicit calibration groups the cameras of one sensor share a group (makeSolverOptions,
+// Conversion.cpp:83-98); a camera whose capture and sensor are both fixed becomes a fixed camera
+// (:120-142).  The camera library that validates the topology is absent from the reference tree;
+// its checks are restated as: bindings to existing records of the same rig, proper rotations,
+// finite centres, a fixed sensor in every rig.
+int loadRig(Oracle& o, const orc_problem* pr) {
+    if (pr->n_rig_captures <= 0) return 0;
+    const int nc = static_cast<int>(o.inputCams.size());
+    if (pr->n_rig_sensors <= 0 || !pr->rig_captures || !pr->rig_capture_info || !pr->rig_sensors ||
+        !pr->rig_sensor_info || !pr->rig_camera_capture || !pr->rig_camera_sensor)
+        return InvalidInput;
+    auto properRotation = [](const double* R) {
+        for (int i = 0; i < 9; ++i)
+            if (!std::isfinite(R[i])) return false;
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) {
+                double v = 0.0;
+                for (int k = 0; k < 3; ++k) v += R[r * 3 + k] * R[c * 3 + k];
+                if (std::fabs(v - (r == c ? 1.0 : 0.0)) > 1e-9) return false;
+            }
+        const double det = R[0] * (R[4] * R[8] - R[5] * R[7]) - R[1] * (R[3] * R[8] - R[5] * R[6]) +
+                           R[2] * (R[3] * R[7] - R[4] * R[6]);
+        return std::fabs(det - 1.0) <= 1e-9;
+    };
+    auto load = [&](const double* rec, int n, std::vector<RigPose>& out) {
+        out.resize(static_cast<size_t>(n));
+        for (int i = 0; i < n; ++i) {
+            std::memcpy(out[i].R, rec + static_cast<size_t>(i) * 12, 9 * sizeof(double));
+            std::memcpy(out[i].C, rec + static_cast<size_t>(i) * 12 + 9, 3 * sizeof(double));
+            if (!properRotation(out[i].R) || !std::isfinite(out[i].C[0]) || !std::isfinite(out[i].C[1]) ||
+                !std::isfinite(out[i].C[2]))
+                return false;
+        }
+        return true;
+    };
+    if (!load(pr->rig_captures, pr->n_rig_captures, o.inputCaptures)) return InvalidInput;
+    if (!load(pr->rig_sensors, pr->n_rig_sensors, o.inputSensors)) return InvalidInput;
+    o.captureInfo.assign(pr->rig_capture_info, pr->rig_capture_info + 2 * pr->n_rig_captures);
+    o.sensorInfo.assign(pr->rig_sensor_info, pr->rig_sensor_info + 2 * pr->n_rig_sensors);
+    o.cameraCapture.assign(pr->rig_camera_capture, pr->rig_camera_capture + nc);
+    o.cameraSensor.assign(pr->rig_camera_sensor, pr->rig_camera_sensor + nc);
+    for (int c = 0; c < nc; ++c) {
+        const int k = o.cameraCapture[c], si = o.cameraSensor[c];
+        if (k < 0 || k >= pr->n_rig_captures || si < 0 || si >= pr->n_rig_sensors) return InvalidInput;
+        if (o.captureInfo[2 * k] != o.sensorInfo[2 * si]) return InvalidInput;
+    }
+    for (int k = 0; k < pr->n_rig_captures; ++k) {
+        bool fixedSensor = false;
+        for (int si = 0; si < pr->n_rig_sensors; ++si)
+            fixedSensor = fixedSensor || (o.sensorInfo[2 * si] == o.captureInfo[2 * k] && o.sensorInfo[2 * si + 1] != 0);
+        if (!fixedSensor) return InvalidInput;
+    }
+    o.hasRig = true;
+    for (int c = 0; c < nc; ++c)
+        composeRigCamera(o.inputCaptures[o.cameraCapture[c]], o.inputSensors[o.cameraSensor[c]], o.inputCams[c]);
+    if (o.groupIds.empty()) o.groupIds = o.cameraSensor;
+    for (int c = 0; c < nc; ++c)
+        if (o.captureInfo[2 * o.cameraCapture[c] + 1] && o.sensorInfo[2 * o.cameraSensor[c] + 1] &&
+            std::find(o.fixedCams.begin(), o.fixedCams.end(), c) == o.fixedCams.end())
+            o.fixedCams.push_back(c);
+    return 0;
+}
+
 void* orc_create(const orc_problem* pr, const orc_options* op, int32_t* status) {
     auto o = std::make_unique<Oracle>();
     o->opt = *op;
@@ -2108,6 +2316,7 @@ void* orc_create(const orc_problem* pr, const orc_options* op, int32_t* status) 
 #endif
     int st = 0;
     if (o->inputCams.empty() || o->nt() == 0) st = InvalidInput;
+    if (!st) st = loadRig(*o, pr);
     if (!st) st = loadControlPoints(*o, pr);
     if (!st) st = loadScaleBars(*o, pr);
     // a problem with scale bars has no online path (canUseReferenceOnlineSchur)
@@ -2117,6 +2326,8 @@ void* orc_create(const orc_problem* pr, const orc_options* op, int32_t* status) 
         prepareActive(*o);
         o->state.cams = o->inputCams;
         o->state.points = o->initialPoints;
+        o->state.captures = o->inputCaptures;
+        o->state.sensors = o->inputSensors;
         initGroups(*o);
         trackBoundaries(*o, std::max(1, std::min<int>(o->threads, static_cast<int>(o->nt()))));
     }
@@ -2125,6 +2336,35 @@ void* orc_create(const orc_problem* pr, const orc_options* op, int32_t* status) 
 }
 
 void orc_destroy(void* h) { delete static_cast<Oracle*>(h); }
+
+int32_t orc_rig(void* h, double* captures, double* sensors, int32_t* capture_block, int32_t* sensor_block) {
+    auto* o = static_cast<Oracle*>(h);
+    if (!o->hasRig) return InvalidInput;
+    const Active& a = o->active;
+    for (size_t k = 0; k < o->state.captures.size(); ++k) {
+        if (captures) {
+            std::memcpy(captures + k * 12, o->state.captures[k].R, 9 * sizeof(double));
+            std::memcpy(captures + k * 12 + 9, o->state.captures[k].C, 3 * sizeof(double));
+        }
+        if (capture_block) {
+            capture_block[k] = -1;
+            for (size_t c = 0; c < o->inputCams.size(); ++c)
+                if (a.rigCaptureIndexByCamera[c] == static_cast<int>(k)) capture_block[k] = a.rigCaptureBlockByCamera[c];
+        }
+    }
+    for (size_t si = 0; si < o->state.sensors.size(); ++si) {
+        if (sensors) {
+            std::memcpy(sensors + si * 12, o->state.sensors[si].R, 9 * sizeof(double));
+            std::memcpy(sensors + si * 12 + 9, o->state.sensors[si].C, 3 * sizeof(double));
+        }
+        if (sensor_block) {
+            sensor_block[si] = -1;
+            for (size_t c = 0; c < o->inputCams.size(); ++c)
+                if (a.rigSensorIndexByCamera[c] == static_cast<int>(si)) sensor_block[si] = a.rigSensorBlockByCamera[c];
+        }
+    }
+    return 0;
+}
 
 int32_t orc_control_point_whitening(const double* record, double* W) { return controlPointWhitening(record, W) ? 1 : 0; }
 

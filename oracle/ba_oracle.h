@@ -62,6 +62,17 @@ typedef struct orc_problem {
     int32_t n_scale_bars;
     const int32_t* scale_bar_tracks;
     const double* scale_bar_data;
+    /* rig topology (Problem::rig): captures (rigToWorldRotation 9, rigCenterInWorld 3) with
+     * (rigId, fixedPose), sensors (cameraToRigRotation 9, cameraCenterInRig 3) with (rigId,
+     * fixedExtrinsic), and the capture and sensor index of every camera; n_rig_captures == 0: none */
+    int32_t n_rig_captures;
+    const double* rig_captures;
+    const int32_t* rig_capture_info;
+    int32_t n_rig_sensors;
+    const double* rig_sensors;
+    const int32_t* rig_sensor_info;
+    const int32_t* rig_camera_capture;
+    const int32_t* rig_camera_sensor;
 } orc_problem;
 
 typedef struct orc_options {
@@ -161,6 +172,9 @@ int32_t orc_general_export(void* handle, double* primary_matrix, double* primary
 /* solveDampedSchurComplement restated on the built equations (dense FP64). */
 int32_t orc_general_solve(void* handle, double damping, double tolerance, double* primary_step,
                           double* eliminated_step, int32_t* converged);
+/* Rig problems: the current captures and sensors (12 doubles each) and the rig block of every
+ * capture and sensor (-1: none); returns InvalidInput without a rig. */
+int32_t orc_rig(void* handle, double* captures, double* sensors, int32_t* capture_block, int32_t* sensor_block);
 /* Full solve from the initial state. */
 int32_t orc_solve(void* handle, orc_report* report, double* cameras_out, double* points_out, int8_t* valid_out,
                   double* rms_before, double* rms_after, double* intrinsics_out);

@@ -28,7 +28,10 @@ class OrcProblem(C.Structure):
                 ("calibration_group_ids", C.c_void_p), ("intrinsic_reference_cameras", C.c_void_p),
                 ("n_control_points", C.c_int32), ("control_point_track", C.c_void_p),
                 ("control_point_data", C.c_void_p), ("n_scale_bars", C.c_int32), ("scale_bar_tracks", C.c_void_p),
-                ("scale_bar_data", C.c_void_p)]
+                ("scale_bar_data", C.c_void_p), ("n_rig_captures", C.c_int32), ("rig_captures", C.c_void_p),
+                ("rig_capture_info", C.c_void_p), ("n_rig_sensors", C.c_int32), ("rig_sensors", C.c_void_p),
+                ("rig_sensor_info", C.c_void_p), ("rig_camera_capture", C.c_void_p),
+                ("rig_camera_sensor", C.c_void_p)]
 
 
 class OrcOptions(C.Structure):
@@ -89,6 +92,7 @@ def lib():
         L.orc_general_export.argtypes = [C.c_void_p] + [C.c_void_p] * 6
         L.orc_general_solve.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_void_p, C.c_void_p,
                                         C.POINTER(C.c_int32)]
+        L.orc_rig.argtypes = [C.c_void_p] + [C.c_void_p] * 4
         L.orc_control_point_whitening.argtypes = [C.c_void_p, C.c_void_p]
         L.orc_control_point_whitening.restype = C.c_int32
         _lib = L
@@ -177,6 +181,19 @@ class Oracle:
                                cp_t.size, _ptr(cp_t) if cp_t.size else None, _ptr(cp_d) if cp_t.size else None,
                                sb_d.shape[0], _ptr(sb_t) if sb_d.shape[0] else None,
                                _ptr(sb_d) if sb_d.shape[0] else None)
+        rig = getattr(p, "rig", None)
+        if rig is not None and rig.captures:
+            arrs = rig.arrays(p.n_cameras)
+            self._keep += list(arrs)
+            cap, cap_info, sen, sen_info, cam_cap, cam_sen = arrs
+            self.desc.n_rig_captures = cap.shape[0]
+            self.desc.rig_captures = _ptr(cap)
+            self.desc.rig_capture_info = _ptr(cap_info)
+            self.desc.n_rig_sensors = sen.shape[0]
+            self.desc.rig_sensors = _ptr(sen)
+            self.desc.rig_sensor_info = _ptr(sen_info)
+            self.desc.rig_camera_capture = _ptr(cam_cap)
+            self.desc.rig_camera_sensor = _ptr(cam_sen)
         self.opts = make_options(options, num_threads, linear_solver, residual_gate)
         g = p.gauge
         self.opts.gauge_policy = int(g.policy)
@@ -316,5 +333,22 @@ class Oracle:
         intr = np.zeros((max(1, p.n_cameras), _P))
         lib().orc_solve(self.h, C.byref(rep), _ptr(cams), _ptr(pts), _ptr(valid), _ptr(rb), _ptr(ra), _ptr(intr))
         n_groups = self.info()["intrinsic_blocks"]
-        return {"report": rep.as_dict(), "cameras": cams, "points": pts, "valid": valid.astype(bool),
-                "rms_before": rb, "rms_after": ra, "intrinsics": intr[:n_groups]}
+        out = {"report": rep.as_dict(), "cameras": cams, "points": pts, "valid": valid.astype(bool),
+               "rms_before": rb, "rms_after": ra, "intrinsics": intr[:n_groups]}
+        rig = self.rig()
+        if rig is not None:
+            out.update(rig)
+        return out
+
+    def rig(self):
+        """Rig problems: current captures and sensors (12 doubles each) and their rig blocks."""
+        rig = getattr(self.problem, "rig", None)
+        if rig is None or not rig.captures:
+            return None
+        cap = np.zeros((len(rig.captures), 12))
+        sen = np.zeros((len(rig.sensors), 12))
+        kb = np.zeros(len(rig.captures), np.int32)
+        sb = np.zeros(len(rig.sensors), np.int32)
+        if lib().orc_rig(self.h, _ptr(cap), _ptr(sen), _ptr(kb), _ptr(sb)) != 0:
+            return None
+        return {"captures": cap, "sensors": sen, "capture_block": kb, "sensor_block": sb}

@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 OBJ_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libpbgpu.so")
-SOURCES = ["pb_host.cpp", "pb_assemble.cu", "pb_kernels.cu", "pb_pcg.cu", "pb_dense.cu", "pb_solver.cu", "pb_noalloc.cu", "pb_batch.cu", "pb_adjoint.cu", "pb_bne.cpp", "pb_schur.cu", "pb_survey.cu"]
+SOURCES = ["pb_host.cpp", "pb_assemble.cu", "pb_kernels.cu", "pb_pcg.cu", "pb_dense.cu", "pb_solver.cu", "pb_noalloc.cu", "pb_batch.cu", "pb_adjoint.cu", "pb_bne.cpp", "pb_schur.cu", "pb_survey.cu", "pb_rig.cu"]
 HEADERS = ["pb_internal.h", "pb_device.cuh", "pb_kernels.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -177,6 +177,221 @@ bool cp_valid(const double* data, double* W) {
     return cp_whitening(data, W);
 }
 
+namespace {
+
+// A rotation stored row-major is usable when it is finite and orthonormal with determinant +1
+// (to 1e-9 on every entry of R R^T - I and on det - 1).
+bool rotation_ok(const double* R) {
+    for (int i = 0; i < 9; ++i)
+        if (!std::isfinite(R[i])) return false;
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) {
+            const double v = R[r * 3] * R[c * 3] + R[r * 3 + 1] * R[c * 3 + 1] + R[r * 3 + 2] * R[c * 3 + 2];
+            if (std::fabs(v - (r == c ? 1.0 : 0.0)) > 1e-9) return false;
+        }
+    const double det = R[0] * (R[4] * R[8] - R[5] * R[7]) - R[1] * (R[3] * R[8] - R[5] * R[6]) +
+                       R[2] * (R[3] * R[7] - R[4] * R[6]);
+    return std::fabs(det - 1.0) <= 1e-9;
+}
+
+// The rig topology of the problem: its records, the binding of every camera, and the composed
+// camera poses R = R_rig R_sensor, C = C_rig + R_rig c_sensor written into the input cameras
+// (composeRigCameras, called by runConcreteBackend, src/solver.cpp:282; the README's "Rig BA"
+// states the composition).  The composition function lives in the camera library, which is not
+// part of the reference tree; its checks are restated: every camera bound to an existing capture
+// and sensor of the same rig, proper rotations, finite centres, and at least one fixed sensor in
+// every rig that has a capture (it defines the rig body frame).
+int load_rig(const pb_problem_desc* pr, HostModel* m, std::string* err) {
+    RigModel& R = m->rig;
+    R = RigModel{};
+    if (pr->n_rig_captures < 0 || pr->n_rig_sensors < 0) { *err = "rig record counts must be non-negative"; return PB_SOLVE_INVALID_INPUT; }
+    if (pr->n_rig_captures == 0) return 0;
+    if (pr->n_rig_sensors <= 0 || !pr->rig_captures || !pr->rig_capture_info || !pr->rig_sensors ||
+        !pr->rig_sensor_info || !pr->rig_camera_capture || !pr->rig_camera_sensor) {
+        *err = "rig topology arrays missing";
+        return PB_SOLVE_INVALID_INPUT;
+    }
+    R.on = true;
+    R.ncap = pr->n_rig_captures;
+    R.nsen = pr->n_rig_sensors;
+    R.cap_in.assign(pr->rig_captures, pr->rig_captures + static_cast<size_t>(R.ncap) * 12);
+    R.sen_in.assign(pr->rig_sensors, pr->rig_sensors + static_cast<size_t>(R.nsen) * 12);
+    R.cap_info.assign(pr->rig_capture_info, pr->rig_capture_info + static_cast<size_t>(R.ncap) * 2);
+    R.sen_info.assign(pr->rig_sensor_info, pr->rig_sensor_info + static_cast<size_t>(R.nsen) * 2);
+    for (int k = 0; k < R.ncap; ++k)
+        if (!rotation_ok(&R.cap_in[k * 12]) || !finite3(&R.cap_in[k * 12 + 9])) {
+            *err = "rig capture " + std::to_string(k) + " has an invalid pose";
+            return PB_SOLVE_INVALID_INPUT;
+        }
+    for (int s = 0; s < R.nsen; ++s)
+        if (!rotation_ok(&R.sen_in[s * 12]) || !finite3(&R.sen_in[s * 12 + 9])) {
+            *err = "rig sensor " + std::to_string(s) + " has an invalid extrinsic";
+            return PB_SOLVE_INVALID_INPUT;
+        }
+    R.cam_capture.assign(pr->rig_camera_capture, pr->rig_camera_capture + m->nc);
+    R.cam_sensor.assign(pr->rig_camera_sensor, pr->rig_camera_sensor + m->nc);
+    for (int c = 0; c < m->nc; ++c) {
+        const int k = R.cam_capture[c], s = R.cam_sensor[c];
+        if (k < 0 || k >= R.ncap || s < 0 || s >= R.nsen) {
+            *err = "camera " + std::to_string(c) + " has no rig binding";
+            return PB_SOLVE_INVALID_INPUT;
+        }
+        if (pr->rig_capture_info[2 * k] != pr->rig_sensor_info[2 * s]) {
+            *err = "camera " + std::to_string(c) + " binds a capture and a sensor of different rigs";
+            return PB_SOLVE_INVALID_INPUT;
+        }
+    }
+    for (int k = 0; k < R.ncap; ++k) {
+        const int rig = pr->rig_capture_info[2 * k];
+        bool fixed_sensor = false;
+        for (int s = 0; s < R.nsen && !fixed_sensor; ++s)
+            fixed_sensor = pr->rig_sensor_info[2 * s] == rig && pr->rig_sensor_info[2 * s + 1] != 0;
+        if (!fixed_sensor) {
+            *err = "rig " + std::to_string(rig) + " has no fixed sensor to define its body frame";
+            return PB_SOLVE_INVALID_INPUT;
+        }
+    }
+    for (int c = 0; c < m->nc; ++c) {
+        const double* cp = &R.cap_in[static_cast<size_t>(R.cam_capture[c]) * 12];
+        const double* sp = &R.sen_in[static_cast<size_t>(R.cam_sensor[c]) * 12];
+        double* cam = &m->cams_in[static_cast<size_t>(c) * kCamStride];
+        for (int r = 0; r < 3; ++r)
+            for (int q = 0; q < 3; ++q)
+                cam[r * 3 + q] = cp[r * 3] * sp[q] + cp[r * 3 + 1] * sp[3 + q] + cp[r * 3 + 2] * sp[6 + q];
+        for (int r = 0; r < 3; ++r)
+            cam[9 + r] = cp[9 + r] + cp[r * 3] * sp[9] + cp[r * 3 + 1] * sp[10] + cp[r * 3 + 2] * sp[11];
+    }
+    return 0;
+}
+
+// Rig problems: the reference's block pairs over the rig numbering (prepareOffDiagonalTopology,
+// BundleAdjustPlaMatrixReferenceSchur.cpp:568-659: the capture, sensor and intrinsic blocks of an
+// observation pairwise, and all blocks of the observations of an eliminated track), the CSR of the
+// rig pose blocks, and the term lists that map the camera-block system onto it.  A camera block a
+// (camera c) enters the rig system through its capture block with Mc and its sensor block with
+// Ms, so rig block (I, J) = sum over camera-block CSR entries (a, b), I in chain(a), J in chain(b),
+// of M_aI^T S_ab M_bJ.
+void build_rig_pattern(HostModel* m, const std::vector<unsigned char>& use) {
+    RigModel& R = m->rig;
+    const int P = R.P, nrb = R.nrb, nc = m->nc;
+    std::vector<int> intr(nc, -1), cb(nc, -1), sb(nc, -1);
+    for (int c = 0; c < nc; ++c) {
+        if (m->intrinsic_block[c] >= 0) intr[c] = nrb + m->calib_group[c];
+        if (!R.capture_block.empty()) {
+            cb[c] = R.capture_block[R.cam_capture[c]];
+            sb[c] = R.sensor_block[R.cam_sensor[c]];
+        }
+    }
+    std::vector<char> bits(static_cast<size_t>(P) * P, 0);
+    auto connect = [&](int a, int b) {
+        if (a < 0 || b < 0 || a == b) return;
+        bits[static_cast<size_t>(std::min(a, b)) * P + std::max(a, b)] = 1;
+    };
+    std::vector<int> tb;
+    for (int t = 0; t < m->nt; ++t) {
+        if (!m->active_track[t]) continue;
+        tb.clear();
+        for (long long k = m->offs[t]; k < m->offs[t + 1]; ++k) {
+            if (!use[k]) continue;
+            const int c = m->obs_cam[k];
+            const int ob[3] = {cb[c], sb[c], intr[c]};
+            connect(ob[0], ob[1]);
+            connect(ob[0], ob[2]);
+            connect(ob[1], ob[2]);
+            if (m->track_block[t] >= 0)
+                for (int v : ob)
+                    if (v >= 0) tb.push_back(v);
+        }
+        if (m->track_block[t] < 0) continue;
+        std::sort(tb.begin(), tb.end());
+        tb.erase(std::unique(tb.begin(), tb.end()), tb.end());
+        for (size_t l = 0; l < tb.size(); ++l)
+            for (size_t r = l + 1; r < tb.size(); ++r) connect(tb[l], tb[r]);
+    }
+    R.pairs.clear();
+    for (int r = 0; r < P; ++r)
+        for (int q = r + 1; q < P; ++q)
+            if (bits[static_cast<size_t>(r) * P + q]) R.pairs.emplace_back(r, q);
+    // rig pose CSR: the pose-pose pairs plus the diagonal
+    std::vector<std::vector<int>> rows(nrb);
+    for (int i = 0; i < nrb; ++i) rows[i].push_back(i);
+    for (const auto& pq : R.pairs)
+        if (pq.second < nrb) {
+            rows[pq.first].push_back(pq.second);
+            rows[pq.second].push_back(pq.first);
+        }
+    R.row_ptr.assign(nrb + 1, 0);
+    R.col_idx.clear();
+    R.diag_pos.assign(nrb, -1);
+    for (int i = 0; i < nrb; ++i) {
+        std::sort(rows[i].begin(), rows[i].end());
+        for (int c : rows[i]) {
+            if (c == i) R.diag_pos[i] = static_cast<int>(R.col_idx.size());
+            R.col_idx.push_back(c);
+        }
+        R.row_ptr[i + 1] = static_cast<int>(R.col_idx.size());
+    }
+    auto csr_pos = [&](int i, int j) {
+        const int* b = R.col_idx.data() + R.row_ptr[i];
+        const int* e = R.col_idx.data() + R.row_ptr[i + 1];
+        const int* f = std::lower_bound(b, e, j);
+        return (f != e && *f == j) ? static_cast<int>(f - R.col_idx.data()) : -1;
+    };
+    // upper rig blocks and their terms, in CSR order
+    R.up_pos.clear();
+    R.up_tpos.clear();
+    std::vector<int> up_of(R.col_idx.size(), -1);
+    for (int i = 0; i < nrb; ++i)
+        for (int p = R.row_ptr[i]; p < R.row_ptr[i + 1]; ++p) {
+            const int j = R.col_idx[p];
+            if (j < i) continue;
+            up_of[p] = static_cast<int>(R.up_pos.size());
+            R.up_pos.push_back(p);
+            R.up_tpos.push_back(j == i ? -1 : csr_pos(j, i));
+        }
+    const int nup = static_cast<int>(R.up_pos.size());
+    std::vector<std::vector<int>> lists(nup);
+    const int ncb = m->ncb;
+    for (int a = 0; a < ncb; ++a) {
+        const int ca[2] = {R.cb_cap_block[a], R.cb_sen_block[a]};
+        for (int p = m->row_ptr[a]; p < m->row_ptr[a + 1]; ++p) {
+            const int b = m->col_idx[p];
+            const int cbk[2] = {R.cb_cap_block[b], R.cb_sen_block[b]};
+            for (int sa = 0; sa < 2; ++sa)
+                for (int sbk = 0; sbk < 2; ++sbk) {
+                    const int I = ca[sa], J = cbk[sbk];
+                    if (I < 0 || J < 0 || I > J) continue;
+                    const int q = csr_pos(I, J);
+                    // every pair of chained blocks is in the reference topology: a miss would be a
+                    // planner bug, and the term is then dropped rather than written out of bounds
+                    if (q < 0) continue;
+                    lists[up_of[q]].push_back(p);
+                    lists[up_of[q]].push_back(a << 2 | sa << 1 | sbk);
+                }
+        }
+    }
+    R.term_begin.assign(nup + 1, 0);
+    R.terms.clear();
+    for (int u = 0; u < nup; ++u) {
+        R.terms.insert(R.terms.end(), lists[u].begin(), lists[u].end());
+        R.term_begin[u + 1] = static_cast<int>(R.terms.size() / 2);
+    }
+    // camera blocks per rig block
+    std::vector<std::vector<int>> per(nrb);
+    for (int a = 0; a < ncb; ++a) {
+        if (R.cb_cap_block[a] >= 0) per[R.cb_cap_block[a]].push_back(a << 1);
+        if (R.cb_sen_block[a] >= 0) per[R.cb_sen_block[a]].push_back(a << 1 | 1);
+    }
+    R.blk_begin.assign(nrb + 1, 0);
+    R.blk_items.clear();
+    for (int i = 0; i < nrb; ++i) {
+        R.blk_items.insert(R.blk_items.end(), per[i].begin(), per[i].end());
+        R.blk_begin[i + 1] = static_cast<int>(R.blk_items.size());
+    }
+}
+
+}  // namespace
+
 int build_host_model(const pb_problem_desc* pr, const pb_solve_options* op, HostModel* m, std::string* err) {
     if (!pr || !op) { *err = "null problem or options"; return PB_SOLVE_INVALID_INPUT; }
     if (pr->n_cameras <= 0 || pr->n_tracks <= 0 || !pr->cameras || !pr->track_offsets || !pr->points) {
@@ -210,6 +425,21 @@ int build_host_model(const pb_problem_desc* pr, const pb_solve_options* op, Host
     m->group_ids = pr->calibration_group_ids
                        ? std::vector<int>(pr->calibration_group_ids, pr->calibration_group_ids + m->nc)
                        : std::vector<int>();
+    // --- rig topology: composed camera poses; without explicit calibration groups the cameras of
+    // one sensor share one intrinsic block (makeSolverOptions, Conversion.cpp:83-98); a camera
+    // whose capture pose and sensor extrinsic are both fixed is a fixed camera (:120-142)
+    {
+        const int rc = load_rig(pr, m, err);
+        if (rc) return rc;
+        const RigModel& R = m->rig;
+        if (R.on) {
+            if (m->group_ids.empty()) m->group_ids = R.cam_sensor;
+            for (int c = 0; c < m->nc; ++c)
+                if (R.cap_info[2 * R.cam_capture[c] + 1] && R.sen_info[2 * R.cam_sensor[c] + 1] &&
+                    std::find(m->fixed_cams.begin(), m->fixed_cams.end(), c) == m->fixed_cams.end())
+                    m->fixed_cams.push_back(c);
+        }
+    }
     for (int c = 0; c < m->nc; ++c) {
         const double* cam = &m->cams_in[static_cast<size_t>(c) * kCamStride];
         for (int i = 0; i < 21; ++i)
@@ -240,7 +470,9 @@ int build_host_model(const pb_problem_desc* pr, const pb_solve_options* op, Host
     // BundleAdjustPlaMatrixConstraints.cpp:90-116)
     m->cp_track.clear();
     m->cp_rec.clear();
-    m->ref_param = pr->n_control_points <= 0;
+    // a rig selects the plain parameterisation (useReferencePointParameterization,
+    // BundleAdjustPlaMatrixAssembly.cpp:24-30)
+    m->ref_param = pr->n_control_points <= 0 && !m->rig.on;
     m->cp_huber = op->control_point_huber_delta;
     std::vector<double> cp_points;  // valid targets of tracks with usable observations
     std::vector<char> cp_usable_track;
@@ -472,9 +704,44 @@ int build_host_model(const pb_problem_desc* pr, const pb_solve_options* op, Host
             for (long long k = m->offs[t]; k < m->offs[t + 1]; ++k)
                 if (usable(k)) cam_has_residual[m->obs_cam[k]] = 1;
     m->ncb = 0;
-    if (op->refine_camera_pose)
+    RigModel& rig = m->rig;
+    if (op->refine_camera_pose && !rig.on) {
         for (int c = 0; c < nc; ++c)
             if (cam_has_residual[c] && !fixed_cam[c]) m->camera_block[c] = m->ncb++;
+    } else if (op->refine_camera_pose) {
+        // rig blocks (BundleAdjustPlaMatrixProblem.cpp:156-199): a capture with residuals gets a
+        // block unless it is fixed, one of its cameras is fixed, or it holds the gauge scale
+        // camera; a sensor with residuals gets one unless its extrinsic is fixed; sensor blocks
+        // follow the capture blocks
+        rig.capture_block.assign(rig.ncap, -1);
+        rig.sensor_block.assign(rig.nsen, -1);
+        std::vector<char> cap_res(rig.ncap, 0), cap_fixed(rig.ncap, 0), sen_res(rig.nsen, 0);
+        for (int k = 0; k < rig.ncap; ++k) cap_fixed[k] = rig.cap_info[2 * k + 1] != 0;
+        for (int c = 0; c < nc; ++c) {
+            const int k = rig.cam_capture[c], s = rig.cam_sensor[c];
+            cap_res[k] = cap_res[k] || cam_has_residual[c];
+            cap_fixed[k] = cap_fixed[k] || fixed_cam[c] || c == m->gauge_scale;
+            sen_res[s] = sen_res[s] || cam_has_residual[c];
+        }
+        rig.ncapb = rig.nsenb = 0;
+        for (int k = 0; k < rig.ncap; ++k)
+            if (cap_res[k] && !cap_fixed[k]) rig.capture_block[k] = rig.ncapb++;
+        for (int s = 0; s < rig.nsen; ++s)
+            if (sen_res[s] && !rig.sen_info[2 * s + 1]) rig.sensor_block[s] = rig.ncapb + rig.nsenb++;
+        rig.nrb = rig.ncapb + rig.nsenb;
+        // camera blocks of the kernels: every camera with residuals whose pose has a free part
+        rig.cb_camera.clear();
+        rig.cb_cap_block.clear();
+        rig.cb_sen_block.clear();
+        for (int c = 0; c < nc; ++c) {
+            const int kb = rig.capture_block[rig.cam_capture[c]], sb = rig.sensor_block[rig.cam_sensor[c]];
+            if (!cam_has_residual[c] || (kb < 0 && sb < 0)) continue;
+            m->camera_block[c] = m->ncb++;
+            rig.cb_camera.push_back(c);
+            rig.cb_cap_block.push_back(kb);
+            rig.cb_sen_block.push_back(sb);
+        }
+    }
     m->P = m->ncb;
     m->ng = 0;
     m->ni = 0;
@@ -517,6 +784,7 @@ int build_host_model(const pb_problem_desc* pr, const pb_solve_options* op, Host
         }
     }
     m->P += m->npr;
+    if (rig.on) rig.P = rig.nrb + m->ng + m->npr;
 
     // --- intrinsic groups (initializeIntrinsicGroups, BundleAdjustPlaMatrixModel.cpp:84-231)
     m->groups.assign(m->ng, HostGroup{});
@@ -677,6 +945,7 @@ int build_host_model(const pb_problem_desc* pr, const pb_solve_options* op, Host
                 }
                 m->up_csr_t.push_back(pt);
             }
+        if (rig.on) build_rig_pattern(m, use);
     }
 
     // --- processing order: active tracks sorted by their smallest pose block so that a chunk of
@@ -747,6 +1016,13 @@ int build_host_model(const pb_problem_desc* pr, const pb_solve_options* op, Host
         mix(nc); mix(nt); mix(m->no); mix(m->ncb); mix(m->ng); mix(m->ni);
         for (size_t i = 0; i < m->p_obs_orig.size(); ++i) { mix(m->p_obs_orig[i]); mix(m->obs_cam[m->p_obs_orig[i]]); }
         for (int t : m->trk_order) mix(t);
+        if (m->rig.on) {
+            const RigModel& R = m->rig;
+            mix(R.nrb);
+            for (int c = 0; c < nc; ++c) { mix(R.cam_capture[c]); mix(R.cam_sensor[c]); }
+            for (int v : R.capture_block) mix(v);
+            for (int v : R.sensor_block) mix(v);
+        }
         m->structure_hash = static_cast<long long>(h);
     }
     m->chunks_ready[0] = m->chunks_ready[1] = false;

@@ -48,6 +48,7 @@ struct Shape {
     int nbar;            // scale bars
     double bar_huber;    // Huber delta of the scale-bar residuals (m)
     float loss_scale_hi, loss_scale_lo;  // loss_scale as float-float (mixed-path linearisation)
+    int rig;             // 1: camera blocks are chained to rig blocks (no gauge tangent, damping after the map)
 };
 
 // float-float pair (hi, lo) of device state copies: CUDA's float2 in device code, a struct of the
@@ -156,6 +157,33 @@ struct ChunkSet {
     int n() const { return static_cast<int>(obs_begin.empty() ? 0 : obs_begin.size() - 1); }
 };
 
+// Rig topology of a problem and the map of the camera-block reduced system onto the rig's pose
+// blocks.  Rig blocks: captures 0 .. ncapb - 1, then sensors ncapb .. nrb - 1.
+struct RigModel {
+    bool on = false;
+    int ncap = 0, nsen = 0;
+    std::vector<double> cap_in, sen_in;            // 12 per capture / sensor (input)
+    std::vector<int> cap_info, sen_info;           // 2 per capture / sensor: rig id, fixed flag
+    std::vector<int> cam_capture, cam_sensor;      // per camera
+    std::vector<int> capture_block, sensor_block;  // per capture / sensor: rig block, or -1
+    int ncapb = 0, nsenb = 0, nrb = 0;
+    // per camera block (kernel numbering): its camera, rig blocks of its capture and sensor (-1)
+    std::vector<int> cb_camera, cb_cap_block, cb_sen_block;
+    // CSR of the rig pose blocks (both triangles, diagonal always present)
+    std::vector<int> row_ptr, col_idx, diag_pos;
+    // per upper rig block (row-major over the CSR, i <= j): its CSR position, the position of its
+    // transpose (-1 on the diagonal), and its terms [term_begin[u], term_begin[u + 1]): camera
+    // block CSR positions p of blocks (a, b) with the rig block's row in a's chain and its column
+    // in b's, two ints each: p, then a << 2 | (row is a's sensor) << 1 | (column is b's sensor)
+    std::vector<int> up_pos, up_tpos, term_begin, terms;
+    // per rig block: the camera blocks chained to it, coded a << 1 | (the block is a's sensor)
+    std::vector<int> blk_begin, blk_items;
+    // the reference's numbering: primary blocks (rig blocks, groups, promoted points) and the
+    // upper block pairs of prepareOffDiagonalTopology over them
+    int P = 0;
+    std::vector<std::pair<int, int>> pairs;
+};
+
 struct HostModel {
     int nc = 0, nt = 0;
     long long no = 0;
@@ -183,6 +211,11 @@ struct HostModel {
     std::vector<int> track_prom;  // original track -> promoted index, or -1
     int npr = 0;
     bool force_general = false;   // scale bars: the online path is not available
+    // rig topology (Problem::rig).  The assembly runs on one 6-column pose block per camera with
+    // a free capture or sensor (a "camera block" of the kernels, camera_block[c]); the reduced
+    // system is then mapped to the pose blocks of the rig (captures, then sensors) by the
+    // per-camera chain rule J_capture = J_camera Mc, J_sensor = J_camera Ms (pb_rig.cu).
+    RigModel rig;
     int gauge_anchor = -1, gauge_scale = -1;
     double gauge_baseline = 0.0;
     int loss = 0;

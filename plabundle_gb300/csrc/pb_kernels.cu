@@ -141,7 +141,8 @@ __global__ void k_finalize(Shape S, DevPtrs D, double* __restrict__ vals, double
                            double* __restrict__ rhs_b, double* __restrict__ direct_b, double* __restrict__ result,
                            double damping) {
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-    if (tid < S.ncb * 6) {
+    // rig problems damp the diagonal of the rig pose blocks after the map (pb_rig.cu) instead
+    if (tid < S.ncb * 6 && !S.rig) {
         const int i = tid / 6, a = tid - i * 6;
         double* d = vals + static_cast<size_t>(D.diag_pos[i]) * 36 + a * 7;
         const double v = *d;
@@ -789,10 +790,12 @@ void launch_effective(const Shape& S, const DevPtrs& D, cudaStream_t st) {
 }
 
 void launch_cost(const Shape& S, const DevPtrs& D, const double* step_c, const double* step_p, const double* alphas,
-                 int n_alpha, int use_trial, double* part, double* out, cudaStream_t st) {
+                 int n_alpha, int use_trial, double* part, double* out, cudaStream_t st, const RigDev* rig) {
     if (use_trial) {
         const int n = n_alpha * S.nc;
         k_trial_cameras<<<(n + 127) / 128, 128, 0, st>>>(S, D, step_c, alphas, n_alpha);
+        // rig cameras: poses composed from the trial captures and sensors
+        if (rig) launch_rig_trial(*rig, S.nc, alphas, n_alpha, D.cams_trial, st);
     }
     const int nblk = static_cast<int>(std::max<long long>(1, (S.nop + 255) / 256));
     k_cost_batch<<<nblk, 256, 0, st>>>(S, D, step_p, alphas, n_alpha, use_trial, part);

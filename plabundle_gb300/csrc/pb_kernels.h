@@ -82,8 +82,60 @@ void launch_linearize_export(const Shape& S, const DevPtrs& D, double* res, doub
 void pb_set_assemble_smem_f32(size_t bytes);
 void pb_set_assemble_smem_f64(size_t bytes);
 void launch_effective(const Shape& S, const DevPtrs& D, cudaStream_t st);
+// Rig problems (pb_rig.cu): capture and sensor state, the chain maps of the camera blocks and the
+// reduced system over the rig's pose blocks (captures, then sensors).
+struct RigDev {
+    int ncap, nsen, nrb, ncb, nup, nnzb;
+    double* cap_state;   // ncap * 12: rotation (9), centre (3)
+    double* sen_state;   // nsen * 12
+    double* cap_input;
+    double* sen_input;
+    double* cap_trial;   // kMaxAlpha * ncap * 12
+    double* sen_trial;   // kMaxAlpha * nsen * 12
+    double* cap_saved;   // snapshots of pb_gpu_save_state
+    double* sen_saved;
+    int* cam_capture;    // nc
+    int* cam_sensor;     // nc
+    int* capture_block;  // ncap: rig block or -1
+    int* sensor_block;   // nsen
+    int* cb_camera;      // ncb: camera of each camera block
+    int* cb_cap;         // ncb: capture rig block, or -1
+    int* cb_sen;         // ncb: sensor rig block, or -1
+    double* maps;        // ncb * 72: Mc (6x6 row-major, camera delta = Mc capture delta), then Ms
+    // rig pose CSR and the term lists of the map (see RigModel)
+    int* row_ptr;
+    int* col_idx;
+    int* diag_pos;
+    int* up_pos;
+    int* up_tpos;
+    int* term_begin;
+    int* terms;          // 2 per term: camera-block CSR position, a << 2 | sensor row << 1 | sensor column
+    const int* cb_col_idx;  // column indices of the camera-block CSR
+    int* blk_begin;
+    int* blk_items;
+    // the rig system: pose blocks, border (6 nrb x nbw) and its transpose, right-hand side
+    double* vals;
+    double* border;
+    double* border_t;
+    double* rhs;
+    double* xv;          // the solution mapped back to camera blocks (6 ncb + nbw)
+    double* step_r;      // the rig solution (6 nrb + nbw), read by the trial states
+    double* sq;          // squared sum of the rig solution's pose and intrinsic entries
+};
+void launch_rig_maps(const RigDev& R, cudaStream_t st);
+// The camera-block system (vals, border of width nbw, rhs of 6 ncb + nbw) onto the rig blocks;
+// the rig pose diagonal damped by finalizePrimaryDiagonal(1 + damping, 1).
+void launch_rig_transform(const RigDev& R, const double* vals, const double* border, const double* rhs, int nbw,
+                          double damping, cudaStream_t st);
+// xr (6 nrb + nbw) -> R.xv (6 ncb + nbw), R.step_r = xr, R.sq = sum of xr^2 over 6 nrb + nglob.
+void launch_rig_expand(const RigDev& R, const double* xr, int nbw, int nglob, cudaStream_t st);
+// Trial captures, sensors and composed camera poses (pose entries 0-11 of the trial cameras).
+void launch_rig_trial(const RigDev& R, int nc, const double* alphas, int n_alpha, double* cams_trial, cudaStream_t st);
+void launch_rig_accept(const RigDev& R, int a, cudaStream_t st);
+
 void launch_cost(const Shape& S, const DevPtrs& D, const double* step_c, const double* step_p, const double* alphas,
-                 int n_alpha, int use_trial, double* part, double* out, cudaStream_t st);
+                 int n_alpha, int use_trial, double* part, double* out, cudaStream_t st,
+                 const RigDev* rig = nullptr);
 void launch_accept(const Shape& S, const DevPtrs& D, const double* step_p, double alpha, int a, cudaStream_t st);
 // Scale bars (pb_survey.cu): the extended system of the current state (`flags` bit 2: a promoted
 // observation did not project; `bar_cost`: the bars' robust cost), the split of its solution into

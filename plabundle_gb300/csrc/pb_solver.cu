@@ -182,6 +182,10 @@ struct pb_gpu_ctx {
     PcgSystem<double> sysx{};
     int* ext_flags = nullptr;
     double* bar_d = nullptr;  // bar cost of the current state, then of the trial states
+    // rigs: capture / sensor state and the reduced system over the rig's pose blocks (pb_rig.cu)
+    bool rig_on = false;
+    RigDev rig{};
+    PcgSystem<double> sysr{};
 };
 
 namespace {
@@ -236,9 +240,12 @@ void upload_structure(pb_gpu_ctx* c) {
     S.nnzb = static_cast<int>(m.col_idx.size());
     S.loss = m.loss;
     S.loss_scale = m.loss_scale;
-    S.gauge_anchor = m.gauge_anchor;
-    S.gauge_scale = m.gauge_scale;
-    S.gauge_baseline = m.gauge_baseline;
+    // a rig camera never takes the gauge tangent (cameraPosePrimaryTerms,
+    // BundleAdjustPlaMatrixAssembly.cpp:204): the capture of the scale camera is fixed instead
+    S.rig = m.rig.on ? 1 : 0;
+    S.gauge_anchor = m.rig.on ? -1 : m.gauge_anchor;
+    S.gauge_scale = m.rig.on ? -1 : m.gauge_scale;
+    S.gauge_baseline = m.rig.on ? 0.0 : m.gauge_baseline;
     for (int i = 0; i < kMaxNI; ++i) S.int_cols[i] = i < m.ni ? m.int_cols[i] : 0;
     S.ref_param = m.ref_param ? 1 : 0;
     S.ncp = static_cast<int>(m.cp_proc.size() / 12);
@@ -434,6 +441,68 @@ void upload_structure(pb_gpu_ctx* c) {
         c->ext_flags = A.alloc<int>(1);
         c->bar_d = A.alloc<double>(kMaxAlpha + 2);  // [0] current, [1 .. kMaxAlpha] trials, then the step sum
     }
+    c->rig_on = m.rig.on;
+    if (c->rig_on) {
+        const RigModel& rm = m.rig;
+        RigDev& R = c->rig;
+        R = RigDev{};
+        R.ncap = rm.ncap;
+        R.nsen = rm.nsen;
+        R.nrb = rm.nrb;
+        R.ncb = m.ncb;
+        R.nup = static_cast<int>(rm.up_pos.size());
+        R.nnzb = static_cast<int>(rm.col_idx.size());
+        R.cap_input = upload_new(A, rm.cap_in, st);
+        R.sen_input = upload_new(A, rm.sen_in, st);
+        R.cap_state = A.alloc<double>(rm.cap_in.size());
+        R.sen_state = A.alloc<double>(rm.sen_in.size());
+        R.cap_trial = A.alloc<double>(static_cast<size_t>(kMaxAlpha) * rm.cap_in.size());
+        R.sen_trial = A.alloc<double>(static_cast<size_t>(kMaxAlpha) * rm.sen_in.size());
+        R.cap_saved = A.alloc<double>(rm.cap_in.size());
+        R.sen_saved = A.alloc<double>(rm.sen_in.size());
+        R.cam_capture = upload_new(A, rm.cam_capture, st);
+        R.cam_sensor = upload_new(A, rm.cam_sensor, st);
+        std::vector<int> kb = rm.capture_block, sb = rm.sensor_block;
+        if (kb.empty()) kb.assign(rm.ncap, -1);
+        if (sb.empty()) sb.assign(rm.nsen, -1);
+        R.capture_block = upload_new(A, kb, st);
+        R.sensor_block = upload_new(A, sb, st);
+        R.cb_camera = upload_new(A, rm.cb_camera, st);
+        R.cb_cap = upload_new(A, rm.cb_cap_block, st);
+        R.cb_sen = upload_new(A, rm.cb_sen_block, st);
+        R.maps = A.alloc<double>(static_cast<size_t>(std::max(1, m.ncb)) * 72);
+        R.row_ptr = upload_new(A, rm.row_ptr, st);
+        R.col_idx = upload_new(A, rm.col_idx, st);
+        R.diag_pos = upload_new(A, rm.diag_pos, st);
+        R.up_pos = upload_new(A, rm.up_pos, st);
+        R.up_tpos = upload_new(A, rm.up_tpos, st);
+        R.term_begin = upload_new(A, rm.term_begin, st);
+        R.terms = upload_new(A, rm.terms, st);
+        R.cb_col_idx = D.col_idx;
+        R.blk_begin = upload_new(A, rm.blk_begin, st);
+        R.blk_items = upload_new(A, rm.blk_items, st);
+        const int nbw = c->ext_on ? c->ext.nbx : S.nb;
+        const size_t nr6 = static_cast<size_t>(6) * rm.nrb;
+        R.vals = A.alloc<double>(static_cast<size_t>(std::max(1, R.nnzb)) * 36);
+        R.border = A.alloc<double>(std::max<size_t>(1, nr6 * nbw));
+        R.border_t = A.alloc<double>(std::max<size_t>(1, nr6 * nbw));
+        R.rhs = A.alloc<double>(nr6 + nbw + 1);
+        R.xv = A.alloc<double>(static_cast<size_t>(6) * m.ncb + nbw + 1);
+        R.step_r = A.alloc<double>(nr6 + nbw + 1);
+        R.sq = A.alloc<double>(1);
+        check(cudaMemsetAsync(R.step_r, 0, (nr6 + nbw + 1) * sizeof(double), st), "memset");
+        PcgSystem<double>& sr = c->sysr;
+        sr = c->ext_on ? c->sysx : sy;
+        sr.ncb = rm.nrb;
+        sr.nb = nbw;
+        sr.row_ptr = R.row_ptr;
+        sr.col_idx = R.col_idx;
+        sr.diag_pos = R.diag_pos;
+        sr.vals = R.vals;
+        sr.border = R.border;
+        sr.border_t = R.border_t;
+        sr.Dinv = A.alloc<double>(static_cast<size_t>(std::max(1, rm.nrb)) * 36);
+    }
     c->pcg_grid = pcg_grid_size<double>(S.ncb);
     c->S[0] = c->S[1] = S;
     c->D[0] = c->D[1] = D;
@@ -510,6 +579,40 @@ void ensure_pcg_partials(pb_gpu_ctx* c) {
 void set_assemble_smem(int precision, size_t bytes);
 double extend_system(pb_gpu_ctx* c, double damping);
 
+// Accepts trial `slot` (step length alpha): cameras, groups, points and, for rigs, captures and
+// sensors.
+void accept_trial(pb_gpu_ctx* c, double alpha, int slot) {
+    launch_accept(c->S[0], c->D[0], c->step_p, alpha, slot, c->stream);
+    c->launches += 1;
+    if (c->rig_on) {
+        launch_rig_accept(c->rig, slot, c->stream);
+        c->launches += 1;
+    }
+}
+
+// Rigs: the chain maps at the current state and the rig system of the last assembly.
+void rig_transform(pb_gpu_ctx* c, double damping) {
+    const Shape& S = c->S[0];
+    const int nbw = c->ext_on ? c->ext.nbx : S.nb;
+    launch_rig_maps(c->rig, c->stream);
+    launch_rig_transform(c->rig, c->red.vals, c->ext_on ? c->ext.border : c->red.border,
+                         c->ext_on ? c->ext.rhs : c->red.rhs, nbw, damping, c->stream);
+    c->launches += 2;
+    check(cudaGetLastError(), "rig map launch");
+}
+
+// The solution of the solved system in camera-block numbering: the rig solution mapped back
+// (and its squared sum kept for the step RMS), or the solution itself.
+const double* camera_block_solution(pb_gpu_ctx* c, const double* x) {
+    if (!c->rig_on) return x;
+    const Shape& S = c->S[0];
+    const int nbw = c->ext_on ? c->ext.nbx : S.nb;
+    launch_rig_expand(c->rig, x, nbw, S.nb, c->stream);
+    c->launches += 2;
+    check(cudaGetLastError(), "rig expand launch");
+    return c->rig.xv;
+}
+
 struct Timer {
     pb_gpu_ctx* c;
     int slot;
@@ -555,6 +658,8 @@ void assemble(pb_gpu_ctx* c, double damping, int precision, double* cost, int* f
     // scale bars: every assembly extends the reduced system by the promoted points and adds the
     // bars' cost, so that every solve of this context sees the extended system
     if (c->ext_on && !(*flags & 6)) *cost += extend_system(c, damping);
+    // rigs: the camera-block system onto the rig's pose blocks, damped there
+    if (c->rig_on && !(*flags & 6)) rig_transform(c, damping);
 }
 
 // Reduced solve.  Returns 0 ok, 1 breakdown / not positive definite (retried by the LM driver
@@ -574,12 +679,16 @@ void ensure_dense(pb_gpu_ctx* c) {
     DenseWork<T>& W = dwork<T>(c);
     const Shape& S = c->S[0];
     DeviceArena& A = c->darena;
-    // the system solved: the reduced one, or its extension by promoted points (scale bars)
-    const int nsol = c->ext_on ? c->ext.nx : S.n, nbsol = c->ext_on ? c->ext.nbx : S.nb;
+    // the system solved: the reduced one, its extension by promoted points (scale bars), or
+    // either mapped onto the rig's pose blocks
+    const int nbsol = c->ext_on ? c->ext.nbx : S.nb;
+    const int npose = c->rig_on ? c->model.rig.nrb : S.ncb;
+    const std::vector<int>& prow = c->rig_on ? c->model.rig.row_ptr : c->model.row_ptr;
+    const int nsol = 6 * npose + nbsol;
     W.n = nsol;
     W.nt = std::max(1, (nsol + 63) / 64);
     W.np = W.nt * 64;
-    W.nnzb = S.nnzb;
+    W.nnzb = c->rig_on ? c->rig.nnzb : S.nnzb;
     W.A = A.alloc<T>(static_cast<size_t>(W.np) * W.np);
     W.X = A.alloc<T>(static_cast<size_t>(W.np) * W.np);
     W.Dinv = A.alloc<T>(static_cast<size_t>(W.nt) * 64 * 64);
@@ -594,10 +703,10 @@ void ensure_dense(pb_gpu_ctx* c) {
         // SpMV work items of the CG: 32 pose blocks per item (the longest block row sets the
         // items per row), 256 entries of a border row per item
         int longest = 0;
-        for (int r = 0; r < S.ncb; ++r) longest = std::max(longest, c->model.row_ptr[r + 1] - c->model.row_ptr[r]);
-        W.pose_seg = S.ncb > 0 ? std::max(1, (longest + 31) / 32) : 0;
+        for (int r = 0; r < npose; ++r) longest = std::max(longest, prow[r + 1] - prow[r]);
+        W.pose_seg = npose > 0 ? std::max(1, (longest + 31) / 32) : 0;
         W.border_seg = nbsol > 0 ? (nsol + 255) / 256 : 0;
-        W.qpart = A.alloc<double>(std::max<size_t>(1, 6 * static_cast<size_t>(S.ncb) * W.pose_seg +
+        W.qpart = A.alloc<double>(std::max<size_t>(1, 6 * static_cast<size_t>(npose) * W.pose_seg +
                                                           static_cast<size_t>(nbsol) * W.border_seg));
     }
     W.w = A.alloc<double>(W.n);
@@ -629,8 +738,8 @@ int solve_dense(pb_gpu_ctx* c, double rel, double abs_tol, int max_it, bool* con
     ensure_dense<T>(c);
     DenseWork<T>& W = dwork<T>(c);
     const bool f32 = std::is_same<T, float>::value;
-    const PcgSystem<double>& sys = c->ext_on ? c->sysx : c->sys;
-    const double* rhs = c->ext_on ? c->ext.rhs : c->red.rhs;
+    const PcgSystem<double>& sys = c->rig_on ? c->sysr : (c->ext_on ? c->sysx : c->sys);
+    const double* rhs = c->rig_on ? c->rig.rhs : (c->ext_on ? c->ext.rhs : c->red.rhs);
     // factor reuse across LM iterations: the mixed path's default; the FP64 path on request
     // (pb_solve_options.factor_reuse), which gives an FP64 arm with the mixed path's policy
     const bool reuse = f32 ? c->factor_reuse != 2 : c->factor_reuse == 1;
@@ -646,7 +755,8 @@ int solve_dense(pb_gpu_ctx* c, double rel, double abs_tol, int max_it, bool* con
         if (rc < 0) throw CudaError(std::string("dense CG failed: ") + cudaGetErrorString(cudaGetLastError()));
         if (rc == 0 && *converged) {
             ++c->f32_age;
-            check(cudaMemcpyAsync(c->step_c, W.x, c->S[0].n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream),
+            check(cudaMemcpyAsync(c->step_c, camera_block_solution(c, W.x), c->S[0].n * sizeof(double),
+                                  cudaMemcpyDeviceToDevice, c->stream),
                   "D2D");
             return 0;
         }
@@ -675,7 +785,9 @@ int solve_dense(pb_gpu_ctx* c, double rel, double abs_tol, int max_it, bool* con
     }
     *iterations += spent;
     if (rc) return 1;
-    check(cudaMemcpyAsync(c->step_c, W.x, c->S[0].n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream), "D2D");
+    check(cudaMemcpyAsync(c->step_c, camera_block_solution(c, W.x), c->S[0].n * sizeof(double),
+                          cudaMemcpyDeviceToDevice, c->stream),
+          "D2D");
     return 0;
 }
 
@@ -718,14 +830,24 @@ int solve_reduced(pb_gpu_ctx* c, const pb_solve_options& op, bool* converged, in
     const double rel = op.linear_relative_tolerance > 0 ? op.linear_relative_tolerance
                                                          : (op.general_path ? 1.0e-12 : 2.0e-10);
     const double abs_tol = op.linear_absolute_tolerance > 0 ? op.linear_absolute_tolerance : 1.0e-12;
-    const int max_it = op.max_linear_iterations > 0 ? op.max_linear_iterations : std::max(200, 30 * c->model.P);
+    const int P = c->rig_on ? c->model.rig.P : c->model.P;
+    const int max_it = op.max_linear_iterations > 0 ? op.max_linear_iterations : std::max(200, 30 * P);
     int solver = (op.linear_solver == 1 || op.linear_solver == 2)
                      ? op.linear_solver
                      : (dense_solver_fits(c->S[0].n, c->last_precision) ? 1 : 2);
-    if (c->ext_on) {
+    if (c->ext_on && !c->rig_on) {
         // the promoted points live in the dense border: the dense-factor CG solves the extension
         if (!dense_solver_fits(c->ext.nx, c->last_precision))
             throw std::runtime_error("scale bars need the dense reduced solver, and the reduced dimension exceeds its limit "
+                                     "(32 768 mixed, 16 384 FP64)");
+        solver = 1;
+    }
+    if (c->rig_on) {
+        // the rig system (a few thousand unknowns: captures, sensors, groups, promoted points) is
+        // solved by the dense-factor CG
+        const int nr = 6 * c->model.rig.nrb + (c->ext_on ? c->ext.nbx : c->S[0].nb);
+        if (!dense_solver_fits(nr, c->last_precision))
+            throw std::runtime_error("rig problems need the dense reduced solver, and the rig system exceeds its limit "
                                      "(32 768 mixed, 16 384 FP64)");
         solver = 1;
     }
@@ -762,10 +884,13 @@ void back_substitute(pb_gpu_ctx* c, double* dd, double* point_sq, double* cam_sq
     c->launches += 3;
     check(cudaGetLastError(), "back-substitution launch");
     check(cudaMemcpyAsync(c->h_scratch, c->bs_out, 3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "D2H");
+    if (c->rig_on)
+        check(cudaMemcpyAsync(c->h_scratch + 3, c->rig.sq, sizeof(double), cudaMemcpyDeviceToHost, c->stream), "D2H");
     check(cudaStreamSynchronize(c->stream), "back-substitution");
     *dd = c->h_scratch[0];
     *point_sq = c->h_scratch[1];
-    *cam_sq = c->h_scratch[2];
+    // the step RMS of a rig problem is taken over the rig's parameters, not the cameras'
+    *cam_sq = c->rig_on ? c->h_scratch[3] : c->h_scratch[2];
 }
 
 void eval_costs(pb_gpu_ctx* c, const double* alphas, int n, int use_trial, double* out) {
@@ -777,8 +902,9 @@ void eval_costs(pb_gpu_ctx* c, const double* alphas, int n, int use_trial, doubl
     }
     {
         Timer t(c, 2);
-        launch_cost(S, D, c->step_c, c->step_p, c->alphas_d, n, use_trial, c->cost_part, c->cost_out, c->stream);
-        c->launches += use_trial ? 3 : 2;
+        launch_cost(S, D, c->step_c, c->step_p, c->alphas_d, n, use_trial, c->cost_part, c->cost_out, c->stream,
+                    c->rig_on ? &c->rig : nullptr);
+        c->launches += use_trial ? (c->rig_on ? 4 : 3) : 2;
         if (c->ext_on) {
             launch_bar_cost(S, D, c->step_p, c->alphas_d, n, use_trial, c->bar_d + 1, c->stream);
             c->launches += 1;
@@ -816,7 +942,7 @@ double extend_system(pb_gpu_ctx* c, double damping) {
 // Scale bars: the promoted points' steps of the last extended solve into the point steps;
 // returns their squared sum.
 double promoted_steps(pb_gpu_ctx* c) {
-    const double* xsol = c->last_precision == PB_PRECISION_MIXED ? c->dw32.x : c->dw64.x;
+    const double* xsol = c->rig_on ? c->rig.xv : (c->last_precision == PB_PRECISION_MIXED ? c->dw32.x : c->dw64.x);
     launch_ext_step(c->S[0], c->D[0], xsol, c->step_c, c->step_p, c->bar_d + kMaxAlpha + 1, c->stream);
     c->launches += 1;
     check(cudaGetLastError(), "promoted step launch");
@@ -834,6 +960,14 @@ void reset_state(pb_gpu_ctx* c) {
                           cudaMemcpyDeviceToDevice, st),
           "D2D");
     check(cudaMemcpyAsync(D.points, D.points0, m.trk_order.size() * 3 * sizeof(double), cudaMemcpyDeviceToDevice, st), "D2D");
+    if (c->rig_on) {
+        check(cudaMemcpyAsync(c->rig.cap_state, c->rig.cap_input, m.rig.cap_in.size() * sizeof(double),
+                              cudaMemcpyDeviceToDevice, st),
+              "D2D");
+        check(cudaMemcpyAsync(c->rig.sen_state, c->rig.sen_input, m.rig.sen_in.size() * sizeof(double),
+                              cudaMemcpyDeviceToDevice, st),
+              "D2D");
+    }
     launch_effective(c->S[0], D, st);
     c->launches += 1;
     c->have_system = false;
@@ -895,7 +1029,9 @@ void lm_solve(pb_gpu_ctx* c, const pb_solve_options& op, pb_solve_report* rep) {
     rep->active_tracks = m.active_tracks;
     rep->observation_count = m.obs_count;
     rep->rejected_initial_tracks = m.rejected;
-    rep->camera_blocks = m.ncb;
+    rep->camera_blocks = m.rig.on ? m.rig.nrb : m.ncb;
+    rep->rig_capture_blocks = m.rig.ncapb;
+    rep->rig_sensor_blocks = m.rig.nsenb;
     rep->intrinsic_blocks = m.ng;
     rep->pattern_builds = c->pattern_builds;
     rep->pattern_reuses = c->pattern_reuses;
@@ -923,7 +1059,7 @@ void lm_solve(pb_gpu_ctx* c, const pb_solve_options& op, pb_solve_report* rep) {
     int iterations = 0;
     bool converged = m.P == 0 && m.ntb == 0;
     bool failed = false, cancelled = false;
-    const double n_global = static_cast<double>(6 * m.ncb + m.ng * m.ni);
+    const double n_global = static_cast<double>(6 * (m.rig.on ? m.rig.nrb : m.ncb) + m.ng * m.ni);
     const double n_point = 3.0 * m.ntb;
     auto t_asm = 0.0, t_lin = 0.0, t_bs = 0.0, t_obj = 0.0;
     auto now = [] { return std::chrono::steady_clock::now(); };
@@ -1032,8 +1168,7 @@ void lm_solve(pb_gpu_ctx* c, const pb_solve_options& op, pb_solve_report* rep) {
                                  iterations, precision, current, damping, lit, sweeps, relres, dd, rg, rp,
                                  accepted_slot >= 0 ? accepted_alpha : alpha, cand, accepted_slot >= 0 ? 1 : 0);
                 if (accepted_slot >= 0) {
-                    launch_accept(c->S[0], c->D[0], c->step_p, accepted_alpha, accepted_slot, c->stream);
-                    c->launches += 1;
+                    accept_trial(c, accepted_alpha, accepted_slot);
                     // a large cost decrease means a large change of the reduced matrix: the next
                     // solve refactors instead of trying the kept FP32 factor first
                     c->f32_stale = current - cand > 1e-2 * current;
@@ -1109,7 +1244,9 @@ void lm_solve_general(pb_gpu_ctx* c, const pb_solve_options& op, pb_solve_report
     rep->active_tracks = m.active_tracks;
     rep->observation_count = m.obs_count;
     rep->rejected_initial_tracks = m.rejected;
-    rep->camera_blocks = m.ncb;
+    rep->camera_blocks = m.rig.on ? m.rig.nrb : m.ncb;
+    rep->rig_capture_blocks = m.rig.ncapb;
+    rep->rig_sensor_blocks = m.rig.nsenb;
     rep->promoted_point_blocks = m.npr;
     rep->general_path_used = 1;
     rep->intrinsic_blocks = m.ng;
@@ -1138,7 +1275,7 @@ void lm_solve_general(pb_gpu_ctx* c, const pb_solve_options& op, pb_solve_report
     int iterations = 0;
     bool converged = m.P == 0 && m.ntb == 0 && m.npr == 0;
     bool failed = false, cancelled = false;
-    const double n_global = static_cast<double>(6 * m.ncb + m.ng * m.ni);
+    const double n_global = static_cast<double>(6 * (m.rig.on ? m.rig.nrb : m.ncb) + m.ng * m.ni);
     const double n_point = 3.0 * (m.ntb + m.npr);
     auto t_asm = 0.0, t_lin = 0.0, t_bs = 0.0, t_obj = 0.0;
     auto now = [] { return std::chrono::steady_clock::now(); };
@@ -1252,8 +1389,7 @@ void lm_solve_general(pb_gpu_ctx* c, const pb_solve_options& op, pb_solve_report
                                  iterations, precision, current, damping, lit, relres, dd, rg, rp, accepted_alpha, cand,
                                  accept ? 1 : 0);
                 if (accept) {
-                    launch_accept(c->S[0], c->D[0], c->step_p, accepted_alpha, accepted_slot, c->stream);
-                    c->launches += 1;
+                    accept_trial(c, accepted_alpha, accepted_slot);
                     c->f32_stale = current - cand > 1e-2 * current;
                     current = cand;
                     ++rep->accepted_steps;
@@ -1474,9 +1610,12 @@ pb_status pb_gpu_reset_state(pb_gpu_ctx* c) {
 pb_status pb_gpu_get_sizes(pb_gpu_ctx* c, int64_t* s, double* baseline) {
     if (!c || !s || !c->uploaded) return fail(c, PB_ERR_STATE, "no problem uploaded");
     const HostModel& m = c->model;
-    s[0] = m.nc; s[1] = m.nt; s[2] = m.no; s[3] = m.P; s[4] = m.ncb; s[5] = m.ng; s[6] = m.ntb;
-    s[7] = m.active_tracks; s[8] = m.obs_count; s[9] = m.rejected; s[10] = static_cast<int64_t>(m.pairs.size());
-    s[11] = 6 * m.ncb + m.ng * m.ni; s[12] = m.ni; s[13] = m.gauge_anchor; s[14] = m.gauge_scale;
+    // rig problems report the reference's numbering: rig pose blocks, rig pairs, rig dimension
+    const bool rig = m.rig.on;
+    s[0] = m.nc; s[1] = m.nt; s[2] = m.no; s[3] = rig ? m.rig.P : m.P; s[4] = rig ? m.rig.nrb : m.ncb; s[5] = m.ng;
+    s[6] = m.ntb; s[7] = m.active_tracks; s[8] = m.obs_count; s[9] = m.rejected;
+    s[10] = static_cast<int64_t>(rig ? m.rig.pairs.size() : m.pairs.size());
+    s[11] = 6 * (rig ? m.rig.nrb : m.ncb) + m.ng * m.ni; s[12] = m.ni; s[13] = m.gauge_anchor; s[14] = m.gauge_scale;
     s[15] = m.chunks_ready[1] ? m.chunks[1].n() : (m.chunks_ready[0] ? m.chunks[0].n() : 0);
     if (baseline) *baseline = m.gauge_baseline;
     return PB_OK;
@@ -1489,20 +1628,43 @@ pb_status pb_gpu_get_active(pb_gpu_ctx* c, int8_t* at, int32_t* cb, int32_t* ib,
         if (at) at[t] = m.active_track[t];
         if (tb) tb[t] = m.track_block[t];
     }
+    // rig problems: no camera has a block of its own (ActiveProblem::cameraBlock stays -1) and the
+    // groups follow the rig blocks
     for (int i = 0; i < m.nc; ++i) {
-        if (cb) cb[i] = m.camera_block[i];
-        if (ib) ib[i] = m.intrinsic_block[i];
+        if (cb) cb[i] = m.rig.on ? -1 : m.camera_block[i];
+        if (ib) ib[i] = (m.rig.on && m.intrinsic_block[i] >= 0) ? m.rig.nrb + m.calib_group[i] : m.intrinsic_block[i];
     }
     return PB_OK;
 }
 
 pb_status pb_gpu_get_pairs(pb_gpu_ctx* c, int32_t* pairs) {
     if (!c || !pairs || !c->uploaded) return fail(c, PB_ERR_STATE, "no problem uploaded");
-    for (size_t i = 0; i < c->model.pairs.size(); ++i) {
-        pairs[2 * i] = c->model.pairs[i].first;
-        pairs[2 * i + 1] = c->model.pairs[i].second;
+    const auto& pl = c->model.rig.on ? c->model.rig.pairs : c->model.pairs;
+    for (size_t i = 0; i < pl.size(); ++i) {
+        pairs[2 * i] = pl[i].first;
+        pairs[2 * i + 1] = pl[i].second;
     }
     return PB_OK;
+}
+
+pb_status pb_gpu_get_rig(pb_gpu_ctx* c, double* captures, double* sensors, int32_t* capture_block,
+                         int32_t* sensor_block) {
+    if (!c || !c->uploaded) return fail(c, PB_ERR_STATE, "no problem uploaded");
+    const RigModel& rm = c->model.rig;
+    if (!rm.on || !c->rig_on) return fail(c, PB_ERR_STATE, "the uploaded problem has no rig");
+    try {
+        if (captures)
+            check(cudaMemcpy(captures, c->rig.cap_state, rm.cap_in.size() * sizeof(double), cudaMemcpyDeviceToHost), "D2H");
+        if (sensors)
+            check(cudaMemcpy(sensors, c->rig.sen_state, rm.sen_in.size() * sizeof(double), cudaMemcpyDeviceToHost), "D2H");
+        for (int k = 0; k < rm.ncap; ++k)
+            if (capture_block) capture_block[k] = rm.capture_block.empty() ? -1 : rm.capture_block[k];
+        for (int s = 0; s < rm.nsen; ++s)
+            if (sensor_block) sensor_block[s] = rm.sensor_block.empty() ? -1 : rm.sensor_block[s];
+        return PB_OK;
+    } catch (const std::exception& e) {
+        return fail(c, PB_ERR_CUDA, e.what());
+    }
 }
 
 pb_status pb_gpu_linearize_observations(pb_gpu_ctx* c, int32_t precision, double* res, double* jp, double* jpose,
@@ -1572,31 +1734,39 @@ pb_status pb_gpu_get_reduced(pb_gpu_ctx* c, double* dense, double* rhs, double* 
     try {
         const HostModel& m = c->model;
         const Shape& S = c->S[0];
-        const int n = S.n, nb = S.nb, n6 = 6 * S.ncb;
+        // rig problems: the system over the rig's pose blocks (the one that is solved); its
+        // direct right-hand side is not formed and `direct` is left unwritten
+        const bool rig = c->rig_on;
+        if (rig && c->ext_on) return fail(c, PB_ERR_UNSUPPORTED, "the dense copy of a rig system with scale bars is not provided");
+        const int npose = rig ? m.rig.nrb : S.ncb;
+        const int nnzb = rig ? c->rig.nnzb : S.nnzb;
+        const std::vector<int>& row_ptr = rig ? m.rig.row_ptr : m.row_ptr;
+        const std::vector<int>& col_idx = rig ? m.rig.col_idx : m.col_idx;
+        const int nb = S.nb, n6 = 6 * npose, n = n6 + nb;
         const size_t ts = 8;
-        std::vector<char> vals(static_cast<size_t>(std::max(1, S.nnzb)) * 36 * ts), border(static_cast<size_t>(std::max(1, S.ncb)) * 6 * std::max(1, nb) * ts),
+        std::vector<char> vals(static_cast<size_t>(std::max(1, nnzb)) * 36 * ts), border(static_cast<size_t>(std::max(1, npose)) * 6 * std::max(1, nb) * ts),
             Cm(static_cast<size_t>(std::max(1, nb * nb)) * ts), r(n * ts), d(n * ts);
-        const void* src_vals = c->red.vals;
-        const void* src_border = c->red.border;
+        const void* src_vals = rig ? c->rig.vals : c->red.vals;
+        const void* src_border = rig ? c->rig.border : c->red.border;
         const void* src_C = c->red.Cm;
-        const void* src_r = c->red.rhs;
+        const void* src_r = rig ? c->rig.rhs : c->red.rhs;
         const void* src_d = c->red.direct;
-        check(cudaMemcpy(vals.data(), src_vals, static_cast<size_t>(S.nnzb) * 36 * ts, cudaMemcpyDeviceToHost), "D2H");
+        check(cudaMemcpy(vals.data(), src_vals, static_cast<size_t>(nnzb) * 36 * ts, cudaMemcpyDeviceToHost), "D2H");
         if (nb) {
-            check(cudaMemcpy(border.data(), src_border, static_cast<size_t>(S.ncb) * 6 * nb * ts, cudaMemcpyDeviceToHost), "D2H");
+            check(cudaMemcpy(border.data(), src_border, static_cast<size_t>(npose) * 6 * nb * ts, cudaMemcpyDeviceToHost), "D2H");
             check(cudaMemcpy(Cm.data(), src_C, static_cast<size_t>(nb) * nb * ts, cudaMemcpyDeviceToHost), "D2H");
         }
         check(cudaMemcpy(r.data(), src_r, n * ts, cudaMemcpyDeviceToHost), "D2H");
-        check(cudaMemcpy(d.data(), src_d, n * ts, cudaMemcpyDeviceToHost), "D2H");
+        if (!rig) check(cudaMemcpy(d.data(), src_d, n * ts, cudaMemcpyDeviceToHost), "D2H");
         auto get = [&](const std::vector<char>& v, size_t i) {
             return ts == 8 ? reinterpret_cast<const double*>(v.data())[i]
                            : static_cast<double>(reinterpret_cast<const float*>(v.data())[i]);
         };
         if (dense) {
             std::fill(dense, dense + static_cast<size_t>(n) * n, 0.0);
-            for (int i = 0; i < S.ncb; ++i)
-                for (int p = m.row_ptr[i]; p < m.row_ptr[i + 1]; ++p) {
-                    const int j = m.col_idx[p];
+            for (int i = 0; i < npose; ++i)
+                for (int p = row_ptr[i]; p < row_ptr[i + 1]; ++p) {
+                    const int j = col_idx[p];
                     for (int a = 0; a < 6; ++a)
                         for (int b = 0; b < 6; ++b)
                             dense[static_cast<size_t>(6 * i + a) * n + 6 * j + b] = get(vals, static_cast<size_t>(p) * 36 + a * 6 + b);
@@ -1612,7 +1782,7 @@ pb_status pb_gpu_get_reduced(pb_gpu_ctx* c, double* dense, double* rhs, double* 
         }
         for (int i = 0; i < n; ++i) {
             if (rhs) rhs[i] = get(r, i);
-            if (direct) direct[i] = get(d, i);
+            if (direct && !rig) direct[i] = get(d, i);
         }
         return PB_OK;
     } catch (const std::exception& e) {
@@ -1689,7 +1859,7 @@ pb_status pb_gpu_apply_step(pb_gpu_ctx* c, double alpha) {
     try {
         double cst;
         eval_costs(c, &alpha, 1, 1, &cst);
-        launch_accept(c->S[0], c->D[0], c->step_p, alpha, 0, c->stream);
+        accept_trial(c, alpha, 0);
         check(cudaStreamSynchronize(c->stream), "apply");
         c->have_system = false;
         return PB_OK;
@@ -1804,6 +1974,14 @@ pb_status pb_gpu_save_state(pb_gpu_ctx* c) {
         check(cudaMemcpyAsync(c->snap_cams, D.cams_state, nc * sizeof(double), cudaMemcpyDeviceToDevice, st), "D2D");
         check(cudaMemcpyAsync(c->snap_points, D.points, np * sizeof(double), cudaMemcpyDeviceToDevice, st), "D2D");
         check(cudaMemcpyAsync(c->snap_groups, D.groups, ng * sizeof(double), cudaMemcpyDeviceToDevice, st), "D2D");
+        if (c->rig_on) {
+            check(cudaMemcpyAsync(c->rig.cap_saved, c->rig.cap_state, m.rig.cap_in.size() * sizeof(double),
+                                  cudaMemcpyDeviceToDevice, st),
+                  "D2D");
+            check(cudaMemcpyAsync(c->rig.sen_saved, c->rig.sen_state, m.rig.sen_in.size() * sizeof(double),
+                                  cudaMemcpyDeviceToDevice, st),
+                  "D2D");
+        }
         check(cudaStreamSynchronize(st), "save_state");
         c->snap_valid = true;
         return PB_OK;
@@ -1823,6 +2001,14 @@ pb_status pb_gpu_restore_state(pb_gpu_ctx* c) {
         check(cudaMemcpyAsync(D.cams_state, c->snap_cams, nc * sizeof(double), cudaMemcpyDeviceToDevice, st), "D2D");
         check(cudaMemcpyAsync(D.points, c->snap_points, np * sizeof(double), cudaMemcpyDeviceToDevice, st), "D2D");
         check(cudaMemcpyAsync(D.groups, c->snap_groups, ng * sizeof(double), cudaMemcpyDeviceToDevice, st), "D2D");
+        if (c->rig_on) {
+            check(cudaMemcpyAsync(c->rig.cap_state, c->rig.cap_saved, m.rig.cap_in.size() * sizeof(double),
+                                  cudaMemcpyDeviceToDevice, st),
+                  "D2D");
+            check(cudaMemcpyAsync(c->rig.sen_state, c->rig.sen_saved, m.rig.sen_in.size() * sizeof(double),
+                                  cudaMemcpyDeviceToDevice, st),
+                  "D2D");
+        }
         launch_effective(c->S[0], D, st);
         ++c->launches;
         c->have_system = false;
@@ -1956,7 +2142,8 @@ pb_status adjoint_prepare(pb_gpu_ctx* c) {
     // the exact Hessian is written for the Euler target rotation chart and the scaled point chart
     // of image-only problems; control points switch the solve to the plain parameterisation
     if (!m.ref_param)
-        return fail(c, PB_ERR_UNSUPPORTED, "the backward pass covers image-only problems (no control points or scale bars)");
+        return fail(c, PB_ERR_UNSUPPORTED,
+                    "the backward pass covers image-only problems (no control points, scale bars or rigs)");
     // the point elimination runs over the chunk plan of the arithmetic path last used
     const int prec = c->last_precision == PB_PRECISION_MIXED ? 1 : 0;
     if (prec == 1) prepare_precision<float>(c, prec);

@@ -159,6 +159,14 @@ class Gb300Context:
         return {"cameras": cams, "points": pts, "valid": valid.astype(bool), "rms_before": rb, "rms_after": ra,
                 "intrinsics": intr[:ng]}
 
+    def rig(self):
+        """Rig problems: current captures and sensors (12 doubles each) and their pose blocks."""
+        st = native.rig_state(self.L, self.ctx, self.problem)
+        if st is None:
+            return None
+        cap, sen, kb, sb = st
+        return {"captures": cap, "sensors": sen, "capture_block": kb, "sensor_block": sb}
+
     # ---- snapshot / measurement updates / backward pass -------------------------------------
     def save_state(self):
         self._check(self.L.pb_gpu_save_state(self.ctx), "save_state")

@@ -22,7 +22,7 @@ EXPORTED = [
     "pb_gpu_set_timing",
     "pb_gpu_kernel_times", "pb_gpu_objective_noalloc", "pb_gpu_solve_batch",
     "pb_gpu_save_state", "pb_gpu_restore_state", "pb_gpu_set_observations", "pb_gpu_backward",
-    "pb_gpu_newton_step",
+    "pb_gpu_newton_step", "pb_gpu_get_rig",
     "pb_bne_create", "pb_bne_destroy", "pb_bne_clear_values", "pb_bne_sizes", "pb_bne_add_residual_blocks",
     "pb_bne_add_primary_residual_blocks", "pb_bne_add_primary_residual_block",
     "pb_bne_add_eliminated_residual_block", "pb_bne_add_residual_block", "pb_bne_add_primary_gradient_block",
@@ -44,7 +44,10 @@ class ProblemDesc(C.Structure):
                 ("calibration_group_ids", C.c_void_p), ("intrinsic_reference_cameras", C.c_void_p),
                 ("n_control_points", C.c_int32), ("control_point_track", C.c_void_p),
                 ("control_point_data", C.c_void_p), ("n_scale_bars", C.c_int32), ("scale_bar_tracks", C.c_void_p),
-                ("scale_bar_data", C.c_void_p)]
+                ("scale_bar_data", C.c_void_p), ("n_rig_captures", C.c_int32), ("rig_captures", C.c_void_p),
+                ("rig_capture_info", C.c_void_p), ("n_rig_sensors", C.c_int32), ("rig_sensors", C.c_void_p),
+                ("rig_sensor_info", C.c_void_p), ("rig_camera_capture", C.c_void_p),
+                ("rig_camera_sensor", C.c_void_p)]
 
 
 class SolveOptionsC(C.Structure):
@@ -72,7 +75,8 @@ class SolveReportC(C.Structure):
         "pattern_reuses", "gpu_kernel_launches")] + [(n, C.c_double) for n in (
             "initial_cost", "final_cost", "mean_rms_before", "mean_rms_after", "valid_track_ratio",
             "filter_threshold", "assembly_ms", "linear_ms", "back_substitution_ms", "objective_ms", "total_ms")] + [
-        (n, C.c_int32) for n in ("promoted_point_blocks", "general_path_used")]
+        (n, C.c_int32) for n in ("promoted_point_blocks", "general_path_used", "rig_capture_blocks",
+                                 "rig_sensor_blocks")]
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -167,6 +171,7 @@ def load(build_if_missing: bool = False):
     L.pb_gpu_set_observations.argtypes = [vp, i64, vp, vp, vp]
     L.pb_gpu_backward.argtypes = [vp, vp, vp, vp, vp, vp, vp, C.POINTER(AdjointReportC)]
     L.pb_gpu_newton_step.argtypes = [vp, C.POINTER(dbl), C.POINTER(dbl)]
+    L.pb_gpu_get_rig.argtypes = [vp, vp, vp, vp, vp]
     L.pb_bne_create.argtypes = [i32, i32, i32, i32, C.POINTER(vp)]
     L.pb_bne_destroy.argtypes = [vp]
     L.pb_bne_clear_values.argtypes = [vp]
@@ -207,7 +212,50 @@ def problem_desc(problem):
                        fixed_c.size, _ptr(fixed_c), fixed_t.size, _ptr(fixed_t), _ptr(p.cameraCalibrationGroupIds),
                        _ptr(p.sharedIntrinsicReferenceCameras), cp_track.size, _ptr(cp_track), _ptr(cp_data),
                        sb_data.shape[0], _ptr(sb_tracks), _ptr(sb_data))
+    rig = getattr(p, "rig", None)
+    if rig is not None and not rig.empty() and rig.captures:
+        arrs = rig.arrays(p.n_cameras)
+        keep.extend(arrs)
+        cap, cap_info, sen, sen_info, cam_cap, cam_sen = arrs
+        desc.n_rig_captures = cap.shape[0]
+        desc.rig_captures = _ptr(cap)
+        desc.rig_capture_info = _ptr(cap_info)
+        desc.n_rig_sensors = sen.shape[0]
+        desc.rig_sensors = _ptr(sen)
+        desc.rig_sensor_info = _ptr(sen_info)
+        desc.rig_camera_capture = _ptr(cam_cap)
+        desc.rig_camera_sensor = _ptr(cam_sen)
     return desc, keep
+
+
+def rig_state(L, ctx, problem):
+    """(captures [n, 12], sensors [n, 12], capture blocks, sensor blocks) of the context's current
+    state, or None when the problem has no rig."""
+    rig = getattr(problem, "rig", None)
+    if rig is None or not rig.captures:
+        return None
+    cap = np.zeros((len(rig.captures), 12))
+    sen = np.zeros((len(rig.sensors), 12))
+    kb = np.zeros(len(rig.captures), np.int32)
+    sb = np.zeros(len(rig.sensors), np.int32)
+    check(L, ctx, L.pb_gpu_get_rig(ctx, cap.ctypes.data, sen.ctypes.data, kb.ctypes.data, sb.ctypes.data), "get_rig")
+    return cap, sen, kb, sb
+
+
+def refined_rig(L, ctx, problem):
+    """Result::refinedRig: the problem's rig topology with the accepted capture and sensor
+    parameters, or None without a rig."""
+    import dataclasses
+    st = rig_state(L, ctx, problem)
+    if st is None:
+        return None
+    cap, sen, _, _ = st
+    rig = problem.rig
+    caps = [dataclasses.replace(c, rigToWorldRotation=tuple(cap[i, :9]), rigCenterInWorld=tuple(cap[i, 9:12]))
+            for i, c in enumerate(rig.captures)]
+    sens = [dataclasses.replace(s, cameraToRigRotation=tuple(sen[i, :9]), cameraCenterInRig=tuple(sen[i, 9:12]))
+            for i, s in enumerate(rig.sensors)]
+    return dataclasses.replace(rig, captures=caps, sensors=sens, cameraBindings=list(rig.cameraBindings))
 
 
 def scale_bar_arrays(problem):

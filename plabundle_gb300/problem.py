@@ -147,14 +147,86 @@ class ScaleBarConstraint:
 
 
 @dataclass
+class RigCapture:
+    """placamera::RigCapture: one capture of a rig (rig-to-world rotation, rig centre in world
+    coordinates)."""
+
+    rigId: int = 0
+    captureId: int = 0
+    rigToWorldRotation: Sequence[float] = (1.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0, 1.0)  # row-major
+    rigCenterInWorld: Sequence[float] = (0.0, 0.0, 0.0)
+    fixedPose: bool = False
+
+
+@dataclass
+class RigSensor:
+    """placamera::RigSensor: the extrinsic of one sensor of a rig (camera-to-rig rotation, camera
+    centre in rig coordinates), shared by all captures of the rig."""
+
+    rigId: int = 0
+    sensorId: int = 0
+    cameraToRigRotation: Sequence[float] = (1.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0, 1.0)  # row-major
+    cameraCenterInRig: Sequence[float] = (0.0, 0.0, 0.0)
+    fixedExtrinsic: bool = False
+
+
+@dataclass
+class RigCameraBinding:
+    """placamera::RigCameraBinding: the capture and sensor a camera model is composed from."""
+
+    cameraIndex: int = 0
+    rigId: int = 0
+    captureId: int = 0
+    sensorId: int = 0
+
+
+@dataclass
+class RigTopology:
+    """placamera::RigTopology (Problem::rig, include/plabundle/problem.h:52).  The composed camera
+    is R_camera_world = R_rig_world R_camera_rig, C_camera_world = C_rig_world + R_rig_world
+    C_camera_rig (the reference's README, "Rig BA")."""
+
+    captures: List[RigCapture] = field(default_factory=list)
+    sensors: List[RigSensor] = field(default_factory=list)
+    cameraBindings: List[RigCameraBinding] = field(default_factory=list)
+
+    def empty(self) -> bool:
+        return not self.captures and not self.sensors and not self.cameraBindings
+
+    def arrays(self, n_cameras: int):
+        """The C-ABI arrays: capture records [n, 12] and (rigId, fixedPose) [n, 2], sensor records
+        [n, 12] and (rigId, fixedExtrinsic) [n, 2], and each camera's capture and sensor index
+        (-1 for a camera without a binding; the library rejects it).  Bindings name captures and
+        sensors by (rigId, captureId) and (rigId, sensorId), as the reference looks them up
+        (prepareActiveProblem, BundleAdjustPlaMatrixProblem.cpp:47-66)."""
+        cap = np.array([list(c.rigToWorldRotation) + list(c.rigCenterInWorld) for c in self.captures],
+                       np.float64).reshape(-1, 12)
+        cap_info = np.array([(c.rigId, int(bool(c.fixedPose))) for c in self.captures], np.int32).reshape(-1, 2)
+        sen = np.array([list(s.cameraToRigRotation) + list(s.cameraCenterInRig) for s in self.sensors],
+                       np.float64).reshape(-1, 12)
+        sen_info = np.array([(s.rigId, int(bool(s.fixedExtrinsic))) for s in self.sensors], np.int32).reshape(-1, 2)
+        ck = {(c.rigId, c.captureId): i for i, c in reversed(list(enumerate(self.captures)))}
+        sk = {(s.rigId, s.sensorId): i for i, s in reversed(list(enumerate(self.sensors)))}
+        cam_cap = np.full(n_cameras, -1, np.int32)
+        cam_sen = np.full(n_cameras, -1, np.int32)
+        for b in self.cameraBindings:
+            if 0 <= b.cameraIndex < n_cameras:
+                cam_cap[b.cameraIndex] = ck.get((b.rigId, b.captureId), -1)
+                cam_sen[b.cameraIndex] = sk.get((b.rigId, b.sensorId), -1)
+        return (np.ascontiguousarray(cap), np.ascontiguousarray(cap_info), np.ascontiguousarray(sen),
+                np.ascontiguousarray(sen_info), cam_cap, cam_sen)
+
+
+@dataclass
 class Problem:
     """plabundle::Problem (include/plabundle/problem.h:37-54) for frame cameras.
 
     Control points are the (track, ControlPointConstraint) pairs of Track::controlPointConstraints;
     scale bars are Problem::scaleBarConstraints (their tracks become primary point blocks and the
     problem is solved on the general path, canUseReferenceOnlineSchur,
-    BundleAdjustPlaMatrixReferenceSchur.cpp:667-673).  Rigs, laser planes and ranges, pose priors
-    and the camera-plane constraint are not carried.
+    BundleAdjustPlaMatrixReferenceSchur.cpp:667-673).  `rig` is Problem::rig: captures, sensors and
+    the binding of every camera.  Laser planes and ranges, pose priors and the camera-plane
+    constraint are not carried.
     """
 
     cameras: np.ndarray                 # [n_cameras, 32] float64
@@ -172,6 +244,7 @@ class Problem:
     gauge: Gauge = field(default_factory=Gauge)
     controlPoints: List[Tuple[int, ControlPointConstraint]] = field(default_factory=list)
     scaleBarConstraints: List[ScaleBarConstraint] = field(default_factory=list)
+    rig: RigTopology = field(default_factory=RigTopology)
 
     @property
     def n_cameras(self) -> int:
@@ -455,6 +528,7 @@ class Result:
     points: Optional[RefinedPoint] = None
     refinedCameras: Optional[np.ndarray] = None
     intrinsicGroups: Optional[np.ndarray] = None
+    refinedRig: Optional[RigTopology] = None    # Result::refinedRig (include/plabundle/result.h:149)
 
     def usable(self) -> bool:
         return self.solutionUsable and self.status in (SolveStatus.Success, SolveStatus.NoConvergence)

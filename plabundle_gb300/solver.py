@@ -278,6 +278,7 @@ class Solver:
         result.totalSeconds = r["total_ms"] / 1000.0
         result.refinedCameras = cams
         result.intrinsicGroups = intr[:int(sizes[5])]
+        result.refinedRig = native.refined_rig(L, ctx, problem)
         result.points = RefinedPoint(valid=valid.astype(bool), converged=r["status"] == SolveStatus.Success,
                                      point=pts, rmsBefore=rb, rmsAfter=ra, iterations=r["iterations"])
         result.quality = QualitySummary(totalTracks=p.n_tracks, optimizedTracks=r["optimized_tracks"],

@@ -395,3 +395,162 @@ def with_control_points(problem: Problem, n: int = 12, sigma: float = 0.02, seed
     problem.controlPoints = cps
     return problem
 
+
+
+def _visible_pairs(cams: np.ndarray, X: np.ndarray, zlo: float, zhi: float, cell: float = 25.0):
+    """(point, camera) pairs of every camera that sees a point in front and in frame, sorted by
+    point then camera.  Candidates per camera come from the cells of a ground grid that cover the
+    camera's footprint between the heights zlo and zhi."""
+    x0, y0 = X[:, 0].min(), X[:, 1].min()
+    nx = int((X[:, 0].max() - x0) // cell) + 1
+    ny = int((X[:, 1].max() - y0) // cell) + 1
+    cx = np.clip(((X[:, 0] - x0) // cell).astype(np.int64), 0, nx - 1)
+    cy = np.clip(((X[:, 1] - y0) // cell).astype(np.int64), 0, ny - 1)
+    cid = cy * nx + cx
+    order = np.argsort(cid, kind="stable")
+    start = np.searchsorted(cid[order], np.arange(nx * ny + 1))
+    pis, cis = [], []
+    for c in range(cams.shape[0]):
+        cam = cams[c]
+        R = cam[0:9].reshape(3, 3)
+        C = cam[9:12]
+        w, h = cam[24], cam[25]
+        corners = np.array([[0, 0], [w, 0], [0, h], [w, h]], float)
+        rays = np.stack([(corners[:, 0] - cam[14]) / cam[12], (corners[:, 1] - cam[15]) / cam[13],
+                         np.ones(4)], axis=1) @ R.T
+        if np.any(rays[:, 2] >= -1e-6):
+            continue  # a corner ray does not reach the ground: not an aerial view
+        pts = []
+        for z in (zlo, zhi):
+            t = (z - C[2]) / rays[:, 2]
+            pts.append(C[None, :2] + t[:, None] * rays[:, :2])
+        pts = np.concatenate(pts)
+        gx0 = max(0, int((pts[:, 0].min() - x0) // cell))
+        gx1 = min(nx - 1, int((pts[:, 0].max() - x0) // cell))
+        gy0 = max(0, int((pts[:, 1].min() - y0) // cell))
+        gy1 = min(ny - 1, int((pts[:, 1].max() - y0) // cell))
+        if gx1 < gx0 or gy1 < gy0:
+            continue
+        cand = np.concatenate([order[start[gy * nx + gx0]:start[gy * nx + gx1 + 1]] for gy in range(gy0, gy1 + 1)])
+        if cand.size == 0:
+            continue
+        px, valid = _project_one(cam, X[cand])
+        ok = valid & (px[:, 0] >= 0) & (px[:, 0] < w) & (px[:, 1] >= 0) & (px[:, 1] < h)
+        pis.append(cand[ok])
+        cis.append(np.full(int(ok.sum()), c, np.int32))
+    pi = np.concatenate(pis) if pis else np.zeros(0, np.int64)
+    ci = np.concatenate(cis) if cis else np.zeros(0, np.int32)
+    o = np.lexsort((ci, pi))
+    return pi[o], ci[o]
+
+
+def _choose_views_sparse(pi, ci, n_pts, rng, min_views, max_views):
+    """Per point, a uniformly random subset of min(k, visible) of its visible cameras with
+    k ~ U{min_views..max_views}, in camera order; from sorted (point, camera) pairs."""
+    k = rng.integers(min_views, max_views + 1, n_pts)
+    keys = rng.random(pi.size)
+    o = np.lexsort((keys, pi))
+    start = np.searchsorted(pi[o], np.arange(n_pts + 1))
+    rank = np.arange(pi.size) - np.repeat(start[:-1], np.diff(start))
+    keep = np.zeros(pi.size, bool)
+    keep[o[rank < k[pi[o]]]] = True
+    pi, ci = pi[keep], ci[keep]          # still sorted by (point, camera)
+    counts = np.bincount(pi, minlength=n_pts).astype(np.int64)
+    return counts, ci.astype(np.int32)
+
+
+def rig_grid_problem(seed: int = 21, n_along: int = 30, n_lines: int = 20, n_points: int = 1_500_000,
+                     altitude: float = 100.0, width: float = 6000.0, height: float = 4000.0,
+                     nadir_focal: float = 4000.0, oblique_focal: float = 8000.0, tilt_deg: float = 45.0,
+                     forward_overlap: float = 0.8, side_overlap: float = 0.6, noise: float = 0.7,
+                     outlier_frac: float = 0.05, rot_sigma: float = 0.01, centre_sigma: float = 0.05,
+                     point_sigma: float = 0.05, sensor_rot_sigma: float = 0.003, sensor_centre_sigma: float = 0.01,
+                     min_views: int = 3, max_views: int = 8, n_obliques: int = 4):
+    """Oblique block of 5-camera rigs: captures on a flight grid at `altitude` (nadir overlap
+    80 %/60 %), each with a nadir camera (the rig's fixed body-frame sensor) and `n_obliques`
+    cameras tilted `tilt_deg` forward, backward, left and right, whose extrinsics (rotation and
+    lever arm) are refined.  Points on a sum-of-sinusoids terrain, each observed by a random
+    3..`max_views` of the cameras that see it; pixel noise `noise`, `outlier_frac` outliers.
+    Initial captures are perturbed by N(0, rot_sigma) / N(0, centre_sigma), initial free sensors
+    are the nominal extrinsics (the truth differs by N(0, sensor_rot_sigma) / N(0,
+    sensor_centre_sigma)), initial points by N(0, point_sigma)."""
+    from .problem import RigCameraBinding, RigCapture, RigSensor, RigTopology
+    rng = np.random.default_rng(seed)
+    foot_x = width / nadir_focal * altitude
+    foot_y = height / nadir_focal * altitude
+    step_along = (1 - forward_overlap) * foot_y
+    step_side = (1 - side_overlap) * foot_x
+    tilt = np.deg2rad(tilt_deg)
+    dirs = [np.array([1.0, 0.0]), np.array([-1.0, 0.0]), np.array([0.0, 1.0]), np.array([0.0, -1.0])][:n_obliques]
+    # nominal sensors: nadir (fixed) and obliques, camera-to-rig rotations and lever arms
+    nominal = [(look_at_rotation(np.zeros(3), np.array([0.0, 0.0, -1.0]), up=(0.0, 1.0, 0.0)), np.zeros(3))]
+    for d in dirs:
+        f = np.array([d[0] * np.sin(tilt), d[1] * np.sin(tilt), -np.cos(tilt)])
+        nominal.append((look_at_rotation(np.zeros(3), f, up=(0.0, 0.0, 1.0)),
+                        np.array([0.12 * d[0], 0.12 * d[1], -0.05])))
+    n_sen = len(nominal)
+    truth_sen, init_sen = [], []
+    for s, (Rn, tn) in enumerate(nominal):
+        if s == 0:
+            truth_sen.append((Rn, tn))
+        else:
+            dR = rotation_from_axis_angle(rng.normal(0.0, sensor_rot_sigma, 3))
+            truth_sen.append((dR @ Rn, tn + rng.normal(0.0, sensor_centre_sigma, 3)))
+        init_sen.append((Rn, tn))
+    models = [dict(f=nadir_focal, k=(-0.03, 0.006, 0.0), p=(1e-4, -1e-4))]
+    models += [dict(f=oblique_focal, k=(-0.02, 0.004, 0.0), p=(-1e-4, 1e-4)) for _ in dirs]
+    truth_cap, cap_pos = [], []
+    for line in range(n_lines):
+        for j in range(n_along):
+            yaw = rng.normal(0.0, 0.02)
+            truth_cap.append((rotation_from_axis_angle(np.array([0.0, 0.0, yaw])),
+                              np.array([line * step_side, j * step_along, altitude])))
+    n_cap = len(truth_cap)
+
+    def compose(caps, sens):
+        out = []
+        for k, (Rc, Cc) in enumerate(caps):
+            for s, (Rs, ts) in enumerate(sens):
+                m = models[s]
+                out.append(make_camera(Rc @ Rs, Cc + Rc @ ts, m["f"], m["f"], width / 2, height / 2, k=m["k"],
+                                       p=m["p"], width=width, height=height))
+        return np.array(out)
+
+    cams = compose(truth_cap, truth_sen)
+    hfun = _terrain(rng)
+    margin_x, margin_y = 0.45 * foot_x, 0.45 * foot_y
+    xs = rng.uniform(-margin_x, (n_lines - 1) * step_side + margin_x, n_points)
+    ys = rng.uniform(-margin_y, (n_along - 1) * step_along + margin_y, n_points)
+    X = np.stack([xs, ys, hfun(xs, ys)], axis=1)
+    pi, ci = _visible_pairs(cams, X, X[:, 2].min() - 1.0, X[:, 2].max() + 1.0)
+    counts, cam_idx = _choose_views_sparse(pi, ci, n_points, rng, min_views, max_views)
+    offsets = np.zeros(n_points + 1, np.int64)
+    np.cumsum(counts, out=offsets[1:])
+    pt_idx = np.repeat(np.arange(n_points), counts)
+    px, _ = project(cams, cam_idx, X[pt_idx])
+    px = px + rng.normal(0.0, noise, px.shape)
+    out_mask = rng.random(cam_idx.size) < outlier_frac
+    px[out_mask, 0] = rng.random(out_mask.sum()) * width
+    px[out_mask, 1] = rng.random(out_mask.sum()) * height
+    keep = counts >= 2
+    if not keep.all():
+        X, offsets, cam_idx, px = _drop_tracks(X, offsets, cam_idx, px, keep)
+    init_cap = []
+    for Rc, Cc in truth_cap:
+        dR = rotation_from_axis_angle(rng.normal(0.0, rot_sigma, 3))
+        init_cap.append((dR @ Rc, Cc + rng.normal(0.0, centre_sigma, 3)))
+    cams0 = compose(init_cap, init_sen)
+    X0 = X + rng.normal(0.0, point_sigma, X.shape)
+    rig = RigTopology(
+        captures=[RigCapture(rigId=0, captureId=k, rigToWorldRotation=tuple(R.reshape(9)), rigCenterInWorld=tuple(C))
+                  for k, (R, C) in enumerate(init_cap)],
+        sensors=[RigSensor(rigId=0, sensorId=s, cameraToRigRotation=tuple(R.reshape(9)), cameraCenterInRig=tuple(t),
+                           fixedExtrinsic=(s == 0)) for s, (R, t) in enumerate(init_sen)],
+        cameraBindings=[RigCameraBinding(cameraIndex=k * n_sen + s, rigId=0, captureId=k, sensorId=s)
+                        for k in range(n_cap) for s in range(n_sen)])
+    prob = _problem(cams0, X0, offsets, cam_idx, px, rig=rig)
+    prob.truth_cameras = cams
+    prob.truth_points = X
+    prob.truth_captures = np.array([np.concatenate([R.reshape(9), C]) for R, C in truth_cap])
+    prob.truth_sensors = np.array([np.concatenate([R.reshape(9), t]) for R, t in truth_sen])
+    return prob

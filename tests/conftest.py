@@ -35,5 +35,10 @@ def host_probe(tmp_path_factory):
     L.probe_model.restype = C.c_int
     L.probe_cp_whitening.argtypes = [C.c_void_p, C.c_void_p]
     L.probe_cp_whitening.restype = C.c_int
+    L.probe_rig.argtypes = [C.POINTER(native.ProblemDesc), C.POINTER(native.SolveOptionsC)] + [C.c_void_p] * 4 + \
+        [C.c_int] + [C.c_void_p] * 3
+    L.probe_rig.restype = C.c_int
+    L.probe_rig_terms.argtypes = [C.POINTER(native.ProblemDesc), C.POINTER(native.SolveOptionsC)]
+    L.probe_rig_terms.restype = C.c_int
     L.probe_message.restype = C.c_char_p
     return L

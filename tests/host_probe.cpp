@@ -205,3 +205,94 @@ extern "C" int probe_model(const pb_problem_desc* pr, const pb_solve_options* op
 
 // The host's control-point validation and whitening of one record.
 extern "C" int probe_cp_whitening(const double* rec, double* W) { return pb::cp_valid(rec, W) ? 1 : 0; }
+
+// Rig model of a problem as the host built it (the reference's numbering).
+// out_i (8 ints): [status, rig capture blocks, rig sensor blocks, primary blocks (rig numbering),
+//                  rig pairs, camera blocks of the kernels, n fixed cameras, ref_param];
+// capture_block (captures), sensor_block (sensors), pairs (2 per pair; capacity max_pairs),
+// cameras (n_cameras * 32: the composed input cameras), fixed (n_cameras capacity),
+// groups (n_cameras: calibration group of each camera, -1 without refined intrinsics).
+extern "C" int probe_rig(const pb_problem_desc* pr, const pb_solve_options* op, int* out_i, int* capture_block,
+                         int* sensor_block, int* pairs, int max_pairs, double* cameras, int* fixed, int* groups) {
+    using namespace pb;
+    HostModel m;
+    std::string err;
+    const int rc = build_host_model(pr, op, &m, &err);
+    g_msg = err;
+    out_i[0] = rc;
+    if (rc) return rc;
+    const RigModel& R = m.rig;
+    out_i[1] = R.ncapb;
+    out_i[2] = R.nsenb;
+    out_i[3] = R.P;
+    out_i[4] = static_cast<int>(R.pairs.size());
+    out_i[5] = m.ncb;
+    out_i[6] = static_cast<int>(m.fixed_cams.size());
+    out_i[7] = m.ref_param ? 1 : 0;
+    for (int k = 0; k < R.ncap; ++k) capture_block[k] = R.capture_block.empty() ? -1 : R.capture_block[k];
+    for (int s = 0; s < R.nsen; ++s) sensor_block[s] = R.sensor_block.empty() ? -1 : R.sensor_block[s];
+    for (int i = 0; i < static_cast<int>(R.pairs.size()) && i < max_pairs; ++i) {
+        pairs[2 * i] = R.pairs[i].first;
+        pairs[2 * i + 1] = R.pairs[i].second;
+    }
+    std::copy(m.cams_in.begin(), m.cams_in.end(), cameras);
+    for (size_t i = 0; i < m.fixed_cams.size(); ++i) fixed[i] = m.fixed_cams[i];
+    for (int c = 0; c < m.nc; ++c) groups[c] = m.ng > 0 ? m.calib_group[c] : -1;
+    return 0;
+}
+
+// The rig term lists checked by brute force: every rig block pair (I, J) of the CSR gets exactly the
+// camera-block CSR entries (a, b) with I chained to a and J chained to b, and every rig block the
+// camera blocks chained to it.  Returns 0 when they agree, else the first failing rig block + 1.
+extern "C" int probe_rig_terms(const pb_problem_desc* pr, const pb_solve_options* op) {
+    using namespace pb;
+    HostModel m;
+    std::string err;
+    if (build_host_model(pr, op, &m, &err)) {
+        g_msg = err;
+        return -1;
+    }
+    const RigModel& R = m.rig;
+    const int nrb = R.nrb;
+    std::vector<std::vector<std::pair<int, int>>> want(R.up_pos.size());
+    auto up_index = [&](int I, int J) {
+        for (size_t u = 0; u < R.up_pos.size(); ++u) {
+            const int p = R.up_pos[u];
+            int row = 0;
+            while (R.row_ptr[row + 1] <= p) ++row;
+            if (row == I && R.col_idx[p] == J) return static_cast<int>(u);
+        }
+        return -1;
+    };
+    for (int a = 0; a < m.ncb; ++a)
+        for (int p = m.row_ptr[a]; p < m.row_ptr[a + 1]; ++p) {
+            const int b = m.col_idx[p];
+            const int ra[2] = {R.cb_cap_block[a], R.cb_sen_block[a]}, rb[2] = {R.cb_cap_block[b], R.cb_sen_block[b]};
+            for (int x = 0; x < 2; ++x)
+                for (int y = 0; y < 2; ++y) {
+                    if (ra[x] < 0 || rb[y] < 0 || ra[x] > rb[y]) continue;
+                    const int u = up_index(ra[x], rb[y]);
+                    if (u < 0) return 1 + ra[x];
+                    want[u].emplace_back(p, a << 2 | x << 1 | y);
+                }
+        }
+    for (size_t u = 0; u < want.size(); ++u) {
+        const int n = R.term_begin[u + 1] - R.term_begin[u];
+        if (n != static_cast<int>(want[u].size())) return 1 + static_cast<int>(u);
+        for (int t = 0; t < n; ++t) {
+            const int q = R.term_begin[u] + t;
+            if (R.terms[2 * q] != want[u][t].first || R.terms[2 * q + 1] != want[u][t].second)
+                return 1 + static_cast<int>(u);
+        }
+    }
+    for (int I = 0; I < nrb; ++I) {
+        std::vector<int> items;
+        for (int a = 0; a < m.ncb; ++a) {
+            if (R.cb_cap_block[a] == I) items.push_back(a << 1);
+            if (R.cb_sen_block[a] == I) items.push_back(a << 1 | 1);
+        }
+        const std::vector<int> got(R.blk_items.begin() + R.blk_begin[I], R.blk_items.begin() + R.blk_begin[I + 1]);
+        if (got != items) return 1 + I;
+    }
+    return 0;
+}
