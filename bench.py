@@ -35,7 +35,7 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="aerial",
-                    choices=["aerial", "aerial_gcp", "aerial3000_gcp", "ring", "windows", "adjoint"])
+                    choices=["aerial", "aerial_gcp", "aerial3000_gcp", "rig3000", "ring", "windows", "adjoint"])
     ap.add_argument("--windows", type=int, default=256, help="local-BA windows of the windows workload")
     ap.add_argument("--workers", type=int, default=0,
                     help="worker contexts of the windows workload (0: chosen by the batch autotuner)")
@@ -54,7 +54,7 @@ def parse_args():
 # was generated (tests/golden/aerial_500cam_200kpt_oracle.npz: 36 iterations); the control-point
 # workloads have no CPU fixture and use the iteration counts of the FP64 GPU path on them.  The
 # 20-camera ring is solved in full on the CPU (a fraction of a second), with no scaling.
-FP64_GPU_ITERATIONS = {"aerial_gcp": 21, "aerial3000_gcp": 27}
+FP64_GPU_ITERATIONS = {"aerial_gcp": 21, "aerial3000_gcp": 27, "rig3000": 40}
 
 
 def converged_iterations(workload_name):
@@ -119,6 +119,26 @@ def workload(name, problem=None):
             # complete control-point gauge, plain parameterisation
             synth.with_control_points(prob, n=40, sigma=0.02, seed=3)
             cfg.update(workload=cfg["workload"] + "_40gcp", control_points=len(prob.controlPoints))
+    elif name == "rig3000":
+        # the large oblique survey block: 600 captures of 5-camera rigs (nadir plus four obliques at
+        # 45 degrees; the nadir sensor fixed, the four oblique extrinsics refined jointly), 1.5 M
+        # points, ~8 M observations, 40 control points (2 cm), 10 scale bars (5 mm), 0.7 px noise,
+        # 5 % outliers; the scale bars put the solve on the general path, the reduced solve runs to
+        # 1e-6 relative residual
+        prob = synth.rig_grid_problem(seed=21)
+        synth.with_control_points(prob, n=40, sigma=0.02, seed=3)
+        synth.with_scale_bars(prob, n=10, sigma=0.005, seed=5)
+        opts.solver.imageRobustLoss = ImageRobustLoss.Cauchy
+        opts.solver.imageRobustLossScalePixels = 1.5
+        opts.solver.maxIterations = 200
+        opts.backend.linearRelativeTolerance = 1e-6
+        cfg = {"workload": "rig_block_%dcap_5cam_%dkpt_40gcp_10bars" % (len(prob.rig.captures),
+                                                                       round(prob.n_tracks / 1000)),
+               "cameras": prob.n_cameras, "captures": len(prob.rig.captures), "sensors": len(prob.rig.sensors),
+               "tracks": prob.n_tracks, "observations": prob.n_obs, "control_points": len(prob.controlPoints),
+               "scale_bars": len(prob.scaleBarConstraints), "loss": "cauchy_1.5px", "refined_intrinsics": "none",
+               "linear_relative_tolerance": 1e-6, "max_lm_iterations": opts.solver.maxIterations,
+               "stopping": "step RMS <= 1e-6 (converged)"}
     else:
         prob = synth.ring_problem(seed=7)
         opts.solver.imageRobustLoss = ImageRobustLoss.Huber
@@ -493,6 +513,7 @@ def run_gb300(args, rank, world, local_rank):
     clocks = sampler.stop()
     ms_mixed = max_over_ranks(statistics.mean(t_mixed), world)
     out_mixed = ctx.download()
+    rig_mixed = ctx.rig()
     launches = sum(r["gpu_kernel_launches"] for r in reps_mixed)
 
     # FP64 GPU paths (same kernels in double precision): the trajectory-parity arm refactors the
@@ -501,6 +522,7 @@ def run_gb300(args, rank, world, local_rank):
     ctx.copts.precision = 0
     t_64, reps_64 = timed_solves(max(1, args.steps // 2), 1)
     out_64 = ctx.download()
+    rig_64 = ctx.rig()
     ms_64 = statistics.mean(t_64)
     ctx.copts.factor_reuse = 1
     t_64r, reps_64r = timed_solves(max(1, args.steps // 2), 1)
@@ -662,6 +684,20 @@ def run_gb300(args, rank, world, local_rank):
         "gpu_launches": launches,
         "clocks": clocks,
     }
+    if rig_mixed is not None:
+        # rig block: capture centres and sensor extrinsics of the mixed path against the FP64 path,
+        # and the refined oblique lever arms and rotations against the generator's truth
+        ts = getattr(prob, "truth_sensors", None)
+        line["rig"] = {
+            "capture_blocks": rep_t["rig_capture_blocks"], "sensor_blocks": rep_t["rig_sensor_blocks"],
+            "mixed_vs_fp64_capture_centre_rel_err": float(np.abs(rig_mixed["captures"][:, 9:12] -
+                                                                 rig_64["captures"][:, 9:12]).max() / scale),
+            "mixed_vs_fp64_sensor_max_abs_diff": float(np.abs(rig_mixed["sensors"] - rig_64["sensors"]).max()),
+            "sensor_lever_err_vs_truth_m": None if ts is None else
+            float(np.abs(rig_mixed["sensors"][:, 9:12] - ts[:, 9:12]).max()),
+            "sensor_rotation_err_vs_truth": None if ts is None else
+            float(np.abs(rig_mixed["sensors"][:, :9] - ts[:, :9]).max()),
+            "general_path": bool(rep_t["general_path_used"]), "promoted_point_blocks": rep_t["promoted_point_blocks"]}
     if cpu:
         line["cpu_baseline"] = cpu
     if args.workload == "aerial" and world == 1 and not args.no_secondary:

@@ -84,6 +84,7 @@ void pb_set_assemble_smem_f64(size_t bytes);
 void launch_effective(const Shape& S, const DevPtrs& D, cudaStream_t st);
 // Rig problems (pb_rig.cu): capture and sensor state, the chain maps of the camera blocks and the
 // reduced system over the rig's pose blocks (captures, then sensors).
+constexpr int kRigSegTerms = 64;  // pose terms summed by one warp before the per-block sum
 struct RigDev {
     int ncap, nsen, nrb, ncb, nup, nnzb;
     double* cap_state;   // ncap * 12: rotation (9), centre (3)
@@ -111,6 +112,13 @@ struct RigDev {
     int* term_begin;
     int* terms;          // 2 per term: camera-block CSR position, a << 2 | sensor row << 1 | sensor column
     const int* cb_col_idx;  // column indices of the camera-block CSR
+    // segments of the pose terms (consecutive terms of one upper block, at most kRigSegTerms):
+    // seg_begin[s] first term of segment s (nseg + 1); up_seg_begin[u] first segment of upper
+    // block u (nup + 1); seg_part the segments' partial sums (36 each)
+    int nseg;
+    int* seg_begin;
+    int* up_seg_begin;
+    double* seg_part;
     int* blk_begin;
     int* blk_items;
     // the rig system: pose blocks, border (6 nrb x nbw) and its transpose, right-hand side

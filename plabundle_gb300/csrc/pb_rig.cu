@@ -12,7 +12,8 @@
 // assembly runs unchanged on one 6-column block per camera (the kernels' camera blocks) and the
 // reduced system over the rig's blocks is S_rig[I][J] = sum M_aI^T S[a][b] M_bJ over the camera
 // blocks a, b chained to I and J, B_rig[I] = sum M_aI^T B[a], g_rig[I] = sum M_aI^T g[a].  The
-// sums follow host-built term lists in a fixed order.  The rig pose diagonal is then damped as
+// sums follow host-built term lists in a fixed order: the pose terms of one rig block in segments
+// of kRigSegTerms consecutive terms (one warp each), then the segments in order.  The rig pose diagonal is then damped as
 // finalizePrimaryDiagonal(1 + damping, 1) damps every primary diagonal, the solution is mapped
 // back to the camera blocks (camera delta = Mc capture delta + Ms sensor delta) for the point
 // back-substitution, and the trial states update captures and sensors with the plain pose delta
@@ -88,40 +89,77 @@ __global__ void k_rig_maps(RigDev R) {
         }
 }
 
-// One thread per entry of an upper rig block, per entry of a border row, per rhs entry.
-__global__ void k_rig_transform(RigDev R, const double* __restrict__ vals, const double* __restrict__ border,
-                                const double* __restrict__ rhs, int nbw, double damping) {
-    const long long nU = static_cast<long long>(R.nup) * 36;
+// Pose blocks, first pass: one warp per segment of at most kRigSeg terms of one upper rig block.
+// Per term (camera-block CSR entry p = (a, b) and the sides of its chains) the warp forms
+// Y = S_ab M_b in shared memory and Z = M_a^T Y, and keeps the running sum of Z over the segment's
+// terms in order (lane e holds entries e and e + 32 of the 6x6 block); the partial goes to
+// seg_part[segment].
+__global__ void __launch_bounds__(256) k_rig_segments(RigDev R, const double* __restrict__ vals) {
+    __shared__ double sY[8][36];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int seg = blockIdx.x * 8 + warp;
+    if (seg >= R.nseg) return;
+    double* Y = sY[warp];
+    const int t0 = R.seg_begin[seg], t1 = R.seg_begin[seg + 1];
+    const int e0 = lane, e1 = lane + 32;  // entries (row-major 6x6); e1 valid for lanes 0-3
+    double acc0 = 0.0, acc1 = 0.0;
+    for (int t = t0; t < t1; ++t) {
+        const int p = R.terms[2 * t], code = R.terms[2 * t + 1];
+        const int a = code >> 2, b = R.cb_col_idx[p];
+        const double* Ma = R.maps + static_cast<size_t>(a) * 72 + ((code >> 1) & 1) * 36;
+        const double* Mb = R.maps + static_cast<size_t>(b) * 72 + (code & 1) * 36;
+        const double* Sb = vals + static_cast<size_t>(p) * 36;
+        // Y[k][q] = sum_l S[k][l] Mb[l][q]
+        for (int e = lane; e < 36; e += 32) {
+            const int k = e / 6, q = e - 6 * (e / 6);
+            double v = 0.0;
+            for (int l = 0; l < 6; ++l) v += Sb[k * 6 + l] * Mb[l * 6 + q];
+            Y[e] = v;
+        }
+        __syncwarp();
+        {
+            const int r = e0 / 6, q = e0 - 6 * (e0 / 6);
+            double v = 0.0;
+            for (int k = 0; k < 6; ++k) v += Ma[k * 6 + r] * Y[k * 6 + q];
+            acc0 += v;
+        }
+        if (e1 < 36) {
+            const int r = e1 / 6, q = e1 - 6 * (e1 / 6);
+            double v = 0.0;
+            for (int k = 0; k < 6; ++k) v += Ma[k * 6 + r] * Y[k * 6 + q];
+            acc1 += v;
+        }
+        __syncwarp();
+    }
+    double* out = R.seg_part + static_cast<size_t>(seg) * 36;
+    out[e0] = acc0;
+    if (e1 < 36) out[e1] = acc1;
+}
+
+// Pose blocks, second pass: one thread per entry of an upper rig block sums its segments in order,
+// damps the diagonal (finalizePrimaryDiagonal(1 + damping, 1)) and writes both orientations.
+__global__ void k_rig_pose_sum(RigDev R, double damping) {
+    const long long e = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (e >= static_cast<long long>(R.nup) * 36) return;
+    const int u = static_cast<int>(e / 36), rq = static_cast<int>(e - 36LL * u);
+    const int r = rq / 6, q = rq - 6 * (rq / 6);
+    double v = 0.0;
+    for (int g = R.up_seg_begin[u]; g < R.up_seg_begin[u + 1]; ++g) v += R.seg_part[static_cast<size_t>(g) * 36 + rq];
+    const int tp = R.up_tpos[u];
+    if (tp < 0 && r == q) v = v != 0.0 ? v * (1.0 + damping) : 1.0;
+    R.vals[static_cast<size_t>(R.up_pos[u]) * 36 + rq] = v;
+    if (tp >= 0) R.vals[static_cast<size_t>(tp) * 36 + q * 6 + r] = v;
+}
+
+// Border rows and right-hand side: one thread per entry of a border row and per rhs entry.
+__global__ void k_rig_border_rhs(RigDev R, const double* __restrict__ border, const double* __restrict__ rhs, int nbw) {
     const long long nB = 6LL * R.nrb * nbw;
     const long long nG = 6LL * R.nrb + nbw;
-    const long long tot = nU + nB + nG;
+    const long long tot = nB + nG;
     for (long long e = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; e < tot;
          e += static_cast<long long>(gridDim.x) * blockDim.x) {
-        if (e < nU) {
-            const int u = static_cast<int>(e / 36), rq = static_cast<int>(e - 36LL * u);
-            const int r = rq / 6, q = rq - 6 * (rq / 6);
-            double v = 0.0;
-            for (int t = R.term_begin[u]; t < R.term_begin[u + 1]; ++t) {
-                const int p = R.terms[2 * t], code = R.terms[2 * t + 1];
-                const int a = code >> 2, b = R.cb_col_idx[p];  // camera blocks of the row and column
-                const double* Ma = R.maps + static_cast<size_t>(a) * 72 + ((code >> 1) & 1) * 36;
-                const double* Mb = R.maps + static_cast<size_t>(b) * 72 + (code & 1) * 36;
-                const double* Sb = vals + static_cast<size_t>(p) * 36;
-                double acc = 0.0;
-                for (int k = 0; k < 6; ++k) {
-                    double sm = 0.0;
-                    for (int l = 0; l < 6; ++l) sm += Sb[k * 6 + l] * Mb[l * 6 + q];
-                    acc += Ma[k * 6 + r] * sm;
-                }
-                v += acc;
-            }
-            const int tp = R.up_tpos[u];
-            if (tp < 0 && r == q) v = v != 0.0 ? v * (1.0 + damping) : 1.0;
-            R.vals[static_cast<size_t>(R.up_pos[u]) * 36 + rq] = v;
-            if (tp >= 0) R.vals[static_cast<size_t>(tp) * 36 + q * 6 + r] = v;
-        } else if (e < nU + nB) {
-            const long long f = e - nU;
-            const int row = static_cast<int>(f / nbw), j = static_cast<int>(f - static_cast<long long>(row) * nbw);
+        if (e < nB) {
+            const int row = static_cast<int>(e / nbw), j = static_cast<int>(e - static_cast<long long>(row) * nbw);
             const int I = row / 6, r = row - 6 * I;
             double v = 0.0;
             for (int t = R.blk_begin[I]; t < R.blk_begin[I + 1]; ++t) {
@@ -129,10 +167,10 @@ __global__ void k_rig_transform(RigDev R, const double* __restrict__ vals, const
                 const double* M = R.maps + static_cast<size_t>(a) * 72 + (code & 1) * 36;
                 for (int k = 0; k < 6; ++k) v += M[k * 6 + r] * border[static_cast<size_t>(6 * a + k) * nbw + j];
             }
-            R.border[f] = v;
+            R.border[e] = v;
             R.border_t[static_cast<size_t>(j) * (6 * R.nrb) + row] = v;
         } else {
-            const int i = static_cast<int>(e - nU - nB);
+            const int i = static_cast<int>(e - nB);
             if (i < 6 * R.nrb) {
                 const int I = i / 6, r = i - 6 * I;
                 double v = 0.0;
@@ -227,9 +265,12 @@ void launch_rig_maps(const RigDev& R, cudaStream_t st) {
 
 void launch_rig_transform(const RigDev& R, const double* vals, const double* border, const double* rhs, int nbw,
                           double damping, cudaStream_t st) {
-    const long long tot = static_cast<long long>(R.nup) * 36 + 6LL * R.nrb * nbw + 6LL * R.nrb + nbw;
+    if (R.nseg > 0) k_rig_segments<<<(R.nseg + 7) / 8, 256, 0, st>>>(R, vals);
+    const long long nu = static_cast<long long>(R.nup) * 36;
+    if (nu > 0) k_rig_pose_sum<<<static_cast<unsigned>((nu + 255) / 256), 256, 0, st>>>(R, damping);
+    const long long tot = 6LL * R.nrb * nbw + 6LL * R.nrb + nbw;
     const int grid = static_cast<int>(std::min<long long>(std::max<long long>(1, (tot + 255) / 256), 152LL * 16));
-    k_rig_transform<<<grid, 256, 0, st>>>(R, vals, border, rhs, nbw, damping);
+    k_rig_border_rhs<<<grid, 256, 0, st>>>(R, border, rhs, nbw);
 }
 
 void launch_rig_expand(const RigDev& R, const double* xr, int nbw, int nglob, cudaStream_t st) {

@@ -481,6 +481,19 @@ void upload_structure(pb_gpu_ctx* c) {
         R.cb_col_idx = D.col_idx;
         R.blk_begin = upload_new(A, rm.blk_begin, st);
         R.blk_items = upload_new(A, rm.blk_items, st);
+        {
+            // segments of at most kRigSegTerms consecutive pose terms of one upper block
+            std::vector<int> sb, ub(1, 0);
+            for (int u = 0; u < R.nup; ++u) {
+                for (int t = rm.term_begin[u]; t < rm.term_begin[u + 1]; t += kRigSegTerms) sb.push_back(t);
+                ub.push_back(static_cast<int>(sb.size()));
+            }
+            sb.push_back(rm.term_begin.empty() ? 0 : rm.term_begin.back());
+            R.nseg = static_cast<int>(sb.size()) - 1;
+            R.seg_begin = upload_new(A, sb, st);
+            R.up_seg_begin = upload_new(A, ub, st);
+            R.seg_part = A.alloc<double>(static_cast<size_t>(std::max(1, R.nseg)) * 36);
+        }
         const int nbw = c->ext_on ? c->ext.nbx : S.nb;
         const size_t nr6 = static_cast<size_t>(6) * rm.nrb;
         R.vals = A.alloc<double>(static_cast<size_t>(std::max(1, R.nnzb)) * 36);
@@ -597,7 +610,7 @@ void rig_transform(pb_gpu_ctx* c, double damping) {
     launch_rig_maps(c->rig, c->stream);
     launch_rig_transform(c->rig, c->red.vals, c->ext_on ? c->ext.border : c->red.border,
                          c->ext_on ? c->ext.rhs : c->red.rhs, nbw, damping, c->stream);
-    c->launches += 2;
+    c->launches += 4;
     check(cudaGetLastError(), "rig map launch");
 }
 
@@ -768,16 +781,26 @@ int solve_dense(pb_gpu_ctx* c, double rel, double abs_tol, int max_it, bool* con
     // factorised and grows tenfold on failure.  The FP64 factor starts unshifted.
     double shift = f32 ? c->shift32 : 0.0;
     int st = 0;
+    static const bool trace = std::getenv("PB_GPU_TRACE") != nullptr;
+    const auto tf0 = std::chrono::steady_clock::now();
+    int attempts = 0;
     for (int attempt = 0; attempt < 6; ++attempt) {
+        ++attempts;
         st = dense_factor<T>(sys, W, shift, c->stream, &c->launches);
         if (st < 0) throw CudaError(std::string("dense factorisation failed: ") + cudaGetErrorString(cudaGetLastError()));
         if (st == 0 || (st & 1)) break;
         shift = shift == 0.0 ? 1e-9 : shift * 10.0;
     }
+    const auto tf1 = std::chrono::steady_clock::now();
     if (st) return 1;
     if (f32) c->shift32 = shift;
     const int rc = dense_pcg<T>(sys, W, rhs, rel, abs_tol, max_it, iterations, relres, converged, c->h_scratch + 40,
                                 c->stream, &c->launches);
+    if (trace)
+        std::fprintf(stderr, "PB_GPU_TRACE dense n=%d factor_attempts=%d shift=%.1e factor_ms=%.3f cg_ms=%.3f cg_it=%d\n",
+                     W.n, attempts, shift, std::chrono::duration<double, std::milli>(tf1 - tf0).count(),
+                     std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tf1).count(),
+                     *iterations);
     if (rc < 0) throw CudaError(std::string("dense CG failed: ") + cudaGetErrorString(cudaGetLastError()));
     if (reuse) {
         c->f32_age = rc == 0 ? 1 : -1;

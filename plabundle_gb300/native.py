@@ -299,7 +299,7 @@ def solve_options(options, problem=None) -> SolveOptionsC:
     o.precision = int(Precision.Mixed if b.enablePlaMatrixMixedPrecision else Precision.Fp64)
     o.max_linear_iterations = b.maxLinearIterations
     # 0: the reference's tolerance of the path (2e-10 online, 1e-12 general)
-    o.linear_relative_tolerance = 0.0
+    o.linear_relative_tolerance = float(getattr(b, "linearRelativeTolerance", 0.0))
     o.linear_absolute_tolerance = 1.0e-12
     o.refinement_sweeps = b.refinementSweeps
     o.preconditioner_cluster_size = b.plaMatrixPreconditionerClusterSize

@@ -414,6 +414,9 @@ class BackendOptions:
     # dense-factor reuse across LM iterations: 0 default (mixed path keeps its FP32 factor, FP64
     # path refactors every iteration), 1 keep on both paths, 2 refactor on both paths
     factorReuse: int = 0
+    # relative tolerance of the reduced solve; 0: the reference's tolerance of the path (2e-10 on
+    # the online path, 1e-12 on the general path, BundleAdjustPlaMatrix.cpp:321-330)
+    linearRelativeTolerance: float = 0.0
 
 
 @dataclass

@@ -440,7 +440,8 @@ def _visible_pairs(cams: np.ndarray, X: np.ndarray, zlo: float, zhi: float, cell
         cis.append(np.full(int(ok.sum()), c, np.int32))
     pi = np.concatenate(pis) if pis else np.zeros(0, np.int64)
     ci = np.concatenate(cis) if cis else np.zeros(0, np.int32)
-    o = np.lexsort((ci, pi))
+    # the pairs are grouped by ascending camera: a stable sort by point gives (point, camera) order
+    o = np.argsort(pi, kind="stable")
     return pi[o], ci[o]
 
 
@@ -449,7 +450,9 @@ def _choose_views_sparse(pi, ci, n_pts, rng, min_views, max_views):
     k ~ U{min_views..max_views}, in camera order; from sorted (point, camera) pairs."""
     k = rng.integers(min_views, max_views + 1, n_pts)
     keys = rng.random(pi.size)
-    o = np.lexsort((keys, pi))
+    # order by point, then by the random key (the point index plus a key in [0, 1) is exact in
+    # FP64 for the point counts used here)
+    o = np.argsort(pi.astype(np.float64) + keys)
     start = np.searchsorted(pi[o], np.arange(n_pts + 1))
     rank = np.arange(pi.size) - np.repeat(start[:-1], np.diff(start))
     keep = np.zeros(pi.size, bool)
