@@ -709,9 +709,10 @@ def run_gb300(args, rank, world, local_rank):
 
 
 def secondary_records(prob, local_rank):
-    """Compact records of the windows and backward-pass workloads (their own bench lines, with
-    fewer timed repetitions: 2 timed batches of the 256 windows; 3 backward passes after 3 warm-up
-    passes and a 16-observation finite-difference check)."""
+    """Compact records of the windows, backward-pass and rig-block workloads (their own bench lines,
+    with fewer timed repetitions: 2 timed batches of the 256 windows; 3 backward passes after 3
+    warm-up passes and a 16-observation finite-difference check; 2 timed mixed solves and one of
+    each FP64 arm of the 3 000-camera rig block)."""
     out = {}
     t0 = time.perf_counter()
     out["windows"] = measure_windows(256, 0, 2, 0, 1, local_rank)
@@ -719,7 +720,79 @@ def secondary_records(prob, local_rank):
     t0 = time.perf_counter()
     out["adjoint"] = measure_adjoint(3, 3, 16, 0, 1, local_rank, problem=prob)
     out["adjoint"]["wall_seconds"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    out["rig_block"] = measure_rig_block(local_rank)
+    out["rig_block"]["wall_seconds"] = time.perf_counter() - t0
     return out
+
+
+def measure_rig_block(local_rank, steps=2):
+    """The large oblique survey block (workload rig3000: 600 five-camera rig captures, 1.5 M points,
+    ~8 M observations, 40 control points, 10 scale bars): time to converge of the mixed path (CUDA
+    events, L2 flushed, `steps` timed solves after one warm-up) against the FP64 path with the
+    mixed path's factor reuse and the FP64 path refactoring every iteration (one timed solve each
+    after one warm-up), with the errors between the arms and of the refined sensor extrinsics
+    against the generator's truth."""
+    import numpy as np
+    import torch
+    from plabundle_gb300.device import Gb300Context
+    torch.cuda.set_device(local_rank)
+    t_gen = time.perf_counter()
+    prob, opts, cfg = workload("rig3000")
+    t_gen = time.perf_counter() - t_gen
+    opts.backend.enablePlaMatrixMixedPrecision = True
+    ctx = Gb300Context(local_rank)
+    assert ctx.upload(prob, opts) == 0, ctx.L.pb_gpu_last_error(ctx.ctx)
+    stream = torch.cuda.ExternalStream(ctx.stream_handle())
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def timed(k):
+        ctx.solve()
+        ts, reps = [], []
+        for _ in range(k):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            reps.append(ctx.solve())
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return statistics.mean(ts), reps[-1], ctx.download(), ctx.rig()
+
+    ms_m, rep_m, out_m, rig_m = timed(steps)
+    ctx.copts.precision = 0
+    ctx.copts.factor_reuse = 1
+    ms_r, rep_r, out_r, rig_r = timed(1)
+    ctx.copts.factor_reuse = 2
+    ms_f, rep_f, _, _ = timed(1)
+    ctx.close()
+    C = out_r["cameras"][:, 9:12]
+    scale = float(np.linalg.norm(C - C.mean(0), axis=1).max())
+    ts = prob.truth_sensors
+    return {"metric": "BA time-to-converge, mixed vs FP64 on GB300 (rig block)", "value": ms_m, "unit": "ms",
+            "impl": "gb300", "n_gpus": 1, "steps": steps, "warmup": 1, "higher_is_better": False,
+            "dtype": "f32+f64 (mixed)", "data": "synthetic (seeded)",
+            "config": dict(cfg, l2="flushed between steps (256 MB write)"),
+            "fp64_reuse_path_ms": ms_r, "fp64_refactor_path_ms": ms_f,
+            "speedup_vs_fp64_path": min(ms_r, ms_f) / ms_m, "speedup_vs_fp64_refactor_path": ms_f / ms_m,
+            "iterations": {"mixed": rep_m["iterations"], "fp64_reuse": rep_r["iterations"],
+                           "fp64_refactor": rep_f["iterations"]},
+            "status": {"mixed": rep_m["status"], "fp64_reuse": rep_r["status"], "fp64_refactor": rep_f["status"]},
+            "solve_breakdown_ms": {k: rep_m[k] for k in ("assembly_ms", "linear_ms", "back_substitution_ms",
+                                                         "objective_ms", "total_ms")},
+            "mixed_vs_fp64": {"final_cost_rel_diff": abs(rep_m["final_cost"] - rep_r["final_cost"]) / rep_r["final_cost"],
+                              "camera_centre_rel_err": float(np.abs(out_m["cameras"][:, 9:12] - C).max() / scale),
+                              "capture_centre_rel_err": float(np.abs(rig_m["captures"][:, 9:12] -
+                                                                     rig_r["captures"][:, 9:12]).max() / scale),
+                              "sensor_max_abs_diff": float(np.abs(rig_m["sensors"] - rig_r["sensors"]).max()),
+                              "inlier_mask_identical": bool(np.array_equal(out_m["valid"], out_r["valid"]))},
+            "sensor_lever_err_vs_truth_m": float(np.abs(rig_m["sensors"][:, 9:12] - ts[:, 9:12]).max()),
+            "sensor_rotation_err_vs_truth": float(np.abs(rig_m["sensors"][:, :9] - ts[:, :9]).max()),
+            "rig_blocks": {"captures": rep_m["rig_capture_blocks"], "sensors": rep_m["rig_sensor_blocks"],
+                           "promoted_point_blocks": rep_m["promoted_point_blocks"]},
+            "generator_seconds": t_gen}
 
 
 def main():
