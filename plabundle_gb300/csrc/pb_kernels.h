@@ -85,6 +85,7 @@ void launch_effective(const Shape& S, const DevPtrs& D, cudaStream_t st);
 // Rig problems (pb_rig.cu): capture and sensor state, the chain maps of the camera blocks and the
 // reduced system over the rig's pose blocks (captures, then sensors).
 constexpr int kRigSegTerms = 64;  // pose terms summed by one warp before the per-block sum
+constexpr int kRigItemSeg = 32;   // camera blocks of a rig block summed by one warp (border, rhs)
 struct RigDev {
     int ncap, nsen, nrb, ncb, nup, nnzb;
     double* cap_state;   // ncap * 12: rotation (9), centre (3)
@@ -119,6 +120,13 @@ struct RigDev {
     int* seg_begin;
     int* up_seg_begin;
     double* seg_part;
+    // segments of the camera blocks of one rig block (at most kRigItemSeg): bseg_begin[g] first
+    // item of segment g (nbseg + 1), blk_seg_begin[I] first segment of rig block I (nrb + 1),
+    // bpart the segments' border and rhs partials (6 (nbw + 1) each)
+    int nbseg;
+    int* bseg_begin;
+    int* blk_seg_begin;
+    double* bpart;
     int* blk_begin;
     int* blk_items;
     // the rig system: pose blocks, border (6 nrb x nbw) and its transpose, right-hand side

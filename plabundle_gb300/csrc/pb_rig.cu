@@ -13,7 +13,8 @@
 // reduced system over the rig's blocks is S_rig[I][J] = sum M_aI^T S[a][b] M_bJ over the camera
 // blocks a, b chained to I and J, B_rig[I] = sum M_aI^T B[a], g_rig[I] = sum M_aI^T g[a].  The
 // sums follow host-built term lists in a fixed order: the pose terms of one rig block in segments
-// of kRigSegTerms consecutive terms (one warp each), then the segments in order.  The rig pose diagonal is then damped as
+// of kRigSegTerms consecutive terms (one warp each), then the segments in order; the border and
+// right-hand side over segments of kRigItemSeg camera blocks likewise.  The rig pose diagonal is then damped as
 // finalizePrimaryDiagonal(1 + damping, 1) damps every primary diagonal, the solution is mapped
 // back to the camera blocks (camera delta = Mc capture delta + Ms sensor delta) for the point
 // back-substitution, and the trial states update captures and sensors with the plain pose delta
@@ -109,25 +110,41 @@ __global__ void __launch_bounds__(256) k_rig_segments(RigDev R, const double* __
         const double* Ma = R.maps + static_cast<size_t>(a) * 72 + ((code >> 1) & 1) * 36;
         const double* Mb = R.maps + static_cast<size_t>(b) * 72 + (code & 1) * 36;
         const double* Sb = vals + static_cast<size_t>(p) * 36;
-        // Y[k][q] = sum_l S[k][l] Mb[l][q]
+        // Y[k][q] = sum_l S[k][l] Mb[l][q] over the non-zero entries of the map: Mc has the unit
+        // diagonal and -[L]x in rows 3-5 / columns 0-2, Ms the rotation twice on its diagonal
+        const bool b_sensor = code & 1, a_sensor = (code >> 1) & 1;
         for (int e = lane; e < 36; e += 32) {
             const int k = e / 6, q = e - 6 * (e / 6);
-            double v = 0.0;
-            for (int l = 0; l < 6; ++l) v += Sb[k * 6 + l] * Mb[l * 6 + q];
+            double v;
+            if (!b_sensor) {
+                v = Sb[k * 6 + q];
+                if (q < 3)
+                    for (int j = 0; j < 3; ++j) v += Sb[k * 6 + 3 + j] * Mb[(3 + j) * 6 + q];
+            } else {
+                const int o = q < 3 ? 0 : 3;
+                v = 0.0;
+                for (int j = 0; j < 3; ++j) v += Sb[k * 6 + o + j] * Mb[(o + j) * 6 + q];
+            }
             Y[e] = v;
         }
         __syncwarp();
-        {
-            const int r = e0 / 6, q = e0 - 6 * (e0 / 6);
-            double v = 0.0;
-            for (int k = 0; k < 6; ++k) v += Ma[k * 6 + r] * Y[k * 6 + q];
-            acc0 += v;
-        }
-        if (e1 < 36) {
-            const int r = e1 / 6, q = e1 - 6 * (e1 / 6);
-            double v = 0.0;
-            for (int k = 0; k < 6; ++k) v += Ma[k * 6 + r] * Y[k * 6 + q];
-            acc1 += v;
+        // Z[r][q] = sum_k Ma[k][r] Y[k][q], likewise
+        for (int h = 0; h < 2; ++h) {
+            const int e = h == 0 ? e0 : e1;
+            if (e >= 36) break;
+            const int r = e / 6, q = e - 6 * (e / 6);
+            double v;
+            if (!a_sensor) {
+                v = Y[r * 6 + q];
+                if (r < 3)
+                    for (int j = 0; j < 3; ++j) v += Ma[(3 + j) * 6 + r] * Y[(3 + j) * 6 + q];
+            } else {
+                const int o = r < 3 ? 0 : 3;
+                v = 0.0;
+                for (int j = 0; j < 3; ++j) v += Ma[(o + j) * 6 + r] * Y[(o + j) * 6 + q];
+            }
+            if (h == 0) acc0 += v;
+            else acc1 += v;
         }
         __syncwarp();
     }
@@ -151,39 +168,53 @@ __global__ void k_rig_pose_sum(RigDev R, double damping) {
     if (tp >= 0) R.vals[static_cast<size_t>(tp) * 36 + q * 6 + r] = v;
 }
 
-// Border rows and right-hand side: one thread per entry of a border row and per rhs entry.
-__global__ void k_rig_border_rhs(RigDev R, const double* __restrict__ border, const double* __restrict__ rhs, int nbw) {
-    const long long nB = 6LL * R.nrb * nbw;
-    const long long nG = 6LL * R.nrb + nbw;
-    const long long tot = nB + nG;
-    for (long long e = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; e < tot;
-         e += static_cast<long long>(gridDim.x) * blockDim.x) {
-        if (e < nB) {
-            const int row = static_cast<int>(e / nbw), j = static_cast<int>(e - static_cast<long long>(row) * nbw);
-            const int I = row / 6, r = row - 6 * I;
-            double v = 0.0;
-            for (int t = R.blk_begin[I]; t < R.blk_begin[I + 1]; ++t) {
-                const int code = R.blk_items[t], a = code >> 1;
-                const double* M = R.maps + static_cast<size_t>(a) * 72 + (code & 1) * 36;
+// Border rows and right-hand side, first pass: one warp per (segment of at most kRigItemSeg
+// camera blocks chained to one rig block, row r of that block); the lanes take the border columns
+// and, as column nbw, the right-hand side, and sum M_a[:, r]^T B[a] over the segment's camera
+// blocks in order into bpart[segment][r][column].
+__global__ void __launch_bounds__(256) k_rig_border_seg(RigDev R, const double* __restrict__ border,
+                                                        const double* __restrict__ rhs, int nbw) {
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (gw >= R.nbseg * 6) return;
+    const int g = gw / 6, r = gw - 6 * (gw / 6);
+    const int w = nbw + 1;
+    const int t0 = R.bseg_begin[g], t1 = R.bseg_begin[g + 1];
+    for (int j = lane; j < w; j += 32) {
+        double v = 0.0;
+        for (int t = t0; t < t1; ++t) {
+            const int code = R.blk_items[t], a = code >> 1;
+            const double* M = R.maps + static_cast<size_t>(a) * 72 + (code & 1) * 36;
+            if (j < nbw) {
                 for (int k = 0; k < 6; ++k) v += M[k * 6 + r] * border[static_cast<size_t>(6 * a + k) * nbw + j];
-            }
-            R.border[e] = v;
-            R.border_t[static_cast<size_t>(j) * (6 * R.nrb) + row] = v;
-        } else {
-            const int i = static_cast<int>(e - nB);
-            if (i < 6 * R.nrb) {
-                const int I = i / 6, r = i - 6 * I;
-                double v = 0.0;
-                for (int t = R.blk_begin[I]; t < R.blk_begin[I + 1]; ++t) {
-                    const int code = R.blk_items[t], a = code >> 1;
-                    const double* M = R.maps + static_cast<size_t>(a) * 72 + (code & 1) * 36;
-                    for (int k = 0; k < 6; ++k) v += M[k * 6 + r] * rhs[6 * a + k];
-                }
-                R.rhs[i] = v;
             } else {
-                R.rhs[i] = rhs[6 * R.ncb + (i - 6 * R.nrb)];
+                for (int k = 0; k < 6; ++k) v += M[k * 6 + r] * rhs[6 * a + k];
             }
         }
+        R.bpart[(static_cast<size_t>(g) * 6 + r) * w + j] = v;
+    }
+}
+
+// Second pass: one thread per border entry and rhs entry of a rig block sums its segments in
+// order; the right-hand side's group and promoted-point entries are copied.
+__global__ void k_rig_border_sum(RigDev R, const double* __restrict__ rhs, int nbw) {
+    const int w = nbw + 1;
+    const long long nA = 6LL * R.nrb * w;
+    const long long e = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (e < nA) {
+        const int row = static_cast<int>(e / w), j = static_cast<int>(e - static_cast<long long>(row) * w);
+        const int I = row / 6, r = row - 6 * I;
+        double v = 0.0;
+        for (int g = R.blk_seg_begin[I]; g < R.blk_seg_begin[I + 1]; ++g)
+            v += R.bpart[(static_cast<size_t>(g) * 6 + r) * w + j];
+        if (j < nbw) {
+            R.border[static_cast<size_t>(row) * nbw + j] = v;
+            R.border_t[static_cast<size_t>(j) * (6 * R.nrb) + row] = v;
+        } else {
+            R.rhs[row] = v;
+        }
+    } else if (e < nA + nbw) {
+        const int i = static_cast<int>(e - nA);
+        R.rhs[6 * R.nrb + i] = rhs[6 * R.ncb + i];
     }
 }
 
@@ -268,9 +299,9 @@ void launch_rig_transform(const RigDev& R, const double* vals, const double* bor
     if (R.nseg > 0) k_rig_segments<<<(R.nseg + 7) / 8, 256, 0, st>>>(R, vals);
     const long long nu = static_cast<long long>(R.nup) * 36;
     if (nu > 0) k_rig_pose_sum<<<static_cast<unsigned>((nu + 255) / 256), 256, 0, st>>>(R, damping);
-    const long long tot = 6LL * R.nrb * nbw + 6LL * R.nrb + nbw;
-    const int grid = static_cast<int>(std::min<long long>(std::max<long long>(1, (tot + 255) / 256), 152LL * 16));
-    k_rig_border_rhs<<<grid, 256, 0, st>>>(R, border, rhs, nbw);
+    if (R.nbseg > 0) k_rig_border_seg<<<(R.nbseg * 6 + 7) / 8, 256, 0, st>>>(R, border, rhs, nbw);
+    const long long tot = 6LL * R.nrb * (nbw + 1) + nbw;
+    if (tot > 0) k_rig_border_sum<<<static_cast<unsigned>((tot + 255) / 256), 256, 0, st>>>(R, rhs, nbw);
 }
 
 void launch_rig_expand(const RigDev& R, const double* xr, int nbw, int nglob, cudaStream_t st) {

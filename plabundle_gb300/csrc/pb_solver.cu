@@ -493,6 +493,18 @@ void upload_structure(pb_gpu_ctx* c) {
             R.seg_begin = upload_new(A, sb, st);
             R.up_seg_begin = upload_new(A, ub, st);
             R.seg_part = A.alloc<double>(static_cast<size_t>(std::max(1, R.nseg)) * 36);
+            // segments of at most kRigItemSeg camera blocks of one rig block (border, rhs)
+            std::vector<int> ib, bb(1, 0);
+            for (int I = 0; I < rm.nrb; ++I) {
+                for (int t = rm.blk_begin[I]; t < rm.blk_begin[I + 1]; t += kRigItemSeg) ib.push_back(t);
+                bb.push_back(static_cast<int>(ib.size()));
+            }
+            ib.push_back(rm.blk_begin.empty() ? 0 : rm.blk_begin.back());
+            R.nbseg = static_cast<int>(ib.size()) - 1;
+            R.bseg_begin = upload_new(A, ib, st);
+            R.blk_seg_begin = upload_new(A, bb, st);
+            R.bpart = A.alloc<double>(static_cast<size_t>(std::max(1, R.nbseg)) * 6 *
+                                      ((c->ext_on ? c->ext.nbx : S.nb) + 1));
         }
         const int nbw = c->ext_on ? c->ext.nbx : S.nb;
         const size_t nr6 = static_cast<size_t>(6) * rm.nrb;
@@ -610,7 +622,7 @@ void rig_transform(pb_gpu_ctx* c, double damping) {
     launch_rig_maps(c->rig, c->stream);
     launch_rig_transform(c->rig, c->red.vals, c->ext_on ? c->ext.border : c->red.border,
                          c->ext_on ? c->ext.rhs : c->red.rhs, nbw, damping, c->stream);
-    c->launches += 4;
+    c->launches += 5;
     check(cudaGetLastError(), "rig map launch");
 }
 
