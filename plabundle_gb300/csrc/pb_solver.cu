@@ -1376,12 +1376,24 @@ void lm_solve_general(pb_gpu_ctx* c, const pb_solve_options& op, pb_solve_report
                     continue;
                 }
                 auto tc = now();
-                // directional decrease by a forward difference of the objective along the step
+                // directional decrease by a forward difference of the objective along the step;
+                // the difference point and the first trial (alpha = 1) share one objective pass
+                // (slot 0: the trial, slot 1: the difference point; each slot's sum is formed
+                // on its own, so the costs are those of two separate passes)
                 double dd = 0.0;
+                double first_trial = kNaN;
                 {
                     const double h = 1.0e-4;
                     double fd;
-                    eval_costs(c, &h, 1, 1, &fd);
+                    if (op.line_search_steps > 0) {
+                        const double al2[2] = {1.0, h};
+                        double c2[2];
+                        eval_costs(c, al2, 2, 1, c2);
+                        first_trial = c2[0];
+                        fd = c2[1];
+                    } else {
+                        eval_costs(c, &h, 1, 1, &fd);
+                    }
                     ++rep->objective_evaluations;
                     if (std::isfinite(fd) && fd < current) dd = (current - fd) / h;
                 }
@@ -1394,7 +1406,8 @@ void lm_solve_general(pb_gpu_ctx* c, const pb_solve_options& op, pb_solve_report
                     const int nbatch = std::min(k0 == 0 ? 1 : kMaxAlpha, op.line_search_steps - k0);
                     double al[kMaxAlpha], costs[kMaxAlpha];
                     for (int i = 0; i < nbatch; ++i) al[i] = std::ldexp(1.0, -(k0 + i));
-                    eval_costs(c, al, nbatch, 1, costs);
+                    if (k0 == 0) costs[0] = first_trial;  // evaluated with the difference point
+                    else eval_costs(c, al, nbatch, 1, costs);
                     for (int i = 0; i < nbatch; ++i) {
                         ++rep->objective_evaluations;
                         cand = costs[i];
