@@ -284,6 +284,14 @@ pb_status pb_gpu_solve(pb_gpu_ctx* ctx, const pb_solve_options* options, pb_solv
 pb_status pb_gpu_download_state(pb_gpu_ctx* ctx, double* cameras, double* points, int8_t* valid,
                                 double* rms_before, double* rms_after, double* intrinsics);
 
+/* Cost history of the last pb_gpu_solve (no counterpart in the reference, whose diagnostics keep
+ * only the initial and final costs, include/plabundle/result.h:91-128): the initial cost, then the
+ * cost after every accepted LM step, with the LM iteration (0 for the initial cost) and the host
+ * time in ms since the solve started.  *count receives the number of entries; at most `capacity`
+ * are written; any array may be NULL. */
+pb_status pb_gpu_get_history(pb_gpu_ctx* ctx, int32_t capacity, int32_t* iterations, double* costs, double* ms,
+                             int32_t* count);
+
 /* Rig problems: the current capture and sensor parameters (Result::refinedRig,
  * include/plabundle/result.h:149), 12 doubles each in the layout of pb_problem_desc's
  * rig_captures / rig_sensors, and the pose block of every capture and sensor (-1: fixed or without

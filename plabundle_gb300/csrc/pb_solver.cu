@@ -182,6 +182,10 @@ struct pb_gpu_ctx {
     PcgSystem<double> sysx{};
     int* ext_flags = nullptr;
     double* bar_d = nullptr;  // bar cost of the current state, then of the trial states
+    // cost history of the last solve: the initial cost, then the cost after every accepted step,
+    // with the LM iteration and the host time since the solve started
+    std::vector<int> hist_it;
+    std::vector<double> hist_cost, hist_ms;
     // rigs: capture / sensor state and the reduced system over the rig's pose blocks (pb_rig.cu)
     bool rig_on = false;
     RigDev rig{};
@@ -603,6 +607,12 @@ void ensure_pcg_partials(pb_gpu_ctx* c) {
 
 void set_assemble_smem(int precision, size_t bytes);
 double extend_system(pb_gpu_ctx* c, double damping);
+
+void record_history(pb_gpu_ctx* c, int iteration, double cost, std::chrono::steady_clock::time_point t0) {
+    c->hist_it.push_back(iteration);
+    c->hist_cost.push_back(cost);
+    c->hist_ms.push_back(std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count());
+}
 
 // Accepts trial `slot` (step length alpha): cameras, groups, points and, for rigs, captures and
 // sensors.
@@ -1061,6 +1071,9 @@ void lm_solve(pb_gpu_ctx* c, const pb_solve_options& op, pb_solve_report* rep) {
     std::memset(rep, 0, sizeof(*rep));
     for (double& v : c->kt) v = 0.0;
     c->launches = 0;
+    c->hist_it.clear();
+    c->hist_cost.clear();
+    c->hist_ms.clear();
     rep->active_tracks = m.active_tracks;
     rep->observation_count = m.obs_count;
     rep->rejected_initial_tracks = m.rejected;
@@ -1111,6 +1124,7 @@ void lm_solve(pb_gpu_ctx* c, const pb_solve_options& op, pb_solve_report* rep) {
             eval_costs(c, nullptr, 1, 0, &cst);
             current = cst;
             rep->initial_cost = current;
+            record_history(c, 0, current, t0);
             if (converged) ++rep->objective_evaluations;
         }
         const int budget = std::max(1, op.max_iterations);
@@ -1131,7 +1145,10 @@ void lm_solve(pb_gpu_ctx* c, const pb_solve_options& op, pb_solve_report* rep) {
                 ++rep->objective_evaluations;
                 if (cost_from_assembly) {
                     current = cost;
-                    if (rep->linearizations == 1) rep->initial_cost = current;
+                    if (rep->linearizations == 1) {
+                        rep->initial_cost = current;
+                        record_history(c, 0, current, t0);
+                    }
                 }
                 if (flags & 1) {
                     ++iterations;
@@ -1208,6 +1225,7 @@ void lm_solve(pb_gpu_ctx* c, const pb_solve_options& op, pb_solve_report* rep) {
                     // solve refactors instead of trying the kept FP32 factor first
                     c->f32_stale = current - cand > 1e-2 * current;
                     current = cand;
+                    record_history(c, iterations, current, t0);
                     ++rep->accepted_steps;
                     damping /= 10.0;
                     converged = accepted_alpha * rg <= 1e-6 && accepted_alpha * rp <= 1e-6;
@@ -1276,6 +1294,9 @@ void lm_solve_general(pb_gpu_ctx* c, const pb_solve_options& op, pb_solve_report
     std::memset(rep, 0, sizeof(*rep));
     for (double& v : c->kt) v = 0.0;
     c->launches = 0;
+    c->hist_it.clear();
+    c->hist_cost.clear();
+    c->hist_ms.clear();
     rep->active_tracks = m.active_tracks;
     rep->observation_count = m.obs_count;
     rep->rejected_initial_tracks = m.rejected;
@@ -1324,6 +1345,7 @@ void lm_solve_general(pb_gpu_ctx* c, const pb_solve_options& op, pb_solve_report
             eval_costs(c, nullptr, 1, 0, &cst);
             current = cst;
             rep->initial_cost = current;
+            record_history(c, 0, current, t0);
             if (converged) ++rep->objective_evaluations;
         }
         const int budget = std::max(1, op.max_iterations);
@@ -1345,7 +1367,10 @@ void lm_solve_general(pb_gpu_ctx* c, const pb_solve_options& op, pb_solve_report
                 if (flags & 2) throw std::runtime_error("linearisation produced an invalid projection");
                 if (cost_from_assembly && !linearized) {
                     current = cost;
-                    if (rep->linearizations == 1) rep->initial_cost = current;
+                    if (rep->linearizations == 1) {
+                        rep->initial_cost = current;
+                        record_history(c, 0, current, t0);
+                    }
                 }
                 linearized = true;
                 if (flags & 1) throw std::runtime_error("eliminated point block is not numerically SPD (positive definite)");
@@ -1440,6 +1465,7 @@ void lm_solve_general(pb_gpu_ctx* c, const pb_solve_options& op, pb_solve_report
                     accept_trial(c, accepted_alpha, accepted_slot);
                     c->f32_stale = current - cand > 1e-2 * current;
                     current = cand;
+                    record_history(c, iterations, current, t0);
                     ++rep->accepted_steps;
                     damping /= 10.0;
                     converged = accepted_alpha * rg <= 1e-6 && accepted_alpha * rp <= 1e-6;
@@ -1691,6 +1717,19 @@ pb_status pb_gpu_get_pairs(pb_gpu_ctx* c, int32_t* pairs) {
     for (size_t i = 0; i < pl.size(); ++i) {
         pairs[2 * i] = pl[i].first;
         pairs[2 * i + 1] = pl[i].second;
+    }
+    return PB_OK;
+}
+
+pb_status pb_gpu_get_history(pb_gpu_ctx* c, int32_t capacity, int32_t* iterations, double* costs, double* ms,
+                             int32_t* count) {
+    if (!c || !count || capacity < 0) return fail(c, PB_ERR_INVALID_ARGUMENT, "invalid history request");
+    const int n = static_cast<int>(c->hist_cost.size());
+    *count = n;
+    for (int i = 0; i < std::min(n, capacity); ++i) {
+        if (iterations) iterations[i] = c->hist_it[i];
+        if (costs) costs[i] = c->hist_cost[i];
+        if (ms) ms[i] = c->hist_ms[i];
     }
     return PB_OK;
 }

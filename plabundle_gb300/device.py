@@ -159,6 +159,18 @@ class Gb300Context:
         return {"cameras": cams, "points": pts, "valid": valid.astype(bool), "rms_before": rb, "rms_after": ra,
                 "intrinsics": intr[:ng]}
 
+    def history(self):
+        """Cost history of the last solve: LM iterations, costs and host ms since the solve
+        started (the initial cost, then every accepted step)."""
+        n = C.c_int32(0)
+        self._check(self.L.pb_gpu_get_history(self.ctx, 0, None, None, None, C.byref(n)), "history")
+        it = np.zeros(n.value, np.int32)
+        cost = np.zeros(n.value)
+        ms = np.zeros(n.value)
+        self._check(self.L.pb_gpu_get_history(self.ctx, n.value, it.ctypes.data, cost.ctypes.data, ms.ctypes.data,
+                                               C.byref(n)), "history")
+        return {"iterations": it, "cost": cost, "ms": ms}
+
     def rig(self):
         """Rig problems: current captures and sensors (12 doubles each) and their pose blocks."""
         st = native.rig_state(self.L, self.ctx, self.problem)

@@ -22,7 +22,7 @@ EXPORTED = [
     "pb_gpu_set_timing",
     "pb_gpu_kernel_times", "pb_gpu_objective_noalloc", "pb_gpu_solve_batch",
     "pb_gpu_save_state", "pb_gpu_restore_state", "pb_gpu_set_observations", "pb_gpu_backward",
-    "pb_gpu_newton_step", "pb_gpu_get_rig",
+    "pb_gpu_newton_step", "pb_gpu_get_rig", "pb_gpu_get_history",
     "pb_bne_create", "pb_bne_destroy", "pb_bne_clear_values", "pb_bne_sizes", "pb_bne_add_residual_blocks",
     "pb_bne_add_primary_residual_blocks", "pb_bne_add_primary_residual_block",
     "pb_bne_add_eliminated_residual_block", "pb_bne_add_residual_block", "pb_bne_add_primary_gradient_block",
@@ -172,6 +172,7 @@ def load(build_if_missing: bool = False):
     L.pb_gpu_backward.argtypes = [vp, vp, vp, vp, vp, vp, vp, C.POINTER(AdjointReportC)]
     L.pb_gpu_newton_step.argtypes = [vp, C.POINTER(dbl), C.POINTER(dbl)]
     L.pb_gpu_get_rig.argtypes = [vp, vp, vp, vp, vp]
+    L.pb_gpu_get_history.argtypes = [vp, i32, vp, vp, vp, C.POINTER(i32)]
     L.pb_bne_create.argtypes = [i32, i32, i32, i32, C.POINTER(vp)]
     L.pb_bne_destroy.argtypes = [vp]
     L.pb_bne_clear_values.argtypes = [vp]

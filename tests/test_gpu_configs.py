@@ -120,3 +120,23 @@ def test_aerial_c1_reaches_the_oracle_solution(aerial_c1, mixed):
     # identical inliers, except a track whose after-RMS sits within 1e-6 px of the threshold
     assert all(abs(m) < 1e-6 for m in cmp["flip_margins_px"]) and cmp["inlier_mask_flips"] <= 2, cmp
     np.testing.assert_allclose(rep["initial_cost"], meta["report"]["initial_cost"], rtol=1e-12)
+
+
+@pytest.mark.gpu
+def test_cost_history_of_a_solve():
+    """pb_gpu_get_history: the initial cost, then one entry per accepted step, costs decreasing,
+    the last entry the final cost, host times increasing."""
+    from plabundle_gb300.device import Gb300Context
+    p = synth.ring_problem(seed=7)
+    o = SolveOptions()
+    o.solver.imageRobustLoss = ImageRobustLoss.Huber
+    o.solver.imageRobustLossScalePixels = 1.5
+    ctx = Gb300Context(0)
+    assert ctx.upload(p, o) == 0
+    rep = ctx.solve()
+    h = ctx.history()
+    assert h["cost"].size == rep["accepted_steps"] + 1
+    assert h["iterations"][0] == 0 and h["cost"][0] == rep["initial_cost"]
+    assert h["cost"][-1] == rep["final_cost"]
+    assert np.all(np.diff(h["cost"]) < 0) and np.all(np.diff(h["ms"]) >= 0)
+    assert np.all(np.diff(h["iterations"]) > 0)
