@@ -1134,7 +1134,8 @@ void schedule_owner_tasks(const HostModel* m, int precision, int chunk_obs_start
     if (precision == PB_PRECISION_FP64) {
         // whole pair blocks (6 rows) and cameras (crow rows) by decreasing longest row, ties by
         // position (a deterministic plan); rows inside a group keep their order
-        std::vector<std::pair<long long, int>> groups;
+        thread_local std::vector<std::pair<long long, int>> groups, order;
+        groups.clear();
         groups.reserve(static_cast<size_t>(nslots) + ncl);
         for (int sl = 0; sl < nslots; ++sl) groups.push_back({cost[6 * sl].first, sl});
         for (int l = 0; l < ncl; ++l) {
@@ -1143,7 +1144,7 @@ void schedule_owner_tasks(const HostModel* m, int precision, int chunk_obs_start
             groups.push_back({mx, nslots + l});
         }
         std::stable_sort(groups.begin(), groups.end(), [](const auto& a, const auto& b) { return a.first > b.first; });
-        std::vector<std::pair<long long, int>> order;
+        order.clear();
         order.reserve(cost.size());
         for (const auto& g : groups) {
             if (g.second < nslots) {
@@ -1159,24 +1160,32 @@ void schedule_owner_tasks(const HostModel* m, int precision, int chunk_obs_start
     thread_local std::vector<int> owner;
     owner.assign(nrounds, 0);
     long long load[kAssembleWarps] = {};
+    int nown[kAssembleWarps] = {};
     for (int r = 0; r < nrounds; ++r) {
         long long rc = 0;
         for (int k = 32 * r; k < std::min(ntask, 32 * r + 32); ++k) rc = std::max(rc, cost[k].first);
         const int w = static_cast<int>(std::min_element(load, load + kAssembleWarps) - load);
         load[w] += rc;
         owner[r] = w;
+        ++nown[w];
     }
-    int pos = static_cast<int>(cs.task_list.size());
-    cs.task_list.reserve(cs.task_list.size() + 32 * static_cast<size_t>(nrounds));
+    // each warp's rounds in round order, the warps one after the other
+    const size_t base = cs.task_list.size();
+    cs.task_list.resize(base + 32 * static_cast<size_t>(nrounds));
+    size_t at[kAssembleWarps];
+    size_t pos = base;
     for (int w = 0; w < kAssembleWarps; ++w) {
-        cs.warp_task_begin.push_back(pos);
-        for (int r = 0; r < nrounds; ++r) {
-            if (owner[r] != w) continue;
-            for (int lane = 0; lane < 32; ++lane) {
-                const int k = 32 * r + lane;
-                cs.task_list.push_back(k < ntask ? static_cast<unsigned short>(cost[k].second) : kNoTask);
-            }
-            pos += 32;
+        cs.warp_task_begin.push_back(static_cast<int>(pos));
+        at[w] = pos;
+        pos += 32 * static_cast<size_t>(nown[w]);
+    }
+    unsigned short* out = cs.task_list.data();
+    for (int r = 0; r < nrounds; ++r) {
+        unsigned short* dst = out + at[owner[r]];
+        at[owner[r]] += 32;
+        for (int lane = 0; lane < 32; ++lane) {
+            const int k = 32 * r + lane;
+            dst[lane] = k < ntask ? static_cast<unsigned short>(cost[k].second) : kNoTask;
         }
     }
 }
@@ -1213,26 +1222,29 @@ int plan_range(const HostModel* m, const ChunkLimits& lim, int p_begin, int p_ra
         for (size_t i = 0; i < order.size(); ++i) cs.cams.push_back(ccams[order[i]]);
         for (int o = chunk_obs_start; o < obs_end; ++o)
             if (obs_lcam[o] != 255) obs_lcam[o] = static_cast<unsigned char>(remap[obs_lcam[o]]);
-        std::vector<std::pair<int, int>> rp;
-        rp.reserve(cpairs.size());
+        // the chunk's pairs in remapped local indices, numbered in (lower, upper) order: marked in
+        // the slot matrix, then read out row by row
+        const int ncl = static_cast<int>(ccams.size());
+        slot_of.assign(static_cast<size_t>(ncl) * ncl, -1);
         for (auto& p : cpairs) {
             int a = remap[p.first], b = remap[p.second];
             if (a > b) std::swap(a, b);
-            rp.emplace_back(a, b);
+            slot_of[static_cast<size_t>(a) * ncl + b] = 0;
         }
-        std::sort(rp.begin(), rp.end());
-        const int ncl = static_cast<int>(ccams.size());
-        slot_of.assign(static_cast<size_t>(ncl) * ncl, -1);
-        for (size_t i = 0; i < rp.size(); ++i) {
-            cs.pairs.push_back(rp[i].first | (rp[i].second << 16));
-            cs.pair_upper.push_back(-1);  // resolved once all chunks exist
-            slot_of[static_cast<size_t>(rp[i].first) * ncl + rp[i].second] = static_cast<int>(i);
-        }
+        int nslot = 0;
+        for (int a = 0; a < ncl; ++a)
+            for (int b = a; b < ncl; ++b) {
+                int& sl = slot_of[static_cast<size_t>(a) * ncl + b];
+                if (sl < 0) continue;
+                sl = nslot++;
+                cs.pairs.push_back(a | (b << 16));
+                cs.pair_upper.push_back(-1);  // resolved once all chunks exist
+            }
         // Items of every pair slot, in track order: the observation's own term (oa == ob) on the
         // diagonal slot, and for eliminated tracks the coupling -G_oa G_ob^T of two observations
         // with oa on the lower chunk camera (both orientations when they share a camera).
         // Two passes over the chunk's tracks: count the items of every slot, then place them.
-        std::vector<int> cnt(rp.size() + 1, 0);
+        std::vector<int> cnt(static_cast<size_t>(nslot) + 1, 0);
         const int p_first = chunk_trk_start;
         int p_end = chunk_trk_start;
         while (p_end < p_range_end && m->trk_obs_begin[p_end] < obs_end) ++p_end;
@@ -1269,10 +1281,10 @@ int plan_range(const HostModel* m, const ChunkLimits& lim, int p_begin, int p_ra
             if (pass == 0) {
                 const int base = static_cast<int>(cs.slot_items.size());
                 cnt[0] = base;
-                for (size_t i = 0; i < rp.size(); ++i) cnt[i + 1] += cnt[i];
-                cs.slot_items.resize(static_cast<size_t>(cnt[rp.size()]));
+                for (int i = 0; i < nslot; ++i) cnt[i + 1] += cnt[i];
+                cs.slot_items.resize(static_cast<size_t>(cnt[nslot]));
                 // cnt[i] is now the begin of slot i: the fill position of the second pass
-                for (size_t i = 0; i < rp.size(); ++i) cs.slot_item_begin.push_back(cnt[i + 1]);
+                for (int i = 0; i < nslot; ++i) cs.slot_item_begin.push_back(cnt[i + 1]);
             }
         }
         chunk_trk_start = p_end;
@@ -1292,7 +1304,7 @@ int plan_range(const HostModel* m, const ChunkLimits& lim, int p_begin, int p_ra
                 if (obs_lcam[o] != 255) cs.lcam_obs[cc[obs_lcam[o]]++] = static_cast<unsigned char>(o - chunk_obs_start);
         }
         schedule_owner_tasks(m, lim.precision, chunk_obs_start, obs_end, p_first, p_end, obs_lcam, cs, cs.pair_begin.back(),
-                             static_cast<int>(rp.size()), cs.cam_begin.back(), ncl);
+                             nslot, cs.cam_begin.back(), ncl);
         cs.obs_begin.push_back(obs_end);
         cs.cam_begin.push_back(static_cast<int>(cs.cams.size()));
         cs.pair_begin.push_back(static_cast<int>(cs.pairs.size()));
@@ -1467,16 +1479,29 @@ int build_chunks(HostModel* m, int precision, size_t smem_budget, std::string* e
     for (int u = 0; u < nupper; ++u) up_begin[m->up_row[u] + 1]++;
     for (int i = 0; i < m->ncb; ++i) up_begin[i + 1] += up_begin[i];
     std::vector<int> count_up(nupper + 1, 0), count_cam(m->ncb + 1, 0);
+    // upper block of a camera-block pair: a dense table for up to 1024 camera blocks, else a
+    // binary search in the row
+    const bool dense = m->ncb <= 1024;
+    std::vector<int> up_of;
+    if (dense) {
+        up_of.assign(static_cast<size_t>(m->ncb) * m->ncb, -1);
+        for (int u = 0; u < nupper; ++u) up_of[static_cast<size_t>(m->up_row[u]) * m->ncb + m->up_col[u]] = u;
+    }
     for (int c = 0; c < cs.n(); ++c) {
         for (int s = cs.pair_begin[c]; s < cs.pair_begin[c + 1]; ++s) {
             const int a = cs.pairs[s] & 0xFFFF, b = cs.pairs[s] >> 16;
             const int bi = m->camera_block[cs.cams[cs.cam_begin[c] + a]];
             const int bj = m->camera_block[cs.cams[cs.cam_begin[c] + b]];
-            const int* cb = &m->up_col[up_begin[bi]];
-            const int* ce = &m->up_col[0] + up_begin[bi + 1];
-            const int* f = std::lower_bound(cb, ce, bj);
-            if (f == ce || *f != bj) { *err = "internal: chunk pair outside the reduced pattern"; return PB_SOLVE_NUMERICAL_FAILURE; }
-            const int u = static_cast<int>(f - &m->up_col[0]);
+            int u;
+            if (dense) {
+                u = up_of[static_cast<size_t>(bi) * m->ncb + bj];
+            } else {
+                const int* cb = &m->up_col[up_begin[bi]];
+                const int* ce = &m->up_col[0] + up_begin[bi + 1];
+                const int* f = std::lower_bound(cb, ce, bj);
+                u = (f == ce || *f != bj) ? -1 : static_cast<int>(f - &m->up_col[0]);
+            }
+            if (u < 0) { *err = "internal: chunk pair outside the reduced pattern"; return PB_SOLVE_NUMERICAL_FAILURE; }
             cs.pair_upper[s] = u;
             count_up[u + 1]++;
         }
