@@ -30,8 +30,9 @@ def rig_block(seed=21, n_along=5, n_lines=3, n_points=2500, **kw):
     return synth.rig_grid_problem(seed=seed, n_along=n_along, n_lines=n_lines, n_points=n_points, **kw)
 
 
-def rig_options(mixed=False, general=False, intrinsics=False, iterations=20):
+def rig_options(mixed=False, general=False, intrinsics=False, iterations=20, poses=True):
     o = SolveOptions()
+    o.calibration.refineCameraPose = poses
     o.solver.imageRobustLoss = ImageRobustLoss.Huber
     o.solver.imageRobustLossScalePixels = 1.5
     o.solver.useReferenceOnlineSchur = not general
@@ -65,8 +66,15 @@ def rig_fixed_capture():
     return p
 
 
+def rig_intrinsics_only():
+    """Poses held (CalibrationOptions::refineCameraPose = false): no capture or sensor blocks,
+    only the two calibration groups are refined."""
+    return rig_with_groups()
+
+
 HOST_CASES = [("auto", rig_block, {}), ("groups", rig_with_groups, {"intrinsics": True}),
-              ("survey", rig_survey, {"general": True}), ("fixed", rig_fixed_capture, {})]
+              ("survey", rig_survey, {"general": True}), ("fixed", rig_fixed_capture, {}),
+              ("poses_held", rig_intrinsics_only, {"intrinsics": True, "poses": False})]
 
 
 def host_rig(L, problem, options):
@@ -210,7 +218,7 @@ def test_oracle_rig_gradient_matches_central_differences():
 
 GPU_CASES = [("online", rig_block, {}), ("general", rig_block, {"general": True}),
              ("groups", rig_with_groups, {"intrinsics": True}), ("survey", rig_survey, {"general": True}),
-             ("fixed", rig_fixed_capture, {})]
+             ("fixed", rig_fixed_capture, {}), ("poses_held", rig_intrinsics_only, {"intrinsics": True, "poses": False})]
 
 
 def gpu(problem, options):
