@@ -788,6 +788,24 @@ def measure_rig_block(local_rank, steps=2):
         return statistics.mean(ts), reps[-1], ctx.download(), ctx.rig()
 
     ms_m, rep_m, out_m, rig_m = timed(steps)
+    # end to end through the C ABI from host buffers (upload with the plan reused, solve, download)
+    import ctypes as C
+    from plabundle_gb300 import native
+    desc, keep = native.problem_desc(prob)
+    copts = native.solve_options(opts, prob)
+    copts.precision = 1
+    pp = keep[0]
+    bufs = [np.zeros_like(pp.cameras), np.zeros_like(pp.points), np.zeros(pp.n_tracks, np.int8),
+            np.zeros(pp.n_tracks), np.zeros(pp.n_tracks)]
+    rep_e = native.SolveReportC()
+    e2e = []
+    for _ in range(2):
+        t0 = time.perf_counter()
+        st = ctx.L.pb_gpu_solve_problem(ctx.ctx, C.byref(desc), C.byref(copts), C.byref(rep_e),
+                                        *[b.ctypes.data for b in bufs])
+        e2e.append((time.perf_counter() - t0) * 1e3)
+        assert st == 0
+    h2d, d2h = problem_bytes(prob)
     ctx.copts.precision = 0
     ctx.copts.factor_reuse = 1
     ms_r, rep_r, out_r, rig_r = timed(1)
@@ -818,6 +836,7 @@ def measure_rig_block(local_rank, steps=2):
             "sensor_rotation_err_vs_truth": float(np.abs(rig_m["sensors"][:, :9] - ts[:, :9]).max()),
             "rig_blocks": {"captures": rep_m["rig_capture_blocks"], "sensors": rep_m["rig_sensor_blocks"],
                            "promoted_point_blocks": rep_m["promoted_point_blocks"]},
+            "e2e": {"value": statistics.mean(e2e), "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "generator_seconds": t_gen}
 
 
