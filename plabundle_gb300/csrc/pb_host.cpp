@@ -415,11 +415,32 @@ int build_host_model(const pb_problem_desc* pr, const pb_solve_options* op, Host
         *err = "observation arrays missing";
         return PB_SOLVE_INVALID_INPUT;
     }
-    m->obs_cam.assign(pr->obs_camera, pr->obs_camera + m->no);
-    m->obs_u.assign(pr->obs_u, pr->obs_u + m->no);
-    m->obs_v.assign(pr->obs_v, pr->obs_v + m->no);
-    m->obs_weight.assign(pr->obs_weight, pr->obs_weight + m->no);
-    m->obs_scale.assign(pr->obs_scale, pr->obs_scale + m->no);
+    // the observation arrays, copied by host threads over ranges
+    {
+        const size_t no = static_cast<size_t>(m->no);
+        m->obs_cam.resize(no);
+        m->obs_u.resize(no);
+        m->obs_v.resize(no);
+        m->obs_weight.resize(no);
+        m->obs_scale.resize(no);
+        const int n = static_cast<int>(std::min<long long>(m->no, std::numeric_limits<int>::max()));
+        if (static_cast<long long>(n) == m->no) {
+            parallel_ranges(n, host_threads(m->no), [&](int, int k0, int k1) {
+                const size_t b = static_cast<size_t>(k0), c = static_cast<size_t>(k1 - k0);
+                std::copy_n(pr->obs_camera + b, c, m->obs_cam.data() + b);
+                std::copy_n(pr->obs_u + b, c, m->obs_u.data() + b);
+                std::copy_n(pr->obs_v + b, c, m->obs_v.data() + b);
+                std::copy_n(pr->obs_weight + b, c, m->obs_weight.data() + b);
+                std::copy_n(pr->obs_scale + b, c, m->obs_scale.data() + b);
+            });
+        } else {
+            std::copy_n(pr->obs_camera, no, m->obs_cam.data());
+            std::copy_n(pr->obs_u, no, m->obs_u.data());
+            std::copy_n(pr->obs_v, no, m->obs_v.data());
+            std::copy_n(pr->obs_weight, no, m->obs_weight.data());
+            std::copy_n(pr->obs_scale, no, m->obs_scale.data());
+        }
+    }
     m->fixed_cams.assign(pr->fixed_cameras, pr->fixed_cameras + pr->n_fixed_cameras);
     m->fixed_tracks.assign(pr->fixed_tracks, pr->fixed_tracks + pr->n_fixed_tracks);
     m->group_ids = pr->calibration_group_ids
@@ -1014,7 +1035,26 @@ int build_host_model(const pb_problem_desc* pr, const pb_solve_options* op, Host
         unsigned long long h = 1469598103934665603ull;
         auto mix = [&](long long v) { h = (h ^ static_cast<unsigned long long>(v)) * 1099511628211ull; };
         mix(nc); mix(nt); mix(m->no); mix(m->ncb); mix(m->ng); mix(m->ni);
-        for (size_t i = 0; i < m->p_obs_orig.size(); ++i) { mix(m->p_obs_orig[i]); mix(m->obs_cam[m->p_obs_orig[i]]); }
+        // the processing-order observations in 16 fixed segments hashed by host threads, the
+        // segment hashes mixed in order (the value does not depend on the thread count)
+        {
+            constexpr int kHashSegments = 16;
+            const int nobs = static_cast<int>(m->p_obs_orig.size());
+            unsigned long long seg_h[kHashSegments];
+            parallel_ranges(kHashSegments, std::min(kHashSegments, host_threads(nobs)), [&](int, int s0, int s1) {
+                for (int sgm = s0; sgm < s1; ++sgm) {
+                    unsigned long long g = 1469598103934665603ull;
+                    const int i0 = static_cast<int>(static_cast<long long>(nobs) * sgm / kHashSegments);
+                    const int i1 = static_cast<int>(static_cast<long long>(nobs) * (sgm + 1) / kHashSegments);
+                    for (int i = i0; i < i1; ++i) {
+                        g = (g ^ static_cast<unsigned long long>(m->p_obs_orig[i])) * 1099511628211ull;
+                        g = (g ^ static_cast<unsigned long long>(m->obs_cam[m->p_obs_orig[i]])) * 1099511628211ull;
+                    }
+                    seg_h[sgm] = g;
+                }
+            });
+            for (int sgm = 0; sgm < kHashSegments; ++sgm) mix(static_cast<long long>(seg_h[sgm]));
+        }
         for (int t : m->trk_order) mix(t);
         if (m->rig.on) {
             const RigModel& R = m->rig;
