@@ -243,7 +243,8 @@ pb_status pb_gpu_get_pairs(pb_gpu_ctx* ctx, int32_t* pairs);
 
 /* Kernel (a): per-observation residual, point Jacobian (2x3, scaled), pose Jacobian (2x6 as
  * scattered for the camera block), intrinsic Jacobian (2x13), normal weight, robust cost and a
- * validity flag, at the current state, in the original observation order. */
+ * validity flag, at the current state, in the original observation order.  For a rig problem the
+ * pose Jacobian is the composed camera's own (before the chain to its capture and sensor). */
 pb_status pb_gpu_linearize_observations(pb_gpu_ctx* ctx, int32_t precision, double* residual,
                                         double* point_jacobian, double* pose_jacobian,
                                         double* intrinsic_jacobian, double* normal_weight, double* cost,
@@ -264,6 +265,9 @@ pb_status pb_gpu_get_reduced(pb_gpu_ctx* ctx, double* dense_matrix, double* rhs,
  * systems: block-Jacobi PCG.  One cooperative kernel per solve. */
 pb_status pb_gpu_solve_reduced(pb_gpu_ctx* ctx, double* step, int32_t* converged, int32_t* iterations,
                                double* relative_residual);
+/* (For a rig problem, `step` is the rig solution mapped back to the composed cameras' 6-column
+ * blocks, followed by the intrinsic columns; the rig system itself is the one pb_gpu_get_reduced
+ * copies.) */
 
 /* Kernel (d1): back-substitution (recoverReferencePointSteps, ...ReferenceSchur.cpp:982-1082);
  * eliminated_step is in track-block order. */
