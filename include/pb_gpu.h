@@ -265,9 +265,9 @@ pb_status pb_gpu_get_reduced(pb_gpu_ctx* ctx, double* dense_matrix, double* rhs,
  * systems: block-Jacobi PCG.  One cooperative kernel per solve. */
 pb_status pb_gpu_solve_reduced(pb_gpu_ctx* ctx, double* step, int32_t* converged, int32_t* iterations,
                                double* relative_residual);
-/* (For a rig problem, `step` is the rig solution mapped back to the composed cameras' 6-column
- * blocks, followed by the intrinsic columns; the rig system itself is the one pb_gpu_get_reduced
- * copies.) */
+/* (For a rig problem, `step` is the solution over the rig blocks, captures then sensors, 6 columns
+ * each, followed by the intrinsic columns: the system pb_gpu_get_reduced copies, of the dimension
+ * pb_gpu_get_sizes reports.) */
 
 /* Kernel (d1): back-substitution (recoverReferencePointSteps, ...ReferenceSchur.cpp:982-1082);
  * eliminated_step is in track-block order. */

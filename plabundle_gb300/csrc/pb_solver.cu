@@ -1889,7 +1889,16 @@ pb_status pb_gpu_solve_reduced(pb_gpu_ctx* c, double* step, int32_t* converged, 
         if (converged) *converged = cv ? 1 : 0;
         if (iterations) *iterations = it;
         if (relres) *relres = rr;
-        if (step) check(cudaMemcpy(step, c->step_c, c->S[0].n * sizeof(double), cudaMemcpyDeviceToHost), "D2H");
+        // the solution of the system pb_gpu_get_reduced copies: for a rig problem the rig step
+        // (6 per rig block, then the intrinsic columns), else the camera-block step
+        if (step) {
+            if (c->rig_on)
+                check(cudaMemcpy(step, c->rig.step_r, (6 * c->model.rig.nrb + c->S[0].nb) * sizeof(double),
+                                 cudaMemcpyDeviceToHost),
+                      "D2H");
+            else
+                check(cudaMemcpy(step, c->step_c, c->S[0].n * sizeof(double), cudaMemcpyDeviceToHost), "D2H");
+        }
         if (rc) return fail(c, PB_ERR_SINGULAR_BLOCK, "reduced system is not numerically SPD (positive definite)");
         return PB_OK;
     } catch (const std::exception& e) {

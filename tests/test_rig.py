@@ -267,6 +267,10 @@ def test_rig_reduced_system_matches_oracle(damping):
     np.testing.assert_allclose(cg, co, rtol=1e-12)
     S, rhs, _ = ctx.reduced()
     So, red = orc.dense_reduced()
+    # the solve of that system: the rig step satisfies S x = rhs (FP64 path, CG to 2e-10)
+    step, cv, _, rr = ctx.solve_reduced()
+    assert cv and step.size == S.shape[0]
+    assert np.linalg.norm(S @ step - rhs) <= 1e-8 * np.linalg.norm(rhs)
     s = ctx.sizes()
     nrb, ng, ni = s["camera_blocks"], s["intrinsic_blocks"], s["ni"]
     cols = [q for q in range(9) if (int(ctx.copts.intrinsic_mask) >> q) & 1]
