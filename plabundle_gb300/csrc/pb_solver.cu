@@ -779,7 +779,8 @@ int solve_dense(pb_gpu_ctx* c, double rel, double abs_tol, int max_it, bool* con
     // (pb_solve_options.factor_reuse), which gives an FP64 arm with the mixed path's policy
     const bool reuse = f32 ? c->factor_reuse != 2 : c->factor_reuse == 1;
     int spent = 0;
-    if (reuse && c->f32_age >= 0 && c->f32_age < max_factor_age(c->S[0].n) && !c->f32_stale) {
+    // the age limit follows the dimension of the system factored (the rig system for a rig problem)
+    if (reuse && c->f32_age >= 0 && c->f32_age < max_factor_age(W.n) && !c->f32_stale) {
         // The reduced matrix changes little between LM iterations: the FP32 factor of an earlier
         // one still preconditions the CG on the current FP64 matrix.  A factorisation costs
         // about as much as a hundred CG iterations, so the kept factor is used until the CG
