@@ -282,36 +282,49 @@ void build_rig_pattern(HostModel* m, const std::vector<unsigned char>& use) {
             sb[c] = R.sensor_block[R.cam_sensor[c]];
         }
     }
-    std::vector<char> bits(static_cast<size_t>(P) * P, 0);
-    auto connect = [&](int a, int b) {
-        if (a < 0 || b < 0 || a == b) return;
-        bits[static_cast<size_t>(std::min(a, b)) * P + std::max(a, b)] = 1;
-    };
-    std::vector<int> tb;
-    for (int t = 0; t < m->nt; ++t) {
-        if (!m->active_track[t]) continue;
-        tb.clear();
-        for (long long k = m->offs[t]; k < m->offs[t + 1]; ++k) {
-            if (!use[k]) continue;
-            const int c = m->obs_cam[k];
-            const int ob[3] = {cb[c], sb[c], intr[c]};
-            connect(ob[0], ob[1]);
-            connect(ob[0], ob[2]);
-            connect(ob[1], ob[2]);
-            if (m->track_block[t] >= 0)
-                for (int v : ob)
-                    if (v >= 0) tb.push_back(v);
+    // tracks split over host threads, each setting the pairs of its tracks in its own P x P
+    // bitset; the bitsets are OR-ed and read out row-major (the sorted pair list)
+    const size_t words = (static_cast<size_t>(P) * P + 63) / 64;
+    const int nthreads = host_threads(m->no);
+    std::vector<std::vector<unsigned long long>> bits(nthreads, std::vector<unsigned long long>(words, 0ull));
+    parallel_ranges(m->nt, nthreads, [&](int i, int t0, int t1) {
+        unsigned long long* mask = bits[i].data();
+        auto connect = [&](int a, int b) {
+            if (a < 0 || b < 0 || a == b) return;
+            const size_t bit = static_cast<size_t>(std::min(a, b)) * P + std::max(a, b);
+            mask[bit >> 6] |= 1ull << (bit & 63);
+        };
+        std::vector<int> tb;
+        for (int t = t0; t < t1; ++t) {
+            if (!m->active_track[t]) continue;
+            tb.clear();
+            for (long long k = m->offs[t]; k < m->offs[t + 1]; ++k) {
+                if (!use[k]) continue;
+                const int c = m->obs_cam[k];
+                const int ob[3] = {cb[c], sb[c], intr[c]};
+                connect(ob[0], ob[1]);
+                connect(ob[0], ob[2]);
+                connect(ob[1], ob[2]);
+                if (m->track_block[t] >= 0)
+                    for (int v : ob)
+                        if (v >= 0) tb.push_back(v);
+            }
+            if (m->track_block[t] < 0) continue;
+            std::sort(tb.begin(), tb.end());
+            tb.erase(std::unique(tb.begin(), tb.end()), tb.end());
+            for (size_t l = 0; l < tb.size(); ++l)
+                for (size_t r = l + 1; r < tb.size(); ++r) connect(tb[l], tb[r]);
         }
-        if (m->track_block[t] < 0) continue;
-        std::sort(tb.begin(), tb.end());
-        tb.erase(std::unique(tb.begin(), tb.end()), tb.end());
-        for (size_t l = 0; l < tb.size(); ++l)
-            for (size_t r = l + 1; r < tb.size(); ++r) connect(tb[l], tb[r]);
-    }
+    });
+    std::vector<unsigned long long>& all = bits[0];
+    for (int i = 1; i < nthreads; ++i)
+        for (size_t w = 0; w < words; ++w) all[w] |= bits[i][w];
     R.pairs.clear();
     for (int r = 0; r < P; ++r)
-        for (int q = r + 1; q < P; ++q)
-            if (bits[static_cast<size_t>(r) * P + q]) R.pairs.emplace_back(r, q);
+        for (int q = r + 1; q < P; ++q) {
+            const size_t bit = static_cast<size_t>(r) * P + q;
+            if ((all[bit >> 6] >> (bit & 63)) & 1ull) R.pairs.emplace_back(r, q);
+        }
     // rig pose CSR: the pose-pose pairs plus the diagonal
     std::vector<std::vector<int>> rows(nrb);
     for (int i = 0; i < nrb; ++i) rows[i].push_back(i);
