@@ -632,6 +632,21 @@ def run_gb300(args, rank, world, local_rank):
                                    out_t["rms_after"], out_t["points"], rep_t["final_cost"], rep_t["filter_threshold"])
             vs_oracle["oracle_cpu_solve_seconds"] = fx[0]["wall_seconds"]
             vs_oracle["oracle_cpu"] = f"{fx[0]['threads']} threads, {fx[0]['cpu']} ({fx[0]['machine']})"
+    elif args.workload == "rig3000":
+        sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+        import make_rig_fixture as RFX
+        fx = RFX.load_fixture()
+        if fx is None:
+            vs_oracle = {"unavailable": "fixture absent"}
+        elif RFX.problem_mismatch(fx[0], fx[1], prob):
+            vs_oracle = {"unavailable": "generator does not reproduce the fixture's problem: "
+                                        + RFX.problem_mismatch(fx[0], fx[1], prob)}
+        else:
+            rig_t = ctx.rig()
+            vs_oracle = RFX.compare(fx[0], fx[1], out_t["cameras"], rig_t["captures"], rig_t["sensors"], out_t["valid"],
+                                    out_t["rms_after"], out_t["points"], rep_t["final_cost"], rep_t["filter_threshold"])
+            vs_oracle["oracle_cpu_solve_seconds"] = fx[0]["wall_seconds"]
+            vs_oracle["oracle_cpu"] = f"{fx[0]['threads']} threads, {fx[0]['cpu']} ({fx[0]['machine']})"
 
     # the metric as its name states it: the time until the cost first comes within 1e-6 relative
     # of the converged FP64 cost (the oracle's CPU solve where its fixture matches, else the
@@ -788,6 +803,28 @@ def measure_rig_block(local_rank, steps=2):
         return statistics.mean(ts), reps[-1], ctx.download(), ctx.rig()
 
     ms_m, rep_m, out_m, rig_m = timed(steps)
+    hist_m = ctx.history()
+    # the mixed result against the oracle's converged CPU FP64 solve of the same problem (committed
+    # fixture, compared only when the generator reproduces its problem)
+    vs_oracle, ttc = None, None
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    import make_rig_fixture as RFX
+    fx = RFX.load_fixture()
+    if fx is None:
+        vs_oracle = {"unavailable": "fixture absent"}
+    elif RFX.problem_mismatch(fx[0], fx[1], prob):
+        vs_oracle = {"unavailable": "generator does not reproduce the fixture's problem: "
+                                    + RFX.problem_mismatch(fx[0], fx[1], prob)}
+    else:
+        vs_oracle = RFX.compare(fx[0], fx[1], out_m["cameras"], rig_m["captures"], rig_m["sensors"], out_m["valid"],
+                                out_m["rms_after"], out_m["points"], rep_m["final_cost"], rep_m["filter_threshold"])
+        vs_oracle["oracle_cpu_solve_seconds"] = fx[0]["wall_seconds"]
+        vs_oracle["oracle_cpu"] = f"{fx[0]['threads']} threads, {fx[0]['cpu']} ({fx[0]['machine']})"
+        ref_cost = vs_oracle["oracle_final_cost"]
+        hit = np.nonzero(hist_m["cost"] <= ref_cost * (1.0 + 1e-6))[0]
+        ttc = {"reference_cost": ref_cost,
+               "mixed": None if hit.size == 0 else {"ms": float(hist_m["ms"][hit[0]]),
+                                                    "iteration": int(hist_m["iterations"][hit[0]])}}
     # end to end through the C ABI from host buffers (upload with the plan reused, solve, download)
     import ctypes as C
     from plabundle_gb300 import native
@@ -809,8 +846,16 @@ def measure_rig_block(local_rank, steps=2):
     ctx.copts.precision = 0
     ctx.copts.factor_reuse = 1
     ms_r, rep_r, out_r, rig_r = timed(1)
+    hist_r = ctx.history()
     ctx.copts.factor_reuse = 2
     ms_f, rep_f, _, _ = timed(1)
+    hist_f = ctx.history()
+    if ttc is not None:
+        for key, h in (("fp64_reuse", hist_r), ("fp64_refactor", hist_f)):
+            hit = np.nonzero(h["cost"] <= ttc["reference_cost"] * (1.0 + 1e-6))[0]
+            ttc[key] = None if hit.size == 0 else {"ms": float(h["ms"][hit[0]]), "iteration": int(h["iterations"][hit[0]])}
+        if ttc["mixed"] and ttc.get("fp64_reuse") and ttc.get("fp64_refactor"):
+            ttc["speedup_vs_fp64_path"] = min(ttc["fp64_reuse"]["ms"], ttc["fp64_refactor"]["ms"]) / ttc["mixed"]["ms"]
     ctx.close()
     C = out_r["cameras"][:, 9:12]
     scale = float(np.linalg.norm(C - C.mean(0), axis=1).max())
@@ -832,6 +877,7 @@ def measure_rig_block(local_rank, steps=2):
                                                                      rig_r["captures"][:, 9:12]).max() / scale),
                               "sensor_max_abs_diff": float(np.abs(rig_m["sensors"] - rig_r["sensors"]).max()),
                               "inlier_mask_identical": bool(np.array_equal(out_m["valid"], out_r["valid"]))},
+            "mixed_vs_oracle": vs_oracle, "time_to_1e-6_rel_cost": ttc,
             "sensor_lever_err_vs_truth_m": float(np.abs(rig_m["sensors"][:, 9:12] - ts[:, 9:12]).max()),
             "sensor_rotation_err_vs_truth": float(np.abs(rig_m["sensors"][:, :9] - ts[:, :9]).max()),
             "rig_blocks": {"captures": rep_m["rig_capture_blocks"], "sensors": rep_m["rig_sensor_blocks"],

@@ -140,3 +140,41 @@ def test_cost_history_of_a_solve():
     assert h["cost"][-1] == rep["final_cost"]
     assert np.all(np.diff(h["cost"]) < 0) and np.all(np.diff(h["ms"]) >= 0)
     assert np.all(np.diff(h["iterations"]) > 0)
+
+
+@pytest.fixture(scope="module")
+def rig_block():
+    from golden import make_rig_fixture as FX
+    fx = FX.load_fixture()
+    if fx is None:
+        pytest.skip("the rig-block oracle fixture is absent")
+    prob, opts = FX.rig_workload()
+    why = FX.problem_mismatch(fx[0], fx[1], prob)
+    if why:
+        pytest.skip("the generator does not reproduce the fixture's problem on this machine: " + why)
+    return FX, fx, prob, opts
+
+
+def test_rig_block_reaches_the_oracle_solution(rig_block):
+    """The large oblique survey configuration (600 five-camera rig captures, 1.5 M points, 40
+    control points, 10 scale bars; general path), mixed path run to convergence, against the
+    oracle's converged CPU FP64 solve of the same problem: 1e-6 relative final cost, 1e-5 relative
+    camera and capture centres and sampled points, sensor parameters to 1e-6, identical inliers."""
+    FX, (meta, arrays), prob, opts = rig_block
+    opts.backend.enablePlaMatrixMixedPrecision = True
+    ctx = Gb300Context(0)
+    assert ctx.upload(prob, opts) == 0, ctx.L.pb_gpu_last_error(ctx.ctx)
+    rep = ctx.solve()
+    out = ctx.download()
+    rig = ctx.rig()
+    ctx.close()
+    assert rep["status"] == SolveStatus.Success
+    cmp = FX.compare(meta, arrays, out["cameras"], rig["captures"], rig["sensors"], out["valid"], out["rms_after"],
+                     out["points"], rep["final_cost"], rep["filter_threshold"])
+    assert cmp["final_cost_rel_err"] < 1e-6, cmp
+    assert cmp["camera_centre_rel_err"] < 1e-5, cmp
+    assert cmp["capture_centre_rel_err"] < 1e-5, cmp
+    assert cmp["point_sample_rel_err"] < 1e-5, cmp
+    assert cmp["sensor_max_abs_err"] < 1e-6, cmp
+    assert all(abs(m) < 1e-6 for m in cmp["flip_margins_px"]) and cmp["inlier_mask_flips"] <= 2, cmp
+    np.testing.assert_allclose(rep["initial_cost"], meta["report"]["initial_cost"], rtol=1e-12)
