@@ -12,10 +12,11 @@
 // assembly runs unchanged on one 6-column block per camera (the kernels' camera blocks) and the
 // reduced system over the rig's blocks is S_rig[I][J] = sum M_aI^T S[a][b] M_bJ over the camera
 // blocks a, b chained to I and J, B_rig[I] = sum M_aI^T B[a], g_rig[I] = sum M_aI^T g[a].  The
-// sums follow host-built term lists in a fixed order: the pose terms of one rig block in segments
-// of kRigSegTerms consecutive terms (one warp each), then the segments in order; the border and
-// right-hand side over segments of kRigItemSeg camera blocks likewise.  The rig pose diagonal is then damped as
-// finalizePrimaryDiagonal(1 + damping, 1) damps every primary diagonal, the solution is mapped
+// sums follow host-built term lists in a fixed order: the pose terms of one rig block in
+// segments of kRigSegTerms consecutive terms (one warp each), then the segments in order; the
+// border and right-hand side over segments of kRigItemSeg camera blocks likewise.  The rig pose
+// diagonal is then damped as finalizePrimaryDiagonal(1 + damping, 1) damps every primary
+// diagonal, the solution is mapped
 // back to the camera blocks (camera delta = Mc capture delta + Ms sensor delta) for the point
 // back-substitution, and the trial states update captures and sensors with the plain pose delta
 // (placamera::applyPoseDelta, BundleAdjustPlaMatrixAssembly.cpp:1152-1209: R' = Exp(w) R,
