@@ -142,7 +142,7 @@ def main():
                         out_cameras=ref["cameras"], out_captures=ref["captures"], out_sensors=ref["sensors"],
                         out_intrinsics=np.zeros((0, 13)),
                         out_valid_bits=np.packbits(ref["valid"].astype(np.uint8)),
-                        near_threshold_tracks=near, near_threshold_rms=ref["rms_after"][near],
+                        near_threshold_tracks=near, near_threshold_rms_after=ref["rms_after"][near],
                         point_sample_tracks=idx, point_sample=ref["points"][idx])
     print(json.dumps({"status": report["status"], "iterations": report["iterations"],
                       "final_cost": report["final_cost"], "wall_seconds": wall, "fixture": FIXTURE}))
