@@ -14,7 +14,8 @@ Stored: the oracle's report, the refined cameras (3 000 x 32), captures and sens
 each), the inlier mask (bit-packed), a seeded sample of 4 096 refined points, and the wall time
 of the whole CPU solve with its thread count and CPU model.
 
-    python tests/golden/make_rig_fixture.py [--threads N]    # ~20-30 min on 8 cores
+    python tests/golden/make_rig_fixture.py [--threads N]    # ~80 min on 8 x86 cores (the oracle's
+                                                             # dense damped solve runs on one thread)
 """
 from __future__ import annotations
 
