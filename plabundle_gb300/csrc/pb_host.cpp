@@ -1208,6 +1208,37 @@ void schedule_owner_tasks(const HostModel* m, int precision, int chunk_obs_start
             }
         }
         cost.swap(order);
+    } else {
+        // FP32 path: the rows are grouped by the code path they take, so that a round's lanes run
+        // the same branch.  Pair rows: the rows of diagonal slots (own terms J^T M J) before those
+        // of off-diagonal slots (couplings G G^T).  Camera rows: the gradient rows of every camera,
+        // then the border rows of each camera's own calibration group (own term and intrinsic
+        // coupling), then the border rows of the other groups (coupling only, often empty).  Within
+        // a class the rows keep slot or camera order and row order, so neighbouring lanes read the
+        // same observation records.  Each row sums the same terms in the same order whatever its
+        // lane, so the order changes no result.
+        thread_local std::vector<std::pair<long long, int>> order;
+        order.clear();
+        order.reserve(cost.size());
+        for (int pass = 0; pass < 2; ++pass)
+            for (int sl = 0; sl < nslots; ++sl) {
+                const int pk = cs.pairs[slot0 + sl];
+                if (((pk & 0xFFFF) == (pk >> 16)) == (pass == 0))
+                    for (int x = 0; x < 6; ++x) order.push_back(cost[6 * sl + x]);
+            }
+        auto cam_group = [&](int l) {
+            const int b0 = cs.lcam_obs_begin[lcam0 + l], b1 = cs.lcam_obs_begin[lcam0 + l + 1];
+            return b1 > b0 ? grp[cs.lcam_obs[b0]] : -1;
+        };
+        for (int l = 0; l < ncl; ++l)
+            for (int row = 0; row < std::min(2, crow); ++row) order.push_back(cost[6 * nslots + l * crow + row]);
+        for (int pass = 0; pass < 2; ++pass)
+            for (int l = 0; l < ncl; ++l) {
+                const int g = cam_group(l);
+                for (int row = 2; row < crow; ++row)
+                    if (((row - 2) / ni == g) == (pass == 0)) order.push_back(cost[6 * nslots + l * crow + row]);
+            }
+        cost.swap(order);
     }
     const int nrounds = (ntask + 31) / 32;
     thread_local std::vector<int> owner;
