@@ -1220,12 +1220,19 @@ void schedule_owner_tasks(const HostModel* m, int precision, int chunk_obs_start
         thread_local std::vector<std::pair<long long, int>> order;
         order.clear();
         order.reserve(cost.size());
-        for (int pass = 0; pass < 2; ++pass)
-            for (int sl = 0; sl < nslots; ++sl) {
-                const int pk = cs.pairs[slot0 + sl];
-                if (((pk & 0xFFFF) == (pk >> 16)) == (pass == 0))
-                    for (int x = 0; x < 6; ++x) order.push_back(cost[6 * sl + x]);
+        thread_local std::vector<std::pair<long long, int>> offdiag;
+        offdiag.clear();
+        for (int sl = 0; sl < nslots; ++sl) {
+            const int pk = cs.pairs[slot0 + sl];
+            if ((pk & 0xFFFF) == (pk >> 16)) {
+                for (int x = 0; x < 6; ++x) order.push_back(cost[6 * sl + x]);
+            } else {
+                offdiag.push_back({cost[6 * sl].first, sl});
             }
+        }
+        std::stable_sort(offdiag.begin(), offdiag.end(), [](const auto& a, const auto& b) { return a.first > b.first; });
+        for (const auto& s : offdiag)
+            for (int x = 0; x < 6; ++x) order.push_back(cost[6 * s.second + x]);
         auto cam_group = [&](int l) {
             const int b0 = cs.lcam_obs_begin[lcam0 + l], b1 = cs.lcam_obs_begin[lcam0 + l + 1];
             return b1 > b0 ? grp[cs.lcam_obs[b0]] : -1;
