@@ -1213,35 +1213,41 @@ void schedule_owner_tasks(const HostModel* m, int precision, int chunk_obs_start
         // the same branch.  Pair rows: the rows of diagonal slots (own terms J^T M J) before those
         // of off-diagonal slots (couplings G G^T).  Camera rows: the gradient rows of every camera,
         // then the border rows of each camera's own calibration group (own term and intrinsic
-        // coupling), then the border rows of the other groups (coupling only, often empty).  Within
-        // a class the rows keep slot or camera order and row order, so neighbouring lanes read the
-        // same observation records.  Each row sums the same terms in the same order whatever its
-        // lane, so the order changes no result.
+        // coupling), then the border rows of the other groups (coupling only, often empty).  The
+        // six rows of a slot, and a camera's rows of one class, stay on neighbouring lanes, which
+        // read the same observation records.  Each row sums the same terms in the same order
+        // whatever its lane, so the order changes no result.
         thread_local std::vector<std::pair<long long, int>> order;
         order.clear();
         order.reserve(cost.size());
-        thread_local std::vector<std::pair<long long, int>> offdiag;
+        // pair slots of each class and the cameras by decreasing work (stable: ties keep their
+        // order), so that the lanes of a round loop over similar numbers of terms
+        thread_local std::vector<std::pair<long long, int>> diag, offdiag, cams;
+        diag.clear();
         offdiag.clear();
+        cams.clear();
         for (int sl = 0; sl < nslots; ++sl) {
             const int pk = cs.pairs[slot0 + sl];
-            if ((pk & 0xFFFF) == (pk >> 16)) {
-                for (int x = 0; x < 6; ++x) order.push_back(cost[6 * sl + x]);
-            } else {
-                offdiag.push_back({cost[6 * sl].first, sl});
-            }
+            ((pk & 0xFFFF) == (pk >> 16) ? diag : offdiag).push_back({cost[6 * sl].first, sl});
         }
-        std::stable_sort(offdiag.begin(), offdiag.end(), [](const auto& a, const auto& b) { return a.first > b.first; });
-        for (const auto& s : offdiag)
-            for (int x = 0; x < 6; ++x) order.push_back(cost[6 * s.second + x]);
+        auto by_work = [](const auto& a, const auto& b) { return a.first > b.first; };
+        std::stable_sort(diag.begin(), diag.end(), by_work);
+        std::stable_sort(offdiag.begin(), offdiag.end(), by_work);
+        for (const auto* cls : {&diag, &offdiag})
+            for (const auto& s : *cls)
+                for (int x = 0; x < 6; ++x) order.push_back(cost[6 * s.second + x]);
+        for (int l = 0; l < ncl; ++l)
+            cams.push_back({cs.lcam_obs_begin[lcam0 + l + 1] - cs.lcam_obs_begin[lcam0 + l], l});
+        std::stable_sort(cams.begin(), cams.end(), by_work);
         auto cam_group = [&](int l) {
             const int b0 = cs.lcam_obs_begin[lcam0 + l], b1 = cs.lcam_obs_begin[lcam0 + l + 1];
             return b1 > b0 ? grp[cs.lcam_obs[b0]] : -1;
         };
-        for (int l = 0; l < ncl; ++l)
-            for (int row = 0; row < std::min(2, crow); ++row) order.push_back(cost[6 * nslots + l * crow + row]);
+        for (const auto& c : cams)
+            for (int row = 0; row < std::min(2, crow); ++row) order.push_back(cost[6 * nslots + c.second * crow + row]);
         for (int pass = 0; pass < 2; ++pass)
-            for (int l = 0; l < ncl; ++l) {
-                const int g = cam_group(l);
+            for (const auto& c : cams) {
+                const int l = c.second, g = cam_group(l);
                 for (int row = 2; row < crow; ++row)
                     if (((row - 2) / ni == g) == (pass == 0)) order.push_back(cost[6 * nslots + l * crow + row]);
             }
