@@ -1129,7 +1129,7 @@ struct ChunkLimits {
 //     decreasing cost (lanes of a round then run loops of similar length): 7.16 against 7.77 ms.
 // The schedule only decides which thread owns a task: every output is still summed by one thread
 // in the order of its item list, so results do not depend on it.
-void schedule_owner_tasks(const HostModel* m, int precision, int chunk_obs_start, int obs_end, int p_first, int p_end,
+void schedule_owner_tasks(const HostModel* m, int chunk_obs_start, int obs_end, int p_first, int p_end,
                           const std::vector<unsigned char>& obs_lcam, ChunkSet& cs, int slot0, int nslots,
                           int lcam0, int ncl) {
     const int ng = m->ng, ni = m->ni;
@@ -1184,33 +1184,10 @@ void schedule_owner_tasks(const HostModel* m, int precision, int chunk_obs_start
             cost[id] = {c, id};
         }
     }
-    if (precision == PB_PRECISION_FP64) {
-        // whole pair blocks (6 rows) and cameras (crow rows) by decreasing longest row, ties by
-        // position (a deterministic plan); rows inside a group keep their order
-        thread_local std::vector<std::pair<long long, int>> groups, order;
-        groups.clear();
-        groups.reserve(static_cast<size_t>(nslots) + ncl);
-        for (int sl = 0; sl < nslots; ++sl) groups.push_back({cost[6 * sl].first, sl});
-        for (int l = 0; l < ncl; ++l) {
-            long long mx = 0;
-            for (int row = 0; row < crow; ++row) mx = std::max(mx, cost[6 * nslots + l * crow + row].first);
-            groups.push_back({mx, nslots + l});
-        }
-        std::stable_sort(groups.begin(), groups.end(), [](const auto& a, const auto& b) { return a.first > b.first; });
-        order.clear();
-        order.reserve(cost.size());
-        for (const auto& g : groups) {
-            if (g.second < nslots) {
-                for (int x = 0; x < 6; ++x) order.push_back(cost[6 * g.second + x]);
-            } else {
-                const int l = g.second - nslots;
-                for (int row = 0; row < crow; ++row) order.push_back(cost[6 * nslots + l * crow + row]);
-            }
-        }
-        cost.swap(order);
-    } else {
-        // FP32 path: the rows are grouped by the code path they take, so that a round's lanes run
-        // the same branch.  Pair rows: the rows of diagonal slots (own terms J^T M J) before those
+    {
+        // The rows are grouped by the code path they take, so that a round's lanes run the same
+        // branch (on the FP64 path the FP64 pipe spends a warp instruction's slots on idle lanes
+        // too).  Pair rows: the rows of diagonal slots (own terms J^T M J) before those
         // of off-diagonal slots (couplings G G^T).  Camera rows: the gradient rows of every camera,
         // then the border rows of each camera's own calibration group (own term and intrinsic
         // coupling), then the border rows of the other groups (coupling only, often empty).  The
@@ -1400,7 +1377,7 @@ int plan_range(const HostModel* m, const ChunkLimits& lim, int p_begin, int p_ra
             for (int o = chunk_obs_start; o < obs_end; ++o)
                 if (obs_lcam[o] != 255) cs.lcam_obs[cc[obs_lcam[o]]++] = static_cast<unsigned char>(o - chunk_obs_start);
         }
-        schedule_owner_tasks(m, lim.precision, chunk_obs_start, obs_end, p_first, p_end, obs_lcam, cs, cs.pair_begin.back(),
+        schedule_owner_tasks(m, chunk_obs_start, obs_end, p_first, p_end, obs_lcam, cs, cs.pair_begin.back(),
                              nslot, cs.cam_begin.back(), ncl);
         cs.obs_begin.push_back(obs_end);
         cs.cam_begin.push_back(static_cast<int>(cs.cams.size()));
