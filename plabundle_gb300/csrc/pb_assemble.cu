@@ -85,9 +85,13 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
     double* s_misc = carve<double>(ptr, 40);
     int* s_flags = reinterpret_cast<int*>(s_misc + 32);
     int* s_wcount = reinterpret_cast<int*>(s_misc + 34);
+    int* s_next_entry = reinterpret_cast<int*>(s_misc + 38);  // next intrinsic entry to take
 
     const int obs0 = D.ch_obs_begin[chunk], nobs = D.ch_obs_begin[chunk + 1] - obs0;
-    if (tid == 0) s_flags[0] = 0;
+    if (tid == 0) {
+        s_flags[0] = 0;
+        s_next_entry[0] = 0;
+    }
     __syncthreads();
 
     // ---- A: linearise one observation per thread; FP64 point normal equations
@@ -528,8 +532,13 @@ __global__ void __launch_bounds__(256, 2) k_assemble(Shape S, DevPtrs D, AsmOutT
     // chunk's critical path).  Warps that finish their rows above start here at once.
     {
         P* out = O.part_chunk + static_cast<size_t>(chunk) * chrec;
-        const int nwarps = static_cast<int>(blockDim.x >> 5);
-        for (int e = wid; e < chrec; e += nwarps) {
+        // a warp takes the next entry when it is free (an entry is summed the same way by any
+        // warp, so the order of taking changes no result)
+        for (;;) {
+            int e = 0;
+            if (lane == 0) e = atomicAdd(s_next_entry, 1);
+            e = __shfl_sync(0xffffffffu, e, 0);
+            if (e >= chrec) break;
             Acc<T> acc;
             if (e < nb * nb) {
                 const int i = e / nb, j = e - i * nb;
