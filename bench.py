@@ -72,10 +72,10 @@ def converged_iterations(workload_name):
 # dram__bytes_write.sum of an ncu capture on the 250-camera / 100k-point aerial grid
 # (663 659 observations; profiles/k_assemble_aerial250.md).  The chunk plan is the same at 500
 # cameras, so the traffic scales with the observations.
-ASSEMBLY_DRAM_BYTES_PER_OBS = (38.878976e6 + 253.595136e6) / 663659
+ASSEMBLY_DRAM_BYTES_PER_OBS = (38.440192e6 + 253.206528e6) / 663659
 # Warp instructions of one k_assemble<float> launch per observation (smsp__inst_executed.sum of the
 # same capture).
-ASSEMBLY_INST_PER_OBS = 664110681 / 663659
+ASSEMBLY_INST_PER_OBS = 681889338 / 663659
 SMS = 152  # streaming multiprocessors of a GB300
 
 # What the mixed path keeps in FP64 (everything else of the assembly and the CG preconditioner is
